@@ -1,0 +1,362 @@
+/*
+ * C restatement of the grid-function kernels of src/m_util_r8.f that the
+ * multigrid path calls (copy, interpolation, half/full-weight restriction).
+ *
+ * TEST INFRASTRUCTURE (oracle only). The image has no Fortran compiler, so
+ * these routines stand in for the reference's Fortran 77 when its C sources
+ * are compiled into the CPU checker (oracle/_ref) and are reused by the
+ * oracle port (oracle/port). Each routine follows the Fortran line by line:
+ * 1-based indices, same loop nests, same left-to-right expression order, so
+ * gcc with -ffp-contract=off reproduces the Fortran arithmetic exactly.
+ *
+ * Excision variants (`_ex`, do_ex=1) and the evolution-only routines
+ * (dmdiss3d, linbnd3d, dmrepop3d1, dmrepop3dc1) are not on the elliptic path
+ * and abort if reached.
+ *
+ * Optional call log: when mur8_log_enabled is set, every call records its
+ * kernel id and index arguments so a test can compare the reference's
+ * transfer bookkeeping with another implementation op by op.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include "m_util_r8_c.h"
+
+/* ------------------------------------------------------------- call log -- */
+int mur8_log_enabled = 0;
+mur8_call *mur8_log = 0;
+int mur8_log_n = 0, mur8_log_cap = 0;
+
+static void log_call(int kind, const double *u1, const double *u2, const int *iv, int n)
+{
+   mur8_call *c;
+   int i;
+   if (!mur8_log_enabled) return;
+   if (mur8_log_n == mur8_log_cap) {
+      mur8_log_cap = mur8_log_cap ? 2 * mur8_log_cap : 1024;
+      mur8_log = (mur8_call *)realloc(mur8_log, sizeof(mur8_call) * (size_t)mur8_log_cap);
+   }
+   c = &mur8_log[mur8_log_n++];
+   c->kind = kind;
+   c->u1 = u1;
+   c->u2 = u2;
+   for (i = 0; i < MUR8_NARGS; i++) c->iv[i] = i < n ? iv[i] : 0;
+}
+
+static void not_on_path(const char *who)
+{
+   fprintf(stderr, "m_util_r8 restatement: %s is not on the multigrid path\n", who);
+   abort();
+}
+
+/* Fortran u(nx,ny,nz), 1-based (i,j,k) */
+#define A3(u, nx, ny, i, j, k) (u)[((i)-1) + ((j)-1) * (long)(nx) + ((k)-1) * (long)(nx) * (long)(ny)]
+#define A1(v, i) (v)[(i)-1]
+
+/* src/m_util_r8.f:20-50 */
+static void dmcopy3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                     int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                     int si1, int sj1, int sk1, int si2, int sj2, int sk2)
+{
+   int i, j, k;
+   (void)nz2;
+   if (i1 < 1 || (i1 + (ni - 1) * si1) > nx1) return;
+   if (i2 < 1 || (i2 + (ni - 1) * si2) > nx2) return;
+   if (j1 < 1 || (j1 + (nj - 1) * sj1) > ny1) return;
+   if (j2 < 1 || (j2 + (nj - 1) * sj2) > ny2) return;
+   if (k1 < 1 || (k1 + (nk - 1) * sk1) > nz1) return;
+   if (k2 < 1 || (k2 + (nk - 1) * sk2) > nz2) return;
+   for (i = 1; i <= ni; i++)
+      for (j = 1; j <= nj; j++)
+         for (k = 1; k <= nk; k++)
+            A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) =
+               A3(u1, nx1, ny1, i1 + (i - 1) * si1, j1 + (j - 1) * sj1, k1 + (k - 1) * sk1);
+}
+
+void dmcopy3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, int *ny2, int *nz2,
+               int *i1, int *j1, int *k1, int *i2, int *j2, int *k2, int *ni, int *nj, int *nk,
+               int *si1, int *sj1, int *sk1, int *si2, int *sj2, int *sk2)
+{
+   int iv[21] = {*nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2,
+                 *ni, *nj, *nk, *si1, *sj1, *sk1, *si2, *sj2, *sk2};
+   log_call(MUR8_COPY, u1, u2, iv, 21);
+   dmcopy3d(u1, u2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2, *ni, *nj,
+            *nk, *si1, *sj1, *sk1, *si2, *sj2, *sk2);
+}
+
+/* src/m_util_r8.f:332-360 (linear, irho:1) */
+static void dvi2q1d(const double *v1, double *v2, int i1, int i2, int n1, int n2, int n, int irho,
+                    int s1, int s2)
+{
+   double c0, c1, sg;
+   int i, j;
+   (void)n1; (void)n2;
+   for (i = 1; i <= n; i++) A1(v2, irho * (i - 1) * s2 + i2) = A1(v1, (i - 1) * s1 + i1);
+   for (j = 1; j <= irho - 1; j++) {
+      sg = (j * 1.0) / irho;
+      c0 = 1 - sg;
+      c1 = sg;
+      for (i = 0; i <= n - 2; i++)
+         A1(v2, (irho * i + j) * s2 + i2) = c0 * A1(v1, i * s1 + i1) + c1 * A1(v1, (i + 1) * s1 + i1);
+   }
+}
+
+/* src/m_util_r8.f:65-144 (cubic, one-sided near the ends, linear if n<4) */
+static const double HALF = 0.5, MHALF = -0.5;
+static const double SIXTH = 0.16666666666666667, MSIXTH = -0.16666666666666667;
+
+#define CUBIC_COEFS(sg)                                          \
+   c0 = MSIXTH * ((sg) - 1.0) * ((sg) - 2.0) * ((sg) - 3.0);     \
+   c1 = HALF * (sg) * ((sg) - 2.0) * ((sg) - 3.0);               \
+   c2 = MHALF * (sg) * ((sg) - 1.0) * ((sg) - 3.0);              \
+   c3 = SIXTH * (sg) * ((sg) - 1.0) * ((sg) - 2.0);
+
+static void dvi4q1d(const double *v1, double *v2, int i1, int i2, int n1, int n2, int n, int irho,
+                    int s1, int s2)
+{
+   double c0, c1, c2, c3, sg;
+   int i, j, is, ie;
+   if (n < 4) {
+      dvi2q1d(v1, v2, i1, i2, n1, n2, n, irho, s1, s2);
+      return;
+   }
+   for (i = 1; i <= n; i++) A1(v2, irho * (i - 1) * s2 + i2) = A1(v1, (i - 1) * s1 + i1);
+   if (i1 <= s1) {
+      for (j = 1; j <= irho - 1; j++) {
+         sg = (j * 1.0) / irho;
+         CUBIC_COEFS(sg)
+         A1(v2, j * s2 + i2) = c0 * A1(v1, i1) + c1 * A1(v1, s1 + i1) + c2 * A1(v1, 2 * s1 + i1) +
+                               c3 * A1(v1, 3 * s1 + i1);
+      }
+      is = 1;
+   } else
+      is = 0;
+   if ((i1 + n * s1) > (n1 - 2 * s1)) {
+      ie = n - 3;
+      for (j = 1; j <= irho - 1; j++) {
+         sg = 2.0 + (j * 1.0) / irho;
+         CUBIC_COEFS(sg)
+         A1(v2, (irho * (n - 2) + j) * s2 + i2) =
+            c0 * A1(v1, (n - 4) * s1 + i1) + c1 * A1(v1, (n - 3) * s1 + i1) +
+            c2 * A1(v1, (n - 2) * s1 + i1) + c3 * A1(v1, (n - 1) * s1 + i1);
+      }
+   } else
+      ie = n - 2;
+   for (j = 1; j <= irho - 1; j++) {
+      sg = 1.0 + (j * 1.0) / irho;
+      CUBIC_COEFS(sg)
+      for (i = is; i <= ie; i++)
+         A1(v2, (irho * i + j) * s2 + i2) =
+            c0 * A1(v1, (i - 1) * s1 + i1) + c1 * A1(v1, i * s1 + i1) +
+            c2 * A1(v1, (i + 1) * s1 + i1) + c3 * A1(v1, (i + 2) * s1 + i1);
+   }
+}
+
+static void dviq1d(int ord, double *v, int i12, int n12, int n, int rho, int s1, int s2)
+{
+   if (ord == 2) dvi2q1d(v, v, i12, i12, n12, n12, n, rho, s1, s2);
+   else dvi4q1d(v, v, i12, i12, n12, n12, n, rho, s1, s2);
+}
+
+/* src/m_util_r8.f:473-637 (do_ex=0) */
+void dminterp3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
+                 int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
+                 int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *pirho, int *pjrho,
+                 int *pkrho, int *pord, double *chr1, double *ex, int *do_ex)
+{
+   int nx1 = *pnx1, ny1 = *pny1, nz1 = *pnz1, nx2 = *pnx2, ny2 = *pny2, nz2 = *pnz2;
+   int i1 = *pi1, j1 = *pj1, k1 = *pk1, i2 = *pi2, j2 = *pj2, k2 = *pk2;
+   int ni = *pni, nj = *pnj, nk = *pnk, si1 = *psi1, sj1 = *psj1, sk1 = *psk1;
+   int irho = *pirho, jrho = *pjrho, krho = *pkrho, ord = *pord;
+   int i, j, k;
+   int iv[24] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
+                 ni, nj, nk, si1, sj1, sk1, irho, jrho, krho, ord, *do_ex, 0};
+   (void)chr1; (void)ex;
+   log_call(MUR8_INTERP, u1, u2, iv, 24);
+
+   if (i1 < 1 || (i1 + ni - 1) * si1 > nx1) return;
+   if (i2 < 1 || (i2 + (ni - 1) * irho) > nx2) return;
+   if (j1 < 1 || (j1 + nj - 1) * sj1 > ny1) return;
+   if (j2 < 1 || (j2 + (nj - 1) * jrho) > ny2) return;
+   if (k1 < 1 || (k1 + nk - 1) * sk1 > nz1) return;
+   if (k2 < 1 || (k2 + (nk - 1) * krho) > nz2) return;
+   if (!(ord == 2 || ord == 4)) {
+      fprintf(stderr, "dminterp3d: only ord=2,4 currently supported\n");
+      abort();
+   }
+   if (*do_ex == 1) not_on_path("dminterp3d with excision");
+
+   dmcopy3d(u1, u2, nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk, si1, sj1,
+            sk1, irho, jrho, krho);
+
+   for (j = j2; j <= j2 + (nj - 1) * jrho; j += jrho)
+      for (k = k2; k <= k2 + (nk - 1) * krho; k += krho)
+         dviq1d(ord, &A3(u2, nx2, ny2, 1, j, k), i2, nx2, ni, irho, irho, 1);
+
+   if (nj == 1 && nk == 1) return;
+
+   for (i = i2; i <= i2 + (ni - 1) * irho; i++)
+      for (k = k2; k <= k2 + (nk - 1) * krho; k += krho)
+         dviq1d(ord, &A3(u2, nx2, ny2, i, 1, k), 1 + (j2 - 1) * nx2, nx2 * (ny2 - 1) + 1, nj, jrho,
+                jrho * nx2, nx2);
+
+   if (nk == 1) return;
+
+   for (i = i2; i <= i2 + (ni - 1) * irho; i++)
+      for (j = j2; j <= j2 + (nj - 1) * jrho; j++)
+         dviq1d(ord, &A3(u2, nx2, ny2, i, j, 1), (k2 - 1) * nx2 * ny2 + 1,
+                nx2 * ny2 * (nz2 - 1) + 1, nk, krho, krho * nx2 * ny2, nx2 * ny2);
+}
+
+/* src/m_util_r8.f:649-723 (do_ex=0) */
+void dmhwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
+              int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
+              int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *psi2, int *psj2,
+              int *psk2, double *chr1, double *ex, int *do_ex)
+{
+   int nx1 = *pnx1, ny1 = *pny1, nz1 = *pnz1, nx2 = *pnx2, ny2 = *pny2, nz2 = *pnz2;
+   int i1 = *pi1, j1 = *pj1, k1 = *pk1, i2 = *pi2, j2 = *pj2, k2 = *pk2;
+   int ni = *pni, nj = *pnj, nk = *pnk, si1 = *psi1, sj1 = *psj1, sk1 = *psk1;
+   int si2 = *psi2, sj2 = *psj2, sk2 = *psk2;
+   int i, j, k, w, i0, j0, k0;
+   double sum;
+   int iv[22] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
+                 ni, nj, nk, si1, sj1, sk1, si2, sj2, sk2, *do_ex};
+   (void)chr1; (void)ex;
+   log_call(MUR8_HWR, u1, u2, iv, 22);
+
+   if (i1 < 1 || (i1 + (ni - 1) * si1) > nx1) return;
+   if (i2 < 1 || (i2 + (ni - 1) * si2) > nx2) return;
+   if (j1 < 1 || (j1 + (nj - 1) * sj1) > ny1) return;
+   if (j2 < 1 || (j2 + (nj - 1) * sj2) > ny2) return;
+   if (k1 < 1 || (k1 + (nk - 1) * sk1) > nz1) return;
+   if (k2 < 1 || (k2 + (nk - 1) * sk2) > nz2) return;
+   if (*do_ex == 1) not_on_path("dmhwr3d with excision");
+
+   for (i = 1; i <= ni; i++)
+      for (j = 1; j <= nj; j++)
+         for (k = 1; k <= nk; k++) {
+            i0 = i1 + (i - 1) * si1;
+            j0 = j1 + (j - 1) * sj1;
+            k0 = k1 + (k - 1) * sk1;
+            w = 0;
+            sum = 0;
+            if (i0 > 1 && i0 <= (nx1 - 1)) {
+               w = w + 4;
+               sum = sum + A3(u1, nx1, ny1, i0 - 1, j0, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                     A3(u1, nx1, ny1, i0 + 1, j0, k0);
+            }
+            if (j0 > 1 && j0 <= (ny1 - 1)) {
+               w = w + 4;
+               sum = sum + A3(u1, nx1, ny1, i0, j0 - 1, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                     A3(u1, nx1, ny1, i0, j0 + 1, k0);
+            }
+            if (k0 > 1 && k0 <= (nz1 - 1)) {
+               w = w + 4;
+               sum = sum + A3(u1, nx1, ny1, i0, j0, k0 - 1) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                     A3(u1, nx1, ny1, i0, j0, k0 + 1);
+            }
+            if (w > 0)
+               A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) = sum / w;
+            else
+               A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) =
+                  A3(u1, nx1, ny1, i0, j0, k0);
+         }
+}
+
+/* src/m_util_r8.f:733-830 (do_ex=0) */
+void dmfwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
+              int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
+              int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *psi2, int *psj2,
+              int *psk2, double *chr1, double *ex, int *do_ex)
+{
+   int nx1 = *pnx1, ny1 = *pny1, nz1 = *pnz1, nx2 = *pnx2, ny2 = *pny2, nz2 = *pnz2;
+   int i1 = *pi1, j1 = *pj1, k1 = *pk1, i2 = *pi2, j2 = *pj2, k2 = *pk2;
+   int ni = *pni, nj = *pnj, nk = *pnk, si1 = *psi1, sj1 = *psj1, sk1 = *psk1;
+   int si2 = *psi2, sj2 = *psj2, sk2 = *psk2;
+   int i, j, k, i0, j0, k0, im, jm, km, ip, jp, kp;
+   double *d;
+   int iv[22] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
+                 ni, nj, nk, si1, sj1, sk1, si2, sj2, sk2, *do_ex};
+   (void)chr1; (void)ex;
+   log_call(MUR8_FWR, u1, u2, iv, 22);
+
+   if (i1 < 1 || (i1 + (ni - 1) * si1) > nx1) return;
+   if (i2 < 1 || (i2 + (ni - 1) * si2) > nx2) return;
+   if (j1 < 1 || (j1 + (nj - 1) * sj1) > ny1) return;
+   if (j2 < 1 || (j2 + (nj - 1) * sj2) > ny2) return;
+   if (k1 < 1 || (k1 + (nk - 1) * sk1) > nz1) return;
+   if (k2 < 1 || (k2 + (nk - 1) * sk2) > nz2) return;
+   if (*do_ex == 1) not_on_path("dmfwr3d with excision");
+
+#define U(a, b, c) A3(u1, nx1, ny1, a, b, c)
+   for (i = 1; i <= ni; i++)
+      for (j = 1; j <= nj; j++)
+         for (k = 1; k <= nk; k++) {
+            i0 = i1 + (i - 1) * si1;
+            j0 = j1 + (j - 1) * sj1;
+            k0 = k1 + (k - 1) * sk1;
+            im = i0 - 1; jm = j0 - 1; km = k0 - 1;
+            ip = i0 + 1; jp = j0 + 1; kp = k0 + 1;
+            d = &A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2);
+            if (i0 > 1 && i0 <= (nx1 - 1) && j0 > 1 && j0 <= (ny1 - 1) && k0 > 1 &&
+                k0 <= (nz1 - 1)) {
+               *d = (U(im, jm, km) + 2 * U(i0, jm, km) + U(ip, jm, km) +
+                     2 * U(im, j0, km) + 4 * U(i0, j0, km) + 2 * U(ip, j0, km) +
+                     U(im, jp, km) + 2 * U(i0, jp, km) + U(ip, jp, km) +
+                     2 * U(im, jm, k0) + 4 * U(i0, jm, k0) + 2 * U(ip, jm, k0) +
+                     4 * U(im, j0, k0) + 8 * U(i0, j0, k0) + 4 * U(ip, j0, k0) +
+                     2 * U(im, jp, k0) + 4 * U(i0, jp, k0) + 2 * U(ip, jp, k0) +
+                     U(im, jm, kp) + 2 * U(i0, jm, kp) + U(ip, jm, kp) +
+                     2 * U(im, j0, kp) + 4 * U(i0, j0, kp) + 2 * U(ip, j0, kp) +
+                     U(im, jp, kp) + 2 * U(i0, jp, kp) + U(ip, jp, kp)) / 64.0;
+            } else if (i0 > 1 && i0 <= (nx1 - 1) && j0 > 1 && j0 <= (ny1 - 1)) {
+               *d = (1 * U(im, jm, k0) + 2 * U(i0, jm, k0) + 1 * U(ip, jm, k0) +
+                     2 * U(im, j0, k0) + 4 * U(i0, j0, k0) + 2 * U(ip, j0, k0) +
+                     1 * U(im, jp, k0) + 2 * U(i0, jp, k0) + 1 * U(ip, jp, k0)) / 16.0;
+            } else if (j0 > 1 && j0 <= (ny1 - 1) && k0 > 1 && k0 <= (nz1 - 1)) {
+               *d = (1 * U(i0, jm, km) + 2 * U(i0, jm, k0) + 1 * U(i0, jm, kp) +
+                     2 * U(i0, j0, km) + 4 * U(i0, j0, k0) + 2 * U(i0, j0, kp) +
+                     1 * U(i0, jp, km) + 2 * U(i0, jp, k0) + 1 * U(i0, jp, kp)) / 16.0;
+            } else if (i0 > 1 && i0 <= (nx1 - 1) && k0 > 1 && k0 <= (nz1 - 1)) {
+               *d = (1 * U(im, j0, km) + 2 * U(im, j0, k0) + 1 * U(im, j0, kp) +
+                     2 * U(i0, j0, km) + 4 * U(i0, j0, k0) + 2 * U(i0, j0, kp) +
+                     1 * U(ip, j0, km) + 2 * U(ip, j0, k0) + 1 * U(ip, j0, kp)) / 16.0;
+            } else if (i0 > 1 && i0 <= (nx1 - 1)) {
+               *d = (U(im, j0, k0) + 2 * U(i0, j0, k0) + U(ip, j0, k0)) / 4.0;
+            } else if (j0 > 1 && j0 <= (ny1 - 1)) {
+               *d = (U(i0, jm, k0) + 2 * U(i0, j0, k0) + U(i0, jp, k0)) / 4.0;
+            } else if (k0 > 1 && k0 <= (nz1 - 1)) {
+               *d = (U(i0, j0, km) + 2 * U(i0, j0, k0) + U(i0, j0, kp)) / 4.0;
+            } else {
+               *d = U(i0, j0, k0);
+            }
+         }
+#undef U
+}
+
+/* evolution-only kernels (src/m_util_r8.f:972-2470): not on the elliptic path */
+void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_type, int *even,
+               int *odd, double *mask, double *mask_off, int *nx, int *ny, int *nz, double *chr,
+               double *ex, int *do_ex)
+{
+   (void)f; (void)work; (void)eps; (void)do_bdy; (void)phys_bdy_type; (void)even; (void)odd;
+   (void)mask; (void)mask_off; (void)nx; (void)ny; (void)nz; (void)chr; (void)ex; (void)do_ex;
+   not_on_path("dmdiss3d");
+}
+void linbnd3d_(double *f, int *phys_bdy, int *which_bnd, int *Nx, int *Ny, int *Nz, double *chr,
+               double *ex, int *do_ex)
+{
+   (void)f; (void)phys_bdy; (void)which_bnd; (void)Nx; (void)Ny; (void)Nz; (void)chr; (void)ex;
+   (void)do_ex;
+   not_on_path("linbnd3d");
+}
+void dmrepop3d1_(double *f, double *chr, double *ex, int *io, int *nx, int *ny, int *nz)
+{
+   (void)f; (void)chr; (void)ex; (void)io; (void)nx; (void)ny; (void)nz;
+   not_on_path("dmrepop3d1");
+}
+void dmrepop3dc1_(double *chr, double *ex, int *nx, int *ny, int *nz)
+{
+   (void)chr; (void)ex; (void)nx; (void)ny; (void)nz;
+   not_on_path("dmrepop3dc1");
+}

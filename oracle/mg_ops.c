@@ -1,0 +1,136 @@
+/*
+ * Per-grid elliptic operators of the CPU checker (see oracle/mg_ops.h).
+ *
+ * TEST INFRASTRUCTURE (oracle only). Loop nests, 1-based red/black colouring
+ * mod(i+j+k+pass,2) and expression order follow examples/nbs/num.f:
+ *   lop      num.f:85-123
+ *   residual num.f:129-161  (RMS over cmask==ON interior points)
+ *   relax    num.f:172-246  (two colour passes; RMS of the in-sweep residual)
+ * In 2-D (Nz=1) the k loop is the single plane k=1 and the z terms vanish.
+ */
+#include <math.h>
+#include "mg_ops.h"
+
+#define IDX(g, i, j, k) \
+   (((i)-1) + ((j)-1) * (long)(g)->shape[0] + ((k)-1) * (long)(g)->shape[0] * (long)(g)->shape[1])
+
+static const double TWO_PI = 6.283185307179586;   /* 2*pi */
+static const double TEN_PI = 31.41592653589793;   /* 5*(2*pi) */
+
+/* lap(u) - as in num.f:113-115, left to right */
+static double lap(const oracle_grid *g, const double *v, int i, int j, int k, double dx2,
+                  double dy2, double dz2)
+{
+   double c = v[IDX(g, i, j, k)];
+   double t = (v[IDX(g, i + 1, j, k)] - 2 * c + v[IDX(g, i - 1, j, k)]) / dx2 +
+              (v[IDX(g, i, j + 1, k)] - 2 * c + v[IDX(g, i, j - 1, k)]) / dy2;
+   if (g->dim == 3) t = t + (v[IDX(g, i, j, k + 1)] - 2 * c + v[IDX(g, i, j, k - 1)]) / dz2;
+   return t;
+}
+
+/* L[u] at one point */
+static double op_point(int pde, double t, double u, double s)
+{
+   double p2, p4;
+   switch (pde) {
+   case ORACLE_CONFORMAL:
+      p2 = u * u;
+      p4 = p2 * p2;
+      return t + TWO_PI * s * (p4 * u);
+   case ORACLE_LAPSE:
+      return t - s * u;
+   default:
+      return t - s;
+   }
+}
+
+/* dL/du at one point: the Laplacian diagonal j0 plus the source term */
+static double jac_point(int pde, double j0, double u, double s)
+{
+   double p2;
+   switch (pde) {
+   case ORACLE_CONFORMAL:
+      p2 = u * u;
+      return j0 + TEN_PI * s * (p2 * p2);
+   case ORACLE_LAPSE:
+      return j0 - s;
+   default:
+      return j0;
+   }
+}
+
+static void bounds(const oracle_grid *g, int *ke, int *ks, double *dx2, double *dy2, double *dz2,
+                   double *j0)
+{
+   *dx2 = g->dx[0] * g->dx[0];
+   *dy2 = g->dx[1] * g->dx[1];
+   if (g->dim == 3) {
+      *dz2 = g->dx[2] * g->dx[2];
+      *ks = 2;
+      *ke = g->shape[2] - 1;
+      *j0 = -2 / *dx2 - 2 / *dy2 - 2 / *dz2;
+   } else {
+      *dz2 = 1;
+      *ks = 1;
+      *ke = 1;
+      *j0 = -2 / *dx2 - 2 / *dy2;
+   }
+}
+
+void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, const double *src,
+                const double *cmask)
+{
+   int i, j, k, ks, ke;
+   double dx2, dy2, dz2, j0;
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (i = 2; i <= g->shape[0] - 1; i++)
+      for (j = 2; j <= g->shape[1] - 1; j++)
+         for (k = ks; k <= ke; k++) {
+            long p = IDX(g, i, j, k);
+            if (cmask[p] == ORACLE_CMASK_ON)
+               lv[p] = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], src[p]);
+         }
+}
+
+double oracle_residual(int pde, const oracle_grid *g, double *res, const double *rhs,
+                       const double *v, const double *src, const double *cmask)
+{
+   int i, j, k, ks, ke, sum = 0;
+   double dx2, dy2, dz2, j0, norm = 0;
+   oracle_lop(pde, g, res, v, src, cmask);
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (i = 2; i <= g->shape[0] - 1; i++)
+      for (j = 2; j <= g->shape[1] - 1; j++)
+         for (k = ks; k <= ke; k++) {
+            long p = IDX(g, i, j, k);
+            if (cmask[p] == ORACLE_CMASK_ON) {
+               res[p] = res[p] - rhs[p];
+               norm = norm + res[p] * res[p];
+               sum = sum + 1;
+            }
+         }
+   return sqrt(norm / sum);
+}
+
+double oracle_relax(int pde, const oracle_grid *g, double *v, const double *rhs,
+                    const double *src, const double *cmask)
+{
+   int i, j, k, ks, ke, pass, sum = 0;
+   double dx2, dy2, dz2, j0, norm = 0, res, jac;
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (pass = 0; pass <= 1; pass++)
+      for (i = 2; i <= g->shape[0] - 1; i++)
+         for (j = 2; j <= g->shape[1] - 1; j++)
+            for (k = ks; k <= ke; k++) {
+               long p = IDX(g, i, j, k);
+               int par = (g->dim == 3) ? (i + j + k + pass) : (i + j + pass);
+               if (par % 2 == 0 && cmask[p] == ORACLE_CMASK_ON) {
+                  res = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], src[p]) - rhs[p];
+                  jac = jac_point(pde, j0, v[p], src[p]);
+                  v[p] = v[p] - res / jac;
+                  norm = norm + res * res;
+                  sum = sum + 1;
+               }
+            }
+   return sqrt(norm / sum);
+}

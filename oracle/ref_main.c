@@ -1,0 +1,400 @@
+/*
+ * Driver that runs the REFERENCE's own multigrid solve (amrd/mg.c
+ * solve_elliptics over PAMR's MG hierarchy) on a seeded case, and records
+ * what a GPU implementation must reproduce.
+ *
+ * TEST INFRASTRUCTURE (oracle only). Built by oracle/build_ref.sh from the
+ * reference's C sources in place (src/pamr.c, src/gh.c, src/transfer.c,
+ * src/misc.c, src/io.c, amrd/*.c), the single-rank shims in oracle/shim and
+ * the C restatement of the Fortran kernels (oracle/m_util_r8.c). Output goes
+ * to oracle/_ref/ only.
+ *
+ * usage: ref_mg <param file> <case.bin> <out.bin> [log_ops]
+ *
+ * The parameter file is an AMRD run-time file read by the reference's
+ * init_context() (amrd/io.c:36). case.bin carries the AMR hierarchy and the
+ * initial u and source on every AMR grid. The driver then
+ *   1. composes the hierarchy with PAMR_compose_hierarchy (src/pamr.c:259),
+ *   2. fills u and the source on time level 1,
+ *   3. calls solve_elliptics(1,1,0) (amrd/mg.c:20),
+ * while the application hooks (pattern of examples/nbs/nbs.c:301-351) log
+ * every relax/residual norm, the MG hierarchy, the cmask arrays, and (with
+ * log_ops) every m_util_r8 call with its index arguments.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include "pamr.h"
+#include "amrd.h"
+#include "mg.h"
+#include "mpi.h"
+#include "mg_ops.h"
+#include "m_util_r8_c.h"
+
+/* amrd/io.c:36 (the reference declares it in amrd/io.h, shadowed here by src/io.h) */
+void init_context(char *pfile);
+
+/* ------------------------------------------------------------ case data -- */
+typedef struct {
+   int lev;
+   double bbox[6];
+   int shape[3];
+   long n;
+   double *u, *src;
+} case_grid;
+
+static int c_dim, c_pde, c_ngrids;
+static case_grid *c_grids;
+
+/* --------------------------------------------------------------- output -- */
+static FILE *fout;
+static void rec(int tag, const void *p, long nbytes)
+{
+   fwrite(&tag, 4, 1, fout);
+   fwrite(&nbytes, 8, 1, fout);
+   if (nbytes) fwrite(p, 1, (size_t)nbytes, fout);
+}
+
+/* ------------------------------------------------------------ hook state -- */
+static int gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src;
+
+/* MG hierarchy map, captured at the first hook call */
+#define MAXG 4096
+typedef struct {
+   int L, idx, shape[3], coarsest;
+   double bbox[6];
+   double *gfs[PAMR_MAX_GFNS];
+   int ngfs;
+   int have_child_mask, have_bdy_mask;
+} mg_grid_rec;
+static mg_grid_rec mgmap[MAXG];
+static int n_mgmap = 0, mgh_levels = 0;
+
+static int same_bbox(const double *a, const double *b, int dim)
+{
+   int i;
+   for (i = 0; i < 2 * dim; i++)
+      if (fabs(a[i] - b[i]) > 1e-9 * (1 + fabs(a[i]))) return 0;
+   return 1;
+}
+
+static void capture_mgh(void)
+{
+   int L, valid, idx;
+   if (n_mgmap) return;
+   mgh_levels = PAMR_get_max_lev(PAMR_MGH);
+   PAMR_push_iter();
+   for (L = 1; L <= mgh_levels; L++) {
+      idx = 0;
+      valid = PAMR_init_s_iter(L, PAMR_MGH, 1);
+      while (valid) {
+         mg_grid_rec *r = &mgmap[n_mgmap++];
+         int rank, dim, gw[6], ngfs;
+         double t, *x[3];
+         r->shape[0] = r->shape[1] = r->shape[2] = 1;
+         PAMR_get_g_attribs(&rank, &dim, r->shape, r->bbox, gw, &t, &ngfs, x, r->gfs);
+         PAMR_get_g_coarsest(&r->coarsest);
+         r->ngfs = ngfs;
+         r->L = L;
+         r->idx = idx++;
+         r->have_child_mask = r->have_bdy_mask = 0;
+         valid = PAMR_next_g();
+      }
+   }
+   PAMR_pop_iter();
+}
+
+typedef struct {
+   int dim, shape[3], L, idx;
+   double bbox[6], dx[3];
+   double *gfs[PAMR_MAX_GFNS];
+   mg_grid_rec *rec;
+} cur_grid;
+
+static void ldptr(cur_grid *g)
+{
+   int rank, gw[6], ngfs, i;
+   double t, *x[3];
+   g->shape[0] = g->shape[1] = g->shape[2] = 1;
+   if (!PAMR_get_g_attribs(&rank, &g->dim, g->shape, g->bbox, gw, &t, &ngfs, x, g->gfs)) {
+      fprintf(stderr, "ref_mg: PAMR_get_g_attribs failed\n");
+      exit(2);
+   }
+   PAMR_get_g_level(&g->L);
+   for (i = 0; i < 3; i++) g->dx[i] = 1;
+   for (i = 0; i < g->dim; i++) g->dx[i] = x[i][1] - x[i][0];
+   capture_mgh();
+   g->rec = 0;
+   g->idx = -1;
+   for (i = 0; i < n_mgmap; i++)
+      if (mgmap[i].L == g->L && same_bbox(mgmap[i].bbox, g->bbox, g->dim)) {
+         g->rec = &mgmap[i];
+         g->idx = mgmap[i].idx;
+      }
+}
+
+static void to_ogrid(const cur_grid *g, oracle_grid *o)
+{
+   int i;
+   o->dim = g->dim;
+   for (i = 0; i < 3; i++) {
+      o->shape[i] = g->shape[i];
+      o->dx[i] = g->dx[i];
+   }
+}
+
+/* hook log: kind (0 relax, 1 residual, 2 lop), level, grid index, norm */
+typedef struct { int kind, L, idx, pad; double norm; } hook_rec;
+static hook_rec *hlog;
+static int n_hlog = 0, cap_hlog = 0;
+static void hook_log(int kind, const cur_grid *g, double norm)
+{
+   if (n_hlog == cap_hlog) {
+      cap_hlog = cap_hlog ? 2 * cap_hlog : 4096;
+      hlog = (hook_rec *)realloc(hlog, sizeof(hook_rec) * (size_t)cap_hlog);
+   }
+   hlog[n_hlog].kind = kind;
+   hlog[n_hlog].L = g->L;
+   hlog[n_hlog].idx = g->idx;
+   hlog[n_hlog].pad = 0;
+   hlog[n_hlog].norm = norm;
+   n_hlog++;
+}
+
+/* masks: stored once per (grid, kind) */
+typedef struct { int kind, L, idx, n; double *m; } mask_rec;
+static mask_rec masks[2 * MAXG];
+static int n_masks = 0;
+static void keep_mask(int kind, cur_grid *g)
+{
+   long n = (long)g->shape[0] * g->shape[1] * g->shape[2];
+   mask_rec *m;
+   if (!g->rec) return;
+   if (kind == 0 && g->rec->have_bdy_mask) return;
+   if (kind == 1 && g->rec->have_child_mask) return;
+   if (kind == 0) g->rec->have_bdy_mask = 1; else g->rec->have_child_mask = 1;
+   m = &masks[n_masks++];
+   m->kind = kind;
+   m->L = g->L;
+   m->idx = g->idx;
+   m->n = (int)n;
+   m->m = (double *)malloc(sizeof(double) * (size_t)n);
+   memcpy(m->m, g->gfs[gfn_cmask - 1], sizeof(double) * (size_t)n);
+}
+
+static double h_relax(void)
+{
+   cur_grid g;
+   oracle_grid o;
+   double norm;
+   ldptr(&g);
+   to_ogrid(&g, &o);
+   keep_mask(0, &g);
+   norm = oracle_relax(c_pde, &o, g.gfs[gfn_u - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_src - 1],
+                       g.gfs[gfn_cmask - 1]);
+   hook_log(0, &g, norm);
+   return norm;
+}
+
+static double h_residual(void)
+{
+   cur_grid g;
+   oracle_grid o;
+   double norm;
+   ldptr(&g);
+   to_ogrid(&g, &o);
+   norm = oracle_residual(c_pde, &o, g.gfs[gfn_res - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_u - 1],
+                          g.gfs[gfn_src - 1], g.gfs[gfn_cmask - 1]);
+   hook_log(1, &g, norm);
+   return norm;
+}
+
+static void h_lop(void)
+{
+   cur_grid g;
+   oracle_grid o;
+   ldptr(&g);
+   to_ogrid(&g, &o);
+   keep_mask(1, &g);
+   oracle_lop(c_pde, &o, g.gfs[gfn_lop - 1], g.gfs[gfn_u - 1], g.gfs[gfn_src - 1],
+              g.gfs[gfn_cmask - 1]);
+   hook_log(2, &g, 0);
+}
+
+static void h_noop(void) {}
+
+/* ------------------------------------------------------------- case i/o -- */
+static void read_case(const char *path)
+{
+   FILE *f = fopen(path, "rb");
+   int i, hdr[4];
+   if (!f) { fprintf(stderr, "ref_mg: cannot open %s\n", path); exit(2); }
+   if (fread(hdr, 4, 4, f) != 4) exit(2);
+   c_dim = hdr[0];
+   c_pde = hdr[1];
+   c_ngrids = hdr[2];
+   c_grids = (case_grid *)calloc((size_t)c_ngrids, sizeof(case_grid));
+   for (i = 0; i < c_ngrids; i++) {
+      case_grid *g = &c_grids[i];
+      if (fread(&g->lev, 4, 1, f) != 1) exit(2);
+      if (fread(g->shape, 4, 3, f) != 3) exit(2);
+      if (fread(g->bbox, 8, 6, f) != 6) exit(2);
+      g->n = (long)g->shape[0] * g->shape[1] * g->shape[2];
+      g->u = (double *)malloc(sizeof(double) * (size_t)g->n);
+      g->src = (double *)malloc(sizeof(double) * (size_t)g->n);
+      if (fread(g->u, 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+      if (fread(g->src, 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+   }
+   fclose(f);
+}
+
+static case_grid *match_case_grid(int L, const double *bbox, const int *shape)
+{
+   int i;
+   for (i = 0; i < c_ngrids; i++)
+      if (c_grids[i].lev == L && same_bbox(c_grids[i].bbox, bbox, c_dim)) {
+         if (c_grids[i].shape[0] != shape[0] || c_grids[i].shape[1] != shape[1] ||
+             c_grids[i].shape[2] != shape[2]) {
+            fprintf(stderr, "ref_mg: shape mismatch on level %i\n", L);
+            exit(2);
+         }
+         return &c_grids[i];
+      }
+   fprintf(stderr, "ref_mg: no case grid for a level-%i PAMR grid\n", L);
+   exit(2);
+   return 0;
+}
+
+/* fill (dir=0) or read back (dir=1) u and the source on every AMR grid */
+static void amr_data(int dir, int gu, int gs)
+{
+   int L, valid, Lmax = PAMR_get_max_lev(PAMR_AMRH);
+   for (L = 1; L <= Lmax; L++) {
+      valid = PAMR_init_s_iter(L, PAMR_AMRH, 0);
+      while (valid) {
+         int rank, dim, gw[6], ngfs, shape[3] = {1, 1, 1};
+         double t, *x[3], bbox[6], *gfs[PAMR_MAX_GFNS];
+         case_grid *cg;
+         PAMR_get_g_attribs(&rank, &dim, shape, bbox, gw, &t, &ngfs, x, gfs);
+         cg = match_case_grid(L, bbox, shape);
+         if (dir == 0) {
+            memcpy(gfs[gu - 1], cg->u, sizeof(double) * (size_t)cg->n);
+            memcpy(gfs[gs - 1], cg->src, sizeof(double) * (size_t)cg->n);
+         } else
+            memcpy(cg->u, gfs[gu - 1], sizeof(double) * (size_t)cg->n);
+         valid = PAMR_next_g();
+      }
+   }
+}
+
+/* pointer -> (level, grid index, gfn) for the op log; -1 if a temporary */
+static void resolve(const double *p, int *out)
+{
+   int i, h;
+   out[0] = out[1] = out[2] = -1;
+   for (i = 0; i < n_mgmap; i++)
+      for (h = 0; h < mgmap[i].ngfs; h++)
+         if (mgmap[i].gfs[h] == p) {
+            out[0] = mgmap[i].L;
+            out[1] = mgmap[i].idx;
+            out[2] = h + 1;
+            return;
+         }
+}
+
+int main(int argc, char **argv)
+{
+   int i, num, *lev;
+   double *bbox;
+   int gu_amr, gs_amr;
+   if (argc < 4) {
+      fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops]\n", argv[0]);
+      return 2;
+   }
+   read_case(argv[2]);
+
+   MPI_Init(&argc, &argv);
+   my_rank = 0;
+   app_AMRH_var_clear = h_noop;
+   app_MG_relax = h_relax;
+   app_MG_residual = h_residual;
+   app_L_op = h_lop;
+
+   init_context(argv[1]);
+
+   num = c_ngrids;
+   lev = (int *)malloc(sizeof(int) * (size_t)num);
+   bbox = (double *)malloc(sizeof(double) * 6 * (size_t)num);
+   for (i = 0; i < num; i++) {
+      lev[i] = c_grids[i].lev;
+      memcpy(&bbox[2 * c_dim * i], c_grids[i].bbox, sizeof(double) * 2 * (size_t)c_dim);
+   }
+   {
+      int nlev = 1;
+      for (i = 0; i < num; i++) if (lev[i] > nlev) nlev = lev[i];
+      if (!PAMR_compose_hierarchy(1, nlev, num, lev, bbox, 0.0)) {
+         fprintf(stderr, "ref_mg: PAMR_compose_hierarchy failed\n");
+         return 3;
+      }
+   }
+
+   gu_amr = PAMR_get_gfn("u", PAMR_AMRH, 1);
+   gs_amr = PAMR_get_gfn("rho", PAMR_AMRH, 1);
+   gfn_u = PAMR_get_gfn("u", PAMR_MGH, 0);
+   gfn_res = PAMR_get_gfn("u_res", PAMR_MGH, 0);
+   gfn_lop = PAMR_get_gfn("u_lop", PAMR_MGH, 0);
+   gfn_rhs = PAMR_get_gfn("u_rhs", PAMR_MGH, 0);
+   gfn_cmask = PAMR_get_gfn("cmask", PAMR_MGH, 0);
+   gfn_src = PAMR_get_gfn("rho", PAMR_MGH, 0);
+   if (gu_amr < 0 || gs_amr < 0 || gfn_u < 0 || gfn_res < 0 || gfn_lop < 0 || gfn_rhs < 0 ||
+       gfn_cmask < 0 || gfn_src < 0) {
+      fprintf(stderr, "ref_mg: missing variable definitions\n");
+      return 3;
+   }
+   amr_data(0, gu_amr, gs_amr);
+
+   mur8_log_enabled = (argc > 4 && atoi(argv[4]));
+   solve_elliptics(1, 1, 0);
+   mur8_log_enabled = 0;
+
+   amr_data(1, gu_amr, gs_amr);
+
+   fout = fopen(argv[3], "wb");
+   if (!fout) return 4;
+   {
+      int gf[6] = {gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src};
+      rec(1, &AMRD_curr_MG_iter, 4);
+      rec(2, gf, sizeof(gf));
+      rec(3, hlog, (long)sizeof(hook_rec) * n_hlog);
+   }
+   /* MG hierarchy: per grid L, idx, shape[3], coarsest, bbox[6] */
+   for (i = 0; i < n_mgmap; i++) {
+      struct { int L, idx, shape[3], coarsest; double bbox[6]; } r;
+      r.L = mgmap[i].L;
+      r.idx = mgmap[i].idx;
+      memcpy(r.shape, mgmap[i].shape, sizeof(r.shape));
+      r.coarsest = mgmap[i].coarsest;
+      memcpy(r.bbox, mgmap[i].bbox, sizeof(r.bbox));
+      rec(4, &r, sizeof(r));
+   }
+   for (i = 0; i < n_masks; i++) {
+      int h[4] = {masks[i].kind, masks[i].L, masks[i].idx, masks[i].n};
+      rec(5, h, sizeof(h));
+      rec(6, masks[i].m, 8L * masks[i].n);
+   }
+   for (i = 0; i < c_ngrids; i++) rec(7, c_grids[i].u, 8 * c_grids[i].n);
+   {
+      for (i = 0; i < mur8_log_n; i++) {
+         int r[4 + 6 + MUR8_NARGS];
+         r[0] = mur8_log[i].kind;
+         r[1] = r[2] = r[3] = 0;
+         resolve(mur8_log[i].u1, &r[4]);
+         resolve(mur8_log[i].u2, &r[7]);
+         memcpy(&r[10], mur8_log[i].iv, sizeof(int) * MUR8_NARGS);
+         rec(8, r, sizeof(r));
+      }
+   }
+   fclose(fout);
+   return 0;
+}

@@ -1,0 +1,275 @@
+"""Seeded synthetic elliptic problems on AMR hierarchies.
+
+Every input the solver sees is generated here from a seed, so the GPU path,
+the CPU checker and the benchmark all run on byte-identical arrays.
+
+A hierarchy follows PAMR's conventions (include/pamr.h, src/gh.c):
+vertex-centred grids, level ``L`` has spacing ``dx_1 / 2**(L-1)`` (refinement
+ratio 2), a grid is given by its level and bounding box, and grid functions
+are float64 arrays stored with x fastest (Fortran ``u(Nx,Ny,Nz)``; ``Nz=1`` in
+2-D).
+
+Workloads (names carry their sizes):
+
+* ``poisson2d_<n>``: lap(u) = rho on [-1,1]^2, one n x n grid, u=0 on the
+  boundary; rho is a sum of 8 Gaussians (amplitude U(-1,1), width
+  U(0.05,0.15), centre U(-0.8,0.8)^2).
+* ``conformal3d_<n>_<m>``: lap(psi) + 2 pi rho psi^5 = 0 on [-10,10]^3; base
+  n^3 grid plus two nested 2:1 levels of m^3 boxes centred on the origin;
+  psi = 1 on the boundary and as the initial guess; rho is a sum of 4
+  Gaussians (amplitude U(0,0.005), width U(0.5,2), centre U(-0.5,0.5)^3).
+  Amplitudes ten times larger give a compactness M/R of order one, where the
+  equation has no regular solution and the reference FAS diverges; the
+  coarsest MG grid is 9^3 (min_mg_cwidth 9) so that the Newton-Gauss-Seidel
+  diagonal -6/dx^2 + 10 pi rho psi^4 stays negative there.
+* ``poisson2d_uneven``: lap(u) = rho on [-1,1]^2, 129^2 base grid plus 4
+  refined levels of 8-64 boxes each (odd sides drawn from [17,129], aligned
+  to parent grid lines and clipped to the parent box); rho is a sum of 32
+  Gaussians.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+POISSON, CONFORMAL, LAPSE = 0, 1, 2
+PDE_NAMES = {POISSON: "poisson", CONFORMAL: "conformal", LAPSE: "lapse"}
+
+# transfer operators (values of PAMR's transfer bits, include/pamr.h:92-105)
+STRAIGHT_INJECT, HW_RESTR, FW_RESTR = 1, 2, 3
+
+
+class SplitMix64:
+    """splitmix64 stream; ``uniform()`` returns doubles in [0,1) (53 bits)."""
+
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed: int):
+        self.state = seed & self.MASK
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & self.MASK
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & self.MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & self.MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / 9007199254740992.0))
+
+    def randint(self, lo: int, hi: int) -> int:
+        """uniform integer in [lo, hi]"""
+        return lo + int(self.next_u64() % (hi - lo + 1))
+
+
+@dataclasses.dataclass
+class Grid:
+    level: int                      # 1-based AMR level
+    bbox: Tuple[float, ...]         # (x0,x1,y0,y1[,z0,z1])
+    shape: Tuple[int, int, int]     # (Nx,Ny,Nz), Nz=1 in 2-D
+
+    @property
+    def size(self) -> int:
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+    def coords(self, d: int) -> np.ndarray:
+        n = self.shape[d]
+        lo, hi = self.bbox[2 * d], self.bbox[2 * d + 1]
+        return lo + (hi - lo) / (n - 1) * np.arange(n)
+
+
+@dataclasses.dataclass
+class MGParams:
+    """AMRD multigrid knobs (amrd/io.c:96-109 defaults, amrd/io.c:269-288)."""
+    pre_swp: int = 2
+    pst_swp: int = 2
+    max_iter: int = 60
+    min_iter: int = 1
+    max_citer: int = 5000
+    tol: float = 0.0          # absolute, on the finest-level residual norm
+    crtol: float = 1.0e-3
+    w0_r: float = 1.0
+    w0_i: float = 1.0
+    min_cwidth: int = 3
+    interp_order: int = 2     # order used for the coarse-grid correction (mg_interp2)
+    restr_u: int = HW_RESTR   # mg_hw_restr = [u rho], mg_fw_restr = [u_res]
+    restr_res: int = FW_RESTR
+    restr_src: int = HW_RESTR
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    pde: int
+    dim: int
+    base_shape: Tuple[int, int, int]
+    base_bbox: Tuple[float, ...]
+    grids: List[Grid]
+    u0: List[np.ndarray]
+    src: List[np.ndarray]
+    params: MGParams
+
+    @property
+    def num_levels(self) -> int:
+        return max(g.level for g in self.grids)
+
+    def level_dx(self, level: int) -> List[float]:
+        return [(self.base_bbox[2 * d + 1] - self.base_bbox[2 * d]) / (self.base_shape[d] - 1)
+                / 2 ** (level - 1) for d in range(self.dim)]
+
+    def total_points(self) -> int:
+        return sum(g.size for g in self.grids)
+
+
+def _grid_from_bbox(level: int, bbox: Sequence[float], dx: Sequence[float], dim: int) -> Grid:
+    shape = [1, 1, 1]
+    for d in range(dim):
+        shape[d] = int((bbox[2 * d + 1] - bbox[2 * d]) / dx[d] + 1.5)
+    return Grid(level, tuple(float(b) for b in bbox), tuple(shape))
+
+
+def _mesh(g: Grid, dim: int):
+    """coordinate arrays broadcast to the (Nz,Ny,Nx) memory layout"""
+    x = g.coords(0)[None, None, :]
+    y = g.coords(1)[None, :, None]
+    z = g.coords(2)[:, None, None] if dim == 3 else np.zeros((1, 1, 1))
+    return x, y, z
+
+
+def _gaussians(g: Grid, dim: int, blobs) -> np.ndarray:
+    x, y, z = _mesh(g, dim)
+    out = np.zeros((g.shape[2], g.shape[1], g.shape[0]))
+    for (a, w, c) in blobs:
+        r2 = (x - c[0]) ** 2 + (y - c[1]) ** 2
+        if dim == 3:
+            r2 = r2 + (z - c[2]) ** 2
+        out = out + a * np.exp(-r2 / (w * w))
+    return np.ascontiguousarray(out).reshape(-1)
+
+
+def initial_residual_norm(case: Case) -> float:
+    """max over finest-level grids of the RMS of L[u0] on interior points
+    (the norm the V-cycle returns, amrd/util.c:73-103 with the hooks of
+    examples/nbs/num.f:129-161, rhs = 0)."""
+    lf = case.num_levels
+    dx = case.level_dx(lf)
+    best = 0.0
+    for g, u, s in zip(case.grids, case.u0, case.src):
+        if g.level != lf:
+            continue
+        v = u.reshape(g.shape[2], g.shape[1], g.shape[0])
+        f = s.reshape(v.shape)
+        c = v[..., 1:-1, 1:-1] if case.dim == 2 else v[1:-1, 1:-1, 1:-1]
+        if case.dim == 2:
+            t = ((v[:, 1:-1, 2:] - 2 * c + v[:, 1:-1, :-2]) / (dx[0] * dx[0]) +
+                 (v[:, 2:, 1:-1] - 2 * c + v[:, :-2, 1:-1]) / (dx[1] * dx[1]))
+            fs = f[:, 1:-1, 1:-1]
+        else:
+            t = ((v[1:-1, 1:-1, 2:] - 2 * c + v[1:-1, 1:-1, :-2]) / (dx[0] * dx[0]) +
+                 (v[1:-1, 2:, 1:-1] - 2 * c + v[1:-1, :-2, 1:-1]) / (dx[1] * dx[1]) +
+                 (v[2:, 1:-1, 1:-1] - 2 * c + v[:-2, 1:-1, 1:-1]) / (dx[2] * dx[2]))
+            fs = f[1:-1, 1:-1, 1:-1]
+        if case.pde == POISSON:
+            r = t - fs
+        elif case.pde == CONFORMAL:
+            r = t + 2 * math.pi * fs * c ** 5
+        else:
+            r = t - fs * c
+        best = max(best, float(np.sqrt(np.mean(r * r))))
+    return best
+
+
+def _finish(case: Case, rel_tol: float) -> Case:
+    if rel_tol > 0:
+        case.params.tol = rel_tol * initial_residual_norm(case)
+    return case
+
+
+def poisson2d(n: int = 129, seed: int = 0, rel_tol: float = 1e-10,
+              params: MGParams | None = None) -> Case:
+    rng = SplitMix64(0x5EED0001 + seed)
+    blobs = []
+    for _ in range(8):
+        a = rng.uniform(-1, 1)
+        w = rng.uniform(0.05, 0.15)
+        c = (rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8))
+        blobs.append((a, w, c))
+    bbox = (-1.0, 1.0, -1.0, 1.0)
+    g = Grid(1, bbox, (n, n, 1))
+    case = Case(f"poisson2d_{n}", POISSON, 2, (n, n, 1), bbox, [g],
+                [np.zeros(g.size)], [_gaussians(g, 2, blobs)], params or MGParams())
+    return _finish(case, rel_tol)
+
+
+def conformal3d(n: int = 129, m: int = 65, seed: int = 0, rel_tol: float = 1e-10,
+                params: MGParams | None = None, levels: int = 3) -> Case:
+    rng = SplitMix64(0x5EED0002 + seed)
+    blobs = []
+    for _ in range(4):
+        a = rng.uniform(0.0, 0.005)
+        w = rng.uniform(0.5, 2.0)
+        c = (rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5))
+        blobs.append((a, w, c))
+    bbox = (-10.0, 10.0, -10.0, 10.0, -10.0, 10.0)
+    dx1 = 20.0 / (n - 1)
+    grids = [Grid(1, bbox, (n, n, n))]
+    for lev in range(2, levels + 1):
+        dx = dx1 / 2 ** (lev - 1)
+        h = 0.5 * (m - 1) * dx
+        grids.append(_grid_from_bbox(lev, (-h, h, -h, h, -h, h), [dx] * 3, 3))
+    src = [_gaussians(g, 3, blobs) for g in grids]
+    u0 = [np.ones(g.size) for g in grids]
+    case = Case(f"conformal3d_{n}_{m}" + ("" if levels == 3 else f"_L{levels}"), CONFORMAL, 3,
+                (n, n, n), bbox, grids, u0, src, params or MGParams(min_cwidth=9))
+    return _finish(case, rel_tol)
+
+
+def poisson2d_uneven(seed: int = 0, n: int = 129, levels: int = 5, min_boxes: int = 8,
+                     max_boxes: int = 64, min_side: int = 17, max_side: int = 129,
+                     rel_tol: float = 1e-10, params: MGParams | None = None,
+                     nblobs: int = 32) -> Case:
+    rng = SplitMix64(0x5EED0003 + seed)
+    blobs = []
+    for _ in range(nblobs):
+        a = rng.uniform(-1, 1)
+        w = rng.uniform(0.05, 0.15)
+        c = (rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8))
+        blobs.append((a, w, c))
+    bbox = (-1.0, 1.0, -1.0, 1.0)
+    dx1 = 2.0 / (n - 1)
+    grids = [Grid(1, bbox, (n, n, 1))]
+    parents = [grids[0]]
+    for lev in range(2, levels + 1):
+        dxp = dx1 / 2 ** (lev - 2)
+        dx = dxp / 2
+        nb = rng.randint(min_boxes, max_boxes)
+        mine = []
+        while len(mine) < nb:
+            p = parents[rng.randint(0, len(parents) - 1)]
+            box = []
+            ok = True
+            for d in range(2):
+                pn = p.shape[d]
+                side = 2 * rng.randint((min_side - 1) // 2, (max_side - 1) // 2) + 1
+                cells = (side - 1) // 2                   # parent cells covered
+                p0 = rng.randint(0, max(0, pn - 2))
+                p1 = min(pn - 1, p0 + cells)
+                if p1 - p0 < 2:
+                    ok = False
+                    break
+                lo = p.bbox[2 * d] + p0 * dxp
+                hi = p.bbox[2 * d] + p1 * dxp
+                box += [lo, hi]
+            if not ok:
+                continue
+            mine.append(_grid_from_bbox(lev, box, [dx, dx], 2))
+        grids += mine
+        parents = mine
+    src = [_gaussians(g, 2, blobs) for g in grids]
+    u0 = [np.zeros(g.size) for g in grids]
+    case = Case(f"poisson2d_uneven_s{seed}", POISSON, 2, (n, n, 1), bbox, grids, u0, src,
+                params or MGParams())
+    return _finish(case, rel_tol)
