@@ -1,0 +1,148 @@
+/*
+ * pamr_gb300.h --- C ABI of libpamr_gb300, a GB300 (sm_103a) implementation
+ * of AMRD's FAS multigrid elliptic solve and the PAMR grid-function
+ * transfers it uses.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes (0 =
+ * success; on failure pgb_last_error() describes the problem). Nothing here
+ * exits the process (the reference's AMRD_stop, amrd/util.c:27-34, does).
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the reference project).
+ */
+#ifndef PAMR_GB300_H
+#define PAMR_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* PDE kinds of the device-side level operators; the operator is
+ * L[u] = lap(u) + term, evaluated as the reference hook pattern
+ * examples/nbs/num.f:85-246 does:
+ *   PGB_PDE_POISSON   term = -src               (lap u = rho)
+ *   PGB_PDE_CONFORMAL term = +2 pi src u^5       (conformal factor)
+ *   PGB_PDE_LAPSE     term = -src u              (maximal-slicing lapse) */
+#define PGB_PDE_POISSON 0
+#define PGB_PDE_CONFORMAL 1
+#define PGB_PDE_LAPSE 2
+
+/* transfer operators (PAMR transfer bits, include/pamr.h:92-105) */
+#define PGB_STRAIGHT_INJECT 1
+#define PGB_HW_RESTR 2
+#define PGB_FW_RESTR 3
+
+/* pgb_create flags */
+#define PGB_HOST_ONLY 1      /* build hierarchy and transfer plans only (no GPU) */
+
+/* Multigrid parameters: the AMRD run-time knobs (amrd/io.c:96-109, 269-288,
+ * doc/AMRD_ref.tex:575-631) plus the per-variable transfer operators of
+ * the parameter lists mg_hw_restr / mg_fw_restr / mg_interp2. */
+typedef struct {
+   int pre_swp, pst_swp;        /* MG_pre_swp, MG_pst_swp */
+   int max_iter, min_iter;      /* MG_max_iter, MG_min_iter */
+   int max_citer;               /* MG_max_citer */
+   double tol;                  /* MG_tol (absolute, finest-level residual norm) */
+   double crtol;                /* MG_crtol */
+   double w0_r, w0_i;           /* MG_w0_r, MG_w0_i */
+   int min_cwidth;              /* min_mg_cwidth */
+   int restr_u, restr_res, restr_src;  /* restriction of u, u_res, source */
+   int interp_order;            /* 2 (mg_interp2) or 4 */
+   int interp_buffer;           /* PAMR interp_buffer, default 2 (src/pamr.c:157) */
+} pgb_mg_params;
+
+typedef struct pgb_solver pgb_solver;
+
+/* Last error message of the calling thread. */
+const char *pgb_last_error(void);
+
+/* Default parameters (AMRD defaults, V(2,2), tol 0). */
+void pgb_default_params(pgb_mg_params *p);
+
+/* Builds the AMR hierarchy from `ngrids` grids (level grid_level[i] >= 1,
+ * bounding box grid_bbox[6*i .. 6*i+5] = x0,x1,y0,y1,z0,z1), the MG
+ * hierarchy below/among it, every transfer plan, and (unless
+ * PGB_HOST_ONLY) the device arena on the current CUDA device.
+ * Replaces PAMR_compose_hierarchy (src/pamr.c:259) followed by
+ * PAMR_build_mgh (src/pamr.c:354, src/gh.c:1222); refinement ratio 2. */
+int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox, int ngrids,
+               const int *grid_level, const double *grid_bbox, const pgb_mg_params *params,
+               int flags, pgb_solver **out);
+
+/* Frees the hierarchy and device memory (PAMR_destroy_mgh, src/pamr.c:383). */
+int pgb_destroy(pgb_solver *s);
+
+/* Grid data. Arrays are float64, x fastest (Fortran u(Nx,Ny,Nz)), shape
+ * from pgb_grid_shape. Host-pointer variants copy through the solver's
+ * stream; the *_device variants take device pointers. These replace the
+ * raw gfs pointers applications read via PAMR_get_g_attribs
+ * (src/pamr.c:1706) for the elliptic variable and its source. */
+int pgb_grid_shape(const pgb_solver *s, int grid, int *shape3);
+int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src);
+int pgb_get_grid(pgb_solver *s, int grid, double *u);
+int pgb_set_grid_device(pgb_solver *s, int grid, const double *u, const double *src);
+int pgb_get_grid_device(pgb_solver *s, int grid, double *u);
+
+/* Full solve: rebuilds the MG-only data from the AMR grids (build_mgh's
+ * injections), then V-cycles until the finest residual is <= tol (at least
+ * min_iter, at most max_iter cycles). Replaces solve_elliptics
+ * (amrd/mg.c:20-79). res_per_cycle (may be NULL) receives up to cap
+ * residuals. */
+int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycle, int cap);
+
+/* One FAS V-cycle; *res = finest-level residual. Replaces vcycle
+ * (amrd/mg.c:84-201). pgb_prepare performs the MG-hierarchy initialisation
+ * pgb_solve does before its first cycle. */
+int pgb_prepare(pgb_solver *s);
+int pgb_vcycle(pgb_solver *s, double *res);
+
+/* The solver's CUDA stream (cudaStream_t) for callers that order their own
+ * work around it. */
+void *pgb_stream(pgb_solver *s);
+
+/* Statistics of the last pgb_solve: V-cycles, coarsest-grid iterations
+ * (as the reference counts them), and device time in ms. */
+int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms);
+
+/* Norm trace: when enabled, every norm a hook would return is recorded
+ * (kind 0 relax, 1 residual, 2 = skipped coarsest iterations; level; box;
+ * repeat; norm) -- the device counterpart of MG_trace (amrd/mg.c:138-195). */
+int pgb_trace_enable(pgb_solver *s, int capacity);
+int pgb_trace_fetch(pgb_solver *s, int *kind, int *level, int *box, int *repeat, double *norm,
+                    int cap, int *n);
+
+/* ---------------------------------------------------- hierarchy queries -- */
+int pgb_num_levels(const pgb_solver *s);
+int pgb_level_nbox(const pgb_solver *s, int level);
+/* box `idx` of MG level `level` in PAMR grid-list order */
+int pgb_box_info(const pgb_solver *s, int level, int idx, int *shape3, double *bbox6,
+                 int *coarsest, int *amr_grid);
+/* cmask arrays: kind 0 = set_cmask_bdy (amrd/mg.c:432), 1 = set_cmask_child
+ * (amrd/mg.c:362); values 1.0 (AMRD_CMASK_ON) / 0.0 */
+int pgb_box_cmask(const pgb_solver *s, int level, int idx, int kind, double *out);
+/* transfer plans as index rows (which: 0 sync bw0, 1 sync bw1, 2 sync
+ * coarsest, 3 inject, 4 inject at build, 5 interp); returns the op count
+ * and fills up to cap rows of 24 ints */
+int pgb_plan_dump(const pgb_solver *s, int which, int level, int *rows, int cap);
+
+/* --------------------------------- device m_util_r8 (include/m_util_r8.h) -- */
+/* Same arguments as the Fortran routines (src/m_util_r8.f), by value, on
+ * device arrays; stream may be NULL. No excision (do_ex = 0). */
+int pgb_dmcopy3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                 int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                 int si1, int sj1, int sk1, int si2, int sj2, int sk2, void *stream);
+int pgb_dmhwr3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                int si1, int sj1, int sk1, int si2, int sj2, int sk2, void *stream);
+int pgb_dmfwr3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                int si1, int sj1, int sk1, int si2, int sj2, int sk2, void *stream);
+int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                   int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj,
+                   int nk, int si1, int sj1, int sk1, int irho, int jrho, int krho, int ord,
+                   void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -288,11 +288,24 @@ static void amr_data(int dir, int gu, int gs)
    }
 }
 
-/* pointer -> (level, grid index, gfn) for the op log; -1 if a temporary */
+/* pointer -> (level, grid index, gfn) for the op log; -1 if a temporary.
+ * MG grids on AMR levels alias AMR time-level storage, so the MG-instance
+ * gfns are matched first. */
 static void resolve(const double *p, int *out)
 {
-   int i, h;
+   int i, h, q;
+   int pref[6];
+   pref[0] = gfn_src; pref[1] = gfn_u; pref[2] = gfn_res;
+   pref[3] = gfn_lop; pref[4] = gfn_rhs; pref[5] = gfn_cmask;
    out[0] = out[1] = out[2] = -1;
+   for (i = 0; i < n_mgmap; i++)
+      for (q = 0; q < 6; q++)
+         if (mgmap[i].gfs[pref[q] - 1] == p) {
+            out[0] = mgmap[i].L;
+            out[1] = mgmap[i].idx;
+            out[2] = pref[q];
+            return;
+         }
    for (i = 0; i < n_mgmap; i++)
       for (h = 0; h < mgmap[i].ngfs; h++)
          if (mgmap[i].gfs[h] == p) {

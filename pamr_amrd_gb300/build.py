@@ -1,0 +1,84 @@
+"""Builds libpamr_gb300.so in place: CUDA kernels for sm_103a (nvcc) and the
+C host driver (gcc), linked against the CUDA runtime.
+
+The FP64 kernels are compiled with -fmad=false so that their arithmetic
+rounds like the reference's CPU code; host C is compiled with
+-ffp-contract=off for the same reason.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libpamr_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"]}
+C_SOURCES = ["pgb_plan.c", "pgb_solver.c"]
+
+
+def cuda_home() -> str:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return c
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(nvcc))
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    cuda = cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(OBJ, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers.append(os.path.join(ROOT, "include", "pamr_gb300.h"))
+    jobs, objs = [], []
+    for src, extra in CU_SOURCES.items():
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-I" + CSRC, "-I" + os.path.join(ROOT, "include")] + extra + ["-c", s, "-o", o]
+            jobs.append(cmd)
+    for src in C_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            cmd = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                   "-Wall", "-I" + CSRC, "-I" + os.path.join(ROOT, "include"),
+                   "-I" + os.path.join(cuda, "include"), "-c", s, "-o", o]
+            jobs.append(cmd)
+    procs = [(c, subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+             for c in jobs]
+    for c, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("build failed: " + " ".join(c) + "\n" + out)
+        if verbose and out:
+            print(out)
+    if force or _stale(LIB, objs):
+        cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-L" + os.path.join(cuda, "lib64"),
+                                                           "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: " + r.stdout + r.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,89 @@
+/*
+ * Device-side level descriptors and kernel launchers of libpamr_gb300.
+ * The launchers are plain C entry points (extern "C") called by the C host
+ * driver; every pointer argument is a device pointer.
+ */
+#ifndef PGB_DEV_H
+#define PGB_DEV_H
+
+#include "pgb_internal.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* tile extents: one CTA of 32 x 8 threads; each thread walks PGB_TZ planes
+ * in 3-D. Relax tiles are twice as wide in x because a thread updates one
+ * point of the active colour out of every two. */
+#define PGB_TX 32
+#define PGB_TY 8
+#define PGB_TZ 8
+
+/* one MG level as the kernels see it */
+typedef struct {
+   const pgb_tile *tiles;      /* 32 x 8 x TZ tiles over every box of the level */
+   const pgb_tile *rtiles;     /* 64 x 8 x TZ tiles (relax) */
+   const int *tile_start;      /* per level box: first tile (prefix, nbox+1) */
+   const int *rtile_start;
+   const int *box;             /* level box -> global box index */
+   int ntiles, nrtiles, nbox;
+   int dim;
+   int level;
+} pgb_dlevel;
+
+/* device-side trace of every norm a hook would return (kind 0 relax,
+ * 1 residual), one record per box and call; repeat > 1 marks coarsest-grid
+ * iterations that were skipped because the iteration had reached a cycle */
+typedef struct {
+   int kind, level, box, repeat;
+   double norm;
+} pgb_trace_rec;
+
+typedef struct {
+   int n, cap, overflow, pad;
+   pgb_trace_rec rec[1];
+} pgb_trace;
+
+/* scratch the reductions use (device memory) */
+typedef struct {
+   double *partial;            /* >= 2 * max tiles of any level */
+   unsigned int *counter;      /* one word, zero between kernels */
+   double *box_norm;           /* >= max boxes of any level */
+} pgb_scratch;
+
+/* parameters of the coarsest-grid loop (amrd/mg.c:172-190) */
+typedef struct {
+   int start_iter, max_citer;
+   double crtol;
+   const double *res_dn;       /* res[L] from the down sweep (ctol base) */
+   double *res_out;            /* res[L] after the loop */
+   int *iters_out;             /* iterations executed (for statistics) */
+   double *snap;               /* 2 x (points of the coarsest boxes) doubles */
+   long snap_points;
+   const long *snap_off;       /* per level box: offset of its points in a snapshot */
+} pgb_coarsest_args;
+
+const char *pgb_dev_error(void);
+int pgb_dev_sync(void *stream);
+
+/* FP64 path: every expression follows the reference hooks / Fortran order
+ * and the file is compiled without FMA contraction */
+int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int field_mask, void *stream);
+int pgb_k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc, double *norm_out,
+                pgb_trace *trace, void *stream);
+int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
+                   double *norm_out, pgb_trace *trace, void *stream);
+int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
+int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream);
+int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
+int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream);
+int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
+int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim, void *stream);
+int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
+                   pgb_coarsest_args a, pgb_trace *trace, void *stream);
+int pgb_k_fill(double *p, long n, double v, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

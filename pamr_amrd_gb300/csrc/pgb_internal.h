@@ -1,0 +1,95 @@
+/*
+ * Internal structures shared by the C host code (hierarchy/plan builder,
+ * V-cycle driver) and the CUDA kernels of libpamr_gb300.
+ *
+ * Terminology follows PAMR/AMRD: an AMR "grid" becomes an MG "box" on every
+ * MG level; grid functions per box are u (the elliptic variable f), res
+ * (f_res), lop (f_lop), rhs (f_rhs) and src (the source variable the
+ * operator reads); cmask is kept as two byte masks per box (child mask for
+ * L_op/compute_MG_rhs, boundary mask for relax/residual).
+ */
+#ifndef PGB_INTERNAL_H
+#define PGB_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* grid functions, in PAMR gfn order for the AMRD variable set
+ * (hyperbolic source first, then f, f_res, f_lop, f_rhs; amrd/io.c:708-937) */
+enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, PGB_NF = 5 };
+
+#define PGB_MAXLEV 48
+
+/* box flags */
+#define PGB_BOX_POW2DX 1     /* every dx^2 is a power of two: x/dx2 == x*(1/dx2) exactly */
+#define PGB_BOX_BDY_INTERIOR 2 /* the boundary cmask is ON at every interior point */
+#define PGB_BOX_COARSEST 4
+
+/* device view of one MG box (all pointers are device pointers) */
+typedef struct {
+   double *f[PGB_NF];
+   const uint8_t *cmask_child;   /* set_cmask_child, amrd/mg.c:362-426 */
+   const uint8_t *cmask_bdy;     /* set_cmask_bdy, amrd/mg.c:432-488 */
+   float *w32[3];                /* mixed precision work arrays (correction, rhs, src) */
+   int n[3];                     /* Nx, Ny, Nz (Nz = 1 in 2-D) */
+   int flags;
+   int level;
+   int count;                    /* # interior points with cmask_bdy ON (norm divisor) */
+   double dx2[3];                /* (x(2)-x(1))^2 per dimension */
+   double idx2[3];               /* 1/dx2 when PGB_BOX_POW2DX */
+   double j0;                    /* -2/dx2 - 2/dy2 [- 2/dz2] */
+} pgb_dbox;
+
+/* a tile of a box processed by one CTA */
+typedef struct {
+   int box;          /* global box index */
+   int i0, j0, k0;   /* 0-based tile origin */
+   int slot;         /* partial-sum slot of the box-local reduction */
+} pgb_tile;
+
+/* restriction (inject) op: src/transfer.c:1126-1149 + m_util_r8.f:20-50,649-830 */
+typedef struct {
+   int src_box, dst_box;
+   int i1, j1, k1;        /* fine start, 1-based */
+   int i2, j2, k2;        /* coarse start, 1-based */
+   int ni, nj, nk;        /* coarse extents */
+   int irho;
+   int op[PGB_NF];        /* per grid function: 0 none, 1 straight, 2 HW, 3 FW */
+} pgb_restrict_op;
+
+/* in-level copy (sync): src/transfer.c:1074-1079 */
+typedef struct {
+   int src_box, dst_box;
+   int i1, j1, k1, i2, j2, k2, ni, nj, nk;
+} pgb_copy_op;
+
+/* coarse -> fine interpolation: src/transfer.c:1007-1116 + dminterp3d */
+typedef struct {
+   int src_box, dst_box;
+   int i1i, j1i, k1i;     /* coarse window start, 1-based */
+   int nii, nji, nki;     /* window anchors per dimension */
+   int i2b, j2b, k2b;     /* start inside the interpolated window, 1-based */
+   int i2, j2, k2;        /* fine start, 1-based */
+   int nib, njb, nkb;     /* fine extents */
+   int irho, ord;
+} pgb_interp_op;
+
+/* a list of ops executed as ordered batches; ops within a batch write
+ * disjoint points */
+typedef struct {
+   int nops;
+   int nbatch;
+   int *batch_start;       /* host, nbatch+1 */
+   int *batch_maxpts;      /* host, largest op (in points) of each batch */
+   void *h_ops;            /* host copy */
+   void *d_ops;            /* device copy */
+} pgb_plan;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

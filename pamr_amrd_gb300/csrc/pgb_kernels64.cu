@@ -1,0 +1,867 @@
+/*
+ * FP64 multigrid kernels of libpamr_gb300 (sm_103a).
+ *
+ * This translation unit is compiled with -fmad=false: every product and sum
+ * is rounded separately, in the order of the reference's Fortran/C
+ * expressions, so results match the reference's CPU arithmetic bit for bit
+ * (examples/nbs/num.f:85-246 pattern for the operators, src/m_util_r8.f for
+ * the transfer operators, amrd/mg.c:242-355 for the FAS bookkeeping).
+ * Only the norm reductions are summed in a different (fixed, deterministic)
+ * order, so norms agree to about 1e-15 relative.
+ *
+ * Layout: every grid function of every box is a dense float64 array with x
+ * fastest (Fortran u(Nx,Ny,Nz)); a level's boxes are covered by a list of
+ * tiles, one CTA per tile. All boxes of a level are processed by one launch.
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include "pgb_dev.h"
+
+static __thread char g_err[256];
+
+extern "C" const char *pgb_dev_error(void) { return g_err; }
+
+static int check(const char *what)
+{
+   cudaError_t e = cudaGetLastError();
+   if (e != cudaSuccess) {
+      snprintf(g_err, sizeof(g_err), "%s: %s", what, cudaGetErrorString(e));
+      return 1;
+   }
+   return 0;
+}
+
+extern "C" int pgb_dev_sync(void *stream)
+{
+   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+   if (e != cudaSuccess) {
+      snprintf(g_err, sizeof(g_err), "stream sync: %s", cudaGetErrorString(e));
+      return 1;
+   }
+   return 0;
+}
+
+#define NT (PGB_TX * PGB_TY)
+
+/* ------------------------------------------------------------ operators -- */
+/* 2*pi and 5*2*pi, the constants of the conformal-factor hook */
+#define TWO_PI 6.283185307179586
+#define TEN_PI 31.41592653589793
+
+__device__ __forceinline__ double dterm(const pgb_dbox &b, double num, int d)
+{
+   return (b.flags & PGB_BOX_POW2DX) ? num * b.idx2[d] : num / b.dx2[d];
+}
+
+/* lap(u) at linear index p, num.f:113-115 order */
+__device__ __forceinline__ double lap64(const pgb_dbox &b, const double *u, long p, int dim)
+{
+   long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   double c = u[p];
+   double t = dterm(b, u[p + 1] - 2 * c + u[p - 1], 0) + dterm(b, u[p + sy] - 2 * c + u[p - sy], 1);
+   if (dim == 3) t = t + dterm(b, u[p + sz] - 2 * c + u[p - sz], 2);
+   return t;
+}
+
+__device__ __forceinline__ double op64(int pde, double t, double u, double s)
+{
+   if (pde == 1) {
+      double p2 = u * u, p4 = p2 * p2;
+      return t + TWO_PI * s * (p4 * u);
+   }
+   if (pde == 2) return t - s * u;
+   return t - s;
+}
+
+__device__ __forceinline__ double jac64(int pde, double j0, double u, double s)
+{
+   if (pde == 1) {
+      double p2 = u * u;
+      return j0 + TEN_PI * s * (p2 * p2);
+   }
+   if (pde == 2) return j0 - s;
+   return j0;
+}
+
+__device__ __forceinline__ bool interior(const pgb_dbox &b, int i, int j, int k, int dim)
+{
+   return i >= 1 && i <= b.n[0] - 2 && j >= 1 && j <= b.n[1] - 2 &&
+          (dim == 2 ? k == 0 : (k >= 1 && k <= b.n[2] - 2));
+}
+
+/* deterministic block sum of one double per thread (fixed tree) */
+__device__ double block_sum(double v, double *sm)
+{
+   int t = threadIdx.x + threadIdx.y * blockDim.x;
+   int nt = blockDim.x * blockDim.y;
+   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   if ((t & 31) == 0) sm[t >> 5] = v;
+   __syncthreads();
+   if (t < 32) {
+      v = (t < (nt >> 5)) ? sm[t] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   }
+   __syncthreads();
+   return v;   /* valid in thread 0 */
+}
+
+/* call_rr_app (amrd/util.c:73-103): per-box RMS, max over the level's boxes.
+ * Runs in the last CTA of a launch; sums the per-tile partials in a fixed
+ * order. npart = 1 (residual) or 2 (relax: two colour passes). */
+__device__ void finalize_norm(const pgb_dbox *boxes, const pgb_dlevel &lv, const int *tstart,
+                              int ntiles, int npart, pgb_scratch sc, double *norm_out,
+                              pgb_trace *trace, int kind, double *sm)
+{
+   int t = threadIdx.x + threadIdx.y * blockDim.x;
+   int nt = blockDim.x * blockDim.y;
+   double lres = 0;
+   for (int b = 0; b < lv.nbox; b++) {
+      double v = 0;
+      for (int q = 0; q < npart; q++)
+         for (int s = tstart[b] + t; s < tstart[b + 1]; s += nt) v += __ldcg(&sc.partial[q * ntiles + s]);
+      v = block_sum(v, sm);
+      if (t == 0) {
+         const pgb_dbox &bx = boxes[lv.box[b]];
+         double r = sqrt(v / bx.count);
+         if (b == 0) lres = r;
+         lres = (r > lres) ? r : lres;
+         if (trace) {
+            int n = trace->n;
+            if (n < trace->cap) {
+               pgb_trace_rec rr = {kind, lv.level, b, 1, r};
+               trace->rec[n] = rr;
+               trace->n = n + 1;
+            } else
+               trace->overflow = 1;
+         }
+      }
+   }
+   if (t == 0) {
+      *norm_out = lres;
+      *sc.counter = 0;
+   }
+}
+
+/* true in exactly one CTA: the last one to finish */
+__device__ bool last_block(pgb_scratch sc, int *flag)
+{
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0 && threadIdx.y == 0) {
+      unsigned int total = gridDim.x * gridDim.y;
+      unsigned int v = atomicAdd(sc.counter, 1u);
+      *flag = (v == total - 1);
+   }
+   __syncthreads();
+   return *flag != 0;
+}
+
+/* ---------------------------------------------------------------- relax -- */
+/* one colour pass of relax (num.f:216-241); pass 1 finalizes the norm */
+__global__ void __launch_bounds__(NT) k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                              int pass, pgb_scratch sc, double *norm_out,
+                                              pgb_trace *trace)
+{
+   __shared__ double sm[32];
+   __shared__ int flag;
+   const pgb_tile tl = lv.rtiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   double *u = b.f[PGB_F_U];
+   const double *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
+   double acc = 0;
+   int j = tl.j0 + threadIdx.y;
+   int kz = dim == 3 ? PGB_TZ : 1;
+   for (int kk = 0; kk < kz; kk++) {
+      int k = tl.k0 + kk;
+      int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
+      int i = tl.i0 + 2 * threadIdx.x + par;
+      if (!interior(b, i, j, k, dim)) continue;
+      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      double uc = u[p], s = src[p];
+      double res = op64(pde, lap64(b, u, p, dim), uc, s) - rhs[p];
+      double jac = jac64(pde, b.j0, uc, s);
+      u[p] = uc - res / jac;
+      acc += res * res;
+   }
+   acc = block_sum(acc, sm);
+   if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[pass * lv.nrtiles + blockIdx.x] = acc;
+   if (pass == 1 && last_block(sc, &flag))
+      finalize_norm(boxes, lv, lv.rtile_start, lv.nrtiles, 2, sc, norm_out, trace, 0, sm);
+}
+
+extern "C" int pgb_k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
+                           double *norm_out, pgb_trace *trace, void *stream)
+{
+   dim3 blk(PGB_TX, PGB_TY);
+   cudaStream_t st = (cudaStream_t)stream;
+   if (lv.nrtiles == 0) return 0;
+   k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 0, sc, norm_out, trace);
+   k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 1, sc, norm_out, trace);
+   return check("relax");
+}
+
+/* ------------------------------------------------------------- residual -- */
+/* residual (num.f:129-161): res = L[u] - rhs where cmask is ON */
+__global__ void __launch_bounds__(NT) k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                 pgb_scratch sc, double *norm_out,
+                                                 pgb_trace *trace)
+{
+   __shared__ double sm[32];
+   __shared__ int flag;
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const double *u = b.f[PGB_F_U], *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
+   double *res = b.f[PGB_F_RES];
+   double acc = 0;
+   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   int kz = dim == 3 ? PGB_TZ : 1;
+   for (int kk = 0; kk < kz; kk++) {
+      int k = tl.k0 + kk;
+      if (!interior(b, i, j, k, dim)) continue;
+      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      double r = op64(pde, lap64(b, u, p, dim), u[p], src[p]) - rhs[p];
+      res[p] = r;
+      acc += r * r;
+   }
+   acc = block_sum(acc, sm);
+   if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
+   if (last_block(sc, &flag))
+      finalize_norm(boxes, lv, lv.tile_start, lv.ntiles, 1, sc, norm_out, trace, 1, sm);
+}
+
+extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
+                              double *norm_out, pgb_trace *trace, void *stream)
+{
+   if (lv.ntiles == 0) return 0;
+   k_residual<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
+                                                                             norm_out, trace);
+   return check("residual");
+}
+
+/* ------------------------------------------------ pointwise level passes -- */
+#define FOR_TILE_POINTS(body)                                                        \
+   const pgb_tile tl = lv.tiles[blockIdx.x];                                         \
+   const pgb_dbox b = boxes[tl.box];                                                 \
+   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;                              \
+   int kz = lv.dim == 3 ? PGB_TZ : 1;                                                \
+   if (i < b.n[0] && j < b.n[1])                                                     \
+      for (int kk = 0; kk < kz; kk++) {                                              \
+         int k = tl.k0 + kk;                                                         \
+         if (k >= b.n[2]) break;                                                     \
+         long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);                         \
+         body                                                                        \
+      }
+
+__global__ void __launch_bounds__(NT) k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask)
+{
+   FOR_TILE_POINTS({
+      for (int f = 0; f < PGB_NF; f++)
+         if ((mask >> f) & 1) b.f[f][p] = 0;
+   })
+}
+
+/* app_L_op (num.f:85-123, lop = L[u] at interior cmask-child points) fused
+ * with compute_MG_rhs (amrd/mg.c:271-314): rhs = cmask ? -res*w0_r + lop : 0,
+ * then lop = u. lop was cleared by clear_MG_vars earlier in the same step. */
+__global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                double w0_r)
+{
+   FOR_TILE_POINTS({
+      const double *u = b.f[PGB_F_U];
+      double lopv = 0;
+      int cm = b.cmask_child[p];
+      if (cm && interior(b, i, j, k, lv.dim))
+         lopv = op64(pde, lap64(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
+      b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
+      b.f[PGB_F_LOP][p] = u[p];
+   })
+}
+
+/* compute_cgc first half (amrd/mg.c:332-341): res = (f - lop)/w0_i */
+__global__ void __launch_bounds__(NT) k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv,
+                                                   double w0_i)
+{
+   FOR_TILE_POINTS({ b.f[PGB_F_RES][p] = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) / w0_i; })
+}
+
+/* compute_cgc second half (amrd/mg.c:345-354): f += res */
+__global__ void __launch_bounds__(NT) k_add_res(const pgb_dbox *boxes, pgb_dlevel lv)
+{
+   FOR_TILE_POINTS({ b.f[PGB_F_U][p] += b.f[PGB_F_RES][p]; })
+}
+
+extern "C" int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_clear<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, mask);
+   return check("clear");
+}
+extern "C" int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
+                             void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_lop_rhs<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   return check("lop_rhs");
+}
+extern "C" int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_cgc_coarse<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, w0_i);
+   return check("cgc_coarse");
+}
+extern "C" int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_add_res<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   return check("add_res");
+}
+
+/* --------------------------------------------------------- op-list passes -- */
+/* point q of an ni x nj x nk segment -> (a,b,c) */
+__device__ __forceinline__ void unflat(long q, int ni, int nj, int &a, int &bb, int &c)
+{
+   a = (int)(q % ni);
+   long r = q / ni;
+   bb = (int)(r % nj);
+   c = (int)(r / nj);
+}
+
+__device__ __forceinline__ long lin(const pgb_dbox &b, int i1, int j1, int k1)
+{
+   /* 1-based (Fortran) indices */
+   return (i1 - 1) + (long)b.n[0] * ((j1 - 1) + (long)b.n[1] * (k1 - 1));
+}
+
+/* dmcopy3d with unit strides (src/m_util_r8.f:20-50) */
+__global__ void k_copy(const pgb_dbox *boxes, const pgb_copy_op *ops, int field)
+{
+   const pgb_copy_op o = ops[blockIdx.y];
+   long npts = (long)o.ni * o.nj * o.nk;
+   const pgb_dbox &s = boxes[o.src_box];
+   const pgb_dbox &d = boxes[o.dst_box];
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
+        q += (long)gridDim.x * blockDim.x) {
+      int a, bb, c;
+      unflat(q, o.ni, o.nj, a, bb, c);
+      d.f[field][lin(d, o.i2 + a, o.j2 + bb, o.k2 + c)] = s.f[field][lin(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
+   }
+}
+
+/* dmhwr3d (src/m_util_r8.f:649-723), do_ex = 0, at fine point (i0,j0,k0) */
+__device__ double hwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
+{
+   int w = 0;
+   double sum = 0;
+   long sy = nx1, sz = (long)nx1 * ny1;
+   long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
+   if (i0 > 1 && i0 <= nx1 - 1) {
+      w = w + 4;
+      sum = sum + u[p - 1] + 2 * u[p] + u[p + 1];
+   }
+   if (j0 > 1 && j0 <= ny1 - 1) {
+      w = w + 4;
+      sum = sum + u[p - sy] + 2 * u[p] + u[p + sy];
+   }
+   if (k0 > 1 && k0 <= nz1 - 1) {
+      w = w + 4;
+      sum = sum + u[p - sz] + 2 * u[p] + u[p + sz];
+   }
+   if (w > 0) return sum / w;
+   return u[p];
+}
+
+/* dmfwr3d (src/m_util_r8.f:733-830), do_ex = 0, at fine point (i0,j0,k0) */
+__device__ double fwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
+{
+   const long sy = nx1, sz = (long)nx1 * ny1;
+   const long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
+#define U(di, dj, dk) u[p + (di) + (dj) * sy + (dk) * sz]
+   bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
+   if (ii && jj && kk)
+      return (U(-1, -1, -1) + 2 * U(0, -1, -1) + U(1, -1, -1) +
+              2 * U(-1, 0, -1) + 4 * U(0, 0, -1) + 2 * U(1, 0, -1) +
+              U(-1, 1, -1) + 2 * U(0, 1, -1) + U(1, 1, -1) +
+              2 * U(-1, -1, 0) + 4 * U(0, -1, 0) + 2 * U(1, -1, 0) +
+              4 * U(-1, 0, 0) + 8 * U(0, 0, 0) + 4 * U(1, 0, 0) +
+              2 * U(-1, 1, 0) + 4 * U(0, 1, 0) + 2 * U(1, 1, 0) +
+              U(-1, -1, 1) + 2 * U(0, -1, 1) + U(1, -1, 1) +
+              2 * U(-1, 0, 1) + 4 * U(0, 0, 1) + 2 * U(1, 0, 1) +
+              U(-1, 1, 1) + 2 * U(0, 1, 1) + U(1, 1, 1)) / 64.0;
+   if (ii && jj)
+      return (1 * U(-1, -1, 0) + 2 * U(0, -1, 0) + 1 * U(1, -1, 0) +
+              2 * U(-1, 0, 0) + 4 * U(0, 0, 0) + 2 * U(1, 0, 0) +
+              1 * U(-1, 1, 0) + 2 * U(0, 1, 0) + 1 * U(1, 1, 0)) / 16.0;
+   if (jj && kk)
+      return (1 * U(0, -1, -1) + 2 * U(0, -1, 0) + 1 * U(0, -1, 1) +
+              2 * U(0, 0, -1) + 4 * U(0, 0, 0) + 2 * U(0, 0, 1) +
+              1 * U(0, 1, -1) + 2 * U(0, 1, 0) + 1 * U(0, 1, 1)) / 16.0;
+   if (ii && kk)
+      return (1 * U(-1, 0, -1) + 2 * U(-1, 0, 0) + 1 * U(-1, 0, 1) +
+              2 * U(0, 0, -1) + 4 * U(0, 0, 0) + 2 * U(0, 0, 1) +
+              1 * U(1, 0, -1) + 2 * U(1, 0, 0) + 1 * U(1, 0, 1)) / 16.0;
+   if (ii) return (U(-1, 0, 0) + 2 * U(0, 0, 0) + U(1, 0, 0)) / 4.0;
+   if (jj) return (U(0, -1, 0) + 2 * U(0, 0, 0) + U(0, 1, 0)) / 4.0;
+   if (kk) return (U(0, 0, -1) + 2 * U(0, 0, 0) + U(0, 0, 1)) / 4.0;
+   return U(0, 0, 0);
+#undef U
+}
+
+/* local_transfer delta = +1 (src/transfer.c:1126-1149): per grid function
+ * straight injection, half weighting or full weighting */
+__global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops)
+{
+   const pgb_restrict_op o = ops[blockIdx.y];
+   long npts = (long)o.ni * o.nj * o.nk;
+   const pgb_dbox &s = boxes[o.src_box];
+   const pgb_dbox &d = boxes[o.dst_box];
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
+        q += (long)gridDim.x * blockDim.x) {
+      int a, bb, c;
+      unflat(q, o.ni, o.nj, a, bb, c);
+      int i0 = o.i1 + a * o.irho, j0 = o.j1 + bb * o.irho, k0 = o.k1 + c * o.irho;
+      long pd = lin(d, o.i2 + a, o.j2 + bb, o.k2 + c);
+      for (int f = 0; f < PGB_NF; f++) {
+         int op = o.op[f];
+         if (!op) continue;
+         const double *u = s.f[f];
+         double v;
+         if (op == 1) v = u[lin(s, i0, j0, k0)];
+         else if (op == 2) v = hwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
+         else v = fwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
+         d.f[f][pd] = v;
+      }
+   }
+}
+
+/* one axis of dminterp3d's window (src/m_util_r8.f:65-144, 332-360): the
+ * anchors and weights of window point t; n = 1 means a copied anchor */
+__device__ __forceinline__ int stencil(int t, int irho, int nanch, int ord, int *a, double *cf)
+{
+   int m = t / irho, j = t - m * irho;
+   if (j == 0) {
+      a[0] = m;
+      return 1;
+   }
+   if (ord == 2 || nanch < 4) {
+      double sg = (j * 1.0) / irho;
+      cf[0] = 1 - sg;
+      cf[1] = sg;
+      a[0] = m;
+      a[1] = m + 1;
+      return 2;
+   }
+   double sg;
+   int base;
+   if (m == 0) {                 /* left end: i1 <= s1 always holds for the window */
+      sg = (j * 1.0) / irho;
+      base = 0;
+   } else if (m == nanch - 2) {  /* right end: (i1+n*s1) > (n1-2*s1) always holds */
+      sg = 2.0 + (j * 1.0) / irho;
+      base = nanch - 4;
+   } else {
+      sg = 1.0 + (j * 1.0) / irho;
+      base = m - 1;
+   }
+   const double HALF = 0.5, MHALF = -0.5;
+   const double SIXTH = 0.16666666666666667, MSIXTH = -0.16666666666666667;
+   cf[0] = MSIXTH * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
+   cf[1] = HALF * sg * (sg - 2.0) * (sg - 3.0);
+   cf[2] = MHALF * sg * (sg - 1.0) * (sg - 3.0);
+   cf[3] = SIXTH * sg * (sg - 1.0) * (sg - 2.0);
+   for (int q = 0; q < 4; q++) a[q] = base + q;
+   return 4;
+}
+
+/* sum c[0]*v[0] + c[1]*v[1] + ... left to right (Fortran order) */
+__device__ __forceinline__ double wsum(int n, const double *c, const double *v)
+{
+   if (n == 1) return v[0];
+   double r = c[0] * v[0] + c[1] * v[1];
+   if (n == 4) {
+      r = r + c[2] * v[2];
+      r = r + c[3] * v[3];
+   }
+   return r;
+}
+
+/* local_transfer delta = -1 (src/transfer.c:1085-1116): interpolate the
+ * coarse window (i-lines, then j-lines, then k-lines, as dminterp3d does)
+ * and write the requested fine segment */
+__global__ void k_interp(const pgb_dbox *boxes, const pgb_interp_op *ops, int field, int dim)
+{
+   const pgb_interp_op o = ops[blockIdx.y];
+   long npts = (long)o.nib * o.njb * o.nkb;
+   const pgb_dbox &s = boxes[o.src_box];
+   const pgb_dbox &d = boxes[o.dst_box];
+   const double *u = s.f[field];
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
+        q += (long)gridDim.x * blockDim.x) {
+      int a, bb, c;
+      unflat(q, o.nib, o.njb, a, bb, c);
+      int tx = o.i2b - 1 + a, ty = o.j2b - 1 + bb, tz = o.k2b - 1 + c;
+      int ax[4], ay[4], az[4];
+      double cx[4], cy[4], cz[4];
+      int nx = stencil(tx, o.irho, o.nii, o.ord, ax, cx);
+      int ny = stencil(ty, o.irho, o.nji, o.ord, ay, cy);
+      int nz = dim == 3 ? stencil(tz, o.irho, o.nki, o.ord, az, cz) : 1;
+      if (dim != 3) az[0] = 0;
+      double kv[4];
+      for (int r = 0; r < nz; r++) {
+         double jv[4];
+         for (int qq = 0; qq < ny; qq++) {
+            double iv[4];
+            for (int pp = 0; pp < nx; pp++)
+               iv[pp] = u[lin(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
+            jv[qq] = wsum(nx, cx, iv);
+         }
+         kv[r] = wsum(ny, cy, jv);
+      }
+      d.f[field][lin(d, o.i2 + a, o.j2 + bb, o.k2 + c)] = wsum(nz, cz, kv);
+   }
+}
+
+extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream)
+{
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      int gx = (p->batch_maxpts[bt] + 255) / 256;
+      if (gx > 512) gx = 512;
+      if (n <= 0 || gx <= 0) continue;
+      k_copy<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
+         boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt], field);
+   }
+   return check("copy");
+}
+
+extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *stream)
+{
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      int gx = (p->batch_maxpts[bt] + 255) / 256;
+      if (gx > 1024) gx = 1024;
+      if (n <= 0 || gx <= 0) continue;
+      k_restrict<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
+         boxes, (const pgb_restrict_op *)p->d_ops + p->batch_start[bt]);
+   }
+   return check("restrict");
+}
+
+extern "C" int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim,
+                            void *stream)
+{
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      int gx = (p->batch_maxpts[bt] + 255) / 256;
+      if (gx > 2048) gx = 2048;
+      if (n <= 0 || gx <= 0) continue;
+      k_interp<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
+         boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt], field, dim);
+   }
+   return check("interp");
+}
+
+/* ------------------------------------------------------- coarsest grids -- */
+/* The coarsest-grid loop of vcycle (amrd/mg.c:172-190) in one CTA: relax
+ * the coarsest boxes (both colours), take the call_rr_app norm, sync them
+ * (PAMR_sync(L,0,MGH,1) over coarsest grids only), until res <= ctol or
+ * max_citer. When the state after an iteration equals the state two
+ * iterations earlier, every later iteration repeats that cycle exactly, so
+ * the loop jumps to max_citer and lands on the same state and norm the
+ * reference reaches by iterating. */
+#define CT 1024
+__global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                 const pgb_copy_op *sync_ops, int nsync,
+                                                 pgb_coarsest_args a, pgb_trace *trace)
+{
+   __shared__ double sm[32];
+   __shared__ int s_changed;
+   const int t = threadIdx.x, dim = lv.dim;
+   double ctol = *a.res_dn * a.crtol;
+   double res = ctol + 1, res_prev = 0;
+   int iter = a.start_iter, history = 0;
+   double *prev1 = a.snap, *prev2 = a.snap + a.snap_points;
+   while (iter < a.max_citer && res > ctol) {
+      double lres = 0;
+      int first = 1;
+      for (int b = 0; b < lv.nbox; b++) {
+         const pgb_dbox bx = boxes[lv.box[b]];
+         if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+         long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
+         long npts = ni * nj * nk;
+         double acc = 0;
+         for (int pass = 0; pass < 2; pass++) {
+            for (long q = t; q < npts; q += CT) {
+               int i = 1 + (int)(q % ni), j = 1 + (int)((q / ni) % nj);
+               int k = dim == 3 ? 1 + (int)(q / (ni * nj)) : 0;
+               int par = dim == 3 ? ((i + j + k + 3 + pass) & 1) : ((i + j + 2 + pass) & 1);
+               if (par) continue;
+               long p = i + (long)bx.n[0] * (j + (long)bx.n[1] * k);
+               if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+               double *u = bx.f[PGB_F_U];
+               double uc = u[p], s = bx.f[PGB_F_SRC][p];
+               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
+               double jac = jac64(pde, bx.j0, uc, s);
+               u[p] = uc - r / jac;
+               acc += r * r;
+            }
+            __syncthreads();
+         }
+         acc = block_sum(acc, sm);
+         if (t == 0) {
+            double r = sqrt(acc / bx.count);
+            if (first) lres = r;
+            lres = (r > lres) ? r : lres;
+            first = 0;
+            if (trace) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rr = {0, lv.level, b, 1, r};
+                  trace->rec[n] = rr;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+         }
+         __syncthreads();
+      }
+      /* PAMR_sync(L,0,MGH,1) restricted to the coarsest grids */
+      for (int o = 0; o < nsync; o++) {
+         const pgb_copy_op op = sync_ops[o];
+         const pgb_dbox &s = boxes[op.src_box];
+         const pgb_dbox &d = boxes[op.dst_box];
+         long np = (long)op.ni * op.nj * op.nk;
+         for (long q = t; q < np; q += CT) {
+            int aa, bb, cc;
+            unflat(q, op.ni, op.nj, aa, bb, cc);
+            d.f[PGB_F_U][lin(d, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
+               s.f[PGB_F_U][lin(s, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
+         }
+         __syncthreads();
+      }
+      if (t == 0) sm[0] = lres;
+      __syncthreads();
+      res_prev = res;
+      res = sm[0];
+      __syncthreads();
+      iter++;
+      /* cycle detection on the coarsest boxes' u */
+      if (t == 0) s_changed = 0;
+      __syncthreads();
+      long off = 0;
+      for (int b = 0; b < lv.nbox; b++) {
+         const pgb_dbox bx = boxes[lv.box[b]];
+         if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+         long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+         for (long q = t; q < n; q += CT) {
+            double v = bx.f[PGB_F_U][q];
+            if (history >= 2 && prev2[off + q] != v) s_changed = 1;
+            prev2[off + q] = prev1[off + q];
+            prev1[off + q] = v;
+         }
+         off += n;
+      }
+      __syncthreads();
+      if (history < 2) history++;
+      if (history >= 2 && !s_changed && res > ctol && iter < a.max_citer) {
+         /* state == state two iterations ago: period 1 or 2 */
+         int rem = a.max_citer - iter;
+         if (rem & 1) {
+            /* final state is the previous one: restore it (prev2 now holds it) */
+            long off2 = 0;
+            for (int b = 0; b < lv.nbox; b++) {
+               const pgb_dbox bx = boxes[lv.box[b]];
+               if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+               long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+               for (long q = t; q < n; q += CT) bx.f[PGB_F_U][q] = prev2[off2 + q];
+               off2 += n;
+            }
+            res = res_prev;
+         }
+         if (trace && t == 0) {
+            int n = trace->n;
+            if (n < trace->cap) {
+               pgb_trace_rec rr = {2, lv.level, -1, rem, 0.0};
+               trace->rec[n] = rr;
+               trace->n = n + 1;
+            } else
+               trace->overflow = 1;
+         }
+         iter = a.max_citer;
+         __syncthreads();
+      }
+   }
+   if (t == 0) {
+      *a.res_out = res;
+      if (a.iters_out) *a.iters_out += iter - a.start_iter;
+   }
+}
+
+extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
+                              pgb_coarsest_args a, pgb_trace *trace, void *stream)
+{
+   k_coarsest<<<1, CT, 0, (cudaStream_t)stream>>>(boxes, lv, pde, (const pgb_copy_op *)sync->d_ops,
+                                                  sync->nops, a, trace);
+   return check("coarsest");
+}
+
+__global__ void k_fill(double *p, long n, double v)
+{
+   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+      p[i] = v;
+}
+
+extern "C" int pgb_k_fill(double *p, long n, double v, void *stream)
+{
+   long g = (n + 255) / 256;
+   if (g > 4096) g = 4096;
+   if (g < 1) g = 1;
+   k_fill<<<(int)g, 256, 0, (cudaStream_t)stream>>>(p, n, v);
+   return check("fill");
+}
+
+/* --------------------------------------- m_util_r8 on device arrays (ABI) -- */
+/* Same argument meaning as src/m_util_r8.f; out-of-range segments are a
+ * silent no-op there and here. */
+typedef struct {
+   int nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk;
+   int si1, sj1, sk1, si2, sj2, sk2;
+} mu_args;
+
+static bool mu_in_range(const mu_args &a)
+{
+   if (a.i1 < 1 || (a.i1 + (a.ni - 1) * a.si1) > a.nx1) return false;
+   if (a.i2 < 1 || (a.i2 + (a.ni - 1) * a.si2) > a.nx2) return false;
+   if (a.j1 < 1 || (a.j1 + (a.nj - 1) * a.sj1) > a.ny1) return false;
+   if (a.j2 < 1 || (a.j2 + (a.nj - 1) * a.sj2) > a.ny2) return false;
+   if (a.k1 < 1 || (a.k1 + (a.nk - 1) * a.sk1) > a.nz1) return false;
+   if (a.k2 < 1 || (a.k2 + (a.nk - 1) * a.sk2) > a.nz2) return false;
+   return true;
+}
+
+/* kind 1 copy (dmcopy3d), 2 half weight (dmhwr3d), 3 full weight (dmfwr3d) */
+__global__ void k_mutil(const double *u1, double *u2, mu_args a, int kind)
+{
+   long npts = (long)a.ni * a.nj * a.nk;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
+        q += (long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      unflat(q, a.ni, a.nj, i, j, k);
+      int i0 = a.i1 + i * a.si1, j0 = a.j1 + j * a.sj1, k0 = a.k1 + k * a.sk1;
+      long pd = (a.i2 + i * a.si2 - 1) + (long)a.nx2 * ((a.j2 + j * a.sj2 - 1) + (long)a.ny2 * (a.k2 + k * a.sk2 - 1));
+      double v;
+      if (kind == 1) v = u1[(i0 - 1) + (long)a.nx1 * ((j0 - 1) + (long)a.ny1 * (k0 - 1))];
+      else if (kind == 2) v = hwr(u1, a.nx1, a.ny1, a.nz1, i0, j0, k0);
+      else v = fwr(u1, a.nx1, a.ny1, a.nz1, i0, j0, k0);
+      u2[pd] = v;
+   }
+}
+
+static int mutil_launch(const double *u1, double *u2, mu_args a, int kind, void *stream)
+{
+   if (!mu_in_range(a)) return 0;
+   long npts = (long)a.ni * a.nj * a.nk;
+   long g = (npts + 255) / 256;
+   if (g > 4096) g = 4096;
+   if (g < 1) return 0;
+   k_mutil<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a, kind);
+   return check("m_util_r8");
+}
+
+#define MU_ARGS                                                                          \
+   mu_args a = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk,     \
+                si1, sj1, sk1, si2, sj2, sk2};
+#define MU_SIG                                                                           \
+   const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2, int nz2, \
+      int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk, int si1,  \
+      int sj1, int sk1, int si2, int sj2, int sk2, void *stream
+
+extern "C" int pgb_dmcopy3d(MU_SIG) { MU_ARGS return mutil_launch(u1, u2, a, 1, stream); }
+extern "C" int pgb_dmhwr3d(MU_SIG) { MU_ARGS return mutil_launch(u1, u2, a, 2, stream); }
+extern "C" int pgb_dmfwr3d(MU_SIG) { MU_ARGS return mutil_launch(u1, u2, a, 3, stream); }
+
+/* dminterp3d (src/m_util_r8.f:473-637), do_ex = 0, on a segment of u2.
+ * Cubic lines use one-sided stencils at a segment end only where the
+ * Fortran does (left: start <= rho, right: start + n*rho > N - 2*rho);
+ * segments whose cubic lines would take interior stencils reaching outside
+ * the segment are rejected. */
+typedef struct {
+   int nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk, si1, sj1, sk1;
+   int irho, jrho, krho, ord, dim;
+} mi_args;
+
+__device__ __forceinline__ int mi_stencil(int t, int rho, int n, int ord, int *a, double *cf)
+{
+   return stencil(t, rho, n, ord, a, cf);
+}
+
+__global__ void k_minterp(const double *u1, double *u2, mi_args a)
+{
+   long ex = (long)(a.ni - 1) * a.irho + 1, ey = (long)(a.nj - 1) * a.jrho + 1;
+   long ez = a.dim == 3 ? (long)(a.nk - 1) * a.krho + 1 : 1;
+   long npts = ex * ey * ez;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
+        q += (long)gridDim.x * blockDim.x) {
+      int tx = (int)(q % ex), ty = (int)((q / ex) % ey), tz = (int)(q / (ex * ey));
+      int ax[4], ay[4], az[4];
+      double cx[4], cy[4], cz[4];
+      int nx = mi_stencil(tx, a.irho, a.ni, a.ord, ax, cx);
+      int ny = mi_stencil(ty, a.jrho, a.nj, a.ord, ay, cy);
+      int nz = a.dim == 3 ? mi_stencil(tz, a.krho, a.nk, a.ord, az, cz) : 1;
+      if (a.dim != 3) az[0] = 0;
+      double kv[4];
+      for (int r = 0; r < nz; r++) {
+         double jv[4];
+         for (int qq = 0; qq < ny; qq++) {
+            double iv[4];
+            for (int pp = 0; pp < nx; pp++) {
+               int ci = a.i1 + ax[pp] * a.si1, cj = a.j1 + ay[qq] * a.sj1, ck = a.k1 + az[r] * a.sk1;
+               iv[pp] = u1[(ci - 1) + (long)a.nx1 * ((cj - 1) + (long)a.ny1 * (ck - 1))];
+            }
+            jv[qq] = wsum(nx, cx, iv);
+         }
+         kv[r] = wsum(ny, cy, jv);
+      }
+      long pd = (a.i2 + tx - 1) + (long)a.nx2 * ((a.j2 + ty - 1) + (long)a.ny2 * (a.k2 + tz - 1));
+      u2[pd] = wsum(nz, cz, kv);
+   }
+}
+
+extern "C" int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2,
+                              int ny2, int nz2, int i1, int j1, int k1, int i2, int j2, int k2,
+                              int ni, int nj, int nk, int si1, int sj1, int sk1, int irho, int jrho,
+                              int krho, int ord, void *stream)
+{
+   mi_args a = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk,
+                si1, sj1, sk1, irho, jrho, krho, ord, nz2 > 1 || nk > 1 ? 3 : 2};
+   if (i1 < 1 || (i1 + ni - 1) * si1 > nx1) return 0;
+   if (i2 < 1 || (i2 + (ni - 1) * irho) > nx2) return 0;
+   if (j1 < 1 || (j1 + nj - 1) * sj1 > ny1) return 0;
+   if (j2 < 1 || (j2 + (nj - 1) * jrho) > ny2) return 0;
+   if (k1 < 1 || (k1 + nk - 1) * sk1 > nz1) return 0;
+   if (k2 < 1 || (k2 + (nk - 1) * krho) > nz2) return 0;
+   if (ord != 2 && ord != 4) {
+      snprintf(g_err, sizeof(g_err), "dminterp3d: only ord=2,4 supported");
+      return 12;
+   }
+   if (ord == 4) {
+      int st[3] = {i2, j2, k2}, n[3] = {ni, nj, nk}, r[3] = {irho, jrho, krho}, N[3] = {nx2, ny2, nz2};
+      for (int d = 0; d < 3; d++)
+         if (n[d] >= 4 && !(st[d] <= r[d] && st[d] + n[d] * r[d] > N[d] - 2 * r[d])) {
+            snprintf(g_err, sizeof(g_err),
+                     "dminterp3d: cubic segment needs data outside it (unsupported)");
+            return 12;
+         }
+   }
+   if (nj == 1 && nk == 1) a.dim = 2;
+   long npts = ((long)(ni - 1) * irho + 1) * ((long)(nj - 1) * jrho + 1) *
+               (a.dim == 3 ? (long)(nk - 1) * krho + 1 : 1);
+   long g = (npts + 255) / 256;
+   if (g > 4096) g = 4096;
+   if (g < 1) return 0;
+   k_minterp<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a);
+   return check("dminterp3d");
+}

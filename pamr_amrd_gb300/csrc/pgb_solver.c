@@ -1,0 +1,682 @@
+/*
+ * libpamr_gb300 host driver (C): device arena, plan upload and the FAS
+ * V-cycle of amrd/mg.c:84-201 issued as kernel launches on one stream.
+ *
+ * The control flow is the reference's; every norm stays on the device (the
+ * coarsest-grid loop runs inside one kernel), so a V-cycle needs a single
+ * device-to-host read: the finest residual that solve_elliptics compares
+ * with MG_tol (amrd/mg.c:57).
+ */
+#include <cuda_runtime_api.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "pamr_gb300.h"
+#include "pgb_dev.h"
+#include "pgb_plan.h"
+
+/* norm slots per level */
+enum { N_RELAX_DN = 0, N_RELAX_UP = 1, N_RESID = 2, N_COARSE = 3, N_SLOTS = 4 };
+
+struct pgb_solver {
+   pgb_hier h;
+   int host_only;
+   cudaStream_t stream;
+   char *arena;
+   size_t arena_bytes;
+   pgb_dbox *hbox;          /* host copy of the device box table */
+   pgb_dbox *dbox;
+   pgb_dlevel lv[PGB_MAXLEV + 1];
+   void *d_tables[PGB_MAXLEV + 1];
+   pgb_scratch sc;
+   double *d_norms;         /* [(nlev+1) * N_SLOTS] */
+   int *d_citers;
+   double *d_snap;
+   long snap_points;
+   long *d_snap_off[PGB_MAXLEV + 1];
+   pgb_trace *d_trace;
+   int trace_cap;
+   double *h_res;           /* pinned */
+   cudaEvent_t ev0, ev1;
+   int last_cycles;
+   long last_citers;
+   double last_ms;
+};
+
+static __thread char g_err[512];
+
+const char *pgb_last_error(void) { return g_err; }
+
+static int fail(int code, const char *fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(g_err, sizeof(g_err), fmt, ap);
+   va_end(ap);
+   return code;
+}
+
+#define CU(call)                                                                    \
+   do {                                                                             \
+      cudaError_t e_ = (call);                                                      \
+      if (e_ != cudaSuccess) return fail(10, "%s: %s", #call, cudaGetErrorString(e_)); \
+   } while (0)
+#define KC(call)                                                                    \
+   do {                                                                             \
+      if (call) return fail(11, "%s", pgb_dev_error());                              \
+   } while (0)
+
+void pgb_default_params(pgb_mg_params *p)
+{
+   memset(p, 0, sizeof(*p));
+   p->pre_swp = p->pst_swp = 2;
+   p->max_iter = 50;
+   p->min_iter = 1;
+   p->max_citer = 5000;
+   p->tol = 0;
+   p->crtol = 1.0e-3;
+   p->w0_r = p->w0_i = 1.0;
+   p->min_cwidth = 3;
+   p->restr_u = PGB_HW_RESTR;
+   p->restr_res = PGB_FW_RESTR;
+   p->restr_src = PGB_HW_RESTR;
+   p->interp_order = 2;
+   p->interp_buffer = 2;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* tiles of the boxes of one level; tx = tile width in x */
+static int make_tiles(const pgb_hier *h, int L, int tx, pgb_tile **out, int *start)
+{
+   int b, n = 0, cap = 64;
+   pgb_tile *t = (pgb_tile *)malloc(sizeof(pgb_tile) * (size_t)cap);
+   int tz = h->dim == 3 ? PGB_TZ : 1;
+   for (b = 0; b < h->lev[L].nbox; b++) {
+      const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+      int i, j, k;
+      start[b] = n;
+      for (k = 0; k < bx->shape[2]; k += tz)
+         for (j = 0; j < bx->shape[1]; j += PGB_TY)
+            for (i = 0; i < bx->shape[0]; i += tx) {
+               if (n == cap) {
+                  cap *= 2;
+                  t = (pgb_tile *)realloc(t, sizeof(pgb_tile) * (size_t)cap);
+               }
+               t[n].box = h->lev[L].box[b];
+               t[n].i0 = i;
+               t[n].j0 = j;
+               t[n].k0 = k;
+               t[n].slot = n;
+               n++;
+            }
+   }
+   start[h->lev[L].nbox] = n;
+   *out = t;
+   return n;
+}
+
+static int upload_plan(pgb_plan *p, size_t opsz)
+{
+   if (!p->nops) return 0;
+   CU(cudaMalloc(&p->d_ops, opsz * (size_t)p->nops));
+   CU(cudaMemcpy(p->d_ops, p->h_ops, opsz * (size_t)p->nops, cudaMemcpyHostToDevice));
+   return 0;
+}
+
+static void free_plan_dev(pgb_plan *p)
+{
+   if (p->d_ops) cudaFree(p->d_ops);
+   p->d_ops = 0;
+}
+
+static int setup_device(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   size_t off = 0, *fo;
+   int i, f, L, d, maxt = 1, maxbox = 1;
+   long snap_pts = 0;
+   CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+   CU(cudaEventCreate(&s->ev0));
+   CU(cudaEventCreate(&s->ev1));
+   /* arena layout: per box, 5 float64 grid functions then 2 byte masks */
+   fo = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * (PGB_NF + 2));
+   for (i = 0; i < h->nbox; i++) {
+      const pgb_hbox *b = &h->boxes[i];
+      size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+      for (f = 0; f < PGB_NF; f++) {
+         fo[i * (PGB_NF + 2) + f] = off;
+         off = align256(off + 8 * n);
+      }
+      fo[i * (PGB_NF + 2) + PGB_NF] = off;
+      off = align256(off + n);
+      fo[i * (PGB_NF + 2) + PGB_NF + 1] = off;
+      off = align256(off + n);
+   }
+   s->arena_bytes = off;
+   CU(cudaMalloc((void **)&s->arena, off));
+   CU(cudaMemset(s->arena, 0, off));
+   s->hbox = (pgb_dbox *)calloc((size_t)h->nbox, sizeof(pgb_dbox));
+   for (i = 0; i < h->nbox; i++) {
+      const pgb_hbox *b = &h->boxes[i];
+      pgb_dbox *db = &s->hbox[i];
+      size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+      double dx2[3] = {1, 1, 1};
+      for (f = 0; f < PGB_NF; f++) db->f[f] = (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
+      db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
+      db->cmask_bdy = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF + 1]);
+      CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
+      CU(cudaMemcpy((void *)db->cmask_bdy, b->bdy_mask, n, cudaMemcpyHostToDevice));
+      for (d = 0; d < 3; d++) db->n[d] = b->shape[d];
+      db->flags = b->flags;
+      db->level = b->level;
+      db->count = b->count;
+      /* dx = x(2)-x(1) of the grid's coordinates, dx2 = dx**2 (num.f:191-197) */
+      for (d = 0; d < h->dim; d++) {
+         double dx = b->x[d][1] - b->x[d][0];
+         dx2[d] = dx * dx;
+      }
+      for (d = 0; d < 3; d++) {
+         db->dx2[d] = dx2[d];
+         db->idx2[d] = 1.0 / dx2[d];
+      }
+      if (h->dim == 3) db->j0 = -2 / dx2[0] - 2 / dx2[1] - 2 / dx2[2];
+      else db->j0 = -2 / dx2[0] - 2 / dx2[1];
+   }
+   free(fo);
+   CU(cudaMalloc((void **)&s->dbox, sizeof(pgb_dbox) * (size_t)h->nbox));
+   CU(cudaMemcpy(s->dbox, s->hbox, sizeof(pgb_dbox) * (size_t)h->nbox, cudaMemcpyHostToDevice));
+
+   /* per-level tables: tiles, relax tiles, tile starts, box lists */
+   for (L = 1; L <= h->nlev; L++) {
+      pgb_tile *t = 0, *rt = 0;
+      int nb = h->lev[L].nbox;
+      int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
+      int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
+      int nt = make_tiles(h, L, PGB_TX, &t, ts);
+      int nrt = make_tiles(h, L, 2 * PGB_TX, &rt, rts);
+      size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
+      size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
+      size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
+      size_t b4 = b3 + align256(sizeof(int) * (size_t)(nb + 1));
+      size_t b5 = b4 + align256(sizeof(int) * (size_t)nb);
+      char *dt;
+      CU(cudaMalloc(&s->d_tables[L], b5));
+      dt = (char *)s->d_tables[L];
+      CU(cudaMemcpy(dt + b0, t, sizeof(pgb_tile) * (size_t)nt, cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(dt + b1, rt, sizeof(pgb_tile) * (size_t)nrt, cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(dt + b2, ts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(dt + b3, rts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice));
+      s->lv[L].tiles = (const pgb_tile *)(dt + b0);
+      s->lv[L].rtiles = (const pgb_tile *)(dt + b1);
+      s->lv[L].tile_start = (const int *)(dt + b2);
+      s->lv[L].rtile_start = (const int *)(dt + b3);
+      s->lv[L].box = (const int *)(dt + b4);
+      s->lv[L].ntiles = nt;
+      s->lv[L].nrtiles = nrt;
+      s->lv[L].nbox = nb;
+      s->lv[L].dim = h->dim;
+      s->lv[L].level = L;
+      if (nt > maxt) maxt = nt;
+      if (nrt > maxt) maxt = nrt;
+      if (nb > maxbox) maxbox = nb;
+      free(t);
+      free(rt);
+      free(ts);
+      free(rts);
+      /* snapshot offsets of the coarsest boxes of this level */
+      {
+         long o = 0, *so = (long *)calloc((size_t)nb + 1, sizeof(long));
+         int any = 0;
+         for (i = 0; i < nb; i++) {
+            const pgb_hbox *b = &h->boxes[h->lev[L].box[i]];
+            so[i] = o;
+            if (b->coarsest) {
+               o += (long)b->shape[0] * b->shape[1] * b->shape[2];
+               any = 1;
+            }
+         }
+         so[nb] = o;
+         if (any) {
+            CU(cudaMalloc((void **)&s->d_snap_off[L], sizeof(long) * (size_t)(nb + 1)));
+            CU(cudaMemcpy(s->d_snap_off[L], so, sizeof(long) * (size_t)(nb + 1), cudaMemcpyHostToDevice));
+         }
+         if (o > snap_pts) snap_pts = o;
+         free(so);
+      }
+      if (upload_plan(&h->sync[L][0], sizeof(pgb_copy_op)) ||
+          upload_plan(&h->sync[L][1], sizeof(pgb_copy_op)) ||
+          upload_plan(&h->sync_coarsest[L], sizeof(pgb_copy_op)) ||
+          upload_plan(&h->inject[L], sizeof(pgb_restrict_op)) ||
+          upload_plan(&h->inject_init[L], sizeof(pgb_restrict_op)) ||
+          upload_plan(&h->interp[L], sizeof(pgb_interp_op)))
+         return 10;
+   }
+   CU(cudaMalloc((void **)&s->sc.partial, sizeof(double) * 2 * (size_t)maxt));
+   CU(cudaMalloc((void **)&s->sc.counter, sizeof(unsigned int)));
+   CU(cudaMemset(s->sc.counter, 0, sizeof(unsigned int)));
+   CU(cudaMalloc((void **)&s->sc.box_norm, sizeof(double) * (size_t)maxbox));
+   CU(cudaMalloc((void **)&s->d_norms, sizeof(double) * N_SLOTS * (size_t)(h->nlev + 1)));
+   CU(cudaMemset(s->d_norms, 0, sizeof(double) * N_SLOTS * (size_t)(h->nlev + 1)));
+   CU(cudaMalloc((void **)&s->d_citers, sizeof(int)));
+   s->snap_points = snap_pts;
+   CU(cudaMalloc((void **)&s->d_snap, sizeof(double) * 2 * (size_t)(snap_pts ? snap_pts : 1)));
+   CU(cudaMallocHost((void **)&s->h_res, sizeof(double) * 4));
+   return 0;
+}
+
+int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox, int ngrids,
+               const int *grid_level, const double *grid_bbox, const pgb_mg_params *params,
+               int flags, pgb_solver **out)
+{
+   pgb_solver *s;
+   pgb_hparams hp;
+   int rc;
+   *out = 0;
+   if (pde < 0 || pde > 2) return fail(1, "unknown pde kind %d", pde);
+   if (params->interp_order != 2 && params->interp_order != 4)
+      return fail(1, "interp_order must be 2 or 4");
+   if (params->restr_u < 0 || params->restr_u > 3 || params->restr_res < 0 ||
+       params->restr_res > 3 || params->restr_src < 0 || params->restr_src > 3)
+      return fail(1, "restriction operators must be 0..3");
+   s = (pgb_solver *)calloc(1, sizeof(*s));
+   hp.pre_swp = params->pre_swp;
+   hp.pst_swp = params->pst_swp;
+   hp.max_iter = params->max_iter;
+   hp.min_iter = params->min_iter;
+   hp.max_citer = params->max_citer;
+   hp.tol = params->tol;
+   hp.crtol = params->crtol;
+   hp.w0_r = params->w0_r;
+   hp.w0_i = params->w0_i;
+   hp.min_cwidth = params->min_cwidth;
+   hp.restr_u = params->restr_u;
+   hp.restr_res = params->restr_res;
+   hp.restr_src = params->restr_src;
+   hp.interp_order = params->interp_order;
+   hp.interp_buffer = params->interp_buffer;
+   rc = pgb_hier_build(&s->h, dim, pde, base_shape, base_bbox, ngrids, grid_level, grid_bbox, &hp);
+   if (rc) {
+      fail(2, "hierarchy: %s", s->h.err);
+      pgb_hier_free(&s->h);
+      free(s);
+      return 2;
+   }
+   s->host_only = (flags & PGB_HOST_ONLY) != 0;
+   if (!s->host_only && (rc = setup_device(s))) {
+      pgb_destroy(s);
+      return rc;
+   }
+   *out = s;
+   return 0;
+}
+
+int pgb_destroy(pgb_solver *s)
+{
+   int L;
+   if (!s) return 0;
+   if (!s->host_only) {
+      for (L = 1; L <= s->h.nlev; L++) {
+         free_plan_dev(&s->h.sync[L][0]);
+         free_plan_dev(&s->h.sync[L][1]);
+         free_plan_dev(&s->h.sync_coarsest[L]);
+         free_plan_dev(&s->h.inject[L]);
+         free_plan_dev(&s->h.inject_init[L]);
+         free_plan_dev(&s->h.interp[L]);
+         if (s->d_tables[L]) cudaFree(s->d_tables[L]);
+         if (s->d_snap_off[L]) cudaFree(s->d_snap_off[L]);
+      }
+      if (s->arena) cudaFree(s->arena);
+      if (s->dbox) cudaFree(s->dbox);
+      if (s->sc.partial) cudaFree(s->sc.partial);
+      if (s->sc.counter) cudaFree(s->sc.counter);
+      if (s->sc.box_norm) cudaFree(s->sc.box_norm);
+      if (s->d_norms) cudaFree(s->d_norms);
+      if (s->d_citers) cudaFree(s->d_citers);
+      if (s->d_snap) cudaFree(s->d_snap);
+      if (s->d_trace) cudaFree(s->d_trace);
+      if (s->h_res) cudaFreeHost(s->h_res);
+      if (s->stream) {
+         cudaEventDestroy(s->ev0);
+         cudaEventDestroy(s->ev1);
+         cudaStreamDestroy(s->stream);
+      }
+   }
+   free(s->hbox);
+   pgb_hier_free(&s->h);
+   free(s);
+   return 0;
+}
+
+void *pgb_stream(pgb_solver *s) { return (void *)s->stream; }
+
+/* ---------------------------------------------------------------- data -- */
+static int grid_box(const pgb_solver *s, int grid, const pgb_hbox **b)
+{
+   if (grid < 0 || grid >= s->h.ngrids) return fail(3, "grid %d out of range", grid);
+   *b = &s->h.boxes[s->h.grid_box[grid]];
+   return 0;
+}
+
+int pgb_grid_shape(const pgb_solver *s, int grid, int *shape3)
+{
+   const pgb_hbox *b = 0;
+   if (grid_box(s, grid, &b)) return 3;
+   memcpy(shape3, b->shape, sizeof(int) * 3);
+   return 0;
+}
+
+static int copy_grid(pgb_solver *s, int grid, const double *u, const double *src, double *uout,
+                     enum cudaMemcpyKind kin, enum cudaMemcpyKind kout)
+{
+   const pgb_hbox *b = 0;
+   const pgb_dbox *db;
+   size_t n;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (grid_box(s, grid, &b)) return 3;
+   db = &s->hbox[s->h.grid_box[grid]];
+   n = sizeof(double) * (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+   if (u) CU(cudaMemcpyAsync(db->f[PGB_F_U], u, n, kin, s->stream));
+   if (src) CU(cudaMemcpyAsync(db->f[PGB_F_SRC], src, n, kin, s->stream));
+   if (uout) {
+      CU(cudaMemcpyAsync(uout, db->f[PGB_F_U], n, kout, s->stream));
+      CU(cudaStreamSynchronize(s->stream));
+   }
+   return 0;
+}
+
+int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src)
+{
+   int rc = copy_grid(s, grid, u, src, 0, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+   if (!rc) CU(cudaStreamSynchronize(s->stream));
+   return rc;
+}
+int pgb_get_grid(pgb_solver *s, int grid, double *u)
+{
+   return copy_grid(s, grid, 0, 0, u, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+int pgb_set_grid_device(pgb_solver *s, int grid, const double *u, const double *src)
+{
+   return copy_grid(s, grid, u, src, 0, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
+}
+int pgb_get_grid_device(pgb_solver *s, int grid, double *u)
+{
+   return copy_grid(s, grid, 0, 0, u, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
+}
+
+/* ------------------------------------------------------------- V-cycle -- */
+static double *norm_slot(pgb_solver *s, int L, int k) { return s->d_norms + N_SLOTS * L + k; }
+
+static int lvl_coarsest(const pgb_solver *s, int L)   /* is_coarsest amrd/mg.c:553-567 */
+{
+   int b;
+   for (b = 0; b < s->h.lev[L].nbox; b++)
+      if (s->h.boxes[s->h.lev[L].box[b]].coarsest) return 1;
+   return 0;
+}
+
+static int relax(pgb_solver *s, int L, int slot)
+{
+   KC(pgb_k_relax(s->dbox, s->lv[L], s->h.pde, s->sc, norm_slot(s, L, slot), s->d_trace, s->stream));
+   return 0;
+}
+
+static int sync_field(pgb_solver *s, const pgb_plan *p, int field)
+{
+   if (p->nops) KC(pgb_k_copy(s->dbox, p, field, s->stream));
+   return 0;
+}
+
+/* initialisation the reference performs while building the MG hierarchy
+ * (build_mgh src/gh.c:1222-1365): MG-only grid functions start at zero and
+ * pure MG levels receive u and the source by TF_MGH_INIT injection */
+int pgb_prepare(pgb_solver *s)
+{
+   int L;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   for (L = 1; L <= s->h.nlev; L++) {
+      int mask = (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS);
+      if (!s->h.lev[L].in_amrh) mask |= (1 << PGB_F_U) | (1 << PGB_F_SRC);
+      KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
+   }
+   for (L = s->h.nlev - 1; L >= 1; L--)
+      if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], s->stream));
+   CU(cudaMemsetAsync(s->d_citers, 0, sizeof(int), s->stream));
+   return 0;
+}
+
+static int vcycle_launch(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const pgb_hparams *p = &h->prm;
+   int L, Lf = h->nlev, it;
+   /* clear_MG_vars(Lf) amrd/mg.c:91 */
+   KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
+   for (L = Lf; L > 0; L--) {
+      if (L < Lf) {
+         KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
+                           s->d_trace, s->stream));
+         if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;   /* set_res_sync */
+         /* clear_MG_vars(L): rhs and lop are rewritten whole by lop_rhs below */
+         KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], s->stream));
+         if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
+         KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+      }
+      for (it = 0; it < p->pre_swp; it++) {
+         if (relax(s, L, N_RELAX_DN)) return 11;
+         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
+      }
+   }
+   for (L = 1; L <= Lf; L++) {
+      if (L > 1) {
+         KC(pgb_k_cgc_coarse(s->dbox, s->lv[L - 1], p->w0_i, s->stream));
+         if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
+         KC(pgb_k_add_res(s->dbox, s->lv[L], s->stream));
+      }
+      for (it = 0; it < p->pst_swp; it++) {
+         if (relax(s, L, N_RELAX_UP)) return 11;
+         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
+      }
+      if (lvl_coarsest(s, L)) {
+         pgb_coarsest_args a;
+         a.start_iter = p->pst_swp;
+         a.max_citer = p->max_citer;
+         a.crtol = p->crtol;
+         a.res_dn = norm_slot(s, L, p->pre_swp > 0 ? N_RELAX_DN : N_COARSE);
+         a.res_out = norm_slot(s, L, N_COARSE);
+         a.iters_out = s->d_citers;
+         a.snap = s->d_snap;
+         a.snap_points = s->snap_points;
+         a.snap_off = s->d_snap_off[L];
+         KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
+      }
+      if (L == Lf)
+         KC(pgb_k_residual(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID), s->d_trace,
+                           s->stream));
+   }
+   return 0;
+}
+
+int pgb_vcycle(pgb_solver *s, double *res)
+{
+   int rc;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if ((rc = vcycle_launch(s))) return rc;
+   CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double),
+                      cudaMemcpyDeviceToHost, s->stream));
+   CU(cudaStreamSynchronize(s->stream));
+   *res = s->h_res[0];
+   return 0;
+}
+
+int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycle, int cap)
+{
+   const pgb_hparams *p = &s->h.prm;
+   double res = p->tol + 1;
+   int it = 0, rc, ci = 0;
+   float ms = 0;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   CU(cudaEventRecord(s->ev0, s->stream));
+   if ((rc = pgb_prepare(s))) return rc;
+   while ((it < p->min_iter || res > p->tol) && it < p->max_iter) {
+      if ((rc = pgb_vcycle(s, &res))) return rc;
+      if (res_per_cycle && it < cap) res_per_cycle[it] = res;
+      it++;
+   }
+   CU(cudaEventRecord(s->ev1, s->stream));
+   CU(cudaMemcpyAsync(s->h_res + 1, s->d_citers, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+   CU(cudaStreamSynchronize(s->stream));
+   CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+   memcpy(&ci, s->h_res + 1, sizeof(int));
+   s->last_cycles = it;
+   s->last_citers = ci;
+   s->last_ms = ms;
+   if (iters) *iters = it;
+   if (res_final) *res_final = res;
+   return 0;
+}
+
+int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms)
+{
+   if (vcycles) *vcycles = s->last_cycles;
+   if (coarsest_iters) *coarsest_iters = s->last_citers;
+   if (device_ms) *device_ms = s->last_ms;
+   return 0;
+}
+
+/* ---------------------------------------------------------------- trace -- */
+int pgb_trace_enable(pgb_solver *s, int capacity)
+{
+   int hdr[4] = {0, capacity, 0, 0};
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (s->d_trace) cudaFree(s->d_trace);
+   s->d_trace = 0;
+   s->trace_cap = 0;
+   if (capacity <= 0) return 0;
+   CU(cudaMalloc((void **)&s->d_trace, sizeof(pgb_trace) + sizeof(pgb_trace_rec) * (size_t)capacity));
+   CU(cudaMemcpy(s->d_trace, hdr, sizeof(hdr), cudaMemcpyHostToDevice));
+   s->trace_cap = capacity;
+   return 0;
+}
+
+int pgb_trace_fetch(pgb_solver *s, int *kind, int *level, int *box, int *repeat, double *norm,
+                    int cap, int *n)
+{
+   int hdr[4], i, m;
+   pgb_trace_rec *r;
+   if (!s->d_trace) return fail(5, "trace not enabled");
+   CU(cudaStreamSynchronize(s->stream));
+   CU(cudaMemcpy(hdr, s->d_trace, sizeof(hdr), cudaMemcpyDeviceToHost));
+   m = hdr[0] < cap ? hdr[0] : cap;
+   r = (pgb_trace_rec *)malloc(sizeof(pgb_trace_rec) * (size_t)(m ? m : 1));
+   CU(cudaMemcpy(r, s->d_trace->rec, sizeof(pgb_trace_rec) * (size_t)m, cudaMemcpyDeviceToHost));
+   for (i = 0; i < m; i++) {
+      kind[i] = r[i].kind;
+      level[i] = r[i].level;
+      box[i] = r[i].box;
+      repeat[i] = r[i].repeat;
+      norm[i] = r[i].norm;
+   }
+   free(r);
+   *n = m;
+   hdr[0] = 0;
+   CU(cudaMemcpy(s->d_trace, hdr, sizeof(int), cudaMemcpyHostToDevice));
+   if (hdr[2]) return fail(6, "trace overflowed");
+   return 0;
+}
+
+/* ------------------------------------------------------------ queries -- */
+int pgb_num_levels(const pgb_solver *s) { return s->h.nlev; }
+
+int pgb_level_nbox(const pgb_solver *s, int L)
+{
+   if (L < 1 || L > s->h.nlev) return -1;
+   return s->h.lev[L].nbox;
+}
+
+static const pgb_hbox *lbox(const pgb_solver *s, int L, int idx)
+{
+   if (L < 1 || L > s->h.nlev || idx < 0 || idx >= s->h.lev[L].nbox) return 0;
+   return &s->h.boxes[s->h.lev[L].box[idx]];
+}
+
+int pgb_box_info(const pgb_solver *s, int L, int idx, int *shape3, double *bbox6, int *coarsest,
+                 int *amr_grid)
+{
+   const pgb_hbox *b = lbox(s, L, idx);
+   if (!b) return fail(3, "no box %d on level %d", idx, L);
+   if (shape3) memcpy(shape3, b->shape, sizeof(int) * 3);
+   if (bbox6) memcpy(bbox6, b->bbox, sizeof(double) * 6);
+   if (coarsest) *coarsest = b->coarsest;
+   if (amr_grid) *amr_grid = b->amr_grid;
+   return 0;
+}
+
+int pgb_box_cmask(const pgb_solver *s, int L, int idx, int kind, double *out)
+{
+   const pgb_hbox *b = lbox(s, L, idx);
+   long n, i;
+   const uint8_t *m;
+   if (!b) return fail(3, "no box %d on level %d", idx, L);
+   m = kind ? b->child_mask : b->bdy_mask;
+   n = (long)b->shape[0] * b->shape[1] * b->shape[2];
+   for (i = 0; i < n; i++) out[i] = m[i] ? 1.0 : 0.0;
+   return 0;
+}
+
+static int level_index(const pgb_solver *s, int box)
+{
+   const pgb_hlevel *lv = &s->h.lev[s->h.boxes[box].level];
+   int i;
+   for (i = 0; i < lv->nbox; i++)
+      if (lv->box[i] == box) return i;
+   return -1;
+}
+
+int pgb_plan_dump(const pgb_solver *s, int which, int L, int *rows, int cap)
+{
+   const pgb_plan *p;
+   int i;
+   if (L < 1 || L > s->h.nlev) return -fail(3, "level %d out of range", L);
+   switch (which) {
+   case 0: p = &s->h.sync[L][0]; break;
+   case 1: p = &s->h.sync[L][1]; break;
+   case 2: p = &s->h.sync_coarsest[L]; break;
+   case 3: p = &s->h.inject[L]; break;
+   case 4: p = &s->h.inject_init[L]; break;
+   case 5: p = &s->h.interp[L]; break;
+   default: return -fail(3, "unknown plan %d", which);
+   }
+   for (i = 0; i < p->nops && i < cap; i++) {
+      int *r = rows + 24 * i, sb, db;
+      memset(r, 0, sizeof(int) * 24);
+      if (which <= 2) {
+         const pgb_copy_op *o = (const pgb_copy_op *)p->h_ops + i;
+         sb = o->src_box; db = o->dst_box;
+         r[4] = o->i1; r[5] = o->j1; r[6] = o->k1; r[7] = o->i2; r[8] = o->j2; r[9] = o->k2;
+         r[10] = o->ni; r[11] = o->nj; r[12] = o->nk;
+      } else if (which <= 4) {
+         const pgb_restrict_op *o = (const pgb_restrict_op *)p->h_ops + i;
+         int f;
+         sb = o->src_box; db = o->dst_box;
+         r[4] = o->i1; r[5] = o->j1; r[6] = o->k1; r[7] = o->i2; r[8] = o->j2; r[9] = o->k2;
+         r[10] = o->ni; r[11] = o->nj; r[12] = o->nk; r[13] = o->irho;
+         for (f = 0; f < PGB_NF; f++) r[14 + f] = o->op[f];
+      } else {
+         const pgb_interp_op *o = (const pgb_interp_op *)p->h_ops + i;
+         sb = o->src_box; db = o->dst_box;
+         r[4] = o->i1i; r[5] = o->j1i; r[6] = o->k1i; r[7] = o->nii; r[8] = o->nji; r[9] = o->nki;
+         r[10] = o->i2b; r[11] = o->j2b; r[12] = o->k2b; r[13] = o->i2; r[14] = o->j2; r[15] = o->k2;
+         r[16] = o->nib; r[17] = o->njb; r[18] = o->nkb; r[19] = o->irho; r[20] = o->ord;
+      }
+      r[0] = s->h.boxes[sb].level;
+      r[1] = level_index(s, sb);
+      r[2] = s->h.boxes[db].level;
+      r[3] = level_index(s, db);
+   }
+   return p->nops;
+}

@@ -1,0 +1,215 @@
+"""Python front end of libpamr_gb300 (ctypes over the C ABI in
+include/pamr_gb300.h).
+
+This is the interface the tests and the benchmark call; a C application
+calls the same entry points directly. There is no CPU fallback: if the
+library or a GPU is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .workloads import Case
+
+_lib = None
+
+PLAN_SYNC0, PLAN_SYNC1, PLAN_SYNC_COARSEST, PLAN_INJECT, PLAN_INJECT_INIT, PLAN_INTERP = range(6)
+
+
+class PgbError(RuntimeError):
+    pass
+
+
+class MGParams(C.Structure):
+    _fields_ = [("pre_swp", C.c_int), ("pst_swp", C.c_int), ("max_iter", C.c_int),
+                ("min_iter", C.c_int), ("max_citer", C.c_int), ("tol", C.c_double),
+                ("crtol", C.c_double), ("w0_r", C.c_double), ("w0_i", C.c_double),
+                ("min_cwidth", C.c_int), ("restr_u", C.c_int), ("restr_res", C.c_int),
+                ("restr_src", C.c_int), ("interp_order", C.c_int), ("interp_buffer", C.c_int)]
+
+
+def lib(build: bool = True):
+    """Loads libpamr_gb300.so (building it first if needed)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise PgbError(f"{path} missing: run pamr_amrd_gb300.build.build()")
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int)
+        vp = C.c_void_p
+        L.pgb_last_error.restype = C.c_char_p
+        L.pgb_create.argtypes = [C.c_int, C.c_int, ip, dp, C.c_int, ip, dp, C.POINTER(MGParams),
+                                 C.c_int, C.POINTER(vp)]
+        L.pgb_destroy.argtypes = [vp]
+        L.pgb_grid_shape.argtypes = [vp, C.c_int, ip]
+        L.pgb_set_grid.argtypes = [vp, C.c_int, dp, dp]
+        L.pgb_get_grid.argtypes = [vp, C.c_int, dp]
+        L.pgb_set_grid_device.argtypes = [vp, C.c_int, vp, vp]
+        L.pgb_get_grid_device.argtypes = [vp, C.c_int, vp]
+        L.pgb_solve.argtypes = [vp, ip, dp, dp, C.c_int]
+        L.pgb_prepare.argtypes = [vp]
+        L.pgb_vcycle.argtypes = [vp, dp]
+        L.pgb_stream.argtypes = [vp]
+        L.pgb_stream.restype = vp
+        L.pgb_stats.argtypes = [vp, ip, C.POINTER(C.c_long), dp]
+        L.pgb_trace_enable.argtypes = [vp, C.c_int]
+        L.pgb_trace_fetch.argtypes = [vp, ip, ip, ip, ip, dp, C.c_int, ip]
+        L.pgb_num_levels.argtypes = [vp]
+        L.pgb_level_nbox.argtypes = [vp, C.c_int]
+        L.pgb_box_info.argtypes = [vp, C.c_int, C.c_int, ip, dp, ip, ip]
+        L.pgb_box_cmask.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
+        L.pgb_plan_dump.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int]
+        L.pgb_default_params.argtypes = [C.POINTER(MGParams)]
+        for name in ("pgb_dmcopy3d", "pgb_dmhwr3d", "pgb_dmfwr3d"):
+            getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp]
+        L.pgb_dminterp3d.argtypes = [vp, vp] + [C.c_int] * 22 + [vp]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise PgbError(f"libpamr_gb300 error {rc}: {lib().pgb_last_error().decode()}")
+
+
+def params_from(case: Case) -> MGParams:
+    p = case.params
+    m = MGParams()
+    lib().pgb_default_params(C.byref(m))
+    m.pre_swp, m.pst_swp, m.max_iter, m.min_iter = p.pre_swp, p.pst_swp, p.max_iter, p.min_iter
+    m.max_citer, m.tol, m.crtol, m.w0_r, m.w0_i = p.max_citer, p.tol, p.crtol, p.w0_r, p.w0_i
+    m.min_cwidth, m.restr_u, m.restr_res, m.restr_src = (p.min_cwidth, p.restr_u, p.restr_res,
+                                                         p.restr_src)
+    m.interp_order, m.interp_buffer = p.interp_order, 2
+    return m
+
+
+class Solver:
+    """One AMR hierarchy on the GPU (or, with host_only, just its plans)."""
+
+    def __init__(self, case: Case, host_only: bool = False):
+        L = lib()
+        self.case = case
+        n = len(case.grids)
+        lev = (C.c_int * n)(*[g.level for g in case.grids])
+        bb = np.zeros((n, 6))
+        for i, g in enumerate(case.grids):
+            bb[i, :len(g.bbox)] = g.bbox
+        self._bb = np.ascontiguousarray(bb)
+        shape = (C.c_int * 3)(*case.base_shape)
+        bbox = (C.c_double * 6)(*(list(case.base_bbox) + [0.0] * (6 - len(case.base_bbox))))
+        self._params = params_from(case)
+        h = C.c_void_p()
+        _check(L.pgb_create(case.dim, case.pde, shape, bbox, n, lev, _dp(self._bb),
+                            C.byref(self._params), 1 if host_only else 0, C.byref(h)))
+        self.h = h
+        self.host_only = host_only
+
+    def close(self):
+        if self.h:
+            lib().pgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------- data --
+    def set_inputs(self, u=None, src=None):
+        u = u if u is not None else self.case.u0
+        src = src if src is not None else self.case.src
+        for i, (a, s) in enumerate(zip(u, src)):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            s = np.ascontiguousarray(s, dtype=np.float64)
+            _check(lib().pgb_set_grid(self.h, i, _dp(a), _dp(s)))
+
+    def get_u(self):
+        out = []
+        for g in self.case.grids:
+            a = np.empty(g.size)
+            out.append(a)
+        for i, a in enumerate(out):
+            _check(lib().pgb_get_grid(self.h, i, _dp(a)))
+        return out
+
+    # ------------------------------------------------------------ solve --
+    def solve(self):
+        cap = max(1, self.case.params.max_iter)
+        res = np.zeros(cap)
+        it = C.c_int()
+        rf = C.c_double()
+        _check(lib().pgb_solve(self.h, C.byref(it), C.byref(rf), _dp(res), cap))
+        return {"iters": it.value, "res": res[:it.value].copy(), "res_final": rf.value}
+
+    def prepare(self):
+        _check(lib().pgb_prepare(self.h))
+
+    def vcycle(self) -> float:
+        r = C.c_double()
+        _check(lib().pgb_vcycle(self.h, C.byref(r)))
+        return r.value
+
+    def stats(self):
+        v, c, ms = C.c_int(), C.c_long(), C.c_double()
+        lib().pgb_stats(self.h, C.byref(v), C.byref(c), C.byref(ms))
+        return {"vcycles": v.value, "coarsest_iters": c.value, "device_ms": ms.value}
+
+    def stream(self) -> int:
+        return lib().pgb_stream(self.h)
+
+    def trace_enable(self, cap: int):
+        _check(lib().pgb_trace_enable(self.h, cap))
+        self._trace_cap = cap
+
+    def trace_fetch(self):
+        cap = self._trace_cap
+        k, l, b, r = (np.zeros(cap, dtype=np.int32) for _ in range(4))
+        nrm = np.zeros(cap)
+        n = C.c_int()
+        ip = C.POINTER(C.c_int)
+        _check(lib().pgb_trace_fetch(self.h, k.ctypes.data_as(ip), l.ctypes.data_as(ip),
+                                     b.ctypes.data_as(ip), r.ctypes.data_as(ip), _dp(nrm), cap,
+                                     C.byref(n)))
+        m = n.value
+        return {"kind": k[:m], "L": l[:m], "idx": b[:m], "repeat": r[:m], "norm": nrm[:m]}
+
+    # ---------------------------------------------------------- queries --
+    def num_levels(self) -> int:
+        return lib().pgb_num_levels(self.h)
+
+    def level_nbox(self, L: int) -> int:
+        return lib().pgb_level_nbox(self.h, L)
+
+    def box_info(self, L: int, idx: int):
+        shape = (C.c_int * 3)()
+        bb = (C.c_double * 6)()
+        co, ag = C.c_int(), C.c_int()
+        _check(lib().pgb_box_info(self.h, L, idx, shape, bb, C.byref(co), C.byref(ag)))
+        return {"shape": tuple(shape), "bbox": tuple(bb), "coarsest": co.value,
+                "amr_grid": ag.value}
+
+    def cmask(self, L: int, idx: int, kind: str) -> np.ndarray:
+        sh = self.box_info(L, idx)["shape"]
+        out = np.zeros(sh[0] * sh[1] * sh[2])
+        _check(lib().pgb_box_cmask(self.h, L, idx, 1 if kind == "child" else 0, _dp(out)))
+        return out
+
+    def plan(self, which: int, L: int) -> np.ndarray:
+        n = lib().pgb_plan_dump(self.h, which, L, None, 0)
+        if n < 0:
+            _check(-n)
+        rows = np.zeros((max(n, 1), 24), dtype=np.int32)
+        lib().pgb_plan_dump(self.h, which, L, rows.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return rows[:n]
