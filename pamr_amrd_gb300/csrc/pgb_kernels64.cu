@@ -531,8 +531,9 @@ extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, v
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 512) gx = 512;
       if (n <= 0 || gx <= 0) continue;
-      k_copy<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
-         boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt], field);
+      for (int c0 = 0; c0 < n; c0 += 65535)
+         k_copy<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
+            boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt] + c0, field);
    }
    return check("copy");
 }
@@ -544,8 +545,9 @@ extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *st
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 1024) gx = 1024;
       if (n <= 0 || gx <= 0) continue;
-      k_restrict<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
-         boxes, (const pgb_restrict_op *)p->d_ops + p->batch_start[bt]);
+      for (int c0 = 0; c0 < n; c0 += 65535)
+         k_restrict<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
+            boxes, (const pgb_restrict_op *)p->d_ops + p->batch_start[bt] + c0);
    }
    return check("restrict");
 }
@@ -558,8 +560,9 @@ extern "C" int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field,
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 2048) gx = 2048;
       if (n <= 0 || gx <= 0) continue;
-      k_interp<<<dim3(gx, n), 256, 0, (cudaStream_t)stream>>>(
-         boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt], field, dim);
+      for (int c0 = 0; c0 < n; c0 += 65535)
+         k_interp<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
+            boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt] + c0, field, dim);
    }
    return check("interp");
 }
@@ -568,22 +571,58 @@ extern "C" int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field,
 /* The coarsest-grid loop of vcycle (amrd/mg.c:172-190) in one CTA: relax
  * the coarsest boxes (both colours), take the call_rr_app norm, sync them
  * (PAMR_sync(L,0,MGH,1) over coarsest grids only), until res <= ctol or
- * max_citer. When the state after an iteration equals the state two
- * iterations earlier, every later iteration repeats that cycle exactly, so
- * the loop jumps to max_citer and lands on the same state and norm the
- * reference reaches by iterating. */
+ * max_citer iterations.
+ *
+ * Below the rounding floor the iteration often revisits earlier states. A
+ * 64-bit hash of the state after each iteration is kept for the last
+ * PGB_CHASH iterations; when the current hash equals the one p iterations
+ * back, the state is saved and p more iterations are run: if the state then
+ * equals the saved one exactly, the iteration is periodic with period p, all
+ * norms of the cycle exceed ctol (the loop kept going), and the reference
+ * would repeat the cycle until max_citer. The loop then skips a multiple of
+ * p iterations and runs the remainder, ending on the same state and norm
+ * the reference reaches by iterating. */
 #define CT 1024
+#define PGB_CHASH 256
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)
+{
+   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+   return z ^ (z >> 31);
+}
+
+__device__ unsigned long long block_xor(unsigned long long v, unsigned long long *sm)
+{
+   int t = threadIdx.x;
+   for (int o = 16; o > 0; o >>= 1) v ^= __shfl_down_sync(0xffffffffu, v, o);
+   if ((t & 31) == 0) sm[t >> 5] = v;
+   __syncthreads();
+   if (t < 32) {
+      v = (t < (blockDim.x >> 5)) ? sm[t] : 0ull;
+      for (int o = 16; o > 0; o >>= 1) v ^= __shfl_down_sync(0xffffffffu, v, o);
+      if (t == 0) sm[0] = v;
+   }
+   __syncthreads();
+   v = sm[0];
+   __syncthreads();
+   return v;
+}
+
 __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                  const pgb_copy_op *sync_ops, int nsync,
                                                  pgb_coarsest_args a, pgb_trace *trace)
 {
    __shared__ double sm[32];
-   __shared__ int s_changed;
+   __shared__ unsigned long long smh[32];
+   __shared__ unsigned long long hist[PGB_CHASH];
+   __shared__ int s_flag;
    const int t = threadIdx.x, dim = lv.dim;
    double ctol = *a.res_dn * a.crtol;
-   double res = ctol + 1, res_prev = 0;
-   int iter = a.start_iter, history = 0;
-   double *prev1 = a.snap, *prev2 = a.snap + a.snap_points;
+   double res = ctol + 1;
+   int iter = a.start_iter, nhist = 0;
+   int verify_at = -1, period = 0;
+   double *saved = a.snap;
    while (iter < a.max_citer && res > ctol) {
       double lres = 0;
       int first = 1;
@@ -644,55 +683,71 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
       }
       if (t == 0) sm[0] = lres;
       __syncthreads();
-      res_prev = res;
       res = sm[0];
       __syncthreads();
       iter++;
-      /* cycle detection on the coarsest boxes' u */
-      if (t == 0) s_changed = 0;
+      if (!(iter < a.max_citer && res > ctol)) break;
+
+      /* hash of the state; at a verification point compare with the save */
+      unsigned long long h = 0;
+      if (t == 0) s_flag = 0;
       __syncthreads();
-      long off = 0;
-      for (int b = 0; b < lv.nbox; b++) {
-         const pgb_dbox bx = boxes[lv.box[b]];
-         if (!(bx.flags & PGB_BOX_COARSEST)) continue;
-         long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-         for (long q = t; q < n; q += CT) {
-            double v = bx.f[PGB_F_U][q];
-            if (history >= 2 && prev2[off + q] != v) s_changed = 1;
-            prev2[off + q] = prev1[off + q];
-            prev1[off + q] = v;
+      {
+         long off = 0;
+         for (int b = 0; b < lv.nbox; b++) {
+            const pgb_dbox bx = boxes[lv.box[b]];
+            if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+            long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+            for (long q = t; q < n; q += CT) {
+               double v = bx.f[PGB_F_U][q];
+               unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+               h ^= mix64(bits ^ mix64((unsigned long long)(off + q) + 0x9E3779B97F4A7C15ull));
+               if (iter == verify_at && saved[off + q] != v) s_flag = 1;
+            }
+            off += n;
          }
-         off += n;
       }
-      __syncthreads();
-      if (history < 2) history++;
-      if (history >= 2 && !s_changed && res > ctol && iter < a.max_citer) {
-         /* state == state two iterations ago: period 1 or 2 */
-         int rem = a.max_citer - iter;
-         if (rem & 1) {
-            /* final state is the previous one: restore it (prev2 now holds it) */
-            long off2 = 0;
+      h = block_xor(h, smh);
+      if (iter == verify_at) {
+         if (!s_flag) {
+            /* exact period: skip whole periods, run the remainder */
+            int rem = a.max_citer - iter;
+            int skip = rem - rem % period;
+            if (trace && t == 0 && skip > 0) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rr = {2, lv.level, period, skip, 0.0};
+                  trace->rec[n] = rr;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+            iter += skip;
+            nhist = 0;
+         }
+         verify_at = -1;
+      } else if (verify_at < 0) {
+         int found = 0;
+         int lim = nhist < PGB_CHASH ? nhist : PGB_CHASH;
+         for (int p = 1; p <= lim && !found; p++)
+            if (hist[(nhist - p) % PGB_CHASH] == h) found = p;
+         if (found) {
+            long off = 0;
             for (int b = 0; b < lv.nbox; b++) {
                const pgb_dbox bx = boxes[lv.box[b]];
                if (!(bx.flags & PGB_BOX_COARSEST)) continue;
                long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-               for (long q = t; q < n; q += CT) bx.f[PGB_F_U][q] = prev2[off2 + q];
-               off2 += n;
+               for (long q = t; q < n; q += CT) saved[off + q] = bx.f[PGB_F_U][q];
+               off += n;
             }
-            res = res_prev;
+            period = found;
+            verify_at = iter + found;
          }
-         if (trace && t == 0) {
-            int n = trace->n;
-            if (n < trace->cap) {
-               pgb_trace_rec rr = {2, lv.level, -1, rem, 0.0};
-               trace->rec[n] = rr;
-               trace->n = n + 1;
-            } else
-               trace->overflow = 1;
-         }
-         iter = a.max_citer;
-         __syncthreads();
       }
+      __syncthreads();
+      if (t == 0) hist[nhist % PGB_CHASH] = h;
+      nhist++;
+      __syncthreads();
    }
    if (t == 0) {
       *a.res_out = res;
