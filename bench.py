@@ -1,0 +1,304 @@
+#!/usr/bin/env python
+"""Benchmark: AMRD FAS multigrid solves per second on GB300.
+
+Workload (one step = one elliptic solve): the 3-D conformal-factor equation
+lap(psi) + 2 pi rho psi^5 = 0 on [-10,10]^3, 129^3 base grid plus two nested
+2:1 levels of 65^3 boxes (9 MG levels down to 9^3), V(2,2) FAS cycles until
+the finest residual is 1e-10 of its initial value -- the hierarchy the
+reference's solve_elliptics (amrd/mg.c:20) runs on. Seeded synthetic rho
+(pamr_amrd_gb300.workloads.conformal3d); rank r uses seed r.
+
+Each step resets psi to its initial guess (device copy) and solves; L2 is
+flushed between steps (512 MiB write, outside the timed events). `value` is
+solves/s with inputs resident in HBM; `e2e` is the same through the C ABI
+with host buffers (host->device copy of psi and rho, solve, device->host
+copy of psi). `cpu_baseline` times the oracle port (a C restatement of the
+reference's path) on this machine's host cores.
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+N>1 runs N independent replicas (one per GPU, launched by torch.distributed.run).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s to 1e-10 rel. residual: plain FP64 vs chosen form; smoother HBM GB/s"
+UNIT = "solves/s"
+WORKLOAD = ("conformal3d_129_65: lap(psi)+2*pi*rho*psi^5=0 on [-10,10]^3, 129^3 base + 2 nested "
+            "65^3 levels (9 MG levels), V(2,2) FAS to 1e-10 relative residual")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _case(seed: int):
+    from pamr_amrd_gb300 import workloads as W
+    return W.conformal3d(129, 65, seed=seed)
+
+
+# ------------------------------------------------------------ CPU side --
+def _port_solve(seed: int) -> float:
+    from oracle import portrun
+    t = time.perf_counter()
+    portrun.solve(_case(seed))
+    return time.perf_counter() - t
+
+
+def cpu_round(nproc: int, seed0: int = 0) -> dict:
+    """one bounded sample: nproc oracle-port solves of the workload, one per
+    host core, in parallel (spawned processes)"""
+    from oracle import portrun
+    portrun.build()
+    ctx = mp.get_context("spawn")
+    t = time.perf_counter()
+    with ctx.Pool(nproc) as pool:
+        per = pool.map(_port_solve, [seed0 + i for i in range(nproc)])
+    wall = time.perf_counter() - t
+    return {"solves": nproc, "wall_s": wall, "per_solve_s": statistics.median(per)}
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# -------------------------------------------------------------- clocks --
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            v = float(json.load(f)["hbm_gbs"])
+        return v, "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    """dram bytes per relax sweep of the 129^3 level from the committed ncu
+    summary (profiles/relax_traffic.txt: 'bytes_per_sweep=<n>'), if any"""
+    p = os.path.join(ROOT, "profiles", "relax_traffic.txt")
+    try:
+        for line in open(p):
+            if line.startswith("bytes_per_sweep="):
+                return float(line.split("=", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------- main --
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nproc = min(host_cores(), 32)
+        for _ in range(min(args.warmup, 1)):
+            cpu_round(nproc, seed0=100)
+        rounds = [cpu_round(nproc, seed0=i * nproc) for i in range(args.steps)]
+        solves = sum(r["solves"] for r in rounds)
+        wall = sum(r["wall_s"] for r in rounds)
+        v = solves / wall
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded rho)", "config": {"workload": WORKLOAD,
+                                                             "sample": f"{nproc} solves per step"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": nproc, "kind": "port",
+                                 "sample": f"{nproc} concurrent oracle-port solves per step, "
+                                           f"{args.steps} steps"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import numpy as np
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    from pamr_amrd_gb300 import solver as S
+    case = _case(rank)
+    s = S.Solver(case)
+    # device-resident inputs
+    d_u0 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.u0]
+    d_src = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.src]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(s.stream())
+
+    def step():
+        s.set_inputs_device([t.data_ptr() for t in d_u0], [t.data_ptr() for t in d_src])
+        return s.solve()
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        r = step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(torch.cuda.current_device())
+    launches0 = S.launch_count()
+    times, iters, finals = [], [], []
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        iters.append(r["iters"])
+        finals.append(r["res_final"])
+    torch.cuda.synchronize()
+    wall_ms = 1e3 * (time.perf_counter() - t_wall)
+    launches = S.launch_count() - launches0
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    total_ms = sum(times)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+    converged = all(f <= case.params.tol for f in finals)
+
+    # e2e through the C ABI with host buffers
+    pin_u = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in case.u0]
+    pin_s = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in case.src]
+    out_u = [torch.empty(g.size, dtype=torch.float64).pin_memory() for g in case.grids]
+    h2d = sum(2 * 8 * g.size for g in case.grids)
+    d2h = sum(8 * g.size for g in case.grids)
+    e2e_ms = []
+    for k in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(len(case.grids)):
+            S._check(S.lib().pgb_set_grid(s.h, i, S.C.cast(pin_u[i].data_ptr(), S.C.POINTER(S.C.c_double)),
+                                          S.C.cast(pin_s[i].data_ptr(), S.C.POINTER(S.C.c_double))))
+        s.solve()
+        for i in range(len(case.grids)):
+            S._check(S.lib().pgb_get_grid(s.h, i, S.C.cast(out_u[i].data_ptr(), S.C.POINTER(S.C.c_double))))
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_total = sum(e2e_ms)
+    if dist:
+        t = torch.tensor([e2e_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * args.steps / (e2e_total / 1e3)
+
+    # roofline of the dominant kernel: the relax sweep on the 129^3 level
+    big = max(range(1, s.num_levels() + 1),
+              key=lambda L: max(s.box_info(L, b)["shape"][0] for b in range(s.level_nbox(L))))
+    flush.fill_(1.0)
+    ms_sweep, bytes_sweep = s.time_relax(big, reps=20)
+    achieved = bytes_sweep / (ms_sweep / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": ncu_traffic(), "peak_source": peak_kind,
+            "kernel": "k_relax (red+black sweep, FP64, 129^3 level)",
+            "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nproc = min(host_cores(), 32)
+        cr = cpu_round(nproc)
+        cpu = {"value": cr["solves"] / cr["wall_s"], "unit": UNIT, "cores": nproc, "kind": "port",
+               "sample": f"{nproc} concurrent oracle-port solves of the workload "
+                         f"(median {cr['per_solve_s']:.1f} s per solve)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded rho, rank r uses seed r)",
+                "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write)",
+                           "points": case.total_points(), "mg_levels": s.num_levels(),
+                           "parallelism": f"replicas x{world}"},
+                "chosen_form": "fp64", "fp64_solves_per_s": value,
+                "vcycles_per_solve": statistics.mean(iters), "converged": converged,
+                "wall_ms_timed": wall_ms,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches,
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line))
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -104,6 +104,17 @@ void *pgb_stream(pgb_solver *s);
  * (as the reference counts them), and device time in ms. */
 int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms);
 
+/* Kernel launches this library has issued in the process (all solvers). */
+long long pgb_launch_count(void);
+
+/* Times `reps` red-black relax sweeps (both colours, app_MG_relax on every
+ * box, examples/nbs/num.f:172-246) of MG level `level` on the solver's
+ * current data with CUDA events on its stream; returns the mean time per
+ * sweep and the algorithmic bytes of one sweep (u read and written, rhs and
+ * source read: 32 bytes per interior point). Modifies u on that level. */
+int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
+                   double *bytes_per_sweep);
+
 /* Norm trace: when enabled, every norm a hook would return is recorded
  * (kind 0 relax, 1 residual, 2 = skipped coarsest iterations; level; box;
  * repeat; norm) -- the device counterpart of MG_trace (amrd/mg.c:138-195). */

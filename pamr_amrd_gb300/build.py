@@ -72,8 +72,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose and out:
             print(out)
     if force or _stale(LIB, objs):
-        cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-L" + os.path.join(cuda, "lib64"),
-                                                           "-lcudart"]
+        libdir = os.path.join(cuda, "lib64")
+        cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-L" + libdir, "-lcudart",
+                                                           "-Xlinker", "-rpath",
+                                                           "-Xlinker", libdir]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: " + r.stdout + r.stderr)

@@ -64,6 +64,7 @@ typedef struct {
 } pgb_coarsest_args;
 
 const char *pgb_dev_error(void);
+unsigned long long pgb_dev_launches(void);
 int pgb_dev_sync(void *stream);
 
 /* FP64 path: every expression follows the reference hooks / Fortran order

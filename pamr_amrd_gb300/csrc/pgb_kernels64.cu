@@ -18,8 +18,12 @@
 #include "pgb_dev.h"
 
 static __thread char g_err[256];
+static unsigned long long g_launches = 0;
 
 extern "C" const char *pgb_dev_error(void) { return g_err; }
+extern "C" unsigned long long pgb_dev_launches(void) { return g_launches; }
+
+#define LAUNCHED(n) (g_launches += (unsigned long long)(n))
 
 static int check(const char *what)
 {
@@ -198,7 +202,9 @@ extern "C" int pgb_k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_sc
    cudaStream_t st = (cudaStream_t)stream;
    if (lv.nrtiles == 0) return 0;
    k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 0, sc, norm_out, trace);
+   LAUNCHED(1);
    k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 1, sc, norm_out, trace);
+   LAUNCHED(1);
    return check("relax");
 }
 
@@ -239,6 +245,7 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
    if (lv.ntiles == 0) return 0;
    k_residual<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
                                                                              norm_out, trace);
+   LAUNCHED(1);
    return check("residual");
 }
 
@@ -298,6 +305,7 @@ extern "C" int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask, void 
 {
    if (!lv.ntiles) return 0;
    k_clear<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, mask);
+   LAUNCHED(1);
    return check("clear");
 }
 extern "C" int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
@@ -305,18 +313,21 @@ extern "C" int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, doub
 {
    if (!lv.ntiles) return 0;
    k_lop_rhs<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   LAUNCHED(1);
    return check("lop_rhs");
 }
 extern "C" int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream)
 {
    if (!lv.ntiles) return 0;
    k_cgc_coarse<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, w0_i);
+   LAUNCHED(1);
    return check("cgc_coarse");
 }
 extern "C" int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
 {
    if (!lv.ntiles) return 0;
    k_add_res<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   LAUNCHED(1);
    return check("add_res");
 }
 
@@ -531,9 +542,11 @@ extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, v
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 512) gx = 512;
       if (n <= 0 || gx <= 0) continue;
-      for (int c0 = 0; c0 < n; c0 += 65535)
+      for (int c0 = 0; c0 < n; c0 += 65535) {
          k_copy<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
             boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt] + c0, field);
+         LAUNCHED(1);
+      }
    }
    return check("copy");
 }
@@ -545,9 +558,11 @@ extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *st
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 1024) gx = 1024;
       if (n <= 0 || gx <= 0) continue;
-      for (int c0 = 0; c0 < n; c0 += 65535)
+      for (int c0 = 0; c0 < n; c0 += 65535) {
          k_restrict<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
             boxes, (const pgb_restrict_op *)p->d_ops + p->batch_start[bt] + c0);
+         LAUNCHED(1);
+      }
    }
    return check("restrict");
 }
@@ -560,9 +575,11 @@ extern "C" int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field,
       int gx = (p->batch_maxpts[bt] + 255) / 256;
       if (gx > 2048) gx = 2048;
       if (n <= 0 || gx <= 0) continue;
-      for (int c0 = 0; c0 < n; c0 += 65535)
+      for (int c0 = 0; c0 < n; c0 += 65535) {
          k_interp<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
             boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt] + c0, field, dim);
+         LAUNCHED(1);
+      }
    }
    return check("interp");
 }
@@ -760,6 +777,7 @@ extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, con
 {
    k_coarsest<<<1, CT, 0, (cudaStream_t)stream>>>(boxes, lv, pde, (const pgb_copy_op *)sync->d_ops,
                                                   sync->nops, a, trace);
+   LAUNCHED(1);
    return check("coarsest");
 }
 
@@ -775,6 +793,7 @@ extern "C" int pgb_k_fill(double *p, long n, double v, void *stream)
    if (g > 4096) g = 4096;
    if (g < 1) g = 1;
    k_fill<<<(int)g, 256, 0, (cudaStream_t)stream>>>(p, n, v);
+   LAUNCHED(1);
    return check("fill");
 }
 
@@ -823,6 +842,7 @@ static int mutil_launch(const double *u1, double *u2, mu_args a, int kind, void 
    if (g > 4096) g = 4096;
    if (g < 1) return 0;
    k_mutil<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a, kind);
+   LAUNCHED(1);
    return check("m_util_r8");
 }
 
@@ -918,5 +938,6 @@ extern "C" int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, in
    if (g > 4096) g = 4096;
    if (g < 1) return 0;
    k_minterp<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a);
+   LAUNCHED(1);
    return check("dminterp3d");
 }

@@ -548,6 +548,28 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
    return 0;
 }
 
+long long pgb_launch_count(void) { return (long long)pgb_dev_launches(); }
+
+int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double *bytes_per_sweep)
+{
+   int r, b;
+   float ms = 0;
+   double pts = 0;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (L < 1 || L > s->h.nlev || reps < 1) return fail(3, "bad level or reps");
+   for (b = 0; b < s->h.lev[L].nbox; b++) pts += s->h.boxes[s->h.lev[L].box[b]].count;
+   if (relax(s, L, N_RELAX_UP)) return 11;   /* warm-up */
+   CU(cudaEventRecord(s->ev0, s->stream));
+   for (r = 0; r < reps; r++)
+      if (relax(s, L, N_RELAX_UP)) return 11;
+   CU(cudaEventRecord(s->ev1, s->stream));
+   CU(cudaEventSynchronize(s->ev1));
+   CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+   if (ms_per_sweep) *ms_per_sweep = ms / reps;
+   if (bytes_per_sweep) *bytes_per_sweep = 32.0 * pts;
+   return 0;
+}
+
 /* ---------------------------------------------------------------- trace -- */
 int pgb_trace_enable(pgb_solver *s, int capacity)
 {

@@ -66,11 +66,17 @@ def lib(build: bool = True):
         L.pgb_box_cmask.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
         L.pgb_plan_dump.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int]
         L.pgb_default_params.argtypes = [C.POINTER(MGParams)]
+        L.pgb_launch_count.restype = C.c_longlong
+        L.pgb_time_relax.argtypes = [vp, C.c_int, C.c_int, dp, dp]
         for name in ("pgb_dmcopy3d", "pgb_dmhwr3d", "pgb_dmfwr3d"):
             getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp]
         L.pgb_dminterp3d.argtypes = [vp, vp] + [C.c_int] * 22 + [vp]
         _lib = L
     return _lib
+
+
+def launch_count() -> int:
+    return int(lib().pgb_launch_count())
 
 
 def _dp(a: np.ndarray):
@@ -165,6 +171,15 @@ class Solver:
         v, c, ms = C.c_int(), C.c_long(), C.c_double()
         lib().pgb_stats(self.h, C.byref(v), C.byref(c), C.byref(ms))
         return {"vcycles": v.value, "coarsest_iters": c.value, "device_ms": ms.value}
+
+    def time_relax(self, L: int, reps: int = 20):
+        ms, by = C.c_double(), C.c_double()
+        _check(lib().pgb_time_relax(self.h, L, reps, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
+
+    def set_inputs_device(self, u_ptrs, src_ptrs):
+        for i, (a, b) in enumerate(zip(u_ptrs, src_ptrs)):
+            _check(lib().pgb_set_grid_device(self.h, i, a, b))
 
     def stream(self) -> int:
         return lib().pgb_stream(self.h)

@@ -1,0 +1,81 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference's
+own multigrid solve (oracle/_ref/ref_mg, compiled from the reference's C
+sources by oracle/build_ref.sh) on small seeded cases.
+
+Each fixture stores the case (grids, parameters, initial u and source) and
+what the reference produced: V-cycle count, every relax/residual/L_op hook
+call with its norm, the MG hierarchy, the cmask arrays, the final u on every
+grid and the m_util_r8 call log of the whole solve.
+
+usage: python tests/golden/make_golden.py   (needs oracle/_ref/ref_mg)
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refrun  # noqa: E402
+from pamr_amrd_gb300 import workloads as W  # noqa: E402
+
+
+def cases():
+    return [
+        W.poisson2d(17, seed=0),
+        W.poisson2d(33, seed=1),
+        W.conformal3d(17, 9, seed=0),
+        W.conformal3d(17, 9, seed=3, params=W.MGParams(min_cwidth=5, pre_swp=3, pst_swp=1)),
+        W.poisson2d_uneven(seed=1, n=33, levels=3, min_boxes=2, max_boxes=4, min_side=5,
+                           max_side=17),
+        W.poisson2d_uneven(seed=2, n=65, levels=4, min_boxes=3, max_boxes=8, min_side=9,
+                           max_side=33),
+    ]
+
+
+def save(case, ref, path):
+    p = case.params
+    grids = np.array([[g.level] + list(g.shape) + list(g.bbox) + [0.0] * (6 - len(g.bbox))
+                      for g in case.grids])
+    masks_meta = np.array([[0 if m["kind"] == "bdy" else 1, m["L"], m["idx"]]
+                           for m in ref["masks"]], dtype=np.int32)
+    masks = np.concatenate([m["mask"] for m in ref["masks"]]).astype(np.uint8)
+    mgh = np.array([[r["L"], r["idx"], *r["shape"], r["coarsest"], *r["bbox"]]
+                    for r in ref["mgh"]])
+    h = ref["hooks"]
+    np.savez_compressed(
+        path,
+        name=np.array(case.name), pde=case.pde, dim=case.dim,
+        base_shape=np.array(case.base_shape), base_bbox=np.array(case.base_bbox),
+        grids=grids,
+        u0=np.concatenate(case.u0), src=np.concatenate(case.src),
+        params=np.array([p.pre_swp, p.pst_swp, p.max_iter, p.min_iter, p.max_citer,
+                         p.min_cwidth, p.restr_u, p.restr_res, p.restr_src, p.interp_order]),
+        fparams=np.array([p.tol, p.crtol, p.w0_r, p.w0_i]),
+        iters=ref["iters"],
+        hook_kind=h["kind"].astype(np.int8), hook_L=h["L"].astype(np.int8),
+        hook_idx=h["idx"].astype(np.int16), hook_norm=h["norm"],
+        mgh=mgh, masks_meta=masks_meta, masks=masks,
+        u=np.concatenate(ref["u"]),
+        gfn=np.array([ref["gfn"][k] for k in ("u", "res", "lop", "rhs", "cmask", "src")]),
+        ops=ref["ops"].astype(np.int16) if len(ref["ops"]) else np.zeros((0, 34), np.int16),
+    )
+
+
+def main():
+    if not refrun.available():
+        raise SystemExit("oracle/_ref/ref_mg missing: run oracle/build_ref.sh first")
+    for c in cases():
+        ref = refrun.run_reference(c, log_ops=True)
+        path = os.path.join(HERE, f"{c.name}__{len(c.grids)}g_{c.params.min_cwidth}cw.npz")
+        save(c, ref, path)
+        print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
+              f"{len(ref['ops'])} m_util_r8 calls, {os.path.getsize(path) // 1024} KiB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,108 @@
+"""Loads the golden fixtures of tests/golden/ (made by make_golden.py from
+the compiled reference) back into workload Cases plus the reference's
+recorded outputs."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+
+from pamr_amrd_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def files():
+    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(path: str):
+    z = np.load(path)
+    grids = []
+    for row in z["grids"]:
+        lev, s0, s1, s2 = (int(v) for v in row[:4])
+        dim = int(z["dim"])
+        bbox = tuple(float(v) for v in row[4:4 + 2 * dim])
+        grids.append(W.Grid(lev, bbox, (s0, s1, s2)))
+    ip = [int(v) for v in z["params"]]
+    fp = [float(v) for v in z["fparams"]]
+    params = W.MGParams(pre_swp=ip[0], pst_swp=ip[1], max_iter=ip[2], min_iter=ip[3],
+                        max_citer=ip[4], min_cwidth=ip[5], restr_u=ip[6], restr_res=ip[7],
+                        restr_src=ip[8], interp_order=ip[9], tol=fp[0], crtol=fp[1],
+                        w0_r=fp[2], w0_i=fp[3])
+    sizes = [g.size for g in grids]
+    offs = np.cumsum([0] + sizes)
+    split = lambda a: [a[offs[i]:offs[i + 1]].copy() for i in range(len(grids))]  # noqa: E731
+    case = W.Case(str(z["name"]), int(z["pde"]), int(z["dim"]),
+                  tuple(int(v) for v in z["base_shape"]),
+                  tuple(float(v) for v in z["base_bbox"]), grids,
+                  split(z["u0"]), split(z["src"]), params)
+    masks = []
+    off = 0
+    for kind, L, idx in z["masks_meta"]:
+        mg = [r for r in z["mgh"] if int(r[0]) == L and int(r[1]) == idx][0]
+        n = int(mg[2] * mg[3] * mg[4])
+        masks.append({"kind": ("bdy", "child")[int(kind)], "L": int(L), "idx": int(idx),
+                      "mask": z["masks"][off:off + n].astype(np.float64)})
+        off += n
+    ref = {
+        "iters": int(z["iters"]),
+        "hooks": {"kind": z["hook_kind"].astype(np.int32), "L": z["hook_L"].astype(np.int32),
+                  "idx": z["hook_idx"].astype(np.int32), "norm": z["hook_norm"]},
+        "mgh": [{"L": int(r[0]), "idx": int(r[1]), "shape": (int(r[2]), int(r[3]), int(r[4])),
+                 "coarsest": int(r[5]), "bbox": tuple(float(v) for v in r[6:12])}
+                for r in z["mgh"]],
+        "masks": masks,
+        "u": split(z["u"]),
+        "gfn": dict(zip(("u", "res", "lop", "rhs", "cmask", "src"), (int(v) for v in z["gfn"]))),
+        "ops": z["ops"].astype(np.int64),
+    }
+    return case, ref
+
+
+def finest_residuals(hooks: dict, lf: int) -> np.ndarray:
+    """per-V-cycle finest residual (amrd/mg.c:194) from a hook log"""
+    k, L, n = hooks["kind"], hooks["L"], hooks["norm"]
+    pos = np.nonzero((k == 1) & (L == lf))[0]
+    groups, last = [], None
+    for p in pos:
+        if last is not None and p == last + 1:
+            groups[-1].append(p)
+        else:
+            groups.append([p])
+        last = p
+    out = np.array([max(float(n[i]) for i in g) for g in groups])
+    return out[1::2] if lf > 1 else out
+
+
+def expand_trace(tr: dict):
+    """expands a device trace's periodic-skip markers (kind 2: period in
+    'idx', skipped iterations in 'repeat') into the norms the reference
+    logs for the skipped coarsest-grid iterations"""
+    out = {"kind": [], "L": [], "idx": [], "norm": []}
+    for i in range(len(tr["kind"])):
+        if tr["kind"][i] != 2:
+            for key in ("kind", "L", "idx", "norm"):
+                out[key].append(tr[key][i])
+            continue
+        period, skip, lev = int(tr["idx"][i]), int(tr["repeat"][i]), int(tr["L"][i])
+        # the last `period` iterations' records on this level (one per coarsest box)
+        recs = []
+        j = len(out["kind"]) - 1
+        while j >= 0 and out["kind"][j] == 0 and out["L"][j] == lev:
+            recs.append(j)
+            j -= 1
+        recs = recs[::-1]
+        nbox = 1
+        if recs:
+            first_box = out["idx"][recs[-1]]
+            nbox = 1
+            while nbox < len(recs) and out["idx"][recs[-1 - nbox]] != first_box:
+                nbox += 1
+        cyc = recs[-period * nbox:]
+        for s in range(skip):
+            for jj in cyc[(s % period) * nbox:(s % period + 1) * nbox]:
+                for key in ("kind", "L", "idx", "norm"):
+                    out[key].append(out[key][jj])
+    return {k: np.array(v) for k, v in out.items()}

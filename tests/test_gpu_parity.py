@@ -1,0 +1,86 @@
+"""GPU parity of the plain FP64 path, through the C ABI.
+
+Against the compiled reference (golden fixtures): identical V-cycle count,
+bit-identical solution on every grid, the full sequence of relax/residual
+norms within 1e-12 relative (only the norm summation order differs).
+Against the oracle port at sizes beyond the fixtures: bit-identical
+solution and per-cycle residuals within 1e-12 relative."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+from oracle import portrun
+from pamr_amrd_gb300 import workloads as W
+from pamr_amrd_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+NORM_RTOL = 1e-12   # norms: different summation order only
+
+
+def _solve(case, trace=0):
+    s = Solver(case)
+    s.set_inputs()
+    if trace:
+        s.trace_enable(trace)
+    r = s.solve()
+    r["u"] = s.get_u()
+    r["stats"] = s.stats()
+    if trace:
+        r["trace"] = s.trace_fetch()
+    s.close()
+    return r
+
+
+@pytest.mark.parametrize("path", G.files(), ids=lambda p: p.split("/")[-1][:-4])
+def test_fp64_matches_reference_fixture(path):
+    case, ref = G.load(path)
+    r = _solve(case, trace=200000)
+    assert r["iters"] == ref["iters"]
+    for a, b in zip(r["u"], ref["u"]):
+        assert np.array_equal(a, b)
+    h = ref["hooks"]
+    keep = h["kind"] != 2                      # L_op returns no norm
+    tr = G.expand_trace(r["trace"])
+    assert len(tr["kind"]) == int(keep.sum())
+    assert np.array_equal(tr["kind"], h["kind"][keep])
+    assert np.array_equal(tr["L"], h["L"][keep])
+    assert np.array_equal(tr["idx"], h["idx"][keep])
+    rel = np.abs(tr["norm"] - h["norm"][keep]) / np.maximum(np.abs(h["norm"][keep]), 1e-300)
+    assert float(np.max(rel)) < NORM_RTOL
+    lf = max(m["L"] for m in ref["mgh"])
+    want = G.finest_residuals(h, lf)
+    assert np.max(np.abs(r["res"] - want) / want) < NORM_RTOL
+
+
+LARGER = [
+    lambda: W.poisson2d(129, seed=0),
+    lambda: W.poisson2d(257, seed=2),
+    lambda: W.conformal3d(33, 17, seed=1),
+    lambda: W.conformal3d(65, 33, seed=2),
+    lambda: W.poisson2d_uneven(seed=0, n=129, levels=5, min_boxes=8, max_boxes=24),
+]
+
+
+@pytest.mark.parametrize("make", LARGER, ids=["p2d129", "p2d257", "c3d33", "c3d65", "uneven129"])
+def test_fp64_matches_oracle_port(make):
+    case = make()
+    r = _solve(case)
+    p = portrun.solve(case)
+    assert r["iters"] == p["iters"]
+    for a, b in zip(r["u"], p["u"]):
+        assert np.array_equal(a, b)
+    assert np.max(np.abs(r["res"] - p["res"]) / p["res"]) < NORM_RTOL
+    assert r["res_final"] <= case.params.tol
+
+
+def test_full_size_conformal_converges_and_matches_port():
+    """the benchmark hierarchy (129^3 base + two 65^3 levels): converged to
+    1e-10 relative residual, solution identical to the oracle port"""
+    case = W.conformal3d(129, 65, seed=0)
+    r = _solve(case)
+    assert r["res_final"] <= case.params.tol
+    p = portrun.solve(case)
+    assert r["iters"] == p["iters"]
+    for a, b in zip(r["u"], p["u"]):
+        assert np.array_equal(a, b)

@@ -1,0 +1,55 @@
+"""Host-side bookkeeping of libpamr_gb300 (no GPU needed): the MG hierarchy,
+the cmask arrays and every transfer op must equal the reference's, bit for
+bit (golden fixtures from the compiled reference)."""
+import numpy as np
+import pytest
+
+import bookkeeping as BK
+import golden_cases as G
+from oracle import refrun
+from pamr_amrd_gb300 import workloads as W
+from pamr_amrd_gb300.solver import PgbError, Solver
+
+
+def _check_case(case, ref):
+    s = Solver(case, host_only=True)
+    nb = sum(s.level_nbox(L) for L in range(1, s.num_levels() + 1))
+    assert nb == len(ref["mgh"])
+    for r in ref["mgh"]:
+        b = s.box_info(r["L"], r["idx"])
+        assert b["shape"] == r["shape"]
+        assert b["coarsest"] == r["coarsest"]
+        assert all(b["bbox"][k] == r["bbox"][k] for k in range(2 * case.dim))
+    for m in ref["masks"]:
+        assert np.array_equal(s.cmask(m["L"], m["idx"], m["kind"]), m["mask"])
+    exp = BK.expected_calls(s, BK.reference_gfns(ref), ref["iters"], case.params.pre_swp,
+                            case.params.pst_swp)
+    assert exp.shape == ref["ops"].shape
+    assert np.array_equal(exp, ref["ops"])
+
+
+@pytest.mark.parametrize("path", G.files(), ids=lambda p: p.split("/")[-1][:-4])
+def test_plans_match_reference_fixture(path):
+    case, ref = G.load(path)
+    _check_case(case, ref)
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("seed", [7, 8, 9])
+def test_plans_match_reference_live(seed):
+    case = W.poisson2d_uneven(seed=seed, n=65, levels=4, min_boxes=4, max_boxes=12, min_side=9,
+                              max_side=41)
+    ref = refrun.run_reference(case, log_ops=True)
+    ref["ops"] = ref["ops"].astype(np.int64)
+    _check_case(case, ref)
+
+
+def test_invalid_inputs_are_errors_not_exits():
+    case = W.poisson2d(17)
+    case.params.interp_order = 3
+    with pytest.raises(PgbError):
+        Solver(case, host_only=True)
+    case = W.poisson2d(17)
+    case.grids[0] = W.Grid(0, case.grids[0].bbox, case.grids[0].shape)
+    with pytest.raises(PgbError):
+        Solver(case, host_only=True)
