@@ -3,7 +3,7 @@
 
 Workload (one step = one elliptic solve): the 3-D conformal-factor equation
 lap(psi) + 2 pi rho psi^5 = 0 on [-10,10]^3, 129^3 base grid plus two nested
-2:1 levels of 65^3 boxes (9 MG levels down to 9^3), V(2,2) FAS cycles until
+2:1 levels of 65^3 boxes (7 MG levels down to 9^3), V(2,2) FAS cycles until
 the finest residual is 1e-10 of its initial value -- the hierarchy the
 reference's solve_elliptics (amrd/mg.c:20) runs on. Seeded synthetic rho
 (pamr_amrd_gb300.workloads.conformal3d); rank r uses seed r.
@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 METRIC = "solves/s to 1e-10 rel. residual: plain FP64 vs chosen form; smoother HBM GB/s"
 UNIT = "solves/s"
 WORKLOAD = ("conformal3d_129_65: lap(psi)+2*pi*rho*psi^5=0 on [-10,10]^3, 129^3 base + 2 nested "
-            "65^3 levels (9 MG levels), V(2,2) FAS to 1e-10 relative residual")
+            "65^3 levels (7 MG levels, coarsest 9^3), V(2,2) FAS to 1e-10 relative residual")
 FALLBACK_HBM_GBS = 6800.0
 
 
