@@ -136,6 +136,31 @@ int pgb_box_cmask(const pgb_solver *s, int level, int idx, int kind, double *out
  * and fills up to cap rows of 24 ints */
 int pgb_plan_dump(const pgb_solver *s, int which, int level, int *rows, int cap);
 
+/* ------------------------------------------- residual without allocation -- */
+/* No counterpart in the reference. The residual of ONE grid,
+ * res = L[u] - rhs at interior points where cmask is ON (cmask = NULL: all
+ * interior points), and its RMS norm written to *norm (device double), as
+ * app_MG_residual computes them -- for callers that cannot allocate device
+ * memory when they need it: applications that own and budget all device
+ * memory themselves (as PAMR owns all grid memory), and callers that must
+ * not let a cudaMalloc/cudaFree synchronize the device between their
+ * asynchronous launches. All pointers except shape3/dx3 (host) are device
+ * pointers supplied by the caller; the reduction uses a fixed 64 KiB array
+ * in device global memory that every GPU loading the library holds until
+ * process exit. Limit: the grid must fit in PGB_NOALLOC_MAX_TILES tiles of
+ * 32 x 8 x 8 points (ceil(Nx/32)*ceil(Ny/8)*ceil(Nz/8), Nz term 1 in 2-D;
+ * e.g. 161^3 or 1000 x 1000). The first call on a device looks up the
+ * array's device address; make it before any stream capture. Calls share
+ * the array: calls whose kernels overlap on the GPU race and must not be
+ * issued that way. Returns 0, or 1 bad arguments, 2 grid above the limit,
+ * 3 no device / address lookup failed, 4 launch failed (a message is
+ * printed on stderr). Allocates nothing. */
+#define PGB_NOALLOC_MAX_TILES 4095
+int pgb_residual_norm_noalloc(int pde, int dim, const int *shape3, const double *dx3,
+                              const double *u, const double *rhs, const double *src,
+                              const unsigned char *cmask, double *res, double *norm,
+                              void *stream);
+
 /* --------------------------------- device m_util_r8 (include/m_util_r8.h) -- */
 /* Same arguments as the Fortran routines (src/m_util_r8.f), by value, on
  * device arrays; stream may be NULL. No excision (do_ex = 0). */
