@@ -49,7 +49,17 @@ typedef struct {
    int restr_u, restr_res, restr_src;  /* restriction of u, u_res, source */
    int interp_order;            /* 2 (mg_interp2) or 4 */
    int interp_buffer;           /* PAMR interp_buffer, default 2 (src/pamr.c:157) */
+   int precision;               /* PGB_FP64 (bit-exact with the reference) or PGB_MIXED */
 } pgb_mg_params;
+
+/* precision of pgb_mg_params:
+ *   PGB_FP64  every operation in FP64, results bit-identical to the reference
+ *   PGB_MIXED FP32 smoothing (Gauss-Seidel on the correction of each smoothing
+ *             block) and FP32 prolongation inside FP64 defect correction;
+ *             residuals, restriction, FAS right-hand sides, coarsest-grid
+ *             solve and solution updates stay FP64 */
+#define PGB_FP64 0
+#define PGB_MIXED 1
 
 typedef struct pgb_solver pgb_solver;
 

@@ -58,6 +58,7 @@ typedef struct {
    const double *res_dn;       /* res[L] from the down sweep (ctol base) */
    double *res_out;            /* res[L] after the loop */
    int *iters_out;             /* iterations executed (for statistics) */
+   int stagnation_exit;        /* mixed form: also stop when the norm stops decreasing */
    double *snap;               /* 2 x (points of the coarsest boxes) doubles */
    long snap_points;
    const long *snap_off;       /* per level box: offset of its points in a snapshot */
@@ -83,6 +84,15 @@ int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim, v
 int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                    pgb_coarsest_args a, pgb_trace *trace, void *stream);
 int pgb_k_fill(double *p, long n, double v, void *stream);
+
+/* mixed-precision path (pgb_kernels32.cu) */
+const char *pgb_dev_error32(void);
+unsigned long long pgb_dev_launches32(void);
+int pgb_k_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, void *stream);
+int pgb_k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
+int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
+int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
+int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream);
 
 #ifdef __cplusplus
 }

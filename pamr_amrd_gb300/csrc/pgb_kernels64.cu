@@ -700,10 +700,12 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
       }
       if (t == 0) sm[0] = lres;
       __syncthreads();
+      double res_before = res;
       res = sm[0];
       __syncthreads();
       iter++;
       if (!(iter < a.max_citer && res > ctol)) break;
+      if (a.stagnation_exit && iter > a.start_iter + 1 && res >= res_before) break;
 
       /* hash of the state; at a verification point compare with the save */
       unsigned long long h = 0;

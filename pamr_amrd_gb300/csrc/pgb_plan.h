@@ -44,6 +44,7 @@ typedef struct {
    int min_cwidth;
    int restr_u, restr_res, restr_src;
    int interp_order, interp_buffer;
+   int precision;
 } pgb_hparams;
 
 typedef struct pgb_hier {

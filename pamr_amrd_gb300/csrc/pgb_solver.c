@@ -84,6 +84,7 @@ void pgb_default_params(pgb_mg_params *p)
    p->restr_src = PGB_HW_RESTR;
    p->interp_order = 2;
    p->interp_buffer = 2;
+   p->precision = PGB_FP64;
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -135,7 +136,7 @@ static void free_plan_dev(pgb_plan *p)
 static int setup_device(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
-   size_t off = 0, *fo;
+   size_t off = 0, *fo, *w32o = 0;
    int i, f, L, d, maxt = 1, maxbox = 1;
    long snap_pts = 0;
    CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -155,6 +156,17 @@ static int setup_device(pgb_solver *s)
       fo[i * (PGB_NF + 2) + PGB_NF + 1] = off;
       off = align256(off + n);
    }
+   if (h->prm.precision == PGB_MIXED) {
+      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * 3);
+      for (i = 0; i < h->nbox; i++) {
+         const pgb_hbox *b = &h->boxes[i];
+         size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+         for (f = 0; f < 3; f++) {
+            w32o[i * 3 + f] = off;
+            off = align256(off + 4 * n);
+         }
+      }
+   }
    s->arena_bytes = off;
    CU(cudaMalloc((void **)&s->arena, off));
    CU(cudaMemset(s->arena, 0, off));
@@ -165,6 +177,8 @@ static int setup_device(pgb_solver *s)
       size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       double dx2[3] = {1, 1, 1};
       for (f = 0; f < PGB_NF; f++) db->f[f] = (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
+      if (w32o)
+         for (f = 0; f < 3; f++) db->w32[f] = (float *)(s->arena + w32o[i * 3 + f]);
       db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
       db->cmask_bdy = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF + 1]);
       CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
@@ -186,6 +200,7 @@ static int setup_device(pgb_solver *s)
       else db->j0 = -2 / dx2[0] - 2 / dx2[1];
    }
    free(fo);
+   free(w32o);
    CU(cudaMalloc((void **)&s->dbox, sizeof(pgb_dbox) * (size_t)h->nbox));
    CU(cudaMemcpy(s->dbox, s->hbox, sizeof(pgb_dbox) * (size_t)h->nbox, cudaMemcpyHostToDevice));
 
@@ -298,6 +313,9 @@ int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox,
    hp.restr_src = params->restr_src;
    hp.interp_order = params->interp_order;
    hp.interp_buffer = params->interp_buffer;
+   hp.precision = params->precision;
+   if (hp.precision != PGB_FP64 && hp.precision != PGB_MIXED)
+      return fail(1, "precision must be PGB_FP64 or PGB_MIXED");
    rc = pgb_hier_build(&s->h, dim, pde, base_shape, base_bbox, ngrids, grid_level, grid_bbox, &hp);
    if (rc) {
       fail(2, "hierarchy: %s", s->h.err);
@@ -448,11 +466,42 @@ int pgb_prepare(pgb_solver *s)
    return 0;
 }
 
+#define KC32(call)                                                                  \
+   do {                                                                             \
+      if (call) return fail(11, "%s", pgb_dev_error32());                            \
+   } while (0)
+
+/* one smoothing block (nsweep sweeps + syncs, amrd/mg.c:135-141 / 161-167).
+ * FP64: Newton-GS sweeps. Mixed: FP64 defect, FP32 sweeps on the correction
+ * (synced between boxes like u), FP64 update, then the sync of u. The
+ * coarsest level always smooths in FP64. */
+static int smooth(pgb_solver *s, int L, int nsweep, int slot)
+{
+   pgb_hier *h = &s->h;
+   int it;
+   if (h->prm.precision == PGB_FP64 || L == 1) {
+      for (it = 0; it < nsweep; it++) {
+         if (relax(s, L, slot)) return 11;
+         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
+      }
+      return 0;
+   }
+   if (nsweep <= 0) return 0;
+   KC32(pgb_k_defect(s->dbox, s->lv[L], h->pde, s->stream));
+   for (it = 0; it < nsweep; it++) {
+      KC32(pgb_k_relax32(s->dbox, s->lv[L], s->stream));
+      if (h->sync[L][it ? 1 : 0].nops) KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], s->stream));
+   }
+   KC32(pgb_k_update(s->dbox, s->lv[L], s->stream));
+   if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
+   return 0;
+}
+
 static int vcycle_launch(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
-   int L, Lf = h->nlev, it;
+   int L, Lf = h->nlev;
    /* clear_MG_vars(Lf) amrd/mg.c:91 */
    KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
@@ -466,21 +515,19 @@ static int vcycle_launch(pgb_solver *s)
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
-      for (it = 0; it < p->pre_swp; it++) {
-         if (relax(s, L, N_RELAX_DN)) return 11;
-         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
-      }
+      if (smooth(s, L, p->pre_swp, N_RELAX_DN)) return 11;
    }
    for (L = 1; L <= Lf; L++) {
       if (L > 1) {
          KC(pgb_k_cgc_coarse(s->dbox, s->lv[L - 1], p->w0_i, s->stream));
-         if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
+         if (p->precision == PGB_MIXED) {
+            if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, s->stream));
+         } else {
+            if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
+         }
          KC(pgb_k_add_res(s->dbox, s->lv[L], s->stream));
       }
-      for (it = 0; it < p->pst_swp; it++) {
-         if (relax(s, L, N_RELAX_UP)) return 11;
-         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
-      }
+      if (smooth(s, L, p->pst_swp, N_RELAX_UP)) return 11;
       if (lvl_coarsest(s, L)) {
          pgb_coarsest_args a;
          a.start_iter = p->pst_swp;
@@ -489,6 +536,7 @@ static int vcycle_launch(pgb_solver *s)
          a.res_dn = norm_slot(s, L, p->pre_swp > 0 ? N_RELAX_DN : N_COARSE);
          a.res_out = norm_slot(s, L, N_COARSE);
          a.iters_out = s->d_citers;
+         a.stagnation_exit = p->precision == PGB_MIXED;
          a.snap = s->d_snap;
          a.snap_points = s->snap_points;
          a.snap_off = s->d_snap_off[L];
@@ -548,7 +596,7 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
    return 0;
 }
 
-long long pgb_launch_count(void) { return (long long)pgb_dev_launches(); }
+long long pgb_launch_count(void) { return (long long)(pgb_dev_launches() + pgb_dev_launches32()); }
 
 int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double *bytes_per_sweep)
 {

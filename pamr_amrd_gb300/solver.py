@@ -29,7 +29,8 @@ class MGParams(C.Structure):
                 ("min_iter", C.c_int), ("max_citer", C.c_int), ("tol", C.c_double),
                 ("crtol", C.c_double), ("w0_r", C.c_double), ("w0_i", C.c_double),
                 ("min_cwidth", C.c_int), ("restr_u", C.c_int), ("restr_res", C.c_int),
-                ("restr_src", C.c_int), ("interp_order", C.c_int), ("interp_buffer", C.c_int)]
+                ("restr_src", C.c_int), ("interp_order", C.c_int), ("interp_buffer", C.c_int),
+                ("precision", C.c_int)]
 
 
 def lib(build: bool = True):
@@ -97,6 +98,7 @@ def params_from(case: Case) -> MGParams:
     m.min_cwidth, m.restr_u, m.restr_res, m.restr_src = (p.min_cwidth, p.restr_u, p.restr_res,
                                                          p.restr_src)
     m.interp_order, m.interp_buffer = p.interp_order, 2
+    m.precision = getattr(p, "precision", 0)
     return m
 
 

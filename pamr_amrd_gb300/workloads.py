@@ -98,6 +98,7 @@ class MGParams:
     restr_u: int = HW_RESTR   # mg_hw_restr = [u rho], mg_fw_restr = [u_res]
     restr_res: int = FW_RESTR
     restr_src: int = HW_RESTR
+    precision: int = 0        # 0: FP64 (bit-exact), 1: FP32 smoothing in FP64 defect correction
 
 
 @dataclasses.dataclass

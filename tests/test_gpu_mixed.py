@@ -1,0 +1,53 @@
+"""The mixed-precision form (FP32 smoothing and prolongation inside FP64
+defect correction) against the FP64 oracle: converged to the same relative
+residual, within 1e-9 of the FP64 oracle solution (max abs error relative
+to max |u|), on the golden cases and on larger hierarchies."""
+import copy
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+from oracle import portrun
+from pamr_amrd_gb300 import workloads as W
+from pamr_amrd_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+ERR_RTOL = 1e-9
+
+
+def _mixed(case):
+    c = copy.deepcopy(case)
+    c.params.precision = 1
+    s = Solver(c)
+    s.set_inputs()
+    r = s.solve()
+    r["u"] = s.get_u()
+    s.close()
+    return r
+
+
+def _check(case, ref_u, ref_iters):
+    r = _mixed(case)
+    assert r["res_final"] <= case.params.tol
+    umax = max(float(np.max(np.abs(a))) for a in ref_u)
+    err = max(float(np.max(np.abs(a - b))) for a, b in zip(r["u"], ref_u))
+    assert err <= ERR_RTOL * umax, err / umax
+    assert abs(r["iters"] - ref_iters) <= 2
+
+
+@pytest.mark.parametrize("path", G.files(), ids=lambda p: p.split("/")[-1][:-4])
+def test_mixed_matches_reference_fixture(path):
+    case, ref = G.load(path)
+    _check(case, ref["u"], ref["iters"])
+
+
+@pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=3),
+                                  lambda: W.poisson2d_uneven(seed=4, n=129, levels=5, min_boxes=8,
+                                                             max_boxes=16)],
+                         ids=["c3d65", "uneven129"])
+def test_mixed_matches_oracle_port(make):
+    case = make()
+    p = portrun.solve(case)
+    _check(case, p["u"], p["iters"])
