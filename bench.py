@@ -21,6 +21,7 @@ N>1 runs N independent replicas (one per GPU, launched by torch.distributed.run)
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import multiprocessing as mp
 import os
@@ -185,72 +186,90 @@ def main():
 
     from pamr_amrd_gb300 import solver as S
     case = _case(rank)
-    s = S.Solver(case)
+    case64 = copy.deepcopy(case)
+    case64.params.precision = 0
+    casemx = copy.deepcopy(case)
+    casemx.params.precision = 1
+    s64 = S.Solver(case64)
+    smx = S.Solver(casemx)
     # device-resident inputs
     d_u0 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.u0]
     d_src = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.src]
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.ExternalStream(s.stream())
 
-    def step():
+    def step(s):
         s.set_inputs_device([t.data_ptr() for t in d_u0], [t.data_ptr() for t in d_src])
         return s.solve()
 
-    for _ in range(args.warmup):
-        flush.fill_(1.0)
-        r = step()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clocks = Clocks(torch.cuda.current_device())
-    launches0 = S.launch_count()
-    times, iters, finals = [], [], []
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(1.0)
+    def timed(s, clocks=None):
+        stream = torch.cuda.ExternalStream(s.stream())
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            step(s)
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        r = step()
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-        iters.append(r["iters"])
-        finals.append(r["res_final"])
-    torch.cuda.synchronize()
-    wall_ms = 1e3 * (time.perf_counter() - t_wall)
-    launches = S.launch_count() - launches0
-    clk = clocks.stop()
-    if dist:
-        dist.barrier()
-    total_ms = sum(times)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1e3)
-    converged = all(f <= case.params.tol for f in finals)
+        if dist:
+            dist.barrier()
+        clk = Clocks(torch.cuda.current_device()) if clocks else None
+        l0 = S.launch_count()
+        times, iters, finals = [], [], []
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = step(s)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            iters.append(r["iters"])
+            finals.append(r["res_final"])
+        torch.cuda.synchronize()
+        wall = 1e3 * (time.perf_counter() - t_wall)
+        launches = S.launch_count() - l0
+        ck = clk.stop() if clk else None
+        if dist:
+            dist.barrier()
+        total = sum(times)
+        if dist:
+            t = torch.tensor([total], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return {"total_ms": total, "iters": iters, "finals": finals, "wall_ms": wall,
+                "launches": launches, "clocks": ck}
 
-    # e2e through the C ABI with host buffers
+    tm64 = timed(s64)
+    tmx = timed(smx, clocks=True)
+    value = world * args.steps / (tmx["total_ms"] / 1e3)
+    fp64_value = world * args.steps / (tm64["total_ms"] / 1e3)
+    ms_per_step = tmx["total_ms"] / args.steps
+    converged = all(f <= case.params.tol for f in tmx["finals"] + tm64["finals"])
+    u64, umx = s64.get_u(), smx.get_u()
+    umax = max(float(np.max(np.abs(a))) for a in u64)
+    emax = max(float(np.max(np.abs(a - b))) for a, b in zip(umx, u64))
+    el2 = float(np.sqrt(sum(float(np.sum((a - b) ** 2)) for a, b in zip(umx, u64)) /
+                        sum(a.size for a in u64)))
+
+    # e2e through the C ABI with host buffers (chosen form)
     pin_u = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in case.u0]
     pin_s = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in case.src]
     out_u = [torch.empty(g.size, dtype=torch.float64).pin_memory() for g in case.grids]
     h2d = sum(2 * 8 * g.size for g in case.grids)
     d2h = sum(8 * g.size for g in case.grids)
+    dp = S.C.POINTER(S.C.c_double)
     e2e_ms = []
     for k in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(len(case.grids)):
-            S._check(S.lib().pgb_set_grid(s.h, i, S.C.cast(pin_u[i].data_ptr(), S.C.POINTER(S.C.c_double)),
-                                          S.C.cast(pin_s[i].data_ptr(), S.C.POINTER(S.C.c_double))))
-        s.solve()
+            S._check(S.lib().pgb_set_grid(smx.h, i, S.C.cast(pin_u[i].data_ptr(), dp),
+                                          S.C.cast(pin_s[i].data_ptr(), dp)))
+        smx.solve()
         for i in range(len(case.grids)):
-            S._check(S.lib().pgb_get_grid(s.h, i, S.C.cast(out_u[i].data_ptr(), S.C.POINTER(S.C.c_double))))
+            S._check(S.lib().pgb_get_grid(smx.h, i, S.C.cast(out_u[i].data_ptr(), dp)))
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_total = sum(e2e_ms)
     if dist:
@@ -259,17 +278,22 @@ def main():
         e2e_total = float(t.item())
     e2e_value = world * args.steps / (e2e_total / 1e3)
 
-    # roofline of the dominant kernel: the relax sweep on the 129^3 level
-    big = max(range(1, s.num_levels() + 1),
-              key=lambda L: max(s.box_info(L, b)["shape"][0] for b in range(s.level_nbox(L))))
+    # roofline of the dominant smoother: FP32 sweep of the mixed form on the
+    # 129^3 level (and the FP64 sweep of the plain form beside it)
+    big = max(range(1, smx.num_levels() + 1),
+              key=lambda L: max(smx.box_info(L, b)["shape"][0] for b in range(smx.level_nbox(L))))
     flush.fill_(1.0)
-    ms_sweep, bytes_sweep = s.time_relax(big, reps=20)
+    ms_sweep, bytes_sweep = smx.time_relax(big, reps=20)
+    ms64_sweep, bytes64_sweep = s64.time_relax(big, reps=10)
     achieved = bytes_sweep / (ms_sweep / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": ncu_traffic(), "peak_source": peak_kind,
-            "kernel": "k_relax (red+black sweep, FP64, 129^3 level)",
-            "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep}
+            "kernel": "k_relax32 (FP32 red+black sweep on the correction, 129^3 level)",
+            "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep,
+            "fp64_sweep": {"kernel": "k_relax (FP64 Newton-GS sweep, 129^3 level)",
+                           "ms_per_sweep": ms64_sweep,
+                           "achieved_gbs": bytes64_sweep / (ms64_sweep / 1e3) / 1e9}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -282,20 +306,25 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic (seeded rho, rank r uses seed r)",
                 "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write)",
-                           "points": case.total_points(), "mg_levels": s.num_levels(),
+                           "points": case.total_points(), "mg_levels": smx.num_levels(),
                            "parallelism": f"replicas x{world}"},
-                "chosen_form": "fp64", "fp64_solves_per_s": value,
-                "vcycles_per_solve": statistics.mean(iters), "converged": converged,
-                "wall_ms_timed": wall_ms,
+                "chosen_form": "mixed: FP32 smoothing and prolongation in FP64 defect correction",
+                "fp64_solves_per_s": fp64_value, "speedup_vs_fp64": value / fp64_value,
+                "vcycles_per_solve": statistics.mean(tmx["iters"]),
+                "fp64_vcycles_per_solve": statistics.mean(tm64["iters"]),
+                "converged": converged,
+                "error_vs_fp64_oracle": {"max_abs": emax, "max_rel": emax / umax, "l2": el2},
+                "wall_ms_timed": tmx["wall_ms"],
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": launches,
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+                "gpu_launches": tmx["launches"],
+                "roofline": roof, "cpu_baseline": cpu, "clocks": tmx["clocks"]}
         print(json.dumps(line))
-    s.close()
+    s64.close()
+    smx.close()
     if dist:
         dist.destroy_process_group()
 

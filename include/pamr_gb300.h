@@ -120,8 +120,10 @@ long long pgb_launch_count(void);
 /* Times `reps` red-black relax sweeps (both colours, app_MG_relax on every
  * box, examples/nbs/num.f:172-246) of MG level `level` on the solver's
  * current data with CUDA events on its stream; returns the mean time per
- * sweep and the algorithmic bytes of one sweep (u read and written, rhs and
- * source read: 32 bytes per interior point). Modifies u on that level. */
+ * sweep and the algorithmic bytes of one sweep: FP64 path 32 bytes per
+ * interior point (u read and written, rhs and source read), mixed form 16
+ * (FP32 correction read and written, defect and Jacobian term read).
+ * Modifies u (FP64) or the correction (mixed) on that level. */
 int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
                    double *bytes_per_sweep);
 

@@ -12,8 +12,9 @@
 extern "C" {
 #endif
 
-/* tile extents: one CTA of 32 x 8 threads; each thread walks PGB_TZ planes
- * in 3-D. Relax tiles are twice as wide in x because a thread updates one
+/* tile extents: one CTA of 32 x 8 threads; each thread walks up to PGB_TZ
+ * planes in 3-D (fewer on small levels, so they still spread over the
+ * SMs). Relax tiles are twice as wide in x because a thread updates one
  * point of the active colour out of every two. */
 #define PGB_TX 32
 #define PGB_TY 8
@@ -27,6 +28,7 @@ typedef struct {
    const int *rtile_start;
    const int *box;             /* level box -> global box index */
    int ntiles, nrtiles, nbox;
+   int tz, rtz;                /* planes per tile (3-D) of the two tile lists */
    int dim;
    int level;
 } pgb_dlevel;
@@ -59,6 +61,9 @@ typedef struct {
    double *res_out;            /* res[L] after the loop */
    int *iters_out;             /* iterations executed (for statistics) */
    int stagnation_exit;        /* mixed form: also stop when the norm stops decreasing */
+   int ctol_from_first;        /* mixed form: ctol = crtol x the loop's first norm */
+   long smem_points;           /* points of the level's coarsest boxes (on-chip kernel) */
+   int ncoarse;                /* number of coarsest boxes on the level */
    double *snap;               /* 2 x (points of the coarsest boxes) doubles */
    long snap_points;
    const long *snap_off;       /* per level box: offset of its points in a snapshot */
@@ -93,6 +98,9 @@ int pgb_k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
 int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream);
+int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
+                        double *norm_out, pgb_trace *trace, void *stream);
+int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ typedef struct {
    double *f[PGB_NF];
    const uint8_t *cmask_child;   /* set_cmask_child, amrd/mg.c:362-426 */
    const uint8_t *cmask_bdy;     /* set_cmask_bdy, amrd/mg.c:432-488 */
-   float *w32[3];                /* mixed precision work arrays (correction, rhs, src) */
+   float *w32[4];                /* mixed form: correction, defect, Jacobian term, coarse correction */
    int n[3];                     /* Nx, Ny, Nz (Nz = 1 in 2-D) */
    int flags;
    int level;

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(NT) k_defect(const pgb_dbox *boxes, pgb_dlevel
    if (i >= b.n[0] || j >= b.n[1]) return;
    const double *u = b.f[PGB_F_U], *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   int kz = dim == 3 ? PGB_TZ : 1;
+   int kz = dim == 3 ? lv.tz : 1;
    for (int kk = 0; kk < kz; kk++) {
       int k = tl.k0 + kk;
       if (k >= b.n[2]) break;
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
    const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
    const float j0 = (float)b.j0;
    int j = tl.j0 + threadIdx.y;
-   int kz = dim == 3 ? PGB_TZ : 1;
+   int kz = dim == 3 ? lv.rtz : 1;
    for (int kk = 0; kk < kz; kk++) {
       int k = tl.k0 + kk;
       int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
    const pgb_dbox b = boxes[tl.box];
    int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   int kz = lv.dim == 3 ? PGB_TZ : 1;
+   int kz = lv.dim == 3 ? lv.tz : 1;
    for (int kk = 0; kk < kz; kk++) {
       int k = tl.k0 + kk;
       if (k >= b.n[2]) break;
@@ -361,4 +361,140 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
       }
    }
    return 0;
+}
+
+/* ---------------------------------------- FP64 passes of the mixed form -- */
+/* The mixed form needs FP64 accuracy in its residuals, not the reference's
+ * bit pattern: these variants multiply by 1/dx^2 and let the compiler fuse
+ * multiply-adds, which roughly halves their FP64 instruction count. */
+__device__ __forceinline__ double lapf(const pgb_dbox &b, const double *u, long p, int dim)
+{
+   long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   double c = u[p];
+   double t = (u[p + 1] - 2 * c + u[p - 1]) * b.idx2[0] + (u[p + sy] - 2 * c + u[p - sy]) * b.idx2[1];
+   if (dim == 3) t += (u[p + sz] - 2 * c + u[p - sz]) * b.idx2[2];
+   return t;
+}
+
+__device__ __forceinline__ double opf(int pde, double t, double u, double s)
+{
+   if (pde == 1) {
+      double p2 = u * u;
+      return t + TWO_PI * s * (p2 * p2 * u);
+   }
+   if (pde == 2) return t - s * u;
+   return t - s;
+}
+
+__device__ double block_sum32(double v, double *sm)
+{
+   int t = threadIdx.x + threadIdx.y * blockDim.x;
+   int nt = blockDim.x * blockDim.y;
+   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   if ((t & 31) == 0) sm[t >> 5] = v;
+   __syncthreads();
+   if (t < 32) {
+      v = (t < (nt >> 5)) ? sm[t] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   }
+   __syncthreads();
+   return v;
+}
+
+__global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                      pgb_scratch sc, double *norm_out,
+                                                      pgb_trace *trace)
+{
+   __shared__ double sm[32];
+   __shared__ int last;
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const double *u = b.f[PGB_F_U], *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
+   double *res = b.f[PGB_F_RES];
+   double acc = 0;
+   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   int kz = dim == 3 ? lv.tz : 1;
+   for (int kk = 0; kk < kz; kk++) {
+      int k = tl.k0 + kk;
+      if (!interior32(b, i, j, k, dim)) continue;
+      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      double r = opf(pde, lapf(b, u, p, dim), u[p], src[p]) - rhs[p];
+      res[p] = r;
+      acc += r * r;
+   }
+   acc = block_sum32(acc, sm);
+   if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0 && threadIdx.y == 0)
+      last = (atomicAdd(sc.counter, 1u) == gridDim.x * gridDim.y - 1);
+   __syncthreads();
+   if (!last) return;
+   /* call_rr_app: per-box RMS, max over boxes */
+   int t = threadIdx.x + threadIdx.y * blockDim.x;
+   double lres = 0;
+   for (int bx = 0; bx < lv.nbox; bx++) {
+      double v = 0;
+      for (int s = lv.tile_start[bx] + t; s < lv.tile_start[bx + 1]; s += NT) v += __ldcg(&sc.partial[s]);
+      v = block_sum32(v, sm);
+      if (t == 0) {
+         double r = sqrt(v / boxes[lv.box[bx]].count);
+         if (bx == 0) lres = r;
+         lres = (r > lres) ? r : lres;
+         if (trace) {
+            int n = trace->n;
+            if (n < trace->cap) {
+               pgb_trace_rec rr = {1, lv.level, bx, 1, r};
+               trace->rec[n] = rr;
+               trace->n = n + 1;
+            } else
+               trace->overflow = 1;
+         }
+      }
+   }
+   if (t == 0) {
+      *norm_out = lres;
+      *sc.counter = 0;
+   }
+}
+
+/* L_op + compute_MG_rhs (amrd/mg.c:271-314) for the mixed form */
+__global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                     double w0_r)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const double *u = b.f[PGB_F_U];
+   int kz = lv.dim == 3 ? lv.tz : 1;
+   for (int kk = 0; kk < kz; kk++) {
+      int k = tl.k0 + kk;
+      if (k >= b.n[2]) break;
+      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      double lopv = 0;
+      int cm = b.cmask_child[p];
+      if (cm && interior32(b, i, j, k, lv.dim)) lopv = opf(pde, lapf(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
+      b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
+      b.f[PGB_F_LOP][p] = u[p];
+   }
+}
+
+extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
+                                   double *norm_out, pgb_trace *trace, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_residual_fast<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
+                                                                                  norm_out, trace);
+   return check32("residual_fast");
+}
+
+extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
+                                  void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_lop_rhs_fast<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   return check32("lop_rhs_fast");
 }

@@ -13,9 +13,14 @@
  * fastest (Fortran u(Nx,Ny,Nz)); a level's boxes are covered by a list of
  * tiles, one CTA per tile. All boxes of a level are processed by one launch.
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
 #include "pgb_dev.h"
+
+namespace cg = cooperative_groups;
 
 static __thread char g_err[256];
 static unsigned long long g_launches = 0;
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(NT) k_relax(const pgb_dbox *boxes, pgb_dlevel 
    const double *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
    double acc = 0;
    int j = tl.j0 + threadIdx.y;
-   int kz = dim == 3 ? PGB_TZ : 1;
+   int kz = dim == 3 ? lv.rtz : 1;
    for (int kk = 0; kk < kz; kk++) {
       int k = tl.k0 + kk;
       int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(NT) k_residual(const pgb_dbox *boxes, pgb_dlev
    double *res = b.f[PGB_F_RES];
    double acc = 0;
    int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
-   int kz = dim == 3 ? PGB_TZ : 1;
+   int kz = dim == 3 ? lv.tz : 1;
    for (int kk = 0; kk < kz; kk++) {
       int k = tl.k0 + kk;
       if (!interior(b, i, j, k, dim)) continue;
@@ -254,7 +259,7 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
    const pgb_tile tl = lv.tiles[blockIdx.x];                                         \
    const pgb_dbox b = boxes[tl.box];                                                 \
    int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;                              \
-   int kz = lv.dim == 3 ? PGB_TZ : 1;                                                \
+   int kz = lv.dim == 3 ? lv.tz : 1;                                                \
    if (i < b.n[0] && j < b.n[1])                                                     \
       for (int kk = 0; kk < kz; kk++) {                                              \
          int k = tl.k0 + kk;                                                         \
@@ -635,7 +640,7 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
    __shared__ unsigned long long hist[PGB_CHASH];
    __shared__ int s_flag;
    const int t = threadIdx.x, dim = lv.dim;
-   double ctol = *a.res_dn * a.crtol;
+   double ctol = a.ctol_from_first ? -1.0 : *a.res_dn * a.crtol;
    double res = ctol + 1;
    int iter = a.start_iter, nhist = 0;
    int verify_at = -1, period = 0;
@@ -703,6 +708,10 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
       double res_before = res;
       res = sm[0];
       __syncthreads();
+      if (ctol < 0) {
+         ctol = res * a.crtol;
+         res_before = res * 2;
+      }
       iter++;
       if (!(iter < a.max_citer && res > ctol)) break;
       if (a.stagnation_exit && iter > a.start_iter + 1 && res >= res_before) break;
@@ -774,12 +783,407 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
    }
 }
 
+/* The same loop on a cluster of PGB_CL CTAs (one per SM), for coarsest
+ * levels without overlapping boxes: GB300's FP64 rate per SM is low enough
+ * that one CTA spends ~10 us per sweep of a 9^3 grid. The colour passes are
+ * split over the cluster and separated by cluster barriers; every CTA
+ * combines the per-CTA partial norms and state hashes through distributed
+ * shared memory in the same fixed order, so all CTAs take the same
+ * decisions. Each point is relaxed by exactly one CTA, which also hashes,
+ * saves and compares that point (nothing else changes during the loop). */
+#define PGB_CL 8
+#define CLT 512
+#define MAXCB 8
+__global__ void __cluster_dims__(PGB_CL, 1, 1) __launch_bounds__(CLT)
+   k_coarsest_cl(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_coarsest_args a,
+                 pgb_trace *trace)
+{
+   cg::cluster_group cl = cg::this_cluster();
+   const int rank = (int)cl.block_rank(), t = threadIdx.x, dim = lv.dim;
+   const long gstride = (long)PGB_CL * CLT;
+   __shared__ double part[2][MAXCB];
+   __shared__ unsigned long long hpart[2];
+   __shared__ int fpart[2];
+   __shared__ double sm[32];
+   __shared__ unsigned long long smh[32];
+   __shared__ unsigned long long hist[PGB_CHASH];
+   __shared__ double s_res;
+   __shared__ unsigned long long s_h;
+   __shared__ int s_changed;
+   int cb[MAXCB], ncb = 0;
+   for (int b = 0; b < lv.nbox && ncb < MAXCB; b++)
+      if (boxes[lv.box[b]].flags & PGB_BOX_COARSEST) cb[ncb++] = b;
+   double ctol = a.ctol_from_first ? -1.0 : *a.res_dn * a.crtol;
+   double res = ctol + 1;
+   int iter = a.start_iter, nhist = 0, verify_at = -1, period = 0, it_no = 0;
+   double *saved = a.snap;
+   while (iter < a.max_citer && res > ctol) {
+      const int par = it_no & 1;
+      double acc[MAXCB];
+      unsigned long long h = 0;
+      int diff = 0;
+      for (int c = 0; c < ncb; c++) acc[c] = 0;
+      for (int pass = 0; pass < 2; pass++) {
+         for (int c = 0; c < ncb; c++) {
+            const pgb_dbox bx = boxes[lv.box[cb[c]]];
+            const long off = a.snap_off[cb[c]];
+            long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
+            long hw = (ni + 1) / 2, nslot = hw * nj * nk;   /* one slot per point of the colour */
+            for (long q = (long)t * PGB_CL + rank; q < nslot; q += gstride) {
+               int j = 1 + (int)((q / hw) % nj);
+               int k = dim == 3 ? 1 + (int)(q / (hw * nj)) : 0;
+               int off = dim == 3 ? ((1 + j + k + 3 + pass) & 1) : ((1 + j + 2 + pass) & 1);
+               int i = 1 + 2 * (int)(q % hw) + off;
+               if (i > ni) continue;
+               long p = i + (long)bx.n[0] * (j + (long)bx.n[1] * k);
+               if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+               double *u = bx.f[PGB_F_U];
+               double uc = u[p], s = bx.f[PGB_F_SRC][p];
+               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
+               double jac = jac64(pde, bx.j0, uc, s);
+               double nu = uc - r / jac;
+               u[p] = nu;
+               acc[c] += r * r;
+               unsigned long long bits = (unsigned long long)__double_as_longlong(nu);
+               h ^= mix64(bits ^ mix64((unsigned long long)(off + p) + 0x9E3779B97F4A7C15ull));
+               if (verify_at >= 0 && iter + 1 == verify_at && saved[off + p] != nu) diff = 1;
+               if (verify_at < 0) saved[off + p] = nu;   /* candidate save, kept if a match is found */
+            }
+         }
+         if (pass == 0) cl.sync();
+      }
+      /* per-CTA partials */
+      for (int c = 0; c < ncb; c++) {
+         double v = block_sum(acc[c], sm);
+         if (t == 0) part[par][c] = v;
+      }
+      h = block_xor(h, smh);
+      if (t == 0) s_changed = 0;
+      __syncthreads();
+      if (diff) s_changed = 1;
+      __syncthreads();
+      if (t == 0) {
+         hpart[par] = h;
+         fpart[par] = s_changed;
+      }
+      cl.sync();
+      /* combine over the cluster in rank order (identical in every CTA) */
+      if (t == 0) {
+         double lres = 0;
+         unsigned long long hh = 0;
+         int ch = 0;
+         for (int c = 0; c < ncb; c++) {
+            double v = 0;
+            for (int rr = 0; rr < PGB_CL; rr++) v += cl.map_shared_rank(&part[par][0], rr)[c];
+            const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+            double r = sqrt(v / bx.count);
+            if (c == 0) lres = r;
+            lres = (r > lres) ? r : lres;
+            if (trace && rank == 0) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rec = {0, lv.level, cb[c], 1, r};
+                  trace->rec[n] = rec;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+         }
+         for (int rr = 0; rr < PGB_CL; rr++) {
+            hh ^= *cl.map_shared_rank(&hpart[par], rr);
+            ch |= *cl.map_shared_rank(&fpart[par], rr);
+         }
+         s_res = lres;
+         s_h = hh;
+         s_changed = ch;
+      }
+      __syncthreads();
+      double res_before = res;
+      res = s_res;
+      h = s_h;
+      const int changed = s_changed;
+      it_no++;
+      if (ctol < 0) {
+         ctol = res * a.crtol;
+         res_before = res * 2;
+      }
+      iter++;
+      if (!(iter < a.max_citer && res > ctol)) break;
+      if (a.stagnation_exit && iter > a.start_iter + 1 && res >= res_before) break;
+      if (iter == verify_at) {
+         if (!changed) {
+            int rem = a.max_citer - iter;
+            int skip = rem - rem % period;
+            if (trace && rank == 0 && t == 0 && skip > 0) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rec = {2, lv.level, period, skip, 0.0};
+                  trace->rec[n] = rec;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+            iter += skip;
+            nhist = 0;
+         }
+         verify_at = -1;
+      } else if (verify_at < 0) {
+         int found = 0;
+         int lim = nhist < PGB_CHASH ? nhist : PGB_CHASH;
+         for (int p = 1; p <= lim && !found; p++)
+            if (hist[(nhist - p) % PGB_CHASH] == h) found = p;
+         if (found) {   /* this iteration's values were saved above */
+            period = found;
+            verify_at = iter + found;
+         }
+      }
+      __syncthreads();
+      if (t == 0) hist[nhist % PGB_CHASH] = h;
+      nhist++;
+      __syncthreads();
+   }
+   cl.sync();
+   if (rank == 0 && t == 0) {
+      *a.res_out = res;
+      if (a.iters_out) *a.iters_out += iter - a.start_iter;
+   }
+}
+
+/* ---------------------------------------------- coarsest grids, on chip -- */
+/* Correctly rounded x / d for a divisor d known in advance, with r = RN(1/d)
+ * computed by the host: q0 = RN(x*r), e = x - q0*d (exact with FMA),
+ * q = RN(q0 + e*r). Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34,
+ * 1990; Muller et al., Handbook of Floating-Point Arithmetic, 2018, sec.
+ * 4.7) gives q = RN(x/d) when r = RN(1/d) and q0 is within one ulp of x/d,
+ * barring overflow/underflow; the tests compare it with IEEE division. */
+__device__ __forceinline__ double div_known(double x, double d, double r)
+{
+   double q0 = __dmul_rn(x, r);
+   double e = __fma_rn(-q0, d, x);
+   return __fma_rn(e, r, q0);
+}
+
+/* lap(u) of num.f:113-115 with the divisions by dx^2 done by div_known */
+__device__ __forceinline__ double lap_known(const pgb_dbox &b, const double *u, long p, long sy,
+                                            long sz, int dim)
+{
+   double c = u[p];
+   double t;
+   if (b.flags & PGB_BOX_POW2DX)
+      t = (u[p + 1] - 2 * c + u[p - 1]) * b.idx2[0] + (u[p + sy] - 2 * c + u[p - sy]) * b.idx2[1];
+   else
+      t = div_known(u[p + 1] - 2 * c + u[p - 1], b.dx2[0], b.idx2[0]) +
+          div_known(u[p + sy] - 2 * c + u[p - sy], b.dx2[1], b.idx2[1]);
+   if (dim == 3) {
+      if (b.flags & PGB_BOX_POW2DX) t = t + (u[p + sz] - 2 * c + u[p - sz]) * b.idx2[2];
+      else t = t + div_known(u[p + sz] - 2 * c + u[p - sz], b.dx2[2], b.idx2[2]);
+   }
+   return t;
+}
+
+/* The coarsest-grid loop with the whole coarsest level (u, rhs, source and
+ * the saved state of the cycle check) held in shared memory: below the
+ * rounding floor the loop is latency bound, and keeping the grid on chip
+ * removes the global-memory round trips from every sweep. Same iteration,
+ * same cycle skip and same results as k_coarsest. */
+#define CS_MAXB 16
+__global__ void __launch_bounds__(CT) k_coarsest_smem(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                      const pgb_copy_op *sync_ops, int nsync,
+                                                      pgb_coarsest_args a, pgb_trace *trace)
+{
+   extern __shared__ double dsm[];
+   __shared__ double sm[32];
+   __shared__ unsigned long long smh[32];
+   __shared__ unsigned long long hist[PGB_CHASH];
+   __shared__ int s_flag;
+   __shared__ int cb[CS_MAXB], ncb_s;
+   __shared__ long coff[CS_MAXB + 1];
+   const int t = threadIdx.x, dim = lv.dim;
+   if (t == 0) {
+      int n = 0;
+      long o = 0;
+      for (int b = 0; b < lv.nbox && n < CS_MAXB; b++) {
+         const pgb_dbox &bx = boxes[lv.box[b]];
+         if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+         cb[n] = b;
+         coff[n] = o;
+         o += (long)bx.n[0] * bx.n[1] * bx.n[2];
+         n++;
+      }
+      coff[n] = o;
+      ncb_s = n;
+   }
+   __syncthreads();
+   const int ncb = ncb_s;
+   const long tot = coff[ncb];
+   double *su = dsm, *srhs = dsm + tot, *ssrc = dsm + 2 * tot, *ssave = dsm + 3 * tot;
+   for (int c = 0; c < ncb; c++) {
+      const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+      long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+      for (long q = t; q < n; q += CT) {
+         su[coff[c] + q] = bx.f[PGB_F_U][q];
+         srhs[coff[c] + q] = bx.f[PGB_F_RHS][q];
+         ssrc[coff[c] + q] = bx.f[PGB_F_SRC][q];
+      }
+   }
+   __syncthreads();
+   double ctol = a.ctol_from_first ? -1.0 : *a.res_dn * a.crtol;
+   double res = ctol + 1;
+   int iter = a.start_iter, nhist = 0, verify_at = -1, period = 0;
+   while (iter < a.max_citer && res > ctol) {
+      double lres = 0;
+      for (int c = 0; c < ncb; c++) {
+         const pgb_dbox bx = boxes[lv.box[cb[c]]];
+         double *u = su + coff[c];
+         const double *rhs = srhs + coff[c], *src = ssrc + coff[c];
+         const long sy = bx.n[0], sz = (long)bx.n[0] * bx.n[1];
+         long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
+         long hw = (ni + 1) / 2, nslot = hw * nj * nk;   /* one slot per point of the colour */
+         double acc = 0;
+         for (int pass = 0; pass < 2; pass++) {
+            for (long q = t; q < nslot; q += CT) {
+               int j = 1 + (int)((q / hw) % nj);
+               int k = dim == 3 ? 1 + (int)(q / (hw * nj)) : 0;
+               int off = dim == 3 ? ((1 + j + k + 3 + pass) & 1) : ((1 + j + 2 + pass) & 1);
+               int i = 1 + 2 * (int)(q % hw) + off;
+               if (i > ni) continue;
+               long p = i + sy * j + sz * k;
+               if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+               double uc = u[p], s = src[p];
+               double r = op64(pde, lap_known(bx, u, p, sy, sz, dim), uc, s) - rhs[p];
+               double jac = jac64(pde, bx.j0, uc, s);
+               u[p] = uc - r / jac;
+               acc += r * r;
+            }
+            __syncthreads();
+         }
+         acc = block_sum(acc, sm);
+         if (t == 0) {
+            double r = sqrt(acc / bx.count);
+            if (c == 0) lres = r;
+            lres = (r > lres) ? r : lres;
+            if (trace) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rr = {0, lv.level, cb[c], 1, r};
+                  trace->rec[n] = rr;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+         }
+      }
+      for (int o = 0; o < nsync; o++) {   /* PAMR_sync(L,0,MGH,1) over the coarsest grids */
+         const pgb_copy_op op = sync_ops[o];
+         int cs = -1, cd = -1;
+         for (int c = 0; c < ncb; c++) {
+            if (lv.box[cb[c]] == op.src_box) cs = c;
+            if (lv.box[cb[c]] == op.dst_box) cd = c;
+         }
+         if (cs < 0 || cd < 0) continue;
+         const pgb_dbox &bs = boxes[op.src_box];
+         const pgb_dbox &bd = boxes[op.dst_box];
+         long np = (long)op.ni * op.nj * op.nk;
+         for (long q = t; q < np; q += CT) {
+            int aa, bb, cc;
+            unflat(q, op.ni, op.nj, aa, bb, cc);
+            su[coff[cd] + lin(bd, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
+               su[coff[cs] + lin(bs, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
+         }
+         __syncthreads();
+      }
+      if (t == 0) sm[0] = lres;
+      __syncthreads();
+      double res_before = res;
+      res = sm[0];
+      __syncthreads();
+      if (ctol < 0) {
+         ctol = res * a.crtol;
+         res_before = res * 2;
+      }
+      iter++;
+      if (!(iter < a.max_citer && res > ctol)) break;
+      if (a.stagnation_exit && iter > a.start_iter + 1 && res >= res_before) break;
+      /* hash of the state; compare with the saved state at a verification point */
+      unsigned long long h = 0;
+      if (t == 0) s_flag = 0;
+      __syncthreads();
+      for (long q = t; q < tot; q += CT) {
+         double v = su[q];
+         unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+         h ^= mix64(bits ^ mix64((unsigned long long)q + 0x9E3779B97F4A7C15ull));
+         if (iter == verify_at && ssave[q] != v) s_flag = 1;
+      }
+      h = block_xor(h, smh);
+      if (iter == verify_at) {
+         if (!s_flag) {
+            int rem = a.max_citer - iter;
+            int skip = rem - rem % period;
+            if (trace && t == 0 && skip > 0) {
+               int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rr = {2, lv.level, period, skip, 0.0};
+                  trace->rec[n] = rr;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+            iter += skip;
+            nhist = 0;
+         }
+         verify_at = -1;
+      } else if (verify_at < 0) {
+         int found = 0;
+         int lim = nhist < PGB_CHASH ? nhist : PGB_CHASH;
+         for (int p = 1; p <= lim && !found; p++)
+            if (hist[(nhist - p) % PGB_CHASH] == h) found = p;
+         if (found) {
+            for (long q = t; q < tot; q += CT) ssave[q] = su[q];
+            period = found;
+            verify_at = iter + found;
+         }
+      }
+      __syncthreads();
+      if (t == 0) hist[nhist % PGB_CHASH] = h;
+      nhist++;
+      __syncthreads();
+   }
+   for (int c = 0; c < ncb; c++) {
+      const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+      long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+      for (long q = t; q < n; q += CT) bx.f[PGB_F_U][q] = su[coff[c] + q];
+   }
+   if (t == 0) {
+      *a.res_out = res;
+      if (a.iters_out) *a.iters_out += iter - a.start_iter;
+   }
+}
+
 extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                               pgb_coarsest_args a, pgb_trace *trace, void *stream)
 {
-   k_coarsest<<<1, CT, 0, (cudaStream_t)stream>>>(boxes, lv, pde, (const pgb_copy_op *)sync->d_ops,
-                                                  sync->nops, a, trace);
-   LAUNCHED(1);
+   size_t smem = (size_t)a.smem_points * 4 * sizeof(double);
+   const char *force = getenv("PGB_COARSEST_KERNEL");   /* smem | cluster | single (experiments) */
+   int want_smem = !force || !strcmp(force, "smem");
+   int want_cl = !force || !strcmp(force, "cluster");
+   if (want_smem && a.smem_points > 0 && a.ncoarse <= CS_MAXB && smem <= 200 * 1024) {
+      static int attr_set = 0;
+      if (!attr_set) {
+         cudaFuncSetAttribute(k_coarsest_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+         attr_set = 1;
+      }
+      k_coarsest_smem<<<1, CT, smem, (cudaStream_t)stream>>>(
+         boxes, lv, pde, (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
+      LAUNCHED(1);
+   } else if (want_cl && sync->nops == 0 && lv.nbox <= MAXCB) {
+      k_coarsest_cl<<<PGB_CL, CLT, 0, (cudaStream_t)stream>>>(boxes, lv, pde, a, trace);
+      LAUNCHED(1);
+   } else {
+      k_coarsest<<<1, CT, 0, (cudaStream_t)stream>>>(boxes, lv, pde,
+                                                     (const pgb_copy_op *)sync->d_ops, sync->nops,
+                                                     a, trace);
+      LAUNCHED(1);
+   }
    return check("coarsest");
 }
 

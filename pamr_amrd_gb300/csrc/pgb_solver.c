@@ -39,6 +39,9 @@ struct pgb_solver {
    pgb_trace *d_trace;
    int trace_cap;
    double *h_res;           /* pinned */
+   cudaGraphExec_t gexec;   /* one captured V-cycle (+ read-back of the residual) */
+   int graph_ok;
+   long long graph_kernels; /* kernel launches in the captured V-cycle */
    cudaEvent_t ev0, ev1;
    int last_cycles;
    long last_citers;
@@ -46,6 +49,7 @@ struct pgb_solver {
 };
 
 static __thread char g_err[512];
+static long long g_graph_replayed = 0, g_captured = 0;
 
 const char *pgb_last_error(void) { return g_err; }
 
@@ -89,12 +93,29 @@ void pgb_default_params(pgb_mg_params *p)
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-/* tiles of the boxes of one level; tx = tile width in x */
-static int make_tiles(const pgb_hier *h, int L, int tx, pgb_tile **out, int *start)
+/* planes per tile: the largest of 8, 4, 2, 1 that still gives the level at
+ * least two CTAs per SM of GB300 (152 SMs) */
+static int choose_tz(const pgb_hier *h, int L, int tx)
+{
+   int tz, b;
+   if (h->dim != 3) return 1;
+   for (tz = PGB_TZ; tz > 1; tz /= 2) {
+      long n = 0;
+      for (b = 0; b < h->lev[L].nbox; b++) {
+         const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+         n += (long)((bx->shape[0] + tx - 1) / tx) * ((bx->shape[1] + PGB_TY - 1) / PGB_TY) *
+              ((bx->shape[2] + tz - 1) / tz);
+      }
+      if (n >= 2 * 152) break;
+   }
+   return tz;
+}
+
+/* tiles of the boxes of one level; tx = tile width in x, tz planes deep */
+static int make_tiles(const pgb_hier *h, int L, int tx, int tz, pgb_tile **out, int *start)
 {
    int b, n = 0, cap = 64;
    pgb_tile *t = (pgb_tile *)malloc(sizeof(pgb_tile) * (size_t)cap);
-   int tz = h->dim == 3 ? PGB_TZ : 1;
    for (b = 0; b < h->lev[L].nbox; b++) {
       const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
       int i, j, k;
@@ -157,12 +178,12 @@ static int setup_device(pgb_solver *s)
       off = align256(off + n);
    }
    if (h->prm.precision == PGB_MIXED) {
-      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * 3);
+      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * 4);
       for (i = 0; i < h->nbox; i++) {
          const pgb_hbox *b = &h->boxes[i];
          size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
-         for (f = 0; f < 3; f++) {
-            w32o[i * 3 + f] = off;
+         for (f = 0; f < 4; f++) {
+            w32o[i * 4 + f] = off;
             off = align256(off + 4 * n);
          }
       }
@@ -178,7 +199,7 @@ static int setup_device(pgb_solver *s)
       double dx2[3] = {1, 1, 1};
       for (f = 0; f < PGB_NF; f++) db->f[f] = (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
       if (w32o)
-         for (f = 0; f < 3; f++) db->w32[f] = (float *)(s->arena + w32o[i * 3 + f]);
+         for (f = 0; f < 4; f++) db->w32[f] = (float *)(s->arena + w32o[i * 4 + f]);
       db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
       db->cmask_bdy = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF + 1]);
       CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
@@ -210,8 +231,9 @@ static int setup_device(pgb_solver *s)
       int nb = h->lev[L].nbox;
       int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
       int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
-      int nt = make_tiles(h, L, PGB_TX, &t, ts);
-      int nrt = make_tiles(h, L, 2 * PGB_TX, &rt, rts);
+      int tz = choose_tz(h, L, PGB_TX), rtz = choose_tz(h, L, 2 * PGB_TX);
+      int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
+      int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
       size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
       size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
       size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
@@ -233,6 +255,8 @@ static int setup_device(pgb_solver *s)
       s->lv[L].ntiles = nt;
       s->lv[L].nrtiles = nrt;
       s->lv[L].nbox = nb;
+      s->lv[L].tz = tz;
+      s->lv[L].rtz = rtz;
       s->lv[L].dim = h->dim;
       s->lv[L].level = L;
       if (nt > maxt) maxt = nt;
@@ -357,6 +381,7 @@ int pgb_destroy(pgb_solver *s)
       if (s->d_snap) cudaFree(s->d_snap);
       if (s->d_trace) cudaFree(s->d_trace);
       if (s->h_res) cudaFreeHost(s->h_res);
+      if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
       if (s->stream) {
          cudaEventDestroy(s->ev0);
          cudaEventDestroy(s->ev1);
@@ -474,12 +499,12 @@ int pgb_prepare(pgb_solver *s)
 /* one smoothing block (nsweep sweeps + syncs, amrd/mg.c:135-141 / 161-167).
  * FP64: Newton-GS sweeps. Mixed: FP64 defect, FP32 sweeps on the correction
  * (synced between boxes like u), FP64 update, then the sync of u. The
- * coarsest level always smooths in FP64. */
+ * coarsest-grid loop itself always runs in FP64. */
 static int smooth(pgb_solver *s, int L, int nsweep, int slot)
 {
    pgb_hier *h = &s->h;
    int it;
-   if (h->prm.precision == PGB_FP64 || L == 1) {
+   if (h->prm.precision == PGB_FP64) {
       for (it = 0; it < nsweep; it++) {
          if (relax(s, L, slot)) return 11;
          if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
@@ -501,19 +526,24 @@ static int vcycle_launch(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
-   int L, Lf = h->nlev;
+   int L, Lf = h->nlev, mixed = p->precision == PGB_MIXED;
    /* clear_MG_vars(Lf) amrd/mg.c:91 */
    KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
       if (L < Lf) {
-         KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
-                           s->d_trace, s->stream));
+         if (mixed)
+            KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
+                                     s->d_trace, s->stream));
+         else
+            KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
+                              s->d_trace, s->stream));
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;   /* set_res_sync */
          /* clear_MG_vars(L): rhs and lop are rewritten whole by lop_rhs below */
          KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
          if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
-         KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+         if (mixed) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+         else KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
       if (smooth(s, L, p->pre_swp, N_RELAX_DN)) return 11;
    }
@@ -536,26 +566,84 @@ static int vcycle_launch(pgb_solver *s)
          a.res_dn = norm_slot(s, L, p->pre_swp > 0 ? N_RELAX_DN : N_COARSE);
          a.res_out = norm_slot(s, L, N_COARSE);
          a.iters_out = s->d_citers;
-         a.stagnation_exit = p->precision == PGB_MIXED;
+         a.smem_points = 0;
+         a.ncoarse = 0;
+         {
+            int b;
+            for (b = 0; b < h->lev[L].nbox; b++) {
+               const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+               if (!bx->coarsest) continue;
+               a.smem_points += (long)bx->shape[0] * bx->shape[1] * bx->shape[2];
+               a.ncoarse++;
+            }
+         }
+         a.stagnation_exit = mixed;
+         a.ctol_from_first = mixed;
          a.snap = s->d_snap;
          a.snap_points = s->snap_points;
          a.snap_off = s->d_snap_off[L];
          KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
       }
-      if (L == Lf)
-         KC(pgb_k_residual(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID), s->d_trace,
-                           s->stream));
+      if (L == Lf) {
+         if (mixed)
+            KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
+                                     s->d_trace, s->stream));
+         else
+            KC(pgb_k_residual(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
+                              s->d_trace, s->stream));
+      }
    }
    return 0;
+}
+
+/* The V-cycle's launches never depend on host-side values, so the whole
+ * cycle (and the read-back of the finest residual) is captured once into a
+ * CUDA graph and replayed: one launch per cycle instead of ~100. */
+static int build_graph(pgb_solver *s)
+{
+   cudaGraph_t g = 0;
+   cudaError_t e;
+   long long before = pgb_dev_launches() + pgb_dev_launches32();
+   int rc;
+   CU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+   rc = vcycle_launch(s);
+   if (!rc && cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double),
+                              cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+      rc = fail(10, "graph capture: residual read-back");
+   e = cudaStreamEndCapture(s->stream, &g);
+   if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+   }
+   if (e != cudaSuccess) return fail(10, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+   e = cudaGraphInstantiate(&s->gexec, g, 0);
+   cudaGraphDestroy(g);
+   if (e != cudaSuccess) return fail(10, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+   s->graph_kernels = pgb_dev_launches() + pgb_dev_launches32() - before;
+   g_captured += s->graph_kernels;
+   s->graph_ok = 1;
+   return 0;
+}
+
+static void drop_graph(pgb_solver *s)
+{
+   if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
+   s->graph_ok = 0;
 }
 
 int pgb_vcycle(pgb_solver *s, double *res)
 {
    int rc;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
-   if ((rc = vcycle_launch(s))) return rc;
-   CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double),
-                      cudaMemcpyDeviceToHost, s->stream));
+   if (getenv("PGB_NO_GRAPH")) {
+      if ((rc = vcycle_launch(s))) return rc;
+      CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double),
+                         cudaMemcpyDeviceToHost, s->stream));
+   } else {
+      if (!s->graph_ok && (rc = build_graph(s))) return rc;
+      CU(cudaGraphLaunch(s->gexec, s->stream));
+      g_graph_replayed += s->graph_kernels;
+   }
    CU(cudaStreamSynchronize(s->stream));
    *res = s->h_res[0];
    return 0;
@@ -596,7 +684,10 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
    return 0;
 }
 
-long long pgb_launch_count(void) { return (long long)(pgb_dev_launches() + pgb_dev_launches32()); }
+long long pgb_launch_count(void)
+{
+   return (long long)(pgb_dev_launches() + pgb_dev_launches32()) - g_captured + g_graph_replayed;
+}
 
 int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double *bytes_per_sweep)
 {
@@ -605,16 +696,21 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    double pts = 0;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (L < 1 || L > s->h.nlev || reps < 1) return fail(3, "bad level or reps");
+   int mixed = s->h.prm.precision == PGB_MIXED;
    for (b = 0; b < s->h.lev[L].nbox; b++) pts += s->h.boxes[s->h.lev[L].box[b]].count;
-   if (relax(s, L, N_RELAX_UP)) return 11;   /* warm-up */
-   CU(cudaEventRecord(s->ev0, s->stream));
-   for (r = 0; r < reps; r++)
-      if (relax(s, L, N_RELAX_UP)) return 11;
+   if (mixed) KC32(pgb_k_defect(s->dbox, s->lv[L], s->h.pde, s->stream));
+   for (r = 0; r <= reps; r++) {
+      if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));   /* first sweep warms up */
+      if (mixed) KC32(pgb_k_relax32(s->dbox, s->lv[L], s->stream));
+      else if (relax(s, L, N_RELAX_UP)) return 11;
+   }
    CU(cudaEventRecord(s->ev1, s->stream));
    CU(cudaEventSynchronize(s->ev1));
    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
    if (ms_per_sweep) *ms_per_sweep = ms / reps;
-   if (bytes_per_sweep) *bytes_per_sweep = 32.0 * pts;
+   /* FP64 sweep: u read+write, rhs, src (32 B); FP32 sweep on the
+    * correction: e read+write, defect, Jacobian term (16 B) */
+   if (bytes_per_sweep) *bytes_per_sweep = (mixed ? 16.0 : 32.0) * pts;
    return 0;
 }
 
@@ -623,6 +719,7 @@ int pgb_trace_enable(pgb_solver *s, int capacity)
 {
    int hdr[4] = {0, capacity, 0, 0};
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   drop_graph(s);   /* the trace pointer is baked into the captured launches */
    if (s->d_trace) cudaFree(s->d_trace);
    s->d_trace = 0;
    s->trace_cap = 0;
