@@ -102,7 +102,9 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
 
 /* One FAS V-cycle; *res = finest-level residual. Replaces vcycle
  * (amrd/mg.c:84-201). pgb_prepare performs the MG-hierarchy initialisation
- * pgb_solve does before its first cycle. */
+ * pgb_solve does before its first cycle; pgb_vcycle runs it itself when an
+ * input grid was set (pgb_set_grid*) or a level was swept by pgb_time_relax
+ * since the last pgb_prepare. */
 int pgb_prepare(pgb_solver *s);
 int pgb_vcycle(pgb_solver *s, double *res);
 
@@ -126,6 +128,12 @@ long long pgb_launch_count(void);
  * Modifies u (FP64) or the correction (mixed) on that level. */
 int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
                    double *bytes_per_sweep);
+
+/* Launch shapes the mixed form's autotuner chose for a level at the first
+ * pgb_prepare: tile depth in planes, and FP32 sweeps per launch (0 = one
+ * launch per colour pass, 1 or 2 = shared-memory sweeps); no reference
+ * counterpart. */
+int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per_launch);
 
 /* Norm trace: when enabled, every norm a hook would return is recorded
  * (kind 0 relax, 1 residual, 2 = skipped coarsest iterations; level; box;

@@ -27,7 +27,9 @@ typedef struct {
    const int *tile_start;      /* per level box: first tile (prefix, nbox+1) */
    const int *rtile_start;
    const int *box;             /* level box -> global box index */
-   int ntiles, nrtiles, nbox;
+   const pgb_tile *ctiles;     /* tiles holding a child-covered point or a point some
+                                  interpolation to the next finer level reads */
+   int ntiles, nrtiles, nbox, nctiles;
    int tz, rtz;                /* planes per tile (3-D) of the two tile lists */
    int dim;
    int level;
@@ -64,6 +66,7 @@ typedef struct {
    int ctol_from_first;        /* mixed form: ctol = crtol x the loop's first norm */
    long smem_points;           /* points of the level's coarsest boxes (on-chip kernel) */
    int ncoarse;                /* number of coarsest boxes on the level */
+   double omega;               /* mixed form: over-relaxation factor of the loop */
    double *snap;               /* 2 x (points of the coarsest boxes) doubles */
    long snap_points;
    const long *snap_off;       /* per level box: offset of its points in a snapshot */
@@ -84,7 +87,8 @@ int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, vo
 int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream);
 int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream);
-int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
+/* restricts the fields of field_mask (bit f = grid function f) that the plan's ops carry */
+int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, void *stream);
 int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim, void *stream);
 int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                    pgb_coarsest_args a, pgb_trace *trace, void *stream);
@@ -93,14 +97,18 @@ int pgb_k_fill(double *p, long n, double v, void *stream);
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);
 unsigned long long pgb_dev_launches32(void);
-int pgb_k_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, void *stream);
-int pgb_k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
-int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
+int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
+int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream);
+int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, void *stream);
+int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
+int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream);
 int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream);
 int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
                         double *norm_out, pgb_trace *trace, void *stream);
 int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
+int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
+                         pgb_coarsest_args a, pgb_trace *trace, void *stream);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,7 @@ enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, 
 #define PGB_BOX_POW2DX 1     /* every dx^2 is a power of two: x/dx2 == x*(1/dx2) exactly */
 #define PGB_BOX_BDY_INTERIOR 2 /* the boundary cmask is ON at every interior point */
 #define PGB_BOX_COARSEST 4
+#define PGB_BOX_ISO 8         /* dx^2 is the same in every dimension */
 
 /* device view of one MG box (all pointers are device pointers) */
 typedef struct {

@@ -2,28 +2,41 @@
  * Mixed-precision kernels of libpamr_gb300 (sm_103a): FP32 smoothing and
  * FP32 prolongation inside FP64 defect correction.
  *
- * A smoothing block of the FAS V-cycle (MG_pre_swp or MG_pst_swp sweeps of
- * amrd/mg.c:135-141, 161-167) becomes
- *     d = rhs - L[u]                       (FP64 defect, stored as FP32)
- *     e = 0; sweeps of red-black GS on L'(u) e = d   (FP32)
- *     u = u + e                            (FP64 update)
- * For a linear operator the FP32 sweeps produce, up to FP32 rounding of the
- * correction, exactly the correction the FP64 sweeps would; for the
- * nonlinear conformal factor they are the linearised (Newton) sweeps. The
- * coarse-grid correction (f - lop)/w0 is computed in FP64 and interpolated
- * in FP32 (same nested line order as dminterp3d; FP64 on box boundaries)
- * before the FP64 add. The
- * V-cycle keeps every FP64 piece of the reference: residuals, restriction,
- * FAS right-hand sides, coarsest-grid solve and the finest-level norm.
+ * Every smoothing block of the FAS V-cycle (MG_pre_swp / MG_pst_swp sweeps,
+ * amrd/mg.c:135-141, 161-167) works on a correction E in FP32:
+ *     D = rhs - L[u]   (FP64, stored in FP32)     C = dL/du - lap part (FP32)
+ *     red-black Gauss-Seidel on  lap E + C E = D  (FP32)
+ *     u = u + E        (FP64)
+ * D comes from FP64 passes the V-cycle runs anyway:
+ *   - down sweep, level below the finest: the FAS right-hand-side pass
+ *     (k_fas_defect) evaluates L[u] once for both rhs and D;
+ *   - the residual pass after pre-smoothing (k_residual_fast) leaves
+ *     D = -res for the post-smoothing block of the same level, and on the
+ *     finest level for the next cycle's pre-smoothing block.
+ * The coarse-grid correction (f - lop)/w0 is formed in FP64, stored once in
+ * FP32 (X), interpolated in FP32 and becomes the starting value of E for the
+ * post-smoothing block, so L[u + E] = rhs is solved from the pre-smoothing
+ * residual with no further FP64 pass. Points the smoother never relaxes
+ * (box boundaries, cmask-off points) take the FP64-interpolated correction
+ * instead, so values that only change through corrections never collect
+ * FP32 rounding. The V-cycle keeps every FP64 piece of the reference:
+ * residuals, restriction, FAS right-hand sides, coarsest-grid solve and the
+ * finest-level norm; for the nonlinear conformal operator the FP32 sweeps are
+ * the linearised (Newton) sweeps and the next FP64 residual sees what the
+ * linearisation left out.
  *
- * Compiled with FMA contraction: nothing here is compared bit for bit.
+ * FP64 on this part runs at 2 operations per clock per SM (FP32: 128), so
+ * the FP64 passes here are written for the fewest FP64 instructions: fused
+ * multiply-adds, products with 1/dx^2, and FP32 wherever the value only
+ * steers the smoother. Nothing here is compared bit for bit.
  */
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdio.h>
 #include "pgb_dev.h"
+#include "pgb_opgrid.cuh"
 
 static __thread char g_err32[256];
-extern "C" unsigned long long pgb_dev_launches(void);
 static unsigned long long g_launches32 = 0;
 
 extern "C" unsigned long long pgb_dev_launches32(void) { return g_launches32; }
@@ -43,9 +56,9 @@ extern "C" const char *pgb_dev_error32(void) { return g_err32; }
 
 #define NT (PGB_TX * PGB_TY)
 #define TWO_PI 6.283185307179586
-#define TEN_PI 31.41592653589793
 
-enum { W_E = 0, W_D = 1, W_C = 2 };
+/* the FP32 arrays of a box: correction, defect, Jacobian term, coarse correction */
+enum { W_E = 0, W_D = 1, W_C = 2, W_X = 3 };
 
 __device__ __forceinline__ bool interior32(const pgb_dbox &b, int i, int j, int k, int dim)
 {
@@ -53,88 +66,245 @@ __device__ __forceinline__ bool interior32(const pgb_dbox &b, int i, int j, int 
           (dim == 2 ? k == 0 : (k >= 1 && k <= b.n[2] - 2));
 }
 
-/* FP64 defect d = rhs - L[u] and the FP32 Jacobian term c = dL/du - lap part;
- * e = 0. Points outside the relaxed set get d = 0 so e stays 0 there. */
-__global__ void __launch_bounds__(NT) k_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde)
+/* the points relax visits: interior and cmask_bdy ON (num.f:211-232) */
+__device__ __forceinline__ bool relaxed32(const pgb_dbox &b, int i, int j, int k, long p, int dim)
+{
+   return interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p]);
+}
+
+/* lap u in FP64 (num.f:113-115 up to rounding). Per dimension
+ * RN(u+ - 2u) + u- rounds once at the scale of u (the last add is exact
+ * near convergence, Sterbenz), which keeps the residual's rounding floor at
+ * the reference's; summing the neighbours first would raise it. */
+__device__ __forceinline__ double lapm(const pgb_dbox &b, const double *u, long p, long sy, long sz,
+                                       int dim)
+{
+   const double c = u[p];
+   const double dx = fma(-2.0, c, u[p + 1]) + u[p - 1];
+   const double dy = fma(-2.0, c, u[p + sy]) + u[p - sy];
+   if (b.flags & PGB_BOX_ISO) {
+      if (dim == 3) return ((dx + dy) + (fma(-2.0, c, u[p + sz]) + u[p - sz])) * b.idx2[0];
+      return (dx + dy) * b.idx2[0];
+   }
+   double t = fma(dy, b.idx2[1], dx * b.idx2[0]);
+   if (dim == 3) t = fma(fma(-2.0, c, u[p + sz]) + u[p - sz], b.idx2[2], t);
+   return t;
+}
+
+/* L[u] from lap u for the three operators (Poisson t - s, conformal factor
+ * t + 2 pi s u^5, lapse t - s u; num.f:85-123 pattern) and, in c, the FP32
+ * derivative of the non-Laplacian part (5 * 2 pi s u^4, -s, 0) */
+__device__ __forceinline__ double opjac(int pde, double t, double uc, double s, float &c)
+{
+   if (pde == 1) {
+      double p2 = uc * uc, a = TWO_PI * s * (p2 * p2);
+      c = 5.f * (float)a;
+      return fma(a, uc, t);
+   }
+   if (pde == 2) {
+      c = -(float)s;
+      return fma(-s, uc, t);
+   }
+   c = 0.f;
+   return t - s;
+}
+
+/* Down sweep, levels below the finest: app_L_op + compute_MG_rhs
+ * (amrd/mg.c:271-314) fused with the FP64 defect of the pre-smoothing block:
+ *     rhs = cmask_child ? -res*w0_r + L[u] : 0,   lop = u,
+ *     D = rhs - L[u], C at relaxed points.
+ * E is 0 on entry (every block ends by clearing it). */
+__global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                   double w0_r)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
-   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const double *u = b.f[PGB_F_U], *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
+   const double *__restrict__ u = b.f[PGB_F_U];
+   const double *__restrict__ src = b.f[PGB_F_SRC];
+   const double *__restrict__ res = b.f[PGB_F_RES];
+   double *__restrict__ rhs = b.f[PGB_F_RHS];
+   double *__restrict__ lop = b.f[PGB_F_LOP];
+   float *__restrict__ wd = b.w32[W_D];
+   float *__restrict__ wc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   int kz = dim == 3 ? lv.tz : 1;
-   for (int kk = 0; kk < kz; kk++) {
-      int k = tl.k0 + kk;
-      if (k >= b.n[2]) break;
-      long p = i + sy * j + sz * k;
-      float d = 0.f, c = 0.f;
-      if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
-         double uc = u[p], s = src[p];
-         double t = (u[p + 1] - 2 * uc + u[p - 1]) * b.idx2[0] +
-                    (u[p + sy] - 2 * uc + u[p - sy]) * b.idx2[1];
-         if (dim == 3) t += (u[p + sz] - 2 * uc + u[p - sz]) * b.idx2[2];
-         double l, dc = 0;
-         if (pde == 1) {
-            double p2 = uc * uc, p4 = p2 * p2;
-            l = t + TWO_PI * s * (p4 * uc);
-            dc = TEN_PI * s * p4;
-         } else if (pde == 2) {
-            l = t - s * uc;
-            dc = -s;
-         } else
-            l = t - s;
-         d = (float)(rhs[p] - l);
-         c = (float)dc;
-      }
-      b.w32[W_D][p] = d;
-      b.w32[W_C][p] = c;
-      b.w32[W_E][p] = 0.f;
+   const int kz = dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + sy * j + sz * k;
+      const int cm = b.cmask_child[p];
+      const bool in = interior32(b, i, j, k, dim);
+      const bool rl = in && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p]);
+      const double uc = u[p];
+      double r = 0.0;
+      if (in && (cm || rl)) {
+         float c;
+         const double l = opjac(pde, lapm(b, u, p, sy, sz, dim), uc, src[p], c);
+         if (cm) r = fma(-res[p], w0_r, l);
+         if (rl) {
+            wd[p] = (float)(r - l);
+            wc[p] = c;
+         }
+      } else if (cm)
+         r = -res[p] * w0_r;
+      rhs[p] = r;
+      lop[p] = uc;
    }
 }
 
-/* one colour pass of GS on L'(u) e = d, FP32 (parity as num.f:220) */
+/* one colour pass of Gauss-Seidel on lap E + C E = D, FP32, straight from
+ * global memory (the level's E, D, C stay in L2 between passes); relax
+ * tiles are 64 points wide, a thread updates one point of the active colour
+ * per row (parity as num.f:220) */
 __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, int pass)
 {
    const pgb_tile tl = lv.rtiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
-   float *e = b.w32[W_E];
-   const float *dd = b.w32[W_D], *cc = b.w32[W_C];
+   float *__restrict__ e = b.w32[W_E];
+   const float *__restrict__ dd = b.w32[W_D];
+   const float *__restrict__ cc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
    const float j0 = (float)b.j0;
-   int j = tl.j0 + threadIdx.y;
-   int kz = dim == 3 ? lv.rtz : 1;
-   for (int kk = 0; kk < kz; kk++) {
-      int k = tl.k0 + kk;
-      int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
-      int i = tl.i0 + 2 * threadIdx.x + par;
+   const int j = tl.j0 + threadIdx.y;
+   const int kz = dim == 3 ? lv.rtz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      if (kk >= kz) continue;
+      const int k = tl.k0 + kk;
+      const int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
+      const int i = tl.i0 + 2 * threadIdx.x + par;
       if (!interior32(b, i, j, k, dim)) continue;
-      long p = i + sy * j + sz * k;
+      const long p = i + sy * j + sz * k;
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
-      float ec = e[p], c = cc[p];
+      const float ec = e[p], c = cc[p];
       float t = (e[p + 1] - 2.f * ec + e[p - 1]) * ix + (e[p + sy] - 2.f * ec + e[p - sy]) * iy;
       if (dim == 3) t += (e[p + sz] - 2.f * ec + e[p - sz]) * iz;
-      float r = t + c * ec - dd[p];
-      e[p] = ec - r / (j0 + c);
+      const float r = t + c * ec - dd[p];
+      e[p] = ec - __fdividef(r, j0 + c);
    }
 }
 
-/* u += e (FP64 update) */
-__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv)
+/* The same sweeps staged in shared memory: NS red-black sweeps in one launch.
+ * The CTA stages E of its 32 x 8 x tz tile plus a halo of 2*NS points in
+ * shared memory; colour pass q (0 .. 2*NS-1) updates the active colour on
+ * the tile grown by 2*NS-1-q points, so that every value the next pass reads
+ * is already final, and only the tile is written back. A point's new value
+ * depends only on old values of the other colour and D, C, so neighbouring
+ * CTAs compute identical values on their overlaps. Colour of pass q: the
+ * points with i+j(+k+1)+q even (num.f:220 parity, 0-based indices). NS > 1
+ * is only used on levels with no sync between sweeps. */
+template <int NS>
+__global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv)
+{
+   constexpr int H = 2 * NS;
+   constexpr int SX = PGB_TX + 2 * H, SY = PGB_TY + 2 * H, SZ = PGB_TZ + 2 * H;
+   __shared__ float se[SZ * SY * SX];
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const int tz = dim == 3 ? lv.tz : 1, hz = dim == 3 ? H : 0, nzl = tz + 2 * hz;
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   float *e = b.w32[W_E];
+   const float *dd = b.w32[W_D], *cc = b.w32[W_C];
+   const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
+   const float j0 = (float)b.j0;
+   const bool allbdy = b.flags & PGB_BOX_BDY_INTERIOR;
+   const int t = threadIdx.x + threadIdx.y * PGB_TX;
+   const int gi0 = tl.i0 - H, gj0 = tl.j0 - H, gk0 = tl.k0 - hz;
+   for (int q = t; q < SX * SY * nzl; q += NT) {
+      const int x = q % SX, y = (q / SX) % SY, z = q / (SX * SY);
+      const int gi = gi0 + x, gj = gj0 + y, gk = gk0 + z;
+      float v = 0.f;
+      if (gi >= 0 && gi < b.n[0] && gj >= 0 && gj < b.n[1] && gk >= 0 && gk < b.n[2])
+         v = e[gi + sy * gj + sz * gk];
+      se[x + SX * (y + SY * z)] = v;
+   }
+   __syncthreads();
+#pragma unroll
+   for (int pass = 0; pass < 2 * NS; pass++) {
+      const int g = H - 1 - pass;                    /* growth of this pass's region */
+      const int gz = dim == 3 ? g : 0;
+      const int rx = PGB_TX + 2 * g, ry = PGB_TY + 2 * g, rz = tz + 2 * gz;
+      const int hx = (rx + 1) / 2;                   /* slots per row: every other point */
+      for (int q = t; q < hx * ry * rz; q += NT) {
+         const int xs = q % hx, yy = (q / hx) % ry, zz = q / (hx * ry);
+         const int y = H - g + yy, z = hz - gz + zz;
+         const int gj = gj0 + y, gk = gk0 + z;
+         const int xstart = H - g;
+         /* first x of the row with the active colour */
+         const int par = ((gi0 + xstart + gj + (dim == 3 ? gk + 1 : 0) + pass) & 1);
+         const int x = xstart + par + 2 * xs;
+         if (x >= xstart + rx) continue;
+         const int gi = gi0 + x;
+         if (!interior32(b, gi, gj, gk, dim)) continue;
+         const long p = gi + sy * gj + sz * gk;
+         if (!allbdy && !b.cmask_bdy[p]) continue;
+         const int sp = x + SX * (y + SY * z);
+         const float ec = se[sp], c = cc[p];
+         float tt = (se[sp + 1] - 2.f * ec + se[sp - 1]) * ix + (se[sp + SX] - 2.f * ec + se[sp - SX]) * iy;
+         if (dim == 3) tt += (se[sp + SX * SY] - 2.f * ec + se[sp - SX * SY]) * iz;
+         const float r = tt + c * ec - dd[p];
+         se[sp] = ec - __fdividef(r, j0 + c);
+      }
+      __syncthreads();
+   }
+   for (int q = t; q < PGB_TX * PGB_TY * tz; q += NT) {
+      const int x = q % PGB_TX, y = (q / PGB_TX) % PGB_TY, z = q / (PGB_TX * PGB_TY);
+      const int gi = tl.i0 + x, gj = tl.j0 + y, gk = tl.k0 + z;
+      if (gi < b.n[0] && gj < b.n[1] && gk < b.n[2])
+         e[gi + sy * gj + sz * gk] = se[(x + H) + SX * ((y + H) + SY * (z + hz))];
+   }
+}
+
+/* End of a smoothing block: u += E (FP64) and E = 0. After an interpolated
+ * coarse-grid correction (post = 1) the points the smoother does not relax
+ * take the FP64 correction the interpolation left in res, plus whatever a
+ * sync of E brought in: u += res + (E - RN32(res)). */
+__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
-   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   int kz = lv.dim == 3 ? lv.tz : 1;
-   for (int kk = 0; kk < kz; kk++) {
-      int k = tl.k0 + kk;
-      if (k >= b.n[2]) break;
-      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
-      b.f[PGB_F_U][p] += (double)b.w32[W_E][p];
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+   double *__restrict__ u = b.f[PGB_F_U];
+   float *__restrict__ e = b.w32[W_E];
+   const double *__restrict__ res = b.f[PGB_F_RES];
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      double corr = (double)e[p];
+      if (post && !relaxed32(b, i, j, k, p, lv.dim)) {
+         const double r = res[p];
+         corr += r - (double)(float)r;
+      }
+      u[p] += corr;
+      e[p] = 0.f;
+   }
+}
+
+/* zero the four FP32 arrays (pgb_prepare) */
+__global__ void __launch_bounds__(NT) k_zero32(const pgb_dbox *boxes, pgb_dlevel lv)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      for (int f = 0; f < 4; f++) b.w32[f][p] = 0.f;
    }
 }
 
@@ -143,31 +313,29 @@ __device__ __forceinline__ long lin32(const pgb_dbox &b, int i1, int j1, int k1)
    return (i1 - 1) + (long)b.n[0] * ((j1 - 1) + (long)b.n[1] * (k1 - 1));
 }
 
-/* FP32 copy of the correction along a sync plan (PAMR_sync of e) */
+/* FP32 copy of the correction along a sync plan (PAMR_sync of E) */
 __global__ void k_copy32(const pgb_dbox *boxes, const pgb_copy_op *ops)
 {
-   const pgb_copy_op o = ops[blockIdx.y];
-   long npts = (long)o.ni * o.nj * o.nk;
+   const pgb_copy_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
-        q += (long)gridDim.x * blockDim.x) {
-      int a = (int)(q % o.ni), bb = (int)((q / o.ni) % o.nj), c = (int)(q / ((long)o.ni * o.nj));
+   OP_PLANES(o.ni, o.nj, o.nk, {
       d.w32[W_E][lin32(d, o.i2 + a, o.j2 + bb, o.k2 + c)] =
          s.w32[W_E][lin32(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
-   }
+   })
 }
 
-/* window stencil of dminterp3d in FP32 (linear; cubic with one-sided ends) */
+/* window stencil of dminterp3d (src/m_util_r8.f:65-144) in FP32: linear, or
+ * cubic with one-sided ends; n = 1 marks a copied anchor */
 __device__ __forceinline__ int stencil32(int t, int irho, int nanch, int ord, int *a, float *cf)
 {
-   int m = t / irho, j = t - m * irho;
+   const int m = irho == 2 ? t >> 1 : t / irho, j = t - m * irho;
    if (j == 0) {
       a[0] = m;
       return 1;
    }
    if (ord == 2 || nanch < 4) {
-      float sg = (float)j / irho;
+      const float sg = (irho == 2 ? (float)j * 0.5f : (float)j / irho);
       cf[0] = 1.f - sg;
       cf[1] = sg;
       a[0] = m;
@@ -177,13 +345,13 @@ __device__ __forceinline__ int stencil32(int t, int irho, int nanch, int ord, in
    float sg;
    int base;
    if (m == 0) {
-      sg = (float)j / irho;
+      sg = (irho == 2 ? (float)j * 0.5f : (float)j / irho);
       base = 0;
    } else if (m == nanch - 2) {
-      sg = 2.f + (float)j / irho;
+      sg = 2.f + (irho == 2 ? (float)j * 0.5f : (float)j / irho);
       base = nanch - 4;
    } else {
-      sg = 1.f + (float)j / irho;
+      sg = 1.f + (irho == 2 ? (float)j * 0.5f : (float)j / irho);
       base = m - 1;
    }
    cf[0] = -(1.f / 6.f) * (sg - 1.f) * (sg - 2.f) * (sg - 3.f);
@@ -202,16 +370,16 @@ __device__ __forceinline__ float wsum32(int n, const float *c, const float *v)
    return r;
 }
 
-/* FP64 weights of the same window stencil (used on box-boundary points) */
+/* the same window stencil with FP64 weights */
 __device__ __forceinline__ int stencil64m(int t, int irho, int nanch, int ord, int *a, double *cf)
 {
-   int m = t / irho, j = t - m * irho;
+   const int m = irho == 2 ? t >> 1 : t / irho, j = t - m * irho;
    if (j == 0) {
       a[0] = m;
       return 1;
    }
    if (ord == 2 || nanch < 4) {
-      double sg = (double)j / irho;
+      const double sg = (irho == 2 ? (double)j * 0.5 : (double)j / irho);
       cf[0] = 1.0 - sg;
       cf[1] = sg;
       a[0] = m;
@@ -221,19 +389,19 @@ __device__ __forceinline__ int stencil64m(int t, int irho, int nanch, int ord, i
    double sg;
    int base;
    if (m == 0) {
-      sg = (double)j / irho;
+      sg = (irho == 2 ? (double)j * 0.5 : (double)j / irho);
       base = 0;
    } else if (m == nanch - 2) {
-      sg = 2.0 + (double)j / irho;
+      sg = 2.0 + (irho == 2 ? (double)j * 0.5 : (double)j / irho);
       base = nanch - 4;
    } else {
-      sg = 1.0 + (double)j / irho;
+      sg = 1.0 + (irho == 2 ? (double)j * 0.5 : (double)j / irho);
       base = m - 1;
    }
-   cf[0] = -0.16666666666666667 * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
+   cf[0] = -(1.0 / 6.0) * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
    cf[1] = 0.5 * sg * (sg - 2.0) * (sg - 3.0);
    cf[2] = -0.5 * sg * (sg - 1.0) * (sg - 3.0);
-   cf[3] = 0.16666666666666667 * sg * (sg - 1.0) * (sg - 2.0);
+   cf[3] = (1.0 / 6.0) * sg * (sg - 1.0) * (sg - 2.0);
    for (int q = 0; q < 4; q++) a[q] = base + q;
    return 4;
 }
@@ -246,150 +414,133 @@ __device__ __forceinline__ double wsum64m(int n, const double *c, const double *
    return r;
 }
 
-/* coarse-grid correction, interpolation half: fine res = interpolation of
- * coarse res (amrd/mg.c:343), assigned in plan order like the FP64 path.
- * Interior fine points interpolate in FP32 -- the next FP64 defect sees and
- * corrects their rounding -- while points on a fine box's boundary, which no
- * defect covers (their values only change through these corrections),
- * interpolate in FP64. */
+/* Coarse half of the coarse-grid correction (amrd/mg.c:332-341) on the tiles
+ * the interpolation reads: res = (f - lop)/w0_i in FP64, X = RN32(res). */
+__global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0)
+{
+   const pgb_tile tl = lv.ctiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+      const double r = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) * inv_w0;
+      b.f[PGB_F_RES][p] = r;
+      b.w32[W_X][p] = (float)r;
+   }
+}
+
+/* FP64 interpolation of the coarse res at window point (a, bb, c) of op o
+ * (dminterp3d's line order: i, then j, then k) */
+__device__ double interp_point64(const pgb_interp_op &o, const pgb_dbox &s, int a, int bb, int c, int dim)
+{
+   const double *__restrict__ u = s.f[PGB_F_RES];
+   int ax[4], ay[4], az[4];
+   double cx[4], cy[4], cz[4], kv[4];
+   const int nx = stencil64m(o.i2b - 1 + a, o.irho, o.nii, o.ord, ax, cx);
+   const int ny = stencil64m(o.j2b - 1 + bb, o.irho, o.nji, o.ord, ay, cy);
+   const int nz = dim == 3 ? stencil64m(o.k2b - 1 + c, o.irho, o.nki, o.ord, az, cz) : 1;
+   if (dim != 3) az[0] = 0;
+   for (int r = 0; r < nz; r++) {
+      double jv[4];
+      for (int qq = 0; qq < ny; qq++) {
+         double iv[4];
+         for (int pp = 0; pp < nx; pp++) iv[pp] = u[lin32(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
+         jv[qq] = wsum64m(nx, cx, iv);
+      }
+      kv[r] = wsum64m(ny, cy, jv);
+   }
+   return wsum64m(nz, cz, kv);
+}
+
+/* Fine half (amrd/mg.c:343-354), PAMR_interp in plan order (ops of one
+ * batch write disjoint points, later batches overwrite earlier ones like the
+ * reference's sequential transfers). Relaxed points: E = interpolation of X
+ * in FP32, the start of the post-smoothing block. Other points: the FP64
+ * interpolation of the coarse res into res (k_update adds it) and its FP32
+ * value into E, which the smoother reads as a neighbour. FP64 issues at a
+ * small fraction of the FP32 rate, so FP64 points are kept in dense warps:
+ * on boxes whose interior is all relaxed this kernel does the face rows in
+ * FP64 and leaves the two x-ends of the other rows to k_interp_xedge. */
 __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
 {
-   const pgb_interp_op o = ops[blockIdx.y];
-   long npts = (long)o.nib * o.njb * o.nkb;
+   const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
-   const double *u = s.f[PGB_F_RES];
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
-        q += (long)gridDim.x * blockDim.x) {
-      int a = (int)(q % o.nib), bb = (int)((q / o.nib) % o.njb), c = (int)(q / ((long)o.nib * o.njb));
-      int fi = o.i2 + a, fj = o.j2 + bb, fk = o.k2 + c;
-      bool edge = fi == 1 || fi == d.n[0] || fj == 1 || fj == d.n[1] ||
-                  (dim == 3 && (fk == 1 || fk == d.n[2]));
-      int tx = o.i2b - 1 + a, ty = o.j2b - 1 + bb, tz = o.k2b - 1 + c;
-      int ax[4], ay[4], az[4];
-      double v;
-      if (edge) {
-         double cx[4], cy[4], cz[4], kv[4];
-         int nx = stencil64m(tx, o.irho, o.nii, o.ord, ax, cx);
-         int ny = stencil64m(ty, o.irho, o.nji, o.ord, ay, cy);
-         int nz = dim == 3 ? stencil64m(tz, o.irho, o.nki, o.ord, az, cz) : 1;
-         if (dim != 3) az[0] = 0;
-         for (int r = 0; r < nz; r++) {
-            double jv[4];
-            for (int qq = 0; qq < ny; qq++) {
-               double iv[4];
-               for (int pp = 0; pp < nx; pp++)
-                  iv[pp] = u[lin32(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
-               jv[qq] = wsum64m(nx, cx, iv);
-            }
-            kv[r] = wsum64m(ny, cy, jv);
+   const bool allrel = d.flags & PGB_BOX_BDY_INTERIOR;
+   const float *__restrict__ x = s.w32[W_X];
+   for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
+      const int bb = row % o.njb, c = row / o.njb;
+      const int fj = o.j2 + bb, fk = o.k2 + c;
+      const bool face = fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]));
+      int ay[4], az[4];
+      float cy[4], cz[4];
+      const int ny = stencil32(o.j2b - 1 + bb, o.irho, o.nji, o.ord, ay, cy);
+      const int nz = dim == 3 ? stencil32(o.k2b - 1 + c, o.irho, o.nki, o.ord, az, cz) : 1;
+      if (dim != 3) az[0] = 0;
+      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+         const int fi = o.i2 + a;
+         const long pd = lin32(d, fi, fj, fk);
+         bool fp64;
+         if (allrel) {
+            if (!face && (fi == 1 || fi == d.n[0])) continue;   /* k_interp_xedge */
+            fp64 = face;
+         } else
+            fp64 = !relaxed32(d, fi - 1, fj - 1, fk - 1, pd, dim);
+         if (fp64) {
+            const double v = interp_point64(o, s, a, bb, c, dim);
+            d.f[PGB_F_RES][pd] = v;
+            d.w32[W_E][pd] = (float)v;
+            continue;
          }
-         v = wsum64m(nz, cz, kv);
-      } else {
-         float cx[4], cy[4], cz[4], kv[4];
-         int nx = stencil32(tx, o.irho, o.nii, o.ord, ax, cx);
-         int ny = stencil32(ty, o.irho, o.nji, o.ord, ay, cy);
-         int nz = dim == 3 ? stencil32(tz, o.irho, o.nki, o.ord, az, cz) : 1;
-         if (dim != 3) az[0] = 0;
+         int ax[4];
+         float cx[4], kv[4];
+         const int nx = stencil32(o.i2b - 1 + a, o.irho, o.nii, o.ord, ax, cx);
          for (int r = 0; r < nz; r++) {
             float jv[4];
             for (int qq = 0; qq < ny; qq++) {
                float iv[4];
-               for (int pp = 0; pp < nx; pp++)
-                  iv[pp] = (float)u[lin32(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
+               for (int pp = 0; pp < nx; pp++) iv[pp] = x[lin32(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
                jv[qq] = wsum32(nx, cx, iv);
             }
             kv[r] = wsum32(ny, cy, jv);
          }
-         v = (double)wsum32(nz, cz, kv);
-      }
-      d.f[PGB_F_RES][lin32(d, fi, fj, fk)] = v;
-   }
-}
-
-/* ------------------------------------------------------------ launchers -- */
-extern "C" int pgb_k_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, void *stream)
-{
-   if (!lv.ntiles) return 0;
-   k_defect<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde);
-   return check32("defect");
-}
-
-extern "C" int pgb_k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
-{
-   if (!lv.nrtiles) return 0;
-   k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 0);
-   if (check32("relax32")) return 1;
-   k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 1);
-   return check32("relax32");
-}
-
-extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
-{
-   if (!lv.ntiles) return 0;
-   k_update<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
-   return check32("update");
-}
-
-extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream)
-{
-   for (int bt = 0; bt < p->nbatch; bt++) {
-      int n = p->batch_start[bt + 1] - p->batch_start[bt];
-      int gx = (p->batch_maxpts[bt] + 255) / 256;
-      if (gx > 512) gx = 512;
-      if (n <= 0 || gx <= 0) continue;
-      for (int c0 = 0; c0 < n; c0 += 65535) {
-         k_copy32<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
-            boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt] + c0);
-         if (check32("copy32")) return 1;
+         d.w32[W_E][pd] = wsum32(nz, cz, kv);
       }
    }
-   return 0;
 }
 
-extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream)
+/* the x-ends (fi = 1, n) of the non-face rows of ops into boxes whose
+ * interior is all relaxed, in FP64, one point per thread */
+__global__ void k_interp_xedge(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
 {
-   for (int bt = 0; bt < p->nbatch; bt++) {
-      int n = p->batch_start[bt + 1] - p->batch_start[bt];
-      int gx = (p->batch_maxpts[bt] + 255) / 256;
-      if (gx > 2048) gx = 2048;
-      if (n <= 0 || gx <= 0) continue;
-      for (int c0 = 0; c0 < n; c0 += 65535) {
-         k_interp_mixed<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
-            boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt] + c0, dim);
-         if (check32("interp_mixed")) return 1;
-      }
+   const pgb_interp_op o = ops[blockIdx.z];
+   const pgb_dbox &s = boxes[o.src_box];
+   const pgb_dbox &d = boxes[o.dst_box];
+   if (!(d.flags & PGB_BOX_BDY_INTERIOR)) return;
+   const int rows = o.njb * o.nkb;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * rows; q += gridDim.x * blockDim.x) {
+      const int row = q >> 1;
+      const int a = (q & 1) ? d.n[0] - o.i2 : 1 - o.i2;
+      if (a < 0 || a >= o.nib) continue;
+      const int bb = row % o.njb, c = row / o.njb;
+      const int fj = o.j2 + bb, fk = o.k2 + c;
+      if (fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]))) continue;
+      const long pd = lin32(d, o.i2 + a, fj, fk);
+      const double v = interp_point64(o, s, a, bb, c, dim);
+      d.f[PGB_F_RES][pd] = v;
+      d.w32[W_E][pd] = (float)v;
    }
-   return 0;
-}
-
-/* ---------------------------------------- FP64 passes of the mixed form -- */
-/* The mixed form needs FP64 accuracy in its residuals, not the reference's
- * bit pattern: these variants multiply by 1/dx^2 and let the compiler fuse
- * multiply-adds, which roughly halves their FP64 instruction count. */
-__device__ __forceinline__ double lapf(const pgb_dbox &b, const double *u, long p, int dim)
-{
-   long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   double c = u[p];
-   double t = (u[p + 1] - 2 * c + u[p - 1]) * b.idx2[0] + (u[p + sy] - 2 * c + u[p - sy]) * b.idx2[1];
-   if (dim == 3) t += (u[p + sz] - 2 * c + u[p - sz]) * b.idx2[2];
-   return t;
-}
-
-__device__ __forceinline__ double opf(int pde, double t, double u, double s)
-{
-   if (pde == 1) {
-      double p2 = u * u;
-      return t + TWO_PI * s * (p2 * p2 * u);
-   }
-   if (pde == 2) return t - s * u;
-   return t - s;
 }
 
 __device__ double block_sum32(double v, double *sm)
 {
-   int t = threadIdx.x + threadIdx.y * blockDim.x;
-   int nt = blockDim.x * blockDim.y;
+   const int t = threadIdx.x + threadIdx.y * blockDim.x;
+   const int nt = blockDim.x * blockDim.y;
    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
    if ((t & 31) == 0) sm[t >> 5] = v;
    __syncthreads();
@@ -401,6 +552,10 @@ __device__ double block_sum32(double v, double *sm)
    return v;
 }
 
+/* app_MG_residual (num.f:128-175 pattern) in FP64: res = L[u] - rhs at the
+ * relaxed points, D = -res and C for the next smoothing block of this
+ * level, and call_rr_app's norm (per-box RMS, max over boxes) reduced by the
+ * last CTA to finish. */
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
                                                       pgb_trace *trace)
@@ -410,19 +565,28 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    const pgb_tile tl = lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
-   const double *u = b.f[PGB_F_U], *rhs = b.f[PGB_F_RHS], *src = b.f[PGB_F_SRC];
-   double *res = b.f[PGB_F_RES];
+   const double *__restrict__ u = b.f[PGB_F_U];
+   const double *__restrict__ rhs = b.f[PGB_F_RHS];
+   const double *__restrict__ src = b.f[PGB_F_SRC];
+   double *__restrict__ res = b.f[PGB_F_RES];
+   float *__restrict__ wd = b.w32[W_D];
+   float *__restrict__ wc = b.w32[W_C];
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    double acc = 0;
-   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
-   int kz = dim == 3 ? lv.tz : 1;
-   for (int kk = 0; kk < kz; kk++) {
-      int k = tl.k0 + kk;
-      if (!interior32(b, i, j, k, dim)) continue;
-      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int kz = dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || !interior32(b, i, j, k, dim)) continue;
+      const long p = i + sy * j + sz * k;
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
-      double r = opf(pde, lapf(b, u, p, dim), u[p], src[p]) - rhs[p];
+      float c;
+      const double r = opjac(pde, lapm(b, u, p, sy, sz, dim), u[p], src[p], c) - rhs[p];
       res[p] = r;
-      acc += r * r;
+      wd[p] = (float)(-r);
+      wc[p] = c;
+      acc = fma(r, r, acc);
    }
    acc = block_sum32(acc, sm);
    if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
@@ -433,18 +597,18 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    __syncthreads();
    if (!last) return;
    /* call_rr_app: per-box RMS, max over boxes */
-   int t = threadIdx.x + threadIdx.y * blockDim.x;
+   const int t = threadIdx.x + threadIdx.y * blockDim.x;
    double lres = 0;
    for (int bx = 0; bx < lv.nbox; bx++) {
       double v = 0;
-      for (int s = lv.tile_start[bx] + t; s < lv.tile_start[bx + 1]; s += NT) v += __ldcg(&sc.partial[s]);
+      for (int q = lv.tile_start[bx] + t; q < lv.tile_start[bx + 1]; q += NT) v += __ldcg(&sc.partial[q]);
       v = block_sum32(v, sm);
       if (t == 0) {
-         double r = sqrt(v / boxes[lv.box[bx]].count);
+         const double r = sqrt(v / boxes[lv.box[bx]].count);
          if (bx == 0) lres = r;
          lres = (r > lres) ? r : lres;
          if (trace) {
-            int n = trace->n;
+            const int n = trace->n;
             if (n < trace->cap) {
                pgb_trace_rec rr = {1, lv.level, bx, 1, r};
                trace->rec[n] = rr;
@@ -460,26 +624,267 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    }
 }
 
-/* L_op + compute_MG_rhs (amrd/mg.c:271-314) for the mixed form */
+/* L_op + compute_MG_rhs (amrd/mg.c:271-314) on the cover tiles of the
+ * coarsest level, which the coarsest-grid loop smooths by itself */
 __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                      double w0_r)
 {
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_tile tl = lv.ctiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
-   int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
    const double *u = b.f[PGB_F_U];
-   int kz = lv.dim == 3 ? lv.tz : 1;
-   for (int kk = 0; kk < kz; kk++) {
-      int k = tl.k0 + kk;
-      if (k >= b.n[2]) break;
-      long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + sy * j + sz * k;
       double lopv = 0;
-      int cm = b.cmask_child[p];
-      if (cm && interior32(b, i, j, k, lv.dim)) lopv = opf(pde, lapf(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
-      b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
+      const int cm = b.cmask_child[p];
+      float c;
+      if (cm && interior32(b, i, j, k, lv.dim))
+         lopv = opjac(pde, lapm(b, u, p, sy, sz, lv.dim), u[p], b.f[PGB_F_SRC][p], c);
+      b.f[PGB_F_RHS][p] = cm ? fma(-b.f[PGB_F_RES][p], w0_r, lopv) : 0.0;
       b.f[PGB_F_LOP][p] = u[p];
    }
+}
+
+/* The coarsest-grid loop of the mixed form (amrd/mg.c:172-190: relax the
+ * coarsest grids, sync them, until the norm <= crtol x the first norm or
+ * MG_max_citer) with the whole coarsest level held in shared memory by one
+ * CTA. Each sweep is red-black successive over-relaxation with the factor
+ * omega the host picks for the grid size: the residual r = L[u] - rhs and
+ * the update u -= omega r / J are FP64, only the Jacobian J = dL/du steering
+ * the step is FP32, so the iteration's fixed point is the FP64 solution.
+ * The loop also stops once the norm has not improved for three sweeps (the
+ * FP64 rounding floor). */
+#define CM_MAXB 16
+#define CMT 1024
+__global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                        const pgb_copy_op *sync_ops, int nsync,
+                                                        pgb_coarsest_args a, pgb_trace *trace)
+{
+   extern __shared__ double dsm[];
+   __shared__ double sm[32];
+   __shared__ int cb[CM_MAXB], ncb_s;
+   __shared__ long coff[CM_MAXB + 1];
+   const int t = threadIdx.x, dim = lv.dim;
+   if (t == 0) {
+      int n = 0;
+      long o = 0;
+      for (int b = 0; b < lv.nbox && n < CM_MAXB; b++) {
+         const pgb_dbox &bx = boxes[lv.box[b]];
+         if (!(bx.flags & PGB_BOX_COARSEST)) continue;
+         cb[n] = b;
+         coff[n] = o;
+         o += (long)bx.n[0] * bx.n[1] * bx.n[2];
+         n++;
+      }
+      coff[n] = o;
+      ncb_s = n;
+   }
+   __syncthreads();
+   const int ncb = ncb_s;
+   const long tot = coff[ncb];
+   double *su = dsm, *srhs = dsm + tot, *ssrc = dsm + 2 * tot;
+   for (int c = 0; c < ncb; c++) {
+      const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+      const long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+      for (long q = t; q < n; q += CMT) {
+         su[coff[c] + q] = bx.f[PGB_F_U][q];
+         srhs[coff[c] + q] = bx.f[PGB_F_RHS][q];
+         ssrc[coff[c] + q] = bx.f[PGB_F_SRC][q];
+      }
+   }
+   __syncthreads();
+   const float omega = (float)a.omega;
+   double ctol = -1.0, res = 0.0, best = 0.0;
+   int iter = 0, stall = 0;
+   while (iter < a.max_citer) {
+      double lres = 0;
+      for (int c = 0; c < ncb; c++) {
+         const pgb_dbox bx = boxes[lv.box[cb[c]]];
+         double *u = su + coff[c];
+         const double *rhs = srhs + coff[c], *src = ssrc + coff[c];
+         const long sy = bx.n[0], sz = (long)bx.n[0] * bx.n[1];
+         const long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
+         const long hw = (ni + 1) / 2, nslot = hw * nj * nk;   /* one slot per point of a colour */
+         const float j0 = (float)bx.j0;
+         double acc = 0;
+         for (int pass = 0; pass < 2; pass++) {
+            for (long q = t; q < nslot; q += CMT) {
+               const int j = 1 + (int)((q / hw) % nj);
+               const int k = dim == 3 ? 1 + (int)(q / (hw * nj)) : 0;
+               const int off = dim == 3 ? ((j + k + pass) & 1) : ((j + 1 + pass) & 1);
+               const int i = 1 + 2 * (int)(q % hw) + off;
+               if (i > ni) continue;
+               const long p = i + sy * j + sz * k;
+               if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+               const double uc = u[p];
+               float cj;
+               const double r = opjac(pde, lapm(bx, u, p, sy, sz, dim), uc, src[p], cj) - rhs[p];
+               const float step = __fdividef(omega, j0 + cj);
+               u[p] = fma(-(double)step, r, uc);
+               acc = fma(r, r, acc);
+            }
+            __syncthreads();
+         }
+         acc = block_sum32(acc, sm);
+         if (t == 0) {
+            const double r = sqrt(acc / bx.count);
+            if (c == 0) lres = r;
+            lres = (r > lres) ? r : lres;
+            if (trace) {
+               const int n = trace->n;
+               if (n < trace->cap) {
+                  pgb_trace_rec rr = {0, lv.level, cb[c], 1, r};
+                  trace->rec[n] = rr;
+                  trace->n = n + 1;
+               } else
+                  trace->overflow = 1;
+            }
+         }
+      }
+      for (int o = 0; o < nsync; o++) {   /* PAMR_sync(L,0,MGH,1) over the coarsest grids */
+         const pgb_copy_op op = sync_ops[o];
+         int cs = -1, cd = -1;
+         for (int c = 0; c < ncb; c++) {
+            if (lv.box[cb[c]] == op.src_box) cs = c;
+            if (lv.box[cb[c]] == op.dst_box) cd = c;
+         }
+         if (cs < 0 || cd < 0) continue;
+         const pgb_dbox &bs = boxes[op.src_box];
+         const pgb_dbox &bd = boxes[op.dst_box];
+         const long np = (long)op.ni * op.nj * op.nk;
+         for (long q = t; q < np; q += CMT) {
+            const int aa = (int)(q % op.ni), bb = (int)((q / op.ni) % op.nj),
+                      cc = (int)(q / ((long)op.ni * op.nj));
+            su[coff[cd] + lin32(bd, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
+               su[coff[cs] + lin32(bs, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
+         }
+         __syncthreads();
+      }
+      if (t == 0) sm[0] = lres;
+      __syncthreads();
+      res = sm[0];
+      __syncthreads();
+      iter++;
+      if (ctol < 0) {
+         ctol = res * a.crtol;
+         best = res;
+      } else if (res < best) {
+         best = res;
+         stall = 0;
+      } else if (++stall >= 3)
+         break;
+      if (res <= ctol) break;
+   }
+   for (int c = 0; c < ncb; c++) {
+      const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+      const long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
+      for (long q = t; q < n; q += CMT) bx.f[PGB_F_U][q] = su[coff[c] + q];
+   }
+   if (t == 0) {
+      *a.res_out = res;
+      if (a.iters_out) *a.iters_out += iter;
+   }
+}
+
+/* ------------------------------------------------------------ launchers -- */
+extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
+                                void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_fas_defect<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   return check32("fas_defect");
+}
+
+/* nsweep FP32 sweeps of level L, fuse sweeps per launch (1 or 2) */
+/* nsweep FP32 sweeps of level L: fuse = 0 two global-memory colour passes
+ * per sweep; 1 or 2 = sweeps per launch of the shared-memory kernel */
+extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream)
+{
+   int done = 0;
+   if (!lv.ntiles) return 0;
+   while (done < nsweep) {
+      if (fuse <= 0) {
+         k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 0);
+         if (check32("relax32")) return 1;
+         k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 1);
+         done += 1;
+      } else if (fuse >= 2 && nsweep - done >= 2) {
+         k_sweep32<2><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+         done += 2;
+      } else {
+         k_sweep32<1><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+         done += 1;
+      }
+      if (check32("sweep32")) return 1;
+   }
+   return 0;
+}
+
+extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_update<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post);
+   return check32("update");
+}
+
+extern "C" int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_zero32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   return check32("zero32");
+}
+
+extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream)
+{
+   const pgb_copy_op *h = (const pgb_copy_op *)p->h_ops, *d = (const pgb_copy_op *)p->d_ops;
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      for (int c0 = 0; c0 < n; c0 += 65535) {
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         dim3 g;
+         plane_grid(h + p->batch_start[bt] + c0, m, g);
+         k_copy32<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0);
+         if (check32("copy32")) return 1;
+      }
+   }
+   return 0;
+}
+
+extern "C" int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream)
+{
+   if (!lv.nctiles) return 0;
+   k_cgc_mixed<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, inv_w0);
+   return check32("cgc_mixed");
+}
+
+extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream)
+{
+   const pgb_interp_op *h = (const pgb_interp_op *)p->h_ops, *d = (const pgb_interp_op *)p->d_ops;
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      for (int c0 = 0; c0 < n; c0 += 65535) {
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         const pgb_interp_op *hb = h + p->batch_start[bt] + c0;
+         dim3 g;
+         long mr = 1;
+         row_grid(hb, m, g);
+         k_interp_mixed<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+         if (check32("interp_mixed")) return 1;
+         for (int i = 0; i < m; i++)
+            if ((long)hb[i].njb * hb[i].nkb > mr) mr = (long)hb[i].njb * hb[i].nkb;
+         long gx = (2 * mr + 127) / 128;
+         k_interp_xedge<<<dim3((unsigned)(gx > 65535 ? 65535 : gx), 1, (unsigned)m), 128, 0,
+                          (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+         if (check32("interp_xedge")) return 1;
+      }
+   }
+   return 0;
 }
 
 extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
@@ -494,7 +899,23 @@ extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde
 extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
                                   void *stream)
 {
-   if (!lv.ntiles) return 0;
-   k_lop_rhs_fast<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   if (!lv.nctiles) return 0;
+   k_lop_rhs_fast<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
    return check32("lop_rhs_fast");
+}
+
+/* returns 1 (nothing launched) when the coarsest level does not fit on chip */
+extern "C" int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
+                                    pgb_coarsest_args a, pgb_trace *trace, void *stream)
+{
+   const size_t smem = (size_t)a.smem_points * 3 * sizeof(double);
+   static int attr_set = 0;
+   if (a.smem_points <= 0 || a.ncoarse > CM_MAXB || smem > 200 * 1024) return 1;
+   if (!attr_set) {
+      cudaFuncSetAttribute(k_coarsest_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_set = 1;
+   }
+   k_coarsest_mixed<<<1, CMT, smem, (cudaStream_t)stream>>>(
+      boxes, lv, pde, (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
+   return check32("coarsest_mixed") ? -1 : 0;
 }

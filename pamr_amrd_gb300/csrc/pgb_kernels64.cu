@@ -19,6 +19,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include "pgb_dev.h"
+#include "pgb_opgrid.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -57,9 +58,27 @@ extern "C" int pgb_dev_sync(void *stream)
 #define TWO_PI 6.283185307179586
 #define TEN_PI 31.41592653589793
 
+/* RN(x/d) for a divisor whose correctly rounded reciprocal r = RN(1/d) is
+ * known. q0 = RN(x*r) is within two ulps of x/d; one FMA correction step
+ * q1 = RN(q0 + RN(x - q0*d)*r) leaves it within one ulp (faithful); with a
+ * faithful quotient and r = RN(1/d), Markstein's theorem (P. Markstein, IBM
+ * J. Res. Dev. 34, 1990; Muller et al., Handbook of Floating-Point
+ * Arithmetic, 2018, sec. 4.7) makes the second step RN(x/d) exactly, barring
+ * overflow and underflow. Five FP64 operations instead of a full division;
+ * the GPU tests compare every result path with IEEE division. */
+__device__ __forceinline__ double div_known(double x, double d, double r)
+{
+   double q = __dmul_rn(x, r);
+   double e = __fma_rn(-q, d, x);
+   q = __fma_rn(e, r, q);
+   e = __fma_rn(-q, d, x);
+   return __fma_rn(e, r, q);
+}
+
+/* one term of num.f:113-115: num/dx^2 (a product when 1/dx^2 is exact) */
 __device__ __forceinline__ double dterm(const pgb_dbox &b, double num, int d)
 {
-   return (b.flags & PGB_BOX_POW2DX) ? num * b.idx2[d] : num / b.dx2[d];
+   return (b.flags & PGB_BOX_POW2DX) ? num * b.idx2[d] : div_known(num, b.dx2[d], b.idx2[d]);
 }
 
 /* lap(u) at linear index p, num.f:113-115 order */
@@ -255,15 +274,16 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
 }
 
 /* ------------------------------------------------ pointwise level passes -- */
-#define FOR_TILE_POINTS(body)                                                        \
-   const pgb_tile tl = lv.tiles[blockIdx.x];                                         \
+#define FOR_TILE_POINTS(body) FOR_TILE_POINTS_IN(lv.tiles, body)
+#define FOR_TILE_POINTS_IN(list, body)                                               \
+   const pgb_tile tl = (list)[blockIdx.x];                                           \
    const pgb_dbox b = boxes[tl.box];                                                 \
    int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;                              \
    int kz = lv.dim == 3 ? lv.tz : 1;                                                \
    if (i < b.n[0] && j < b.n[1])                                                     \
-      for (int kk = 0; kk < kz; kk++) {                                              \
+      _Pragma("unroll") for (int kk = 0; kk < PGB_TZ; kk++) {                        \
          int k = tl.k0 + kk;                                                         \
-         if (k >= b.n[2]) break;                                                     \
+         if (kk >= kz || k >= b.n[2]) continue;                                      \
          long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);                         \
          body                                                                        \
       }
@@ -278,11 +298,12 @@ __global__ void __launch_bounds__(NT) k_clear(const pgb_dbox *boxes, pgb_dlevel 
 
 /* app_L_op (num.f:85-123, lop = L[u] at interior cmask-child points) fused
  * with compute_MG_rhs (amrd/mg.c:271-314): rhs = cmask ? -res*w0_r + lop : 0,
- * then lop = u. lop was cleared by clear_MG_vars earlier in the same step. */
+ * then lop = u, on the level's cover tiles (every child-covered point lies in
+ * one; elsewhere rhs keeps the 0 pgb_prepare wrote and lop is never read). */
 __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                 double w0_r)
 {
-   FOR_TILE_POINTS({
+   FOR_TILE_POINTS_IN(lv.ctiles, {
       const double *u = b.f[PGB_F_U];
       double lopv = 0;
       int cm = b.cmask_child[p];
@@ -293,11 +314,12 @@ __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dleve
    })
 }
 
-/* compute_cgc first half (amrd/mg.c:332-341): res = (f - lop)/w0_i */
+/* compute_cgc first half (amrd/mg.c:332-341): res = (f - lop)/w0_i, on the
+ * tiles the interpolation to the finer level reads */
 __global__ void __launch_bounds__(NT) k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv,
                                                    double w0_i)
 {
-   FOR_TILE_POINTS({ b.f[PGB_F_RES][p] = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) / w0_i; })
+   FOR_TILE_POINTS_IN(lv.ctiles, { b.f[PGB_F_RES][p] = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) / w0_i; })
 }
 
 /* compute_cgc second half (amrd/mg.c:345-354): f += res */
@@ -316,15 +338,15 @@ extern "C" int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask, void 
 extern "C" int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
                              void *stream)
 {
-   if (!lv.ntiles) return 0;
-   k_lop_rhs<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   if (!lv.nctiles) return 0;
+   k_lop_rhs<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
    LAUNCHED(1);
    return check("lop_rhs");
 }
 extern "C" int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream)
 {
-   if (!lv.ntiles) return 0;
-   k_cgc_coarse<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, w0_i);
+   if (!lv.nctiles) return 0;
+   k_cgc_coarse<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, w0_i);
    LAUNCHED(1);
    return check("cgc_coarse");
 }
@@ -355,17 +377,20 @@ __device__ __forceinline__ long lin(const pgb_dbox &b, int i1, int j1, int k1)
 /* dmcopy3d with unit strides (src/m_util_r8.f:20-50) */
 __global__ void k_copy(const pgb_dbox *boxes, const pgb_copy_op *ops, int field)
 {
-   const pgb_copy_op o = ops[blockIdx.y];
-   long npts = (long)o.ni * o.nj * o.nk;
+   const pgb_copy_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
-        q += (long)gridDim.x * blockDim.x) {
-      int a, bb, c;
-      unflat(q, o.ni, o.nj, a, bb, c);
+   OP_PLANES(o.ni, o.nj, o.nk, {
       d.f[field][lin(d, o.i2 + a, o.j2 + bb, o.k2 + c)] = s.f[field][lin(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
-   }
+   })
 }
+
+/* The weights of the half- and full-weighting stencils are powers of two,
+ * so w*u is exact and RN(acc + w*u) == fma(w, u, acc): the FMA forms below
+ * give the Fortran sums bit for bit (same left-to-right order) with fewer
+ * FP64 instructions. Divisions by 4, 8, 16 and 64 are exact products; the
+ * division by 12 uses div_known. */
+#define ACC(acc, w, v) __fma_rn((double)(w), (v), (acc))
 
 /* dmhwr3d (src/m_util_r8.f:649-723), do_ex = 0, at fine point (i0,j0,k0) */
 __device__ double hwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
@@ -376,73 +401,83 @@ __device__ double hwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0
    long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
    if (i0 > 1 && i0 <= nx1 - 1) {
       w = w + 4;
-      sum = sum + u[p - 1] + 2 * u[p] + u[p + 1];
+      sum = ACC(sum + u[p - 1], 2, u[p]) + u[p + 1];
    }
    if (j0 > 1 && j0 <= ny1 - 1) {
       w = w + 4;
-      sum = sum + u[p - sy] + 2 * u[p] + u[p + sy];
+      sum = ACC(sum + u[p - sy], 2, u[p]) + u[p + sy];
    }
    if (k0 > 1 && k0 <= nz1 - 1) {
       w = w + 4;
-      sum = sum + u[p - sz] + 2 * u[p] + u[p + sz];
+      sum = ACC(sum + u[p - sz], 2, u[p]) + u[p + sz];
    }
-   if (w > 0) return sum / w;
+   if (w == 12) return div_known(sum, 12.0, 1.0 / 12.0);
+   if (w > 0) return sum * (w == 4 ? 0.25 : 0.125);
    return u[p];
 }
 
-/* dmfwr3d (src/m_util_r8.f:733-830), do_ex = 0, at fine point (i0,j0,k0) */
+/* dmfwr3d (src/m_util_r8.f:733-830), do_ex = 0, at fine point (i0,j0,k0):
+ * the 27-, 9- or 3-point sum in the Fortran order (outer offset first) */
 __device__ double fwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
 {
    const long sy = nx1, sz = (long)nx1 * ny1;
    const long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
-#define U(di, dj, dk) u[p + (di) + (dj) * sy + (dk) * sz]
    bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
-   if (ii && jj && kk)
-      return (U(-1, -1, -1) + 2 * U(0, -1, -1) + U(1, -1, -1) +
-              2 * U(-1, 0, -1) + 4 * U(0, 0, -1) + 2 * U(1, 0, -1) +
-              U(-1, 1, -1) + 2 * U(0, 1, -1) + U(1, 1, -1) +
-              2 * U(-1, -1, 0) + 4 * U(0, -1, 0) + 2 * U(1, -1, 0) +
-              4 * U(-1, 0, 0) + 8 * U(0, 0, 0) + 4 * U(1, 0, 0) +
-              2 * U(-1, 1, 0) + 4 * U(0, 1, 0) + 2 * U(1, 1, 0) +
-              U(-1, -1, 1) + 2 * U(0, -1, 1) + U(1, -1, 1) +
-              2 * U(-1, 0, 1) + 4 * U(0, 0, 1) + 2 * U(1, 0, 1) +
-              U(-1, 1, 1) + 2 * U(0, 1, 1) + U(1, 1, 1)) / 64.0;
-   if (ii && jj)
-      return (1 * U(-1, -1, 0) + 2 * U(0, -1, 0) + 1 * U(1, -1, 0) +
-              2 * U(-1, 0, 0) + 4 * U(0, 0, 0) + 2 * U(1, 0, 0) +
-              1 * U(-1, 1, 0) + 2 * U(0, 1, 0) + 1 * U(1, 1, 0)) / 16.0;
-   if (jj && kk)
-      return (1 * U(0, -1, -1) + 2 * U(0, -1, 0) + 1 * U(0, -1, 1) +
-              2 * U(0, 0, -1) + 4 * U(0, 0, 0) + 2 * U(0, 0, 1) +
-              1 * U(0, 1, -1) + 2 * U(0, 1, 0) + 1 * U(0, 1, 1)) / 16.0;
-   if (ii && kk)
-      return (1 * U(-1, 0, -1) + 2 * U(-1, 0, 0) + 1 * U(-1, 0, 1) +
-              2 * U(0, 0, -1) + 4 * U(0, 0, 0) + 2 * U(0, 0, 1) +
-              1 * U(1, 0, -1) + 2 * U(1, 0, 0) + 1 * U(1, 0, 1)) / 16.0;
-   if (ii) return (U(-1, 0, 0) + 2 * U(0, 0, 0) + U(1, 0, 0)) / 4.0;
-   if (jj) return (U(0, -1, 0) + 2 * U(0, 0, 0) + U(0, 1, 0)) / 4.0;
-   if (kk) return (U(0, 0, -1) + 2 * U(0, 0, 0) + U(0, 0, 1)) / 4.0;
-   return U(0, 0, 0);
-#undef U
+   /* strides of the outer, middle and inner offsets of the sum */
+   long s0, s1, s2;
+   int n0, n1, n2;
+   double scale;
+   if (ii && jj && kk) {
+      s0 = sz; s1 = sy; s2 = 1; n0 = n1 = n2 = 3; scale = 1.0 / 64.0;
+   } else if (ii && jj) {
+      s0 = 0; s1 = sy; s2 = 1; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
+   } else if (jj && kk) {
+      s0 = 0; s1 = sy; s2 = sz; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
+   } else if (ii && kk) {
+      s0 = 0; s1 = 1; s2 = sz; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
+   } else if (ii || jj || kk) {
+      s0 = 0; s1 = 0; s2 = ii ? 1 : (jj ? sy : sz); n0 = n1 = 1; n2 = 3; scale = 0.25;
+   } else
+      return u[p];
+   double acc = 0;
+   bool first = true;
+#pragma unroll
+   for (int a = 0; a < 3; a++) {
+      if (a >= n0) break;
+      int da = n0 == 3 ? a - 1 : 0;
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+         if (b >= n1) break;
+         int db = n1 == 3 ? b - 1 : 0;
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            int dc = c - 1;
+            double v = u[p + da * s0 + db * s1 + dc * s2];
+            int w = (da == 0 ? 2 : 1) * (db == 0 ? 2 : 1) * (dc == 0 ? 2 : 1);
+            if (n0 == 1) w >>= 1;
+            if (n1 == 1) w >>= 1;
+            acc = first ? (w == 1 ? v : (double)w * v) : ACC(acc, w, v);
+            first = false;
+         }
+      }
+   }
+   return acc * scale;
 }
+#undef ACC
 
 /* local_transfer delta = +1 (src/transfer.c:1126-1149): per grid function
  * straight injection, half weighting or full weighting */
-__global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops)
+__global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, int field_mask)
 {
-   const pgb_restrict_op o = ops[blockIdx.y];
-   long npts = (long)o.ni * o.nj * o.nk;
+   const pgb_restrict_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
-        q += (long)gridDim.x * blockDim.x) {
-      int a, bb, c;
-      unflat(q, o.ni, o.nj, a, bb, c);
-      int i0 = o.i1 + a * o.irho, j0 = o.j1 + bb * o.irho, k0 = o.k1 + c * o.irho;
-      long pd = lin(d, o.i2 + a, o.j2 + bb, o.k2 + c);
+   OP_PLANES(o.ni, o.nj, o.nk, {
+      const int i0 = o.i1 + a * o.irho, j0 = o.j1 + bb * o.irho, k0 = o.k1 + c * o.irho;
+      const long pd = lin(d, o.i2 + a, o.j2 + bb, o.k2 + c);
       for (int f = 0; f < PGB_NF; f++) {
-         int op = o.op[f];
-         if (!op) continue;
+         const int op = o.op[f];
+         if (!op || !((field_mask >> f) & 1)) continue;
          const double *u = s.f[f];
          double v;
          if (op == 1) v = u[lin(s, i0, j0, k0)];
@@ -450,20 +485,26 @@ __global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops)
          else v = fwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
          d.f[f][pd] = v;
       }
-   }
+   })
+}
+
+/* (j*1.0)/irho; for the ratio 2 of every MG hierarchy, the exact product j*0.5 */
+__device__ __forceinline__ double frac_rho(int j, int irho)
+{
+   return irho == 2 ? j * 0.5 : (j * 1.0) / irho;
 }
 
 /* one axis of dminterp3d's window (src/m_util_r8.f:65-144, 332-360): the
  * anchors and weights of window point t; n = 1 means a copied anchor */
 __device__ __forceinline__ int stencil(int t, int irho, int nanch, int ord, int *a, double *cf)
 {
-   int m = t / irho, j = t - m * irho;
+   const int m = irho == 2 ? t >> 1 : t / irho, j = t - m * irho;
    if (j == 0) {
       a[0] = m;
       return 1;
    }
    if (ord == 2 || nanch < 4) {
-      double sg = (j * 1.0) / irho;
+      double sg = frac_rho(j, irho);
       cf[0] = 1 - sg;
       cf[1] = sg;
       a[0] = m;
@@ -473,13 +514,13 @@ __device__ __forceinline__ int stencil(int t, int irho, int nanch, int ord, int 
    double sg;
    int base;
    if (m == 0) {                 /* left end: i1 <= s1 always holds for the window */
-      sg = (j * 1.0) / irho;
+      sg = frac_rho(j, irho);
       base = 0;
    } else if (m == nanch - 2) {  /* right end: (i1+n*s1) > (n1-2*s1) always holds */
-      sg = 2.0 + (j * 1.0) / irho;
+      sg = 2.0 + frac_rho(j, irho);
       base = nanch - 4;
    } else {
-      sg = 1.0 + (j * 1.0) / irho;
+      sg = 1.0 + frac_rho(j, irho);
       base = m - 1;
    }
    const double HALF = 0.5, MHALF = -0.5;
@@ -509,63 +550,65 @@ __device__ __forceinline__ double wsum(int n, const double *c, const double *v)
  * and write the requested fine segment */
 __global__ void k_interp(const pgb_dbox *boxes, const pgb_interp_op *ops, int field, int dim)
 {
-   const pgb_interp_op o = ops[blockIdx.y];
-   long npts = (long)o.nib * o.njb * o.nkb;
+   const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    const double *u = s.f[field];
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npts;
-        q += (long)gridDim.x * blockDim.x) {
-      int a, bb, c;
-      unflat(q, o.nib, o.njb, a, bb, c);
-      int tx = o.i2b - 1 + a, ty = o.j2b - 1 + bb, tz = o.k2b - 1 + c;
-      int ax[4], ay[4], az[4];
-      double cx[4], cy[4], cz[4];
-      int nx = stencil(tx, o.irho, o.nii, o.ord, ax, cx);
-      int ny = stencil(ty, o.irho, o.nji, o.ord, ay, cy);
-      int nz = dim == 3 ? stencil(tz, o.irho, o.nki, o.ord, az, cz) : 1;
+   for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
+      const int bb = row % o.njb, c = row / o.njb;
+      const int ty = o.j2b - 1 + bb, tz = o.k2b - 1 + c;
+      int ay[4], az[4];
+      double cy[4], cz[4];
+      const int ny = stencil(ty, o.irho, o.nji, o.ord, ay, cy);
+      const int nz = dim == 3 ? stencil(tz, o.irho, o.nki, o.ord, az, cz) : 1;
       if (dim != 3) az[0] = 0;
-      double kv[4];
-      for (int r = 0; r < nz; r++) {
-         double jv[4];
-         for (int qq = 0; qq < ny; qq++) {
-            double iv[4];
-            for (int pp = 0; pp < nx; pp++)
-               iv[pp] = u[lin(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
-            jv[qq] = wsum(nx, cx, iv);
+      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+         const int tx = o.i2b - 1 + a;
+         int ax[4];
+         double cx[4];
+         const int nx = stencil(tx, o.irho, o.nii, o.ord, ax, cx);
+         double kv[4];
+         for (int r = 0; r < nz; r++) {
+            double jv[4];
+            for (int qq = 0; qq < ny; qq++) {
+               double iv[4];
+               for (int pp = 0; pp < nx; pp++)
+                  iv[pp] = u[lin(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
+               jv[qq] = wsum(nx, cx, iv);
+            }
+            kv[r] = wsum(ny, cy, jv);
          }
-         kv[r] = wsum(ny, cy, jv);
+         d.f[field][lin(d, o.i2 + a, o.j2 + bb, o.k2 + c)] = wsum(nz, cz, kv);
       }
-      d.f[field][lin(d, o.i2 + a, o.j2 + bb, o.k2 + c)] = wsum(nz, cz, kv);
    }
 }
 
 extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream)
 {
+   const pgb_copy_op *h = (const pgb_copy_op *)p->h_ops, *d = (const pgb_copy_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
-      int n = p->batch_start[bt + 1] - p->batch_start[bt];
-      int gx = (p->batch_maxpts[bt] + 255) / 256;
-      if (gx > 512) gx = 512;
-      if (n <= 0 || gx <= 0) continue;
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
       for (int c0 = 0; c0 < n; c0 += 65535) {
-         k_copy<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
-            boxes, (const pgb_copy_op *)p->d_ops + p->batch_start[bt] + c0, field);
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         dim3 g;
+         plane_grid(h + p->batch_start[bt] + c0, m, g);
+         k_copy<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, field);
          LAUNCHED(1);
       }
    }
    return check("copy");
 }
 
-extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *stream)
+extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, void *stream)
 {
+   const pgb_restrict_op *h = (const pgb_restrict_op *)p->h_ops, *d = (const pgb_restrict_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
-      int n = p->batch_start[bt + 1] - p->batch_start[bt];
-      int gx = (p->batch_maxpts[bt] + 255) / 256;
-      if (gx > 1024) gx = 1024;
-      if (n <= 0 || gx <= 0) continue;
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
       for (int c0 = 0; c0 < n; c0 += 65535) {
-         k_restrict<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
-            boxes, (const pgb_restrict_op *)p->d_ops + p->batch_start[bt] + c0);
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         dim3 g;
+         plane_grid(h + p->batch_start[bt] + c0, m, g);
+         k_restrict<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, field_mask);
          LAUNCHED(1);
       }
    }
@@ -575,14 +618,14 @@ extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, void *st
 extern "C" int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim,
                             void *stream)
 {
+   const pgb_interp_op *h = (const pgb_interp_op *)p->h_ops, *d = (const pgb_interp_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
-      int n = p->batch_start[bt + 1] - p->batch_start[bt];
-      int gx = (p->batch_maxpts[bt] + 255) / 256;
-      if (gx > 2048) gx = 2048;
-      if (n <= 0 || gx <= 0) continue;
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
       for (int c0 = 0; c0 < n; c0 += 65535) {
-         k_interp<<<dim3(gx, n - c0 < 65535 ? n - c0 : 65535), 256, 0, (cudaStream_t)stream>>>(
-            boxes, (const pgb_interp_op *)p->d_ops + p->batch_start[bt] + c0, field, dim);
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         dim3 g;
+         row_grid(h + p->batch_start[bt] + c0, m, g);
+         k_interp<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, field, dim);
          LAUNCHED(1);
       }
    }
@@ -950,36 +993,7 @@ __global__ void __cluster_dims__(PGB_CL, 1, 1) __launch_bounds__(CLT)
 }
 
 /* ---------------------------------------------- coarsest grids, on chip -- */
-/* Correctly rounded x / d for a divisor d known in advance, with r = RN(1/d)
- * computed by the host: q0 = RN(x*r), e = x - q0*d (exact with FMA),
- * q = RN(q0 + e*r). Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34,
- * 1990; Muller et al., Handbook of Floating-Point Arithmetic, 2018, sec.
- * 4.7) gives q = RN(x/d) when r = RN(1/d) and q0 is within one ulp of x/d,
- * barring overflow/underflow; the tests compare it with IEEE division. */
-__device__ __forceinline__ double div_known(double x, double d, double r)
-{
-   double q0 = __dmul_rn(x, r);
-   double e = __fma_rn(-q0, d, x);
-   return __fma_rn(e, r, q0);
-}
 
-/* lap(u) of num.f:113-115 with the divisions by dx^2 done by div_known */
-__device__ __forceinline__ double lap_known(const pgb_dbox &b, const double *u, long p, long sy,
-                                            long sz, int dim)
-{
-   double c = u[p];
-   double t;
-   if (b.flags & PGB_BOX_POW2DX)
-      t = (u[p + 1] - 2 * c + u[p - 1]) * b.idx2[0] + (u[p + sy] - 2 * c + u[p - sy]) * b.idx2[1];
-   else
-      t = div_known(u[p + 1] - 2 * c + u[p - 1], b.dx2[0], b.idx2[0]) +
-          div_known(u[p + sy] - 2 * c + u[p - sy], b.dx2[1], b.idx2[1]);
-   if (dim == 3) {
-      if (b.flags & PGB_BOX_POW2DX) t = t + (u[p + sz] - 2 * c + u[p - sz]) * b.idx2[2];
-      else t = t + div_known(u[p + sz] - 2 * c + u[p - sz], b.dx2[2], b.idx2[2]);
-   }
-   return t;
-}
 
 /* The coarsest-grid loop with the whole coarsest level (u, rhs, source and
  * the saved state of the cycle check) held in shared memory: below the
@@ -1050,7 +1064,7 @@ __global__ void __launch_bounds__(CT) k_coarsest_smem(const pgb_dbox *boxes, pgb
                long p = i + sy * j + sz * k;
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
                double uc = u[p], s = src[p];
-               double r = op64(pde, lap_known(bx, u, p, sy, sz, dim), uc, s) - rhs[p];
+               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - rhs[p];
                double jac = jac64(pde, bx.j0, uc, s);
                u[p] = uc - r / jac;
                acc += r * r;

@@ -758,13 +758,16 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    /* AMR-level boxes keep coarsest = 0 except on MG level 1 (gh.c:1137, 1357) */
    for (i = 0; i < h->nbox; i++) {
       pgb_hbox *b = &h->boxes[i];
-      int pow2 = 1;
+      int pow2 = 1, iso = 1;
+      double dx0 = b->x[0][1] - b->x[0][0];
       if (b->level != 1 && b->amr_grid >= 0) b->coarsest = 0;
       for (d = 0; d < dim; d++) {
          double dxo = b->x[d][1] - b->x[d][0];
          if (!is_pow2(dxo * dxo)) pow2 = 0;
+         if (dxo * dxo != dx0 * dx0) iso = 0;
       }
       if (pow2) b->flags |= PGB_BOX_POW2DX;
+      if (iso) b->flags |= PGB_BOX_ISO;
       if (b->coarsest) b->flags |= PGB_BOX_COARSEST;
    }
    build_masks(h);

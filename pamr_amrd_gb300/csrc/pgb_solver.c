@@ -39,6 +39,9 @@ struct pgb_solver {
    pgb_trace *d_trace;
    int trace_cap;
    double *h_res;           /* pinned */
+   int prepared;            /* pgb_prepare ran after the last change of an input grid */
+   int fuse[PGB_MAXLEV + 1]; /* mixed form: FP32 sweeps per launch on levels without syncs */
+   int tuned;               /* the autotuner has run */
    cudaGraphExec_t gexec;   /* one captured V-cycle (+ read-back of the residual) */
    int graph_ok;
    long long graph_kernels; /* kernel launches in the captured V-cycle */
@@ -71,6 +74,12 @@ static int fail(int code, const char *fmt, ...)
    do {                                                                             \
       if (call) return fail(11, "%s", pgb_dev_error());                              \
    } while (0)
+#define KC32(call)                                                                  \
+   do {                                                                             \
+      if (call) return fail(11, "%s", pgb_dev_error32());                            \
+   } while (0)
+
+static void drop_graph(pgb_solver *s);
 
 void pgb_default_params(pgb_mg_params *p)
 {
@@ -109,6 +118,50 @@ static int choose_tz(const pgb_hier *h, int L, int tx)
       if (n >= 2 * 152) break;
    }
    return tz;
+}
+
+/* The subset of a level's tiles that the coarse half of the coarse-grid
+ * correction and the FAS right-hand side have to visit: tiles that contain a
+ * point with the child cmask ON, or a point inside the coarse window of an
+ * interpolation op to level L+1. Elsewhere rhs stays 0 (cleared by
+ * pgb_prepare, never written by a cycle) and lop/res are never read before
+ * the next clear or residual, so skipping those tiles changes no result. */
+static int make_cover_tiles(const pgb_hier *h, int L, const pgb_tile *t, int nt, int tz,
+                            pgb_tile **out)
+{
+   int n = 0, q;
+   pgb_tile *c = (pgb_tile *)malloc(sizeof(pgb_tile) * (size_t)(nt ? nt : 1));
+   const pgb_plan *ip = L < h->nlev ? &h->interp[L + 1] : 0;
+   for (q = 0; q < nt; q++) {
+      const pgb_hbox *bx = &h->boxes[t[q].box];
+      int lo[3] = {t[q].i0, t[q].j0, t[q].k0};
+      int hi[3] = {t[q].i0 + PGB_TX - 1, t[q].j0 + PGB_TY - 1, h->dim == 3 ? t[q].k0 + tz - 1 : 0};
+      int d, i, j, k, hit = 0;
+      for (d = 0; d < 3; d++)
+         if (hi[d] > bx->shape[d] - 1) hi[d] = bx->shape[d] - 1;
+      for (k = lo[2]; k <= hi[2] && !hit; k++)
+         for (j = lo[1]; j <= hi[1] && !hit; j++)
+            for (i = lo[0]; i <= hi[0]; i++)
+               if (bx->child_mask[i + (long)bx->shape[0] * (j + (long)bx->shape[1] * k)]) {
+                  hit = 1;
+                  break;
+               }
+      if (!hit && ip) {
+         const pgb_interp_op *o = (const pgb_interp_op *)ip->h_ops;
+         int m;
+         for (m = 0; m < ip->nops && !hit; m++) {
+            int wlo[3] = {o[m].i1i - 1, o[m].j1i - 1, o[m].k1i - 1};
+            int whi[3] = {wlo[0] + o[m].nii - 1, wlo[1] + o[m].nji - 1, wlo[2] + o[m].nki - 1};
+            if (o[m].src_box != t[q].box) continue;
+            hit = 1;
+            for (d = 0; d < h->dim; d++)
+               if (whi[d] < lo[d] || wlo[d] > hi[d]) hit = 0;
+         }
+      }
+      if (hit) c[n++] = t[q];
+   }
+   *out = c;
+   return n;
 }
 
 /* tiles of the boxes of one level; tx = tile width in x, tz planes deep */
@@ -152,6 +205,66 @@ static void free_plan_dev(pgb_plan *p)
 {
    if (p->d_ops) cudaFree(p->d_ops);
    p->d_ops = 0;
+}
+
+/* (Re)builds the device tables of level L: tiles of tz planes, relax tiles,
+ * tile starts, the box list and the cover tiles. */
+static int level_tables(pgb_solver *s, int L, int tz)
+{
+   pgb_hier *h = &s->h;
+   pgb_tile *t = 0, *rt = 0, *ct = 0;
+   int nb = h->lev[L].nbox, nct;
+   int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
+   int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
+   int rtz = choose_tz(h, L, 2 * PGB_TX);
+   int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
+   int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
+   size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
+   size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
+   size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
+   size_t b4 = b3 + align256(sizeof(int) * (size_t)(nb + 1));
+   size_t b5 = b4 + align256(sizeof(int) * (size_t)nb), b6;
+   char *dt;
+   int rc = 0;
+   nct = make_cover_tiles(h, L, t, nt, tz, &ct);
+   b6 = b5 + align256(sizeof(pgb_tile) * (size_t)(nct ? nct : 1));
+   if (s->d_tables[L]) cudaFree(s->d_tables[L]);
+   s->d_tables[L] = 0;
+   if (cudaMalloc(&s->d_tables[L], b6) != cudaSuccess) {
+      rc = fail(10, "cudaMalloc of the level tables failed");
+      goto out;
+   }
+   dt = (char *)s->d_tables[L];
+   if ((nct && cudaMemcpy(dt + b5, ct, sizeof(pgb_tile) * (size_t)nct, cudaMemcpyHostToDevice)) ||
+       cudaMemcpy(dt + b0, t, sizeof(pgb_tile) * (size_t)nt, cudaMemcpyHostToDevice) ||
+       cudaMemcpy(dt + b1, rt, sizeof(pgb_tile) * (size_t)nrt, cudaMemcpyHostToDevice) ||
+       cudaMemcpy(dt + b2, ts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
+       cudaMemcpy(dt + b3, rts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
+       cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice)) {
+      rc = fail(10, "upload of the level tables failed");
+      goto out;
+   }
+   s->lv[L].tiles = (const pgb_tile *)(dt + b0);
+   s->lv[L].rtiles = (const pgb_tile *)(dt + b1);
+   s->lv[L].tile_start = (const int *)(dt + b2);
+   s->lv[L].rtile_start = (const int *)(dt + b3);
+   s->lv[L].box = (const int *)(dt + b4);
+   s->lv[L].ctiles = (const pgb_tile *)(dt + b5);
+   s->lv[L].nctiles = nct;
+   s->lv[L].ntiles = nt;
+   s->lv[L].nrtiles = nrt;
+   s->lv[L].nbox = nb;
+   s->lv[L].tz = tz;
+   s->lv[L].rtz = rtz;
+   s->lv[L].dim = h->dim;
+   s->lv[L].level = L;
+out:
+   free(t);
+   free(rt);
+   free(ct);
+   free(ts);
+   free(rts);
+   return rc;
 }
 
 static int setup_device(pgb_solver *s)
@@ -227,45 +340,23 @@ static int setup_device(pgb_solver *s)
 
    /* per-level tables: tiles, relax tiles, tile starts, box lists */
    for (L = 1; L <= h->nlev; L++) {
-      pgb_tile *t = 0, *rt = 0;
       int nb = h->lev[L].nbox;
-      int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
-      int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
-      int tz = choose_tz(h, L, PGB_TX), rtz = choose_tz(h, L, 2 * PGB_TX);
-      int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
-      int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
-      size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
-      size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
-      size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
-      size_t b4 = b3 + align256(sizeof(int) * (size_t)(nb + 1));
-      size_t b5 = b4 + align256(sizeof(int) * (size_t)nb);
-      char *dt;
-      CU(cudaMalloc(&s->d_tables[L], b5));
-      dt = (char *)s->d_tables[L];
-      CU(cudaMemcpy(dt + b0, t, sizeof(pgb_tile) * (size_t)nt, cudaMemcpyHostToDevice));
-      CU(cudaMemcpy(dt + b1, rt, sizeof(pgb_tile) * (size_t)nrt, cudaMemcpyHostToDevice));
-      CU(cudaMemcpy(dt + b2, ts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice));
-      CU(cudaMemcpy(dt + b3, rts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice));
-      CU(cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice));
-      s->lv[L].tiles = (const pgb_tile *)(dt + b0);
-      s->lv[L].rtiles = (const pgb_tile *)(dt + b1);
-      s->lv[L].tile_start = (const int *)(dt + b2);
-      s->lv[L].rtile_start = (const int *)(dt + b3);
-      s->lv[L].box = (const int *)(dt + b4);
-      s->lv[L].ntiles = nt;
-      s->lv[L].nrtiles = nrt;
-      s->lv[L].nbox = nb;
-      s->lv[L].tz = tz;
-      s->lv[L].rtz = rtz;
-      s->lv[L].dim = h->dim;
-      s->lv[L].level = L;
-      if (nt > maxt) maxt = nt;
-      if (nrt > maxt) maxt = nrt;
+      if (level_tables(s, L, choose_tz(h, L, PGB_TX))) return 10;
+      s->fuse[L] = 0;
+      /* the reduction scratch holds the partial sums of the most finely
+       * tiled layout the autotuner can pick (one plane per tile) */
+      {
+         long n1 = 0;
+         int b;
+         for (b = 0; b < nb; b++) {
+            const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+            n1 += (long)((bx->shape[0] + PGB_TX - 1) / PGB_TX) * ((bx->shape[1] + PGB_TY - 1) / PGB_TY) *
+                  bx->shape[2];
+         }
+         if (n1 > maxt) maxt = (int)n1;
+         if (s->lv[L].nrtiles > maxt) maxt = s->lv[L].nrtiles;
+      }
       if (nb > maxbox) maxbox = nb;
-      free(t);
-      free(rt);
-      free(ts);
-      free(rts);
       /* snapshot offsets of the coarsest boxes of this level */
       {
          long o = 0, *so = (long *)calloc((size_t)nb + 1, sizeof(long));
@@ -433,7 +524,9 @@ static int copy_grid(pgb_solver *s, int grid, const double *u, const double *src
 
 int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src)
 {
-   int rc = copy_grid(s, grid, u, src, 0, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+   int rc;
+   s->prepared = 0;
+   rc = copy_grid(s, grid, u, src, 0, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
    if (!rc) CU(cudaStreamSynchronize(s->stream));
    return rc;
 }
@@ -443,6 +536,7 @@ int pgb_get_grid(pgb_solver *s, int grid, double *u)
 }
 int pgb_set_grid_device(pgb_solver *s, int grid, const double *u, const double *src)
 {
+   s->prepared = 0;
    return copy_grid(s, grid, u, src, 0, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
 }
 int pgb_get_grid_device(pgb_solver *s, int grid, double *u)
@@ -473,6 +567,72 @@ static int sync_field(pgb_solver *s, const pgb_plan *p, int field)
    return 0;
 }
 
+/* Autotuner of the mixed form, run once per solver at its first
+ * pgb_prepare: for every smoothed level it times the level's smoothing
+ * block (max(pre, post) FP32 sweeps) plus its FP64 residual pass for each
+ * tile depth (8, 4, 2, 1 planes per 32 x 8 tile; 3-D only) and each sweep
+ * kernel: two global-memory colour passes per sweep, one shared-memory
+ * sweep per launch or, on levels without a sync between sweeps, two, and
+ * keeps the fastest. Neither choice changes a computed value (the sweeps
+ * are the same Gauss-Seidel sweeps; only the norm's summation order
+ * follows the tiles). PGB_AUTOTUNE=0 keeps the defaults. */
+static int autotune(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const char *env = getenv("PGB_AUTOTUNE");
+   int L, changed = 0;
+   int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
+   s->tuned = 1;
+   if ((env && !strcmp(env, "0")) || nsw < 1) return 0;
+   for (L = 2; L <= h->nlev; L++) {
+      static const int tzs[4] = {8, 4, 2, 1};
+      int ntz = h->dim == 3 ? 4 : 1, a, f, best_tz = s->lv[L].tz, best_f = s->fuse[L];
+      int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
+      float best = 1e30f;
+      for (a = 0; a < ntz; a++) {
+         if (h->dim == 3 && tzs[a] != s->lv[L].tz) {
+            if (level_tables(s, L, tzs[a])) return 10;
+            changed = 1;
+         }
+         for (f = 0; f <= (can_fuse ? 2 : 1); f++) {
+            float ms = 0;
+            int r;
+            for (r = 0; r < 4; r++) {   /* one warm-up, three timed */
+               if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));
+               KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, s->stream));
+               KC32(pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0,
+                                        s->stream));
+            }
+            CU(cudaEventRecord(s->ev1, s->stream));
+            CU(cudaEventSynchronize(s->ev1));
+            CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            if (ms < best) {
+               best = ms;
+               best_tz = s->lv[L].tz;
+               best_f = f;
+            }
+         }
+      }
+      if (best_tz != s->lv[L].tz) {
+         if (level_tables(s, L, best_tz)) return 10;
+         changed = 1;
+      }
+      s->fuse[L] = best_f;
+   }
+   if (changed) drop_graph(s);
+   return 0;
+}
+
+int pgb_level_tuning(pgb_solver *s, int L, int *tile_planes, int *sweeps_per_launch)
+{
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (L < 1 || L > s->h.nlev) return fail(3, "level %d out of range", L);
+   if (tile_planes) *tile_planes = s->lv[L].tz;
+   if (sweeps_per_launch)   /* 0: one launch per colour pass */
+      *sweeps_per_launch = (s->fuse[L] > 1 && (s->h.sync[L][0].nops || s->h.sync[L][1].nops)) ? 1 : s->fuse[L];
+   return 0;
+}
+
 /* initialisation the reference performs while building the MG hierarchy
  * (build_mgh src/gh.c:1222-1365): MG-only grid functions start at zero and
  * pure MG levels receive u and the source by TF_MGH_INIT injection */
@@ -486,114 +646,184 @@ int pgb_prepare(pgb_solver *s)
       KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
    }
    for (L = s->h.nlev - 1; L >= 1; L--)
-      if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], s->stream));
+      if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, s->stream));
+   if (s->h.prm.precision == PGB_MIXED) {
+      if (!s->tuned) {
+         int rc = autotune(s);
+         if (rc) return rc;
+      }
+      /* FP32 correction arrays start at 0; the finest level's first
+       * pre-smoothing defect is the initial residual */
+      for (L = 1; L <= s->h.nlev; L++)
+         if (pgb_k_zero32(s->dbox, s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
+      if (pgb_k_residual_fast(s->dbox, s->lv[s->h.nlev], s->h.pde, s->sc,
+                              norm_slot(s, s->h.nlev, N_RESID), 0, s->stream))
+         return fail(11, "%s", pgb_dev_error32());
+   }
    CU(cudaMemsetAsync(s->d_citers, 0, sizeof(int), s->stream));
+   s->prepared = 1;
    return 0;
 }
 
-#define KC32(call)                                                                  \
-   do {                                                                             \
-      if (call) return fail(11, "%s", pgb_dev_error32());                            \
-   } while (0)
 
-/* one smoothing block (nsweep sweeps + syncs, amrd/mg.c:135-141 / 161-167).
- * FP64: Newton-GS sweeps. Mixed: FP64 defect, FP32 sweeps on the correction
- * (synced between boxes like u), FP64 update, then the sync of u. The
- * coarsest-grid loop itself always runs in FP64. */
+/* one smoothing block of the FP64 form (nsweep Newton-GS sweeps + syncs,
+ * amrd/mg.c:135-141 / 161-167) */
 static int smooth(pgb_solver *s, int L, int nsweep, int slot)
 {
    pgb_hier *h = &s->h;
    int it;
-   if (h->prm.precision == PGB_FP64) {
-      for (it = 0; it < nsweep; it++) {
-         if (relax(s, L, slot)) return 11;
-         if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
-      }
-      return 0;
-   }
-   if (nsweep <= 0) return 0;
-   KC32(pgb_k_defect(s->dbox, s->lv[L], h->pde, s->stream));
    for (it = 0; it < nsweep; it++) {
-      KC32(pgb_k_relax32(s->dbox, s->lv[L], s->stream));
-      if (h->sync[L][it ? 1 : 0].nops) KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], s->stream));
+      if (relax(s, L, slot)) return 11;
+      if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
    }
-   KC32(pgb_k_update(s->dbox, s->lv[L], s->stream));
-   if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
    return 0;
 }
 
-static int vcycle_launch(pgb_solver *s)
+/* fills the coarsest-grid loop's arguments for level L */
+static void coarsest_args(pgb_solver *s, int L, pgb_coarsest_args *a)
 {
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
-   int L, Lf = h->nlev, mixed = p->precision == PGB_MIXED;
+   int b, mixed = p->precision == PGB_MIXED, nmax = 0, d;
+   memset(a, 0, sizeof(*a));
+   a->start_iter = mixed ? 0 : p->pst_swp;
+   a->max_citer = p->max_citer;
+   a->crtol = p->crtol;
+   a->res_dn = norm_slot(s, L, p->pre_swp > 0 ? N_RELAX_DN : N_COARSE);
+   a->res_out = norm_slot(s, L, N_COARSE);
+   a->iters_out = s->d_citers;
+   for (b = 0; b < h->lev[L].nbox; b++) {
+      const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+      if (!bx->coarsest) continue;
+      a->smem_points += (long)bx->shape[0] * bx->shape[1] * bx->shape[2];
+      a->ncoarse++;
+      for (d = 0; d < h->dim; d++)
+         if (bx->shape[d] > nmax) nmax = bx->shape[d];
+   }
+   a->stagnation_exit = mixed;
+   a->ctol_from_first = mixed;
+   /* red-black SOR factor of the model problem, 2/(1 + sin(pi h)) */
+   a->omega = nmax > 3 ? 2.0 / (1.0 + sin(3.141592653589793 / (nmax - 1))) : 1.0;
+   a->snap = s->d_snap;
+   a->snap_points = s->snap_points;
+   a->snap_off = s->d_snap_off[L];
+}
+
+static int vcycle_fp64(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const pgb_hparams *p = &h->prm;
+   int L, Lf = h->nlev;
    /* clear_MG_vars(Lf) amrd/mg.c:91 */
    KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
       if (L < Lf) {
-         if (mixed)
-            KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
-                                     s->d_trace, s->stream));
-         else
-            KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
-                              s->d_trace, s->stream));
+         KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
+                           s->d_trace, s->stream));
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;   /* set_res_sync */
-         /* clear_MG_vars(L): rhs and lop are rewritten whole by lop_rhs below */
+         /* clear_MG_vars(L): rhs and lop are rewritten by lop_rhs below */
          KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
-         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], s->stream));
+         /* the source restriction of MG-only levels (TF_INJECT_TO_MG_LEV) is left
+          * out: it reads and writes the same values every cycle, and
+          * pgb_prepare's build-time injection (same ops, same operator) has
+          * already put them in place */
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
-         if (mixed) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
-         else KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+         KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
       if (smooth(s, L, p->pre_swp, N_RELAX_DN)) return 11;
    }
    for (L = 1; L <= Lf; L++) {
       if (L > 1) {
          KC(pgb_k_cgc_coarse(s->dbox, s->lv[L - 1], p->w0_i, s->stream));
-         if (p->precision == PGB_MIXED) {
-            if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, s->stream));
-         } else {
-            if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
-         }
+         if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
          KC(pgb_k_add_res(s->dbox, s->lv[L], s->stream));
       }
       if (smooth(s, L, p->pst_swp, N_RELAX_UP)) return 11;
       if (lvl_coarsest(s, L)) {
          pgb_coarsest_args a;
-         a.start_iter = p->pst_swp;
-         a.max_citer = p->max_citer;
-         a.crtol = p->crtol;
-         a.res_dn = norm_slot(s, L, p->pre_swp > 0 ? N_RELAX_DN : N_COARSE);
-         a.res_out = norm_slot(s, L, N_COARSE);
-         a.iters_out = s->d_citers;
-         a.smem_points = 0;
-         a.ncoarse = 0;
-         {
-            int b;
-            for (b = 0; b < h->lev[L].nbox; b++) {
-               const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
-               if (!bx->coarsest) continue;
-               a.smem_points += (long)bx->shape[0] * bx->shape[1] * bx->shape[2];
-               a.ncoarse++;
-            }
-         }
-         a.stagnation_exit = mixed;
-         a.ctol_from_first = mixed;
-         a.snap = s->d_snap;
-         a.snap_points = s->snap_points;
-         a.snap_off = s->d_snap_off[L];
+         coarsest_args(s, L, &a);
          KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
       }
-      if (L == Lf) {
-         if (mixed)
-            KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
-                                     s->d_trace, s->stream));
-         else
-            KC(pgb_k_residual(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
-                              s->d_trace, s->stream));
-      }
+      if (L == Lf)
+         KC(pgb_k_residual(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID), s->d_trace,
+                           s->stream));
    }
    return 0;
+}
+
+/* FP32 sweeps on the correction E of level L, synced between boxes like u */
+static int sweeps32(pgb_solver *s, int L, int nsweep)
+{
+   pgb_hier *h = &s->h;
+   int it;
+   if (!h->sync[L][0].nops && !h->sync[L][1].nops) {
+      KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsweep, s->fuse[L], s->stream));
+      return 0;
+   }
+   for (it = 0; it < nsweep; it++) {
+      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] > 1 ? 1 : s->fuse[L], s->stream));
+      if (h->sync[L][it ? 1 : 0].nops) KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], s->stream));
+   }
+   return 0;
+}
+
+/* The mixed form of the V-cycle (same transfers and the same FP64 residual,
+ * restriction and norm as vcycle_fp64; the arithmetic of each smoothing
+ * block is described in pgb_kernels32.cu). The finest level's pre-smoothing
+ * defect is the residual the previous cycle ended with (pgb_prepare
+ * computes the first); the coarsest level is smoothed by the coarsest-grid
+ * loop alone. */
+static int vcycle_mixed(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const pgb_hparams *p = &h->prm;
+   int L, Lf = h->nlev;
+   KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
+   for (L = Lf; L > 0; L--) {
+      if (L < Lf) {
+         KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
+                                  s->d_trace, s->stream));
+         if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
+         KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->stream));
+         if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
+         if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+         else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+      }
+      if (L > 1 && p->pre_swp > 0) {
+         if (sweeps32(s, L, p->pre_swp)) return 11;
+         KC32(pgb_k_update(s->dbox, s->lv[L], 0, s->stream));
+         if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
+      }
+   }
+   for (L = 1; L <= Lf; L++) {
+      if (L > 1) {
+         KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
+         if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, s->stream));
+         if (sweeps32(s, L, p->pst_swp)) return 11;
+         KC32(pgb_k_update(s->dbox, s->lv[L], 1, s->stream));
+         if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
+      } else if (lvl_coarsest(s, L)) {
+         pgb_coarsest_args a;
+         int rc;
+         coarsest_args(s, L, &a);
+         rc = pgb_k_coarsest_mixed(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace,
+                                   s->stream);
+         if (rc < 0) return fail(11, "%s", pgb_dev_error32());
+         if (rc > 0)   /* too large for one CTA's shared memory: the FP64 loop */
+            KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
+      }
+      if (L == Lf)
+         KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
+                                  s->d_trace, s->stream));
+   }
+   return 0;
+}
+
+static int vcycle_launch(pgb_solver *s)
+{
+   return s->h.prm.precision == PGB_MIXED ? vcycle_mixed(s) : vcycle_fp64(s);
 }
 
 /* The V-cycle's launches never depend on host-side values, so the whole
@@ -635,6 +865,7 @@ int pgb_vcycle(pgb_solver *s, double *res)
 {
    int rc;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (!s->prepared && (rc = pgb_prepare(s))) return rc;
    if (getenv("PGB_NO_GRAPH")) {
       if ((rc = vcycle_launch(s))) return rc;
       CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double),
@@ -698,10 +929,10 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    if (L < 1 || L > s->h.nlev || reps < 1) return fail(3, "bad level or reps");
    int mixed = s->h.prm.precision == PGB_MIXED;
    for (b = 0; b < s->h.lev[L].nbox; b++) pts += s->h.boxes[s->h.lev[L].box[b]].count;
-   if (mixed) KC32(pgb_k_defect(s->dbox, s->lv[L], s->h.pde, s->stream));
+   s->prepared = 0;   /* the sweeps change the level: the next cycle starts from pgb_prepare */
    for (r = 0; r <= reps; r++) {
       if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));   /* first sweep warms up */
-      if (mixed) KC32(pgb_k_relax32(s->dbox, s->lv[L], s->stream));
+      if (mixed) KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, 0, s->stream));
       else if (relax(s, L, N_RELAX_UP)) return 11;
    }
    CU(cudaEventRecord(s->ev1, s->stream));

@@ -69,6 +69,7 @@ def lib(build: bool = True):
         L.pgb_default_params.argtypes = [C.POINTER(MGParams)]
         L.pgb_launch_count.restype = C.c_longlong
         L.pgb_time_relax.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+        L.pgb_level_tuning.argtypes = [vp, C.c_int, ip, ip]
         for name in ("pgb_dmcopy3d", "pgb_dmhwr3d", "pgb_dmfwr3d"):
             getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp]
         L.pgb_dminterp3d.argtypes = [vp, vp] + [C.c_int] * 22 + [vp]
@@ -173,6 +174,12 @@ class Solver:
         v, c, ms = C.c_int(), C.c_long(), C.c_double()
         lib().pgb_stats(self.h, C.byref(v), C.byref(c), C.byref(ms))
         return {"vcycles": v.value, "coarsest_iters": c.value, "device_ms": ms.value}
+
+    def level_tuning(self, L: int):
+        """(tile planes, FP32 sweeps per launch) the autotuner chose for level L"""
+        tz, f = C.c_int(), C.c_int()
+        _check(lib().pgb_level_tuning(self.h, L, C.byref(tz), C.byref(f)))
+        return tz.value, f.value
 
     def time_relax(self, L: int, reps: int = 20):
         ms, by = C.c_double(), C.c_double()

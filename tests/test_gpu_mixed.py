@@ -51,3 +51,26 @@ def test_mixed_matches_oracle_port(make):
     case = make()
     p = portrun.solve(case)
     _check(case, p["u"], p["iters"])
+
+
+def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
+    """The autotuner only picks tile depth and sweeps per launch: the solution
+    and the cycle count match a solve with the default shapes."""
+    case = W.conformal3d(65, 33, seed=1)
+    case.params.precision = 1
+    s = Solver(case)
+    s.set_inputs()
+    r1 = s.solve()
+    u1 = s.get_u()
+    shapes = [s.level_tuning(L) for L in range(2, s.num_levels() + 1)]
+    s.close()
+    assert all(tz in (1, 2, 4, 8) and f in (0, 1, 2) for tz, f in shapes), shapes
+    monkeypatch.setenv("PGB_AUTOTUNE", "0")
+    s = Solver(case)
+    s.set_inputs()
+    r2 = s.solve()
+    u2 = s.get_u()
+    s.close()
+    assert r1["iters"] == r2["iters"]
+    umax = max(float(np.max(np.abs(a))) for a in u2)
+    assert max(float(np.max(np.abs(a - b))) for a, b in zip(u1, u2)) <= 1e-13 * umax
