@@ -97,7 +97,8 @@ int pgb_k_fill(double *p, long n, double v, void *stream);
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);
 unsigned long long pgb_dev_launches32(void);
-int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
+int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover, void *stream);
+int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream);
 int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, void *stream);
 int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);

@@ -72,6 +72,36 @@ __device__ __forceinline__ bool relaxed32(const pgb_dbox &b, int i, int j, int k
    return interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p]);
 }
 
+/* FP32 <-> FP64 conversions in integer arithmetic. A conversion
+ * instruction issues on the FP64 pipe, which runs at 1/64 of the FP32 rate
+ * here; these take the integer pipes instead. f2d is exact except that FP32
+ * subnormals (below 1.2e-38) become 0; d2f rounds toward zero (relative error
+ * below 2^-23) and flushes results below the FP32 normal range to 0. Both
+ * only touch values that steer the FP32 smoother or enter an FP64 sum as a
+ * correction. */
+__device__ __forceinline__ double f2d(float f)
+{
+   const unsigned int b = __float_as_uint(f);
+   const unsigned int e = (b >> 23) & 0xffu;
+   const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
+   const unsigned long long ed = e == 0xffu ? 2047ull : (unsigned long long)(e + 896u);
+   const unsigned long long v = sgn | (ed << 52) | ((unsigned long long)(b & 0x7fffffu) << 29);
+   return __longlong_as_double((long long)(e ? v : sgn));
+}
+
+__device__ __forceinline__ float d2f(double d)
+{
+   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+   const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
+   const int e = (int)((hi >> 20) & 0x7ffu) - 896;       /* FP32 biased exponent */
+   const unsigned int sgn = hi & 0x80000000u;
+   const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+   unsigned int r = sgn | ((unsigned int)e << 23) | m;
+   r = e <= 0 ? sgn : r;
+   r = e >= 255 ? (sgn | 0x7f800000u | (((hi >> 20) & 0x7ffu) == 0x7ffu && (m | (hi & 0xfffffu) | lo) ? 0x400000u : 0u)) : r;
+   return __uint_as_float(r);
+}
+
 /* lap u in FP64 (num.f:113-115 up to rounding). Per dimension
  * RN(u+ - 2u) + u- rounds once at the scale of u (the last add is exact
  * near convergence, Sterbenz), which keeps the residual's rounding floor at
@@ -91,6 +121,22 @@ __device__ __forceinline__ double lapm(const pgb_dbox &b, const double *u, long 
    return t;
 }
 
+/* lapm with the centre and the two z neighbours supplied by the caller
+ * (a thread walking its tile's planes keeps them in registers) */
+__device__ __forceinline__ double lapw(const pgb_dbox &b, const double *u, long p, long sy, double c,
+                                       double zm, double zp, int dim)
+{
+   const double dx = fma(-2.0, c, u[p + 1]) + u[p - 1];
+   const double dy = fma(-2.0, c, u[p + sy]) + u[p - sy];
+   if (b.flags & PGB_BOX_ISO) {
+      if (dim == 3) return ((dx + dy) + (fma(-2.0, c, zp) + zm)) * b.idx2[0];
+      return (dx + dy) * b.idx2[0];
+   }
+   double t = fma(dy, b.idx2[1], dx * b.idx2[0]);
+   if (dim == 3) t = fma(fma(-2.0, c, zp) + zm, b.idx2[2], t);
+   return t;
+}
+
 /* L[u] from lap u for the three operators (Poisson t - s, conformal factor
  * t + 2 pi s u^5, lapse t - s u; num.f:85-123 pattern) and, in c, the FP32
  * derivative of the non-Laplacian part (5 * 2 pi s u^4, -s, 0) */
@@ -98,11 +144,11 @@ __device__ __forceinline__ double opjac(int pde, double t, double uc, double s, 
 {
    if (pde == 1) {
       double p2 = uc * uc, a = TWO_PI * s * (p2 * p2);
-      c = 5.f * (float)a;
+      c = 5.f * d2f(a);
       return fma(a, uc, t);
    }
    if (pde == 2) {
-      c = -(float)s;
+      c = -d2f(s);
       return fma(-s, uc, t);
    }
    c = 0.f;
@@ -113,11 +159,13 @@ __device__ __forceinline__ double opjac(int pde, double t, double uc, double s, 
  * (amrd/mg.c:271-314) fused with the FP64 defect of the pre-smoothing block:
  *     rhs = cmask_child ? -res*w0_r + L[u] : 0,   lop = u,
  *     D = rhs - L[u], C at relaxed points.
- * E is 0 on entry (every block ends by clearing it). */
+ * E is 0 on entry (every block ends by clearing it). With cover = 1 only
+ * the level's cover tiles are visited: elsewhere rhs stays 0 and D is the
+ * FP32 update k_defect32 made at the end of the previous post-smoothing. */
 __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                   double w0_r)
+                                                   double w0_r, int cover)
 {
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_tile tl = cover ? lv.ctiles[blockIdx.x] : lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
@@ -131,28 +179,31 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
    float *__restrict__ wc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int kz = dim == 3 ? lv.tz : 1;
+   long p = i + sy * j + sz * tl.k0;
+   double zm = (dim == 3 && tl.k0 > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
-   for (int kk = 0; kk < PGB_TZ; kk++) {
+   for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
       const int k = tl.k0 + kk;
       if (kk >= kz || k >= b.n[2]) continue;
-      const long p = i + sy * j + sz * k;
+      const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
       const int cm = b.cmask_child[p];
       const bool in = interior32(b, i, j, k, dim);
       const bool rl = in && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p]);
-      const double uc = u[p];
       double r = 0.0;
       if (in && (cm || rl)) {
          float c;
-         const double l = opjac(pde, lapm(b, u, p, sy, sz, dim), uc, src[p], c);
+         const double l = opjac(pde, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c);
          if (cm) r = fma(-res[p], w0_r, l);
          if (rl) {
-            wd[p] = (float)(r - l);
+            wd[p] = d2f(r - l);
             wc[p] = c;
          }
       } else if (cm)
          r = -res[p] * w0_r;
       rhs[p] = r;
       lop[p] = uc;
+      zm = uc;
+      uc = zp;
    }
 }
 
@@ -262,10 +313,42 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
    }
 }
 
+/* D = D - (lap E + C E) at the relaxed points, FP32, before the update that
+ * adds E to u: the defect of u + E, linearised, for the next cycle's
+ * pre-smoothing on a level whose points outside the cover tiles do not
+ * change in between (no sync, no injection there). The next FP64 residual
+ * (after that pre-smoothing) is computed from u itself. */
+__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const float *__restrict__ e = b.w32[W_E];
+   const float *__restrict__ cc = b.w32[W_C];
+   float *__restrict__ dd = b.w32[W_D];
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
+   const int kz = dim == 3 ? lv.tz : 1;
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + kk;
+      if (kk >= kz || k >= b.n[2]) continue;
+      const long p = i + sy * j + sz * k;
+      if (!relaxed32(b, i, j, k, p, dim)) continue;
+      const float ec = e[p];
+      float t = (e[p + 1] - 2.f * ec + e[p - 1]) * ix + (e[p + sy] - 2.f * ec + e[p - sy]) * iy;
+      if (dim == 3) t += (e[p + sz] - 2.f * ec + e[p - sz]) * iz;
+      dd[p] = dd[p] - (t + cc[p] * ec);
+   }
+}
+
 /* End of a smoothing block: u += E (FP64) and E = 0. After an interpolated
  * coarse-grid correction (post = 1) the points the smoother does not relax
  * take the FP64 correction the interpolation left in res, plus whatever a
- * sync of E brought in: u += res + (E - RN32(res)). */
+ * sync of E brought in: u += res + (E - d2f(res)), exactly res when E still
+ * holds the d2f(res) the interpolation wrote. */
 __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
@@ -281,10 +364,10 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
       const int k = tl.k0 + kk;
       if (kk >= kz || k >= b.n[2]) continue;
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
-      double corr = (double)e[p];
+      double corr = f2d(e[p]);
       if (post && !relaxed32(b, i, j, k, p, lv.dim)) {
          const double r = res[p];
-         corr += r - (double)(float)r;
+         corr += r - f2d(d2f(r));
       }
       u[p] += corr;
       e[p] = 0.f;
@@ -430,13 +513,13 @@ __global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dle
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       const double r = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) * inv_w0;
       b.f[PGB_F_RES][p] = r;
-      b.w32[W_X][p] = (float)r;
+      b.w32[W_X][p] = d2f(r);
    }
 }
 
 /* FP64 interpolation of the coarse res at window point (a, bb, c) of op o
  * (dminterp3d's line order: i, then j, then k) */
-__device__ double interp_point64(const pgb_interp_op &o, const pgb_dbox &s, int a, int bb, int c, int dim)
+__device__ __noinline__ double interp_point64(const pgb_interp_op &o, const pgb_dbox &s, int a, int bb, int c, int dim)
 {
    const double *__restrict__ u = s.f[PGB_F_RES];
    int ax[4], ay[4], az[4];
@@ -464,8 +547,8 @@ __device__ double interp_point64(const pgb_interp_op &o, const pgb_dbox &s, int 
  * interpolation of the coarse res into res (k_update adds it) and its FP32
  * value into E, which the smoother reads as a neighbour. FP64 issues at a
  * small fraction of the FP32 rate, so FP64 points are kept in dense warps:
- * on boxes whose interior is all relaxed this kernel does the face rows in
- * FP64 and leaves the two x-ends of the other rows to k_interp_xedge. */
+ * on boxes whose interior is all relaxed this kernel leaves the face rows
+ * and the two x-ends of the other rows to k_interp_edges. */
 __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
 {
    const pgb_interp_op o = ops[blockIdx.z];
@@ -487,14 +570,14 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
          const long pd = lin32(d, fi, fj, fk);
          bool fp64;
          if (allrel) {
-            if (!face && (fi == 1 || fi == d.n[0])) continue;   /* k_interp_xedge */
-            fp64 = face;
+            if (face || fi == 1 || fi == d.n[0]) continue;   /* k_interp_edges */
+            fp64 = false;
          } else
             fp64 = !relaxed32(d, fi - 1, fj - 1, fk - 1, pd, dim);
          if (fp64) {
             const double v = interp_point64(o, s, a, bb, c, dim);
             d.f[PGB_F_RES][pd] = v;
-            d.w32[W_E][pd] = (float)v;
+            d.w32[W_E][pd] = d2f(v);
             continue;
          }
          int ax[4];
@@ -514,16 +597,88 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
    }
 }
 
-/* the x-ends (fi = 1, n) of the non-face rows of ops into boxes whose
- * interior is all relaxed, in FP64, one point per thread */
-__global__ void k_interp_xedge(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
+/* k_interp_mixed for ops of ratio 2 and linear order (every MG hierarchy
+ * with the default interpolation): the FP32 value of a fine point is the mean
+ * of its (up to 8 distinct) coarse corners, counted with multiplicity. */
+__global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
+{
+   const pgb_interp_op o = ops[blockIdx.z];
+   const pgb_dbox &s = boxes[o.src_box];
+   const pgb_dbox &d = boxes[o.dst_box];
+   const bool allrel = d.flags & PGB_BOX_BDY_INTERIOR;
+   const float *__restrict__ x = s.w32[W_X];
+   float *__restrict__ e = d.w32[W_E];
+   double *__restrict__ res = d.f[PGB_F_RES];
+   const long sny = s.n[0], snz = (long)s.n[0] * s.n[1];
+   const long dny = d.n[0], dnz = (long)d.n[0] * d.n[1];
+   for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
+      const int bb = row % o.njb, c = row / o.njb;
+      const int fj = o.j2 + bb, fk = o.k2 + c;
+      const bool face = fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]));
+      if (allrel && face) continue;
+      const int ty = o.j2b - 1 + bb, tz = dim == 3 ? o.k2b - 1 + c : 0;
+      const long oy = (ty & 1) ? sny : 0, oz = (tz & 1) ? snz : 0;
+      const long rowc = (o.j1i - 1 + (ty >> 1)) * sny + (dim == 3 ? (o.k1i - 1 + (tz >> 1)) * snz : 0);
+      const long rowf = (long)(fj - 1) * dny + (long)(fk - 1) * dnz;
+      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+         const int fi = o.i2 + a;
+         const long pd = rowf + fi - 1;
+         const int tx = o.i2b - 1 + a, ox = tx & 1;
+         if (allrel) {
+            if (face || fi == 1 || fi == d.n[0]) continue;   /* k_interp_edges */
+         } else if (!relaxed32(d, fi - 1, fj - 1, fk - 1, pd, dim)) {
+            const double *c0 = s.f[PGB_F_RES] + rowc + (o.i1i - 1 + (tx >> 1));
+            const double v = 0.125 * (((c0[0] + c0[ox]) + (c0[oy] + c0[ox + oy])) +
+                                      ((c0[oz] + c0[ox + oz]) + (c0[oy + oz] + c0[ox + oy + oz])));
+            res[pd] = v;
+            e[pd] = d2f(v);
+            continue;
+         }
+         const float *c0 = x + rowc + (o.i1i - 1 + (tx >> 1));
+         const float v = ((c0[0] + c0[ox]) + (c0[oy] + c0[ox + oy])) +
+                         ((c0[oz] + c0[ox + oz]) + (c0[oy + oz] + c0[ox + oy + oz]));
+         e[pd] = 0.125f * v;
+      }
+   }
+}
+
+/* The FP64 points of ops into boxes whose interior is all relaxed: the rows
+ * on a box face (j or k at the box boundary), blockIdx.y < 2*(njb+nkb)
+ * picking the face and the row on it, and, for the remaining blockIdx.y,
+ * the two x-ends (fi = 1, n) of the other rows, one per thread. */
+__global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, int dim)
 {
    const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    if (!(d.flags & PGB_BOX_BDY_INTERIOR)) return;
+   const int y = blockIdx.y, nface = 2 * (o.njb + o.nkb);
+   if (y < nface) {
+      int bb, c;
+      if (y < 2 * o.nkb) {
+         bb = ((y / o.nkb) ? d.n[1] : 1) - o.j2;
+         c = y % o.nkb;
+      } else {
+         if (dim != 3) return;
+         const int y2 = y - 2 * o.nkb;
+         c = ((y2 / o.njb) ? d.n[2] : 1) - o.k2;
+         bb = y2 % o.njb;
+         const int fj = o.j2 + bb;
+         if (fj == 1 || fj == d.n[1]) return;   /* done as a j face */
+      }
+      if (bb < 0 || bb >= o.njb || c < 0 || c >= o.nkb) return;
+      const int fj = o.j2 + bb, fk = o.k2 + c;
+      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+         const long pd = lin32(d, o.i2 + a, fj, fk);
+         const double v = interp_point64(o, s, a, bb, c, dim);
+         d.f[PGB_F_RES][pd] = v;
+         d.w32[W_E][pd] = d2f(v);
+      }
+      return;
+   }
+   if (blockIdx.x) return;
    const int rows = o.njb * o.nkb;
-   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * rows; q += gridDim.x * blockDim.x) {
+   for (int q = (y - nface) * blockDim.x + threadIdx.x; q < 2 * rows; q += (gridDim.y - nface) * blockDim.x) {
       const int row = q >> 1;
       const int a = (q & 1) ? d.n[0] - o.i2 : 1 - o.i2;
       if (a < 0 || a >= o.nib) continue;
@@ -533,7 +688,7 @@ __global__ void k_interp_xedge(const pgb_dbox *boxes, const pgb_interp_op *ops, 
       const long pd = lin32(d, o.i2 + a, fj, fk);
       const double v = interp_point64(o, s, a, bb, c, dim);
       d.f[PGB_F_RES][pd] = v;
-      d.w32[W_E][pd] = (float)v;
+      d.w32[W_E][pd] = d2f(v);
    }
 }
 
@@ -575,18 +730,25 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    double acc = 0;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    const int kz = dim == 3 ? lv.tz : 1;
+   if (i < b.n[0] && j < b.n[1]) {
+      long p = i + sy * j + sz * tl.k0;
+      double zm = (dim == 3 && tl.k0 > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
-   for (int kk = 0; kk < PGB_TZ; kk++) {
-      const int k = tl.k0 + kk;
-      if (kk >= kz || !interior32(b, i, j, k, dim)) continue;
-      const long p = i + sy * j + sz * k;
-      if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
-      float c;
-      const double r = opjac(pde, lapm(b, u, p, sy, sz, dim), u[p], src[p], c) - rhs[p];
-      res[p] = r;
-      wd[p] = (float)(-r);
-      wc[p] = c;
-      acc = fma(r, r, acc);
+      for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
+         const int k = tl.k0 + kk;
+         if (kk >= kz || k >= b.n[2]) continue;
+         const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
+         if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
+            float c;
+            const double r = opjac(pde, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c) - rhs[p];
+            res[p] = r;
+            wd[p] = d2f(-r);
+            wc[p] = c;
+            acc = fma(r, r, acc);
+         }
+         zm = uc;
+         uc = zp;
+      }
    }
    acc = block_sum32(acc, sm);
    if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
@@ -793,12 +955,20 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
 }
 
 /* ------------------------------------------------------------ launchers -- */
-extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
+extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover,
                                 void *stream)
 {
-   if (!lv.ntiles) return 0;
-   k_fas_defect<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   const int n = cover ? lv.nctiles : lv.ntiles;
+   if (!n) return 0;
+   k_fas_defect<<<n, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r, cover);
    return check32("fas_defect");
+}
+
+extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   k_defect32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   return check32("defect32");
 }
 
 /* nsweep FP32 sweeps of level L, fuse sweeps per launch (1 or 2) */
@@ -873,15 +1043,30 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
          const pgb_interp_op *hb = h + p->batch_start[bt] + c0;
          dim3 g;
          long mr = 1;
+         int lin2 = 1;
          row_grid(hb, m, g);
-         k_interp_mixed<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
-         if (check32("interp_mixed")) return 1;
-         for (int i = 0; i < m; i++)
+         for (int i = 0; i < m; i++) {
             if ((long)hb[i].njb * hb[i].nkb > mr) mr = (long)hb[i].njb * hb[i].nkb;
-         long gx = (2 * mr + 127) / 128;
-         k_interp_xedge<<<dim3((unsigned)(gx > 65535 ? 65535 : gx), 1, (unsigned)m), 128, 0,
-                          (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
-         if (check32("interp_xedge")) return 1;
+            if (hb[i].irho != 2 || (hb[i].ord != 2 && (hb[i].nii >= 4 || hb[i].nji >= 4 || (dim == 3 && hb[i].nki >= 4))))
+               lin2 = 0;
+         }
+         if (lin2)
+            k_interp_lin2<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+         else
+            k_interp_mixed<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+         if (check32("interp_mixed")) return 1;
+         {
+            int mi = 1;
+            long mf = 1;
+            for (int i = 0; i < m; i++) {
+               if (hb[i].nib > mi) mi = hb[i].nib;
+               if (2L * (hb[i].njb + hb[i].nkb) > mf) mf = 2L * (hb[i].njb + hb[i].nkb);
+            }
+            long gy = mf + (2 * mr + 127) / 128;   /* face rows, then x-end chunks */
+            k_interp_edges<<<dim3((unsigned)((mi + 127) / 128), (unsigned)(gy > 65535 ? 65535 : gy), (unsigned)m),
+                             128, 0, (cudaStream_t)stream>>>(d + p->batch_start[bt] + c0, boxes, dim);
+            if (check32("interp_edges")) return 1;
+         }
       }
    }
    return 0;

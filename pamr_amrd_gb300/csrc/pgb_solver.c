@@ -42,6 +42,8 @@ struct pgb_solver {
    int prepared;            /* pgb_prepare ran after the last change of an input grid */
    int fuse[PGB_MAXLEV + 1]; /* mixed form: FP32 sweeps per launch on levels without syncs */
    int tuned;               /* the autotuner has run */
+   int dnext[PGB_MAXLEV + 1]; /* mixed form: pre-smoothing defect from the FP32 update (see
+                               k_defect32) outside the cover tiles */
    cudaGraphExec_t gexec;   /* one captured V-cycle (+ read-back of the residual) */
    int graph_ok;
    long long graph_kernels; /* kernel launches in the captured V-cycle */
@@ -659,6 +661,19 @@ int pgb_prepare(pgb_solver *s)
       if (pgb_k_residual_fast(s->dbox, s->lv[s->h.nlev], s->h.pde, s->sc,
                               norm_slot(s, s->h.nlev, N_RESID), 0, s->stream))
          return fail(11, "%s", pgb_dev_error32());
+      /* Levels below the finest whose cover tiles are a minority, with no
+       * sync between boxes: between a post-smoothing and the next
+       * pre-smoothing their points outside the cover tiles do not change,
+       * so the pre-smoothing defect there is carried over in FP32; the
+       * first one is computed here. */
+      for (L = 2; L < s->h.nlev; L++) {
+         const pgb_hier *h = &s->h;
+         s->dnext[L] = h->prm.pre_swp > 0 && !h->sync[L][0].nops && !h->sync[L][1].nops &&
+                       2 * s->lv[L].nctiles < s->lv[L].ntiles;
+         if (s->dnext[L] &&
+             pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, h->prm.w0_r, 0, s->stream))
+            return fail(11, "%s", pgb_dev_error32());
+      }
    }
    CU(cudaMemsetAsync(s->d_citers, 0, sizeof(int), s->stream));
    s->prepared = 1;
@@ -789,7 +804,7 @@ static int vcycle_mixed(pgb_solver *s)
          if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
-         else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
+         else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
       }
       if (L > 1 && p->pre_swp > 0) {
          if (sweeps32(s, L, p->pre_swp)) return 11;
@@ -802,6 +817,7 @@ static int vcycle_mixed(pgb_solver *s)
          KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
          if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, s->stream));
          if (sweeps32(s, L, p->pst_swp)) return 11;
+         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 1, s->stream));
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       } else if (lvl_coarsest(s, L)) {
