@@ -285,7 +285,9 @@ def main():
     big = max(range(1, smx.num_levels() + 1),
               key=lambda L: max(smx.box_info(L, b)["shape"][0] for b in range(smx.level_nbox(L))))
     flush.fill_(1.0)
+    torch.cuda.nvtx.range_push("time_relax_mixed")
     ms_sweep, bytes_sweep = smx.time_relax(big, reps=20)
+    torch.cuda.nvtx.range_pop()
     ms64_sweep, bytes64_sweep = s64.time_relax(big, reps=10)
     achieved = bytes_sweep / (ms_sweep / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()

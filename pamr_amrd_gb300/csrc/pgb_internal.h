@@ -43,6 +43,7 @@ typedef struct {
    double dx2[3];                /* (x(2)-x(1))^2 per dimension */
    double idx2[3];               /* 1/dx2 when PGB_BOX_POW2DX */
    double j0;                    /* -2/dx2 - 2/dy2 [- 2/dz2] */
+   float fidx2[3], fj0;          /* FP32 copies of idx2 and j0 (mixed form) */
 } pgb_dbox;
 
 /* a tile of a box processed by one CTA */

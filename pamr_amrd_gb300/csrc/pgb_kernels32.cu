@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
    const float *__restrict__ dd = b.w32[W_D];
    const float *__restrict__ cc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
-   const float j0 = (float)b.j0;
+   const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
+   const float j0 = b.fj0;
    const int j = tl.j0 + threadIdx.y;
    const int kz = dim == 3 ? lv.rtz : 1;
 #pragma unroll
@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    float *e = b.w32[W_E];
    const float *dd = b.w32[W_D], *cc = b.w32[W_C];
-   const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
-   const float j0 = (float)b.j0;
+   const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
+   const float j0 = b.fj0;
    const bool allbdy = b.flags & PGB_BOX_BDY_INTERIOR;
    const int t = threadIdx.x + threadIdx.y * PGB_TX;
    const int gi0 = tl.i0 - H, gj0 = tl.j0 - H, gk0 = tl.k0 - hz;
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
    const float *__restrict__ cc = b.w32[W_C];
    float *__restrict__ dd = b.w32[W_D];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   const float ix = (float)b.idx2[0], iy = (float)b.idx2[1], iz = (float)b.idx2[2];
+   const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
    const int kz = dim == 3 ? lv.tz : 1;
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
@@ -823,7 +823,7 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
  * The loop also stops once the norm has not improved for three sweeps (the
  * FP64 rounding floor). */
 #define CM_MAXB 16
-#define CMT 1024
+#define CMT 256
 __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                         const pgb_copy_op *sync_ops, int nsync,
                                                         pgb_coarsest_args a, pgb_trace *trace)
@@ -873,7 +873,7 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
          const long sy = bx.n[0], sz = (long)bx.n[0] * bx.n[1];
          const long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
          const long hw = (ni + 1) / 2, nslot = hw * nj * nk;   /* one slot per point of a colour */
-         const float j0 = (float)bx.j0;
+         const float j0 = bx.fj0;
          double acc = 0;
          for (int pass = 0; pass < 2; pass++) {
             for (long q = t; q < nslot; q += CMT) {

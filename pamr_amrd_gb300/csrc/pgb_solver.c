@@ -218,7 +218,7 @@ static int level_tables(pgb_solver *s, int L, int tz)
    int nb = h->lev[L].nbox, nct;
    int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
    int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
-   int rtz = choose_tz(h, L, 2 * PGB_TX);
+   int rtz = tz;
    int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
    int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
    size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
@@ -334,6 +334,8 @@ static int setup_device(pgb_solver *s)
       }
       if (h->dim == 3) db->j0 = -2 / dx2[0] - 2 / dx2[1] - 2 / dx2[2];
       else db->j0 = -2 / dx2[0] - 2 / dx2[1];
+      for (d = 0; d < 3; d++) db->fidx2[d] = (float)db->idx2[d];
+      db->fj0 = (float)db->j0;
    }
    free(fo);
    free(w32o);
