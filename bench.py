@@ -126,9 +126,10 @@ def measured_peak_hbm():
 
 
 def ncu_traffic():
-    """dram bytes per relax sweep of the 129^3 level from the committed ncu
-    summary (profiles/relax_traffic.txt: 'bytes_per_sweep=<n>'), if any"""
-    p = os.path.join(ROOT, "profiles", "relax_traffic.txt")
+    """dram bytes per FP32 sweep (two colour passes) of the 129^3 level from
+    the committed ncu summary (profiles/k_relax32_129cube_traffic.txt:
+    'bytes_per_sweep=<n>'), if any"""
+    p = os.path.join(ROOT, "profiles", "k_relax32_129cube_traffic.txt")
     try:
         for line in open(p):
             if line.startswith("bytes_per_sweep="):
