@@ -198,6 +198,25 @@ int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, int nz1, int 
                    int nk, int si1, int sj1, int sk1, int irho, int jrho, int krho, int ord,
                    void *stream);
 
+/* Excision variants (do_ex = 1 in the Fortran): chr1 is the mask of u1 on
+ * the device (a point is excised where chr1 == ex). dmhwr3d_ex and
+ * dmfwr3d_ex replace dmhwr3d/dmfwr3d(..., chr1, ex, 1) (src/m_util_r8.f:
+ * 649-723, 733-949); dminterp3d_ex replaces dminterp3d(..., chr1, ex, 1)
+ * (src/m_util_r8.f:473-637 with dvi2q1d_ex/dvi4q1d_ex) and, like it,
+ * overwrites parts of u2's excised zone. */
+int pgb_dmhwr3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                   int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                   int si1, int sj1, int sk1, int si2, int sj2, int sk2, const double *chr1,
+                   double ex, void *stream);
+int pgb_dmfwr3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                   int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                   int si1, int sj1, int sk1, int si2, int sj2, int sk2, const double *chr1,
+                   double ex, void *stream);
+int pgb_dminterp3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                      int nz2, int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj,
+                      int nk, int si1, int sj1, int sk1, int irho, int jrho, int krho, int ord,
+                      const double *chr1, double ex, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

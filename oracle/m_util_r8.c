@@ -9,9 +9,16 @@
  * 1-based indices, same loop nests, same left-to-right expression order, so
  * gcc with -ffp-contract=off reproduces the Fortran arithmetic exactly.
  *
- * Excision variants (`_ex`, do_ex=1) and the evolution-only routines
- * (dmdiss3d, linbnd3d, dmrepop3d1, dmrepop3dc1) are not on the elliptic path
- * and abort if reached.
+ * The excision variants (do_ex=1: dvi2q1d_ex, dvi4q1d_ex, init_chrt,
+ * and_chrt, the excised paths of dminterp3d and dmhwr3d, dmfwr3d_ex) are
+ * restated too, including two quirks of the Fortran: dmfwr3d_ex's k-only
+ * branch adds w3d(i,1,k) (the segment index i, read through the array's
+ * column-major storage; an index past its 27 entries, undefined in the
+ * Fortran, counts as weight 0 here) and dvi4q1d_ex's right-side
+ * extrapolation tests i <= i1s-4*s1. No Fortran compiler is available, so
+ * these are pinned by known-answer tests, not by running the reference.
+ * The evolution-only routines (dmdiss3d, linbnd3d, dmrepop3d1, dmrepop3dc1)
+ * are not on the elliptic path and abort if reached.
  *
  * Optional call log: when mur8_log_enabled is set, every call records its
  * kernel id and index arguments so a test can compare the reference's
@@ -157,7 +164,184 @@ static void dviq1d(int ord, double *v, int i12, int n12, int n, int rho, int s1,
    else dvi4q1d(v, v, i12, i12, n12, n12, n, rho, s1, s2);
 }
 
-/* src/m_util_r8.f:473-637 (do_ex=0) */
+/* src/m_util_r8.f:368-421: linear interpolation with excision. v1 and v2
+ * alias in every call dminterp3d makes; chr1/i3/s3 describe v1's mask on
+ * the coarse grid. Writes into the excised zone. */
+static void dvi2q1d_ex(double *v1, double *v2, int i1, int i2, int n1, int n2, int n, int irho,
+                       int s1, int s2, const double *chr1, int i3, int n3, int s3, double ex)
+{
+   double c0, c1, sg;
+   int i, j, i10, i30;
+   (void)n2; (void)n3;
+   for (i = 1; i <= n; i++) {
+      i10 = (i - 1) * s1 + i1;
+      i30 = (i - 1) * s3 + i3;
+      if (A1(chr1, i30) == ex) {
+         if (i10 > 3 * s1 && A1(chr1, i30 - s3) != ex && A1(chr1, i30 - 2 * s3) != ex &&
+             A1(chr1, i30 - 3 * s3) != ex)
+            A1(v1, i10) = 3 * (A1(v1, i10 - s1) - A1(v1, i10 - 2 * s1)) + A1(v1, i10 - 3 * s1);
+         else if (i10 <= (n1 - 3 * s1) && A1(chr1, i30 + s3) != ex && A1(chr1, i30 + 2 * s3) != ex &&
+                  A1(chr1, i30 + 3 * s3) != ex)
+            A1(v1, i10) = 3 * (A1(v1, i10 + s1) - A1(v1, i10 + 2 * s1)) + A1(v1, i10 + 3 * s1);
+         else if (i10 > 2 * s1 && A1(chr1, i30 - s3) != ex && A1(chr1, i30 - 2 * s3) != ex)
+            A1(v1, i10) = 2 * A1(v1, i10 - s1) - A1(v1, i10 - 2 * s1);
+         else if (i10 <= (n1 - 2 * s1) && A1(chr1, i30 + s3) != ex && A1(chr1, i30 + 2 * s3) != ex)
+            A1(v1, i10) = 2 * A1(v1, i10 + s1) - A1(v1, i10 + 2 * s1);
+         else if (i10 > s1 && A1(chr1, i30 - s3) != ex)
+            A1(v1, i10) = A1(v1, i10 - s1);
+         else if (i10 <= (n1 - s1) && A1(chr1, i30 + s3) != ex)
+            A1(v1, i10) = A1(v1, i10 + s1);
+      }
+      A1(v2, irho * (i - 1) * s2 + i2) = A1(v1, i10);
+   }
+   for (j = 1; j <= irho - 1; j++) {
+      sg = (j * 1.0) / irho;
+      c0 = 1 - sg;
+      c1 = sg;
+      for (i = 0; i <= n - 2; i++) {
+         i10 = (irho * i + j) * s2 + i2;
+         A1(v2, i10) = c0 * A1(v1, i * s1 + i1) + c1 * A1(v1, (i + 1) * s1 + i1);
+      }
+   }
+}
+
+/* src/m_util_r8.f:153-319: cubic interpolation with excision; falls back
+ * to dvi2q1d_ex first when a non-excised run of the (extended) coarse line
+ * is shorter than 4, then overwrites with the cubic stencils that apply */
+static void dvi4q1d_ex(double *v1, double *v2, int i1, int i2, int n1, int n2, int n, int irho,
+                       int s1, int s2, const double *chr1, int i3, int n3, int s3, double ex)
+{
+   double c0[20], c1[20], c2[20], c3[20], sg;
+   int i, j, cn, j0, i1s, i1e, i10, i30, init_2;
+   if (irho > 20) {
+      fprintf(stderr, "dvi4q1d_ex : irho expected to be less than 20\n");
+      abort();
+   }
+   i = 3;
+   i1s = i1;
+   while (i > 0 && i1s > s1) {
+      i1s = i1s - s1;
+      i = i - 1;
+   }
+   i = 3;
+   i1e = i1 + (n - 1) * s1;
+   while (i > 0 && i1e < (n1 - s1)) {
+      i1e = i1e + s1;
+      i = i - 1;
+   }
+   cn = 0;
+   init_2 = 0;
+   for (i = i1s; i <= i1e; i += s1) {
+      if (A1(chr1, (i - i1) * s3 / s1 + i3) == ex || i == i1e) {
+         if (cn > 0 && cn < 4) init_2 = 1;
+         else cn = 0;
+      } else
+         cn = cn + 1;
+   }
+   if (init_2) dvi2q1d_ex(v1, v2, i1, i2, n1, n2, n, irho, s1, s2, chr1, i3, n3, s3, ex);
+
+#define CH(off) A1(chr1, i3 + s3 * ((off) - i1) / s1)
+   for (i = i1s; i <= i1e; i += s1) {
+      if (CH(i) == ex) {
+         if (i >= (i1s + 3 * s1) && CH(i - s1) != ex && CH(i - 2 * s1) != ex && CH(i - 3 * s1) != ex) {
+            if (i >= (i1s + 4 * s1) && CH(i - 4 * s1) != ex)
+               A1(v1, i) = 4 * (A1(v1, i - s1) + A1(v1, i - 3 * s1)) - 6 * A1(v1, i - 2 * s1) -
+                           A1(v1, i - 4 * s1);
+            else
+               A1(v1, i) = 3 * (A1(v1, i - s1) - A1(v1, i - 2 * s1)) + A1(v1, i - 3 * s1);
+         } else if (i <= (i1e - 3 * s1) && CH(i + s1) != ex && CH(i + 2 * s1) != ex &&
+                    CH(i + 3 * s1) != ex) {
+            if (i <= (i1s - 4 * s1) && CH(i + 4 * s1) != ex)
+               A1(v1, i) = 4 * (A1(v1, i + s1) + A1(v1, i + 3 * s1)) - 6 * A1(v1, i + 2 * s1) -
+                           A1(v1, i + 4 * s1);
+            else
+               A1(v1, i) = 3 * (A1(v1, i + s1) - A1(v1, i + 2 * s1)) + A1(v1, i + 3 * s1);
+         }
+      }
+      if (i >= i1 && i <= (i1 + (n - 1) * s1)) A1(v2, irho * ((i - i1) / s1) * s2 + i2) = A1(v1, i);
+   }
+#undef CH
+
+   for (j = 1; j <= irho - 1; j++) {   /* left boundary cells */
+      sg = (j * 1.0) / irho;
+      c0[j - 1] = MSIXTH * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
+      c1[j - 1] = HALF * sg * (sg - 2.0) * (sg - 3.0);
+      c2[j - 1] = MHALF * sg * (sg - 1.0) * (sg - 3.0);
+      c3[j - 1] = SIXTH * sg * (sg - 1.0) * (sg - 2.0);
+   }
+   for (i = 1; i <= n - 1; i++) {
+      i10 = (i - 1) * s1 + i1;
+      i30 = (i - 1) * s3 + i3;
+      j0 = (i - 1) * irho * s2 + i2;
+      if (i10 <= (i1e - 3 * s1) && A1(chr1, i30 + s3) != ex && A1(chr1, i30 + 2 * s3) != ex &&
+          ((i == 1 && i10 == i1s) ||
+           (i10 >= (i1s + s1) && A1(chr1, i30) != ex && A1(chr1, i30 - s3) == ex) ||
+           A1(chr1, i30) == ex))
+         for (j = 1; j <= irho - 1; j++)
+            A1(v2, j * s2 + j0) = c0[j - 1] * A1(v1, i10) + c1[j - 1] * A1(v1, s1 + i10) +
+                                  c2[j - 1] * A1(v1, 2 * s1 + i10) + c3[j - 1] * A1(v1, 3 * s1 + i10);
+   }
+   for (j = 1; j <= irho - 1; j++) {   /* right boundary cells */
+      sg = 2.0 + (j * 1.0) / irho;
+      c0[j - 1] = MSIXTH * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
+      c1[j - 1] = HALF * sg * (sg - 2.0) * (sg - 3.0);
+      c2[j - 1] = MHALF * sg * (sg - 1.0) * (sg - 3.0);
+      c3[j - 1] = SIXTH * sg * (sg - 1.0) * (sg - 2.0);
+   }
+   for (i = 1; i <= n - 1; i++) {
+      i10 = (i - 1) * s1 + i1;
+      i30 = (i - 1) * s3 + i3;
+      j0 = (i - 1) * irho * s2 + i2;
+      if (i10 >= (i1s + 2 * s1) && A1(chr1, i30 - s3) != ex &&
+          ((i == (n - 1) && i10 == (i1e - s1)) ||
+           (i10 <= (i1e - s1) && A1(chr1, i30) != ex && A1(chr1, i30 + s3) == ex)))
+         for (j = 1; j <= irho - 1; j++)
+            A1(v2, j * s2 + j0) = c0[j - 1] * A1(v1, i10 - 2 * s1) + c1[j - 1] * A1(v1, i10 - s1) +
+                                  c2[j - 1] * A1(v1, i10) + c3[j - 1] * A1(v1, i10 + s1);
+   }
+   for (j = 1; j <= irho - 1; j++) {   /* interior */
+      sg = 1.0 + (j * 1.0) / irho;
+      c0[j - 1] = MSIXTH * (sg - 1.0) * (sg - 2.0) * (sg - 3.0);
+      c1[j - 1] = HALF * sg * (sg - 2.0) * (sg - 3.0);
+      c2[j - 1] = MHALF * sg * (sg - 1.0) * (sg - 3.0);
+      c3[j - 1] = SIXTH * sg * (sg - 1.0) * (sg - 2.0);
+   }
+   for (i = 1; i <= n; i++) {
+      i10 = (i - 1) * s1 + i1;
+      i30 = (i - 1) * s3 + i3;
+      j0 = (i - 1) * irho * s2 + i2;
+      if (A1(chr1, i30) != ex && i10 >= (i1s + s1) && A1(chr1, i30 - s3) != ex &&
+          i10 <= (i1e - 2 * s1) && A1(chr1, i30 + s3) != ex)
+         for (j = 1; j <= irho - 1; j++)
+            A1(v2, j0 + j * s2) = c0[j - 1] * A1(v1, i10 - s1) + c1[j - 1] * A1(v1, i10) +
+                                  c2[j - 1] * A1(v1, i10 + s1) + c3[j - 1] * A1(v1, i10 + 2 * s1);
+   }
+}
+
+/* src/m_util_r8.f:426-456 */
+static void init_chrt(double *chrt, const double *chr1, int n, int s3)
+{
+   int i;
+   for (i = 1; i <= n; i++) A1(chrt, i) = A1(chr1, (i - 1) * s3 + 1);
+}
+
+static void and_chrt(double *chrt, const double *chr1, int n, int s3, double ex)
+{
+   int i;
+   for (i = 1; i <= n; i++) {
+      if (A1(chrt, i) == ex && A1(chr1, (i - 1) * s3 + 1) == ex) A1(chrt, i) = ex;
+      else A1(chrt, i) = ex + 1;
+   }
+}
+
+static void dviq1d_ex(int ord, double *v, int i12, int n12, int n, int rho, int s1, int s2,
+                      const double *chr, int i3, int n3, int s3, double ex)
+{
+   if (ord == 2) dvi2q1d_ex(v, v, i12, i12, n12, n12, n, rho, s1, s2, chr, i3, n3, s3, ex);
+   else dvi4q1d_ex(v, v, i12, i12, n12, n12, n, rho, s1, s2, chr, i3, n3, s3, ex);
+}
+
+/* src/m_util_r8.f:473-637 */
 void dminterp3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
                  int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
                  int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *pirho, int *pjrho,
@@ -170,7 +354,6 @@ void dminterp3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *p
    int i, j, k;
    int iv[24] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
                  ni, nj, nk, si1, sj1, sk1, irho, jrho, krho, ord, *do_ex, 0};
-   (void)chr1; (void)ex;
    log_call(MUR8_INTERP, u1, u2, iv, 24);
 
    if (i1 < 1 || (i1 + ni - 1) * si1 > nx1) return;
@@ -183,10 +366,54 @@ void dminterp3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *p
       fprintf(stderr, "dminterp3d: only ord=2,4 currently supported\n");
       abort();
    }
-   if (*do_ex == 1) not_on_path("dminterp3d with excision");
+   if (*do_ex == 1 && (nx1 > 3000 || ny1 > 3000 || nz1 > 3000)) {
+      fprintf(stderr, "dminterp3d: nmax too small\n");
+      abort();
+   }
 
    dmcopy3d(u1, u2, nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2, ni, nj, nk, si1, sj1,
             sk1, irho, jrho, krho);
+
+   if (*do_ex == 1) {
+      double exv = *ex, *chrt = (double *)malloc(sizeof(double) * 3000);
+      for (j = j2; j <= j2 + (nj - 1) * jrho; j += jrho)
+         for (k = k2; k <= k2 + (nk - 1) * krho; k += krho)
+            dviq1d_ex(ord, &A3(u2, nx2, ny2, 1, j, k), i2, nx2, ni, irho, irho, 1,
+                      &A3(chr1, nx1, ny1, 1, j1 + sj1 * (j - j2) / jrho, k1 + sk1 * (k - k2) / krho),
+                      i1, nx1, si1, exv);
+      if (!(nj == 1 && nk == 1)) {
+         for (i = i2; i <= i2 + (ni - 1) * irho; i++)
+            for (k = k2; k <= k2 + (nk - 1) * krho; k += krho) {
+               init_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho), 1, k1 + sk1 * ((k - k2) / krho)),
+                         ny1, nx1);
+               if ((i - i2) % irho != 0)
+                  and_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho + 1), 1,
+                                     k1 + sk1 * ((k - k2) / krho)), ny1, nx1, exv);
+               dviq1d_ex(ord, &A3(u2, nx2, ny2, i, 1, k), 1 + (j2 - 1) * nx2, nx2 * (ny2 - 1) + 1, nj,
+                         jrho, jrho * nx2, nx2, chrt, j1, ny1, sj1, exv);
+            }
+         if (nk != 1)
+            for (i = i2; i <= i2 + (ni - 1) * irho; i++)
+               for (j = j2; j <= j2 + (nj - 1) * jrho; j++) {
+                  init_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho), j1 + sj1 * ((j - j2) / jrho), 1),
+                            nz1, nx1 * ny1);
+                  if ((i - i2) % irho != 0)
+                     and_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho + 1),
+                                        j1 + sj1 * ((j - j2) / jrho), 1), nz1, nx1 * ny1, exv);
+                  if ((j - j2) % jrho != 0)
+                     and_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho),
+                                        j1 + sj1 * ((j - j2) / jrho + 1), 1), nz1, nx1 * ny1, exv);
+                  if ((j - j2) % jrho != 0 && (i - i2) % irho != 0)
+                     and_chrt(chrt, &A3(chr1, nx1, ny1, i1 + si1 * ((i - i2) / irho + 1),
+                                        j1 + sj1 * ((j - j2) / jrho + 1), 1), nz1, nx1 * ny1, exv);
+                  dviq1d_ex(ord, &A3(u2, nx2, ny2, i, j, 1), (k2 - 1) * nx2 * ny2 + 1,
+                            nx2 * ny2 * (nz2 - 1) + 1, nk, krho, krho * nx2 * ny2, nx2 * ny2, chrt,
+                            k1, nz1, sk1, exv);
+               }
+      }
+      free(chrt);
+      return;
+   }
 
    for (j = j2; j <= j2 + (nj - 1) * jrho; j += jrho)
       for (k = k2; k <= k2 + (nk - 1) * krho; k += krho)
@@ -207,7 +434,7 @@ void dminterp3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *p
                 nx2 * ny2 * (nz2 - 1) + 1, nk, krho, krho * nx2 * ny2, nx2 * ny2);
 }
 
-/* src/m_util_r8.f:649-723 (do_ex=0) */
+/* src/m_util_r8.f:649-723 */
 void dmhwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
               int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
               int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *psi2, int *psj2,
@@ -221,7 +448,6 @@ void dmhwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
    double sum;
    int iv[22] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
                  ni, nj, nk, si1, sj1, sk1, si2, sj2, sk2, *do_ex};
-   (void)chr1; (void)ex;
    log_call(MUR8_HWR, u1, u2, iv, 22);
 
    if (i1 < 1 || (i1 + (ni - 1) * si1) > nx1) return;
@@ -230,8 +456,7 @@ void dmhwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
    if (j2 < 1 || (j2 + (nj - 1) * sj2) > ny2) return;
    if (k1 < 1 || (k1 + (nk - 1) * sk1) > nz1) return;
    if (k2 < 1 || (k2 + (nk - 1) * sk2) > nz2) return;
-   if (*do_ex == 1) not_on_path("dmhwr3d with excision");
-
+#define C3(a, b, c) A3(chr1, nx1, ny1, a, b, c)
    for (i = 1; i <= ni; i++)
       for (j = 1; j <= nj; j++)
          for (k = 1; k <= nk; k++) {
@@ -241,29 +466,131 @@ void dmhwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
             w = 0;
             sum = 0;
             if (i0 > 1 && i0 <= (nx1 - 1)) {
-               w = w + 4;
-               sum = sum + A3(u1, nx1, ny1, i0 - 1, j0, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
-                     A3(u1, nx1, ny1, i0 + 1, j0, k0);
+               if (*do_ex == 0 || (C3(i0 - 1, j0, k0) != *ex && C3(i0, j0, k0) != *ex &&
+                                   C3(i0 + 1, j0, k0) != *ex)) {
+                  w = w + 4;
+                  sum = sum + A3(u1, nx1, ny1, i0 - 1, j0, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                        A3(u1, nx1, ny1, i0 + 1, j0, k0);
+               }
             }
             if (j0 > 1 && j0 <= (ny1 - 1)) {
-               w = w + 4;
-               sum = sum + A3(u1, nx1, ny1, i0, j0 - 1, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
-                     A3(u1, nx1, ny1, i0, j0 + 1, k0);
+               if (*do_ex == 0 || (C3(i0, j0 - 1, k0) != *ex && C3(i0, j0, k0) != *ex &&
+                                   C3(i0, j0 + 1, k0) != *ex)) {
+                  w = w + 4;
+                  sum = sum + A3(u1, nx1, ny1, i0, j0 - 1, k0) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                        A3(u1, nx1, ny1, i0, j0 + 1, k0);
+               }
             }
             if (k0 > 1 && k0 <= (nz1 - 1)) {
-               w = w + 4;
-               sum = sum + A3(u1, nx1, ny1, i0, j0, k0 - 1) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
-                     A3(u1, nx1, ny1, i0, j0, k0 + 1);
+               if (*do_ex == 0 || (C3(i0, j0, k0 - 1) != *ex && C3(i0, j0, k0) != *ex &&
+                                   C3(i0, j0, k0 + 1) != *ex)) {
+                  w = w + 4;
+                  sum = sum + A3(u1, nx1, ny1, i0, j0, k0 - 1) + 2 * A3(u1, nx1, ny1, i0, j0, k0) +
+                        A3(u1, nx1, ny1, i0, j0, k0 + 1);
+               }
             }
-            if (w > 0)
+            if (*do_ex == 1 && C3(i0, j0, k0) == *ex)
+               A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) = 0;
+            else if (w > 0)
                A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) = sum / w;
             else
                A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) =
                   A3(u1, nx1, ny1, i0, j0, k0);
          }
+#undef C3
 }
 
-/* src/m_util_r8.f:733-830 (do_ex=0) */
+/* src/m_util_r8.f:835-949, called by dmfwr3d when do_ex=1 (bounds already
+ * checked) */
+static const int W3D[27] = {1, 2, 1, 2, 4, 2, 1, 2, 1, 2, 4, 2, 4, 8, 4, 2, 4, 2, 1, 2, 1, 2, 4, 2, 1, 2, 1};
+/* Fortran w3d(a,b,c) through its column-major storage */
+static int w3d(int a, int b, int c)
+{
+   int o = (a - 1) + 3 * (b - 1) + 9 * (c - 1);
+   return o >= 0 && o < 27 ? W3D[o] : 0;
+}
+
+static void dmfwr3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, int nx2, int ny2,
+                       int i1, int j1, int k1, int i2, int j2, int k2, int ni, int nj, int nk,
+                       int si1, int sj1, int sk1, int si2, int sj2, int sk2, const double *chr1,
+                       double ex)
+{
+   int i, j, k, i0, j0, k0, im, jm, km, ip, jp, kp, i01, j01, k01, w;
+   double sum;
+   (void)nz1;
+#define U(a, b, c) A3(u1, nx1, ny1, a, b, c)
+#define C3(a, b, c) A3(chr1, nx1, ny1, a, b, c)
+   for (i = 1; i <= ni; i++)
+      for (j = 1; j <= nj; j++)
+         for (k = 1; k <= nk; k++) {
+            i0 = i1 + (i - 1) * si1;
+            j0 = j1 + (j - 1) * sj1;
+            k0 = k1 + (k - 1) * sk1;
+            im = i0 - 1; jm = j0 - 1; km = k0 - 1;
+            ip = i0 + 1; jp = j0 + 1; kp = k0 + 1;
+            sum = 0;
+            w = 0;
+            if (i0 > 1 && i0 <= (nx1 - 1) && j0 > 1 && j0 <= (ny1 - 1) && k0 > 1 && k0 <= (nz1 - 1)) {
+               for (i01 = im; i01 <= ip; i01++)
+                  for (j01 = jm; j01 <= jp; j01++)
+                     for (k01 = km; k01 <= kp; k01++)
+                        if (C3(i01, j01, k01) != ex) {
+                           sum = sum + w3d(i01 - im + 1, j01 - jm + 1, k01 - km + 1) * U(i01, j01, k01);
+                           w = w + w3d(i01 - im + 1, j01 - jm + 1, k01 - km + 1);
+                        }
+            } else if (i0 > 1 && i0 <= (nx1 - 1) && j0 > 1 && j0 <= (ny1 - 1)) {
+               for (i01 = im; i01 <= ip; i01++)
+                  for (j01 = jm; j01 <= jp; j01++)
+                     if (C3(i01, j01, k0) != ex) {
+                        sum = sum + w3d(i01 - im + 1, j01 - jm + 1, 1) * U(i01, j01, k0);
+                        w = w + w3d(i01 - im + 1, j01 - jm + 1, 1);
+                     }
+            } else if (j0 > 1 && j0 <= (ny1 - 1) && k0 > 1 && k0 <= (nz1 - 1)) {
+               for (j01 = jm; j01 <= jp; j01++)
+                  for (k01 = km; k01 <= kp; k01++)
+                     if (C3(i0, j01, k01) != ex) {
+                        sum = sum + w3d(1, j01 - jm + 1, k01 - km + 1) * U(i0, j01, k01);
+                        w = w + w3d(1, j01 - jm + 1, k01 - km + 1);
+                     }
+            } else if (i0 > 1 && i0 <= (nx1 - 1) && k0 > 1 && k0 <= (nz1 - 1)) {
+               for (i01 = im; i01 <= ip; i01++)
+                  for (k01 = km; k01 <= kp; k01++)
+                     if (C3(i01, j0, k01) != ex) {
+                        sum = sum + w3d(i01 - im + 1, 1, k01 - km + 1) * U(i01, j0, k01);
+                        w = w + w3d(i01 - im + 1, 1, k01 - km + 1);
+                     }
+            } else if (i0 > 1 && i0 <= (nx1 - 1)) {
+               for (i01 = im; i01 <= ip; i01++)
+                  if (C3(i01, j0, k0) != ex) {
+                     sum = sum + w3d(i01 - im + 1, 1, 1) * U(i01, j0, k0);
+                     w = w + w3d(i01 - im + 1, 1, 1);
+                  }
+            } else if (j0 > 1 && j0 <= (ny1 - 1)) {
+               for (j01 = jm; j01 <= jp; j01++)
+                  if (C3(i0, j01, k0) != ex) {
+                     sum = sum + w3d(1, j01 - jm + 1, 1) * U(i0, j01, k0);
+                     w = w + w3d(1, j01 - jm + 1, 1);
+                  }
+            } else if (k0 > 1 && k0 <= (nz1 - 1)) {
+               for (k01 = km; k01 <= kp; k01++)
+                  if (C3(i0, j0, k01) != ex) {
+                     sum = sum + w3d(1, 1, k01 - km + 1) * U(i0, j0, k01);
+                     w = w + w3d(i, 1, k01 - km + 1);   /* as written in the Fortran */
+                  }
+            } else {
+               sum = U(i0, j0, k0);
+               w = 1;
+            }
+            if (w == 0 || C3(i0, j0, k0) == ex)
+               A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) = 0;
+            else
+               A3(u2, nx2, ny2, i2 + (i - 1) * si2, j2 + (j - 1) * sj2, k2 + (k - 1) * sk2) = sum / w;
+         }
+#undef U
+#undef C3
+}
+
+/* src/m_util_r8.f:733-830 */
 void dmfwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2, int *pny2,
               int *pnz2, int *pi1, int *pj1, int *pk1, int *pi2, int *pj2, int *pk2, int *pni,
               int *pnj, int *pnk, int *psi1, int *psj1, int *psk1, int *psi2, int *psj2,
@@ -277,7 +604,6 @@ void dmfwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
    double *d;
    int iv[22] = {nx1, ny1, nz1, nx2, ny2, nz2, i1, j1, k1, i2, j2, k2,
                  ni, nj, nk, si1, sj1, sk1, si2, sj2, sk2, *do_ex};
-   (void)chr1; (void)ex;
    log_call(MUR8_FWR, u1, u2, iv, 22);
 
    if (i1 < 1 || (i1 + (ni - 1) * si1) > nx1) return;
@@ -286,7 +612,11 @@ void dmfwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
    if (j2 < 1 || (j2 + (nj - 1) * sj2) > ny2) return;
    if (k1 < 1 || (k1 + (nk - 1) * sk1) > nz1) return;
    if (k2 < 1 || (k2 + (nk - 1) * sk2) > nz2) return;
-   if (*do_ex == 1) not_on_path("dmfwr3d with excision");
+   if (*do_ex == 1) {
+      dmfwr3d_ex(u1, u2, nx1, ny1, nz1, nx2, ny2, i1, j1, k1, i2, j2, k2, ni, nj, nk, si1, sj1, sk1,
+                 si2, sj2, sk2, chr1, *ex);
+      return;
+   }
 
 #define U(a, b, c) A3(u1, nx1, ny1, a, b, c)
    for (i = 1; i <= ni; i++)

@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libpamr_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"], "pgb_noalloc.cu": ["-fmad=false"],
-              "pgb_kernels32.cu": []}
+              "pgb_mutil_ex.cu": ["-fmad=false"], "pgb_kernels32.cu": []}
 C_SOURCES = ["pgb_plan.c", "pgb_solver.c"]
 
 

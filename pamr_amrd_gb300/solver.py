@@ -73,6 +73,9 @@ def lib(build: bool = True):
         for name in ("pgb_dmcopy3d", "pgb_dmhwr3d", "pgb_dmfwr3d"):
             getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp]
         L.pgb_dminterp3d.argtypes = [vp, vp] + [C.c_int] * 22 + [vp]
+        for name in ("pgb_dmhwr3d_ex", "pgb_dmfwr3d_ex"):
+            getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp, C.c_double, vp]
+        L.pgb_dminterp3d_ex.argtypes = [vp, vp] + [C.c_int] * 22 + [vp, C.c_double, vp]
         _lib = L
     return _lib
 

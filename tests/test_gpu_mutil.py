@@ -76,3 +76,74 @@ def test_device_interp_window(ord_, geom):
     torch.cuda.synchronize()
     assert rc == 0
     assert np.array_equal(d2.cpu().numpy(), want)
+
+
+# ------------------------------------------------------ excision (do_ex=1) --
+EX = 1.0
+
+
+def _mask(rng, n, nblobs=3):
+    """0/EX mask with a few excised balls (and a sprinkling of single points)"""
+    nx, ny, nz = n
+    X, Y, Z = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    m = np.zeros((nx, ny, nz))
+    for _ in range(nblobs):
+        c = [rng.uniform(0, nx), rng.uniform(0, ny), rng.uniform(0, nz)]
+        r = rng.uniform(0.8, 0.25 * min(nx, ny, max(nz, 4)))
+        m[(X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2 <= r * r] = EX
+    m[rng.random(m.shape) < 0.02] = EX
+    return np.ascontiguousarray(m.transpose(2, 1, 0)).reshape(-1)
+
+
+EX_RESTRICT = [
+    (17, 17, 17, 9, 9, 9, 1, 1, 1, 1, 1, 1, 9, 9, 9, 2, 2, 2, 1, 1, 1),
+    (33, 21, 1, 17, 11, 1, 3, 1, 1, 2, 1, 1, 14, 11, 1, 2, 2, 1, 1, 1, 1),
+    (21, 19, 15, 11, 10, 8, 1, 1, 1, 1, 1, 1, 11, 10, 8, 2, 2, 2, 1, 1, 1),
+]
+
+
+@pytest.mark.parametrize("kind", ["dmhwr3d", "dmfwr3d"])
+@pytest.mark.parametrize("args", EX_RESTRICT)
+def test_device_excised_restriction(kind, args):
+    rng = np.random.default_rng(3)
+    u1 = rng.standard_normal(args[0] * args[1] * args[2])
+    chr1 = _mask(rng, args[0:3])
+    u2 = rng.standard_normal(args[3] * args[4] * args[5])
+    want = u2.copy()
+    ex = C.c_double(EX)
+    getattr(_cpu(), kind + "_")(_dp(u1), _dp(want), *[_ip(v) for v in args], _dp(chr1), C.byref(ex), _ip(1))
+    d1, d2, dc = _dev(u1), _dev(u2), _dev(chr1)
+    rc = getattr(lib(), "pgb_" + kind + "_ex")(d1.data_ptr(), d2.data_ptr(), *args, dc.data_ptr(), EX, None)
+    torch.cuda.synchronize()
+    assert rc == 0
+    assert np.array_equal(d2.cpu().numpy(), want)
+
+
+# coarse grid, window (i1,j1,k1, ni,nj,nk) and the fine start, chosen so that
+# every mask index the routines read stays inside the coarse grid
+EX_INTERP = [
+    ((9, 9, 9), (1, 1, 1, 9, 9, 9), (1, 1, 1)),        # whole grid onto an aligned fine grid
+    ((13, 11, 1), (1, 1, 1, 13, 11, 1), (1, 1, 1)),    # 2-D
+    ((16, 15, 14), (5, 4, 5, 7, 8, 6), (9, 7, 9)),     # inner window, fine margin of 4 cells
+]
+
+
+@pytest.mark.parametrize("ord_", [2, 4])
+@pytest.mark.parametrize("geom", EX_INTERP)
+def test_device_excised_interp(ord_, geom):
+    (nx1, ny1, nz1), (i1, j1, k1, ni, nj, nk), (i2, j2, k2) = geom
+    rng = np.random.default_rng(4)
+    u1 = rng.standard_normal(nx1 * ny1 * nz1)
+    chr1 = _mask(rng, (nx1, ny1, nz1))
+    n2 = [i2 - 1 + (ni - 1) * 2 + 1 + (i2 - 1), j2 - 1 + (nj - 1) * 2 + 1 + (j2 - 1),
+          (k2 - 1 + (nk - 1) * 2 + 1 + (k2 - 1)) if nk > 1 else 1]
+    u2 = rng.standard_normal(n2[0] * n2[1] * n2[2])
+    want = u2.copy()
+    args = [nx1, ny1, nz1, *n2, i1, j1, k1, i2, j2, k2, ni, nj, nk, 1, 1, 1, 2, 2, 2, ord_]
+    ex = C.c_double(EX)
+    _cpu().dminterp3d_(_dp(u1), _dp(want), *[_ip(v) for v in args], _dp(chr1), C.byref(ex), _ip(1))
+    d1, d2, dc = _dev(u1), _dev(u2), _dev(chr1)
+    rc = lib().pgb_dminterp3d_ex(d1.data_ptr(), d2.data_ptr(), *args, dc.data_ptr(), EX, None)
+    torch.cuda.synchronize()
+    assert rc == 0
+    assert np.array_equal(d2.cpu().numpy(), want)
