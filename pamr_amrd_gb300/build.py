@@ -16,6 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpamr_gb300.so")
+LIB_F77 = os.path.join(os.path.dirname(LIB), "libpamr_gb300_f77.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"], "pgb_noalloc.cu": ["-fmad=false"],
@@ -77,6 +78,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-L" + libdir, "-lcudart",
                                                            "-Xlinker", "-rpath",
                                                            "-Xlinker", libdir]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: " + r.stdout + r.stderr)
+    # the Fortran-ABI drop-in (m_util_r8.h symbols on host arrays) over LIB
+    fsrc = os.path.join(CSRC, "pgb_f77.c")
+    if force or _stale(LIB_F77, [fsrc, LIB] + headers):
+        libdir = os.path.join(cuda, "lib64")
+        cmd = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-Wall",
+               "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(cuda, "include"),
+               fsrc, "-o", LIB_F77, "-L" + os.path.dirname(LIB), "-lpamr_gb300",
+               "-L" + libdir, "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + libdir]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: " + r.stdout + r.stderr)

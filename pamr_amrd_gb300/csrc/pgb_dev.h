@@ -73,6 +73,7 @@ typedef struct {
 } pgb_coarsest_args;
 
 const char *pgb_dev_error(void);
+void pgb_note_error(const char *msg);   /* sets the message pgb_last_error returns */
 unsigned long long pgb_dev_launches(void);
 int pgb_dev_sync(void *stream);
 
@@ -93,6 +94,9 @@ int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim, v
 int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                    pgb_coarsest_args a, pgb_trace *trace, void *stream);
 int pgb_k_fill(double *p, long n, double v, void *stream);
+
+/* excision m_util_r8 kernels (pgb_mutil_ex.cu) */
+unsigned long long pgb_dev_launches_ex(void);
 
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);

@@ -1,0 +1,119 @@
+/*
+ * Fortran-ABI drop-in for the m_util_r8 routines an application may call
+ * (include/m_util_r8.h:33-66): dmcopy3d_, dmhwr3d_, dmfwr3d_ and
+ * dminterp3d_ with every argument by pointer, on HOST arrays, as the
+ * reference's Fortran takes them. Built as its own library
+ * (libpamr_gb300_f77.so) so that an application links it in place of the
+ * reference's m_util_r8 object without any source change. Each call copies
+ * u1 (and chr1 when excising) and u2 to the device, runs the device
+ * routine of libpamr_gb300 (pgb_dm*, pgb_dm*_ex), and copies u2 back; device
+ * buffers are kept between calls and grown when needed. The Fortran
+ * routines return silently on out-of-range segments; so do these. Errors
+ * the Fortran would report with `stop` (unsupported order) are printed and
+ * leave u2 unchanged.
+ */
+#include <cuda_runtime_api.h>
+#include <stdio.h>
+#include "pamr_gb300.h"
+
+static double *d_buf[3];
+static size_t d_cap[3];
+
+static double *dev(int which, const double *h, size_t n)
+{
+   if (n > d_cap[which]) {
+      if (d_buf[which]) cudaFree(d_buf[which]);
+      d_buf[which] = 0;
+      d_cap[which] = 0;
+      if (cudaMalloc((void **)&d_buf[which], n * sizeof(double)) != cudaSuccess) return 0;
+      d_cap[which] = n;
+   }
+   if (h && cudaMemcpy(d_buf[which], h, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      return 0;
+   return d_buf[which];
+}
+
+static void report(const char *who, int rc)
+{
+   if (rc) fprintf(stderr, "%s: %s\n", who, pgb_last_error());
+}
+
+static int back(double *u2, const double *d2, size_t n)
+{
+   return cudaMemcpy(u2, d2, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess;
+}
+
+void dmcopy3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, int *ny2, int *nz2,
+               int *i1, int *j1, int *k1, int *i2, int *j2, int *k2, int *ni, int *nj, int *nk,
+               int *si1, int *sj1, int *sk1, int *si2, int *sj2, int *sk2)
+{
+   size_t n1 = (size_t)*nx1 * *ny1 * *nz1, n2 = (size_t)*nx2 * *ny2 * *nz2;
+   double *d1 = dev(0, u1, n1), *d2 = dev(1, u2, n2);
+   int rc;
+   if (!d1 || !d2) {
+      fprintf(stderr, "dmcopy3d: device buffers unavailable\n");
+      return;
+   }
+   rc = pgb_dmcopy3d(d1, d2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2, *ni,
+                     *nj, *nk, *si1, *sj1, *sk1, *si2, *sj2, *sk2, 0);
+   if (!rc) rc = back(u2, d2, n2);
+   report("dmcopy3d", rc);
+}
+
+#define RESTRICT_BODY(name, plain, excised)                                                    \
+   size_t n1 = (size_t)*nx1 * *ny1 * *nz1, n2 = (size_t)*nx2 * *ny2 * *nz2;                  \
+   double *d1 = dev(0, u1, n1), *d2 = dev(1, u2, n2), *dc = 0;                               \
+   int rc;                                                                                   \
+   if (*do_ex == 1) dc = dev(2, chr1, n1);                                                   \
+   if (!d1 || !d2 || (*do_ex == 1 && !dc)) {                                                 \
+      fprintf(stderr, name ": device buffers unavailable\n");                                \
+      return;                                                                                \
+   }                                                                                         \
+   if (*do_ex == 1)                                                                          \
+      rc = excised(d1, d2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2, \
+                   *ni, *nj, *nk, *si1, *sj1, *sk1, *si2, *sj2, *sk2, dc, *ex, 0);            \
+   else                                                                                      \
+      rc = plain(d1, d2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2,   \
+                 *ni, *nj, *nk, *si1, *sj1, *sk1, *si2, *sj2, *sk2, 0);                       \
+   if (!rc) rc = back(u2, d2, n2);                                                           \
+   report(name, rc);
+
+void dmhwr3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, int *ny2, int *nz2,
+              int *i1, int *j1, int *k1, int *i2, int *j2, int *k2, int *ni, int *nj, int *nk,
+              int *si1, int *sj1, int *sk1, int *si2, int *sj2, int *sk2, double *chr1, double *ex,
+              int *do_ex)
+{
+   RESTRICT_BODY("dmhwr3d", pgb_dmhwr3d, pgb_dmhwr3d_ex)
+}
+
+void dmfwr3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, int *ny2, int *nz2,
+              int *i1, int *j1, int *k1, int *i2, int *j2, int *k2, int *ni, int *nj, int *nk,
+              int *si1, int *sj1, int *sk1, int *si2, int *sj2, int *sk2, double *chr1, double *ex,
+              int *do_ex)
+{
+   RESTRICT_BODY("dmfwr3d", pgb_dmfwr3d, pgb_dmfwr3d_ex)
+}
+
+void dminterp3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, int *ny2,
+                 int *nz2, int *i1, int *j1, int *k1, int *i2, int *j2, int *k2, int *ni, int *nj,
+                 int *nk, int *si1, int *sj1, int *sk1, int *irho, int *jrho, int *krho, int *ord,
+                 double *chr1, double *ex, int *do_ex)
+{
+   size_t n1 = (size_t)*nx1 * *ny1 * *nz1, n2 = (size_t)*nx2 * *ny2 * *nz2;
+   double *d1 = dev(0, u1, n1), *d2 = dev(1, u2, n2), *dc = 0;
+   int rc;
+   if (*do_ex == 1) dc = dev(2, chr1, n1);
+   if (!d1 || !d2 || (*do_ex == 1 && !dc)) {
+      fprintf(stderr, "dminterp3d: device buffers unavailable\n");
+      return;
+   }
+   if (*do_ex == 1)
+      rc = pgb_dminterp3d_ex(d1, d2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2,
+                             *k2, *ni, *nj, *nk, *si1, *sj1, *sk1, *irho, *jrho, *krho, *ord, dc,
+                             *ex, 0);
+   else
+      rc = pgb_dminterp3d(d1, d2, *nx1, *ny1, *nz1, *nx2, *ny2, *nz2, *i1, *j1, *k1, *i2, *j2, *k2,
+                          *ni, *nj, *nk, *si1, *sj1, *sk1, *irho, *jrho, *krho, *ord, 0);
+   if (!rc) rc = back(u2, d2, n2);
+   report("dminterp3d", rc);
+}

@@ -1263,7 +1263,11 @@ static int mutil_launch(const double *u1, double *u2, mu_args a, int kind, void 
    if (g < 1) return 0;
    k_mutil<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a, kind);
    LAUNCHED(1);
-   return check("m_util_r8");
+   if (check("m_util_r8")) {
+      pgb_note_error(g_err);
+      return 11;
+   }
+   return 0;
 }
 
 #define MU_ARGS                                                                          \
@@ -1340,6 +1344,7 @@ extern "C" int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, in
    if (k2 < 1 || (k2 + (nk - 1) * krho) > nz2) return 0;
    if (ord != 2 && ord != 4) {
       snprintf(g_err, sizeof(g_err), "dminterp3d: only ord=2,4 supported");
+      pgb_note_error(g_err);
       return 12;
    }
    if (ord == 4) {
@@ -1348,6 +1353,7 @@ extern "C" int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, in
          if (n[d] >= 4 && !(st[d] <= r[d] && st[d] + n[d] * r[d] > N[d] - 2 * r[d])) {
             snprintf(g_err, sizeof(g_err),
                      "dminterp3d: cubic segment needs data outside it (unsupported)");
+            pgb_note_error(g_err);
             return 12;
          }
    }
@@ -1359,5 +1365,9 @@ extern "C" int pgb_dminterp3d(const double *u1, double *u2, int nx1, int ny1, in
    if (g < 1) return 0;
    k_minterp<<<(int)g, 256, 0, (cudaStream_t)stream>>>(u1, u2, a);
    LAUNCHED(1);
-   return check("dminterp3d");
+   if (check("dminterp3d")) {
+      pgb_note_error(g_err);
+      return 11;
+   }
+   return 0;
 }

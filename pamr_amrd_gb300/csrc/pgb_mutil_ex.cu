@@ -30,9 +30,17 @@ static int check_ex(const char *what)
    cudaError_t e = cudaGetLastError();
    if (e != cudaSuccess) {
       snprintf(g_err_ex, sizeof(g_err_ex), "%s: %s", what, cudaGetErrorString(e));
+      pgb_note_error(g_err_ex);
       return 1;
    }
    return 0;
+}
+
+static int arg_error(const char *msg)
+{
+   snprintf(g_err_ex, sizeof(g_err_ex), "%s", msg);
+   pgb_note_error(g_err_ex);
+   return 12;
 }
 
 /* 1-based Fortran element v(i) */
@@ -309,18 +317,10 @@ extern "C" int pgb_dminterp3d_ex(const double *u1, double *u2, int nx1, int ny1,
    if (j2 < 1 || (j2 + (nj - 1) * jrho) > ny2) return 0;
    if (k1 < 1 || (k1 + nk - 1) * sk1 > nz1) return 0;
    if (k2 < 1 || (k2 + (nk - 1) * krho) > nz2) return 0;
-   if (ord != 2 && ord != 4) {
-      snprintf(g_err_ex, sizeof(g_err_ex), "dminterp3d: only ord=2,4 supported");
-      return 12;
-   }
-   if (nx1 > 3000 || ny1 > 3000 || nz1 > 3000) {
-      snprintf(g_err_ex, sizeof(g_err_ex), "dminterp3d: nmax too small");
-      return 12;
-   }
-   if (ord == 4 && (irho > 20 || jrho > 20 || krho > 20)) {
-      snprintf(g_err_ex, sizeof(g_err_ex), "dvi4q1d_ex : irho expected to be less than 20");
-      return 12;
-   }
+   if (ord != 2 && ord != 4) return arg_error("dminterp3d: only ord=2,4 supported");
+   if (nx1 > 3000 || ny1 > 3000 || nz1 > 3000) return arg_error("dminterp3d: nmax too small");
+   if (ord == 4 && (irho > 20 || jrho > 20 || krho > 20))
+      return arg_error("dvi4q1d_ex : irho expected to be less than 20");
    {
       long n = (long)ni * nj * nk, g = (n + 127) / 128;
       k_mex_copy<<<(int)(g > 4096 ? 4096 : g), 128, 0, st>>>(u1, u2, a);

@@ -58,6 +58,9 @@ static long long g_graph_replayed = 0, g_captured = 0;
 
 const char *pgb_last_error(void) { return g_err; }
 
+/* lets the device entry points that take no solver (pgb_dm*) report too */
+void pgb_note_error(const char *msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
+
 static int fail(int code, const char *fmt, ...)
 {
    va_list ap;
@@ -935,7 +938,8 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
 
 long long pgb_launch_count(void)
 {
-   return (long long)(pgb_dev_launches() + pgb_dev_launches32()) - g_captured + g_graph_replayed;
+   return (long long)(pgb_dev_launches() + pgb_dev_launches32() + pgb_dev_launches_ex()) - g_captured +
+          g_graph_replayed;
 }
 
 int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double *bytes_per_sweep)

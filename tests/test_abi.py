@@ -29,3 +29,12 @@ def test_library_is_built_in_tree():
     path = build.build()
     assert os.path.dirname(path) == os.path.dirname(build.__file__)
     ctypes.CDLL(path)
+
+
+def test_fortran_abi_dropin_exports_m_util_r8_symbols():
+    """libpamr_gb300_f77.so carries the reference's m_util_r8.h entry points
+    (Fortran ABI, trailing underscore) so an application relinks unchanged"""
+    build.build()
+    L = ctypes.CDLL(build.LIB_F77)
+    for name in ("dmcopy3d_", "dmhwr3d_", "dmfwr3d_", "dminterp3d_"):
+        assert hasattr(L, name), name
