@@ -217,6 +217,47 @@ int pgb_dminterp3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, i
                       int nk, int si1, int sj1, int sk1, int irho, int jrho, int krho, int ord,
                       const double *chr1, double ex, void *stream);
 
+/* ------------------------------------------------- learned initial guess -- */
+/* No reference counterpart. BF16 tensor-core 3x3x3 convolution (tcgen05,
+ * FP32 accumulation) on the channel-blocked, zero-padded activation layout
+ * of the learned initial guess: act[cb][vtot][8] BF16 for channel block cb
+ * (8 channels), voxel (x,y,z) of a W x H x D volume at index
+ * margin + (x+1) + (W+2)*((y+1) + (H+2)*(z+1)); everything else zero.
+ * pgb_conv3d_geometry returns vtot and margin; pgb_conv3d_pack_weights turns
+ * FP32 weights w[27][cin][cout] (tap = dz*9 + dy*3 + dx) into the kernel's
+ * BF16 image (adjoint = 1: the image of the transposed convolution, with
+ * cin and cout exchanged); pgb_conv3d_bf16 computes
+ * out = [relu](conv(in) + bias) (bias may be NULL), writing zero on the
+ * padding. Channel counts 16, 32 or 64; W >= 8. err (device int, may be
+ * NULL) is set when a wait inside the kernel runs out. */
+int pgb_conv3d_geometry(int W, int H, int D, long *vtot, long *margin);
+int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int adjoint, void *stream);
+int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H, int D,
+                    int cin, int cout, int relu, int *err, void *stream);
+
+/* The learned initial guess: a 4-level convolutional encoder-decoder
+ * (16/32/64/64 channels, two 3x3x3 convolutions per encoder level, one per
+ * decoder level, additive skips, ReLU) from a source rho on an n^3 grid
+ * (points 0..n-2 seen by the net; n-1 a multiple of 8, n >= 65) to a guess
+ * of u, zero on the grid boundary. Forward and backward-data convolutions
+ * of the inner ten layers run on the tensor cores (BF16, FP32
+ * accumulation); weight gradients and the 1-channel first and last layers
+ * on CUDA cores; Adam on FP32 master weights. rho and u are device n^3
+ * arrays (x fastest); the training target is FP32. Scales: the net reads
+ * s_in * rho and predicts u / s_out. */
+typedef struct pgb_net pgb_net;
+int pgb_net_create(int n, unsigned long long seed, pgb_net **out);
+void pgb_net_destroy(pgb_net *net);
+int pgb_net_set_scales(pgb_net *net, double s_in, double s_out);
+long pgb_net_num_params(pgb_net *net);
+/* which = 0 parameters, 1 gradients (of the last pgb_net_loss_grad or
+ * train step); to_device = 1 uploads (parameters only) */
+int pgb_net_params(pgb_net *net, int which, float *host, int to_device);
+int pgb_net_predict(pgb_net *net, const double *rho, double *u, void *stream);
+int pgb_net_loss_grad(pgb_net *net, const double *rho, const float *u_target, double *loss, void *stream);
+int pgb_net_train_step(pgb_net *net, const double *rho, const float *u_target, float lr, double *loss,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

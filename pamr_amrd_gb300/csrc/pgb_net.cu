@@ -1,0 +1,1085 @@
+/*
+ * Learned initial guess of libpamr_gb300: BF16 tensor-core 3x3x3
+ * convolutions (tcgen05.mma, FP32 accumulation in tensor memory) and the
+ * other kernels of a 4-level convolutional encoder-decoder that maps a
+ * source rho to a guess of the solution u, with its training step (forward,
+ * backward, Adam) on the GPU. The data layout is described in pgb_net.h.
+ *
+ * Convolution as an implicit GEMM: one CTA computes a tile of 128
+ * consecutive padded voxels (M = 128) for all output channels (N = Cout),
+ * K = 27 taps x Cin in steps of 16 channels. For each of the three z-taps
+ * the CTA bulk-copies, per y-tap and channel block, the run of 130 voxels
+ * the three x-taps read (x-taps are offsets of 16 bytes into it), plus the
+ * weights of those nine taps, waits on an mbarrier, and one thread issues
+ * the 9*Cin/16 MMAs. Operands are K-major without swizzle: a core matrix is
+ * 8 voxels (rows) x 8 channels (16 bytes); SBO = 128 bytes between
+ * consecutive 8-voxel groups, LBO = the distance between the two channel
+ * blocks of a 16-channel step. The epilogue reads the accumulator with
+ * tcgen05.ld (one voxel per thread), adds the bias, applies ReLU, writes
+ * BF16 and re-zeroes the padding.
+ */
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include "pgb_dev.h"
+#include "pgb_net.h"
+
+static __thread char g_err_net[256];
+static unsigned long long g_launches_net = 0;
+
+extern "C" unsigned long long pgb_dev_launches_net(void) { return g_launches_net; }
+
+static int check_net(const char *what)
+{
+   g_launches_net++;
+   cudaError_t e = cudaGetLastError();
+   if (e != cudaSuccess) {
+      snprintf(g_err_net, sizeof(g_err_net), "%s: %s", what, cudaGetErrorString(e));
+      pgb_note_error(g_err_net);
+      return 1;
+   }
+   return 0;
+}
+
+static int arg_err(const char *msg)
+{
+   snprintf(g_err_net, sizeof(g_err_net), "%s", msg);
+   pgb_note_error(g_err_net);
+   return 12;
+}
+
+/* ------------------------------------------------------------ PTX pieces -- */
+__device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+   uint64_t t;
+   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+   return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)), "r"(bytes)
+                : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t phase)
+{
+   uint32_t ok;
+   asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                " selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(s_addr(bar)), "r"(phase)
+                : "memory");
+   return ok != 0;
+}
+
+/* waits for the phase with a limit of about one second; false on timeout */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase)
+{
+   const uint64_t t0 = global_ns();
+   while (!mbar_try(bar, phase))
+      if (global_ns() - t0 > 1000000000ull) return false;
+   return true;
+}
+
+/* 1-D bulk copy global -> shared, completion counted on bar (16-byte
+ * aligned addresses, size a multiple of 16) */
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+                   "r"(s_addr(dst)), "l"(src), "r"(bytes), "r"(s_addr(bar))
+                : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols)
+{
+   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_addr(dst)),
+                "r"(ncols)
+                : "memory");
+   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+/* D[tmem] (+)= A[smem] x B[smem], M x N x 16, BF16 in, FP32 accumulate */
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+   asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(s_addr(bar))
+                : "memory");
+}
+
+/* 32 lanes x 16 consecutive 32-bit columns: thread t gets lane (base + t) */
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+   uint32_t r[16];
+   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+/* shared-memory matrix descriptor, no swizzle (layout type 0), version 1 */
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+   return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+/* instruction descriptor, kind::f16: FP32 D, BF16 A and B, both K-major */
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+/* ------------------------------------------------------------ geometry -- */
+static pgb_lvgeom make_geom(int W, int H, int D)
+{
+   pgb_lvgeom g;
+   g.W = W;
+   g.H = H;
+   g.D = D;
+   g.Wp = W + 2;
+   g.Hp = H + 2;
+   g.Dp = D + 2;
+   g.plane = (long)g.Wp * g.Hp;
+   g.margin = g.plane + g.Wp + 2 + 128;
+   g.vtot = 2 * g.margin + g.plane * g.Dp;
+   g.p0 = g.plane;
+   g.ntile = (int)((D * g.plane + 127) / 128);
+   return g;
+}
+
+/* ------------------------------------------------- tensor-core 3x3x3 conv -- */
+#define CONV_RUN 130   /* voxels of one y/z-tap run (x-taps -1, 0, +1 of 128 outputs) */
+
+template <int CIN, int COUT>
+struct ConvSmem {
+   static constexpr int KS = CIN / 16;                        /* 16-channel K steps per tap */
+   static constexpr int A_BYTES = 3 * (CIN / 8) * CONV_RUN * 16;
+   static constexpr int W_BYTES = 9 * CIN * COUT * 2;         /* nine taps of one z-tap */
+   static constexpr int LOAD_BYTES = A_BYTES + W_BYTES;      /* bulk-copied per z-tap */
+   /* 40 KB beyond the operands: every shared-memory address an MMA could
+    * form from these descriptors stays inside the allocation */
+   static constexpr int BYTES = LOAD_BYTES + 40 * 1024;
+   static constexpr int NCOL = COUT < 32 ? 32 : COUT;         /* TMEM columns (power of 2) */
+};
+
+/* Weight image (global, BF16): for z-tap dz, the nine (dy,dx) taps, K steps
+ * ks, half h, output channel co, 8 input channels:
+ *   wimg[dz][dy*3+dx][ks][h][co][8] = w[tap][16ks + 8h + e][co] */
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16 *in, __nv_bfloat16 *out,
+                                                 const __nv_bfloat16 *wimg, const float *bias,
+                                                 pgb_lvgeom g, int relu, int *err)
+{
+   typedef ConvSmem<CIN, COUT> S;
+   extern __shared__ __align__(128) uint8_t smem[];
+   uint8_t *sA = smem, *sW = smem + S::A_BYTES;
+   __shared__ __align__(8) uint64_t bar_load, bar_mma;
+   __shared__ uint32_t tmem_base;
+   __shared__ int s_fail;
+   const int tid = threadIdx.x, warp = tid >> 5;
+   const long T = g.p0 + 128L * blockIdx.x;
+
+   if (warp == 0) tmem_alloc(&tmem_base, S::NCOL);
+   if (tid == 0) {
+      mbar_init(&bar_load, 1);
+      mbar_init(&bar_mma, 1);
+      mbar_fence_init();
+      s_fail = 0;
+   }
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t taddr = tmem_base;
+   constexpr uint32_t IDESC = idesc_bf16(128, COUT);
+
+   for (int dz = 0; dz < 3; dz++) {
+      if (tid == 0) {
+         mbar_expect_tx(&bar_load, S::LOAD_BYTES);
+         for (int dy = 0; dy < 3; dy++)
+            for (int cb = 0; cb < CIN / 8; cb++) {
+               const long v = g.margin + T + (dz - 1) * g.plane + (dy - 1) * (long)g.Wp - 1;
+               bulk_g2s(sA + (dy * (CIN / 8) + cb) * CONV_RUN * 16, in + ((long)cb * g.vtot + v) * 8,
+                        CONV_RUN * 16, &bar_load);
+            }
+         bulk_g2s(sW, wimg + (long)dz * (S::W_BYTES / 2), S::W_BYTES, &bar_load);
+      }
+      if (!mbar_wait(&bar_load, dz & 1)) s_fail = 1;
+      __syncthreads();
+      if (s_fail) break;
+      if (tid == 0) {
+         tc_fence_after();
+         for (int dy = 0; dy < 3; dy++)
+            for (int dx = 0; dx < 3; dx++)
+               for (int ks = 0; ks < S::KS; ks++) {
+                  const uint32_t a = s_addr(sA) + ((dy * (CIN / 8) + 2 * ks) * CONV_RUN + dx) * 16;
+                  const uint32_t b = s_addr(sW) + (((dy * 3 + dx) * S::KS + ks) * 2 * COUT) * 16;
+                  mma_bf16(taddr, sdesc(a, CONV_RUN * 16, 128), sdesc(b, COUT * 16, 128), IDESC,
+                           (dz | dy | dx | ks) != 0);
+               }
+         mma_commit(&bar_mma);
+      }
+      if (!mbar_wait(&bar_mma, dz & 1)) s_fail = 1;
+      __syncthreads();
+      if (s_fail) break;
+   }
+
+   if (!s_fail) {
+      tc_fence_after();
+      const long P = T + tid;   /* this thread's voxel (TMEM lane tid) */
+      const long x = P % g.Wp, y = (P / g.Wp) % g.Hp, z = P / g.plane;
+      const bool pad = x == 0 || x == g.Wp - 1 || y == 0 || y == g.Hp - 1 || z == 0 || z >= g.Dp - 1;
+      const uint32_t tw = taddr + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+      for (int c16 = 0; c16 < COUT / 16; c16++) {
+         float v[16];
+         tmem_ld16(tw + c16 * 16, v);
+#pragma unroll
+         for (int h = 0; h < 2; h++) {
+            uint32_t pk[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+               float a0 = v[h * 8 + 2 * e], a1 = v[h * 8 + 2 * e + 1];
+               if (bias) {
+                  a0 += bias[c16 * 16 + h * 8 + 2 * e];
+                  a1 += bias[c16 * 16 + h * 8 + 2 * e + 1];
+               }
+               if (relu) {
+                  a0 = fmaxf(a0, 0.f);
+                  a1 = fmaxf(a1, 0.f);
+               }
+               if (pad) a0 = a1 = 0.f;
+               __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
+               pk[e] = *reinterpret_cast<uint32_t *>(&b2);
+            }
+            const long cb = c16 * 2 + h;
+            *reinterpret_cast<uint4 *>(out + (cb * g.vtot + g.margin + P) * 8) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+         }
+      }
+   } else {
+      /* a wait ran out: give the copies and MMAs in flight another bounded
+       * chance to land before the shared and tensor memory are released */
+      mbar_wait(&bar_load, 0);
+      mbar_wait(&bar_mma, 0);
+      if (tid == 0 && err) atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(taddr, S::NCOL);
+}
+
+template <int CIN, int COUT>
+static int launch_conv(const void *in, void *out, const void *wimg, const float *bias, const pgb_lvgeom &g,
+                       int relu, int *err, cudaStream_t st)
+{
+   typedef ConvSmem<CIN, COUT> S;
+   static bool attr = false;
+   if (!attr) {
+      if (cudaFuncSetAttribute(k_conv_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES) !=
+          cudaSuccess)
+         return check_net("conv attribute");
+      attr = true;
+   }
+   k_conv_tc<CIN, COUT><<<g.ntile, 128, S::BYTES, st>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out,
+                                                         (const __nv_bfloat16 *)wimg, bias, g, relu, err);
+   return check_net("conv_tc") ? 11 : 0;
+}
+
+#define CONV_CASE(a, b) \
+   if (cin == a && cout == b) return launch_conv<a, b>(in, out, wimg, bias, g, relu, err, st);
+
+static int conv_dispatch(int cin, int cout, const void *in, void *out, const void *wimg, const float *bias,
+                         const pgb_lvgeom &g, int relu, int *err, cudaStream_t st)
+{
+   CONV_CASE(16, 16)
+   CONV_CASE(16, 32)
+   CONV_CASE(16, 64)
+   CONV_CASE(32, 16)
+   CONV_CASE(32, 32)
+   CONV_CASE(32, 64)
+   CONV_CASE(64, 16)
+   CONV_CASE(64, 32)
+   CONV_CASE(64, 64)
+   return arg_err("conv3d: channel counts must be 16, 32 or 64");
+}
+
+/* w[27][cin][cout] FP32 (tap = dz*9 + dy*3 + dx) -> the kernel's BF16 image;
+ * flip = 1 makes the image of the adjoint convolution (tap 26 - t, channels
+ * swapped: the image then has cin' = cout, cout' = cin) */
+__global__ void k_pack_weights(const float *w, __nv_bfloat16 *img, int cin, int cout, int flip)
+{
+   const int ci_n = flip ? cout : cin, co_n = flip ? cin : cout;   /* channels of the packed conv */
+   const int ks_n = ci_n / 16;
+   const long n = 27L * ci_n * co_n;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+      /* q enumerates the image: [dz][t9][ks][h][co][e] */
+      const int e = (int)(q % 8);
+      long r = q / 8;
+      const int co = (int)(r % co_n);
+      r /= co_n;
+      const int h = (int)(r % 2);
+      r /= 2;
+      const int ks = (int)(r % ks_n);
+      r /= ks_n;
+      const int t9 = (int)(r % 9), dz = (int)(r / 9);
+      const int tap = dz * 9 + t9, ci = 16 * ks + 8 * h + e;
+      float v;
+      if (flip) v = w[((long)(26 - tap) * cin + co) * cout + ci];   /* adjoint: w[26-t][co'][ci'] */
+      else v = w[((long)tap * cin + ci) * cout + co];
+      img[q] = __float2bfloat16_rn(v);
+   }
+}
+
+extern "C" int pgb_conv3d_geometry(int W, int H, int D, long *vtot, long *margin)
+{
+   pgb_lvgeom g = make_geom(W, H, D);
+   if (vtot) *vtot = g.vtot;
+   if (margin) *margin = g.margin;
+   return 0;
+}
+
+extern "C" int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int adjoint, void *stream)
+{
+   if ((cin % 16) || (cout % 16)) return arg_err("pack_weights: channel counts must be multiples of 16");
+   k_pack_weights<<<256, 256, 0, (cudaStream_t)stream>>>(w, (__nv_bfloat16 *)img, cin, cout, adjoint);
+   return check_net("pack_weights") ? 11 : 0;
+}
+
+extern "C" int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H,
+                               int D, int cin, int cout, int relu, int *err, void *stream)
+{
+   if (W < 8 || H < 1 || D < 1) return arg_err("conv3d: volume too small");
+   pgb_lvgeom g = make_geom(W, H, D);
+   return conv_dispatch(cin, cout, in, out, wimg, bias, g, relu, err, (cudaStream_t)stream);
+}
+
+/* ------------------------------------------- CUDA-core kernels of the net -- */
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ long vox(const pgb_lvgeom &g, int x, int y, int z)
+{
+   return g.margin + (x + 1) + (long)g.Wp * ((y + 1) + (long)g.Hp * (z + 1));
+}
+
+__device__ __forceinline__ void load8(const bf16 *a, long idx, float *v)
+{
+   const uint4 u = *reinterpret_cast<const uint4 *>(a + idx * 8);
+   const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+   for (int e = 0; e < 4; e++) {
+      float2 f = __bfloat1622float2(h[e]);
+      v[2 * e] = f.x;
+      v[2 * e + 1] = f.y;
+   }
+}
+
+__device__ __forceinline__ void store8(bf16 *a, long idx, const float *v)
+{
+   uint32_t pk[4];
+#pragma unroll
+   for (int e = 0; e < 4; e++) {
+      __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+      pk[e] = *reinterpret_cast<uint32_t *>(&b2);
+   }
+   *reinterpret_cast<uint4 *>(a + idx * 8) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+}
+
+/* first layer, 1 -> 16 channels: a0 = relu(conv(s_in * rho) + b); rho is
+ * the n^3 FP64 grid, the net sees its points 0..n-2 in each dimension
+ * (zero beyond) */
+__global__ void k_in_fwd(const double *rho, int n, float s_in, const float *w, const float *b, bf16 *out,
+                         pgb_lvgeom g)
+{
+   const long nv = (long)g.W * g.H * g.D;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      float acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; c++) acc[c] = b[c];
+      for (int t = 0; t < 27; t++) {
+         const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
+         if (xx < 0 || yy < 0 || zz < 0 || xx >= g.W || yy >= g.H || zz >= g.D) continue;
+         const float r = s_in * (float)rho[xx + (long)n * (yy + (long)n * zz)];
+#pragma unroll
+         for (int c = 0; c < 16; c++) acc[c] = fmaf(r, w[t * 16 + c], acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 16; c++) acc[c] = fmaxf(acc[c], 0.f);
+      const long p = vox(g, x, y, z);
+      store8(out, p, acc);
+      store8(out, g.vtot + p, acc + 8);
+   }
+}
+
+/* last layer, 16 -> 1 channel, no activation: up = conv(a) + b, as FP32 on
+ * the net volume (x fastest) */
+__global__ void k_out_fwd(const bf16 *a, const float *w, const float *b, float *up, pgb_lvgeom g)
+{
+   const long nv = (long)g.W * g.H * g.D;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      const long p = vox(g, x, y, z);
+      float acc = b[0];
+      for (int t = 0; t < 27; t++) {
+         const long o = (t / 9 - 1) * g.plane + ((t / 3) % 3 - 1) * (long)g.Wp + (t % 3 - 1);
+#pragma unroll
+         for (int cb = 0; cb < 2; cb++) {
+            float v[8];
+            load8(a, (long)cb * g.vtot + p + o, v);
+#pragma unroll
+            for (int e = 0; e < 8; e++) acc = fmaf(v[e], w[t * 16 + cb * 8 + e], acc);
+         }
+      }
+      up[q] = acc;
+   }
+}
+
+/* u (n^3 FP64) = s_out * up on points 1..n-2 of the net volume, 0 on the
+ * grid's boundary points */
+__global__ void k_out_store(const float *up, double *u, int n, double s_out, pgb_lvgeom g)
+{
+   const long nn = (long)n * n * n;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % n), y = (int)((q / n) % n), z = (int)(q / ((long)n * n));
+      double v = 0.0;
+      if (x > 0 && y > 0 && z > 0 && x < n - 1 && y < n - 1 && z < n - 1)
+         v = s_out * (double)up[x + (long)g.W * (y + (long)g.H * z)];
+      u[q] = v;
+   }
+}
+
+/* MSE over points 1..n-2: loss += sum (up - ut/s_out)^2 / N, gup = dloss/dup */
+__global__ void k_loss(const float *up, const float *ut, int n, float inv_s_out, float *gup, double *loss,
+                       pgb_lvgeom g)
+{
+   __shared__ double sm[8];
+   const long nv = (long)g.W * g.H * g.D;
+   const double inv_n = 1.0 / ((double)(n - 2) * (n - 2) * (n - 2));
+   double acc = 0;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      float gr = 0.f;
+      if (x > 0 && y > 0 && z > 0) {
+         const float d = up[q] - inv_s_out * ut[x + (long)n * (y + (long)n * z)];
+         acc += (double)d * d;
+         gr = (float)(2.0 * inv_n) * d;
+      }
+      gup[q] = gr;
+   }
+   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      double s = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sm[i];
+      atomicAdd(loss, s * inv_n);
+   }
+}
+
+/* last layer backward-data: ga (16 ch, BF16 layout) = adjoint conv of gup */
+__global__ void k_out_bwd_data(const float *gup, const float *w, bf16 *ga, pgb_lvgeom g)
+{
+   const long nv = (long)g.W * g.H * g.D;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      float acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; c++) acc[c] = 0.f;
+      for (int t = 0; t < 27; t++) {   /* the output voxel v - off(t) reads this voxel with tap t */
+         const int xx = x - (t % 3 - 1), yy = y - ((t / 3) % 3 - 1), zz = z - (t / 9 - 1);
+         if (xx < 0 || yy < 0 || zz < 0 || xx >= g.W || yy >= g.H || zz >= g.D) continue;
+         const float gv = gup[xx + (long)g.W * (yy + (long)g.H * zz)];
+#pragma unroll
+         for (int c = 0; c < 16; c++) acc[c] = fmaf(gv, w[t * 16 + c], acc[c]);
+      }
+      const long p = vox(g, x, y, z);
+      store8(ga, p, acc);
+      store8(ga, g.vtot + p, acc + 8);
+   }
+}
+
+__device__ void block_add(float v, float *red, float *dst)
+{
+   red[threadIdx.x] = v;
+   __syncthreads();
+   for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+      if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0 && dst) atomicAdd(dst, red[0]);
+   __syncthreads();
+}
+
+/* last layer dW: dw[t][c] += sum_v a[v + off t][c] gup[v] (cin = 16), db */
+__global__ void k_out_bwd_w(const bf16 *a, const float *gup, float *dw, float *db, pgb_lvgeom g)
+{
+   __shared__ float red[256];
+   const int t = blockIdx.y;
+   const long o = (t / 9 - 1) * g.plane + ((t / 3) % 3 - 1) * (long)g.Wp + (t % 3 - 1);
+   const long nv = (long)g.W * g.H * g.D;
+   float acc[16], ab = 0.f;
+#pragma unroll
+   for (int c = 0; c < 16; c++) acc[c] = 0.f;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      const float gv = gup[q];
+      const long p = vox(g, x, y, z) + o;
+      float v[8];
+#pragma unroll
+      for (int cb = 0; cb < 2; cb++) {
+         load8(a, (long)cb * g.vtot + p, v);
+#pragma unroll
+         for (int e = 0; e < 8; e++) acc[cb * 8 + e] = fmaf(v[e], gv, acc[cb * 8 + e]);
+      }
+      ab += gv;
+   }
+#pragma unroll
+   for (int c = 0; c < 16; c++) block_add(acc[c], red, &dw[t * 16 + c]);
+   block_add(ab, red, t == 13 ? db : 0);
+}
+
+/* first layer dW: dw[t][c] += sum_v s_in rho[v + off t] gz[v][c], db[c] += sum gz */
+__global__ void k_in_bwd_w(const double *rho, int n, float s_in, const bf16 *gz, float *dw, float *db, pgb_lvgeom g)
+{
+   __shared__ float red[256];
+   const int t = blockIdx.y;
+   const int ox = t % 3 - 1, oy = (t / 3) % 3 - 1, oz = t / 9 - 1;
+   const long nv = (long)g.W * g.H * g.D;
+   float acc[16], ab[16];
+#pragma unroll
+   for (int c = 0; c < 16; c++) acc[c] = ab[c] = 0.f;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+      const int xx = x + ox, yy = y + oy, zz = z + oz;
+      float r = 0.f;
+      if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D)
+         r = s_in * (float)rho[xx + (long)n * (yy + (long)n * zz)];
+      const long p = vox(g, x, y, z);
+      float v[8];
+#pragma unroll
+      for (int cb = 0; cb < 2; cb++) {
+         load8(gz, (long)cb * g.vtot + p, v);
+#pragma unroll
+         for (int e = 0; e < 8; e++) {
+            acc[cb * 8 + e] = fmaf(r, v[e], acc[cb * 8 + e]);
+            ab[cb * 8 + e] += v[e];
+         }
+      }
+   }
+#pragma unroll
+   for (int c = 0; c < 16; c++) block_add(acc[c], red, &dw[t * 16 + c]);
+#pragma unroll
+   for (int c = 0; c < 16; c++) block_add(ab[c], red, t == 13 ? &db[c] : 0);
+}
+
+/* g = g * (y > 0) over the interior voxels of all channel blocks */
+__global__ void k_relu_bwd(bf16 *gv, const bf16 *y, int nch, pgb_lvgeom g)
+{
+   const long nv = (long)g.W * g.H * g.D, n = nv * (nch / 8);
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+      const long cb = q / nv, r = q % nv;
+      const int x = (int)(r % g.W), yy = (int)((r / g.W) % g.H), z = (int)(r / ((long)g.W * g.H));
+      const long idx = cb * g.vtot + vox(g, x, yy, z);
+      float a[8], b[8];
+      load8(gv, idx, a);
+      load8(y, idx, b);
+#pragma unroll
+      for (int e = 0; e < 8; e++) a[e] = b[e] > 0.f ? a[e] : 0.f;
+      store8(gv, idx, a);
+   }
+}
+
+/* 2x2x2 average pool (fine f -> coarse c); backward: f += c/8 on the eight
+ * children */
+__global__ void k_pool(bf16 *f, bf16 *c, int nch, pgb_lvgeom gf, pgb_lvgeom gc, int backward)
+{
+   const long nv = (long)gc.W * gc.H * gc.D, n = nv * (nch / 8);
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+      const long cb = q / nv, r = q % nv;
+      const int x = (int)(r % gc.W), y = (int)((r / gc.W) % gc.H), z = (int)(r / ((long)gc.W * gc.H));
+      const long ic = cb * gc.vtot + vox(gc, x, y, z);
+      float s[8], v[8];
+      if (!backward) {
+#pragma unroll
+         for (int e = 0; e < 8; e++) s[e] = 0.f;
+         for (int k = 0; k < 8; k++) {
+            load8(f, cb * gf.vtot + vox(gf, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + (k >> 2)), v);
+#pragma unroll
+            for (int e = 0; e < 8; e++) s[e] += v[e];
+         }
+#pragma unroll
+         for (int e = 0; e < 8; e++) s[e] *= 0.125f;
+         store8(c, ic, s);
+      } else {
+         load8(c, ic, s);
+         for (int k = 0; k < 8; k++) {
+            const long i = cb * gf.vtot + vox(gf, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + (k >> 2));
+            load8(f, i, v);
+#pragma unroll
+            for (int e = 0; e < 8; e++) v[e] += 0.125f * s[e];
+            store8(f, i, v);
+         }
+      }
+   }
+}
+
+/* nearest upsample + skip: out(fine) = up(c) + skip. backward: out (coarse)
+ * = sum over the eight children of c (the fine gradient) */
+__global__ void k_up(const bf16 *c, const bf16 *skip, bf16 *out, int nch, pgb_lvgeom gf, pgb_lvgeom gc, int backward)
+{
+   if (!backward) {
+      const long nv = (long)gf.W * gf.H * gf.D, n = nv * (nch / 8);
+      for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+         const long cb = q / nv, r = q % nv;
+         const int x = (int)(r % gf.W), y = (int)((r / gf.W) % gf.H), z = (int)(r / ((long)gf.W * gf.H));
+         const long i = cb * gf.vtot + vox(gf, x, y, z);
+         float a[8], b[8];
+         load8(c, cb * gc.vtot + vox(gc, x >> 1, y >> 1, z >> 1), a);
+         load8(skip, i, b);
+#pragma unroll
+         for (int e = 0; e < 8; e++) a[e] += b[e];
+         store8(out, i, a);
+      }
+   } else {
+      const long nv = (long)gc.W * gc.H * gc.D, n = nv * (nch / 8);
+      for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+         const long cb = q / nv, r = q % nv;
+         const int x = (int)(r % gc.W), y = (int)((r / gc.W) % gc.H), z = (int)(r / ((long)gc.W * gc.H));
+         float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
+         for (int k = 0; k < 8; k++) {
+            load8(c, cb * gf.vtot + vox(gf, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + (k >> 2)), v);
+#pragma unroll
+            for (int e = 0; e < 8; e++) s[e] += v[e];
+         }
+         store8(out, cb * gc.vtot + vox(gc, x, y, z), s);
+      }
+   }
+}
+
+/* a += b over the interior (skip-connection gradients) */
+__global__ void k_add(bf16 *a, const bf16 *b, int nch, pgb_lvgeom g)
+{
+   const long nv = (long)g.W * g.H * g.D, n = nv * (nch / 8);
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+      const long cb = q / nv, r = q % nv;
+      const int x = (int)(r % g.W), y = (int)((r / g.W) % g.H), z = (int)(r / ((long)g.W * g.H));
+      const long i = cb * g.vtot + vox(g, x, y, z);
+      float u[8], v[8];
+      load8(a, i, u);
+      load8(b, i, v);
+#pragma unroll
+      for (int e = 0; e < 8; e++) u[e] += v[e];
+      store8(a, i, u);
+   }
+}
+
+/* Weight gradient of a tensor-core layer, FP32 on CUDA cores:
+ * dw[t][ci][co] += sum_v x[v + off t][ci] * gz[v][co], db[co] += sum gz.
+ * blockIdx.y = tap; each thread owns up to 16 (ci, co) pairs; voxels in
+ * chunks of WCH staged in shared memory (gz is zero on the padding, so the
+ * chunks run over whole padded planes). */
+#define WCH 64
+__global__ void __launch_bounds__(256) k_conv_bwd_w(const bf16 *x, const bf16 *gz, float *dw, float *db, int cin,
+                                                    int cout, pgb_lvgeom g)
+{
+   extern __shared__ float sh[];
+   float *xs = sh, *gs = sh + WCH * cin;
+   const int t = blockIdx.y;
+   const long o = (t / 9 - 1) * g.plane + ((t / 3) % 3 - 1) * (long)g.Wp + (t % 3 - 1);
+   const int npair = cin * cout, per = (npair + 255) / 256;   /* <= 16 */
+   float acc[16], ab = 0.f;
+#pragma unroll
+   for (int k = 0; k < 16; k++) acc[k] = 0.f;
+   const long total = (long)g.D * g.plane;
+   for (long base = (long)blockIdx.x * WCH; base < total; base += (long)gridDim.x * WCH) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < WCH * (cin / 8 + cout / 8); q += blockDim.x) {
+         const int vv = q % WCH, b8 = q / WCH;
+         const long P = g.p0 + base + vv;
+         float v[8];
+         if (base + vv < total) {
+            if (b8 < cin / 8) load8(x, (long)b8 * g.vtot + g.margin + P + o, v);
+            else load8(gz, (long)(b8 - cin / 8) * g.vtot + g.margin + P, v);
+         } else
+            for (int e = 0; e < 8; e++) v[e] = 0.f;
+         float *d = b8 < cin / 8 ? xs + vv * cin + b8 * 8 : gs + vv * cout + (b8 - cin / 8) * 8;
+         for (int e = 0; e < 8; e++) d[e] = v[e];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+         const int pr = threadIdx.x + k * 256;
+         if (k >= per || pr >= npair) break;
+         const int ci = pr / cout, co = pr % cout;
+         float s = acc[k];
+         for (int vv = 0; vv < WCH; vv++) s = fmaf(xs[vv * cin + ci], gs[vv * cout + co], s);
+         acc[k] = s;
+      }
+      if (t == 13 && (int)threadIdx.x < cout)
+         for (int vv = 0; vv < WCH; vv++) ab += gs[vv * cout + threadIdx.x];
+   }
+#pragma unroll
+   for (int k = 0; k < 16; k++) {
+      const int pr = threadIdx.x + k * 256;
+      if (k < per && pr < npair) atomicAdd(&dw[((long)t * cin + pr / cout) * cout + pr % cout], acc[k]);
+   }
+   if (t == 13 && (int)threadIdx.x < cout) atomicAdd(&db[threadIdx.x], ab);
+}
+
+/* Adam on FP32 parameters */
+__global__ void k_adam(float *w, const float *gw, float *m, float *v, long n, float lr, float b1, float b2,
+                       float c1, float c2, float eps)
+{
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+      const float gq = gw[q];
+      const float mq = b1 * m[q] + (1.f - b1) * gq, vq = b2 * v[q] + (1.f - b2) * gq * gq;
+      m[q] = mq;
+      v[q] = vq;
+      w[q] -= lr * (mq * c1) / (sqrtf(vq * c2) + eps);
+   }
+}
+
+/* ------------------------------------------------------ the network (host) -- */
+/* 4-level encoder-decoder on an (n-1)^3 volume (points 0..n-2 of an n^3
+ * grid): 16, 32, 64, 64 channels; two 3x3x3 convolutions per encoder
+ * level, 2x2x2 average pooling down, nearest upsampling plus the encoder's
+ * activation (additive skip) up, one convolution per decoder level, ReLU
+ * after every convolution but the last. The first (1 -> 16) and last
+ * (16 -> 1) convolutions run on CUDA cores, the ten others on the tensor
+ * cores (forward, and backward-data through the adjoint image). */
+enum { NTC = 10 };
+static const int TC_LEV[NTC] = {0, 1, 1, 2, 2, 3, 3, 2, 1, 0};
+static const int TC_CIN[NTC] = {16, 16, 32, 32, 64, 64, 64, 64, 32, 16};
+static const int TC_COUT[NTC] = {16, 32, 32, 64, 64, 64, 64, 32, 16, 16};
+/* activations: a0 a1 | b0 a2 a3 | b1 a4 a5 | b2 a6 a7 | c2 a8 | c1 a9 | c0 a10 */
+enum { A0, A1, B0, A2, A3, B1, A4, A5, B2, A6, A7, C2, A8, C1, A9, C0, A10, NACT };
+static const int ACT_LEV[NACT] = {0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3, 2, 2, 1, 1, 0, 0};
+static const int ACT_CH[NACT] = {16, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 64, 32, 32, 16, 16, 16};
+
+struct pgb_net {
+   int n;
+   pgb_lvgeom g[4];
+   double s_in, s_out;
+   long np;                       /* parameter count */
+   float *p, *gp, *m, *v;         /* parameters, gradients, Adam moments */
+   long off_tc_w[NTC], off_tc_b[NTC], off_in_w, off_in_b, off_out_w, off_out_b;
+   bf16 *img[NTC], *img_adj[NTC];
+   bf16 *act[NACT], *grad[NACT];
+   float *up, *gup;
+   double *d_loss;
+   int *d_err;
+   long step;
+};
+
+static size_t act_bytes(const pgb_lvgeom &g, int ch) { return (size_t)(ch / 8) * g.vtot * 16; }
+
+static uint64_t splitmix(uint64_t *s)
+{
+   uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+   return z ^ (z >> 31);
+}
+
+static double gauss(uint64_t *s)
+{
+   double u1 = ((splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+   double u2 = ((splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+   return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+static int repack(pgb_net *net, cudaStream_t st)
+{
+   for (int l = 0; l < NTC; l++) {
+      const float *w = net->p + net->off_tc_w[l];
+      if (pgb_conv3d_pack_weights(w, net->img[l], TC_CIN[l], TC_COUT[l], 0, st) ||
+          pgb_conv3d_pack_weights(w, net->img_adj[l], TC_CIN[l], TC_COUT[l], 1, st))
+         return 11;
+   }
+   return 0;
+}
+
+extern "C" void pgb_net_destroy(pgb_net *net)
+{
+   if (!net) return;
+   cudaFree(net->p);
+   cudaFree(net->gp);
+   cudaFree(net->m);
+   cudaFree(net->v);
+   for (int l = 0; l < NTC; l++) {
+      cudaFree(net->img[l]);
+      cudaFree(net->img_adj[l]);
+   }
+   for (int a = 0; a < NACT; a++) {
+      cudaFree(net->act[a]);
+      cudaFree(net->grad[a]);
+   }
+   cudaFree(net->up);
+   cudaFree(net->gup);
+   cudaFree(net->d_loss);
+   cudaFree(net->d_err);
+   free(net);
+}
+
+extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
+{
+   *out = 0;
+   if (n < 65 || (n - 1) % 8 != 0) return arg_err("pgb_net_create: n-1 must be a multiple of 8, n >= 65");
+   pgb_net *net = (pgb_net *)calloc(1, sizeof(pgb_net));
+   net->n = n;
+   net->s_in = net->s_out = 1.0;
+   for (int l = 0; l < 4; l++) {
+      const int e = (n - 1) >> l;
+      net->g[l] = make_geom(e, e, e);
+   }
+   long o = 0;
+   net->off_in_w = o; o += 27 * 16;
+   net->off_in_b = o; o += 16;
+   for (int l = 0; l < NTC; l++) {
+      net->off_tc_w[l] = o; o += 27L * TC_CIN[l] * TC_COUT[l];
+      net->off_tc_b[l] = o; o += TC_COUT[l];
+   }
+   net->off_out_w = o; o += 27 * 16;
+   net->off_out_b = o; o += 1;
+   net->np = o;
+   const size_t nv = (size_t)(n - 1) * (n - 1) * (n - 1);
+   bool ok = cudaMalloc((void **)&net->p, o * 4) == cudaSuccess && cudaMalloc((void **)&net->gp, o * 4) == cudaSuccess &&
+             cudaMalloc((void **)&net->m, o * 4) == cudaSuccess && cudaMalloc((void **)&net->v, o * 4) == cudaSuccess &&
+             cudaMalloc((void **)&net->up, nv * 4) == cudaSuccess && cudaMalloc((void **)&net->gup, nv * 4) == cudaSuccess &&
+             cudaMalloc((void **)&net->d_loss, 8) == cudaSuccess && cudaMalloc((void **)&net->d_err, 4) == cudaSuccess;
+   for (int l = 0; l < NTC && ok; l++)
+      ok = cudaMalloc((void **)&net->img[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess &&
+           cudaMalloc((void **)&net->img_adj[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess;
+   for (int a = 0; a < NACT && ok; a++) {
+      const size_t b = act_bytes(net->g[ACT_LEV[a]], ACT_CH[a]);
+      ok = cudaMalloc((void **)&net->act[a], b) == cudaSuccess && cudaMalloc((void **)&net->grad[a], b) == cudaSuccess &&
+           cudaMemset(net->act[a], 0, b) == cudaSuccess && cudaMemset(net->grad[a], 0, b) == cudaSuccess;
+   }
+   if (!ok) {
+      pgb_net_destroy(net);
+      return arg_err("pgb_net_create: device allocation failed");
+   }
+   /* He-normal weights (the last layer scaled down), zero biases */
+   float *h = (float *)calloc(o, 4);
+   uint64_t s = seed ? seed : 1;
+   for (int k = 0; k < 27 * 16; k++) h[net->off_in_w + k] = (float)(gauss(&s) * sqrt(2.0 / 27.0));
+   for (int l = 0; l < NTC; l++)
+      for (long k = 0; k < 27L * TC_CIN[l] * TC_COUT[l]; k++)
+         h[net->off_tc_w[l] + k] = (float)(gauss(&s) * sqrt(2.0 / (27.0 * TC_CIN[l])));
+   for (int k = 0; k < 27 * 16; k++) h[net->off_out_w + k] = (float)(0.1 * gauss(&s) * sqrt(1.0 / (27.0 * 16)));
+   cudaMemcpy(net->p, h, o * 4, cudaMemcpyHostToDevice);
+   free(h);
+   cudaMemset(net->m, 0, o * 4);
+   cudaMemset(net->v, 0, o * 4);
+   cudaMemset(net->d_err, 0, 4);
+   if (repack(net, 0)) {
+      pgb_net_destroy(net);
+      return 11;
+   }
+   *out = net;
+   return 0;
+}
+
+extern "C" int pgb_net_set_scales(pgb_net *net, double s_in, double s_out)
+{
+   net->s_in = s_in;
+   net->s_out = s_out;
+   return 0;
+}
+
+extern "C" long pgb_net_num_params(pgb_net *net) { return net->np; }
+
+/* which = 0 parameters, 1 gradients; to_device = 1 uploads (parameters) */
+extern "C" int pgb_net_params(pgb_net *net, int which, float *host, int to_device)
+{
+   float *d = which ? net->gp : net->p;
+   cudaError_t e = to_device ? cudaMemcpy(d, host, net->np * 4, cudaMemcpyHostToDevice)
+                             : cudaMemcpy(host, d, net->np * 4, cudaMemcpyDeviceToHost);
+   if (e != cudaSuccess) return arg_err("pgb_net_params: copy failed");
+   if (to_device && !which) return repack(net, 0);
+   return 0;
+}
+
+#define GRID_1D 1216
+#define NETK(call, name)                 \
+   do {                                  \
+      call;                              \
+      if (check_net(name)) return 11;    \
+   } while (0)
+
+static int tc(pgb_net *net, int l, const bf16 *in, bf16 *out, int adjoint, cudaStream_t st)
+{
+   const pgb_lvgeom &g = net->g[TC_LEV[l]];
+   if (!adjoint)
+      return conv_dispatch(TC_CIN[l], TC_COUT[l], in, out, net->img[l], net->p + net->off_tc_b[l], g, 1,
+                           net->d_err, st);
+   return conv_dispatch(TC_COUT[l], TC_CIN[l], in, out, net->img_adj[l], 0, g, 0, net->d_err, st);
+}
+
+static int forward(pgb_net *net, const double *rho, cudaStream_t st)
+{
+   bf16 **a = net->act;
+   pgb_lvgeom *g = net->g;
+   NETK((k_in_fwd<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->p + net->off_in_w,
+                                            net->p + net->off_in_b, a[A0], g[0])), "net in");
+   if (tc(net, 0, a[A0], a[A1], 0, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A1], a[B0], 16, g[0], g[1], 0)), "net pool");
+   if (tc(net, 1, a[B0], a[A2], 0, st) || tc(net, 2, a[A2], a[A3], 0, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A3], a[B1], 32, g[1], g[2], 0)), "net pool");
+   if (tc(net, 3, a[B1], a[A4], 0, st) || tc(net, 4, a[A4], a[A5], 0, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A5], a[B2], 64, g[2], g[3], 0)), "net pool");
+   if (tc(net, 5, a[B2], a[A6], 0, st) || tc(net, 6, a[A6], a[A7], 0, st)) return 11;
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A7], a[A5], a[C2], 64, g[2], g[3], 0)), "net up");
+   if (tc(net, 7, a[C2], a[A8], 0, st)) return 11;
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A8], a[A3], a[C1], 32, g[1], g[2], 0)), "net up");
+   if (tc(net, 8, a[C1], a[A9], 0, st)) return 11;
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A9], a[A1], a[C0], 16, g[0], g[1], 0)), "net up");
+   if (tc(net, 9, a[C0], a[A10], 0, st)) return 11;
+   NETK((k_out_fwd<<<GRID_1D, 256, 0, st>>>(a[A10], net->p + net->off_out_w, net->p + net->off_out_b, net->up,
+                                             g[0])), "net out");
+   return 0;
+}
+
+extern "C" int pgb_net_predict(pgb_net *net, const double *rho, double *u, void *stream)
+{
+   cudaStream_t st = (cudaStream_t)stream;
+   if (forward(net, rho, st)) return 11;
+   NETK((k_out_store<<<GRID_1D, 256, 0, st>>>(net->up, u, net->n, net->s_out, net->g[0])), "net store");
+   return 0;
+}
+
+static int wgrad(pgb_net *net, int l, const bf16 *x, const bf16 *gz, cudaStream_t st)
+{
+   const pgb_lvgeom &g = net->g[TC_LEV[l]];
+   const long chunks = ((long)g.D * g.plane + WCH - 1) / WCH;
+   const int nblk = (int)(chunks < 96 ? chunks : 96);
+   const size_t sh = (size_t)WCH * (TC_CIN[l] + TC_COUT[l]) * 4;
+   NETK((k_conv_bwd_w<<<dim3(nblk, 27), 256, sh, st>>>(x, gz, net->gp + net->off_tc_w[l], net->gp + net->off_tc_b[l],
+                                                         TC_CIN[l], TC_COUT[l], g)),
+        "net wgrad");
+   return 0;
+}
+
+/* loss and gradients of all parameters for one (rho, u) pair */
+static int loss_grad(pgb_net *net, const double *rho, const float *ut, cudaStream_t st)
+{
+   bf16 **a = net->act, **G = net->grad;
+   pgb_lvgeom *g = net->g;
+   if (forward(net, rho, st)) return 11;
+   if (cudaMemsetAsync(net->gp, 0, net->np * 4, st) != cudaSuccess ||
+       cudaMemsetAsync(net->d_loss, 0, 8, st) != cudaSuccess)
+      return check_net("net memset");
+   const int acc_bufs[3] = {A1, A3, A5};   /* gradients that two paths add into */
+   for (int k : acc_bufs)
+      if (cudaMemsetAsync(G[k], 0, act_bytes(g[ACT_LEV[k]], ACT_CH[k]), st) != cudaSuccess)
+         return check_net("net memset");
+   NETK((k_loss<<<GRID_1D, 256, 0, st>>>(net->up, ut, net->n, (float)(1.0 / net->s_out), net->gup, net->d_loss, g[0])),
+        "net loss");
+   NETK((k_out_bwd_w<<<dim3(96, 27), 256, 0, st>>>(a[A10], net->gup, net->gp + net->off_out_w, net->gp + net->off_out_b,
+                                                    g[0])), "net out w");
+   NETK((k_out_bwd_data<<<GRID_1D, 256, 0, st>>>(net->gup, net->p + net->off_out_w, G[A10], g[0])), "net out data");
+#define RELU(k, ch, lev) NETK((k_relu_bwd<<<GRID_1D, 256, 0, st>>>(G[k], a[k], ch, g[lev])), "net relu")
+   /* decoder: output gradient -> relu -> dW, input gradient = adjoint conv */
+   RELU(A10, 16, 0);
+   if (wgrad(net, 9, a[C0], G[A10], st) || tc(net, 9, G[A10], G[C0], 1, st)) return 11;
+   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A1], G[C0], 16, g[0])), "net add");
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C0], 0, G[A9], 16, g[0], g[1], 1)), "net up bwd");
+   RELU(A9, 16, 1);
+   if (wgrad(net, 8, a[C1], G[A9], st) || tc(net, 8, G[A9], G[C1], 1, st)) return 11;
+   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A3], G[C1], 32, g[1])), "net add");
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C1], 0, G[A8], 32, g[1], g[2], 1)), "net up bwd");
+   RELU(A8, 32, 2);
+   if (wgrad(net, 7, a[C2], G[A8], st) || tc(net, 7, G[A8], G[C2], 1, st)) return 11;
+   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A5], G[C2], 64, g[2])), "net add");
+   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C2], 0, G[A7], 64, g[2], g[3], 1)), "net up bwd");
+   /* bottom and encoder */
+   RELU(A7, 64, 3);
+   if (wgrad(net, 6, a[A6], G[A7], st) || tc(net, 6, G[A7], G[A6], 1, st)) return 11;
+   RELU(A6, 64, 3);
+   if (wgrad(net, 5, a[B2], G[A6], st) || tc(net, 5, G[A6], G[B2], 1, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A5], G[B2], 64, g[2], g[3], 1)), "net pool bwd");
+   RELU(A5, 64, 2);
+   if (wgrad(net, 4, a[A4], G[A5], st) || tc(net, 4, G[A5], G[A4], 1, st)) return 11;
+   RELU(A4, 64, 2);
+   if (wgrad(net, 3, a[B1], G[A4], st) || tc(net, 3, G[A4], G[B1], 1, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A3], G[B1], 32, g[1], g[2], 1)), "net pool bwd");
+   RELU(A3, 32, 1);
+   if (wgrad(net, 2, a[A2], G[A3], st) || tc(net, 2, G[A3], G[A2], 1, st)) return 11;
+   RELU(A2, 32, 1);
+   if (wgrad(net, 1, a[B0], G[A2], st) || tc(net, 1, G[A2], G[B0], 1, st)) return 11;
+   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A1], G[B0], 16, g[0], g[1], 1)), "net pool bwd");
+   RELU(A1, 16, 0);
+   if (wgrad(net, 0, a[A0], G[A1], st) || tc(net, 0, G[A1], G[A0], 1, st)) return 11;
+   RELU(A0, 16, 0);
+   NETK((k_in_bwd_w<<<dim3(96, 27), 256, 0, st>>>(rho, net->n, (float)net->s_in, G[A0], net->gp + net->off_in_w,
+                                                   net->gp + net->off_in_b, g[0])), "net in w");
+#undef RELU
+   return 0;
+}
+
+static int read_loss(pgb_net *net, double *loss, cudaStream_t st)
+{
+   int e = 0;
+   if (cudaMemcpyAsync(loss, net->d_loss, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+       cudaMemcpyAsync(&e, net->d_err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+       cudaStreamSynchronize(st) != cudaSuccess)
+      return arg_err("net: reading the loss back failed");
+   if (e) return arg_err("net: a wait inside a tensor-core convolution ran out");
+   return 0;
+}
+
+extern "C" int pgb_net_loss_grad(pgb_net *net, const double *rho, const float *ut, double *loss, void *stream)
+{
+   cudaStream_t st = (cudaStream_t)stream;
+   if (loss_grad(net, rho, ut, st)) return 11;
+   return read_loss(net, loss, st);
+}
+
+extern "C" int pgb_net_train_step(pgb_net *net, const double *rho, const float *ut, float lr, double *loss,
+                                  void *stream)
+{
+   cudaStream_t st = (cudaStream_t)stream;
+   if (loss_grad(net, rho, ut, st)) return 11;
+   net->step++;
+   const float b1 = 0.9f, b2 = 0.999f;
+   const float c1 = (float)(1.0 / (1.0 - pow(b1, (double)net->step)));
+   const float c2 = (float)(1.0 / (1.0 - pow(b2, (double)net->step)));
+   NETK((k_adam<<<GRID_1D, 256, 0, st>>>(net->p, net->gp, net->m, net->v, net->np, lr, b1, b2, c1, c2, 1e-8f)),
+        "net adam");
+   if (repack(net, st)) return 11;
+   return loss ? read_loss(net, loss, st) : 0;
+}
