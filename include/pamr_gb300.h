@@ -235,12 +235,13 @@ int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int ad
 int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H, int D,
                     int cin, int cout, int relu, int *err, void *stream);
 
-/* The learned initial guess: a 4-level convolutional encoder-decoder
- * (16/32/64/64 channels, two 3x3x3 convolutions per encoder level, one per
- * decoder level, additive skips, ReLU) from a source rho on an n^3 grid
- * (points 0..n-2 seen by the net; n-1 a multiple of 8, n >= 65) to a guess
- * of u, zero on the grid boundary. Forward and backward-data convolutions
- * of the inner ten layers run on the tensor cores (BF16, FP32
+/* The learned initial guess: a 6-level convolutional encoder-decoder
+ * (16/32/64/64/64/64 channels, levels halving down to (n-1)/32 points a
+ * side, two 3x3x3 convolutions per encoder level, one per decoder level,
+ * additive skips, ReLU) from a source rho on an n^3 grid (points 0..n-2
+ * seen by the net; n-1 a multiple of 32, n >= 65) to a guess of u, zero on
+ * the grid boundary. Forward and backward-data convolutions of the inner
+ * sixteen layers run on the tensor cores (BF16, FP32
  * accumulation); weight gradients and the 1-channel first and last layers
  * on CUDA cores; Adam on FP32 master weights. rho and u are device n^3
  * arrays (x fastest); the training target is FP32. Scales: the net reads

@@ -774,25 +774,64 @@ __global__ void k_adam(float *w, const float *gw, float *m, float *v, long n, fl
 }
 
 /* ------------------------------------------------------ the network (host) -- */
-/* 4-level encoder-decoder on an (n-1)^3 volume (points 0..n-2 of an n^3
- * grid): 16, 32, 64, 64 channels; two 3x3x3 convolutions per encoder
- * level, 2x2x2 average pooling down, nearest upsampling plus the encoder's
- * activation (additive skip) up, one convolution per decoder level, ReLU
- * after every convolution but the last. The first (1 -> 16) and last
- * (16 -> 1) convolutions run on CUDA cores, the ten others on the tensor
- * cores (forward, and backward-data through the adjoint image). */
-enum { NTC = 10 };
-static const int TC_LEV[NTC] = {0, 1, 1, 2, 2, 3, 3, 2, 1, 0};
-static const int TC_CIN[NTC] = {16, 16, 32, 32, 64, 64, 64, 64, 32, 16};
-static const int TC_COUT[NTC] = {16, 32, 32, 64, 64, 64, 64, 32, 16, 16};
-/* activations: a0 a1 | b0 a2 a3 | b1 a4 a5 | b2 a6 a7 | c2 a8 | c1 a9 | c0 a10 */
-enum { A0, A1, B0, A2, A3, B1, A4, A5, B2, A6, A7, C2, A8, C1, A9, C0, A10, NACT };
-static const int ACT_LEV[NACT] = {0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3, 2, 2, 1, 1, 0, 0};
-static const int ACT_CH[NACT] = {16, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 64, 32, 32, 16, 16, 16};
+/* NLEV-level encoder-decoder on an (n-1)^3 volume (points 0..n-2 of an n^3
+ * grid), levels halving down to (n-1)/32 points a side so that the
+ * coarsest convolutions see the whole volume (the solution of the Poisson
+ * equation at a point depends on the source everywhere). LCH[v] channels
+ * on level v; two 3x3x3 convolutions per encoder level (one after the
+ * input convolution on level 0), 2x2x2 average pooling down, nearest
+ * upsampling plus the encoder's activation (additive skip) up, one
+ * convolution per decoder level, ReLU after every convolution but the
+ * last. The first (1 -> 16) and last (16 -> 1) convolutions run on CUDA
+ * cores, the others on the tensor cores (forward, and backward-data
+ * through the adjoint image).
+ *
+ * Tensor-core layers in parameter order: 0 = level 0 encoder; 2v-1, 2v =
+ * level v encoder (LCH[v-1] -> LCH[v], LCH[v] -> LCH[v]); then the decoder
+ * from level NLEV-2 up to 0, level v mapping LCH[v] -> LCH[max(v-1, 0)] so
+ * that its output adds onto the skip of level v-1. */
+enum { NLEV = 6, NTC = 3 * NLEV - 2 };
+static const int LCH[NLEV] = {16, 32, 64, 64, 64, 64};
+static int TC_LEV[NTC], TC_CIN[NTC], TC_COUT[NTC];
+static int dec_layer(int v) { return 2 * (NLEV - 1) + 1 + (NLEV - 2 - v); }
+
+static void layer_table()
+{
+   TC_LEV[0] = 0, TC_CIN[0] = TC_COUT[0] = LCH[0];
+   for (int v = 1; v < NLEV; v++) {
+      TC_LEV[2 * v - 1] = TC_LEV[2 * v] = v;
+      TC_CIN[2 * v - 1] = LCH[v - 1];
+      TC_COUT[2 * v - 1] = TC_CIN[2 * v] = TC_COUT[2 * v] = LCH[v];
+   }
+   for (int v = NLEV - 2; v >= 0; v--) {
+      const int l = dec_layer(v);
+      TC_LEV[l] = v;
+      TC_CIN[l] = LCH[v];
+      TC_COUT[l] = LCH[v > 0 ? v - 1 : 0];
+   }
+}
+
+/* activations per level: E0, E1 (encoder), P (pooled input, v >= 1), C
+ * (upsampled decoder + skip, v <= NLEV-2), D (decoder output, v <= NLEV-2) */
+enum { K_E0, K_E1, K_P, K_C, K_D, NKIND };
+enum { NACT = NKIND * NLEV };
+static int act_id(int kind, int v) { return kind * NLEV + v; }
+
+static int act_ch(int kind, int v)
+{
+   if (kind == K_P) return LCH[v - 1];
+   if (kind == K_D) return LCH[v > 0 ? v - 1 : 0];
+   return LCH[v];
+}
+
+static bool act_used(int kind, int v)
+{
+   return !((kind == K_P && v == 0) || ((kind == K_C || kind == K_D) && v == NLEV - 1));
+}
 
 struct pgb_net {
    int n;
-   pgb_lvgeom g[4];
+   pgb_lvgeom g[NLEV];
    double s_in, s_out;
    long np;                       /* parameter count */
    float *p, *gp, *m, *v;         /* parameters, gradients, Adam moments */
@@ -858,22 +897,25 @@ extern "C" void pgb_net_destroy(pgb_net *net)
 extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
 {
    *out = 0;
-   if (n < 65 || (n - 1) % 8 != 0) return arg_err("pgb_net_create: n-1 must be a multiple of 8, n >= 65");
+   const int step = 1 << (NLEV - 1);
+   if (n < 2 * step + 1 || (n - 1) % step != 0)
+      return arg_err("pgb_net_create: n-1 must be a multiple of 32, n >= 65");
+   layer_table();
    pgb_net *net = (pgb_net *)calloc(1, sizeof(pgb_net));
    net->n = n;
    net->s_in = net->s_out = 1.0;
-   for (int l = 0; l < 4; l++) {
+   for (int l = 0; l < NLEV; l++) {
       const int e = (n - 1) >> l;
       net->g[l] = make_geom(e, e, e);
    }
    long o = 0;
-   net->off_in_w = o; o += 27 * 16;
-   net->off_in_b = o; o += 16;
+   net->off_in_w = o; o += 27 * LCH[0];
+   net->off_in_b = o; o += LCH[0];
    for (int l = 0; l < NTC; l++) {
       net->off_tc_w[l] = o; o += 27L * TC_CIN[l] * TC_COUT[l];
       net->off_tc_b[l] = o; o += TC_COUT[l];
    }
-   net->off_out_w = o; o += 27 * 16;
+   net->off_out_w = o; o += 27 * LCH[0];
    net->off_out_b = o; o += 1;
    net->np = o;
    const size_t nv = (size_t)(n - 1) * (n - 1) * (n - 1);
@@ -884,11 +926,14 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
    for (int l = 0; l < NTC && ok; l++)
       ok = cudaMalloc((void **)&net->img[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess &&
            cudaMalloc((void **)&net->img_adj[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess;
-   for (int a = 0; a < NACT && ok; a++) {
-      const size_t b = act_bytes(net->g[ACT_LEV[a]], ACT_CH[a]);
-      ok = cudaMalloc((void **)&net->act[a], b) == cudaSuccess && cudaMalloc((void **)&net->grad[a], b) == cudaSuccess &&
-           cudaMemset(net->act[a], 0, b) == cudaSuccess && cudaMemset(net->grad[a], 0, b) == cudaSuccess;
-   }
+   for (int k = 0; k < NKIND && ok; k++)
+      for (int v = 0; v < NLEV && ok; v++) {
+         if (!act_used(k, v)) continue;
+         const int a = act_id(k, v);
+         const size_t b = act_bytes(net->g[v], act_ch(k, v));
+         ok = cudaMalloc((void **)&net->act[a], b) == cudaSuccess && cudaMalloc((void **)&net->grad[a], b) == cudaSuccess &&
+              cudaMemset(net->act[a], 0, b) == cudaSuccess && cudaMemset(net->grad[a], 0, b) == cudaSuccess;
+      }
    if (!ok) {
       pgb_net_destroy(net);
       return arg_err("pgb_net_create: device allocation failed");
@@ -896,11 +941,12 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
    /* He-normal weights (the last layer scaled down), zero biases */
    float *h = (float *)calloc(o, 4);
    uint64_t s = seed ? seed : 1;
-   for (int k = 0; k < 27 * 16; k++) h[net->off_in_w + k] = (float)(gauss(&s) * sqrt(2.0 / 27.0));
+   for (int k = 0; k < 27 * LCH[0]; k++) h[net->off_in_w + k] = (float)(gauss(&s) * sqrt(2.0 / 27.0));
    for (int l = 0; l < NTC; l++)
       for (long k = 0; k < 27L * TC_CIN[l] * TC_COUT[l]; k++)
          h[net->off_tc_w[l] + k] = (float)(gauss(&s) * sqrt(2.0 / (27.0 * TC_CIN[l])));
-   for (int k = 0; k < 27 * 16; k++) h[net->off_out_w + k] = (float)(0.1 * gauss(&s) * sqrt(1.0 / (27.0 * 16)));
+   for (int k = 0; k < 27 * LCH[0]; k++)
+      h[net->off_out_w + k] = (float)(0.1 * gauss(&s) * sqrt(1.0 / (27.0 * LCH[0])));
    cudaMemcpy(net->p, h, o * 4, cudaMemcpyHostToDevice);
    free(h);
    cudaMemset(net->m, 0, o * 4);
@@ -950,27 +996,31 @@ static int tc(pgb_net *net, int l, const bf16 *in, bf16 *out, int adjoint, cudaS
    return conv_dispatch(TC_COUT[l], TC_CIN[l], in, out, net->img_adj[l], 0, g, 0, net->d_err, st);
 }
 
+/* what level v's upsampling reads: the coarsest encoder output for the
+ * level above the bottom, else the decoder output of level v+1 */
+static int coarse_src(int v) { return v + 1 == NLEV - 1 ? act_id(K_E1, NLEV - 1) : act_id(K_D, v + 1); }
+
 static int forward(pgb_net *net, const double *rho, cudaStream_t st)
 {
    bf16 **a = net->act;
    pgb_lvgeom *g = net->g;
+#define A(k, v) a[act_id(k, v)]
    NETK((k_in_fwd<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->p + net->off_in_w,
-                                            net->p + net->off_in_b, a[A0], g[0])), "net in");
-   if (tc(net, 0, a[A0], a[A1], 0, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A1], a[B0], 16, g[0], g[1], 0)), "net pool");
-   if (tc(net, 1, a[B0], a[A2], 0, st) || tc(net, 2, a[A2], a[A3], 0, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A3], a[B1], 32, g[1], g[2], 0)), "net pool");
-   if (tc(net, 3, a[B1], a[A4], 0, st) || tc(net, 4, a[A4], a[A5], 0, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(a[A5], a[B2], 64, g[2], g[3], 0)), "net pool");
-   if (tc(net, 5, a[B2], a[A6], 0, st) || tc(net, 6, a[A6], a[A7], 0, st)) return 11;
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A7], a[A5], a[C2], 64, g[2], g[3], 0)), "net up");
-   if (tc(net, 7, a[C2], a[A8], 0, st)) return 11;
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A8], a[A3], a[C1], 32, g[1], g[2], 0)), "net up");
-   if (tc(net, 8, a[C1], a[A9], 0, st)) return 11;
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[A9], a[A1], a[C0], 16, g[0], g[1], 0)), "net up");
-   if (tc(net, 9, a[C0], a[A10], 0, st)) return 11;
-   NETK((k_out_fwd<<<GRID_1D, 256, 0, st>>>(a[A10], net->p + net->off_out_w, net->p + net->off_out_b, net->up,
+                                            net->p + net->off_in_b, A(K_E0, 0), g[0])), "net in");
+   if (tc(net, 0, A(K_E0, 0), A(K_E1, 0), 0, st)) return 11;
+   for (int v = 1; v < NLEV; v++) {
+      NETK((k_pool<<<GRID_1D, 256, 0, st>>>(A(K_E1, v - 1), A(K_P, v), LCH[v - 1], g[v - 1], g[v], 0)), "net pool");
+      if (tc(net, 2 * v - 1, A(K_P, v), A(K_E0, v), 0, st) || tc(net, 2 * v, A(K_E0, v), A(K_E1, v), 0, st))
+         return 11;
+   }
+   for (int v = NLEV - 2; v >= 0; v--) {
+      NETK((k_up<<<GRID_1D, 256, 0, st>>>(a[coarse_src(v)], A(K_E1, v), A(K_C, v), LCH[v], g[v], g[v + 1], 0)),
+           "net up");
+      if (tc(net, dec_layer(v), A(K_C, v), A(K_D, v), 0, st)) return 11;
+   }
+   NETK((k_out_fwd<<<GRID_1D, 256, 0, st>>>(A(K_D, 0), net->p + net->off_out_w, net->p + net->off_out_b, net->up,
                                              g[0])), "net out");
+#undef A
    return 0;
 }
 
@@ -994,6 +1044,16 @@ static int wgrad(pgb_net *net, int l, const bf16 *x, const bf16 *gz, cudaStream_
    return 0;
 }
 
+/* backward of one ReLU convolution x -> y: the gradient of y (taken through
+ * the ReLU in place) gives the weight gradient and the gradient of x */
+static int conv_bwd(pgb_net *net, int l, int x, int y, cudaStream_t st)
+{
+   bf16 **a = net->act, **G = net->grad;
+   NETK((k_relu_bwd<<<GRID_1D, 256, 0, st>>>(G[y], a[y], TC_COUT[l], net->g[TC_LEV[l]])), "net relu");
+   if (wgrad(net, l, a[x], G[y], st) || tc(net, l, G[y], G[x], 1, st)) return 11;
+   return 0;
+}
+
 /* loss and gradients of all parameters for one (rho, u) pair */
 static int loss_grad(pgb_net *net, const double *rho, const float *ut, cudaStream_t st)
 {
@@ -1003,51 +1063,38 @@ static int loss_grad(pgb_net *net, const double *rho, const float *ut, cudaStrea
    if (cudaMemsetAsync(net->gp, 0, net->np * 4, st) != cudaSuccess ||
        cudaMemsetAsync(net->d_loss, 0, 8, st) != cudaSuccess)
       return check_net("net memset");
-   const int acc_bufs[3] = {A1, A3, A5};   /* gradients that two paths add into */
-   for (int k : acc_bufs)
-      if (cudaMemsetAsync(G[k], 0, act_bytes(g[ACT_LEV[k]], ACT_CH[k]), st) != cudaSuccess)
+   /* the encoder outputs above the bottom take gradients along two paths
+    * (skip and pooling): they accumulate from zero */
+   for (int v = 0; v < NLEV - 1; v++)
+      if (cudaMemsetAsync(G[act_id(K_E1, v)], 0, act_bytes(g[v], LCH[v]), st) != cudaSuccess)
          return check_net("net memset");
    NETK((k_loss<<<GRID_1D, 256, 0, st>>>(net->up, ut, net->n, (float)(1.0 / net->s_out), net->gup, net->d_loss, g[0])),
         "net loss");
-   NETK((k_out_bwd_w<<<dim3(96, 27), 256, 0, st>>>(a[A10], net->gup, net->gp + net->off_out_w, net->gp + net->off_out_b,
+   const int d0 = act_id(K_D, 0);
+   NETK((k_out_bwd_w<<<dim3(96, 27), 256, 0, st>>>(a[d0], net->gup, net->gp + net->off_out_w, net->gp + net->off_out_b,
                                                     g[0])), "net out w");
-   NETK((k_out_bwd_data<<<GRID_1D, 256, 0, st>>>(net->gup, net->p + net->off_out_w, G[A10], g[0])), "net out data");
-#define RELU(k, ch, lev) NETK((k_relu_bwd<<<GRID_1D, 256, 0, st>>>(G[k], a[k], ch, g[lev])), "net relu")
-   /* decoder: output gradient -> relu -> dW, input gradient = adjoint conv */
-   RELU(A10, 16, 0);
-   if (wgrad(net, 9, a[C0], G[A10], st) || tc(net, 9, G[A10], G[C0], 1, st)) return 11;
-   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A1], G[C0], 16, g[0])), "net add");
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C0], 0, G[A9], 16, g[0], g[1], 1)), "net up bwd");
-   RELU(A9, 16, 1);
-   if (wgrad(net, 8, a[C1], G[A9], st) || tc(net, 8, G[A9], G[C1], 1, st)) return 11;
-   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A3], G[C1], 32, g[1])), "net add");
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C1], 0, G[A8], 32, g[1], g[2], 1)), "net up bwd");
-   RELU(A8, 32, 2);
-   if (wgrad(net, 7, a[C2], G[A8], st) || tc(net, 7, G[A8], G[C2], 1, st)) return 11;
-   NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[A5], G[C2], 64, g[2])), "net add");
-   NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[C2], 0, G[A7], 64, g[2], g[3], 1)), "net up bwd");
-   /* bottom and encoder */
-   RELU(A7, 64, 3);
-   if (wgrad(net, 6, a[A6], G[A7], st) || tc(net, 6, G[A7], G[A6], 1, st)) return 11;
-   RELU(A6, 64, 3);
-   if (wgrad(net, 5, a[B2], G[A6], st) || tc(net, 5, G[A6], G[B2], 1, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A5], G[B2], 64, g[2], g[3], 1)), "net pool bwd");
-   RELU(A5, 64, 2);
-   if (wgrad(net, 4, a[A4], G[A5], st) || tc(net, 4, G[A5], G[A4], 1, st)) return 11;
-   RELU(A4, 64, 2);
-   if (wgrad(net, 3, a[B1], G[A4], st) || tc(net, 3, G[A4], G[B1], 1, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A3], G[B1], 32, g[1], g[2], 1)), "net pool bwd");
-   RELU(A3, 32, 1);
-   if (wgrad(net, 2, a[A2], G[A3], st) || tc(net, 2, G[A3], G[A2], 1, st)) return 11;
-   RELU(A2, 32, 1);
-   if (wgrad(net, 1, a[B0], G[A2], st) || tc(net, 1, G[A2], G[B0], 1, st)) return 11;
-   NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[A1], G[B0], 16, g[0], g[1], 1)), "net pool bwd");
-   RELU(A1, 16, 0);
-   if (wgrad(net, 0, a[A0], G[A1], st) || tc(net, 0, G[A1], G[A0], 1, st)) return 11;
-   RELU(A0, 16, 0);
-   NETK((k_in_bwd_w<<<dim3(96, 27), 256, 0, st>>>(rho, net->n, (float)net->s_in, G[A0], net->gp + net->off_in_w,
+   NETK((k_out_bwd_data<<<GRID_1D, 256, 0, st>>>(net->gup, net->p + net->off_out_w, G[d0], g[0])), "net out data");
+   /* decoder, fine to coarse */
+   for (int v = 0; v <= NLEV - 2; v++) {
+      const int c = act_id(K_C, v);
+      if (conv_bwd(net, dec_layer(v), c, act_id(K_D, v), st)) return 11;
+      NETK((k_add<<<GRID_1D, 256, 0, st>>>(G[act_id(K_E1, v)], G[c], LCH[v], g[v])), "net add");
+      NETK((k_up<<<GRID_1D, 256, 0, st>>>(G[c], 0, G[coarse_src(v)], LCH[v], g[v], g[v + 1], 1)), "net up bwd");
+   }
+   /* encoder, coarse to fine */
+   for (int v = NLEV - 1; v >= 1; v--) {
+      const int p = act_id(K_P, v);
+      if (conv_bwd(net, 2 * v, act_id(K_E0, v), act_id(K_E1, v), st) ||
+          conv_bwd(net, 2 * v - 1, p, act_id(K_E0, v), st))
+         return 11;
+      NETK((k_pool<<<GRID_1D, 256, 0, st>>>(G[act_id(K_E1, v - 1)], G[p], LCH[v - 1], g[v - 1], g[v], 1)),
+           "net pool bwd");
+   }
+   const int e0 = act_id(K_E0, 0);
+   if (conv_bwd(net, 0, e0, act_id(K_E1, 0), st)) return 11;
+   NETK((k_relu_bwd<<<GRID_1D, 256, 0, st>>>(G[e0], a[e0], LCH[0], g[0])), "net relu");
+   NETK((k_in_bwd_w<<<dim3(96, 27), 256, 0, st>>>(rho, net->n, (float)net->s_in, G[e0], net->gp + net->off_in_w,
                                                    net->gp + net->off_in_b, g[0])), "net in w");
-#undef RELU
    return 0;
 }
 

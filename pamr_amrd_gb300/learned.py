@@ -1,5 +1,5 @@
 """Learned initial guess of the multigrid solve (binding of pgb_net_* in
-libpamr_gb300): a 4-level convolutional encoder-decoder from the source rho
+libpamr_gb300): a 6-level convolutional encoder-decoder from the source rho
 to a guess of u, trained on (rho, u) pairs the plain multigrid generates.
 The kernels (BF16 tensor-core convolutions, training step) are in
 pamr_amrd_gb300/csrc/pgb_net.cu; this module only sequences calls."""
@@ -43,12 +43,26 @@ def conv_lib():
 
 
 class Net:
-    """n: grid points per side of the solve (n-1 a multiple of 8, n >= 65)"""
+    """n: grid points per side of the solve (n-1 a multiple of 32, n >= 65)"""
 
-    # layer table in parameter order: (name, cin, cout)
-    LAYERS = [("in", 1, 16)] + [(f"tc{i}", a, b) for i, (a, b) in enumerate(
-        [(16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (64, 64), (64, 64), (64, 32), (32, 16),
-         (16, 16)])] + [("out", 16, 1)]
+    # levels and channels per level (pgb_net.cu: NLEV, LCH)
+    NLEV = 6
+    LCH = (16, 32, 64, 64, 64, 64)
+
+    @classmethod
+    def dec_layer(cls, v: int) -> int:
+        """index of the tensor-core layer of level v's decoder"""
+        return 2 * (cls.NLEV - 1) + 1 + (cls.NLEV - 2 - v)
+
+    @classmethod
+    def layers(cls):
+        """layer table in parameter order: (name, cin, cout)"""
+        ch = cls.LCH
+        tcl = [(ch[0], ch[0])]
+        for v in range(1, cls.NLEV):
+            tcl += [(ch[v - 1], ch[v]), (ch[v], ch[v])]
+        tcl += [(ch[v], ch[max(v - 1, 0)]) for v in range(cls.NLEV - 2, -1, -1)]
+        return [("in", 1, ch[0])] + [(f"tc{i}", a, b) for i, (a, b) in enumerate(tcl)] + [("out", ch[0], 1)]
 
     def __init__(self, n: int, seed: int = 1):
         L = _bind()
@@ -56,6 +70,8 @@ class Net:
         _check(L.pgb_net_create(n, seed, C.byref(h)))
         self.h, self.n = h, n
         self.s_in = self.s_out = 1.0
+        if self.num_params() != sum(27 * ci * co + co for _, ci, co in self.LAYERS):
+            raise RuntimeError("pgb_net: layer table of the library and of learned.py differ")
 
     def close(self):
         if self.h:
@@ -107,3 +123,122 @@ class Net:
         _check(lib().pgb_net_train_step(self.h, rho_ptr, ut_ptr, lr, C.byref(loss) if want_loss else None,
                                         stream))
         return loss.value if want_loss else None
+
+
+Net.LAYERS = Net.layers()
+
+
+# ------------------------------------------------ data, training, use ----
+def rho_on_device(n: int, blobs, torch):
+    """poisson3d's source on the device (FP64, x fastest), from its blobs"""
+    x = torch.linspace(-10.0, 10.0, n, dtype=torch.float64, device="cuda")
+    Z, Y, X = torch.meshgrid(x, x, x, indexing="ij")
+    r = torch.zeros_like(X)
+    for a, w, c in blobs:
+        r += a * torch.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / (w * w))
+    return r.reshape(-1).contiguous()
+
+
+def source_charge(rho, h: float) -> float:
+    """sum |rho| h^3: the scale of a sample (rho a device tensor)"""
+    return max(float(rho.abs().sum()) * h ** 3, 1e-300)
+
+
+class Scaled:
+    """The equation is linear in rho, so every sample is scaled by its own
+    source charge Q: the net reads rho / Q and predicts u / (gain * Q),
+    `gain` (max |u| / Q over the training pairs) fixed at training, so that
+    inputs and targets are of order one whatever the source's size."""
+
+    def __init__(self, net: Net, gain: float, h: float):
+        self.net, self.gain, self.h = net, gain, h
+
+    def _scale(self, rho) -> None:
+        q = source_charge(rho, self.h)
+        self.net.set_scales(1.0 / q, self.gain * q)
+
+    def train_step(self, rho, ut, lr: float, want_loss: bool = True):
+        self._scale(rho)
+        return self.net.train_step(rho.data_ptr(), ut.data_ptr(), lr, want_loss=want_loss)
+
+    def predict(self, rho, u, stream=None):
+        self._scale(rho)
+        self.net.predict(rho.data_ptr(), u.data_ptr(), stream)
+
+
+def make_dataset(n: int, seeds, torch, cycles: int = 12, precision: int = 1):
+    """(rho, u) training pairs from the plain multigrid: for each seed the
+    poisson3d source and the solution after `cycles` V-cycles (about 1e-12
+    of the initial residual); u kept as FP32 on the device"""
+    import copy
+    from . import workloads as W
+    from .solver import Solver
+    case = copy.deepcopy(W.poisson3d(n, seed=0, rel_tol=0))
+    case.params.precision = precision
+    case.params.tol = 0.0
+    case.params.max_iter = cycles
+    case.params.min_iter = cycles
+    s = Solver(case)
+    zero = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    u = torch.empty(n ** 3, dtype=torch.float64, device="cuda")
+    blobs, U = [], torch.empty(len(seeds), n ** 3, dtype=torch.float32, device="cuda")
+    for k, seed in enumerate(seeds):
+        b = W.poisson3d_blobs(seed)
+        rho = rho_on_device(n, b, torch)
+        s.set_inputs_device([zero.data_ptr()], [rho.data_ptr()])
+        s.solve()
+        _check(lib().pgb_get_grid_device(s.h, 0, u.data_ptr()))
+        torch.cuda.synchronize()
+        U[k] = u.float()
+        blobs.append(b)
+    s.close()
+    return blobs, U
+
+
+def fit_gain(n: int, blobs, U, torch) -> float:
+    h = 20.0 / (n - 1)
+    return max(float(U[i].abs().max()) / source_charge(rho_on_device(n, b, torch), h) for i, b in enumerate(blobs))
+
+
+def train(model: Scaled, blobs, U, torch, epochs: int = 2, lr: float = 1e-3, lr_end: float = 1e-5, seed: int = 0,
+          log=None):
+    """Adam over the pairs, one pair per step, cosine learning-rate decay;
+    returns the mean loss of each epoch"""
+    n, N = model.net.n, len(blobs)
+    order = np.random.default_rng(seed)
+    steps, k, out = epochs * N, 0, []
+    for ep in range(epochs):
+        tot = 0.0
+        for i in order.permutation(N):
+            rate = lr_end + 0.5 * (lr - lr_end) * (1 + np.cos(np.pi * k / max(1, steps - 1)))
+            tot += model.train_step(rho_on_device(n, blobs[i], torch), U[i], float(rate))
+            k += 1
+        out.append(tot / N)
+        if log:
+            log(f"epoch {ep}: mean loss {out[-1]:.4e}")
+    return out
+
+
+class GuessPolicy:
+    """Uses the net's guess as the initial u of a solve while it cuts
+    V-cycles. The plain solve always runs to tolerance after the guess, so
+    a bad guess costs cycles, never accuracy; when guessed solves stop
+    needing fewer cycles than the last unguessed one (`patience` times in a
+    row) the policy goes back to the plain initial guess (u = 0)."""
+
+    def __init__(self, patience: int = 2):
+        self.patience, self.strikes, self.plain_cycles, self.enabled = patience, 0, None, True
+
+    def use_guess(self) -> bool:
+        return self.enabled and self.plain_cycles is not None
+
+    def record(self, cycles: int, guessed: bool):
+        if not guessed:
+            self.plain_cycles = cycles
+            return
+        if self.plain_cycles is not None and cycles >= self.plain_cycles:
+            self.strikes += 1
+            if self.strikes >= self.patience:
+                self.enabled = False
+        else:
+            self.strikes = 0

@@ -205,6 +205,38 @@ def poisson2d(n: int = 129, seed: int = 0, rel_tol: float = 1e-10,
     return _finish(case, rel_tol)
 
 
+def poisson3d_blobs(seed: int = 0):
+    """the four Gaussians (amplitude, width, centre) of poisson3d"""
+    rng = SplitMix64(0x5EED0005 + seed)
+    blobs = []
+    for _ in range(4):
+        a = rng.uniform(0.0, 0.05)
+        w = rng.uniform(0.5, 2.0)
+        c = (rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5))
+        blobs.append((a, w, c))
+    return blobs
+
+
+def poisson3d_charge(blobs) -> float:
+    """the integral of poisson3d's source over all space (each Gaussian
+    a * exp(-r^2 / w^2) holds a * pi^(3/2) * w^3); the boundary cuts off a
+    negligible tail"""
+    return sum(a * math.pi ** 1.5 * w ** 3 for a, w, _ in blobs)
+
+
+def poisson3d(n: int = 129, seed: int = 0, rel_tol: float = 1e-10,
+              params: MGParams | None = None) -> Case:
+    """the learned-initial-guess workload: lap u = rho on [-10,10]^3, one
+    n^3 grid, u = 0 on the boundary, rho = 4 Gaussians drawn like
+    conformal3d's source (amplitude U(0, 0.05): the linear equation has no
+    existence limit)"""
+    bbox = (-10.0, 10.0, -10.0, 10.0, -10.0, 10.0)
+    g = Grid(1, bbox, (n, n, n))
+    case = Case(f"poisson3d_{n}", POISSON, 3, (n, n, n), bbox, [g], [np.zeros(g.size)],
+                [_gaussians(g, 3, poisson3d_blobs(seed))], params or MGParams())
+    return _finish(case, rel_tol)
+
+
 def conformal3d(n: int = 129, m: int = 65, seed: int = 0, rel_tol: float = 1e-10,
                 params: MGParams | None = None, levels: int = 3) -> Case:
     rng = SplitMix64(0x5EED0002 + seed)

@@ -105,15 +105,13 @@ def _torch_net(net, flat, x):
         return torch.relu(y) if relu else y
 
     up = lambda a: F.interpolate(a, scale_factor=2, mode="nearest")  # noqa: E731
-    a0 = conv("in", x)
-    a1 = conv("tc0", a0)
-    a3 = conv("tc2", conv("tc1", F.avg_pool3d(a1, 2)))
-    a5 = conv("tc4", conv("tc3", F.avg_pool3d(a3, 2)))
-    a7 = conv("tc6", conv("tc5", F.avg_pool3d(a5, 2)))
-    a8 = conv("tc7", up(a7) + a5)
-    a9 = conv("tc8", up(a8) + a3)
-    a10 = conv("tc9", up(a9) + a1)
-    return conv("out", a10, relu=False), P
+    e1 = [conv("tc0", conv("in", x))]
+    for v in range(1, net.NLEV):
+        e1.append(conv(f"tc{2 * v}", conv(f"tc{2 * v - 1}", F.avg_pool3d(e1[v - 1], 2))))
+    d = e1[-1]
+    for v in range(net.NLEV - 2, -1, -1):
+        d = conv(f"tc{net.dec_layer(v)}", up(d) + e1[v])
+    return conv("out", d, relu=False), P
 
 
 def _smooth_field(n, rng, amp=1.0):
