@@ -17,6 +17,10 @@ reference's path) on this machine's host cores.
 
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 N>1 runs N independent replicas (one per GPU, launched by torch.distributed.run).
+
+python bench.py --workload poisson3d_learned [--pairs P --epochs E] trains the
+learned initial guess on P multigrid-generated pairs and prints one line
+comparing plain solves with guessed ones (V-cycles and solves/s).
 """
 from __future__ import annotations
 
@@ -139,6 +143,119 @@ def ncu_traffic():
     return None
 
 
+# ------------------------------------------------ learned initial guess --
+LEARNED_WORKLOAD = ("poisson3d_129: lap u = rho on [-10,10]^3, one 129^3 grid (6 MG levels), "
+                    "rho = 4 seeded Gaussians, V(2,2) to 1e-10 relative residual; guess = 6-level "
+                    "BF16 tensor-core encoder-decoder trained on multigrid-generated pairs")
+
+
+def learned_main(args):
+    """plain solves against solves started from the net's guess (prediction
+    plus energy-norm rescale, timed with the solve), both precision forms,
+    on held-out sources; the guess policy's solves/s is `value`"""
+    import numpy as np
+    import torch
+    from pamr_amrd_gb300 import learned as Lm
+    from pamr_amrd_gb300 import solver as S
+    from pamr_amrd_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    n = 129
+    h = 20.0 / (n - 1)
+    t0 = time.perf_counter()
+    blobs, U = Lm.make_dataset(n, range(args.pairs), torch)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    gain = Lm.fit_gain(n, blobs, U, torch)
+    model = Lm.Scaled(Lm.Net(n, seed=1), gain, h)
+    t0 = time.perf_counter()
+    losses = Lm.train(model, blobs, U, torch, epochs=args.epochs, lr=args.lr)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del U
+
+    seeds = [100000 + k for k in range(args.warmup + args.steps)]
+    rhos = [Lm.rho_on_device(n, W.poisson3d_blobs(sd), torch) for sd in seeds]
+    zero = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    guess = torch.zeros_like(zero)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for prec, form in ((0, "fp64"), (1, "mixed")):
+        case = W.poisson3d(n, seed=seeds[0])
+        case.params.precision = prec
+        sv = S.Solver(case)
+        st = torch.cuda.ExternalStream(sv.stream())
+        u_plain = torch.empty_like(zero)
+        res = {"plain": [], "guess": []}
+        errs = []
+        for k, rho in enumerate(rhos):
+            for mode in ("plain", "guess"):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                if mode == "guess":
+                    model.predict(rho, guess, sv.stream())
+                    sv.set_inputs_device([guess.data_ptr()], [rho.data_ptr()])
+                else:
+                    sv.set_inputs_device([zero.data_ptr()], [rho.data_ptr()])
+                r = sv.solve()
+                e1.record(st)
+                e1.synchronize()
+                if k < args.warmup:
+                    continue
+                res[mode].append((e0.elapsed_time(e1), r["iters"], r["res_final"] <= case.params.tol))
+                if mode == "plain":
+                    S._check(S.lib().pgb_get_grid_device(sv.h, 0, u_plain.data_ptr()))
+            if k >= args.warmup and prec == 1:
+                model.predict(rho, guess, sv.stream())
+                torch.cuda.synchronize()
+                d = guess - u_plain
+                errs.append((float(d.abs().max() / u_plain.abs().max()),
+                             float(d.norm() / u_plain.norm())))
+        # the guess policy over the same sources: one plain solve first, then
+        # guesses while they cut cycles
+        pol = Lm.GuessPolicy()
+        pol_ms, used = 0.0, 0
+        for k in range(args.steps):
+            use = pol.use_guess()
+            ms, it, _ = res["guess" if use else "plain"][k]
+            pol.record(it, use, ms)
+            pol_ms += ms
+            used += use
+        out[form] = {
+            "plain_solves_per_s": 1e3 * args.steps / sum(m for m, _, _ in res["plain"]),
+            "guess_solves_per_s": 1e3 * args.steps / sum(m for m, _, _ in res["guess"]),
+            "policy_solves_per_s": 1e3 * args.steps / pol_ms,
+            "plain_vcycles": statistics.mean(i for _, i, _ in res["plain"]),
+            "guess_vcycles": statistics.mean(i for _, i, _ in res["guess"]),
+            "policy_guessed_solves": used, "policy_enabled_at_end": pol.enabled,
+            "all_converged": all(c for _, _, c in res["plain"] + res["guess"])}
+        sv.close()
+    # prediction alone (forward + rescale)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for _ in range(3):
+        model.predict(rhos[0], guess)
+    ev[0].record()
+    for _ in range(10):
+        model.predict(rhos[0], guess)
+    ev[1].record()
+    torch.cuda.synchronize()
+    mx = out["mixed"]
+    line = {"metric": "poisson3d_129 solves/s with the learned initial guess (guess policy), mixed form",
+            "value": mx["policy_solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 / mx["policy_solves_per_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 guess + f32/f64 solve",
+            "data": "synthetic (seeded rho; training seeds 0..pairs-1, timed on held-out seeds 100000+)",
+            "config": {"workload": LEARNED_WORKLOAD, "l2": "flushed between steps (512 MiB write)",
+                       "pairs": args.pairs, "epochs": args.epochs, "lr": args.lr},
+            "forms": out, "predict_ms": ev[0].elapsed_time(ev[1]) / 10,
+            "guess_error_vs_solution": {"max_rel": statistics.mean(e[0] for e in errs),
+                                        "l2_rel": statistics.mean(e[1] for e in errs)},
+            "training": {"dataset_s": t_data, "train_s": t_train, "epoch_loss": losses,
+                         "params": model.net.num_params()}}
+    print(json.dumps(line))
+
+
 # ---------------------------------------------------------------- main --
 def main():
     ap = argparse.ArgumentParser()
@@ -147,7 +264,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="conformal3d", choices=["conformal3d", "poisson3d_learned"],
+                    help="poisson3d_learned: solves with and without the learned initial guess")
+    ap.add_argument("--pairs", type=int, default=2000, help="training pairs (poisson3d_learned)")
+    ap.add_argument("--epochs", type=int, default=4, help="training epochs (poisson3d_learned)")
+    ap.add_argument("--lr", type=float, default=1e-3, help="peak learning rate (poisson3d_learned)")
     args = ap.parse_args()
+    if args.workload == "poisson3d_learned":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned initial guess"}))
+        elif int(os.environ.get("RANK", "0")) == 0:
+            learned_main(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -227,8 +227,11 @@ int pgb_dminterp3d_ex(const double *u1, double *u2, int nx1, int ny1, int nz1, i
  * FP32 weights w[27][cin][cout] (tap = dz*9 + dy*3 + dx) into the kernel's
  * BF16 image (adjoint = 1: the image of the transposed convolution, with
  * cin and cout exchanged); pgb_conv3d_bf16 computes
- * out = [relu](conv(in) + bias) (bias may be NULL), writing zero on the
- * padding. Channel counts 16, 32 or 64; W >= 8. err (device int, may be
+ * out = [act](conv(in) + bias) (bias may be NULL; act, applied when
+ * relu = 1, is leaky ReLU with negative slope 1/8), writing zero on the
+ * padding. Channel counts 16, 32 or 64; any volume of at least one
+ * voxel (the margins absorb the over-reach of the last 128-voxel tile on
+ * small volumes). err (device int, may be
  * NULL) is set when a wait inside the kernel runs out. */
 int pgb_conv3d_geometry(int W, int H, int D, long *vtot, long *margin);
 int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int adjoint, void *stream);
@@ -238,7 +241,7 @@ int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bi
 /* The learned initial guess: a 6-level convolutional encoder-decoder
  * (16/32/64/64/64/64 channels, levels halving down to (n-1)/32 points a
  * side, two 3x3x3 convolutions per encoder level, one per decoder level,
- * additive skips, ReLU) from a source rho on an n^3 grid (points 0..n-2
+ * additive skips, leaky ReLU) from a source rho on an n^3 grid (points 0..n-2
  * seen by the net; n-1 a multiple of 32, n >= 65) to a guess of u, zero on
  * the grid boundary. Forward and backward-data convolutions of the inner
  * sixteen layers run on the tensor cores (BF16, FP32
@@ -251,10 +254,20 @@ int pgb_net_create(int n, unsigned long long seed, pgb_net **out);
 void pgb_net_destroy(pgb_net *net);
 int pgb_net_set_scales(pgb_net *net, double s_in, double s_out);
 long pgb_net_num_params(pgb_net *net);
+/* on = 1: all biases held at zero (cleared now, not trained), making the
+ * net positively homogeneous, net(c rho) = c net(rho) for c > 0 -- the
+ * right form for a guess of a linear equation's solution */
+int pgb_net_set_bias_free(pgb_net *net, int on);
 /* which = 0 parameters, 1 gradients (of the last pgb_net_loss_grad or
  * train step); to_device = 1 uploads (parameters only) */
 int pgb_net_params(pgb_net *net, int which, float *host, int to_device);
 int pgb_net_predict(pgb_net *net, const double *rho, double *u, void *stream);
+/* Scales a guess u of lap u = rho (u = 0 on the boundary, uniform spacing
+ * h, both device n^3 arrays) by alpha = <u, rho> / <u, lap u>, the factor
+ * that minimises the error of alpha u in the energy norm of -lap: a net
+ * whose shape is right but whose amplitude is off gets the amplitude from
+ * the equation. Runs on the device (no host synchronisation). */
+int pgb_net_rescale(pgb_net *net, const double *rho, double *u, double h, void *stream);
 int pgb_net_loss_grad(pgb_net *net, const double *rho, const float *u_target, double *loss, void *stream);
 int pgb_net_train_step(pgb_net *net, const double *rho, const float *u_target, float lr, double *loss,
                        void *stream);

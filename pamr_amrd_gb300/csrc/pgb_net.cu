@@ -15,7 +15,7 @@
  * 8 voxels (rows) x 8 channels (16 bytes); SBO = 128 bytes between
  * consecutive 8-voxel groups, LBO = the distance between the two channel
  * blocks of a 16-channel step. The epilogue reads the accumulator with
- * tcgen05.ld (one voxel per thread), adds the bias, applies ReLU, writes
+ * tcgen05.ld (one voxel per thread), adds the bias, applies the activation, writes
  * BF16 and re-zeroes the padding.
  */
 #include <cuda_runtime.h>
@@ -182,6 +182,12 @@ static pgb_lvgeom make_geom(int W, int H, int D)
    return g;
 }
 
+/* the activation after every convolution but the last: leaky ReLU with
+ * negative slope 1/8 (a power of two: scaling commutes with it and with
+ * every rounding, so a bias-free net stays exactly homogeneous) */
+#define LEAK 0.125f
+__device__ __forceinline__ float leaky(float a) { return a > 0.f ? a : LEAK * a; }
+
 /* ------------------------------------------------- tensor-core 3x3x3 conv -- */
 #define CONV_RUN 130   /* voxels of one y/z-tap run (x-taps -1, 0, +1 of 128 outputs) */
 
@@ -279,8 +285,8 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16 *in, __nv_b
                   a1 += bias[c16 * 16 + h * 8 + 2 * e + 1];
                }
                if (relu) {
-                  a0 = fmaxf(a0, 0.f);
-                  a1 = fmaxf(a1, 0.f);
+                  a0 = leaky(a0);
+                  a1 = leaky(a1);
                }
                if (pad) a0 = a1 = 0.f;
                __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
@@ -382,7 +388,7 @@ extern "C" int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int c
 extern "C" int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H,
                                int D, int cin, int cout, int relu, int *err, void *stream)
 {
-   if (W < 8 || H < 1 || D < 1) return arg_err("conv3d: volume too small");
+   if (W < 1 || H < 1 || D < 1) return arg_err("conv3d: empty volume");
    pgb_lvgeom g = make_geom(W, H, D);
    return conv_dispatch(cin, cout, in, out, wimg, bias, g, relu, err, (cudaStream_t)stream);
 }
@@ -418,7 +424,7 @@ __device__ __forceinline__ void store8(bf16 *a, long idx, const float *v)
    *reinterpret_cast<uint4 *>(a + idx * 8) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 }
 
-/* first layer, 1 -> 16 channels: a0 = relu(conv(s_in * rho) + b); rho is
+/* first layer, 1 -> 16 channels: a0 = leaky(conv(s_in * rho) + b); rho is
  * the n^3 FP64 grid, the net sees its points 0..n-2 in each dimension
  * (zero beyond) */
 __global__ void k_in_fwd(const double *rho, int n, float s_in, const float *w, const float *b, bf16 *out,
@@ -438,7 +444,7 @@ __global__ void k_in_fwd(const double *rho, int n, float s_in, const float *w, c
          for (int c = 0; c < 16; c++) acc[c] = fmaf(r, w[t * 16 + c], acc[c]);
       }
 #pragma unroll
-      for (int c = 0; c < 16; c++) acc[c] = fmaxf(acc[c], 0.f);
+      for (int c = 0; c < 16; c++) acc[c] = leaky(acc[c]);
       const long p = vox(g, x, y, z);
       store8(out, p, acc);
       store8(out, g.vtot + p, acc + 8);
@@ -480,6 +486,44 @@ __global__ void k_out_store(const float *up, double *u, int n, double s_out, pgb
          v = s_out * (double)up[x + (long)g.W * (y + (long)g.H * z)];
       u[q] = v;
    }
+}
+
+/* Energy-norm scaling of a guess of lap u = rho (u = 0 on the boundary,
+ * spacing h): with A = -lap (symmetric positive definite), the factor that
+ * minimises |alpha u - u*|_A is alpha = <u, rho> / <u, lap u>. This kernel
+ * accumulates the two sums over the interior points in FP64; k_scale_guess
+ * applies alpha (1 when the denominator is zero). */
+__global__ void k_energy_dots(const double *rho, const double *u, int n, double inv_h2, double *dots)
+{
+   __shared__ double sm[2][8];
+   const long nn = (long)n * n * n, s1 = n, s2 = (long)n * n;
+   double a = 0, b = 0;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(q % n), y = (int)((q / n) % n), z = (int)(q / s2);
+      if (x == 0 || y == 0 || z == 0 || x == n - 1 || y == n - 1 || z == n - 1) continue;
+      const double c = u[q];
+      const double lap = (u[q - 1] + u[q + 1] + u[q - s1] + u[q + s1] + u[q - s2] + u[q + s2] - 6.0 * c) * inv_h2;
+      a += c * rho[q];
+      b += c * lap;
+   }
+   for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+   }
+   if ((threadIdx.x & 31) == 0) sm[0][threadIdx.x >> 5] = a, sm[1][threadIdx.x >> 5] = b;
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      double ta = 0, tb = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) ta += sm[0][i], tb += sm[1][i];
+      atomicAdd(&dots[0], ta);
+      atomicAdd(&dots[1], tb);
+   }
+}
+
+__global__ void k_scale_guess(double *u, long nn, const double *dots)
+{
+   const double alpha = dots[1] != 0.0 ? dots[0] / dots[1] : 1.0;
+   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) u[q] *= alpha;
 }
 
 /* MSE over points 1..n-2: loss += sum (up - ut/s_out)^2 / N, gup = dloss/dup */
@@ -606,7 +650,8 @@ __global__ void k_in_bwd_w(const double *rho, int n, float s_in, const bf16 *gz,
    for (int c = 0; c < 16; c++) block_add(ab[c], red, t == 13 ? &db[c] : 0);
 }
 
-/* g = g * (y > 0) over the interior voxels of all channel blocks */
+/* g = g * leaky'(y) (1 where y > 0, else LEAK) over the interior voxels of
+ * all channel blocks */
 __global__ void k_relu_bwd(bf16 *gv, const bf16 *y, int nch, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D, n = nv * (nch / 8);
@@ -618,7 +663,7 @@ __global__ void k_relu_bwd(bf16 *gv, const bf16 *y, int nch, pgb_lvgeom g)
       load8(gv, idx, a);
       load8(y, idx, b);
 #pragma unroll
-      for (int e = 0; e < 8; e++) a[e] = b[e] > 0.f ? a[e] : 0.f;
+      for (int e = 0; e < 8; e++) a[e] = b[e] > 0.f ? a[e] : LEAK * a[e];
       store8(gv, idx, a);
    }
 }
@@ -781,7 +826,7 @@ __global__ void k_adam(float *w, const float *gw, float *m, float *v, long n, fl
  * on level v; two 3x3x3 convolutions per encoder level (one after the
  * input convolution on level 0), 2x2x2 average pooling down, nearest
  * upsampling plus the encoder's activation (additive skip) up, one
- * convolution per decoder level, ReLU after every convolution but the
+ * convolution per decoder level, leaky ReLU after every convolution but the
  * last. The first (1 -> 16) and last (16 -> 1) convolutions run on CUDA
  * cores, the others on the tensor cores (forward, and backward-data
  * through the adjoint image).
@@ -840,8 +885,10 @@ struct pgb_net {
    bf16 *act[NACT], *grad[NACT];
    float *up, *gup;
    double *d_loss;
+   double *d_dots;                /* energy-norm scaling sums */
    int *d_err;
    long step;
+   int bias_free;
 };
 
 static size_t act_bytes(const pgb_lvgeom &g, int ch) { return (size_t)(ch / 8) * g.vtot * 16; }
@@ -890,6 +937,7 @@ extern "C" void pgb_net_destroy(pgb_net *net)
    cudaFree(net->up);
    cudaFree(net->gup);
    cudaFree(net->d_loss);
+   cudaFree(net->d_dots);
    cudaFree(net->d_err);
    free(net);
 }
@@ -922,7 +970,8 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
    bool ok = cudaMalloc((void **)&net->p, o * 4) == cudaSuccess && cudaMalloc((void **)&net->gp, o * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->m, o * 4) == cudaSuccess && cudaMalloc((void **)&net->v, o * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->up, nv * 4) == cudaSuccess && cudaMalloc((void **)&net->gup, nv * 4) == cudaSuccess &&
-             cudaMalloc((void **)&net->d_loss, 8) == cudaSuccess && cudaMalloc((void **)&net->d_err, 4) == cudaSuccess;
+             cudaMalloc((void **)&net->d_loss, 8) == cudaSuccess && cudaMalloc((void **)&net->d_err, 4) == cudaSuccess &&
+             cudaMalloc((void **)&net->d_dots, 16) == cudaSuccess;
    for (int l = 0; l < NTC && ok; l++)
       ok = cudaMalloc((void **)&net->img[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess &&
            cudaMalloc((void **)&net->img_adj[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess;
@@ -964,6 +1013,34 @@ extern "C" int pgb_net_set_scales(pgb_net *net, double s_in, double s_out)
 {
    net->s_in = s_in;
    net->s_out = s_out;
+   return 0;
+}
+
+/* the bias entries of the parameter vector: (offset, count) pairs */
+static int bias_ranges(const pgb_net *net, long *off, long *cnt)
+{
+   int k = 0;
+   off[k] = net->off_in_b, cnt[k++] = LCH[0];
+   for (int l = 0; l < NTC; l++) off[k] = net->off_tc_b[l], cnt[k++] = TC_COUT[l];
+   off[k] = net->off_out_b, cnt[k++] = 1;
+   return k;
+}
+
+/* on = 1 holds every bias at zero (set now, gradients dropped before each
+ * Adam step): the net is then positively homogeneous, net(c rho) = c
+ * net(rho) for c > 0, which is what a guess of a linear equation's
+ * solution should be */
+extern "C" int pgb_net_set_bias_free(pgb_net *net, int on)
+{
+   net->bias_free = on;
+   if (!on) return 0;
+   long off[NTC + 2], cnt[NTC + 2];
+   const int k = bias_ranges(net, off, cnt);
+   for (int i = 0; i < k; i++)
+      if (cudaMemset(net->p + off[i], 0, cnt[i] * 4) != cudaSuccess ||
+          cudaMemset(net->m + off[i], 0, cnt[i] * 4) != cudaSuccess ||
+          cudaMemset(net->v + off[i], 0, cnt[i] * 4) != cudaSuccess)
+         return arg_err("pgb_net_set_bias_free: clearing the biases failed");
    return 0;
 }
 
@@ -1032,6 +1109,17 @@ extern "C" int pgb_net_predict(pgb_net *net, const double *rho, double *u, void 
    return 0;
 }
 
+extern "C" int pgb_net_rescale(pgb_net *net, const double *rho, double *u, double h, void *stream)
+{
+   cudaStream_t st = (cudaStream_t)stream;
+   if (!(h > 0)) return arg_err("pgb_net_rescale: spacing must be positive");
+   if (cudaMemsetAsync(net->d_dots, 0, 16, st) != cudaSuccess) return check_net("net memset");
+   const long nn = (long)net->n * net->n * net->n;
+   NETK((k_energy_dots<<<GRID_1D, 256, 0, st>>>(rho, u, net->n, 1.0 / (h * h), net->d_dots)), "net energy dots");
+   NETK((k_scale_guess<<<GRID_1D, 256, 0, st>>>(u, nn, net->d_dots)), "net scale guess");
+   return 0;
+}
+
 static int wgrad(pgb_net *net, int l, const bf16 *x, const bf16 *gz, cudaStream_t st)
 {
    const pgb_lvgeom &g = net->g[TC_LEV[l]];
@@ -1044,8 +1132,9 @@ static int wgrad(pgb_net *net, int l, const bf16 *x, const bf16 *gz, cudaStream_
    return 0;
 }
 
-/* backward of one ReLU convolution x -> y: the gradient of y (taken through
- * the ReLU in place) gives the weight gradient and the gradient of x */
+/* backward of one activated convolution x -> y: the gradient of y (taken
+ * through the activation in place) gives the weight gradient and the
+ * gradient of x */
 static int conv_bwd(pgb_net *net, int l, int x, int y, cudaStream_t st)
 {
    bf16 **a = net->act, **G = net->grad;
@@ -1121,6 +1210,12 @@ extern "C" int pgb_net_train_step(pgb_net *net, const double *rho, const float *
 {
    cudaStream_t st = (cudaStream_t)stream;
    if (loss_grad(net, rho, ut, st)) return 11;
+   if (net->bias_free) {
+      long off[NTC + 2], cnt[NTC + 2];
+      const int k = bias_ranges(net, off, cnt);
+      for (int i = 0; i < k; i++)
+         if (cudaMemsetAsync(net->gp + off[i], 0, cnt[i] * 4, st) != cudaSuccess) return check_net("net memset");
+   }
    net->step++;
    const float b1 = 0.9f, b2 = 0.999f;
    const float c1 = (float)(1.0 / (1.0 - pow(b1, (double)net->step)));

@@ -24,10 +24,12 @@ def _bind():
     L.pgb_net_destroy.argtypes = [_vp]
     L.pgb_net_destroy.restype = None
     L.pgb_net_set_scales.argtypes = [_vp, C.c_double, C.c_double]
+    L.pgb_net_set_bias_free.argtypes = [_vp, C.c_int]
     L.pgb_net_num_params.argtypes = [_vp]
     L.pgb_net_num_params.restype = C.c_long
     L.pgb_net_params.argtypes = [_vp, C.c_int, C.POINTER(C.c_float), C.c_int]
     L.pgb_net_predict.argtypes = [_vp, _vp, _vp, _vp]
+    L.pgb_net_rescale.argtypes = [_vp, _vp, _vp, C.c_double, _vp]
     L.pgb_net_loss_grad.argtypes = [_vp, _vp, _vp, _dp, _vp]
     L.pgb_net_train_step.argtypes = [_vp, _vp, _vp, C.c_float, _dp, _vp]
     L.pgb_conv3d_geometry.argtypes = [C.c_int] * 3 + [_vp, _vp]
@@ -88,6 +90,9 @@ class Net:
         self.s_in, self.s_out = s_in, s_out
         _check(lib().pgb_net_set_scales(self.h, s_in, s_out))
 
+    def set_bias_free(self, on: bool = True):
+        _check(lib().pgb_net_set_bias_free(self.h, 1 if on else 0))
+
     def num_params(self) -> int:
         return int(lib().pgb_net_num_params(self.h))
 
@@ -112,6 +117,10 @@ class Net:
 
     def predict(self, rho_ptr: int, u_ptr: int, stream=None):
         _check(lib().pgb_net_predict(self.h, rho_ptr, u_ptr, stream))
+
+    def rescale(self, rho_ptr: int, u_ptr: int, h: float, stream=None):
+        """energy-norm optimal amplitude of the guess (pgb_net_rescale)"""
+        _check(lib().pgb_net_rescale(self.h, rho_ptr, u_ptr, h, stream))
 
     def loss_grad(self, rho_ptr: int, ut_ptr: int, stream=None) -> float:
         loss = C.c_double()
@@ -145,13 +154,16 @@ def source_charge(rho, h: float) -> float:
 
 
 class Scaled:
-    """The equation is linear in rho, so every sample is scaled by its own
-    source charge Q: the net reads rho / Q and predicts u / (gain * Q),
-    `gain` (max |u| / Q over the training pairs) fixed at training, so that
-    inputs and targets are of order one whatever the source's size."""
+    """The equation is linear in rho: the net is made bias-free (positively
+    homogeneous, so scaling rho scales its guess exactly) and every sample
+    is scaled by its own source charge Q: the net reads rho / Q and
+    predicts u / (gain * Q), `gain` (max |u| / Q over the training pairs)
+    fixed at training, so that inputs and targets are of order one
+    whatever the source's size."""
 
     def __init__(self, net: Net, gain: float, h: float):
         self.net, self.gain, self.h = net, gain, h
+        net.set_bias_free(True)
 
     def _scale(self, rho) -> None:
         q = source_charge(rho, self.h)
@@ -161,9 +173,13 @@ class Scaled:
         self._scale(rho)
         return self.net.train_step(rho.data_ptr(), ut.data_ptr(), lr, want_loss=want_loss)
 
-    def predict(self, rho, u, stream=None):
+    def predict(self, rho, u, stream=None, rescale: bool = True):
+        """the guess of u for source rho (device tensors), its amplitude set
+        by the energy norm unless rescale is False"""
         self._scale(rho)
         self.net.predict(rho.data_ptr(), u.data_ptr(), stream)
+        if rescale:
+            self.net.rescale(rho.data_ptr(), u.data_ptr(), self.h, stream)
 
 
 def make_dataset(n: int, seeds, torch, cycles: int = 12, precision: int = 1):
@@ -220,23 +236,26 @@ def train(model: Scaled, blobs, U, torch, epochs: int = 2, lr: float = 1e-3, lr_
 
 
 class GuessPolicy:
-    """Uses the net's guess as the initial u of a solve while it cuts
-    V-cycles. The plain solve always runs to tolerance after the guess, so
-    a bad guess costs cycles, never accuracy; when guessed solves stop
-    needing fewer cycles than the last unguessed one (`patience` times in a
-    row) the policy goes back to the plain initial guess (u = 0)."""
+    """Uses the net's guess as the initial u of a solve while it pays. The
+    plain solve always runs to tolerance after the guess, so a bad guess
+    costs time, never accuracy. A guessed solve that needs no fewer
+    V-cycles than the last unguessed one, or takes no less time (the
+    prediction included), is a strike; `patience` strikes in a row send
+    the policy back to the plain initial guess (u = 0) for good."""
 
     def __init__(self, patience: int = 2):
-        self.patience, self.strikes, self.plain_cycles, self.enabled = patience, 0, None, True
+        self.patience, self.strikes, self.enabled = patience, 0, True
+        self.plain_cycles = self.plain_ms = None
 
     def use_guess(self) -> bool:
         return self.enabled and self.plain_cycles is not None
 
-    def record(self, cycles: int, guessed: bool):
+    def record(self, cycles: int, guessed: bool, ms: float | None = None):
         if not guessed:
-            self.plain_cycles = cycles
+            self.plain_cycles, self.plain_ms = cycles, ms
             return
-        if self.plain_cycles is not None and cycles >= self.plain_cycles:
+        slower = ms is not None and self.plain_ms is not None and ms >= self.plain_ms
+        if self.plain_cycles is not None and (cycles >= self.plain_cycles or slower):
             self.strikes += 1
             if self.strikes >= self.patience:
                 self.enabled = False

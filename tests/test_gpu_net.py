@@ -48,7 +48,7 @@ def from_layout(act, P, shape):
 
 
 @pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 64), (64, 64), (64, 16)])
-@pytest.mark.parametrize("vol", [(16, 12, 10), (128, 6, 5)])
+@pytest.mark.parametrize("vol", [(16, 12, 10), (128, 6, 5), (4, 4, 4), (2, 2, 2)])
 @pytest.mark.parametrize("adjoint", [0, 1])
 def test_conv3d_matches_torch(cin, cout, vol, adjoint):
     L = _lib()
@@ -81,7 +81,7 @@ def test_conv3d_matches_torch(cin, cout, vol, adjoint):
         ref = torch.nn.functional.conv_transpose3d(xin, wt, padding=1)
     else:
         ref = torch.nn.functional.conv3d(xin, wt, padding=1)
-    ref = torch.relu(ref[0] + bias.view(-1, 1, 1, 1)).permute(1, 2, 3, 0)
+    ref = torch.nn.functional.leaky_relu(ref[0] + bias.view(-1, 1, 1, 1), 0.125).permute(1, 2, 3, 0)
     got = from_layout(out, P, (D, H, W, co_))
     tol = 1e-2 * ref.abs() + 2e-3 * ref.abs().max()
     assert torch.all((got - ref).abs() <= tol), float((got - ref).abs().max())
@@ -102,7 +102,7 @@ def _torch_net(net, flat, x):
         w, b = P[name]
         wt = w.reshape(3, 3, 3, w.shape[1], w.shape[2]).permute(4, 3, 0, 1, 2)
         y = F.conv3d(a, wt, b, padding=1)
-        return torch.relu(y) if relu else y
+        return F.leaky_relu(y, 0.125) if relu else y
 
     up = lambda a: F.interpolate(a, scale_factor=2, mode="nearest")  # noqa: E731
     e1 = [conv("tc0", conv("in", x))]
@@ -177,4 +177,55 @@ def test_net_training_reduces_the_loss():
     torch.cuda.synchronize()
     uu = u.cpu().numpy().reshape(n, n, n)
     assert np.all(uu[0] == 0) and np.all(uu[:, :, -1] == 0) and np.isfinite(uu).all()
+    net.close()
+
+
+def test_bias_free_net_is_homogeneous():
+    """with the biases held at zero the guess scales with the source: a
+    power-of-two factor commutes with every rounding, so exactly"""
+    from pamr_amrd_gb300.learned import Net
+    n = 65
+    rng = np.random.default_rng(9)
+    net = Net(n, seed=6)
+    net.set_bias_free(True)
+    rho = _smooth_field(n, rng)
+    ut = (0.5 * _smooth_field(n, rng)).astype(np.float32)
+    d_rho = torch.from_numpy(rho.reshape(-1)).cuda()
+    d_ut = torch.from_numpy(ut.reshape(-1)).cuda()
+    for _ in range(5):
+        net.train_step(d_rho.data_ptr(), d_ut.data_ptr(), 1e-3)
+    p = net.split(net.params(0))
+    assert all(not np.any(b) for _, b in p.values())
+    u1 = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    u4 = torch.zeros_like(u1)
+    d_rho4 = 4.0 * d_rho
+    net.predict(d_rho.data_ptr(), u1.data_ptr())
+    net.predict(d_rho4.data_ptr(), u4.data_ptr())
+    torch.cuda.synchronize()
+    assert float(u1.abs().max()) > 0
+    assert torch.equal(u4, 4.0 * u1)
+    net.close()
+
+
+def test_rescale_restores_the_amplitude():
+    """a guess that is the solution times 0.6 comes back as the solution: the
+    energy-norm factor <u, rho> / <u, lap u> is exactly 1/0.6 there"""
+    from pamr_amrd_gb300.learned import Net
+    n, h = 65, 0.25
+    x = np.arange(n) * h
+    L = (n - 1) * h
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    u = np.sin(np.pi * X / L) * np.sin(2 * np.pi * Y / L) * np.sin(np.pi * Z / L) * (1 + 0.3 * X / L)
+    u[0], u[-1], u[:, 0], u[:, -1], u[:, :, 0], u[:, :, -1] = 0, 0, 0, 0, 0, 0
+    rho = np.zeros_like(u)
+    c = u[1:-1, 1:-1, 1:-1]
+    rho[1:-1, 1:-1, 1:-1] = (u[2:, 1:-1, 1:-1] + u[:-2, 1:-1, 1:-1] + u[1:-1, 2:, 1:-1] + u[1:-1, :-2, 1:-1]
+                             + u[1:-1, 1:-1, 2:] + u[1:-1, 1:-1, :-2] - 6 * c) / h ** 2
+    net = Net(n, seed=2)
+    d_rho = torch.from_numpy(rho.reshape(-1).copy()).cuda()
+    d_u = torch.from_numpy(0.6 * u.reshape(-1)).cuda()
+    net.rescale(d_rho.data_ptr(), d_u.data_ptr(), h)
+    torch.cuda.synchronize()
+    got = d_u.cpu().numpy()
+    assert np.abs(got - u.reshape(-1)).max() <= 1e-12 * np.abs(u).max()
     net.close()
