@@ -21,6 +21,8 @@ N>1 runs N independent replicas (one per GPU, launched by torch.distributed.run)
 python bench.py --workload poisson3d_learned [--pairs P --epochs E] trains the
 learned initial guess on P multigrid-generated pairs and prints one line
 comparing plain solves with guessed ones (V-cycles and solves/s).
+python bench.py --workload lapse_bo [--bo-steps S] times the lapse solves of
+an S-step Berger-Oliger sequence (default 400) in both forms.
 """
 from __future__ import annotations
 
@@ -143,6 +145,139 @@ def ncu_traffic():
     return None
 
 
+def sweep_beyond_l2(S, torch, np, peak, n: int = 385):
+    """the same FP32 sweep on one n^3 grid whose three FP32 arrays (3 x 228
+    MB at n = 385) exceed the 129 MB L2, so that each sweep streams them
+    from HBM: the HBM efficiency of the smoother itself, apart from the
+    launch and L2 latency that bound it on the workload's 129^3 level"""
+    from pamr_amrd_gb300 import workloads as W
+    bbox = (-10.0, 10.0, -10.0, 10.0, -10.0, 10.0)
+    g = W.Grid(1, bbox, (n, n, n))
+    prm = W.MGParams()
+    prm.precision = 1
+    case = W.Case(f"poisson3d_{n}", W.POISSON, 3, (n, n, n), bbox, [g], [], [], prm)
+    sv = S.Solver(case)
+    z = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()   # the solver copies on its own stream
+    sv.set_inputs_device([z.data_ptr()], [z.data_ptr()])
+    sv.prepare()
+    L = sv.num_levels()
+    ms, by = sv.time_relax(L, reps=10)
+    tz, fuse = sv.level_tuning(L)
+    sv.close()
+    gbs = by / (ms / 1e3) / 1e9
+    return {"grid": f"{n}^3", "ms_per_sweep": ms, "bytes_per_sweep": by, "achieved": gbs,
+            "frac": gbs / peak, "tuned": {"tile_planes": tz, "sweeps_per_launch": fuse}}
+
+
+# --------------------------------------------- Berger-Oliger lapse run --
+LAPSE_WORKLOAD = ("lapse2d_bo_257_L4: maximal-slicing lapse lap(alpha) = alpha*S at every coarse step of a "
+                  "400-step Berger-Oliger sequence (Courant 0.5), 257^2 base on [-10,10]^2 + 3 nested 2:1 "
+                  "levels (3.7 M points), S = breathing Gaussian shell, each solve warm-started from the "
+                  "previous lapse, V(2,2) to 1e-10 of the step-0 residual")
+
+
+def _lapse_port_solve(seed: int) -> float:
+    from oracle import portrun
+    from pamr_amrd_gb300 import workloads as W
+    t = time.perf_counter()
+    portrun.solve(W.lapse2d_bo(257, seed=seed, levels=4))
+    return time.perf_counter() - t
+
+
+def lapse_main(args):
+    """the whole lapse sequence in both forms: per coarse step the shell's
+    source is evaluated on the device, the solve starts from the previous
+    step's lapse and runs to the fixed tolerance"""
+    import numpy as np
+    import torch
+    from pamr_amrd_gb300 import solver as S
+    from pamr_amrd_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    steps = args.bo_steps
+    case = W.lapse2d_bo(257, seed=0, levels=4, steps=steps)
+    r0, amp, w = W.lapse_shell(0)
+    radius = []
+    for g in case.grids:
+        x = torch.tensor(g.coords(0), device="cuda").view(1, -1)
+        y = torch.tensor(g.coords(1), device="cuda").view(-1, 1)
+        radius.append(torch.sqrt(x * x + y * y).reshape(-1).contiguous())
+    src = [torch.empty_like(r) for r in radius]
+    ones = [torch.ones_like(r) for r in radius]
+    u = [torch.empty_like(r) for r in radius]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()   # the solver copies on its own stream
+    out, finals = {}, {}
+    for prec, form in ((0, "fp64"), (1, "mixed")):
+        c = copy.deepcopy(case)
+        c.params.precision = prec
+        sv = S.Solver(c)
+        st = torch.cuda.ExternalStream(sv.stream())
+
+        def run(k, start):
+            R = W.shell_radius(r0, k, steps)
+            with torch.cuda.stream(st):
+                for s_, r_ in zip(src, radius):
+                    torch.mul(torch.exp(-((r_ - R) / w) ** 2), amp, out=s_)
+            sv.set_inputs_device([a.data_ptr() for a in start], [a.data_ptr() for a in src])
+            res = sv.solve()
+            for i, a in enumerate(u):
+                S._check(S.lib().pgb_get_grid_device(sv.h, i, a.data_ptr()))
+            return res
+
+        for _ in range(args.warmup):   # cold solves of step 0, untimed
+            run(0, ones)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        clk = Clocks(torch.cuda.current_device()) if prec == 1 else None
+        l0 = S.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        iters, ok = [], True
+        for k in range(steps):
+            r = run(k, ones if k == 0 else u)
+            iters.append(r["iters"])
+            ok = ok and r["res_final"] <= c.params.tol
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[form] = {"solves_per_s": 1e3 * steps / ms, "ms_per_solve": ms / steps,
+                     "vcycles_per_solve": statistics.mean(iters), "vcycles_step0": iters[0],
+                     "all_converged": ok, "gpu_launches": S.launch_count() - l0,
+                     "clocks": clk.stop() if clk else None}
+        finals[form] = [a.cpu().numpy() for a in u]
+        sv.close()
+    umax = max(float(np.abs(a).max()) for a in finals["fp64"])
+    emax = max(float(np.abs(a - b).max()) for a, b in zip(finals["mixed"], finals["fp64"]))
+    cpu = None
+    if not args.no_cpu_baseline:
+        nproc = min(host_cores(), 16)
+        from oracle import portrun
+        portrun.build()
+        ctx = mp.get_context("spawn")
+        t = time.perf_counter()
+        with ctx.Pool(nproc) as pool:
+            per = pool.map(_lapse_port_solve, list(range(nproc)))
+        wall = time.perf_counter() - t
+        cpu = {"value": nproc / wall, "unit": "solves/s", "cores": nproc, "kind": "port",
+               "sample": f"{nproc} concurrent oracle-port cold solves of step 0 (seeds 0..{nproc - 1}; "
+                         f"median {statistics.median(per):.1f} s per solve)"}
+    mx = out["mixed"]
+    line = {"metric": "lapse solves/s over a Berger-Oliger sequence, mixed form (FP64 form beside it)",
+            "value": mx["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": mx["ms_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded shell: radius, amplitude, width from seed 0)",
+            "config": {"workload": LAPSE_WORKLOAD, "points": case.total_points(),
+                       "l2": "not flushed between steps: the sequence runs back to back (3.7 M points, "
+                             "arrays larger than L2)"},
+            "forms": out, "fp64_solves_per_s": out["fp64"]["solves_per_s"],
+            "speedup_vs_fp64": mx["solves_per_s"] / out["fp64"]["solves_per_s"],
+            "error_vs_fp64_final_step": {"max_abs": emax, "max_rel": emax / umax},
+            "gpu_launches": mx["gpu_launches"], "cpu_baseline": cpu, "clocks": mx["clocks"]}
+    print(json.dumps(line))
+
+
 # ------------------------------------------------ learned initial guess --
 LEARNED_WORKLOAD = ("poisson3d_129: lap u = rho on [-10,10]^3, one 129^3 grid (6 MG levels), "
                     "rho = 4 seeded Gaussians, V(2,2) to 1e-10 relative residual; guess = 6-level "
@@ -235,11 +370,14 @@ def learned_main(args):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     for _ in range(3):
         model.predict(rhos[0], guess)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("predict_only")   # lets a profiler select these launches
     ev[0].record()
     for _ in range(10):
         model.predict(rhos[0], guess)
     ev[1].record()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     mx = out["mixed"]
     line = {"metric": "poisson3d_129 solves/s with the learned initial guess (guess policy), mixed form",
             "value": mx["policy_solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
@@ -264,12 +402,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="conformal3d", choices=["conformal3d", "poisson3d_learned"],
-                    help="poisson3d_learned: solves with and without the learned initial guess")
+    ap.add_argument("--workload", default="conformal3d", choices=["conformal3d", "poisson3d_learned", "lapse_bo"],
+                    help="poisson3d_learned: solves with and without the learned initial guess; "
+                         "lapse_bo: the lapse solves of a Berger-Oliger sequence")
+    ap.add_argument("--bo-steps", type=int, default=400, help="coarse steps of the sequence (lapse_bo)")
     ap.add_argument("--pairs", type=int, default=2000, help="training pairs (poisson3d_learned)")
     ap.add_argument("--epochs", type=int, default=4, help="training epochs (poisson3d_learned)")
     ap.add_argument("--lr", type=float, default=1e-3, help="peak learning rate (poisson3d_learned)")
     args = ap.parse_args()
+    if args.workload == "lapse_bo":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "timed by this line's cpu_baseline "
+                                                                   "(the oracle port of the reference's path)"}))
+        elif int(os.environ.get("RANK", "0")) == 0:
+            lapse_main(args)
+        return
     if args.workload == "poisson3d_learned":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned initial guess"}))
@@ -422,11 +569,14 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": ncu_traffic(), "peak_source": peak_kind,
-            "kernel": "k_relax32 (FP32 red+black sweep on the correction, 129^3 level)",
+            "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level)",
+            "tuned": dict(zip(("tile_planes", "sweeps_per_launch"), smx.level_tuning(big))),
             "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep,
             "fp64_sweep": {"kernel": "k_relax (FP64 Newton-GS sweep, 129^3 level)",
                            "ms_per_sweep": ms64_sweep,
                            "achieved_gbs": bytes64_sweep / (ms64_sweep / 1e3) / 1e9}}
+
+    roof["beyond_l2"] = sweep_beyond_l2(S, torch, np, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -125,7 +125,10 @@ long long pgb_launch_count(void);
  * sweep and the algorithmic bytes of one sweep: FP64 path 32 bytes per
  * interior point (u read and written, rhs and source read), mixed form 16
  * (FP32 correction read and written, defect and Jacobian term read).
- * Modifies u (FP64) or the correction (mixed) on that level. */
+ * The mixed form times its sweeps as a smoothing block of the V-cycle runs
+ * them (blocks of MG_pre_swp sweeps with the level's tuned tile depth and
+ * sweeps per launch; the autotuner runs first if it has not). Modifies u
+ * (FP64) or the correction (mixed) on that level. */
 int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
                    double *bytes_per_sweep);
 

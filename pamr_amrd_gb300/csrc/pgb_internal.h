@@ -31,11 +31,14 @@ enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, 
 #define PGB_BOX_ISO 8         /* dx^2 is the same in every dimension */
 
 /* device view of one MG box (all pointers are device pointers) */
+#define PGB_NW32 5   /* FP32 work arrays per box (mixed form) */
+
 typedef struct {
    double *f[PGB_NF];
    const uint8_t *cmask_child;   /* set_cmask_child, amrd/mg.c:362-426 */
    const uint8_t *cmask_bdy;     /* set_cmask_bdy, amrd/mg.c:432-488 */
-   float *w32[4];                /* mixed form: correction, defect, Jacobian term, coarse correction */
+   float *w32[PGB_NW32];         /* mixed form: correction, defect, Jacobian term, coarse correction,
+                                  * second correction buffer (fused sweeps write it) */
    int n[3];                     /* Nx, Ny, Nz (Nz = 1 in 2-D) */
    int flags;
    int level;

@@ -58,7 +58,7 @@ extern "C" const char *pgb_dev_error32(void) { return g_err32; }
 #define TWO_PI 6.283185307179586
 
 /* the FP32 arrays of a box: correction, defect, Jacobian term, coarse correction */
-enum { W_E = 0, W_D = 1, W_C = 2, W_X = 3 };
+enum { W_E = 0, W_D = 1, W_C = 2, W_X = 3, W_E2 = 4 };
 
 __device__ __forceinline__ bool interior32(const pgb_dbox &b, int i, int j, int k, int dim)
 {
@@ -207,6 +207,22 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
    }
 }
 
+/* The Gauss-Seidel update of one point of lap E + C E = D, FP32, written
+ * with explicit roundings so that every kernel that relaxes (colour passes
+ * from global memory, fused sweeps in shared memory) computes the same
+ * bits: t = sum over dimensions of (e+ - 2 e + e-) * idx2 (the first a
+ * product, the others fused), r = (c e + t) - d, e - r / (j0 + c). */
+__device__ __forceinline__ float gs32(float ec, float xm, float xp, float ym, float yp, float zm, float zp,
+                                      float c, float d, float ix, float iy, float iz, float j0, bool d3)
+{
+   const float m2 = -2.f * ec;   /* exact */
+   float t = __fmul_rn(__fadd_rn(__fadd_rn(xp, m2), xm), ix);
+   t = __fmaf_rn(__fadd_rn(__fadd_rn(yp, m2), ym), iy, t);
+   if (d3) t = __fmaf_rn(__fadd_rn(__fadd_rn(zp, m2), zm), iz, t);
+   const float r = __fsub_rn(__fmaf_rn(c, ec, t), d);
+   return __fsub_rn(ec, __fdividef(r, __fadd_rn(j0, c)));
+}
+
 /* one colour pass of Gauss-Seidel on lap E + C E = D, FP32, straight from
  * global memory (the level's E, D, C stay in L2 between passes); relax
  * tiles are 64 points wide, a thread updates one point of the active colour
@@ -233,25 +249,27 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
       if (!interior32(b, i, j, k, dim)) continue;
       const long p = i + sy * j + sz * k;
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
-      const float ec = e[p], c = cc[p];
-      float t = (e[p + 1] - 2.f * ec + e[p - 1]) * ix + (e[p + sy] - 2.f * ec + e[p - sy]) * iy;
-      if (dim == 3) t += (e[p + sz] - 2.f * ec + e[p - sz]) * iz;
-      const float r = t + c * ec - dd[p];
-      e[p] = ec - __fdividef(r, j0 + c);
+      const bool d3 = dim == 3;
+      e[p] = gs32(e[p], e[p - 1], e[p + 1], e[p - sy], e[p + sy], d3 ? e[p - sz] : 0.f, d3 ? e[p + sz] : 0.f,
+                  cc[p], dd[p], ix, iy, iz, j0, d3);
    }
 }
 
 /* The same sweeps staged in shared memory: NS red-black sweeps in one launch.
- * The CTA stages E of its 32 x 8 x tz tile plus a halo of 2*NS points in
- * shared memory; colour pass q (0 .. 2*NS-1) updates the active colour on
- * the tile grown by 2*NS-1-q points, so that every value the next pass reads
- * is already final, and only the tile is written back. A point's new value
- * depends only on old values of the other colour and D, C, so neighbouring
- * CTAs compute identical values on their overlaps. Colour of pass q: the
- * points with i+j(+k+1)+q even (num.f:220 parity, 0-based indices). NS > 1
- * is only used on levels with no sync between sweeps. */
+ * The CTA stages the correction of its 32 x 8 x tz tile plus a halo of
+ * 2*NS points from slot `src` in shared memory; colour pass q (0 ..
+ * 2*NS-1) updates the active colour on the tile grown by 2*NS-1-q points,
+ * so that every value the next pass reads is already final, and only the
+ * tile is written, to slot `dst`. A point's new value depends only on old
+ * values of the other colour and D, C, so neighbouring CTAs compute
+ * identical values on their overlaps; since no CTA writes the slot the
+ * others stage from, the halo is the old correction whatever the CTAs'
+ * order, and the result is that of the in-place colour passes bit for bit.
+ * Colour of pass q: the points with i+j(+k+1)+q even (num.f:220 parity,
+ * 0-based indices). NS > 1 is only used on levels with no sync between
+ * sweeps. */
 template <int NS>
-__global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv)
+__global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int src, int dst)
 {
    constexpr int H = 2 * NS;
    constexpr int SX = PGB_TX + 2 * H, SY = PGB_TY + 2 * H, SZ = PGB_TZ + 2 * H;
@@ -261,7 +279,8 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
    const int dim = lv.dim;
    const int tz = dim == 3 ? lv.tz : 1, hz = dim == 3 ? H : 0, nzl = tz + 2 * hz;
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   float *e = b.w32[W_E];
+   const float *e = b.w32[src];
+   float *eo = b.w32[dst];
    const float *dd = b.w32[W_D], *cc = b.w32[W_C];
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
    const float j0 = b.fj0;
@@ -297,11 +316,9 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
          const long p = gi + sy * gj + sz * gk;
          if (!allbdy && !b.cmask_bdy[p]) continue;
          const int sp = x + SX * (y + SY * z);
-         const float ec = se[sp], c = cc[p];
-         float tt = (se[sp + 1] - 2.f * ec + se[sp - 1]) * ix + (se[sp + SX] - 2.f * ec + se[sp - SX]) * iy;
-         if (dim == 3) tt += (se[sp + SX * SY] - 2.f * ec + se[sp - SX * SY]) * iz;
-         const float r = tt + c * ec - dd[p];
-         se[sp] = ec - __fdividef(r, j0 + c);
+         const bool d3 = dim == 3;
+         se[sp] = gs32(se[sp], se[sp - 1], se[sp + 1], se[sp - SX], se[sp + SX], d3 ? se[sp - SX * SY] : 0.f,
+                       d3 ? se[sp + SX * SY] : 0.f, cc[p], dd[p], ix, iy, iz, j0, d3);
       }
       __syncthreads();
    }
@@ -309,7 +326,27 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
       const int x = q % PGB_TX, y = (q / PGB_TX) % PGB_TY, z = q / (PGB_TX * PGB_TY);
       const int gi = tl.i0 + x, gj = tl.j0 + y, gk = tl.k0 + z;
       if (gi < b.n[0] && gj < b.n[1] && gk < b.n[2])
-         e[gi + sy * gj + sz * gk] = se[(x + H) + SX * ((y + H) + SY * (z + hz))];
+         eo[gi + sy * gj + sz * gk] = se[(x + H) + SX * ((y + H) + SY * (z + hz))];
+   }
+}
+
+/* E = the correction in slot src, over the level's tiles (the end of an
+ * odd number of fused sweep launches) */
+__global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel lv, int src)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+   const float *__restrict__ a = b.w32[src];
+   float *__restrict__ e = b.w32[W_E];
+   for (int kk = 0; kk < kz; kk++) {
+      const int k = tl.k0 + kk;
+      if (k >= b.n[2]) break;
+      const long p = i + sy * j + sz * k;
+      e[p] = a[p];
    }
 }
 
@@ -976,22 +1013,34 @@ extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream
  * per sweep; 1 or 2 = sweeps per launch of the shared-memory kernel */
 extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream)
 {
-   int done = 0;
+   int done = 0, src = W_E, dst = W_E2;
    if (!lv.ntiles) return 0;
-   while (done < nsweep) {
-      if (fuse <= 0) {
+   if (fuse <= 0) {   /* in place, one launch per colour pass */
+      for (; done < nsweep; done++) {
          k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 0);
          if (check32("relax32")) return 1;
          k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 1);
-         done += 1;
-      } else if (fuse >= 2 && nsweep - done >= 2) {
-         k_sweep32<2><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+         if (check32("relax32")) return 1;
+      }
+      return 0;
+   }
+   /* fused launches alternate between the two correction slots */
+   while (done < nsweep) {
+      if (fuse >= 2 && nsweep - done >= 2) {
+         k_sweep32<2><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src, dst);
          done += 2;
       } else {
-         k_sweep32<1><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+         k_sweep32<1><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src, dst);
          done += 1;
       }
       if (check32("sweep32")) return 1;
+      const int t = src;
+      src = dst;
+      dst = t;
+   }
+   if (src != W_E) {
+      k_copy_e<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src);
+      if (check32("copy_e")) return 1;
    }
    return 0;
 }

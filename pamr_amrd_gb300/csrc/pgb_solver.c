@@ -296,12 +296,12 @@ static int setup_device(pgb_solver *s)
       off = align256(off + n);
    }
    if (h->prm.precision == PGB_MIXED) {
-      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * 4);
+      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * PGB_NW32);
       for (i = 0; i < h->nbox; i++) {
          const pgb_hbox *b = &h->boxes[i];
          size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
-         for (f = 0; f < 4; f++) {
-            w32o[i * 4 + f] = off;
+         for (f = 0; f < PGB_NW32; f++) {
+            w32o[i * PGB_NW32 + f] = off;
             off = align256(off + 4 * n);
          }
       }
@@ -317,7 +317,7 @@ static int setup_device(pgb_solver *s)
       double dx2[3] = {1, 1, 1};
       for (f = 0; f < PGB_NF; f++) db->f[f] = (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
       if (w32o)
-         for (f = 0; f < 4; f++) db->w32[f] = (float *)(s->arena + w32o[i * 4 + f]);
+         for (f = 0; f < PGB_NW32; f++) db->w32[f] = (float *)(s->arena + w32o[i * PGB_NW32 + f]);
       db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
       db->cmask_bdy = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF + 1]);
       CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
@@ -586,10 +586,20 @@ static int sync_field(pgb_solver *s, const pgb_plan *p, int field)
 static int autotune(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
-   const char *env = getenv("PGB_AUTOTUNE");
+   const char *env = getenv("PGB_AUTOTUNE"), *force = getenv("PGB_SWEEP_FUSE");
    int L, changed = 0;
    int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
    s->tuned = 1;
+   if (force && force[0] >= '0' && force[0] <= '2' && !force[1]) {
+      /* one sweep shape on every level instead of the measured choice */
+      for (L = 2; L <= h->nlev; L++) {
+         int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
+         int f = force[0] - '0';
+         s->fuse[L] = f > 1 && !can_fuse ? 1 : f;
+      }
+      drop_graph(s);
+      return 0;
+   }
    if ((env && !strcmp(env, "0")) || nsw < 1) return 0;
    for (L = 2; L <= h->nlev; L++) {
       static const int tzs[4] = {8, 4, 2, 1};
@@ -951,16 +961,21 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    if (L < 1 || L > s->h.nlev || reps < 1) return fail(3, "bad level or reps");
    int mixed = s->h.prm.precision == PGB_MIXED;
    for (b = 0; b < s->h.lev[L].nbox; b++) pts += s->h.boxes[s->h.lev[L].box[b]].count;
+   /* the mixed form's sweeps run as a smoothing block of the V-cycle does
+    * (pre_swp sweeps with the level's tuned tile depth and sweeps per
+    * launch, no sync between them) */
+   int nsw = mixed && s->h.prm.pre_swp > 0 ? s->h.prm.pre_swp : 1;
+   if (mixed && !s->tuned && autotune(s)) return 10;
    s->prepared = 0;   /* the sweeps change the level: the next cycle starts from pgb_prepare */
    for (r = 0; r <= reps; r++) {
-      if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));   /* first sweep warms up */
-      if (mixed) KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, 0, s->stream));
+      if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));   /* first block warms up */
+      if (mixed) KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, s->fuse[L], s->stream));
       else if (relax(s, L, N_RELAX_UP)) return 11;
    }
    CU(cudaEventRecord(s->ev1, s->stream));
    CU(cudaEventSynchronize(s->ev1));
    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-   if (ms_per_sweep) *ms_per_sweep = ms / reps;
+   if (ms_per_sweep) *ms_per_sweep = ms / ((double)reps * nsw);
    /* FP64 sweep: u read+write, rhs, src (32 B); FP32 sweep on the
     * correction: e read+write, defect, Jacobian term (16 B) */
    if (bytes_per_sweep) *bytes_per_sweep = (mixed ? 16.0 : 32.0) * pts;

@@ -198,9 +198,12 @@ def make_dataset(n: int, seeds, torch, cycles: int = 12, precision: int = 1):
     zero = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
     u = torch.empty(n ** 3, dtype=torch.float64, device="cuda")
     blobs, U = [], torch.empty(len(seeds), n ** 3, dtype=torch.float32, device="cuda")
+    st = torch.cuda.ExternalStream(s.stream())
+    torch.cuda.synchronize()
     for k, seed in enumerate(seeds):
         b = W.poisson3d_blobs(seed)
-        rho = rho_on_device(n, b, torch)
+        with torch.cuda.stream(st):   # ordered before the solver's copy of it
+            rho = rho_on_device(n, b, torch)
         s.set_inputs_device([zero.data_ptr()], [rho.data_ptr()])
         s.solve()
         _check(lib().pgb_get_grid_device(s.h, 0, u.data_ptr()))

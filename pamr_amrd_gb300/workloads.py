@@ -260,6 +260,66 @@ def conformal3d(n: int = 129, m: int = 65, seed: int = 0, rel_tol: float = 1e-10
     return _finish(case, rel_tol)
 
 
+def lapse_shell(seed: int = 0):
+    """(radius, amplitude, width) of lapse2d_bo's Gaussian shell"""
+    rng = SplitMix64(0x5EED0004 + seed)
+    return rng.uniform(2.0, 6.0), rng.uniform(0.01, 0.1), rng.uniform(0.3, 1.0)
+
+
+def shell_radius(r0: float, step: int, steps: int) -> float:
+    """the shell breathes once over the run: R = r0 (1 + sin(2 pi step / steps) / 4)"""
+    return r0 * (1.0 + 0.25 * math.sin(2.0 * math.pi * step / steps))
+
+
+def lapse_source(g: Grid, radius: float, amp: float, width: float) -> np.ndarray:
+    """S = amp exp(-((r - radius) / width)^2) on grid g (2-D)"""
+    x, y, _ = _mesh(g, 2)
+    r = np.sqrt(x * x + y * y)
+    out = amp * np.exp(-((r - radius) / width) ** 2) * np.ones((1, g.shape[1], g.shape[0]))
+    return np.ascontiguousarray(out).reshape(-1)
+
+
+def lapse2d_bo_grids(n: int, seed: int, levels: int):
+    """the fixed hierarchy of lapse2d_bo: the n^2 base grid on [-10,10]^2
+    and one centred box per refined level (ratio 2), each covering the
+    shell's whole excursion plus three widths, nested half a unit inside
+    its parent, edges on the parent's grid lines"""
+    r0, _, w = lapse_shell(seed)
+    bbox = (-10.0, 10.0, -10.0, 10.0)
+    dx1 = 20.0 / (n - 1)
+    grids = [Grid(1, bbox, (n, n, 1))]
+    half = min(9.0, 1.25 * r0 + 3.0 * w + 1.0)
+    for lev in range(2, levels + 1):
+        dxp = dx1 / 2 ** (lev - 2)
+        h = dxp * math.floor(half / dxp)
+        grids.append(_grid_from_bbox(lev, (-h, h, -h, h), [dxp / 2] * 2, 2))
+        half = h - 0.5
+    return bbox, grids
+
+
+def lapse2d_bo(n: int = 257, seed: int = 0, levels: int = 4, step: int = 0, steps: int = 400,
+               rel_tol: float = 1e-10, params: MGParams | None = None) -> Case:
+    """one coarse step of the Berger-Oliger lapse sequence: the
+    maximal-slicing lapse equation lap(alpha) = alpha S on the fixed
+    hierarchy of lapse2d_bo_grids, alpha = 1 on the outer boundary (initial
+    guess alpha = 1), S = the Gaussian shell at `step` of `steps` coarse
+    steps (Courant 0.5: dt = dx/2 on the base grid; the shell's radius
+    follows shell_radius). The tolerance is rel_tol times the initial
+    residual of step 0, the same absolute tolerance for every step of the
+    sequence, as AMRD keeps MG_tol fixed during a run."""
+    r0, amp, w = lapse_shell(seed)
+    bbox, grids = lapse2d_bo_grids(n, seed, levels)
+    u0 = [np.ones(g.size) for g in grids]
+    src0 = [lapse_source(g, shell_radius(r0, 0, steps), amp, w) for g in grids]
+    case = Case(f"lapse2d_bo_{n}_L{levels}_s{seed}", LAPSE, 2, (n, n, 1), bbox, grids, u0, src0,
+                params or MGParams())
+    _finish(case, rel_tol)
+    if step:
+        case.src = [lapse_source(g, shell_radius(r0, step, steps), amp, w) for g in grids]
+        case.name += f"_t{step}"
+    return case
+
+
 def poisson2d_uneven(seed: int = 0, n: int = 129, levels: int = 5, min_boxes: int = 8,
                      max_boxes: int = 64, min_side: int = 17, max_side: int = 129,
                      rel_tol: float = 1e-10, params: MGParams | None = None,

@@ -7,7 +7,8 @@ what the reference produced: V-cycle count, every relax/residual/L_op hook
 call with its norm, the MG hierarchy, the cmask arrays, the final u on every
 grid and the m_util_r8 call log of the whole solve.
 
-usage: python tests/golden/make_golden.py   (needs oracle/_ref/ref_mg)
+usage: python tests/golden/make_golden.py [--all]   (needs oracle/_ref/ref_mg)
+Writes the fixtures that are missing; --all rewrites every one.
 """
 from __future__ import annotations
 
@@ -34,6 +35,8 @@ def cases():
                            max_side=17),
         W.poisson2d_uneven(seed=2, n=65, levels=4, min_boxes=3, max_boxes=8, min_side=9,
                            max_side=33),
+        W.lapse2d_bo(17, seed=0, levels=3),
+        W.lapse2d_bo(17, seed=1, levels=3, step=100),
     ]
 
 
@@ -70,8 +73,10 @@ def main():
     if not refrun.available():
         raise SystemExit("oracle/_ref/ref_mg missing: run oracle/build_ref.sh first")
     for c in cases():
-        ref = refrun.run_reference(c, log_ops=True)
         path = os.path.join(HERE, f"{c.name}__{len(c.grids)}g_{c.params.min_cwidth}cw.npz")
+        if os.path.exists(path) and "--all" not in sys.argv:
+            continue
+        ref = refrun.run_reference(c, log_ops=True)
         save(c, ref, path)
         print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
               f"{len(ref['ops'])} m_util_r8 calls, {os.path.getsize(path) // 1024} KiB")

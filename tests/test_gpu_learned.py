@@ -26,6 +26,7 @@ def test_guessed_solve_converges_to_the_plain_solution(precision):
     sv = Solver(case)
     rho = Lm.rho_on_device(n, W.poisson3d_blobs(100000), torch)
     zero = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()   # the solver copies on its own stream
     sv.set_inputs_device([zero.data_ptr()], [rho.data_ptr()])
     r0 = sv.solve()
     u0 = np.concatenate(sv.get_u())

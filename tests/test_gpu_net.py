@@ -3,7 +3,7 @@ convolution (pgb_conv3d_bf16, tcgen05) against a plain PyTorch FP32
 convolution of the same BF16-rounded inputs and weights: outputs agree to
 BF16 rounding and the padding stays zero; the adjoint weight image gives
 the transposed convolution. The whole network's loss and gradients against
-a PyTorch FP32 replica, and training lowering the loss."""
+a PyTorch FP32 replica on the CPU, and training lowering the loss."""
 import numpy as np
 import pytest
 
@@ -93,9 +93,10 @@ def test_conv3d_matches_torch(cin, cout, vol, adjoint):
 
 # ------------------------------------------------------------- the network --
 def _torch_net(net, flat, x):
-    """plain FP32 PyTorch replica of the network (same parameters)"""
+    """plain FP32 PyTorch replica of the network (same parameters), on the
+    CPU: the oracle of the GPU forward and backward kernels"""
     F = torch.nn.functional
-    P = {k: (torch.tensor(w).cuda().requires_grad_(True), torch.tensor(b).cuda().requires_grad_(True))
+    P = {k: (torch.tensor(w).requires_grad_(True), torch.tensor(b).requires_grad_(True))
          for k, (w, b) in net.split(flat.copy()).items()}
 
     def conv(name, a, relu=True):
@@ -145,9 +146,9 @@ def test_net_gradients_match_torch_fp32():
         if name.startswith("tc"):
             pb[o:o + k] = torch.tensor(pb[o:o + k]).to(torch.bfloat16).float().numpy()
         o += k + co
-    x = torch.tensor(2.0 * rho[:n - 1, :n - 1, :n - 1], dtype=torch.float32).cuda()[None, None]
+    x = torch.tensor(2.0 * rho[:n - 1, :n - 1, :n - 1], dtype=torch.float32)[None, None]
     y, P = _torch_net(net, pb, x)
-    tgt = torch.tensor(ut[:n - 1, :n - 1, :n - 1] / 0.5).cuda()[None, None]
+    tgt = torch.tensor(ut[:n - 1, :n - 1, :n - 1] / 0.5)[None, None]
     d = (y - tgt)[..., 1:, 1:, 1:]
     ref_loss = (d * d).mean()
     ref_loss.backward()

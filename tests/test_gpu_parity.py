@@ -59,10 +59,13 @@ LARGER = [
     lambda: W.conformal3d(33, 17, seed=1),
     lambda: W.conformal3d(65, 33, seed=2),
     lambda: W.poisson2d_uneven(seed=0, n=129, levels=5, min_boxes=8, max_boxes=24),
+    lambda: W.lapse2d_bo(65, seed=2, levels=4),
+    lambda: W.lapse2d_bo(65, seed=3, levels=4, step=300),
 ]
 
 
-@pytest.mark.parametrize("make", LARGER, ids=["p2d129", "p2d257", "c3d33", "c3d65", "uneven129"])
+@pytest.mark.parametrize("make", LARGER, ids=["p2d129", "p2d257", "c3d33", "c3d65", "uneven129",
+                                              "lapse65", "lapse65_t300"])
 def test_fp64_matches_oracle_port(make):
     case = make()
     r = _solve(case)
@@ -84,3 +87,22 @@ def test_full_size_conformal_converges_and_matches_port():
     assert r["iters"] == p["iters"]
     for a, b in zip(r["u"], p["u"]):
         assert np.array_equal(a, b)
+
+
+def test_lapse_sequence_warm_started_matches_port():
+    """three coarse steps of the Berger-Oliger lapse sequence, each solve
+    started from the previous step's lapse: the same V-cycle counts and
+    bit-identical lapse as the oracle port doing the same"""
+    u_gpu = u_port = None
+    for k in range(3):
+        case = W.lapse2d_bo(33, seed=4, levels=4, step=k, steps=8)
+        cg, cp = case, W.lapse2d_bo(33, seed=4, levels=4, step=k, steps=8)
+        if k:
+            cg.u0, cp.u0 = [a.copy() for a in u_gpu], [a.copy() for a in u_port]
+        r = _solve(cg)
+        p = portrun.solve(cp)
+        assert r["iters"] == p["iters"]
+        for a, b in zip(r["u"], p["u"]):
+            assert np.array_equal(a, b)
+        assert r["res_final"] <= case.params.tol
+        u_gpu, u_port = r["u"], p["u"]
