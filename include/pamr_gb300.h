@@ -133,9 +133,10 @@ int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
                    double *bytes_per_sweep);
 
 /* Launch shapes the mixed form's autotuner chose for a level at the first
- * pgb_prepare: tile depth in planes, and FP32 sweeps per launch (0 = one
- * launch per colour pass, 1 or 2 = shared-memory sweeps); no reference
- * counterpart. */
+ * pgb_prepare: tile depth in planes, and the FP32 sweep kernel (0 = one
+ * launch per colour pass, 1 or 2 = sweeps per launch staged in shared
+ * memory, 3 = one sweep per launch in one pass over memory, marching
+ * through the tile's planes; 3-D levels); no reference counterpart. */
 int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per_launch);
 
 /* Norm trace: when enabled, every norm a hook would return is recorded

@@ -29,8 +29,9 @@ typedef struct {
    const int *box;             /* level box -> global box index */
    const pgb_tile *ctiles;     /* tiles holding a child-covered point or a point some
                                   interpolation to the next finer level reads */
-   int ntiles, nrtiles, nbox, nctiles;
-   int tz, rtz;                /* planes per tile (3-D) of the two tile lists */
+   const pgb_tile *ztiles;     /* 32 x 8 x ztz columns (one-pass marching sweep, 3-D) */
+   int ntiles, nrtiles, nbox, nctiles, nztiles;
+   int tz, rtz, ztz;           /* planes per tile (3-D) of the tile lists */
    int dim;
    int level;
 } pgb_dlevel;

@@ -330,6 +330,138 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
    }
 }
 
+/* One red-black sweep in one pass over memory (3-D levels): the CTA owns a
+ * 32 x 8 column of ztz planes (a ztile) and marches through it, two planes
+ * per step. Planes of the old correction (slot src), D and C, each with a
+ * halo of two points, stream into 8-plane rings in shared memory by
+ * cp.async, one step ahead of use. Step k (k, k+1 landed): the first colour
+ * of planes k-1 and k on the column grown by one point (from old
+ * second-colour values), then the second colour of planes k-2 and k-1 on
+ * the column (from the new first-colour values of the planes around them),
+ * then planes k-2 and k-1 are written to slot dst. The first colour of the
+ * planes just outside the chunk is recomputed for the purpose; as in
+ * k_sweep32 no CTA writes the slot the others read, so every value equals
+ * that of the in-place colour passes bit for bit. Traffic: each array once
+ * per sweep (16 B per point) plus halo re-reads, against two passes over
+ * every array for the colour-pass kernels. */
+#define ZX (PGB_TX + 4)
+#define ZY (PGB_TY + 4)
+#define ZR 8            /* ring depth (planes) */
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float *src, bool valid)
+{
+   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlevel lv, int src, int dst)
+{
+   constexpr int PL = ZX * ZY;   /* floats per staged plane */
+   __shared__ float se[ZR * PL], sd[ZR * PL], sc[ZR * PL];
+   const pgb_tile tl = lv.ztiles[blockIdx.x];
+   const pgb_dbox *bp = boxes + tl.box;
+   const int n0 = bp->n[0], n1 = bp->n[1], n2 = bp->n[2];
+   const long sz = (long)n0 * n1;
+   const float *__restrict__ e = bp->w32[src];
+   float *__restrict__ eo = bp->w32[dst];
+   const float *__restrict__ dd = bp->w32[W_D];
+   const float *__restrict__ cc = bp->w32[W_C];
+   const uint8_t *__restrict__ cmb = (bp->flags & PGB_BOX_BDY_INTERIOR) ? nullptr : bp->cmask_bdy;
+   const float ix = bp->fidx2[0], iy = bp->fidx2[1], iz = bp->fidx2[2];
+   const float j0 = bp->fj0;
+   const int t = threadIdx.x + threadIdx.y * PGB_TX;
+   const int gi0 = tl.i0 - 2, gj0 = tl.j0 - 2;
+   const int k0 = tl.k0, k1 = min(tl.k0 + lv.ztz, n2);   /* planes [k0, k1) written */
+
+   /* what a thread does is the same on every plane: its staged points (two
+    * at most), its point of each colour pass for both parities, and its
+    * store, as offsets within a plane */
+   const uint32_t ue = (uint32_t)__cvta_generic_to_shared(se), ud = (uint32_t)__cvta_generic_to_shared(sd),
+                  uc = (uint32_t)__cvta_generic_to_shared(sc);
+   int lso[2], lgo[2];
+   bool lin[2], lany[2];
+#pragma unroll
+   for (int u = 0; u < 2; u++) {
+      const int q = t + u * NT, x = q % ZX, y = q / ZX, gi = gi0 + x, gj = gj0 + y;
+      lany[u] = q < PL;
+      lin[u] = lany[u] && gi >= 0 && gi < n0 && gj >= 0 && gj < n1;
+      lso[u] = 4 * q;
+      lgo[u] = lin[u] ? gi + n0 * gj : 0;
+   }
+   int rso[2][2], rgo[2][2], rpar[2];   /* [pass][parity] */
+   bool rok[2][2];
+#pragma unroll
+   for (int pass = 0; pass < 2; pass++) {
+      const int grow = 1 - pass, w = PGB_TX + 2 * grow, h = PGB_TY + 2 * grow, slots = (w + 1) / 2;
+      const int y = 2 - grow + t / slots, gj = gj0 + y, xs = 2 - grow;
+      rpar[pass] = (gi0 + xs + gj + 1 + pass) & 1;   /* parity at plane 0; flips with the plane */
+#pragma unroll
+      for (int par = 0; par < 2; par++) {
+         const int x = xs + par + 2 * (t % slots), gi = gi0 + x;
+         rok[pass][par] = t < slots * h && x < xs + w && gi >= 1 && gi <= n0 - 2 && gj >= 1 && gj <= n1 - 2;
+         rso[pass][par] = y * ZX + x;
+         rgo[pass][par] = rok[pass][par] ? gi + n0 * gj : 0;
+      }
+   }
+   const int sxs = 2 + t % PGB_TX, sys_ = 2 + t / PGB_TX;
+   const bool sok = gi0 + sxs < n0 && gj0 + sys_ < n1;
+   const int sso = sys_ * ZX + sxs;
+   const long sgo = (long)(gi0 + sxs) + (long)n0 * (gj0 + sys_);
+
+   auto fetch = [&](int k) {   /* plane k's copies (none outside the box or past what the chunk reads) */
+      if (k < 0 || k >= n2 || k > k1 + 1) return;
+      const long koff = sz * k;
+      const uint32_t r = 4u * (uint32_t)((k & (ZR - 1)) * PL);
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+         if (lany[u]) {
+            const long g = lin[u] ? koff + lgo[u] : 0;
+            cp_async4(ue + r + lso[u], e + g, lin[u]);
+            cp_async4(ud + r + lso[u], dd + g, lin[u]);
+            cp_async4(uc + r + lso[u], cc + g, lin[u]);
+         }
+   };
+   /* colour `pass` of plane kp */
+   auto relax = [&](int pass, int kp) {
+      const bool active = pass == 0 ? (kp >= k0 - 1 && kp <= k1) : (kp >= k0 && kp < k1);
+      const bool odd = (rpar[pass] + kp) & 1;   /* registers, not an indexed array */
+      const bool ok = odd ? rok[pass][1] : rok[pass][0];
+      const int o = odd ? rso[pass][1] : rso[pass][0], go = odd ? rgo[pass][1] : rgo[pass][0];
+      if (active && kp >= 1 && kp <= n2 - 2 && ok && (!cmb || cmb[go + sz * kp])) {
+         const int r = (kp & (ZR - 1)) * PL;
+         const float *m = se + ((kp - 1) & (ZR - 1)) * PL, *pl = se + ((kp + 1) & (ZR - 1)) * PL;
+         float *c = se + r;
+         c[o] = gs32(c[o], c[o - 1], c[o + 1], c[o - ZX], c[o + ZX], m[o], pl[o], sc[r + o], sd[r + o], ix, iy, iz,
+                     j0, true);
+      }
+   };
+
+   fetch(k0 - 2);
+   fetch(k0 - 1);
+   cp_async_commit();
+   for (int k = k0 - 2; k <= k1 + 1; k += 2) {
+      cp_async_wait_all();   /* planes k, k+1 */
+      __syncthreads();
+      fetch(k + 2);
+      fetch(k + 3);
+      cp_async_commit();
+      relax(0, k - 1);
+      relax(0, k);
+      __syncthreads();
+      relax(1, k - 2);
+      relax(1, k - 1);
+      __syncthreads();
+#pragma unroll
+      for (int kw = k - 2; kw < k; kw++)   /* planes finished at this step */
+         if (kw >= k0 && kw < k1 && sok) eo[sgo + sz * kw] = se[(kw & (ZR - 1)) * PL + sso];
+   }
+   cp_async_wait_all();
+}
+#undef ZX
+#undef ZY
+#undef ZR
+
 /* E = the correction in slot src, over the level's tiles (the end of an
  * odd number of fused sweep launches) */
 __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel lv, int src)
@@ -1026,7 +1158,10 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
    }
    /* fused launches alternate between the two correction slots */
    while (done < nsweep) {
-      if (fuse >= 2 && nsweep - done >= 2) {
+      if (fuse == 3 && lv.dim == 3) {
+         k_sweep32z<<<lv.nztiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src, dst);
+         done += 1;
+      } else if (fuse >= 2 && fuse != 3 && nsweep - done >= 2) {
          k_sweep32<2><<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src, dst);
          done += 2;
       } else {

@@ -217,13 +217,15 @@ static void free_plan_dev(pgb_plan *p)
 static int level_tables(pgb_solver *s, int L, int tz)
 {
    pgb_hier *h = &s->h;
-   pgb_tile *t = 0, *rt = 0, *ct = 0;
+   pgb_tile *t = 0, *rt = 0, *ct = 0, *zt = 0;
    int nb = h->lev[L].nbox, nct;
    int *ts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
    int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
-   int rtz = tz;
+   int *zts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
+   int rtz = tz, ztz = h->dim == 3 ? 4 * tz : 1;
    int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
    int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
+   int nzt = make_tiles(h, L, PGB_TX, ztz, &zt, zts);
    size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
    size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
    size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
@@ -233,9 +235,10 @@ static int level_tables(pgb_solver *s, int L, int tz)
    int rc = 0;
    nct = make_cover_tiles(h, L, t, nt, tz, &ct);
    b6 = b5 + align256(sizeof(pgb_tile) * (size_t)(nct ? nct : 1));
+   size_t b7 = b6 + align256(sizeof(pgb_tile) * (size_t)nzt);
    if (s->d_tables[L]) cudaFree(s->d_tables[L]);
    s->d_tables[L] = 0;
-   if (cudaMalloc(&s->d_tables[L], b6) != cudaSuccess) {
+   if (cudaMalloc(&s->d_tables[L], b7) != cudaSuccess) {
       rc = fail(10, "cudaMalloc of the level tables failed");
       goto out;
    }
@@ -245,7 +248,8 @@ static int level_tables(pgb_solver *s, int L, int tz)
        cudaMemcpy(dt + b1, rt, sizeof(pgb_tile) * (size_t)nrt, cudaMemcpyHostToDevice) ||
        cudaMemcpy(dt + b2, ts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
        cudaMemcpy(dt + b3, rts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
-       cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice)) {
+       cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice) ||
+       cudaMemcpy(dt + b6, zt, sizeof(pgb_tile) * (size_t)nzt, cudaMemcpyHostToDevice)) {
       rc = fail(10, "upload of the level tables failed");
       goto out;
    }
@@ -256,6 +260,9 @@ static int level_tables(pgb_solver *s, int L, int tz)
    s->lv[L].box = (const int *)(dt + b4);
    s->lv[L].ctiles = (const pgb_tile *)(dt + b5);
    s->lv[L].nctiles = nct;
+   s->lv[L].ztiles = (const pgb_tile *)(dt + b6);
+   s->lv[L].nztiles = nzt;
+   s->lv[L].ztz = ztz;
    s->lv[L].ntiles = nt;
    s->lv[L].nrtiles = nrt;
    s->lv[L].nbox = nb;
@@ -267,8 +274,10 @@ out:
    free(t);
    free(rt);
    free(ct);
+   free(zt);
    free(ts);
    free(rts);
+   free(zts);
    return rc;
 }
 
@@ -590,12 +599,13 @@ static int autotune(pgb_solver *s)
    int L, changed = 0;
    int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
    s->tuned = 1;
-   if (force && force[0] >= '0' && force[0] <= '2' && !force[1]) {
+   if (force && force[0] >= '0' && force[0] <= '3' && !force[1]) {
       /* one sweep shape on every level instead of the measured choice */
       for (L = 2; L <= h->nlev; L++) {
          int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
          int f = force[0] - '0';
-         s->fuse[L] = f > 1 && !can_fuse ? 1 : f;
+         if (f == 3 && h->dim != 3) f = 1;
+         s->fuse[L] = f == 2 && !can_fuse ? 1 : f;
       }
       drop_graph(s);
       return 0;
@@ -611,7 +621,8 @@ static int autotune(pgb_solver *s)
             if (level_tables(s, L, tzs[a])) return 10;
             changed = 1;
          }
-         for (f = 0; f <= (can_fuse ? 2 : 1); f++) {
+         for (f = 0; f <= (h->dim == 3 ? 3 : can_fuse ? 2 : 1); f++) {
+            if (f == 2 && !can_fuse) continue;
             float ms = 0;
             int r;
             for (r = 0; r < 4; r++) {   /* one warm-up, three timed */
@@ -645,8 +656,8 @@ int pgb_level_tuning(pgb_solver *s, int L, int *tile_planes, int *sweeps_per_lau
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (L < 1 || L > s->h.nlev) return fail(3, "level %d out of range", L);
    if (tile_planes) *tile_planes = s->lv[L].tz;
-   if (sweeps_per_launch)   /* 0: one launch per colour pass */
-      *sweeps_per_launch = (s->fuse[L] > 1 && (s->h.sync[L][0].nops || s->h.sync[L][1].nops)) ? 1 : s->fuse[L];
+   if (sweeps_per_launch)   /* 0: one launch per colour pass; 3: one-pass z-marching sweep */
+      *sweeps_per_launch = (s->fuse[L] == 2 && (s->h.sync[L][0].nops || s->h.sync[L][1].nops)) ? 1 : s->fuse[L];
    return 0;
 }
 
@@ -792,7 +803,7 @@ static int sweeps32(pgb_solver *s, int L, int nsweep)
       return 0;
    }
    for (it = 0; it < nsweep; it++) {
-      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] > 1 ? 1 : s->fuse[L], s->stream));
+      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] == 2 ? 1 : s->fuse[L], s->stream));
       if (h->sync[L][it ? 1 : 0].nops) KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], s->stream));
    }
    return 0;
