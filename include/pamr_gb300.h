@@ -242,6 +242,29 @@ int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int ad
 int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H, int D,
                     int cin, int cout, int relu, int *err, void *stream);
 
+/* Berger-Oliger bookkeeping of the elliptic variables on the device, for
+ * an application that keeps them there across coarse steps. Grids are host
+ * arrays of device pointers with their AMR levels (level[g]) and point
+ * counts (n[g]); all work is queued on `stream`.
+ * pgb_mg_extrap: the new-time-level guess of one grid on a level > 1
+ *   (amrd/evolve.c:344-366): method 0 (AMRD_MG_EXTRAP_2ND_FROM_ETM1)
+ *   mgf0 = f1 etm1 + f2 etm2 with f1, f2 from tnp1, the parent's tnp1_lm1
+ *   and dt_lm1; method 1 (AMRD_MG_EXTRAP_2ND_FROM_TN)
+ *   mgf0 = mgf1 + dt/dt_lm1 (etm2 - etm1).
+ * pgb_update_mg_extrap_vars: update_mg_extrap_vars (amrd/evolve.c:1640-1700):
+ *   etm1 -> etm2, mgf1 -> etm1, and on levels > 1 with eps_c != 0
+ *   etm2 += (etm1 - brs)(1 - eps_c/net_rho); rho_tm as PAMR_get_rho returns it.
+ * pgb_set_mg_brs_vars: set_mg_brs_vars (amrd/evolve.c:1621-1638), brs = mgf1
+ *   on levels L1..L2.
+ * Bit-exact with the reference's loops. */
+int pgb_mg_extrap(int method, double tnp1, double tnp1_lm1, double dt, double dt_lm1, double *mgf0,
+                  const double *mgf1, const double *etm1, const double *etm2, long n, void *stream);
+int pgb_update_mg_extrap_vars(int L1, int Lf, const int *rho_tm, int ngrids, const int *level,
+                              double *const *etm1, double *const *etm2, const double *const *mgf1,
+                              const double *const *brs, const long *n, double eps_c, void *stream);
+int pgb_set_mg_brs_vars(int L1, int L2, int ngrids, const int *level, double *const *brs,
+                        const double *const *mgf1, const long *n, void *stream);
+
 /* The learned initial guess: a 6-level convolutional encoder-decoder
  * (16/32/64/64/64/64 channels, levels halving down to (n-1)/32 points a
  * side, two 3x3x3 convolutions per encoder level, one per decoder level,

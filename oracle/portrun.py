@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "port", "libmgport.so")
 SOURCES = [os.path.join(HERE, "port", "mg_port.c"), os.path.join(HERE, "mg_ops.c"),
-           os.path.join(HERE, "m_util_r8.c")]
+           os.path.join(HERE, "m_util_r8.c"), os.path.join(HERE, "bo_ops.c")]
 
 
 def build(force: bool = False) -> str:

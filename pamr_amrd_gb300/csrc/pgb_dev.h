@@ -99,6 +99,7 @@ int pgb_k_fill(double *p, long n, double v, void *stream);
 /* excision m_util_r8 kernels (pgb_mutil_ex.cu) */
 unsigned long long pgb_dev_launches_ex(void);
 unsigned long long pgb_dev_launches_net(void);   /* pgb_net.cu */
+unsigned long long pgb_dev_launches_bo(void);    /* pgb_bo.cu */
 
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);
