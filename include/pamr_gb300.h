@@ -242,6 +242,16 @@ int pgb_conv3d_pack_weights(const float *w, void *img, int cin, int cout, int ad
 int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bias, int W, int H, int D,
                     int cin, int cout, int relu, int *err, void *stream);
 
+/* Kreiss-Oliger dissipation, dmdiss3d (src/m_util_r8.f:1690-1956;
+ * include/m_util_r8.h:33-36), on device arrays f, work, eps (eps[0] is the
+ * coefficient, as eps(1,1,1)), mask; phys_bdy_type is a host array of 6.
+ * Bit-exact with the Fortran; the excised path (do_ex != 0) is rejected
+ * (error 12). Called by AMRD after each step on the dissipated variables
+ * (amrd/evolve.c:430, 509, 957). */
+int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_bdy, const int *phys_bdy_type,
+                 int even, int odd, const double *mask, double mask_off, int nx, int ny, int nz,
+                 const double *chr, double ex, int do_ex, void *stream);
+
 /* Berger-Oliger bookkeeping of the elliptic variables on the device, for
  * an application that keeps them there across coarse steps. Grids are host
  * arrays of device pointers with their AMR levels (level[g]) and point

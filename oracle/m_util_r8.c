@@ -17,8 +17,10 @@
  * Fortran, counts as weight 0 here) and dvi4q1d_ex's right-side
  * extrapolation tests i <= i1s-4*s1. No Fortran compiler is available, so
  * these are pinned by known-answer tests, not by running the reference.
- * The evolution-only routines (dmdiss3d, linbnd3d, dmrepop3d1, dmrepop3dc1)
- * are not on the elliptic path and abort if reached.
+ * dmdiss3d (Kreiss-Oliger dissipation, the evolution kernel next to the
+ * elliptic solve) is restated without its excised path (dmdiss3d_ex). The
+ * other evolution-only routines (linbnd3d, dmrepop3d1, dmrepop3dc1) are not
+ * on the path and abort if reached.
  *
  * Optional call log: when mur8_log_enabled is set, every call records its
  * kernel id and index arguments so a test can compare the reference's
@@ -664,14 +666,99 @@ void dmfwr3d_(double *u1, double *u2, int *pnx1, int *pny1, int *pnz1, int *pnx2
 #undef U
 }
 
-/* evolution-only kernels (src/m_util_r8.f:972-2470): not on the elliptic path */
+/* Kreiss-Oliger dissipation term of one point along one dimension
+ * (src/m_util_r8.f:1736-1801 for i, 1803-1868 for j, 1870-1935 for k): w
+ * points at work(i,j,k), s is the stride of the dimension, p the 1-based
+ * position along it and n its extent; lo/hi are the faces' cdo_bdy and
+ * phys_bdy_type. Same branches and expression order as the Fortran. */
+static double diss_hf(const double *w, long s, int p, int n, int cdo_lo, int cdo_hi, int pbt_lo, int pbt_hi,
+                      int even, int odd)
+{
+   const double w4 = 1.0 / 16.0, w3 = 1.0 / 8.0, w2 = 1.0 / 4.0;
+   double f_hf = 0;
+#define W(o) w[(o) * s]
+   if (p > 2 && p < (n - 1)) {
+      f_hf = w4 * (W(-2) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   } else {
+      if (cdo_lo != 0 && n >= 5) {
+         if (p == 2 && pbt_lo == odd)
+            f_hf = w4 * ((-W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+         else if (p == 2 && pbt_lo == even)
+            f_hf = w4 * ((W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+         else if (p == 2)
+            f_hf = w3 * (-W(-1) + 3 * W(0) - 3 * W(1) + W(2));
+         else if (p == 1 && pbt_lo == odd)
+            f_hf = w4 * ((-W(2)) + W(2) - 4 * ((-W(1)) + W(1)) + 6 * W(0));
+         else if (p == 1 && pbt_lo == even)
+            f_hf = w4 * ((W(2)) + W(2) - 4 * ((W(1)) + W(1)) + 6 * W(0));
+         else if (p == 1)
+            f_hf = w2 * (W(0) - 2 * W(1) + W(2));
+      }
+      if (cdo_hi != 0 && n >= 5) {
+         if (p == (n - 1) && pbt_hi == odd)
+            f_hf = w4 * (W(-2) + (-W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+         else if (p == (n - 1) && pbt_hi == even)
+            f_hf = w4 * (W(-2) + (W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+         else if (p == (n - 1))
+            f_hf = w3 * (-W(1) + 3 * W(0) - 3 * W(-1) + W(-2));
+         else if (p == n && pbt_hi == odd)
+            f_hf = w4 * (W(-2) + (-W(-2)) - 4 * (W(-1) + (-W(-1))) + 6 * W(0));
+         else if (p == n && pbt_hi == even)
+            f_hf = w4 * (W(-2) + (W(-2)) - 4 * (W(-1) + (W(-1))) + 6 * W(0));
+         else if (p == n)
+            f_hf = w2 * (W(0) - 2 * W(-1) + W(-2));
+      }
+   }
+#undef W
+   return f_hf;
+}
+
+/* dmdiss3d (src/m_util_r8.f:1690-1956), the path without excision:
+ * independent sweeps (ind_sweeps = .true.), one pass per dimension of
+ * extent > 1 (npass 1, 2 or 3); each pass copies f to work and subtracts
+ * eps(1,1,1) times the dissipation term along its dimension at every point
+ * whose mask is not mask_off. The excised path (dmdiss3d_ex) is not on the
+ * restated path and aborts. */
 void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_type, int *even,
                int *odd, double *mask, double *mask_off, int *nx, int *ny, int *nz, double *chr,
                double *ex, int *do_ex)
 {
-   (void)f; (void)work; (void)eps; (void)do_bdy; (void)phys_bdy_type; (void)even; (void)odd;
-   (void)mask; (void)mask_off; (void)nx; (void)ny; (void)nz; (void)chr; (void)ex; (void)do_ex;
-   not_on_path("dmdiss3d");
+   const int Nx = *nx, Ny = *ny, Nz = *nz;
+   const long sy = Nx, sz = (long)Nx * Ny, ntot = (long)Nx * Ny * Nz;
+   int cdo_bdy[6], i, j, k, pass, npass;
+   long q;
+   double eps_eff;
+   (void)chr;
+   (void)ex;
+   if (*do_ex != 0) not_on_path("dmdiss3d_ex");
+   for (i = 0; i < 6; i++) {
+      cdo_bdy[i] = *do_bdy;
+      if (phys_bdy_type[i] == *even || phys_bdy_type[i] == *odd) cdo_bdy[i] = 1;
+   }
+   eps_eff = eps[0];
+   npass = 1;
+   if (Ny > 1) npass = 2;
+   if (Nz > 1) npass = 3;
+   for (pass = 1; pass <= npass; pass++) {
+      for (q = 0; q < ntot; q++) work[q] = f[q];
+      for (i = 1; i <= Nx; i++)
+         for (j = 1; j <= Ny; j++)
+            for (k = 1; k <= Nz; k++) {
+               const long c = (i - 1) + sy * (j - 1) + sz * (k - 1);
+               double f_hf;
+               if (mask[c] == *mask_off) continue;
+               if (pass == 1)
+                  f_hf = diss_hf(work + c, 1, i, Nx, cdo_bdy[0], cdo_bdy[1], phys_bdy_type[0], phys_bdy_type[1],
+                                 *even, *odd);
+               else if (pass == 2)
+                  f_hf = diss_hf(work + c, sy, j, Ny, cdo_bdy[2], cdo_bdy[3], phys_bdy_type[2], phys_bdy_type[3],
+                                 *even, *odd);
+               else
+                  f_hf = diss_hf(work + c, sz, k, Nz, cdo_bdy[4], cdo_bdy[5], phys_bdy_type[4], phys_bdy_type[5],
+                                 *even, *odd);
+               f[c] = f[c] - eps_eff * f_hf;
+            }
+   }
 }
 void linbnd3d_(double *f, int *phys_bdy, int *which_bnd, int *Nx, int *Ny, int *Nz, double *chr,
                double *ex, int *do_ex)

@@ -100,6 +100,7 @@ int pgb_k_fill(double *p, long n, double v, void *stream);
 unsigned long long pgb_dev_launches_ex(void);
 unsigned long long pgb_dev_launches_net(void);   /* pgb_net.cu */
 unsigned long long pgb_dev_launches_bo(void);    /* pgb_bo.cu */
+unsigned long long pgb_dev_launches_diss(void);  /* pgb_diss.cu */
 
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);

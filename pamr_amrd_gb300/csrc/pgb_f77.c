@@ -1,7 +1,7 @@
 /*
  * Fortran-ABI drop-in for the m_util_r8 routines an application may call
- * (include/m_util_r8.h:33-66): dmcopy3d_, dmhwr3d_, dmfwr3d_ and
- * dminterp3d_ with every argument by pointer, on HOST arrays, as the
+ * (include/m_util_r8.h:33-66): dmcopy3d_, dmhwr3d_, dmfwr3d_,
+ * dminterp3d_ and dmdiss3d_ with every argument by pointer, on HOST arrays, as the
  * reference's Fortran takes them. Built as its own library
  * (libpamr_gb300_f77.so) so that an application links it in place of the
  * reference's m_util_r8 object without any source change. Each call copies
@@ -16,8 +16,8 @@
 #include <stdio.h>
 #include "pamr_gb300.h"
 
-static double *d_buf[3];
-static size_t d_cap[3];
+static double *d_buf[5];
+static size_t d_cap[5];
 
 static double *dev(int which, const double *h, size_t n)
 {
@@ -116,4 +116,25 @@ void dminterp3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2,
                           *ni, *nj, *nk, *si1, *sj1, *sk1, *irho, *jrho, *krho, *ord, 0);
    if (!rc) rc = back(u2, d2, n2);
    report("dminterp3d", rc);
+}
+
+/* Kreiss-Oliger dissipation (src/m_util_r8.f:1690-1956): f, work, eps(1)
+ * and mask to the device, pgb_dmdiss3d, f and work back. The excised path
+ * (do_ex != 0) is reported and leaves f unchanged. */
+void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_type, int *even, int *odd,
+               double *mask, double *mask_off, int *nx, int *ny, int *nz, double *chr, double *ex, int *do_ex)
+{
+   size_t n = (size_t)*nx * *ny * *nz;
+   double *df = dev(0, f, n), *dw = dev(1, 0, n), *de = dev(2, eps, 1), *dm = dev(3, mask, n);
+   int rc;
+   (void)chr;
+   if (!df || !dw || !de || !dm) {
+      fprintf(stderr, "dmdiss3d: device buffers unavailable\n");
+      return;
+   }
+   rc = pgb_dmdiss3d(df, dw, de, *do_bdy, phys_bdy_type, *even, *odd, dm, *mask_off, *nx, *ny, *nz, 0, *ex,
+                     *do_ex, 0);
+   if (!rc) rc = back(f, df, n);
+   if (!rc) rc = back(work, dw, n);
+   report("dmdiss3d", rc);
 }

@@ -1,0 +1,74 @@
+"""Kreiss-Oliger dissipation on the GPU (pgb_dmdiss3d, and dmdiss3d_ of
+the Fortran-ABI drop-in library on host arrays) against the oracle's
+restatement of dmdiss3d, bit for bit: 1-, 2- and 3-D grids, random data
+and masks, every face's parity (even, odd, neither) with do_bdy 0 and 1;
+f and work both compared. The excised path is refused."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import portrun
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+D = C.POINTER(C.c_double)
+EVEN, ODD, OTHER = 3, 4, 0
+
+
+def _oracle(f, eps, do_bdy, pbt, mask, shape):
+    lib = C.CDLL(portrun.build())
+    f = f.copy()
+    work = np.zeros_like(f)
+    e = np.array([eps])
+    ci = lambda v: C.byref(C.c_int(v))  # noqa: E731
+    lib.dmdiss3d_(f.ctypes.data_as(D), work.ctypes.data_as(D), e.ctypes.data_as(D), ci(do_bdy), (C.c_int * 6)(*pbt),
+                  ci(EVEN), ci(ODD), mask.ctypes.data_as(D), C.byref(C.c_double(0.0)), ci(shape[0]), ci(shape[1]),
+                  ci(shape[2]), e.ctypes.data_as(D), C.byref(C.c_double(0.0)), ci(0))
+    return f, work
+
+
+def _case(seed, shape):
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(shape))
+    f = rng.standard_normal(n)
+    mask = (rng.random(n) > 0.3).astype(np.float64)
+    pbt = tuple(int(v) for v in rng.choice([EVEN, ODD, OTHER], 6))
+    return f, mask, pbt, float(rng.uniform(0.1, 0.9))
+
+
+@pytest.mark.parametrize("shape", [(33, 29, 21), (41, 37, 1), (57, 1, 1), (5, 6, 7)])
+@pytest.mark.parametrize("do_bdy", [0, 1])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_dmdiss3d_matches_oracle(shape, do_bdy, seed):
+    from pamr_amrd_gb300.solver import lib
+    f, mask, pbt, eps = _case(seed * 100 + do_bdy, shape)
+    want_f, want_w = _oracle(f, eps, do_bdy, pbt, mask, shape)
+    df, dw = torch.from_numpy(f.copy()).cuda(), torch.zeros(f.size, dtype=torch.float64, device="cuda")
+    de, dm = torch.tensor([eps], dtype=torch.float64, device="cuda"), torch.from_numpy(mask).cuda()
+    L = lib()
+    L.pgb_dmdiss3d.argtypes = [C.c_void_p] * 3 + [C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_void_p,
+                                                  C.c_double] + [C.c_int] * 3 + [C.c_void_p, C.c_double, C.c_int,
+                                                                                 C.c_void_p]
+    rc = L.pgb_dmdiss3d(df.data_ptr(), dw.data_ptr(), de.data_ptr(), do_bdy, (C.c_int * 6)(*pbt), EVEN, ODD,
+                        dm.data_ptr(), 0.0, *shape, None, 0.0, 0, None)
+    torch.cuda.synchronize()
+    assert rc == 0
+    assert np.array_equal(df.cpu().numpy(), want_f)
+    assert np.array_equal(dw.cpu().numpy(), want_w)
+    assert rc == 0 and L.pgb_dmdiss3d(df.data_ptr(), dw.data_ptr(), de.data_ptr(), do_bdy, (C.c_int * 6)(*pbt),
+                                      EVEN, ODD, dm.data_ptr(), 0.0, *shape, None, 0.0, 1, None) == 12
+
+
+def test_fortran_abi_dmdiss3d_matches_oracle():
+    from pamr_amrd_gb300 import build
+    shape = (31, 23, 17)
+    f, mask, pbt, eps = _case(7, shape)
+    want_f, want_w = _oracle(f, eps, 1, pbt, mask, shape)
+    L = C.CDLL(build.LIB_F77)
+    got, work, e = f.copy(), np.zeros_like(f), np.array([eps])
+    ci = lambda v: C.byref(C.c_int(v))  # noqa: E731
+    L.dmdiss3d_(got.ctypes.data_as(D), work.ctypes.data_as(D), e.ctypes.data_as(D), ci(1), (C.c_int * 6)(*pbt),
+                ci(EVEN), ci(ODD), mask.ctypes.data_as(D), C.byref(C.c_double(0.0)), ci(shape[0]), ci(shape[1]),
+                ci(shape[2]), e.ctypes.data_as(D), C.byref(C.c_double(0.0)), ci(0))
+    assert np.array_equal(got, want_f) and np.array_equal(work, want_w)
