@@ -252,6 +252,15 @@ int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_bdy, const i
                  int even, int odd, const double *mask, double mask_off, int nx, int ny, int nz,
                  const double *chr, double ex, int do_ex, void *stream);
 
+/* Linear approach to the boundaries, linbnd3d (src/m_util_r8.f:1957-2252;
+ * include/m_util_r8.h:38-39) on a device array f (chr: device mask when
+ * do_ex != 0); phys_bdy is a host array of 6 (1 physical, 0 AMR);
+ * which_bnd 1 physical, 2 AMR, 3 both. Bit-exact with the Fortran; the
+ * invalid extents the Fortran stops on return an error, and so does
+ * Ny = 1 with Nz > 1, where the Fortran indexes outside f. */
+int pgb_linbnd3d(double *f, const int *phys_bdy, int which_bnd, int Nx, int Ny, int Nz,
+                 const double *chr, double ex, int do_ex, void *stream);
+
 /* Berger-Oliger bookkeeping of the elliptic variables on the device, for
  * an application that keeps them there across coarse steps. Grids are host
  * arrays of device pointers with their AMR levels (level[g]) and point

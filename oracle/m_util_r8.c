@@ -18,9 +18,10 @@
  * extrapolation tests i <= i1s-4*s1. No Fortran compiler is available, so
  * these are pinned by known-answer tests, not by running the reference.
  * dmdiss3d (Kreiss-Oliger dissipation, the evolution kernel next to the
- * elliptic solve) is restated without its excised path (dmdiss3d_ex). The
- * other evolution-only routines (linbnd3d, dmrepop3d1, dmrepop3dc1) are not
- * on the path and abort if reached.
+ * elliptic solve) is restated without its excised path (dmdiss3d_ex), and
+ * linbnd3d (linear approach to the boundaries) fully. The other
+ * evolution-only routines (dmrepop3d1, dmrepop3dc1) are not on the path and
+ * abort if reached.
  *
  * Optional call log: when mur8_log_enabled is set, every call records its
  * kernel id and index arguments so a test can compare the reference's
@@ -760,12 +761,179 @@ void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_
             }
    }
 }
+/* linbnd3d (src/m_util_r8.f:1957-2252): linear approach to the physical
+ * (which_bnd 1), AMR (2) or all (3) boundaries: the points one in from a
+ * selected face become the mean of their two neighbours across it, edge
+ * and corner points of the mean of 4 and 8, in the Fortran's statement
+ * order (later statements read what earlier ones wrote). As in the
+ * Fortran, the corner conditions read (A .and. B) .or. (all .and. X): the
+ * excision test X applies only when all faces are selected. Returns 1 where
+ * the Fortran stops (invalid extents; which_bnd outside 1..3, where its pf
+ * would be undefined; Ny = 1 with Nz > 1, where it indexes outside f). */
+int oracle_linbnd3d(double *f, const int *phys_bdy, int which_bnd, int Nx, int Ny, int Nz, const double *chr,
+                    double ex, int do_ex)
+{
+#define F(i, j, k) f[((i)-1) + (long)Nx * (((j)-1) + (long)Ny * ((k)-1))]
+#define X(i, j, k) (chr[((i)-1) + (long)Nx * (((j)-1) + (long)Ny * ((k)-1))] != ex)
+#define PB(n) (phys_bdy[(n)-1] == pf || all)
+   int i, j, k, pf = -1, all = 0;
+   const int ne = do_ex == 0;
+   /* the Fortran stops on the first three; with Ny = 1 and Nz > 1 its corner
+    * statements index j = Ny-2 < 1, outside f: refused here */
+   if (Nx < 3 || Ny == 2 || Nz == 2 || (Ny == 1 && Nz > 1)) return 1;
+   if (which_bnd == 3)
+      all = 1;   /* the Fortran leaves pf undefined here; -1 matches no face code (0 or 1) */
+   else if (which_bnd == 1)
+      pf = 1;
+   else if (which_bnd == 2)
+      pf = 0;
+   else
+      return 1;
+   const int jlo = Ny < 2 ? Ny : 2, jhi = 1 > Ny - 1 ? 1 : Ny - 1;
+   const int klo = Nz < 2 ? Nz : 2, khi = 1 > Nz - 1 ? 1 : Nz - 1;
+
+   if (PB(1)) {
+      for (j = jlo; j <= jhi; j++)
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(3, j, k) && X(1, j, k))) F(2, j, k) = 0.5 * (F(3, j, k) + F(1, j, k));
+      if (Ny > 1 && PB(3))
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(3, 3, k) && X(3, 1, k) && X(1, 3, k) && X(1, 1, k)))
+               F(2, 2, k) = 0.25 * (F(3, 3, k) + F(1, 3, k) + F(3, 1, k) + F(1, 1, k));
+      if (Ny > 1 && PB(4))
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(3, Ny - 2, k) && X(1, Ny - 2, k) && X(3, Ny, k) && X(1, Ny, k)))
+               F(2, Ny - 1, k) = 0.25 * (F(3, Ny - 2, k) + F(1, Ny - 2, k) + F(3, Ny, k) + F(1, Ny, k));
+      if (Nz > 1 && PB(5))
+         for (j = 2; j <= Ny - 1; j++)
+            if (ne || (X(3, j, 3) && X(1, j, 3) && X(3, j, 1) && X(1, j, 1)))
+               F(2, j, 2) = 0.25 * (F(3, j, 3) + F(1, j, 3) + F(3, j, 1) + F(1, j, 1));
+      if (Nz > 1 && PB(6))
+         for (j = 2; j <= Ny - 1; j++)
+            if (ne || (X(3, j, Nz - 2) && X(1, j, Nz - 2) && X(3, j, Nz) && X(1, j, Nz)))
+               F(2, j, Nz - 1) = 0.25 * (F(3, j, Nz - 2) + F(1, j, Nz - 2) + F(3, j, Nz) + F(1, j, Nz));
+      if (Nz > 1 && ((phys_bdy[2] == pf && phys_bdy[4] == pf) ||
+                     (all && (ne || (X(3, 3, 3) && X(1, 3, 3) && X(3, 1, 3) && X(3, 3, 1) && X(1, 1, 3) &&
+                                     X(1, 3, 1) && X(3, 1, 1) && X(1, 1, 1))))))
+         F(2, 2, 2) = 0.125 * (F(3, 3, 3) + F(1, 3, 3) + F(3, 1, 3) + F(3, 3, 1) + F(1, 1, 3) + F(1, 3, 1) +
+                               F(3, 1, 1) + F(1, 1, 1));
+      if (Nz > 1 && ((phys_bdy[3] == pf && phys_bdy[4] == pf) ||
+                     (all && (ne || (X(3, Ny - 2, 3) && X(1, Ny - 2, 3) && X(3, Ny, 3) && X(3, Ny - 2, 1) &&
+                                     X(1, Ny, 3) && X(1, Ny - 2, 1) && X(3, Ny, 1) && X(1, Ny, 1))))))
+         F(2, Ny - 1, 2) = 0.125 * (F(3, Ny - 2, 3) + F(1, Ny - 2, 3) + F(3, Ny, 3) + F(3, Ny - 2, 1) +
+                                    F(1, Ny, 3) + F(1, Ny - 2, 1) + F(3, Ny, 1) + F(1, Ny, 1));
+      if (Nz > 1 && ((phys_bdy[2] == pf && phys_bdy[5] == pf) ||
+                     (all && (ne || (X(3, 3, Nz - 2) && X(1, 3, Nz - 2) && X(3, 1, Nz - 2) && X(3, 3, Nz) &&
+                                     X(1, 1, Nz - 2) && X(1, 3, Nz) && X(3, 1, Nz) && X(1, 1, Nz))))))
+         F(2, 2, Nz - 1) = 0.125 * (F(3, 3, Nz - 2) + F(1, 3, Nz - 2) + F(3, 1, Nz - 2) + F(3, 3, Nz) +
+                                    F(1, 1, Nz - 2) + F(1, 3, Nz) + F(3, 1, Nz) + F(1, 1, Nz));
+      if (Nz > 1 && ((phys_bdy[3] == pf && phys_bdy[5] == pf) ||
+                     (all && (ne || (X(3, Ny - 2, Nz - 2) && X(1, Ny - 2, Nz - 2) && X(3, Ny, Nz - 2) &&
+                                     X(3, Ny - 2, Nz) && X(1, Ny, Nz - 2) && X(1, Ny - 2, Nz) && X(3, Ny, Nz) &&
+                                     X(1, Ny, Nz))))))
+         F(2, Ny - 1, Nz - 1) = 0.125 * (F(3, Ny - 2, Nz - 2) + F(1, Ny - 2, Nz - 2) + F(3, Ny, Nz - 2) +
+                                         F(3, Ny - 2, Nz) + F(1, Ny, Nz - 2) + F(1, Ny - 2, Nz) + F(3, Ny, Nz) +
+                                         F(1, Ny, Nz));
+   }
+
+   if (PB(2)) {
+      for (j = jlo; j <= jhi; j++)
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(Nx - 2, j, k) && X(Nx, j, k))) F(Nx - 1, j, k) = 0.5 * (F(Nx - 2, j, k) + F(Nx, j, k));
+      if (Ny > 1 && PB(3))
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(Nx - 2, 3, k) && X(Nx, 3, k) && X(Nx - 2, 1, k) && X(Nx, 1, k)))
+               F(Nx - 1, 2, k) = 0.25 * (F(Nx - 2, 3, k) + F(Nx, 3, k) + F(Nx - 2, 1, k) + F(Nx, 1, k));
+      if (Ny > 1 && PB(4))
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(Nx - 2, Ny - 2, k) && X(Nx, Ny - 2, k) && X(Nx - 2, Ny, k) && X(Nx, Ny, k)))
+               F(Nx - 1, Ny - 1, k) =
+                   0.25 * (F(Nx - 2, Ny - 2, k) + F(Nx, Ny - 2, k) + F(Nx - 2, Ny, k) + F(Nx, Ny, k));
+      if (Nz > 1 && PB(5))
+         for (j = 2; j <= Ny - 1; j++)
+            if (ne || (X(Nx - 2, j, 3) && X(Nx, j, 3) && X(Nx - 2, j, 1) && X(Nx, j, 1)))
+               F(Nx - 1, j, 2) = 0.25 * (F(Nx - 2, j, 3) + F(Nx, j, 3) + F(Nx - 2, j, 1) + F(Nx, j, 1));
+      if (Nz > 1 && PB(6))
+         for (j = 2; j <= Ny - 1; j++)
+            if (ne || (X(Nx - 2, j, Nz - 2) && X(Nx, j, Nz - 2) && X(Nx - 2, j, Nz) && X(Nx, j, Nz)))
+               F(Nx - 1, j, Nz - 1) =
+                   0.25 * (F(Nx - 2, j, Nz - 2) + F(Nx, j, Nz - 2) + F(Nx - 2, j, Nz) + F(Nx, j, Nz));
+      if (Nz > 1 && ((phys_bdy[2] == pf && phys_bdy[4] == pf) ||
+                     (all && (ne || (X(Nx - 2, 3, 3) && X(Nx, 3, 3) && X(Nx - 2, 1, 3) && X(Nx - 2, 3, 1) &&
+                                     X(Nx, 1, 3) && X(Nx, 3, 1) && X(Nx - 2, 1, 1) && X(Nx, 1, 1))))))
+         F(Nx - 1, 2, 2) = 0.125 * (F(Nx - 2, 3, 3) + F(Nx, 3, 3) + F(Nx - 2, 1, 3) + F(Nx - 2, 3, 1) +
+                                    F(Nx, 1, 3) + F(Nx, 3, 1) + F(Nx - 2, 1, 1) + F(Nx, 1, 1));
+      if (Nz > 1 && ((phys_bdy[3] == pf && phys_bdy[4] == pf) ||
+                     (all && (ne || (X(Nx - 2, Ny - 2, 3) && X(Nx, Ny - 2, 3) && X(Nx - 2, Ny, 3) &&
+                                     X(Nx - 2, Ny - 2, 1) && X(Nx, Ny, 3) && X(Nx, Ny - 2, 1) &&
+                                     X(Nx - 2, Ny, 1) && X(Nx, Ny, 1))))))
+         F(Nx - 1, Ny - 1, 2) = 0.125 * (F(Nx - 2, Ny - 2, 3) + F(Nx, Ny - 2, 3) + F(Nx - 2, Ny, 3) +
+                                         F(Nx - 2, Ny - 2, 1) + F(Nx, Ny, 3) + F(Nx, Ny - 2, 1) +
+                                         F(Nx - 2, Ny, 1) + F(Nx, Ny, 1));
+      if (Nz > 1 && ((phys_bdy[2] == pf && phys_bdy[5] == pf) ||
+                     (all && (ne || (X(Nx - 2, 3, Nz - 2) && X(Nx, 3, Nz - 2) && X(Nx - 2, 1, Nz - 2) &&
+                                     X(Nx - 2, 3, Nz) && X(Nx, 1, Nz - 2) && X(Nx, 3, Nz) && X(Nx - 2, 1, Nz) &&
+                                     X(Nx, 1, Nz))))))
+         F(Nx - 1, 2, Nz - 1) = 0.125 * (F(Nx - 2, 3, Nz - 2) + F(Nx, 3, Nz - 2) + F(Nx - 2, 1, Nz - 2) +
+                                         F(Nx - 2, 3, Nz) + F(Nx, 1, Nz - 2) + F(Nx, 3, Nz) + F(Nx - 2, 1, Nz) +
+                                         F(Nx, 1, Nz));
+      if (Nz > 1 && ((phys_bdy[3] == pf && phys_bdy[5] == pf) ||
+                     (all && (ne || (X(Nx - 2, Ny - 2, Nz - 2) && X(Nx, Ny, Nz) && X(Nx, Ny - 2, Nz - 2) &&
+                                     X(Nx - 2, Ny, Nz - 2) && X(Nx - 2, Ny - 2, Nz) && X(Nx, Ny, Nz - 2) &&
+                                     X(Nx, Ny - 2, Nz) && X(Nx - 2, Ny, Nz))))))
+         F(Nx - 1, Ny - 1, Nz - 1) = 0.125 * (F(Nx - 2, Ny - 2, Nz - 2) + F(Nx, Ny, Nz) + F(Nx, Ny - 2, Nz - 2) +
+                                              F(Nx - 2, Ny, Nz - 2) + F(Nx - 2, Ny - 2, Nz) + F(Nx, Ny, Nz - 2) +
+                                              F(Nx, Ny - 2, Nz) + F(Nx - 2, Ny, Nz));
+   }
+
+   if (Ny > 1 && PB(3)) {
+      for (i = 3; i <= Nx - 2; i++)
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(i, 3, k) && X(i, 1, k))) F(i, 2, k) = 0.5 * (F(i, 3, k) + F(i, 1, k));
+      if (Nz > 1 && PB(5))
+         for (i = 3; i <= Nx - 2; i++)
+            if (ne || (X(i, 3, 3) && X(i, 1, 3) && X(i, 3, 1) && X(i, 1, 1)))
+               F(i, 2, 2) = 0.25 * (F(i, 3, 3) + F(i, 1, 3) + F(i, 3, 1) + F(i, 1, 1));
+      if (Nz > 1 && PB(6))
+         for (i = 3; i <= Nx - 2; i++)
+            if (ne || (X(i, 3, Nz - 2) && X(i, 1, Nz - 2) && X(i, 3, Nz) && X(i, 1, Nz)))
+               F(i, 2, Nz - 1) = 0.25 * (F(i, 3, Nz - 2) + F(i, 1, Nz - 2) + F(i, 3, Nz) + F(i, 1, Nz));
+   }
+
+   if (Ny > 1 && PB(4)) {
+      for (i = 3; i <= Nx - 2; i++)
+         for (k = klo; k <= khi; k++)
+            if (ne || (X(i, Ny - 2, k) && X(i, Ny, k))) F(i, Ny - 1, k) = 0.5 * (F(i, Ny - 2, k) + F(i, Ny, k));
+      if (Nz > 1 && PB(5))
+         for (i = 3; i <= Nx - 2; i++)
+            if (ne || (X(i, Ny - 2, 3) && X(i, Ny, 3) && X(i, Ny - 2, 1) && X(i, Ny, 1)))
+               F(i, Ny - 1, 2) = 0.25 * (F(i, Ny - 2, 3) + F(i, Ny, 3) + F(i, Ny - 2, 1) + F(i, Ny, 1));
+      if (Nz > 1 && PB(6))
+         for (i = 3; i <= Nx - 2; i++)
+            if (ne || (X(i, Ny - 2, Nz - 2) && X(i, Ny, Nz - 2) && X(i, Ny - 2, Nz) && X(i, Ny, Nz)))
+               F(i, Ny - 1, Nz - 1) =
+                   0.25 * (F(i, Ny - 2, Nz - 2) + F(i, Ny, Nz - 2) + F(i, Ny - 2, Nz) + F(i, Ny, Nz));
+   }
+
+   if (Nz > 1 && PB(5))
+      for (i = 3; i <= Nx - 2; i++)
+         for (j = 3; j <= Ny - 2; j++)
+            if (ne || (X(i, j, 3) && X(i, j, 1))) F(i, j, 2) = 0.5 * (F(i, j, 3) + F(i, j, 1));
+
+   if (Nz > 1 && PB(6))
+      for (i = 3; i <= Nx - 2; i++)
+         for (j = 3; j <= Ny - 2; j++)
+            if (ne || (X(i, j, Nz - 2) && X(i, j, Nz))) F(i, j, Nz - 1) = 0.5 * (F(i, j, Nz - 2) + F(i, j, Nz));
+#undef F
+#undef X
+#undef PB
+   return 0;
+}
+
 void linbnd3d_(double *f, int *phys_bdy, int *which_bnd, int *Nx, int *Ny, int *Nz, double *chr,
                double *ex, int *do_ex)
 {
-   (void)f; (void)phys_bdy; (void)which_bnd; (void)Nx; (void)Ny; (void)Nz; (void)chr; (void)ex;
-   (void)do_ex;
-   not_on_path("linbnd3d");
+   if (oracle_linbnd3d(f, phys_bdy, *which_bnd, *Nx, *Ny, *Nz, chr, *ex, *do_ex)) not_on_path("linbnd3d (invalid)");
 }
 void dmrepop3d1_(double *f, double *chr, double *ex, int *io, int *nx, int *ny, int *nz)
 {

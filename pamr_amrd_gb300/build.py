@@ -20,7 +20,7 @@ LIB_F77 = os.path.join(os.path.dirname(LIB), "libpamr_gb300_f77.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"], "pgb_noalloc.cu": ["-fmad=false"],
-              "pgb_mutil_ex.cu": ["-fmad=false"], "pgb_bo.cu": ["-fmad=false"], "pgb_diss.cu": ["-fmad=false"], "pgb_kernels32.cu": [],
+              "pgb_mutil_ex.cu": ["-fmad=false"], "pgb_bo.cu": ["-fmad=false"], "pgb_diss.cu": ["-fmad=false"], "pgb_linbnd.cu": ["-fmad=false"], "pgb_kernels32.cu": [],
               "pgb_net.cu": []}
 C_SOURCES = ["pgb_plan.c", "pgb_solver.c"]
 

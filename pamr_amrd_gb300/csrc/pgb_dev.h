@@ -101,6 +101,7 @@ unsigned long long pgb_dev_launches_ex(void);
 unsigned long long pgb_dev_launches_net(void);   /* pgb_net.cu */
 unsigned long long pgb_dev_launches_bo(void);    /* pgb_bo.cu */
 unsigned long long pgb_dev_launches_diss(void);  /* pgb_diss.cu */
+unsigned long long pgb_dev_launches_lb(void);    /* pgb_linbnd.cu */
 
 /* mixed-precision path (pgb_kernels32.cu) */
 const char *pgb_dev_error32(void);

@@ -1,7 +1,7 @@
 /*
  * Fortran-ABI drop-in for the m_util_r8 routines an application may call
  * (include/m_util_r8.h:33-66): dmcopy3d_, dmhwr3d_, dmfwr3d_,
- * dminterp3d_ and dmdiss3d_ with every argument by pointer, on HOST arrays, as the
+ * dminterp3d_, dmdiss3d_ and linbnd3d_ with every argument by pointer, on HOST arrays, as the
  * reference's Fortran takes them. Built as its own library
  * (libpamr_gb300_f77.so) so that an application links it in place of the
  * reference's m_util_r8 object without any source change. Each call copies
@@ -137,4 +137,22 @@ void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_
    if (!rc) rc = back(f, df, n);
    if (!rc) rc = back(work, dw, n);
    report("dmdiss3d", rc);
+}
+
+/* linear approach to the boundaries (src/m_util_r8.f:1957-2252): f (and chr
+ * when excising) to the device, pgb_linbnd3d, f back */
+void linbnd3d_(double *f, int *phys_bdy, int *which_bnd, int *Nx, int *Ny, int *Nz, double *chr, double *ex,
+               int *do_ex)
+{
+   size_t n = (size_t)*Nx * *Ny * *Nz;
+   double *df = dev(0, f, n), *dc = 0;
+   int rc;
+   if (*do_ex != 0) dc = dev(2, chr, n);
+   if (!df || (*do_ex != 0 && !dc)) {
+      fprintf(stderr, "linbnd3d: device buffers unavailable\n");
+      return;
+   }
+   rc = pgb_linbnd3d(df, phys_bdy, *which_bnd, *Nx, *Ny, *Nz, dc, *ex, *do_ex, 0);
+   if (!rc) rc = back(f, df, n);
+   report("linbnd3d", rc);
 }

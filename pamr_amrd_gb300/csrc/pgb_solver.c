@@ -960,7 +960,8 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
 long long pgb_launch_count(void)
 {
    return (long long)(pgb_dev_launches() + pgb_dev_launches32() + pgb_dev_launches_ex() +
-                      pgb_dev_launches_net() + pgb_dev_launches_bo() + pgb_dev_launches_diss()) - g_captured + g_graph_replayed;
+                      pgb_dev_launches_net() + pgb_dev_launches_bo() + pgb_dev_launches_diss() +
+                      pgb_dev_launches_lb()) - g_captured + g_graph_replayed;
 }
 
 int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double *bytes_per_sweep)

@@ -36,5 +36,5 @@ def test_fortran_abi_dropin_exports_m_util_r8_symbols():
     (Fortran ABI, trailing underscore) so an application relinks unchanged"""
     build.build()
     L = ctypes.CDLL(build.LIB_F77)
-    for name in ("dmcopy3d_", "dmhwr3d_", "dmfwr3d_", "dminterp3d_", "dmdiss3d_"):
+    for name in ("dmcopy3d_", "dmhwr3d_", "dmfwr3d_", "dminterp3d_", "dmdiss3d_", "linbnd3d_"):
         assert hasattr(L, name), name
