@@ -116,6 +116,16 @@ void *pgb_stream(pgb_solver *s);
  * (as the reference counts them), and device time in ms. */
 int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms);
 
+/* Checkpoint and restart of the device hierarchy's elliptic data (no
+ * counterpart format in the reference, whose checkpoints are SDF files of
+ * every grid function written through bbhutil, src/pamr.c:1908-1978,
+ * 2042-2075): pgb_checkpoint_save writes, per input grid, its level, shape,
+ * bounding box, u and source to `path`; pgb_checkpoint_load restores them
+ * into a solver created on the same hierarchy (checked bit for bit) and
+ * fails without changing it when the file does not match. */
+int pgb_checkpoint_save(pgb_solver *s, const char *path);
+int pgb_checkpoint_load(pgb_solver *s, const char *path);
+
 /* Kernel launches this library has issued in the process (all solvers). */
 long long pgb_launch_count(void);
 

@@ -994,6 +994,94 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    return 0;
 }
 
+/* ------------------------------------------------------------ checkpoint -- */
+/* File layout (little-endian as written by the host): "PGBCKPT1", int32
+ * version, dim, pde, ngrids; per input grid int32 level, shape[3], double
+ * bbox[6], then u and the source (float64, x fastest). */
+#define CKPT_MAGIC "PGBCKPT1"
+#define CKPT_VERSION 1
+
+int pgb_checkpoint_save(pgb_solver *s, const char *path)
+{
+   FILE *f;
+   int g, rc = 0;
+   const int hdr[4] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids};
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (!(f = fopen(path, "wb"))) return fail(5, "checkpoint: cannot open %s for writing", path);
+   if (fwrite(CKPT_MAGIC, 1, 8, f) != 8 || fwrite(hdr, sizeof(int), 4, f) != 4) rc = fail(5, "checkpoint: write failed");
+   for (g = 0; g < s->h.ngrids && !rc; g++) {
+      const pgb_hbox *b = &s->h.boxes[s->h.grid_box[g]];
+      const pgb_dbox *db = &s->hbox[s->h.grid_box[g]];
+      const size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+      const int meta[4] = {b->level, b->shape[0], b->shape[1], b->shape[2]};
+      double *buf = (double *)malloc(sizeof(double) * n);
+      int k;
+      if (!buf) {
+         rc = fail(10, "checkpoint: host buffer");
+         break;
+      }
+      if (fwrite(meta, sizeof(int), 4, f) != 4 || fwrite(b->bbox, sizeof(double), 6, f) != 6)
+         rc = fail(5, "checkpoint: write failed");
+      for (k = 0; k < 2 && !rc; k++) {
+         if (cudaMemcpyAsync(buf, db->f[k ? PGB_F_SRC : PGB_F_U], sizeof(double) * n, cudaMemcpyDeviceToHost,
+                             s->stream) != cudaSuccess ||
+             cudaStreamSynchronize(s->stream) != cudaSuccess)
+            rc = fail(11, "checkpoint: device read failed");
+         else if (fwrite(buf, sizeof(double), n, f) != n)
+            rc = fail(5, "checkpoint: write failed");
+      }
+      free(buf);
+   }
+   if (fclose(f) && !rc) rc = fail(5, "checkpoint: close failed");
+   return rc;
+}
+
+int pgb_checkpoint_load(pgb_solver *s, const char *path)
+{
+   FILE *f;
+   char magic[8];
+   int hdr[4], g, rc = 0, ng = s->h.ngrids;
+   double **buf;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (!(f = fopen(path, "rb"))) return fail(5, "checkpoint: cannot open %s", path);
+   if (fread(magic, 1, 8, f) != 8 || memcmp(magic, CKPT_MAGIC, 8) || fread(hdr, sizeof(int), 4, f) != 4) {
+      fclose(f);
+      return fail(6, "checkpoint: %s is not a checkpoint", path);
+   }
+   if (hdr[0] != CKPT_VERSION || hdr[1] != s->h.dim || hdr[2] != s->h.pde || hdr[3] != ng) {
+      fclose(f);
+      return fail(6, "checkpoint: version, dimension, equation or grid count differ from the solver's");
+   }
+   /* the whole file is read and checked before the solver's data changes */
+   buf = (double **)calloc(2 * (size_t)ng, sizeof(double *));
+   for (g = 0; g < ng && !rc; g++) {
+      const pgb_hbox *b = &s->h.boxes[s->h.grid_box[g]];
+      const size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+      int meta[4];
+      double bb[6];
+      if (fread(meta, sizeof(int), 4, f) != 4 || fread(bb, sizeof(double), 6, f) != 6) {
+         rc = fail(6, "checkpoint: truncated");
+         break;
+      }
+      if (meta[0] != b->level || meta[1] != b->shape[0] || meta[2] != b->shape[1] || meta[3] != b->shape[2] ||
+          memcmp(bb, b->bbox, sizeof(bb))) {
+         rc = fail(6, "checkpoint: grid %d differs from the solver's hierarchy", g);
+         break;
+      }
+      buf[2 * g] = (double *)malloc(sizeof(double) * n);
+      buf[2 * g + 1] = (double *)malloc(sizeof(double) * n);
+      if (!buf[2 * g] || !buf[2 * g + 1])
+         rc = fail(10, "checkpoint: host buffer");
+      else if (fread(buf[2 * g], sizeof(double), n, f) != n || fread(buf[2 * g + 1], sizeof(double), n, f) != n)
+         rc = fail(6, "checkpoint: truncated");
+   }
+   fclose(f);
+   for (g = 0; g < ng && !rc; g++) rc = pgb_set_grid(s, g, buf[2 * g], buf[2 * g + 1]);
+   for (g = 0; g < 2 * ng; g++) free(buf[g]);
+   free(buf);
+   return rc;
+}
+
 /* ---------------------------------------------------------------- trace -- */
 int pgb_trace_enable(pgb_solver *s, int capacity)
 {

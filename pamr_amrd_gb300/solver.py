@@ -189,6 +189,16 @@ class Solver:
         _check(lib().pgb_time_relax(self.h, L, reps, C.byref(ms), C.byref(by)))
         return ms.value, by.value
 
+    def checkpoint_save(self, path: str):
+        L = lib()
+        L.pgb_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]
+        _check(L.pgb_checkpoint_save(self.h, path.encode()))
+
+    def checkpoint_load(self, path: str):
+        L = lib()
+        L.pgb_checkpoint_load.argtypes = [C.c_void_p, C.c_char_p]
+        _check(L.pgb_checkpoint_load(self.h, path.encode()))
+
     def set_inputs_device(self, u_ptrs, src_ptrs):
         for i, (a, b) in enumerate(zip(u_ptrs, src_ptrs)):
             _check(lib().pgb_set_grid_device(self.h, i, a, b))
