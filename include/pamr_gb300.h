@@ -116,6 +116,14 @@ void *pgb_stream(pgb_solver *s);
  * (as the reference counts them), and device time in ms. */
 int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms);
 
+/* Interpolation of u on the AMR hierarchy from AMR level lc to lc+1:
+ * amr_bdy_width = 0 replaces PAMR_interp(lc, tl, PAMR_AMRH) (src/pamr.c:623),
+ * the whole overlap; amr_bdy_width > 0 replaces PAMR_AMR_bdy_interp(lc, tl,
+ * width) (src/pamr.c:645), the band of that width along the fine grids'
+ * AMR boundaries. order 2 or 4 (the variable's amr_interp order); same
+ * transfer lists and dminterp3d arithmetic as the reference, bit-exact. */
+int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order);
+
 /* Checkpoint and restart of the device hierarchy's elliptic data (no
  * counterpart format in the reference, whose checkpoints are SDF files of
  * every grid function written through bbhutil, src/pamr.c:1908-1978,

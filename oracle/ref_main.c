@@ -9,14 +9,16 @@
  * the C restatement of the Fortran kernels (oracle/m_util_r8.c). Output goes
  * to oracle/_ref/ only.
  *
- * usage: ref_mg <param file> <case.bin> <out.bin> [log_ops]
+ * usage: ref_mg <param file> <case.bin> <out.bin> [log_ops [interp:lc:width]]
  *
  * The parameter file is an AMRD run-time file read by the reference's
  * init_context() (amrd/io.c:36). case.bin carries the AMR hierarchy and the
  * initial u and source on every AMR grid. The driver then
  *   1. composes the hierarchy with PAMR_compose_hierarchy (src/pamr.c:259),
  *   2. fills u and the source on time level 1,
- *   3. calls solve_elliptics(1,1,0) (amrd/mg.c:20),
+ *   3. calls solve_elliptics(1,1,0) (amrd/mg.c:20), or with interp:lc:width
+ *      one PAMR_interp (width 0) or PAMR_AMR_bdy_interp (width > 0) of u
+ *      from AMR level lc to lc+1 instead,
  * while the application hooks (pattern of examples/nbs/nbs.c:301-351) log
  * every relax/residual norm, the MG hierarchy, the cmask arrays, and (with
  * log_ops) every m_util_r8 call with its index arguments.
@@ -321,8 +323,13 @@ int main(int argc, char **argv)
    int i, num, *lev;
    double *bbox;
    int gu_amr, gs_amr;
+   int amr_lc = 0, amr_width = -1;
    if (argc < 4) {
-      fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops]\n", argv[0]);
+      fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops [interp:lc:width]]\n", argv[0]);
+      return 2;
+   }
+   if (argc > 5 && sscanf(argv[5], "interp:%d:%d", &amr_lc, &amr_width) != 2) {
+      fprintf(stderr, "ref_mg: bad interpolation mode %s\n", argv[5]);
       return 2;
    }
    read_case(argv[2]);
@@ -368,7 +375,18 @@ int main(int argc, char **argv)
    amr_data(0, gu_amr, gs_amr);
 
    mur8_log_enabled = (argc > 4 && atoi(argv[4]));
-   solve_elliptics(1, 1, 0);
+   if (amr_width >= 0) {
+      /* instead of the solve: one AMR-hierarchy interpolation of u (time
+       * level 1) from level amr_lc to amr_lc+1, over the whole overlap
+       * (PAMR_interp, src/pamr.c:623) or a boundary band of the fine grids
+       * (PAMR_AMR_bdy_interp, src/pamr.c:645) */
+      int ok = amr_width == 0 ? PAMR_interp(amr_lc, 1, PAMR_AMRH) : PAMR_AMR_bdy_interp(amr_lc, 1, amr_width);
+      if (!ok) {
+         fprintf(stderr, "ref_mg: AMR interpolation failed\n");
+         return 3;
+      }
+   } else
+      solve_elliptics(1, 1, 0);
    mur8_log_enabled = 0;
 
    amr_data(1, gu_amr, gs_amr);

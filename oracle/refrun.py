@@ -31,7 +31,10 @@ def available() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def param_file(case) -> str:
+def param_file(case, amr_interp_order: int = 0) -> str:
+    """AMRD run-time parameters of ``case``; amr_interp_order 2 or 4 also
+    lists u in amr_interp2/amr_interp4 (its AMR interpolation order,
+    amrd/io.c:771-772)"""
     p = case.params
     dim = case.dim
     lines = [
@@ -83,6 +86,8 @@ def param_file(case) -> str:
                   "mg_fw_restr := [ " + " ".join(f'"{n}"' for n in fw) + " ]"]
     if p.interp_order != 2:
         raise ValueError("AMRD's coarse-grid correction interpolates with mg_interp2 only")
+    if amr_interp_order:
+        lines += [f"num_amr_interp{amr_interp_order} := 1", f'amr_interp{amr_interp_order} := [ "u" ]']
     return "\n".join(lines) + "\n"
 
 
@@ -106,9 +111,13 @@ def _records(buf: bytes):
 
 
 def run_reference(case, log_ops: bool = False, workdir: str | None = None,
-                  timeout: float = 3600) -> dict:
+                  timeout: float = 3600, amr_interp=None) -> dict:
     """Runs ref_mg on ``case``; returns iterations, hook log, MG hierarchy,
-    cmask arrays, final u per input grid and (optionally) the m_util_r8 op log."""
+    cmask arrays, final u per input grid and (optionally) the m_util_r8 op log.
+    With amr_interp = (lc, width, order) the solve is replaced by one
+    PAMR_interp (width 0) or PAMR_AMR_bdy_interp (width > 0) of u from AMR
+    level lc to lc+1 with interpolation order 2 or 4; "u" then holds the
+    AMR grids after it."""
     if not available():
         raise RuntimeError("oracle/_ref/ref_mg is not built (oracle/build_ref.sh)")
     with tempfile.TemporaryDirectory(dir=workdir) as td:
@@ -116,10 +125,11 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         cf = os.path.join(td, "case.bin")
         of = os.path.join(td, "out.bin")
         with open(pf, "w") as f:
-            f.write(param_file(case))
+            f.write(param_file(case, amr_interp[2] if amr_interp else 0))
         with open(cf, "wb") as f:
             f.write(case_bytes(case))
-        r = subprocess.run([REF_BIN, pf, cf, of] + (["1"] if log_ops else []),
+        extra = ["1" if log_ops else "0"] + ([f"interp:{amr_interp[0]}:{amr_interp[1]}"] if amr_interp else [])
+        r = subprocess.run([REF_BIN, pf, cf, of] + extra,
                            capture_output=True, text=True, timeout=timeout, cwd=td)
         if r.returncode != 0:
             raise RuntimeError(f"ref_mg failed ({r.returncode}): {r.stdout[-2000:]} {r.stderr[-2000:]}")

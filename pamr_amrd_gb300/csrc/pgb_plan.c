@@ -192,14 +192,38 @@ static void build_owned(const pgb_hier *h, const pgb_hlevel *lev, int interior, 
       }
 }
 
-/* build_complete_gsl src/transfer.c:465-504 (AMR_bdy_only = 0) */
-static void build_complete(const pgb_hier *h, const pgb_hlevel *lev, int comm_mode, segv *out)
+/* build_complete_gsl src/transfer.c:465-504: every grid of the level, or
+ * with AMR_bdy_only > 0 the band of that width along the grids' AMR
+ * boundaries: the union minus each grid shrunk by the width away from the
+ * physical boundary, subtracted grid by grid as gsl_subtract
+ * (src/transfer.c:287-314) orders the pieces */
+static void build_complete(const pgb_hier *h, const pgb_hlevel *lev, int comm_mode, int amr_bdy_only, segv *out)
 {
-   int b;
+   int b, c;
    seg s;
+   segv all = {0, 0, 0}, inner = {0, 0, 0};
    for (b = 0; b < lev->nbox; b++)
-      if (box_in_comm(h, lev->box[b], comm_mode) && seg_of_box(h, lev->box[b], 0, 0, &s))
-         sv_push(out, &s);
+      if (box_in_comm(h, lev->box[b], comm_mode) && seg_of_box(h, lev->box[b], 0, 0, &s)) {
+         sv_push(&all, &s);
+         if (amr_bdy_only > 0 && seg_of_box(h, lev->box[b], 0, amr_bdy_only, &s)) sv_push(&inner, &s);
+      }
+   if (amr_bdy_only <= 0) {
+      for (c = 0; c < all.n; c++) sv_push(out, &all.v[c]);
+   } else {
+      segv cur = all;
+      all.v = 0;
+      all.n = all.cap = 0;
+      for (b = 0; b < inner.n; b++) {
+         segv next = {0, 0, 0};
+         for (c = 0; c < cur.n; c++) gs_subtract(h, &cur.v[c], &inner.v[b], &next);
+         sv_free(&cur);
+         cur = next;
+      }
+      for (c = 0; c < cur.n; c++) sv_push(out, &cur.v[c]);
+      sv_free(&cur);
+   }
+   sv_free(&all);
+   sv_free(&inner);
 }
 
 /* gs_and src/transfer.c:325-356 */
@@ -337,8 +361,18 @@ static void make_batches(pgb_plan *p, const rect *r, const long *pts)
 enum { COMM_SYNC, COMM_INJECT, COMM_INTERP };
 
 /* communicate() src/pamr.c:533-593 + local_transfer, as an op plan */
+static void plan_comm_bdy(pgb_hier *h, int kind, int l1, int l2, int interior, int extend, int comm_mode,
+                          int amr_bdy_only, const int *field_ops, pgb_plan *out);
+
 static void plan_comm(pgb_hier *h, int kind, int l1, int l2, int interior, int extend,
                       int comm_mode, const int *field_ops, pgb_plan *out)
+{
+   plan_comm_bdy(h, kind, l1, l2, interior, extend, comm_mode, 0, field_ops, out);
+}
+
+/* communicate (src/pamr.c:533-593) as a flat op list, for one transfer kind */
+static void plan_comm_bdy(pgb_hier *h, int kind, int l1, int l2, int interior, int extend, int comm_mode,
+                          int amr_bdy_only, const int *field_ops, pgb_plan *out)
 {
    segv src = {0, 0, 0}, dst = {0, 0, 0}, ps = {0, 0, 0}, pd = {0, 0, 0};
    opv ops = {0, 0, 0, 0};
@@ -352,7 +386,7 @@ static void plan_comm(pgb_hier *h, int kind, int l1, int l2, int interior, int e
    else if (kind == COMM_INJECT) ops.sz = sizeof(pgb_restrict_op);
    else ops.sz = sizeof(pgb_interp_op);
    build_owned(h, &h->lev[l1], interior, extend, comm_mode, &src);
-   build_complete(h, &h->lev[l2], comm_mode, &dst);
+   build_complete(h, &h->lev[l2], comm_mode, amr_bdy_only, &dst);
    build_pairs(h, &src, &dst, &ps, &pd);
    rects = (rect *)malloc(sizeof(rect) * (size_t)(ps.n + 1));
    pts = (long *)malloc(sizeof(long) * (size_t)(ps.n + 1));
@@ -802,6 +836,38 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    }
    if (h->err[0]) return 2;
    return 0;
+}
+
+/* MG level of AMR level L (the L-th level kept in the AMR hierarchy), 0 if none */
+static int amr_level_to_mg(const pgb_hier *h, int L)
+{
+   int l, k = 0;
+   for (l = 1; l <= h->nlev; l++)
+      if (h->lev[l].in_amrh && ++k == L) return l;
+   return 0;
+}
+
+int pgb_plan_amr_interp(pgb_hier *h, int lc, int amr_bdy_width, int order, pgb_plan *out)
+{
+   int ops[PGB_NF], f;
+   const int mc = amr_level_to_mg(h, lc), mf = amr_level_to_mg(h, lc + 1);
+   memset(out, 0, sizeof(*out));
+   if (!mc || !mf) {
+      snprintf(h->err, sizeof(h->err), "AMR levels %d and %d are not both in the hierarchy", lc, lc + 1);
+      return 1;
+   }
+   for (f = 0; f < PGB_NF; f++) ops[f] = order;
+   h->err[0] = 0;
+   plan_comm_bdy(h, COMM_INTERP, mc, mf, 0, 1, 0, amr_bdy_width, ops, out);
+   return h->err[0] ? 2 : 0;
+}
+
+void pgb_plan_release(pgb_plan *p)
+{
+   free(p->batch_start);
+   free(p->batch_maxpts);
+   free(p->h_ops);
+   memset(p, 0, sizeof(*p));
 }
 
 static void plan_free(pgb_plan *p)

@@ -73,6 +73,11 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
                    int ngrids, const int *grid_level, const double *grid_bbox,
                    const pgb_hparams *prm);
 void pgb_hier_free(pgb_hier *h);
+/* PAMR_interp / PAMR_AMR_bdy_interp (src/pamr.c:623-661) from AMR level lc
+ * to lc+1 as an interpolation op list of the given order (2 or 4); the
+ * caller releases it with pgb_plan_release (host side) */
+int pgb_plan_amr_interp(pgb_hier *h, int lc, int amr_bdy_width, int order, pgb_plan *out);
+void pgb_plan_release(pgb_plan *p);
 
 #ifdef __cplusplus
 }

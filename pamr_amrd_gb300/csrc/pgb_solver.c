@@ -994,6 +994,30 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    return 0;
 }
 
+/* ------------------------------------------------- AMR-hierarchy transfers -- */
+int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order)
+{
+   pgb_plan p;
+   int rc;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (order != 2 && order != 4) return fail(3, "interpolation order must be 2 or 4");
+   if (amr_bdy_width < 0) return fail(3, "AMR boundary width must be >= 0");
+   if ((rc = pgb_plan_amr_interp(&s->h, lc, amr_bdy_width, order, &p)) != 0) {
+      pgb_plan_release(&p);
+      return fail(3, "%s", s->h.err);
+   }
+   rc = upload_plan(&p, sizeof(pgb_interp_op));
+   if (!rc && p.nops) {
+      if (pgb_k_interp(s->dbox, &p, PGB_F_U, s->h.dim, s->stream) ||
+          cudaStreamSynchronize(s->stream) != cudaSuccess)
+         rc = fail(11, "AMR interpolation failed");
+   }
+   free_plan_dev(&p);
+   pgb_plan_release(&p);
+   s->prepared = 0;   /* u changed */
+   return rc;
+}
+
 /* ------------------------------------------------------------ checkpoint -- */
 /* File layout (little-endian as written by the host): "PGBCKPT1", int32
  * version, dim, pde, ngrids; per input grid int32 level, shape[3], double

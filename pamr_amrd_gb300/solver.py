@@ -189,6 +189,10 @@ class Solver:
         _check(lib().pgb_time_relax(self.h, L, reps, C.byref(ms), C.byref(by)))
         return ms.value, by.value
 
+    def amr_interp(self, lc: int, amr_bdy_width: int = 0, order: int = 2):
+        """PAMR_interp (width 0) / PAMR_AMR_bdy_interp of u from AMR level lc to lc+1"""
+        _check(lib().pgb_amr_interp(self.h, lc, amr_bdy_width, order))
+
     def checkpoint_save(self, path: str):
         L = lib()
         L.pgb_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]

@@ -2,8 +2,10 @@
 own multigrid solve (oracle/_ref/ref_mg, compiled from the reference's C
 sources by oracle/build_ref.sh) on small seeded cases.
 
-Each fixture stores the case (grids, parameters, initial u and source) and
-what the reference produced: V-cycle count, every relax/residual/L_op hook
+The amr_interp_* fixtures store a case's grids, the seed of its random u,
+the transfer (AMR level, boundary width, order) and the points the
+reference's PAMR_interp / PAMR_AMR_bdy_interp changed, with their values. The others store the case (grids,
+parameters, initial u and source) and what the reference's solve produced: V-cycle count, every relax/residual/L_op hook
 call with its norm, the MG hierarchy, the cmask arrays, the final u on every
 grid and the m_util_r8 call log of the whole solve.
 
@@ -38,6 +40,42 @@ def cases():
         W.lapse2d_bo(17, seed=0, levels=3),
         W.lapse2d_bo(17, seed=1, levels=3, step=100),
     ]
+
+
+def interp_cases():
+    """(case with seeded random u, (lc, AMR boundary width, order)) for the
+    AMR-hierarchy interpolation fixtures"""
+    out = []
+    for make, specs in (
+            (lambda: W.poisson2d_uneven(seed=1, n=33, levels=3, min_boxes=2, max_boxes=4, min_side=5,
+                                        max_side=17), [(1, 0, 2), (1, 2, 4), (2, 0, 4), (2, 1, 2)]),
+            (lambda: W.poisson2d_uneven(seed=2, n=65, levels=4, min_boxes=3, max_boxes=8, min_side=9,
+                                        max_side=33), [(2, 0, 4), (3, 2, 2), (3, 3, 4)]),
+            (lambda: W.conformal3d(17, 9, seed=0), [(1, 0, 2), (1, 1, 4), (2, 2, 4)])):
+        for spec in specs:
+            c = make()
+            seed = len(out) + 11
+            c.u0 = interp_u0(c, seed)
+            out.append((c, spec, seed))
+    return out
+
+
+def interp_u0(case, seed):
+    """the seeded random u the interpolation fixtures start from"""
+    rng = np.random.default_rng(seed)
+    return [rng.standard_normal(g.size) for g in case.grids]
+
+
+def save_interp(case, spec, seed, u_after, path):
+    """the case's grids, the seed of u, the transfer, and the points the
+    reference's interpolation changed (index into the concatenated grids, value)"""
+    grids = np.array([[g.level] + list(g.shape) + list(g.bbox) + [0.0] * (6 - len(g.bbox))
+                      for g in case.grids])
+    before, after = np.concatenate(case.u0), np.concatenate(u_after)
+    idx = np.nonzero(after != before)[0].astype(np.int32)
+    np.savez_compressed(path, name=np.array(case.name), pde=case.pde, dim=case.dim,
+                        base_shape=np.array(case.base_shape), base_bbox=np.array(case.base_bbox),
+                        grids=grids, seed=seed, spec=np.array(spec), idx=idx, val=after[idx])
 
 
 def save(case, ref, path):
@@ -80,6 +118,15 @@ def main():
         save(c, ref, path)
         print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
               f"{len(ref['ops'])} m_util_r8 calls, {os.path.getsize(path) // 1024} KiB")
+    for c, spec, seed in interp_cases():
+        lc, w, o = spec
+        path = os.path.join(HERE, f"amr_interp_{c.name}_L{lc}_w{w}_o{o}.npz")
+        if os.path.exists(path) and "--all" not in sys.argv:
+            continue
+        ref = refrun.run_reference(c, amr_interp=spec)
+        save_interp(c, spec, seed, ref["u"], path)
+        changed = sum(int(np.sum(a != b)) for a, b in zip(ref["u"], c.u0))
+        print(f"{os.path.basename(path)}: {changed} points interpolated, {os.path.getsize(path) // 1024} KiB")
 
 
 if __name__ == "__main__":

@@ -14,7 +14,36 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def files():
-    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """the solve fixtures"""
+    return sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(f).startswith("amr_interp_"))
+
+
+def interp_files():
+    """the AMR-hierarchy interpolation fixtures"""
+    return sorted(glob.glob(os.path.join(GOLDEN, "amr_interp_*.npz")))
+
+
+def load_interp(path: str):
+    """(case with the fixture's seeded random u and zero source, (lc, width,
+    order), u the reference's PAMR_interp / PAMR_AMR_bdy_interp left on every
+    grid)"""
+    z = np.load(path)
+    dim = int(z["dim"])
+    grids = []
+    for row in z["grids"]:
+        lev, s0, s1, s2 = (int(v) for v in row[:4])
+        grids.append(W.Grid(lev, tuple(float(v) for v in row[4:4 + 2 * dim]), (s0, s1, s2)))
+    rng = np.random.default_rng(int(z["seed"]))
+    u0 = [rng.standard_normal(g.size) for g in grids]
+    case = W.Case(str(z["name"]), int(z["pde"]), dim, tuple(int(v) for v in z["base_shape"]),
+                  tuple(float(v) for v in z["base_bbox"]), grids, u0, [np.zeros(g.size) for g in grids],
+                  W.MGParams(min_cwidth=9 if int(z["pde"]) == W.CONFORMAL else 3))
+    after = np.concatenate(u0)
+    after[z["idx"]] = z["val"]
+    offs = np.cumsum([0] + [g.size for g in grids])
+    u = [after[offs[i]:offs[i + 1]].copy() for i in range(len(grids))]
+    return case, tuple(int(v) for v in z["spec"]), u
 
 
 def load(path: str):
