@@ -306,7 +306,7 @@ int pgb_set_mg_brs_vars(int L1, int L2, int ngrids, const int *level, double *co
  * (16/32/64/64/64/64 channels, levels halving down to (n-1)/32 points a
  * side, two 3x3x3 convolutions per encoder level, one per decoder level,
  * additive skips, leaky ReLU) from a source rho on an n^3 grid (points 0..n-2
- * seen by the net; n-1 a multiple of 32, n >= 65) to a guess of u, zero on
+ * seen by the net; n-1 a multiple of 32, 65 <= n <= 513) to a guess of u, zero on
  * the grid boundary. Forward and backward-data convolutions of the inner
  * sixteen layers run on the tensor cores (BF16, FP32
  * accumulation); weight gradients and the 1-channel first and last layers

@@ -325,12 +325,268 @@ static int launch_conv(const void *in, void *out, const void *wimg, const float 
    return check_net("conv_tc") ? 11 : 0;
 }
 
+/* ------------------------------------- tensor-core 3x3x3 conv, z-marching -- */
+/* The same convolution for 16/32-channel layers, persistent and pipelined.
+ * Tiles are 128 consecutive padded voxels of one plane (tile j of plane z
+ * starts at p0 + z plane + 128 j; the last tile of a plane is cut at the
+ * plane's end). A work unit is one tile column j over a chunk of planes;
+ * the CTA marches it in z. The operands of one input plane (three runs of
+ * 130 voxels per channel block, y-taps -1..1) are one pipeline stage,
+ * bulk-copied once and used by the three output planes that read it
+ * (z-taps), so each plane's runs cross L2 -> shared memory once per unit
+ * instead of three times. Roles: warp 0 lane 0 streams stages into a
+ * ring of NST stages (full/empty mbarriers); warp 1 lane 0 issues the 27 x CIN/16
+ * MMAs of a tile into one of two TMEM accumulators (commits free the
+ * input stage the next tile no longer reads, and hand the accumulator to
+ * the epilogue); warps 2-5 read an accumulator (tcgen05.ld, one voxel per
+ * thread), add the bias, apply the activation, zero padding voxels, store
+ * BF16, and hand the accumulator back. The layer's weights stay in shared
+ * memory for the whole kernel. Every wait is bounded; on a timeout the
+ * roles stop, the error flag is set and TMEM is freed. */
+#define CZ_THREADS 192
+
+template <int CIN, int COUT>
+struct ConvZSmem {
+   /* a tile reads three stages; the rest stream in behind them. 16-channel
+    * inputs keep a shorter ring so that three CTAs (three MMA issuers)
+    * share an SM */
+   static constexpr int NST = CIN == 16 ? 4 : 6;
+   static constexpr int KS = CIN / 16;
+   static constexpr int STAGE = 3 * (CIN / 8) * CONV_RUN * 16;   /* one input plane's runs */
+   static constexpr int W_ALL = 27 * CIN * COUT * 2;             /* all taps, packed image */
+   /* no slack: the highest byte an A descriptor reaches (last run block,
+    * x-tap +1, second K half, row group 15) is the last byte of its stage,
+    * and a B descriptor stays inside its tap's 2 x COUT x 16 bytes */
+   static constexpr int BYTES = W_ALL + NST * STAGE;
+   static constexpr int NCOL = COUT < 32 ? 32 : COUT;            /* columns of one accumulator */
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_addr(bar)) : "memory");
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(CZ_THREADS) k_conv_tcz(const __nv_bfloat16 *in, __nv_bfloat16 *out,
+                                                         const __nv_bfloat16 *wimg, const float *bias, pgb_lvgeom g,
+                                                         int relu, int jt, int zc, int nunit, int *err)
+{
+   typedef ConvZSmem<CIN, COUT> S;
+   extern __shared__ __align__(128) uint8_t smem[];
+   uint8_t *sW = smem, *sA = smem + S::W_ALL;
+   __shared__ __align__(8) uint64_t full[S::NST], empty[S::NST], tfull[2], tempty[2], wbar;
+   __shared__ uint32_t tmem_base;
+   __shared__ int s_fail_;
+   volatile int &s_fail = s_fail_;
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+   if (warp == 0) tmem_alloc(&tmem_base, 2 * S::NCOL);
+   if (tid == 0) {
+      for (int s = 0; s < S::NST; s++) {
+         mbar_init(&full[s], 1);
+         mbar_init(&empty[s], 1);
+      }
+      for (int b = 0; b < 2; b++) {
+         mbar_init(&tfull[b], 1);
+         mbar_init(&tempty[b], 4);
+      }
+      mbar_init(&wbar, 1);
+      mbar_fence_init();
+      s_fail = 0;
+   }
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t taddr = tmem_base;
+   constexpr uint32_t IDESC = idesc_bf16(128, COUT);
+
+   if (warp == 0) {
+      /* producer */
+      if (lane == 0) {
+         mbar_expect_tx(&wbar, S::W_ALL);
+         bulk_g2s(sW, wimg, S::W_ALL, &wbar);
+         uint32_t cnt = 0;
+         for (int u = blockIdx.x; u < nunit && !s_fail; u += gridDim.x) {
+            const int j = u % jt, z0 = (u / jt) * zc, z1 = min(g.D, z0 + zc);
+            for (int zz = z0 - 1; zz <= z1 && !s_fail; zz++, cnt++) {
+               const int s = cnt % S::NST;
+               if (!mbar_wait(&empty[s], ((cnt / S::NST) & 1) ^ 1)) {
+                  s_fail = 1;
+                  break;
+               }
+               mbar_expect_tx(&full[s], S::STAGE);
+               const long T = g.p0 + (long)zz * g.plane + 128L * j;
+               for (int dy = 0; dy < 3; dy++)
+                  for (int cb = 0; cb < CIN / 8; cb++) {
+                     const long v = g.margin + T + (dy - 1) * (long)g.Wp - 1;
+                     bulk_g2s(sA + s * S::STAGE + (dy * (CIN / 8) + cb) * CONV_RUN * 16,
+                              in + ((long)cb * g.vtot + v) * 8, CONV_RUN * 16, &full[s]);
+                  }
+            }
+         }
+         /* tail: every stage handed out is released (its last MMAs done)
+          * before the CTA exits, so no arrival lands after the memory is freed */
+         for (uint32_t k = cnt > S::NST ? cnt - S::NST : 0; k < cnt && !s_fail; k++)
+            if (!mbar_wait(&empty[k % S::NST], (k / S::NST) & 1)) s_fail = 1;
+      }
+   } else if (warp == 1) {
+      /* MMA issuer */
+      if (lane == 0) {
+         bool ok = mbar_wait(&wbar, 0);
+         uint32_t cnt = 0, tc = 0;
+         const uint64_t a_desc0 = sdesc(s_addr(sA), CONV_RUN * 16, 128), b_desc0 = sdesc(s_addr(sW), COUT * 16, 128);
+         for (int u = blockIdx.x; u < nunit && ok && !s_fail; u += gridDim.x) {
+            const int z0 = (u / jt) * zc, z1 = min(g.D, z0 + zc);
+            const uint32_t base = cnt;   /* stage sequence number of plane z0-1 */
+            /* planes z0-1 and z0 */
+            for (int q = 0; q < 2 && ok; q++)
+               ok = mbar_wait(&full[(base + q) % S::NST], ((base + q) / S::NST) & 1);
+            for (int z = z0; z < z1 && ok; z++, tc++) {
+               const uint32_t nz = base + (z - z0) + 2;   /* plane z+1 */
+               ok = mbar_wait(&full[nz % S::NST], (nz / S::NST) & 1) &&
+                    mbar_wait(&tempty[tc & 1], ((tc >> 1) & 1) ^ 1);
+               if (!ok) break;
+               tc_fence_after();
+               const uint32_t acc = taddr + (tc & 1) * S::NCOL;
+#pragma unroll
+               for (int dz = 0; dz < 3; dz++) {
+                  const uint32_t st = (base + (z - z0) + dz) % S::NST;
+                  /* descriptors are linear in the address (14-bit field of
+                   * address / 16, no carry below 256 KB): one base each, plus
+                   * compile-time offsets */
+                  const uint64_t da = a_desc0 + ((st * S::STAGE) >> 4);
+#pragma unroll
+                  for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                     for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+                        for (int ks = 0; ks < S::KS; ks++) {
+                           const uint32_t ao = ((dy * (CIN / 8) + 2 * ks) * CONV_RUN + dx) * 16;
+                           const uint32_t bo = ((((dz * 3 + dy) * 3 + dx) * S::KS + ks) * 2 * COUT) * 16;
+                           mma_bf16(acc, da + (ao >> 4), b_desc0 + (bo >> 4), IDESC, (dz | dy | dx | ks) != 0);
+                        }
+               }
+               mma_commit(&empty[(base + (z - z0)) % S::NST]);   /* plane z-1 is done */
+               mma_commit(&tfull[tc & 1]);
+            }
+            if (ok) {   /* planes z1-1 and z1 are done too */
+               mma_commit(&empty[(base + (z1 - z0)) % S::NST]);
+               mma_commit(&empty[(base + (z1 - z0) + 1) % S::NST]);
+               cnt = base + (z1 - z0) + 2;
+            }
+         }
+         if (!ok) s_fail = 1;
+      }
+   } else {
+      /* epilogue: warps 2..5 own TMEM lanes 32 (warp % 4) .. + 31 */
+      const int row = 32 * (warp & 3) + lane;
+      const int plane = (int)g.plane;
+      float bv[COUT];
+#pragma unroll
+      for (int c = 0; c < COUT; c++) bv[c] = bias ? bias[c] : 0.f;
+      uint32_t tc = 0;
+      for (int u = blockIdx.x; u < nunit && !s_fail; u += gridDim.x) {
+         const int j = u % jt, z0 = (u / jt) * zc, z1 = min(g.D, z0 + zc);
+         for (int z = z0; z < z1; z++, tc++) {
+            if (!mbar_wait(&tfull[tc & 1], (tc >> 1) & 1)) {
+               s_fail = 1;
+               break;
+            }
+            tc_fence_after();
+            const int q = 128 * j + row;                                  /* offset in the plane */
+            const long P = g.p0 + (long)z * g.plane + q;                  /* this thread's voxel */
+            const bool mine = q < plane;                                  /* not the next plane's */
+            const int y = q / g.Wp, x = q - y * g.Wp;
+            const bool pad = x == 0 || x == g.Wp - 1 || y == 0 || y == g.Hp - 1;
+            const uint32_t tw = taddr + (tc & 1) * S::NCOL + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll
+            for (int c16 = 0; c16 < COUT / 16; c16++) {
+               float v[16];
+               tmem_ld16(tw + c16 * 16, v);
+#pragma unroll
+               for (int h = 0; h < 2; h++) {
+                  uint32_t pk[4];
+#pragma unroll
+                  for (int e = 0; e < 4; e++) {
+                     float a0 = v[h * 8 + 2 * e] + bv[c16 * 16 + h * 8 + 2 * e];
+                     float a1 = v[h * 8 + 2 * e + 1] + bv[c16 * 16 + h * 8 + 2 * e + 1];
+                     if (relu) {
+                        a0 = leaky(a0);
+                        a1 = leaky(a1);
+                     }
+                     if (pad) a0 = a1 = 0.f;
+                     __nv_bfloat162 b2 = __floats2bfloat162_rn(a0, a1);
+                     pk[e] = *reinterpret_cast<uint32_t *>(&b2);
+                  }
+                  if (mine) {
+                     const long cb = c16 * 2 + h;
+                     *reinterpret_cast<uint4 *>(out + (cb * g.vtot + g.margin + P) * 8) =
+                         make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                  }
+               }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[tc & 1]);
+         }
+         if (s_fail) break;
+      }
+   }
+   __syncthreads();
+   if (s_fail) {
+      /* let copies and MMAs in flight land (about a millisecond) before the
+       * shared and tensor memory are released */
+      const uint64_t t0 = global_ns();
+      while (global_ns() - t0 < 1000000ull) {
+      }
+      if (tid == 0 && err) atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(taddr, 2 * S::NCOL);
+}
+
+template <int CIN, int COUT>
+static int launch_convz(const void *in, void *out, const void *wimg, const float *bias, const pgb_lvgeom &g,
+                        int relu, int *err, cudaStream_t st)
+{
+   typedef ConvZSmem<CIN, COUT> S;
+   static bool attr = false;
+   if (!attr) {
+      if (cudaFuncSetAttribute(k_conv_tcz<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES) !=
+          cudaSuccess)
+         return check_net("convz attribute");
+      attr = true;
+   }
+   const int jt = (int)((g.plane + 127) / 128);
+   const int per_sm = (227 * 1024) / (S::BYTES + 1024) > 0 ? (227 * 1024) / (S::BYTES + 1024) : 1;
+   const int want = 2 * 152 * per_sm;
+   int zc = 32;
+   while (zc > 1 && (long)jt * ((g.D + zc - 1) / zc) < want) zc /= 2;
+   const int nunit = jt * ((g.D + zc - 1) / zc);
+   const int grid = nunit < 152 * per_sm ? nunit : 152 * per_sm;
+   k_conv_tcz<CIN, COUT><<<grid, CZ_THREADS, S::BYTES, st>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out,
+                                                             (const __nv_bfloat16 *)wimg, bias, g, relu, jt, zc,
+                                                             nunit, err);
+   return check_net("conv_tcz") ? 11 : 0;
+}
+
 #define CONV_CASE(a, b) \
    if (cin == a && cout == b) return launch_conv<a, b>(in, out, wimg, bias, g, relu, err, st);
+
+#define CONVZ_CASE(a, b) \
+   if (cin == a && cout == b) return launch_convz<a, b>(in, out, wimg, bias, g, relu, err, st);
 
 static int conv_dispatch(int cin, int cout, const void *in, void *out, const void *wimg, const float *bias,
                          const pgb_lvgeom &g, int relu, int *err, cudaStream_t st)
 {
+   /* 16/32-channel layers: the z-marching pipelined kernel; 64-channel
+    * layers (weights too large to keep resident beside the stages): one CTA
+    * per tile */
+   CONVZ_CASE(16, 16)
+   CONVZ_CASE(16, 32)
+   CONVZ_CASE(32, 16)
+   CONVZ_CASE(32, 32)
    CONV_CASE(16, 16)
    CONV_CASE(16, 32)
    CONV_CASE(16, 64)
@@ -351,7 +607,7 @@ __global__ void k_pack_weights(const float *w, __nv_bfloat16 *img, int cin, int 
    const int ci_n = flip ? cout : cin, co_n = flip ? cin : cout;   /* channels of the packed conv */
    const int ks_n = ci_n / 16;
    const long n = 27L * ci_n * co_n;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
       /* q enumerates the image: [dz][t9][ks][h][co][e] */
       const int e = (int)(q % 8);
       long r = q / 8;
@@ -396,6 +652,17 @@ extern "C" int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, cons
 /* ------------------------------------------- CUDA-core kernels of the net -- */
 typedef __nv_bfloat16 bf16;
 
+/* x, y, z of voxel q of the interior volume (x fastest), in 32-bit
+ * arithmetic: volumes here stay below 2^31 voxels (pgb_net_create bounds n) */
+__device__ __forceinline__ void xyz(int q, const pgb_lvgeom &g, int &x, int &y, int &z)
+{
+   const int wh = g.W * g.H;
+   z = q / wh;
+   const int r = q - z * wh;
+   y = r / g.W;
+   x = r - y * g.W;
+}
+
 __device__ __forceinline__ long vox(const pgb_lvgeom &g, int x, int y, int z)
 {
    return g.margin + (x + 1) + (long)g.Wp * ((y + 1) + (long)g.Hp * (z + 1));
@@ -426,51 +693,99 @@ __device__ __forceinline__ void store8(bf16 *a, long idx, const float *v)
 
 /* first layer, 1 -> 16 channels: a0 = leaky(conv(s_in * rho) + b); rho is
  * the n^3 FP64 grid, the net sees its points 0..n-2 in each dimension
- * (zero beyond) */
-__global__ void k_in_fwd(const double *rho, int n, float s_in, const float *w, const float *b, bf16 *out,
-                         pgb_lvgeom g)
+ * (zero beyond), read here through its FP32 copy r32 */
+/* r32 = s_in * rho as FP32 in the level-0 padded layout (one channel,
+ * zero on the padding and margins, which nothing writes), converted once
+ * per voxel: the first layer and its weight gradient read each value 27
+ * times, at fixed offsets without bounds tests */
+__global__ void k_rho32(const double *rho, int n, float s_in, float *r32, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
-      float acc[16];
-#pragma unroll
-      for (int c = 0; c < 16; c++) acc[c] = b[c];
-      for (int t = 0; t < 27; t++) {
-         const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
-         if (xx < 0 || yy < 0 || zz < 0 || xx >= g.W || yy >= g.H || zz >= g.D) continue;
-         const float r = s_in * (float)rho[xx + (long)n * (yy + (long)n * zz)];
-#pragma unroll
-         for (int c = 0; c < 16; c++) acc[c] = fmaf(r, w[t * 16 + c], acc[c]);
-      }
-#pragma unroll
-      for (int c = 0; c < 16; c++) acc[c] = leaky(acc[c]);
-      const long p = vox(g, x, y, z);
-      store8(out, p, acc);
-      store8(out, g.vtot + p, acc + 8);
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
+      int x, y, z;
+      xyz(q, g, x, y, z);
+      r32[vox(g, x, y, z)] = s_in * (float)rho[x + (long)n * (y + (long)n * z)];
    }
+}
+
+__global__ void k_in_fwd(const float *r32, const float *w, const float *b, bf16 *out, pgb_lvgeom g)
+{
+   /* one voxel per thread: with a loop over voxels the compiler would keep
+    * all 432 weights in registers across it */
+   __shared__ float4 sw[27 * 4];   /* the weights, staged once per block */
+   for (int i = threadIdx.x; i < 27 * 4; i += blockDim.x)
+      sw[i] = make_float4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+   __syncthreads();
+   const int q = blockIdx.x * blockDim.x + threadIdx.x;
+   if (q >= g.W * g.H * g.D) return;
+   int x, y, z;
+   xyz(q, g, x, y, z);
+   float acc[16];
+#pragma unroll
+   for (int c = 0; c < 16; c++) acc[c] = b[c];
+   const long p0 = vox(g, x, y, z);
+#pragma unroll 3
+   for (int t = 0; t < 27; t++) {
+      const float r = r32[p0 + (t / 9 - 1) * g.plane + ((t / 3) % 3 - 1) * (long)g.Wp + (t % 3 - 1)];
+#pragma unroll
+      for (int c4 = 0; c4 < 4; c4++) {
+         const float4 wv = sw[t * 4 + c4];
+         acc[4 * c4] = fmaf(r, wv.x, acc[4 * c4]);
+         acc[4 * c4 + 1] = fmaf(r, wv.y, acc[4 * c4 + 1]);
+         acc[4 * c4 + 2] = fmaf(r, wv.z, acc[4 * c4 + 2]);
+         acc[4 * c4 + 3] = fmaf(r, wv.w, acc[4 * c4 + 3]);
+      }
+   }
+#pragma unroll
+   for (int c = 0; c < 16; c++) acc[c] = leaky(acc[c]);
+   store8(out, p0, acc);
+   store8(out, g.vtot + p0, acc + 8);
 }
 
 /* last layer, 16 -> 1 channel, no activation: up = conv(a) + b, as FP32 on
  * the net volume (x fastest) */
 __global__ void k_out_fwd(const bf16 *a, const float *w, const float *b, float *up, pgb_lvgeom g)
 {
-   const long nv = (long)g.W * g.H * g.D;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
-      const long p = vox(g, x, y, z);
-      float acc = b[0];
-      for (int t = 0; t < 27; t++) {
-         const long o = (t / 9 - 1) * g.plane + ((t / 3) % 3 - 1) * (long)g.Wp + (t % 3 - 1);
+   /* a thread computes four voxels along z: each 16-channel vector it loads
+    * serves every output plane that reads it; each output still sums its
+    * taps in tap order (z, then y, then x), as one voxel per thread would */
+   __shared__ float4 sw[27 * 4];   /* the weights, staged once per block */
+   for (int i = threadIdx.x; i < 27 * 4; i += blockDim.x)
+      sw[i] = make_float4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+   __syncthreads();
+   const int zb = (g.D + 3) / 4;
+   const long nw = (long)g.W * g.H * zb;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nw; q += gridDim.x * blockDim.x) {
+      int x, y, z0;
+      xyz(q, g, x, y, z0);
+      z0 *= 4;
+      const int nz = g.D - z0 < 4 ? g.D - z0 : 4;
+      float acc[4];
 #pragma unroll
-         for (int cb = 0; cb < 2; cb++) {
-            float v[8];
-            load8(a, (long)cb * g.vtot + p + o, v);
+      for (int k = 0; k < 4; k++) acc[k] = b[0];
+      for (int zz = z0 - 1; zz <= z0 + nz; zz++)
 #pragma unroll
-            for (int e = 0; e < 8; e++) acc = fmaf(v[e], w[t * 16 + cb * 8 + e], acc);
+         for (int t9 = 0; t9 < 9; t9++) {
+            const long p = vox(g, x + t9 % 3 - 1, y + t9 / 3 - 1, zz);
+            float v[16];
+            load8(a, p, v);
+            load8(a, g.vtot + p, v + 8);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+               const int dz = zz - (z0 + k) + 1;
+               if (k >= nz || dz < 0 || dz > 2) continue;
+               const float4 *wt = sw + (dz * 9 + t9) * 4;
+#pragma unroll
+               for (int c4 = 0; c4 < 4; c4++) {
+                  const float4 wv = wt[c4];
+                  acc[k] = fmaf(v[4 * c4], wv.x, acc[k]);
+                  acc[k] = fmaf(v[4 * c4 + 1], wv.y, acc[k]);
+                  acc[k] = fmaf(v[4 * c4 + 2], wv.z, acc[k]);
+                  acc[k] = fmaf(v[4 * c4 + 3], wv.w, acc[k]);
+               }
+            }
          }
-      }
-      up[q] = acc;
+      for (int k = 0; k < nz; k++) up[x + (long)g.W * (y + (long)g.H * (z0 + k))] = acc[k];
    }
 }
 
@@ -479,8 +794,8 @@ __global__ void k_out_fwd(const bf16 *a, const float *w, const float *b, float *
 __global__ void k_out_store(const float *up, double *u, int n, double s_out, pgb_lvgeom g)
 {
    const long nn = (long)n * n * n;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % n), y = (int)((q / n) % n), z = (int)(q / ((long)n * n));
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x) {
+      const int z = q / (n * n), r = q - z * n * n, y = r / n, x = r - y * n;
       double v = 0.0;
       if (x > 0 && y > 0 && z > 0 && x < n - 1 && y < n - 1 && z < n - 1)
          v = s_out * (double)up[x + (long)g.W * (y + (long)g.H * z)];
@@ -498,8 +813,8 @@ __global__ void k_energy_dots(const double *rho, const double *u, int n, double 
    __shared__ double sm[2][8];
    const long nn = (long)n * n * n, s1 = n, s2 = (long)n * n;
    double a = 0, b = 0;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % n), y = (int)((q / n) % n), z = (int)(q / s2);
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x) {
+      const int z = q / (n * n), r = q - z * n * n, y = r / n, x = r - y * n;
       if (x == 0 || y == 0 || z == 0 || x == n - 1 || y == n - 1 || z == n - 1) continue;
       const double c = u[q];
       const double lap = (u[q - 1] + u[q + 1] + u[q - s1] + u[q + s1] + u[q - s2] + u[q + s2] - 6.0 * c) * inv_h2;
@@ -523,7 +838,7 @@ __global__ void k_energy_dots(const double *rho, const double *u, int n, double 
 __global__ void k_scale_guess(double *u, long nn, const double *dots)
 {
    const double alpha = dots[1] != 0.0 ? dots[0] / dots[1] : 1.0;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nn; q += (long)gridDim.x * blockDim.x) u[q] *= alpha;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x) u[q] *= alpha;
 }
 
 /* MSE over points 1..n-2: loss += sum (up - ut/s_out)^2 / N, gup = dloss/dup */
@@ -534,8 +849,9 @@ __global__ void k_loss(const float *up, const float *ut, int n, float inv_s_out,
    const long nv = (long)g.W * g.H * g.D;
    const double inv_n = 1.0 / ((double)(n - 2) * (n - 2) * (n - 2));
    double acc = 0;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
+      int x, y, z;
+      xyz(q, g, x, y, z);
       float gr = 0.f;
       if (x > 0 && y > 0 && z > 0) {
          const float d = up[q] - inv_s_out * ut[x + (long)n * (y + (long)n * z)];
@@ -558,8 +874,9 @@ __global__ void k_loss(const float *up, const float *ut, int n, float inv_s_out,
 __global__ void k_out_bwd_data(const float *gup, const float *w, bf16 *ga, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
+      int x, y, z;
+      xyz(q, g, x, y, z);
       float acc[16];
 #pragma unroll
       for (int c = 0; c < 16; c++) acc[c] = 0.f;
@@ -598,8 +915,9 @@ __global__ void k_out_bwd_w(const bf16 *a, const float *gup, float *dw, float *d
    float acc[16], ab = 0.f;
 #pragma unroll
    for (int c = 0; c < 16; c++) acc[c] = 0.f;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
+      int x, y, z;
+      xyz(q, g, x, y, z);
       const float gv = gup[q];
       const long p = vox(g, x, y, z) + o;
       float v[8];
@@ -617,7 +935,7 @@ __global__ void k_out_bwd_w(const bf16 *a, const float *gup, float *dw, float *d
 }
 
 /* first layer dW: dw[t][c] += sum_v s_in rho[v + off t] gz[v][c], db[c] += sum gz */
-__global__ void k_in_bwd_w(const double *rho, int n, float s_in, const bf16 *gz, float *dw, float *db, pgb_lvgeom g)
+__global__ void k_in_bwd_w(const float *r32, const bf16 *gz, float *dw, float *db, pgb_lvgeom g)
 {
    __shared__ float red[256];
    const int t = blockIdx.y;
@@ -626,13 +944,11 @@ __global__ void k_in_bwd_w(const double *rho, int n, float s_in, const bf16 *gz,
    float acc[16], ab[16];
 #pragma unroll
    for (int c = 0; c < 16; c++) acc[c] = ab[c] = 0.f;
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += (long)gridDim.x * blockDim.x) {
-      const int x = (int)(q % g.W), y = (int)((q / g.W) % g.H), z = (int)(q / ((long)g.W * g.H));
-      const int xx = x + ox, yy = y + oy, zz = z + oz;
-      float r = 0.f;
-      if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D)
-         r = s_in * (float)rho[xx + (long)n * (yy + (long)n * zz)];
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
+      int x, y, z;
+      xyz(q, g, x, y, z);
       const long p = vox(g, x, y, z);
+      const float r = r32[p + oz * g.plane + oy * (long)g.Wp + ox];   /* zero on the padding */
       float v[8];
 #pragma unroll
       for (int cb = 0; cb < 2; cb++) {
@@ -655,8 +971,8 @@ __global__ void k_in_bwd_w(const double *rho, int n, float s_in, const bf16 *gz,
 __global__ void k_relu_bwd(bf16 *gv, const bf16 *y, int nch, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D, n = nv * (nch / 8);
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-      const long cb = q / nv, r = q % nv;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
+      const int cb = q / (int)nv, r = q - cb * (int)nv;
       const int x = (int)(r % g.W), yy = (int)((r / g.W) % g.H), z = (int)(r / ((long)g.W * g.H));
       const long idx = cb * g.vtot + vox(g, x, yy, z);
       float a[8], b[8];
@@ -673,8 +989,8 @@ __global__ void k_relu_bwd(bf16 *gv, const bf16 *y, int nch, pgb_lvgeom g)
 __global__ void k_pool(bf16 *f, bf16 *c, int nch, pgb_lvgeom gf, pgb_lvgeom gc, int backward)
 {
    const long nv = (long)gc.W * gc.H * gc.D, n = nv * (nch / 8);
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-      const long cb = q / nv, r = q % nv;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
+      const int cb = q / (int)nv, r = q - cb * (int)nv;
       const int x = (int)(r % gc.W), y = (int)((r / gc.W) % gc.H), z = (int)(r / ((long)gc.W * gc.H));
       const long ic = cb * gc.vtot + vox(gc, x, y, z);
       float s[8], v[8];
@@ -708,8 +1024,8 @@ __global__ void k_up(const bf16 *c, const bf16 *skip, bf16 *out, int nch, pgb_lv
 {
    if (!backward) {
       const long nv = (long)gf.W * gf.H * gf.D, n = nv * (nch / 8);
-      for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-         const long cb = q / nv, r = q % nv;
+      for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
+         const int cb = q / (int)nv, r = q - cb * (int)nv;
          const int x = (int)(r % gf.W), y = (int)((r / gf.W) % gf.H), z = (int)(r / ((long)gf.W * gf.H));
          const long i = cb * gf.vtot + vox(gf, x, y, z);
          float a[8], b[8];
@@ -721,8 +1037,8 @@ __global__ void k_up(const bf16 *c, const bf16 *skip, bf16 *out, int nch, pgb_lv
       }
    } else {
       const long nv = (long)gc.W * gc.H * gc.D, n = nv * (nch / 8);
-      for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-         const long cb = q / nv, r = q % nv;
+      for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
+         const int cb = q / (int)nv, r = q - cb * (int)nv;
          const int x = (int)(r % gc.W), y = (int)((r / gc.W) % gc.H), z = (int)(r / ((long)gc.W * gc.H));
          float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
          for (int k = 0; k < 8; k++) {
@@ -739,8 +1055,8 @@ __global__ void k_up(const bf16 *c, const bf16 *skip, bf16 *out, int nch, pgb_lv
 __global__ void k_add(bf16 *a, const bf16 *b, int nch, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D, n = nv * (nch / 8);
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-      const long cb = q / nv, r = q % nv;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
+      const int cb = q / (int)nv, r = q - cb * (int)nv;
       const int x = (int)(r % g.W), y = (int)((r / g.W) % g.H), z = (int)(r / ((long)g.W * g.H));
       const long i = cb * g.vtot + vox(g, x, y, z);
       float u[8], v[8];
@@ -809,7 +1125,7 @@ __global__ void __launch_bounds__(256) k_conv_bwd_w(const bf16 *x, const bf16 *g
 __global__ void k_adam(float *w, const float *gw, float *m, float *v, long n, float lr, float b1, float b2,
                        float c1, float c2, float eps)
 {
-   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)n; q += gridDim.x * blockDim.x) {
       const float gq = gw[q];
       const float mq = b1 * m[q] + (1.f - b1) * gq, vq = b2 * v[q] + (1.f - b2) * gq * gq;
       m[q] = mq;
@@ -883,7 +1199,7 @@ struct pgb_net {
    long off_tc_w[NTC], off_tc_b[NTC], off_in_w, off_in_b, off_out_w, off_out_b;
    bf16 *img[NTC], *img_adj[NTC];
    bf16 *act[NACT], *grad[NACT];
-   float *up, *gup;
+   float *up, *gup, *r32;
    double *d_loss;
    double *d_dots;                /* energy-norm scaling sums */
    int *d_err;
@@ -936,6 +1252,7 @@ extern "C" void pgb_net_destroy(pgb_net *net)
    }
    cudaFree(net->up);
    cudaFree(net->gup);
+   cudaFree(net->r32);
    cudaFree(net->d_loss);
    cudaFree(net->d_dots);
    cudaFree(net->d_err);
@@ -946,8 +1263,8 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
 {
    *out = 0;
    const int step = 1 << (NLEV - 1);
-   if (n < 2 * step + 1 || (n - 1) % step != 0)
-      return arg_err("pgb_net_create: n-1 must be a multiple of 32, n >= 65");
+   if (n < 2 * step + 1 || (n - 1) % step != 0 || n > 513)
+      return arg_err("pgb_net_create: n-1 must be a multiple of 32, 65 <= n <= 513");
    layer_table();
    pgb_net *net = (pgb_net *)calloc(1, sizeof(pgb_net));
    net->n = n;
@@ -970,6 +1287,8 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
    bool ok = cudaMalloc((void **)&net->p, o * 4) == cudaSuccess && cudaMalloc((void **)&net->gp, o * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->m, o * 4) == cudaSuccess && cudaMalloc((void **)&net->v, o * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->up, nv * 4) == cudaSuccess && cudaMalloc((void **)&net->gup, nv * 4) == cudaSuccess &&
+             cudaMalloc((void **)&net->r32, net->g[0].vtot * 4) == cudaSuccess &&
+             cudaMemset(net->r32, 0, net->g[0].vtot * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->d_loss, 8) == cudaSuccess && cudaMalloc((void **)&net->d_err, 4) == cudaSuccess &&
              cudaMalloc((void **)&net->d_dots, 16) == cudaSuccess;
    for (int l = 0; l < NTC && ok; l++)
@@ -1082,8 +1401,10 @@ static int forward(pgb_net *net, const double *rho, cudaStream_t st)
    bf16 **a = net->act;
    pgb_lvgeom *g = net->g;
 #define A(k, v) a[act_id(k, v)]
-   NETK((k_in_fwd<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->p + net->off_in_w,
-                                            net->p + net->off_in_b, A(K_E0, 0), g[0])), "net in");
+   NETK((k_rho32<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->r32, g[0])), "net rho32");
+   NETK((k_in_fwd<<<(g[0].W * g[0].H * g[0].D + 255) / 256, 256, 0, st>>>(net->r32, net->p + net->off_in_w,
+                                                                          net->p + net->off_in_b, A(K_E0, 0), g[0])),
+        "net in");
    if (tc(net, 0, A(K_E0, 0), A(K_E1, 0), 0, st)) return 11;
    for (int v = 1; v < NLEV; v++) {
       NETK((k_pool<<<GRID_1D, 256, 0, st>>>(A(K_E1, v - 1), A(K_P, v), LCH[v - 1], g[v - 1], g[v], 0)), "net pool");
@@ -1182,7 +1503,7 @@ static int loss_grad(pgb_net *net, const double *rho, const float *ut, cudaStrea
    const int e0 = act_id(K_E0, 0);
    if (conv_bwd(net, 0, e0, act_id(K_E1, 0), st)) return 11;
    NETK((k_relu_bwd<<<GRID_1D, 256, 0, st>>>(G[e0], a[e0], LCH[0], g[0])), "net relu");
-   NETK((k_in_bwd_w<<<dim3(96, 27), 256, 0, st>>>(rho, net->n, (float)net->s_in, G[e0], net->gp + net->off_in_w,
+   NETK((k_in_bwd_w<<<dim3(96, 27), 256, 0, st>>>(net->r32, G[e0], net->gp + net->off_in_w,
                                                    net->gp + net->off_in_b, g[0])), "net in w");
    return 0;
 }

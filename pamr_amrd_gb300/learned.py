@@ -45,7 +45,7 @@ def conv_lib():
 
 
 class Net:
-    """n: grid points per side of the solve (n-1 a multiple of 32, n >= 65)"""
+    """n: grid points per side of the solve (n-1 a multiple of 32, 65 <= n <= 513)"""
 
     # levels and channels per level (pgb_net.cu: NLEV, LCH)
     NLEV = 6

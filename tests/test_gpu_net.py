@@ -47,8 +47,8 @@ def from_layout(act, P, shape):
     return out.reshape(D, H, W, Cn)
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 64), (64, 64), (64, 16)])
-@pytest.mark.parametrize("vol", [(16, 12, 10), (128, 6, 5), (4, 4, 4), (2, 2, 2)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 16), (32, 32), (32, 64), (64, 64), (64, 16)])
+@pytest.mark.parametrize("vol", [(16, 12, 10), (128, 6, 5), (4, 4, 4), (2, 2, 2), (40, 24, 37)])
 @pytest.mark.parametrize("adjoint", [0, 1])
 def test_conv3d_matches_torch(cin, cout, vol, adjoint):
     L = _lib()
