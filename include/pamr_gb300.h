@@ -263,9 +263,11 @@ int pgb_conv3d_bf16(const void *in, void *out, const void *wimg, const float *bi
 /* Kreiss-Oliger dissipation, dmdiss3d (src/m_util_r8.f:1690-1956;
  * include/m_util_r8.h:33-36), on device arrays f, work, eps (eps[0] is the
  * coefficient, as eps(1,1,1)), mask; phys_bdy_type is a host array of 6.
- * Bit-exact with the Fortran; the excised path (do_ex != 0) is rejected
- * (error 12). Called by AMRD after each step on the dissipated variables
- * (amrd/evolve.c:430, 509, 957). */
+ * Bit-exact with the Fortran, including the excised path (do_ex != 0,
+ * dmdiss3d_ex, src/m_util_r8.f:972-1332: chr a device mask, eps per point
+ * when do_ex < 0), where stencils that would leave the array in the
+ * Fortran are skipped. Called by AMRD after each step on the dissipated
+ * variables (amrd/evolve.c:430, 509, 957). */
 int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_bdy, const int *phys_bdy_type,
                  int even, int odd, const double *mask, double mask_off, int nx, int ny, int nz,
                  const double *chr, double ex, int do_ex, void *stream);

@@ -18,7 +18,7 @@
  * extrapolation tests i <= i1s-4*s1. No Fortran compiler is available, so
  * these are pinned by known-answer tests, not by running the reference.
  * dmdiss3d (Kreiss-Oliger dissipation, the evolution kernel next to the
- * elliptic solve) is restated without its excised path (dmdiss3d_ex), and
+ * elliptic solve) is restated with its excised path (dmdiss3d_ex), and
  * linbnd3d (linear approach to the boundaries) fully. The other
  * evolution-only routines (dmrepop3d1, dmrepop3dc1) are not on the path and
  * abort if reached.
@@ -714,12 +714,98 @@ static double diss_hf(const double *w, long s, int p, int n, int cdo_lo, int cdo
    return f_hf;
 }
 
+/* The excised variant's term along one dimension (src/m_util_r8.f:1017-1114
+ * for i; the j and k blocks repeat it): the Fortran's thirteen branches in
+ * order. X(o): the neighbour at offset o is inside the line and not excised;
+ * the Fortran tests chr without range guards, so on short lines it reads
+ * outside the array there: a neighbour outside counts as excised here, which
+ * skips exactly the branches whose stencil would leave the array. */
+static double diss_hf_ex(const double *w, const double *ch, double ex, long s, int p, int n, int pbt_lo,
+                         int pbt_hi, int even, int odd, int bo1, int bo2)
+{
+   const double w4 = 1.0 / 16.0, w3 = 1.0 / 8.0, w2 = 1.0 / 4.0;
+#define W(o) w[(o) * s]
+#define X(o) (p + (o) >= 1 && p + (o) <= n && ch[(o) * s] != ex)
+   if (p > 2 && p < (n - 1) && X(-2) && X(-1) && X(2) && X(1))
+      return w4 * (W(-2) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 2 && pbt_lo == odd && X(-1) && X(2) && X(1))
+      return w4 * ((-W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 1 && pbt_lo == odd && X(2) && X(1))
+      return w4 * ((-W(2)) + W(2) - 4 * ((-W(1)) + W(1)) + 6 * W(0));
+   if (p == n - 1 && pbt_hi == odd && X(1) && X(-2) && X(-1))
+      return w4 * (W(-2) + (-W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == n && pbt_hi == odd && X(-2) && X(-1))
+      return w4 * (W(-2) + (-W(-2)) - 4 * (W(-1) + (-W(-1))) + 6 * W(0));
+   if (p == 2 && pbt_lo == even && X(-1) && X(2) && X(1))
+      return w4 * ((W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 1 && pbt_lo == even && X(2) && X(1))
+      return w4 * ((W(2)) + W(2) - 4 * ((W(1)) + W(1)) + 6 * W(0));
+   if (p == n - 1 && pbt_hi == even && X(1) && X(-2) && X(-1))
+      return w4 * (W(-2) + (W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == n && pbt_hi == even && X(-2) && X(-1))
+      return w4 * (W(-2) + (W(-2)) - 4 * (W(-1) + (W(-1))) + 6 * W(0));
+   if (p > (2 - bo1) && p < (n - 1) && X(-1) && X(1) && X(2))
+      return w3 * (-W(-1) + 3 * W(0) - 3 * W(1) + W(2));
+   if (p > 2 && p < (n - 1 + bo1) && X(-1) && X(1) && X(-2))
+      return w3 * (-W(1) + 3 * W(0) - 3 * W(-1) + W(-2));
+   if ((p > (2 - bo2) || (p == 2 && ch[(1 - p) * s] == ex)) && p < (n - 1) && X(1) && X(2))
+      return w2 * (W(0) - 2 * W(1) + W(2));
+   if (p > 2 && (p < (n - 1 + bo2) || (p == n - 1 && ch[(n - p) * s] == ex)) && X(-1) && X(-2))
+      return w2 * (W(0) - 2 * W(-1) + W(-2));
+#undef W
+#undef X
+   return 0;
+}
+
+/* dmdiss3d_ex (src/m_util_r8.f:972-1332) with ind_sweeps = .true.: points
+ * whose mask is on and that are not excised; bo1, bo2 from do_bdy (with
+ * no_uc_ex_diss = .true., do_bdy = 0 disables the one-sided branches except
+ * next to an excised end point); eps(1,1,1) when do_ex > 0, eps(i,j,k) per
+ * point when do_ex < 0 */
+static void diss_ex(double *f, double *work, const double *eps, int do_bdy, const int *pbt, int even, int odd,
+                    const double *mask, double mask_off, int Nx, int Ny, int Nz, const double *chr, double ex,
+                    int do_ex)
+{
+   const long sy = Nx, sz = (long)Nx * Ny, ntot = (long)Nx * Ny * Nz;
+   int bo1, bo2, i, j, k, pass, npass, mx = Nx;
+   long q;
+   if (Ny > mx) mx = Ny;
+   if (Nz > mx) mx = Nz;
+   if (do_bdy == 0) {
+      bo1 = -mx;
+      bo2 = bo1;
+   } else {
+      bo1 = 1;
+      bo2 = 2;
+   }
+   npass = 1;
+   if (Ny > 1) npass = 2;
+   if (Nz > 1) npass = 3;
+   for (pass = 1; pass <= npass; pass++) {
+      for (q = 0; q < ntot; q++) work[q] = f[q];
+      for (i = 1; i <= Nx; i++)
+         for (j = 1; j <= Ny; j++)
+            for (k = 1; k <= Nz; k++) {
+               const long c = (i - 1) + sy * (j - 1) + sz * (k - 1);
+               double f_hf, eps_eff = do_ex < 0 ? eps[c] : eps[0];
+               if (!(mask[c] != mask_off && chr[c] != ex)) continue;
+               if (pass == 1)
+                  f_hf = diss_hf_ex(work + c, chr + c, ex, 1, i, Nx, pbt[0], pbt[1], even, odd, bo1, bo2);
+               else if (pass == 2)
+                  f_hf = diss_hf_ex(work + c, chr + c, ex, sy, j, Ny, pbt[2], pbt[3], even, odd, bo1, bo2);
+               else
+                  f_hf = diss_hf_ex(work + c, chr + c, ex, sz, k, Nz, pbt[4], pbt[5], even, odd, bo1, bo2);
+               f[c] = f[c] - eps_eff * f_hf;
+            }
+   }
+}
+
 /* dmdiss3d (src/m_util_r8.f:1690-1956), the path without excision:
  * independent sweeps (ind_sweeps = .true.), one pass per dimension of
  * extent > 1 (npass 1, 2 or 3); each pass copies f to work and subtracts
  * eps(1,1,1) times the dissipation term along its dimension at every point
- * whose mask is not mask_off. The excised path (dmdiss3d_ex) is not on the
- * restated path and aborts. */
+ * whose mask is not mask_off. With do_ex != 0 the Fortran calls
+ * dmdiss3d_ex, restated above (diss_ex). */
 void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_type, int *even,
                int *odd, double *mask, double *mask_off, int *nx, int *ny, int *nz, double *chr,
                double *ex, int *do_ex)
@@ -729,9 +815,10 @@ void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_
    int cdo_bdy[6], i, j, k, pass, npass;
    long q;
    double eps_eff;
-   (void)chr;
-   (void)ex;
-   if (*do_ex != 0) not_on_path("dmdiss3d_ex");
+   if (*do_ex != 0) {
+      diss_ex(f, work, eps, *do_bdy, phys_bdy_type, *even, *odd, mask, *mask_off, Nx, Ny, Nz, chr, *ex, *do_ex);
+      return;
+   }
    for (i = 0; i < 6; i++) {
       cdo_bdy[i] = *do_bdy;
       if (phys_bdy_type[i] == *even || phys_bdy_type[i] == *odd) cdo_bdy[i] = 1;

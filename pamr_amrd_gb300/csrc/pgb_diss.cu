@@ -7,7 +7,9 @@
  * and then, one thread per point, subtracts eps(1,1,1) times the
  * 4th-difference dissipation term along its dimension where the mask is
  * not mask_off, with the Fortran's one-sided and parity variants at the
- * faces. The excised path (do_ex != 0, dmdiss3d_ex) is rejected.
+ * faces; with do_ex != 0 the excised variant (dmdiss3d_ex,
+ * src/m_util_r8.f:972-1332), which also skips excised points and switches
+ * to one-sided stencils next to them.
  */
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -85,6 +87,73 @@ __device__ __forceinline__ double diss_hf(const double *w, long s, int p, int n,
    return f_hf;
 }
 
+/* The excised variant's term along one dimension (dmdiss3d_ex,
+ * src/m_util_r8.f:1017-1114 and its j, k repeats): the Fortran's thirteen
+ * branches in order. X(o): the neighbour at offset o is inside the line
+ * and not excised; the Fortran tests chr without range guards and reads
+ * outside the array on short lines: a neighbour outside counts as excised
+ * here, which skips exactly the branches whose stencil would leave the
+ * array (so no access leaves it). */
+__device__ __forceinline__ double diss_hf_ex(const double *w, const double *ch, double ex, long s, int p, int n,
+                                             int pbt_lo, int pbt_hi, int even, int odd, int bo1, int bo2)
+{
+   const double w4 = 1.0 / 16.0, w3 = 1.0 / 8.0, w2 = 1.0 / 4.0;
+#define W(o) w[(o) * s]
+#define X(o) (p + (o) >= 1 && p + (o) <= n && ch[(o) * s] != ex)
+   if (p > 2 && p < (n - 1) && X(-2) && X(-1) && X(2) && X(1))
+      return w4 * (W(-2) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 2 && pbt_lo == odd && X(-1) && X(2) && X(1))
+      return w4 * ((-W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 1 && pbt_lo == odd && X(2) && X(1))
+      return w4 * ((-W(2)) + W(2) - 4 * ((-W(1)) + W(1)) + 6 * W(0));
+   if (p == n - 1 && pbt_hi == odd && X(1) && X(-2) && X(-1))
+      return w4 * (W(-2) + (-W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == n && pbt_hi == odd && X(-2) && X(-1))
+      return w4 * (W(-2) + (-W(-2)) - 4 * (W(-1) + (-W(-1))) + 6 * W(0));
+   if (p == 2 && pbt_lo == even && X(-1) && X(2) && X(1))
+      return w4 * ((W(0)) + W(2) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == 1 && pbt_lo == even && X(2) && X(1))
+      return w4 * ((W(2)) + W(2) - 4 * ((W(1)) + W(1)) + 6 * W(0));
+   if (p == n - 1 && pbt_hi == even && X(1) && X(-2) && X(-1))
+      return w4 * (W(-2) + (W(0)) - 4 * (W(-1) + W(1)) + 6 * W(0));
+   if (p == n && pbt_hi == even && X(-2) && X(-1))
+      return w4 * (W(-2) + (W(-2)) - 4 * (W(-1) + (W(-1))) + 6 * W(0));
+   if (p > (2 - bo1) && p < (n - 1) && X(-1) && X(1) && X(2))
+      return w3 * (-W(-1) + 3 * W(0) - 3 * W(1) + W(2));
+   if (p > 2 && p < (n - 1 + bo1) && X(-1) && X(1) && X(-2))
+      return w3 * (-W(1) + 3 * W(0) - 3 * W(-1) + W(-2));
+   if ((p > (2 - bo2) || (p == 2 && ch[(1 - p) * s] == ex)) && p < (n - 1) && X(1) && X(2))
+      return w2 * (W(0) - 2 * W(1) + W(2));
+   if (p > 2 && (p < (n - 1 + bo2) || (p == n - 1 && ch[(n - p) * s] == ex)) && X(-1) && X(-2))
+      return w2 * (W(0) - 2 * W(-1) + W(-2));
+#undef W
+#undef X
+   return 0;
+}
+
+/* one pass along dimension d of the excised variant: points whose mask is
+ * on and that are not excised; eps[0] when do_ex > 0, eps per point when
+ * do_ex < 0 */
+__global__ void k_diss_ex(double *f, const double *work, const double *eps, const double *mask, double mask_off,
+                          const double *chr, double ex, int do_ex, int nx, int ny, int nz, int d, int pbt_lo,
+                          int pbt_hi, int even, int odd, int bo1, int bo2)
+{
+   const long sy = nx, sz = (long)nx * ny, n = sz * nz;
+   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+      if (!(mask[c] != mask_off && chr[c] != ex)) continue;
+      const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / sz);
+      const double eps_eff = do_ex < 0 ? eps[c] : eps[0];
+      double f_hf;
+      if (d == 0)
+         f_hf = diss_hf_ex(work + c, chr + c, ex, 1, i + 1, nx, pbt_lo, pbt_hi, even, odd, bo1, bo2);
+      else if (d == 1)
+         f_hf = diss_hf_ex(work + c, chr + c, ex, sy, j + 1, ny, pbt_lo, pbt_hi, even, odd, bo1, bo2);
+      else
+         f_hf = diss_hf_ex(work + c, chr + c, ex, sz, k + 1, nz, pbt_lo, pbt_hi, even, odd, bo1, bo2);
+      f[c] = f[c] - eps_eff * f_hf;
+   }
+}
+
 /* one pass along dimension d (0, 1, 2): f -= eps[0] * term(work) where the
  * mask is on; x fastest, one thread per point */
 __global__ void k_diss(double *f, const double *work, const double *eps, const double *mask, double mask_off,
@@ -110,11 +179,9 @@ extern "C" int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_b
                             int even, int odd, const double *mask, double mask_off, int nx, int ny, int nz,
                             const double *chr, double ex, int do_ex, void *stream)
 {
-   (void)chr;
-   (void)ex;
    cudaStream_t st = (cudaStream_t)stream;
-   if (do_ex != 0) return fail_diss("pgb_dmdiss3d: the excised path (dmdiss3d_ex) is not supported", 12);
    if (nx < 1 || ny < 1 || nz < 1) return fail_diss("pgb_dmdiss3d: empty grid", 3);
+   if (do_ex != 0 && !chr) return fail_diss("pgb_dmdiss3d: do_ex needs chr", 3);
    int cdo[6];
    for (int i = 0; i < 6; i++) {
       cdo[i] = do_bdy;
@@ -126,11 +193,21 @@ extern "C" int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_b
    const long n = (long)nx * ny * nz;
    const long blocks = (n + 255) / 256;
    const unsigned grid = (unsigned)(blocks < 4864 ? blocks : 4864);
+   /* the excised variant's one-sided branches (dmdiss3d_ex): bo1, bo2 from
+    * do_bdy, with no_uc_ex_diss = .true. */
+   int mx = nx > ny ? nx : ny;
+   mx = mx > nz ? mx : nz;
+   const int bo1 = do_bdy == 0 ? -mx : 1, bo2 = do_bdy == 0 ? -mx : 2;
    for (int d = 0; d < npass; d++) {
       if (cudaMemcpyAsync(work, f, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
          return check_diss("pgb_dmdiss3d copy");
-      const DissFace fc = {cdo[2 * d], cdo[2 * d + 1], phys_bdy_type[2 * d], phys_bdy_type[2 * d + 1]};
-      k_diss<<<grid, 256, 0, st>>>(f, work, eps, mask, mask_off, nx, ny, nz, d, fc, even, odd);
+      if (do_ex != 0)
+         k_diss_ex<<<grid, 256, 0, st>>>(f, work, eps, mask, mask_off, chr, ex, do_ex, nx, ny, nz, d,
+                                         phys_bdy_type[2 * d], phys_bdy_type[2 * d + 1], even, odd, bo1, bo2);
+      else {
+         const DissFace fc = {cdo[2 * d], cdo[2 * d + 1], phys_bdy_type[2 * d], phys_bdy_type[2 * d + 1]};
+         k_diss<<<grid, 256, 0, st>>>(f, work, eps, mask, mask_off, nx, ny, nz, d, fc, even, odd);
+      }
       if (check_diss("pgb_dmdiss3d")) return 11;
    }
    return 0;

@@ -118,21 +118,21 @@ void dminterp3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2,
    report("dminterp3d", rc);
 }
 
-/* Kreiss-Oliger dissipation (src/m_util_r8.f:1690-1956): f, work, eps(1)
- * and mask to the device, pgb_dmdiss3d, f and work back. The excised path
- * (do_ex != 0) is reported and leaves f unchanged. */
+/* Kreiss-Oliger dissipation (src/m_util_r8.f:1690-1956 and its excised
+ * variant): f, work, eps (one value, or every point when do_ex < 0), mask
+ * and chr (when excising) to the device, pgb_dmdiss3d, f and work back */
 void dmdiss3d_(double *f, double *work, double *eps, int *do_bdy, int *phys_bdy_type, int *even, int *odd,
                double *mask, double *mask_off, int *nx, int *ny, int *nz, double *chr, double *ex, int *do_ex)
 {
    size_t n = (size_t)*nx * *ny * *nz;
-   double *df = dev(0, f, n), *dw = dev(1, 0, n), *de = dev(2, eps, 1), *dm = dev(3, mask, n);
+   double *df = dev(0, f, n), *dw = dev(1, 0, n), *de = dev(2, eps, *do_ex < 0 ? n : 1), *dm = dev(3, mask, n);
+   double *dc = *do_ex != 0 ? dev(4, chr, n) : 0;
    int rc;
-   (void)chr;
-   if (!df || !dw || !de || !dm) {
+   if (!df || !dw || !de || !dm || (*do_ex != 0 && !dc)) {
       fprintf(stderr, "dmdiss3d: device buffers unavailable\n");
       return;
    }
-   rc = pgb_dmdiss3d(df, dw, de, *do_bdy, phys_bdy_type, *even, *odd, dm, *mask_off, *nx, *ny, *nz, 0, *ex,
+   rc = pgb_dmdiss3d(df, dw, de, *do_bdy, phys_bdy_type, *even, *odd, dm, *mask_off, *nx, *ny, *nz, dc, *ex,
                      *do_ex, 0);
    if (!rc) rc = back(f, df, n);
    if (!rc) rc = back(work, dw, n);

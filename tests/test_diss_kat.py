@@ -79,3 +79,65 @@ def test_three_passes_multiply(lib):
     f[3, 3, 3] = 1.0
     out, _ = diss(lib, f.reshape(-1), shape=(n, n, n))
     assert out.reshape(n, n, n)[3, 3, 3] == (13 / 16) ** 3
+
+
+def diss_ex(lib, f, chr_, eps=0.5, do_bdy=1, pbt=(OTHER,) * 6, do_ex=1, shape=None, ex=-1.0, mask=None):
+    nx, ny, nz = shape or (f.size, 1, 1)
+    f = np.ascontiguousarray(f, dtype=np.float64).copy()
+    work = np.zeros_like(f)
+    mask = np.ones_like(f) if mask is None else np.ascontiguousarray(mask, dtype=np.float64)
+    e = np.ascontiguousarray(np.atleast_1d(eps), dtype=np.float64)
+    c = np.ascontiguousarray(chr_, dtype=np.float64)
+    ci = lambda v: C.byref(C.c_int(v))  # noqa: E731
+    lib.dmdiss3d_(f.ctypes.data_as(D), work.ctypes.data_as(D), e.ctypes.data_as(D), ci(do_bdy),
+                  (C.c_int * 6)(*pbt), ci(EVEN), ci(ODD), mask.ctypes.data_as(D), C.byref(C.c_double(0.0)),
+                  ci(nx), ci(ny), ci(nz), c.ctypes.data_as(D), C.byref(C.c_double(ex)), ci(do_ex))
+    return f
+
+
+@pytest.mark.parametrize("pbt", [(OTHER,) * 6, (EVEN, ODD, ODD, EVEN, OTHER, EVEN)])
+def test_excised_path_without_excision_equals_the_plain_path(lib, pbt):
+    """with no excised point, do_bdy = 1 and lines of 5 or more, the
+    excised branches reduce to the plain ones (same stencils, same order)"""
+    rng = np.random.default_rng(5)
+    shape = (9, 7, 6)
+    f = rng.standard_normal(int(np.prod(shape)))
+    plain, _ = diss(lib, f, do_bdy=1, pbt=pbt, shape=shape)
+    ex = diss_ex(lib, f, np.zeros_like(f), do_bdy=1, pbt=pbt, shape=shape)
+    assert np.array_equal(plain, ex)
+
+
+def test_one_sided_next_to_an_excised_point(lib):
+    f = np.zeros(11)
+    f[5] = 1.0                        # i = 6
+    chr_ = np.zeros(11)
+    chr_[6] = -1.0                    # i = 7 excised
+    out = diss_ex(lib, f, chr_, do_bdy=1)
+    assert out[6] == 0.0              # the excised point is left alone
+    assert out[5] == 1 - 0.5 * 0.25   # i = 6: w2 (f(i) - 2 f(i-1) + f(i-2)) = 1/4
+    # i = 5: X(+2) fails, so the one-sided 3rd difference towards the left: w3 (-f(i+1) + 3 f(i) - 3 f(i-1) + f(i-2))
+    assert out[4] == -0.5 * (1 / 8) * (-1.0)
+
+
+def test_do_bdy_zero_keeps_only_the_end_rule(lib):
+    f = np.zeros(11)
+    f[5] = 1.0
+    chr_ = np.zeros(11)
+    chr_[6] = -1.0
+    out = diss_ex(lib, f, chr_, do_bdy=0)
+    assert out[5] == 1.0 and out[4] == 0.0   # one-sided branches off with do_bdy = 0
+    chr_ = np.zeros(11)
+    chr_[0] = -1.0                            # i = 1 excised: i = 2 takes w2 towards the right
+    g = np.zeros(11)
+    g[1] = 1.0
+    out = diss_ex(lib, g, chr_, do_bdy=0)
+    assert out[1] == 1 - 0.5 * 0.25
+
+
+def test_per_point_eps_with_negative_do_ex(lib):
+    f = np.zeros(9)
+    f[4] = 1.0
+    eps = np.full(9, 0.5)
+    eps[4] = 0.25
+    out = diss_ex(lib, f, np.zeros(9), eps=eps, do_ex=-1)
+    assert out[4] == 1 - 0.25 * 6 / 16 and out[3] == 0.5 * 4 / 16

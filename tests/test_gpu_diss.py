@@ -2,7 +2,8 @@
 the Fortran-ABI drop-in library on host arrays) against the oracle's
 restatement of dmdiss3d, bit for bit: 1-, 2- and 3-D grids, random data
 and masks, every face's parity (even, odd, neither) with do_bdy 0 and 1;
-f and work both compared. The excised path is refused."""
+f and work both compared; the excised variant with random excision masks,
+a scalar or per-point eps, and lines shorter than its stencils."""
 import ctypes as C
 
 import numpy as np
@@ -56,8 +57,43 @@ def test_dmdiss3d_matches_oracle(shape, do_bdy, seed):
     assert rc == 0
     assert np.array_equal(df.cpu().numpy(), want_f)
     assert np.array_equal(dw.cpu().numpy(), want_w)
-    assert rc == 0 and L.pgb_dmdiss3d(df.data_ptr(), dw.data_ptr(), de.data_ptr(), do_bdy, (C.c_int * 6)(*pbt),
-                                      EVEN, ODD, dm.data_ptr(), 0.0, *shape, None, 0.0, 1, None) == 12
+    assert L.pgb_dmdiss3d(df.data_ptr(), dw.data_ptr(), de.data_ptr(), do_bdy, (C.c_int * 6)(*pbt), EVEN, ODD,
+                          dm.data_ptr(), 0.0, *shape, None, 0.0, 1, None) == 3   # excising needs chr
+
+
+def _oracle_ex(f, eps, do_bdy, pbt, mask, shape, chr_, do_ex):
+    lib = C.CDLL(portrun.build())
+    f = f.copy()
+    work = np.zeros_like(f)
+    ci = lambda v: C.byref(C.c_int(v))  # noqa: E731
+    lib.dmdiss3d_(f.ctypes.data_as(D), work.ctypes.data_as(D), eps.ctypes.data_as(D), ci(do_bdy), (C.c_int * 6)(*pbt),
+                  ci(EVEN), ci(ODD), mask.ctypes.data_as(D), C.byref(C.c_double(0.0)), ci(shape[0]), ci(shape[1]),
+                  ci(shape[2]), chr_.ctypes.data_as(D), C.byref(C.c_double(-1.0)), ci(do_ex))
+    return f, work
+
+
+@pytest.mark.parametrize("shape", [(33, 29, 21), (41, 37, 1), (57, 1, 1), (5, 6, 7), (4, 3, 1)])
+@pytest.mark.parametrize("do_bdy", [0, 1])
+@pytest.mark.parametrize("do_ex", [1, -1])
+def test_excised_dmdiss3d_matches_oracle(shape, do_bdy, do_ex):
+    from pamr_amrd_gb300.solver import lib
+    f, mask, pbt, e0 = _case(sum(shape) + 7 * do_bdy + do_ex, shape)
+    rng = np.random.default_rng(sum(shape))
+    chr_ = np.where(rng.random(f.size) < 0.2, -1.0, 0.0)
+    eps = rng.uniform(0.1, 0.9, f.size) if do_ex < 0 else np.array([e0])
+    want_f, want_w = _oracle_ex(f, eps, do_bdy, pbt, mask, shape, chr_, do_ex)
+    df, dw = torch.from_numpy(f.copy()).cuda(), torch.zeros(f.size, dtype=torch.float64, device="cuda")
+    de, dm, dc = (torch.from_numpy(a.copy()).cuda() for a in (eps, mask, chr_))
+    L = lib()
+    L.pgb_dmdiss3d.argtypes = [C.c_void_p] * 3 + [C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_void_p,
+                                                  C.c_double] + [C.c_int] * 3 + [C.c_void_p, C.c_double, C.c_int,
+                                                                                 C.c_void_p]
+    rc = L.pgb_dmdiss3d(df.data_ptr(), dw.data_ptr(), de.data_ptr(), do_bdy, (C.c_int * 6)(*pbt), EVEN, ODD,
+                        dm.data_ptr(), 0.0, *shape, dc.data_ptr(), -1.0, do_ex, None)
+    torch.cuda.synchronize()
+    assert rc == 0
+    assert np.array_equal(df.cpu().numpy(), want_f)
+    assert np.array_equal(dw.cpu().numpy(), want_w)
 
 
 def test_fortran_abi_dmdiss3d_matches_oracle():
