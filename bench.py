@@ -48,8 +48,19 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 def _case(seed: int):
+    """the workload of rank `seed` (each replica solves its own source)"""
     from pamr_amrd_gb300 import workloads as W
     return W.conformal3d(129, 65, seed=seed)
+
+
+def max_over_ranks(x: float, dist, torch, device: str) -> float:
+    """the job's time is its slowest replica's: MAX over ranks (identity
+    without a process group); device "cuda" under NCCL, "cpu" under gloo"""
+    if not dist:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ------------------------------------------------------------ CPU side --
@@ -538,11 +549,7 @@ def main():
         ck = clk.stop() if clk else None
         if dist:
             dist.barrier()
-        total = sum(times)
-        if dist:
-            t = torch.tensor([total], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total = float(t.item())
+        total = max_over_ranks(sum(times), dist, torch, "cuda")
         return {"total_ms": total, "iters": iters, "finals": finals, "wall_ms": wall,
                 "launches": launches, "clocks": ck}
 
@@ -577,11 +584,7 @@ def main():
         for i in range(len(case.grids)):
             S._check(S.lib().pgb_get_grid(smx.h, i, S.C.cast(out_u[i].data_ptr(), dp)))
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_total = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = max_over_ranks(sum(e2e_ms), dist, torch, "cuda")
     e2e_value = world * args.steps / (e2e_total / 1e3)
 
     # roofline of the dominant smoother: FP32 sweep of the mixed form on the
