@@ -45,31 +45,76 @@ static unsigned grid_for(long n)
    return (unsigned)(b < 4864 ? (b < 1 ? 1 : b) : 4864);   /* 152 SMs x 32 */
 }
 
+/* Element-wise kernels: each thread handles BO_UNROLL elements a block
+ * stride apart per iteration, all loads issued before any store, so that
+ * enough loads are in flight to stream the arrays at HBM speed. */
+#define BO_UNROLL 4
+
 /* mgf0 = f1 etm1 + f2 etm2 (AMRD_MG_EXTRAP_2ND_FROM_ETM1) */
 __global__ void k_extrap_etm1(double *mgf0, const double *etm1, const double *etm2, double f1, double f2, long n)
 {
-   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x)
-      mgf0[j] = f1 * etm1[j] + f2 * etm2[j];
+   const long step = (long)gridDim.x * blockDim.x;
+   for (long j0 = blockIdx.x * (long)blockDim.x + threadIdx.x; j0 < n; j0 += BO_UNROLL * step) {
+      double a[BO_UNROLL], b[BO_UNROLL];
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         a[u] = j < n ? etm1[j] : 0.0;
+         b[u] = j < n ? etm2[j] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         if (j < n) mgf0[j] = f1 * a[u] + f2 * b[u];
+      }
+   }
 }
 
 /* mgf0 = mgf1 + (dt/dt_lm1) (etm2 - etm1) (AMRD_MG_EXTRAP_2ND_FROM_TN) */
 __global__ void k_extrap_tn(double *mgf0, const double *mgf1, const double *etm1, const double *etm2, double ratio,
                             long n)
 {
-   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x)
-      mgf0[j] = mgf1[j] + ratio * (etm2[j] - etm1[j]);
+   const long step = (long)gridDim.x * blockDim.x;
+   for (long j0 = blockIdx.x * (long)blockDim.x + threadIdx.x; j0 < n; j0 += BO_UNROLL * step) {
+      double m[BO_UNROLL], a[BO_UNROLL], b[BO_UNROLL];
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         m[u] = j < n ? mgf1[j] : 0.0;
+         a[u] = j < n ? etm1[j] : 0.0;
+         b[u] = j < n ? etm2[j] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         if (j < n) mgf0[j] = m[u] + ratio * (b[u] - a[u]);
+      }
+   }
 }
 
 /* etm2 = etm1, etm1 = mgf1, and with correct: etm2 += (etm1 - brs) f */
 __global__ void k_extrap_rotate(double *etm1, double *etm2, const double *mgf1, const double *brs, double f,
                                 int correct, long n)
 {
-   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
-      const double e1 = etm1[j], m = mgf1[j];
-      double e2 = e1;
-      etm1[j] = m;
-      if (correct) e2 += (m - brs[j]) * f;
-      etm2[j] = e2;
+   const long step = (long)gridDim.x * blockDim.x;
+   for (long j0 = blockIdx.x * (long)blockDim.x + threadIdx.x; j0 < n; j0 += BO_UNROLL * step) {
+      double e1[BO_UNROLL], m[BO_UNROLL], r[BO_UNROLL];
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         e1[u] = j < n ? etm1[j] : 0.0;
+         m[u] = j < n ? mgf1[j] : 0.0;
+         r[u] = (correct && j < n) ? brs[j] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < BO_UNROLL; u++) {
+         const long j = j0 + u * step;
+         if (j >= n) continue;
+         double e2 = e1[u];
+         if (correct) e2 += (m[u] - r[u]) * f;
+         etm1[j] = m[u];
+         etm2[j] = e2;
+      }
    }
 }
 

@@ -138,10 +138,10 @@ __global__ void k_diss_ex(double *f, const double *work, const double *eps, cons
                           const double *chr, double ex, int do_ex, int nx, int ny, int nz, int d, int pbt_lo,
                           int pbt_hi, int even, int odd, int bo1, int bo2)
 {
-   const long sy = nx, sz = (long)nx * ny, n = sz * nz;
-   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+   const int sy = nx, sz = nx * ny, n = sz * nz;   /* below 2^31 points (checked by the caller) */
+   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
       if (!(mask[c] != mask_off && chr[c] != ex)) continue;
-      const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / sz);
+      const int k = c / sz, r = c - k * sz, j = r / nx, i = r - j * nx;
       const double eps_eff = do_ex < 0 ? eps[c] : eps[0];
       double f_hf;
       if (d == 0)
@@ -159,11 +159,11 @@ __global__ void k_diss_ex(double *f, const double *work, const double *eps, cons
 __global__ void k_diss(double *f, const double *work, const double *eps, const double *mask, double mask_off,
                        int nx, int ny, int nz, int d, DissFace fc, int even, int odd)
 {
-   const long sy = nx, sz = (long)nx * ny, n = sz * nz;
+   const int sy = nx, sz = nx * ny, n = sz * nz;   /* below 2^31 points (checked by the caller) */
    const double eps_eff = eps[0];
-   for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
       if (mask[c] == mask_off) continue;
-      const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / sz);
+      const int k = c / sz, r = c - k * sz, j = r / nx, i = r - j * nx;
       double f_hf;
       if (d == 0)
          f_hf = diss_hf(work + c, 1, i + 1, nx, fc, even, odd);
@@ -181,6 +181,7 @@ extern "C" int pgb_dmdiss3d(double *f, double *work, const double *eps, int do_b
 {
    cudaStream_t st = (cudaStream_t)stream;
    if (nx < 1 || ny < 1 || nz < 1) return fail_diss("pgb_dmdiss3d: empty grid", 3);
+   if ((long)nx * ny * nz >= (1L << 31)) return fail_diss("pgb_dmdiss3d: grid of 2^31 points or more", 3);
    if (do_ex != 0 && !chr) return fail_diss("pgb_dmdiss3d: do_ex needs chr", 3);
    int cdo[6];
    for (int i = 0; i < 6; i++) {
