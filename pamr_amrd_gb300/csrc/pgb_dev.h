@@ -68,6 +68,7 @@ typedef struct {
    long smem_points;           /* points of the level's coarsest boxes (on-chip kernel) */
    int ncoarse;                /* number of coarsest boxes on the level */
    double omega;               /* mixed form: over-relaxation factor of the loop */
+   int inner_sweeps;           /* mixed form: FP32 sweeps per FP64 defect correction */
    double *snap;               /* 2 x (points of the coarsest boxes) doubles */
    long snap_points;
    const long *snap_off;       /* per level box: offset of its points in a snapshot */
@@ -107,13 +108,13 @@ unsigned long long pgb_dev_launches_lb(void);    /* pgb_linbnd.cu */
 const char *pgb_dev_error32(void);
 unsigned long long pgb_dev_launches32(void);
 int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover, void *stream);
-int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
-int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream);
-int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, void *stream);
+int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream);
+int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, int *slot, void *stream);
+int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot, void *stream);
 int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
-int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream);
+int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream);
 int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream);
-int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream);
+int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream);
 int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
                         double *norm_out, pgb_trace *trace, void *stream);
 int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);

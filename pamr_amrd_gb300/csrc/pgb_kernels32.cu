@@ -58,7 +58,15 @@ extern "C" const char *pgb_dev_error32(void) { return g_err32; }
 #define TWO_PI 6.283185307179586
 
 /* the FP32 arrays of a box: correction, defect, Jacobian term, coarse correction */
-enum { W_E = 0, W_D = 1, W_C = 2, W_X = 3, W_E2 = 4 };
+enum { W_E = PGB_W32_E, W_D = 1, W_C = 2, W_X = 3, W_E2 = PGB_W32_E2 };
+
+/* the correction array of slot sl (W_E or W_E2), selected without indexing
+ * a register copy of the box by a runtime value (which would move the copy
+ * to local memory) */
+__device__ __forceinline__ float *eslot(const pgb_dbox &b, int sl)
+{
+   return sl == W_E2 ? b.w32[W_E2] : b.w32[W_E];
+}
 
 __device__ __forceinline__ bool interior32(const pgb_dbox &b, int i, int j, int k, int dim)
 {
@@ -279,8 +287,8 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
    const int dim = lv.dim;
    const int tz = dim == 3 ? lv.tz : 1, hz = dim == 3 ? H : 0, nzl = tz + 2 * hz;
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   const float *e = b.w32[src];
-   float *eo = b.w32[dst];
+   const float *e = eslot(b, src);
+   float *eo = eslot(b, dst);
    const float *dd = b.w32[W_D], *cc = b.w32[W_C];
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
    const float j0 = b.fj0;
@@ -472,7 +480,7 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
    if (i >= b.n[0] || j >= b.n[1]) return;
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int kz = lv.dim == 3 ? lv.tz : 1;
-   const float *__restrict__ a = b.w32[src];
+   const float *__restrict__ a = eslot(b, src);
    float *__restrict__ e = b.w32[W_E];
    for (int kk = 0; kk < kz; kk++) {
       const int k = tl.k0 + kk;
@@ -487,14 +495,14 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
  * pre-smoothing on a level whose points outside the cover tiles do not
  * change in between (no sync, no injection there). The next FP64 residual
  * (after that pre-smoothing) is computed from u itself. */
-__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv)
+__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const float *__restrict__ e = b.w32[W_E];
+   const float *__restrict__ e = eslot(b, slot);
    const float *__restrict__ cc = b.w32[W_C];
    float *__restrict__ dd = b.w32[W_D];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
@@ -513,12 +521,16 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
    }
 }
 
-/* End of a smoothing block: u += E (FP64) and E = 0. After an interpolated
- * coarse-grid correction (post = 1) the points the smoother does not relax
- * take the FP64 correction the interpolation left in res, plus whatever a
- * sync of E brought in: u += res + (E - d2f(res)), exactly res when E still
- * holds the d2f(res) the interpolation wrote. */
-__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post)
+/* End of a smoothing block: u += E (FP64, E from the slot the sweeps
+ * ended in) and E = 0 in slot zslot, where the next block starts (the same
+ * slot costs no extra traffic). After an
+ * interpolated coarse-grid correction (post = 1) the points the smoother
+ * does not relax take the FP64 correction the interpolation left in res,
+ * plus whatever a sync of E brought in: u += res + (E - d2f(res)), exactly
+ * res when E still holds the d2f(res) the interpolation wrote (the fused
+ * sweeps copy unrelaxed points from slot to slot). */
+__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
+                                               int zslot)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
    const pgb_dbox b = boxes[tl.box];
@@ -526,14 +538,15 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
    if (i >= b.n[0] || j >= b.n[1]) return;
    const int kz = lv.dim == 3 ? lv.tz : 1;
    double *__restrict__ u = b.f[PGB_F_U];
-   float *__restrict__ e = b.w32[W_E];
+   const float *es = eslot(b, slot);
+   float *e = eslot(b, zslot);
    const double *__restrict__ res = b.f[PGB_F_RES];
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
       const int k = tl.k0 + kk;
       if (kk >= kz || k >= b.n[2]) continue;
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
-      double corr = f2d(e[p]);
+      double corr = f2d(es[p]);
       if (post && !relaxed32(b, i, j, k, p, lv.dim)) {
          const double r = res[p];
          corr += r - f2d(d2f(r));
@@ -565,15 +578,16 @@ __device__ __forceinline__ long lin32(const pgb_dbox &b, int i1, int j1, int k1)
    return (i1 - 1) + (long)b.n[0] * ((j1 - 1) + (long)b.n[1] * (k1 - 1));
 }
 
-/* FP32 copy of the correction along a sync plan (PAMR_sync of E) */
-__global__ void k_copy32(const pgb_dbox *boxes, const pgb_copy_op *ops)
+/* FP32 copy of the correction in slot `slot` along a sync plan (PAMR_sync
+ * of E) */
+__global__ void k_copy32(const pgb_dbox *boxes, const pgb_copy_op *ops, int slot)
 {
    const pgb_copy_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    OP_PLANES(o.ni, o.nj, o.nk, {
-      d.w32[W_E][lin32(d, o.i2 + a, o.j2 + bb, o.k2 + c)] =
-         s.w32[W_E][lin32(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
+      eslot(d, slot)[lin32(d, o.i2 + a, o.j2 + bb, o.k2 + c)] =
+         eslot(s, slot)[lin32(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
    })
 }
 
@@ -718,7 +732,7 @@ __device__ __noinline__ double interp_point64(const pgb_interp_op &o, const pgb_
  * small fraction of the FP32 rate, so FP64 points are kept in dense warps:
  * on boxes whose interior is all relaxed this kernel leaves the face rows
  * and the two x-ends of the other rows to k_interp_edges. */
-__global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
+__global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim, int slot)
 {
    const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
@@ -746,7 +760,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
          if (fp64) {
             const double v = interp_point64(o, s, a, bb, c, dim);
             d.f[PGB_F_RES][pd] = v;
-            d.w32[W_E][pd] = d2f(v);
+            eslot(d, slot)[pd] = d2f(v);
             continue;
          }
          int ax[4];
@@ -761,7 +775,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
             }
             kv[r] = wsum32(ny, cy, jv);
          }
-         d.w32[W_E][pd] = wsum32(nz, cz, kv);
+         eslot(d, slot)[pd] = wsum32(nz, cz, kv);
       }
    }
 }
@@ -769,14 +783,15 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
 /* k_interp_mixed for ops of ratio 2 and linear order (every MG hierarchy
  * with the default interpolation): the FP32 value of a fine point is the mean
  * of its (up to 8 distinct) coarse corners, counted with multiplicity. */
-__global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim)
+__global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim,
+                                                         int slot)
 {
    const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    const bool allrel = d.flags & PGB_BOX_BDY_INTERIOR;
    const float *__restrict__ x = s.w32[W_X];
-   float *__restrict__ e = d.w32[W_E];
+   float *__restrict__ e = eslot(d, slot);
    double *__restrict__ res = d.f[PGB_F_RES];
    const long sny = s.n[0], snz = (long)s.n[0] * s.n[1];
    const long dny = d.n[0], dnz = (long)d.n[0] * d.n[1];
@@ -815,7 +830,7 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
  * on a box face (j or k at the box boundary), blockIdx.y < 2*(njb+nkb)
  * picking the face and the row on it, and, for the remaining blockIdx.y,
  * the two x-ends (fi = 1, n) of the other rows, one per thread. */
-__global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, int dim)
+__global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, int dim, int slot)
 {
    const pgb_interp_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
@@ -841,7 +856,7 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
          const long pd = lin32(d, o.i2 + a, fj, fk);
          const double v = interp_point64(o, s, a, bb, c, dim);
          d.f[PGB_F_RES][pd] = v;
-         d.w32[W_E][pd] = d2f(v);
+         eslot(d, slot)[pd] = d2f(v);
       }
       return;
    }
@@ -857,7 +872,7 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
       const long pd = lin32(d, o.i2 + a, fj, fk);
       const double v = interp_point64(o, s, a, bb, c, dim);
       d.f[PGB_F_RES][pd] = v;
-      d.w32[W_E][pd] = d2f(v);
+      eslot(d, slot)[pd] = d2f(v);
    }
 }
 
@@ -984,13 +999,21 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
 
 /* The coarsest-grid loop of the mixed form (amrd/mg.c:172-190: relax the
  * coarsest grids, sync them, until the norm <= crtol x the first norm or
- * MG_max_citer) with the whole coarsest level held in shared memory by one
- * CTA. Each sweep is red-black successive over-relaxation with the factor
- * omega the host picks for the grid size: the residual r = L[u] - rhs and
- * the update u -= omega r / J are FP64, only the Jacobian J = dL/du steering
- * the step is FP32, so the iteration's fixed point is the FP64 solution.
- * The loop also stops once the norm has not improved for three sweeps (the
- * FP64 rounding floor). */
+ * MG_max_citer), as defect correction with the whole coarsest level in
+ * shared memory of one CTA:
+ *   r = L[u] - rhs in FP64 at the relaxed points and its norm (per-box RMS,
+ *   max over boxes); stop once it is <= crtol x the first one;
+ *   lap E + C E = -r from E = 0 by a fixed number of red-black SOR sweeps in
+ *   FP32 (factor omega and the count from the host, enough for a reduction
+ *   by crtol), the coarsest boxes' sync applied to E after each sweep;
+ *   u += E in FP64, and again from the FP64 residual.
+ * FP64 runs at 1/64 of the FP32 rate here, so the FP64 work is one residual
+ * pass per correction instead of one per sweep; the FP64 norm decides when
+ * to stop, so the result is the FP64 solution to crtol. A correction that
+ * fails to halve the FP64 norm means the rounding floor is reached, and the
+ * loop stops there. Each thread's points of either colour are listed once
+ * (relaxed points only), so no sweep recomputes indices. Sweeps count
+ * against MG_max_citer. */
 #define CM_MAXB 16
 #define CMT 256
 __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
@@ -999,68 +1022,71 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
 {
    extern __shared__ double dsm[];
    __shared__ double sm[32];
-   __shared__ int cb[CM_MAXB], ncb_s;
-   __shared__ long coff[CM_MAXB + 1];
+   __shared__ int cb[CM_MAXB], coff[CM_MAXB + 1], ncol[CM_MAXB][2], ncb_s;
    const int t = threadIdx.x, dim = lv.dim;
+   const bool d3 = dim == 3;
    if (t == 0) {
-      int n = 0;
-      long o = 0;
+      int n = 0, o = 0;
       for (int b = 0; b < lv.nbox && n < CM_MAXB; b++) {
          const pgb_dbox &bx = boxes[lv.box[b]];
          if (!(bx.flags & PGB_BOX_COARSEST)) continue;
          cb[n] = b;
          coff[n] = o;
-         o += (long)bx.n[0] * bx.n[1] * bx.n[2];
+         ncol[n][0] = ncol[n][1] = 0;
+         o += bx.n[0] * bx.n[1] * bx.n[2];
          n++;
       }
       coff[n] = o;
       ncb_s = n;
    }
    __syncthreads();
-   const int ncb = ncb_s;
-   const long tot = coff[ncb];
-   double *su = dsm, *srhs = dsm + tot, *ssrc = dsm + 2 * tot;
+   const int ncb = ncb_s, tot = coff[ncb];
+   double *su = dsm;
+   float *se = (float *)(dsm + tot), *sd = se + tot, *sc = sd + tot;
+   int *sl = (int *)(sc + tot);   /* per box: colour-0 points from the front, colour-1 from the back */
    for (int c = 0; c < ncb; c++) {
       const pgb_dbox &bx = boxes[lv.box[cb[c]]];
-      const long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-      for (long q = t; q < n; q += CMT) {
+      const int n = bx.n[0] * bx.n[1] * bx.n[2];
+      for (int q = t; q < n; q += CMT) {
          su[coff[c] + q] = bx.f[PGB_F_U][q];
-         srhs[coff[c] + q] = bx.f[PGB_F_RHS][q];
-         ssrc[coff[c] + q] = bx.f[PGB_F_SRC][q];
+         se[coff[c] + q] = 0.f;
+      }
+      const int sy = bx.n[0], sz = bx.n[0] * bx.n[1];
+      const int ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = d3 ? bx.n[2] - 2 : 1;
+      for (int q = t; q < ni * nj * nk; q += CMT) {
+         const int i = 1 + q % ni, j = 1 + (q / ni) % nj, k = d3 ? 1 + q / (ni * nj) : 0;
+         const int p = i + sy * j + sz * k;
+         if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+         /* colour: the pass of num.f:220's red-black order */
+         const int col = d3 ? ((i + j + k + 1) & 1) : ((i + j) & 1);
+         const int slot = atomicAdd(&ncol[c][col], 1);
+         sl[coff[c] + (col ? n - 1 - slot : slot)] = p;
       }
    }
    __syncthreads();
    const float omega = (float)a.omega;
-   double ctol = -1.0, res = 0.0, best = 0.0;
-   int iter = 0, stall = 0;
-   while (iter < a.max_citer) {
+   double ctol = -1.0, res = 0.0, prev = 0.0;
+   int sweeps = 0;
+   for (;;) {
+      /* FP64 residual: D = -r, C, norm */
       double lres = 0;
       for (int c = 0; c < ncb; c++) {
-         const pgb_dbox bx = boxes[lv.box[cb[c]]];
-         double *u = su + coff[c];
-         const double *rhs = srhs + coff[c], *src = ssrc + coff[c];
-         const long sy = bx.n[0], sz = (long)bx.n[0] * bx.n[1];
-         const long ni = bx.n[0] - 2, nj = bx.n[1] - 2, nk = dim == 3 ? bx.n[2] - 2 : 1;
-         const long hw = (ni + 1) / 2, nslot = hw * nj * nk;   /* one slot per point of a colour */
-         const float j0 = bx.fj0;
+         const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+         const double *u = su + coff[c];
+         const double *__restrict__ rhs = bx.f[PGB_F_RHS];
+         const double *__restrict__ src = bx.f[PGB_F_SRC];
+         float *d = sd + coff[c], *cj = sc + coff[c];
+         const int *lst = sl + coff[c];
+         const int n = bx.n[0] * bx.n[1] * bx.n[2], nrel = ncol[c][0] + ncol[c][1];
+         const int sy = bx.n[0], sz = bx.n[0] * bx.n[1];
          double acc = 0;
-         for (int pass = 0; pass < 2; pass++) {
-            for (long q = t; q < nslot; q += CMT) {
-               const int j = 1 + (int)((q / hw) % nj);
-               const int k = dim == 3 ? 1 + (int)(q / (hw * nj)) : 0;
-               const int off = dim == 3 ? ((j + k + pass) & 1) : ((j + 1 + pass) & 1);
-               const int i = 1 + 2 * (int)(q % hw) + off;
-               if (i > ni) continue;
-               const long p = i + sy * j + sz * k;
-               if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
-               const double uc = u[p];
-               float cj;
-               const double r = opjac(pde, lapm(bx, u, p, sy, sz, dim), uc, src[p], cj) - rhs[p];
-               const float step = __fdividef(omega, j0 + cj);
-               u[p] = fma(-(double)step, r, uc);
-               acc = fma(r, r, acc);
-            }
-            __syncthreads();
+         for (int q = t; q < nrel; q += CMT) {
+            const int p = lst[q < ncol[c][0] ? q : n - nrel + q];
+            float cv;
+            const double r = opjac(pde, lapm(bx, u, p, sy, sz, dim), u[p], src[p], cv) - rhs[p];
+            d[p] = d2f(-r);
+            cj[p] = cv;
+            acc = fma(r, r, acc);
          }
          acc = block_sum32(acc, sm);
          if (t == 0) {
@@ -1068,58 +1094,87 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
             if (c == 0) lres = r;
             lres = (r > lres) ? r : lres;
             if (trace) {
-               const int n = trace->n;
-               if (n < trace->cap) {
-                  pgb_trace_rec rr = {0, lv.level, cb[c], 1, r};
-                  trace->rec[n] = rr;
-                  trace->n = n + 1;
+               const int nt = trace->n;
+               if (nt < trace->cap) {
+                  pgb_trace_rec *rr = &trace->rec[nt];
+                  rr->kind = 0;
+                  rr->level = lv.level;
+                  rr->box = cb[c];
+                  rr->repeat = 1;
+                  rr->norm = r;
+                  trace->n = nt + 1;
                } else
                   trace->overflow = 1;
             }
          }
       }
-      for (int o = 0; o < nsync; o++) {   /* PAMR_sync(L,0,MGH,1) over the coarsest grids */
-         const pgb_copy_op op = sync_ops[o];
-         int cs = -1, cd = -1;
-         for (int c = 0; c < ncb; c++) {
-            if (lv.box[cb[c]] == op.src_box) cs = c;
-            if (lv.box[cb[c]] == op.dst_box) cd = c;
-         }
-         if (cs < 0 || cd < 0) continue;
-         const pgb_dbox &bs = boxes[op.src_box];
-         const pgb_dbox &bd = boxes[op.dst_box];
-         const long np = (long)op.ni * op.nj * op.nk;
-         for (long q = t; q < np; q += CMT) {
-            const int aa = (int)(q % op.ni), bb = (int)((q / op.ni) % op.nj),
-                      cc = (int)(q / ((long)op.ni * op.nj));
-            su[coff[cd] + lin32(bd, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
-               su[coff[cs] + lin32(bs, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
-         }
-         __syncthreads();
-      }
       if (t == 0) sm[0] = lres;
       __syncthreads();
       res = sm[0];
       __syncthreads();
-      iter++;
-      if (ctol < 0) {
+      if (ctol < 0)
          ctol = res * a.crtol;
-         best = res;
-      } else if (res < best) {
-         best = res;
-         stall = 0;
-      } else if (++stall >= 3)
-         break;
-      if (res <= ctol) break;
+      else if (!(res <= 0.5 * prev))
+         break;   /* the last correction did not halve the norm: rounding floor */
+      if (res <= ctol || sweeps >= a.max_citer) break;
+      prev = res;
+      /* FP32 SOR on the correction */
+      for (int it = 0; it < a.inner_sweeps && sweeps < a.max_citer; it++, sweeps++) {
+         for (int pass = 0; pass < 2; pass++) {
+            for (int c = 0; c < ncb; c++) {
+               const pgb_dbox &bx = boxes[lv.box[cb[c]]];
+               float *e = se + coff[c];
+               const float *d = sd + coff[c], *cj = sc + coff[c];
+               const int n = bx.n[0] * bx.n[1] * bx.n[2], m = ncol[c][pass];
+               const int *lst = sl + coff[c] + (pass ? n - m : 0);
+               const int sy = bx.n[0], sz = bx.n[0] * bx.n[1];
+               const float ix = bx.fidx2[0], iy = bx.fidx2[1], iz = bx.fidx2[2], j0 = bx.fj0;
+               for (int q = t; q < m; q += CMT) {
+                  const int p = lst[q];
+                  const float ec = e[p], m2 = -2.f * ec, cp = cj[p];
+                  float tl = __fmul_rn(__fadd_rn(__fadd_rn(e[p + 1], m2), e[p - 1]), ix);
+                  tl = __fmaf_rn(__fadd_rn(__fadd_rn(e[p + sy], m2), e[p - sy]), iy, tl);
+                  if (d3) tl = __fmaf_rn(__fadd_rn(__fadd_rn(e[p + sz], m2), e[p - sz]), iz, tl);
+                  const float r = __fsub_rn(__fmaf_rn(cp, ec, tl), d[p]);
+                  e[p] = __fsub_rn(ec, __fdividef(omega * r, __fadd_rn(j0, cp)));
+               }
+            }
+            __syncthreads();
+         }
+         for (int o = 0; o < nsync; o++) {   /* PAMR_sync(L,0,MGH,1) over the coarsest grids, on E */
+            const pgb_copy_op op = sync_ops[o];
+            int cs = -1, cd = -1;
+            for (int c = 0; c < ncb; c++) {
+               if (lv.box[cb[c]] == op.src_box) cs = c;
+               if (lv.box[cb[c]] == op.dst_box) cd = c;
+            }
+            if (cs < 0 || cd < 0) continue;
+            const pgb_dbox &bs = boxes[op.src_box];
+            const pgb_dbox &bd = boxes[op.dst_box];
+            const int np = op.ni * op.nj * op.nk;
+            for (int q = t; q < np; q += CMT) {
+               const int aa = q % op.ni, bb = (q / op.ni) % op.nj, cc = q / (op.ni * op.nj);
+               se[coff[cd] + lin32(bd, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
+                  se[coff[cs] + lin32(bs, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
+            }
+            __syncthreads();
+         }
+      }
+      /* u += E where E was set (relaxed and synced points; 0 elsewhere) */
+      for (int q = t; q < tot; q += CMT) {
+         su[q] += f2d(se[q]);
+         se[q] = 0.f;
+      }
+      __syncthreads();
    }
    for (int c = 0; c < ncb; c++) {
       const pgb_dbox &bx = boxes[lv.box[cb[c]]];
-      const long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-      for (long q = t; q < n; q += CMT) bx.f[PGB_F_U][q] = su[coff[c] + q];
+      const int n = bx.n[0] * bx.n[1] * bx.n[2];
+      for (int q = t; q < n; q += CMT) bx.f[PGB_F_U][q] = su[coff[c] + q];
    }
    if (t == 0) {
       *a.res_out = res;
-      if (a.iters_out) *a.iters_out += iter;
+      if (a.iters_out) *a.iters_out += sweeps;
    }
 }
 
@@ -1133,21 +1188,30 @@ extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, d
    return check32("fas_defect");
 }
 
-extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
+extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream)
 {
    if (!lv.ntiles) return 0;
-   k_defect32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   k_defect32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot);
    return check32("defect32");
 }
 
-/* nsweep FP32 sweeps of level L, fuse sweeps per launch (1 or 2) */
 /* nsweep FP32 sweeps of level L: fuse = 0 two global-memory colour passes
- * per sweep; 1 or 2 = sweeps per launch of the shared-memory kernel */
-extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, void *stream)
+ * per sweep (in place, slot W_E); 1 or 2 = sweeps per launch of the
+ * shared-memory kernel, 3 = the one-pass marching kernel (3-D). The fused
+ * kernels read one slot and write the other; *slot says where the
+ * correction starts and, on return, where it ends, which the block's
+ * consumers (sync, defect, update) read. */
+extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, int *slot,
+                             void *stream)
 {
-   int done = 0, src = W_E, dst = W_E2;
+   int done = 0, src = *slot, dst = src == W_E ? W_E2 : W_E;
    if (!lv.ntiles) return 0;
    if (fuse <= 0) {   /* in place, one launch per colour pass */
+      if (src != W_E) {
+         k_copy_e<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src);
+         if (check32("copy_e")) return 1;
+         *slot = W_E;
+      }
       for (; done < nsweep; done++) {
          k_relax32<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, 0);
          if (check32("relax32")) return 1;
@@ -1173,17 +1237,15 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
       src = dst;
       dst = t;
    }
-   if (src != W_E) {
-      k_copy_e<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src);
-      if (check32("copy_e")) return 1;
-   }
+   *slot = src;
    return 0;
 }
 
-extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, void *stream)
+extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot,
+                            void *stream)
 {
    if (!lv.ntiles) return 0;
-   k_update<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post);
+   k_update<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot);
    return check32("update");
 }
 
@@ -1194,7 +1256,7 @@ extern "C" int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
    return check32("zero32");
 }
 
-extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stream)
+extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream)
 {
    const pgb_copy_op *h = (const pgb_copy_op *)p->h_ops, *d = (const pgb_copy_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
@@ -1203,7 +1265,7 @@ extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, void *stre
          const int m = n - c0 < 65535 ? n - c0 : 65535;
          dim3 g;
          plane_grid(h + p->batch_start[bt] + c0, m, g);
-         k_copy32<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0);
+         k_copy32<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, slot);
          if (check32("copy32")) return 1;
       }
    }
@@ -1217,7 +1279,7 @@ extern "C" int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_
    return check32("cgc_mixed");
 }
 
-extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, void *stream)
+extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream)
 {
    const pgb_interp_op *h = (const pgb_interp_op *)p->h_ops, *d = (const pgb_interp_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
@@ -1235,9 +1297,9 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
                lin2 = 0;
          }
          if (lin2)
-            k_interp_lin2<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+            k_interp_lin2<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim, slot);
          else
-            k_interp_mixed<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim);
+            k_interp_mixed<<<g, 128, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, dim, slot);
          if (check32("interp_mixed")) return 1;
          {
             int mi = 1;
@@ -1248,7 +1310,7 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
             }
             long gy = mf + (2 * mr + 127) / 128;   /* face rows, then x-end chunks */
             k_interp_edges<<<dim3((unsigned)((mi + 127) / 128), (unsigned)(gy > 65535 ? 65535 : gy), (unsigned)m),
-                             128, 0, (cudaStream_t)stream>>>(d + p->batch_start[bt] + c0, boxes, dim);
+                             128, 0, (cudaStream_t)stream>>>(d + p->batch_start[bt] + c0, boxes, dim, slot);
             if (check32("interp_edges")) return 1;
          }
       }
@@ -1277,7 +1339,8 @@ extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
 extern "C" int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                                     pgb_coarsest_args a, pgb_trace *trace, void *stream)
 {
-   const size_t smem = (size_t)a.smem_points * 3 * sizeof(double);
+   /* u (FP64), E, D, C (FP32) and the point lists (int) per point */
+   const size_t smem = (size_t)a.smem_points * (sizeof(double) + 3 * sizeof(float) + sizeof(int));
    static int attr_set = 0;
    if (a.smem_points <= 0 || a.ncoarse > CM_MAXB || smem > 200 * 1024) return 1;
    if (!attr_set) {

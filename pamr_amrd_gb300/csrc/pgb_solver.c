@@ -41,6 +41,7 @@ struct pgb_solver {
    double *h_res;           /* pinned */
    int prepared;            /* pgb_prepare ran after the last change of an input grid */
    int fuse[PGB_MAXLEV + 1]; /* mixed form: FP32 sweeps per launch on levels without syncs */
+   int eslot[PGB_MAXLEV + 1]; /* mixed form: slot of E = 0 after a level's pre-smoothing block */
    int tuned;               /* the autotuner has run */
    int dnext[PGB_MAXLEV + 1]; /* mixed form: pre-smoothing defect from the FP32 update (see
                                k_defect32) outside the cover tiles */
@@ -627,7 +628,8 @@ static int autotune(pgb_solver *s)
             int r;
             for (r = 0; r < 4; r++) {   /* one warm-up, three timed */
                if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));
-               KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, s->stream));
+               int slot = PGB_W32_E;
+               KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, &slot, s->stream));
                KC32(pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0,
                                         s->stream));
             }
@@ -745,6 +747,13 @@ static void coarsest_args(pgb_solver *s, int L, pgb_coarsest_args *a)
    a->ctol_from_first = mixed;
    /* red-black SOR factor of the model problem, 2/(1 + sin(pi h)) */
    a->omega = nmax > 3 ? 2.0 / (1.0 + sin(3.141592653589793 / (nmax - 1))) : 1.0;
+   {
+      /* enough sweeps for the SOR error (about k (omega-1)^k after k sweeps)
+       * to fall below crtol/4 in one correction */
+      double rho = a->omega - 1.0 > 0.2 ? a->omega - 1.0 : 0.2, tgt = p->crtol > 0 ? p->crtol / 4 : 1e-6;
+      int m = (int)ceil(log(tgt) / log(rho)) + 3;
+      a->inner_sweeps = m < 2 ? 2 : m > 64 ? 64 : m;
+   }
    a->snap = s->d_snap;
    a->snap_points = s->snap_points;
    a->snap_off = s->d_snap_off[L];
@@ -793,18 +802,20 @@ static int vcycle_fp64(pgb_solver *s)
    return 0;
 }
 
-/* FP32 sweeps on the correction E of level L, synced between boxes like u */
-static int sweeps32(pgb_solver *s, int L, int nsweep)
+/* FP32 sweeps on the correction E of level L, synced between boxes like u;
+ * the block starts from slot *slot, which receives the slot it ends in */
+static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
 {
    pgb_hier *h = &s->h;
    int it;
    if (!h->sync[L][0].nops && !h->sync[L][1].nops) {
-      KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsweep, s->fuse[L], s->stream));
+      KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsweep, s->fuse[L], slot, s->stream));
       return 0;
    }
    for (it = 0; it < nsweep; it++) {
-      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] == 2 ? 1 : s->fuse[L], s->stream));
-      if (h->sync[L][it ? 1 : 0].nops) KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], s->stream));
+      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] == 2 ? 1 : s->fuse[L], slot, s->stream));
+      if (h->sync[L][it ? 1 : 0].nops)
+         KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], *slot, s->stream));
    }
    return 0;
 }
@@ -832,19 +843,27 @@ static int vcycle_mixed(pgb_solver *s)
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
       }
+      /* the correction slots: every cycle starts each level from E = 0 in
+       * PGB_W32_E; the pre-smoothing block leaves E = 0 in the slot it ends
+       * in, where the post-smoothing block starts, and that block zeroes
+       * PGB_W32_E again (which the captured graph relies on) */
+      s->eslot[L] = PGB_W32_E;
       if (L > 1 && p->pre_swp > 0) {
-         if (sweeps32(s, L, p->pre_swp)) return 11;
-         KC32(pgb_k_update(s->dbox, s->lv[L], 0, s->stream));
+         int slot = PGB_W32_E;
+         if (sweeps32(s, L, p->pre_swp, &slot)) return 11;
+         KC32(pgb_k_update(s->dbox, s->lv[L], 0, slot, slot, s->stream));
+         s->eslot[L] = slot;
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       }
    }
    for (L = 1; L <= Lf; L++) {
       if (L > 1) {
+         int slot = s->eslot[L];
          KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
-         if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, s->stream));
-         if (sweeps32(s, L, p->pst_swp)) return 11;
-         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], s->stream));
-         KC32(pgb_k_update(s->dbox, s->lv[L], 1, s->stream));
+         if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream));
+         if (sweeps32(s, L, p->pst_swp, &slot)) return 11;
+         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->stream));
+         KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       } else if (lvl_coarsest(s, L)) {
          pgb_coarsest_args a;
@@ -981,7 +1000,8 @@ int pgb_time_relax(pgb_solver *s, int L, int reps, double *ms_per_sweep, double 
    s->prepared = 0;   /* the sweeps change the level: the next cycle starts from pgb_prepare */
    for (r = 0; r <= reps; r++) {
       if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));   /* first block warms up */
-      if (mixed) KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, s->fuse[L], s->stream));
+      int slot = PGB_W32_E;
+      if (mixed) KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, s->fuse[L], &slot, s->stream));
       else if (relax(s, L, N_RELAX_UP)) return 11;
    }
    CU(cudaEventRecord(s->ev1, s->stream));
