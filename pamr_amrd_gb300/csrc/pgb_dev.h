@@ -90,8 +90,9 @@ int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, vo
 int pgb_k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv, double w0_i, void *stream);
 int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream);
-/* restricts the fields of field_mask (bit f = grid function f) that the plan's ops carry */
-int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, void *stream);
+/* restricts the fields of field_mask (bit f = grid function f) that the plan's ops carry;
+ * res32 = 1: the full weighting of res from the mixed form's FP32 copy of -res */
+int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, int res32, void *stream);
 int pgb_k_interp(const pgb_dbox *boxes, const pgb_plan *p, int field, int dim, void *stream);
 int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                    pgb_coarsest_args a, pgb_trace *trace, void *stream);

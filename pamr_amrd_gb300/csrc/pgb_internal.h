@@ -33,6 +33,7 @@ enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, 
 /* device view of one MG box (all pointers are device pointers) */
 #define PGB_NW32 5   /* FP32 work arrays per box (mixed form) */
 #define PGB_W32_E 0   /* slot of the correction E a smoothing block starts from */
+#define PGB_W32_D 1   /* FP32 defect D (-res after the residual pass) */
 #define PGB_W32_E2 4  /* second correction slot of the fused sweeps */
 
 typedef struct {

@@ -894,7 +894,7 @@ __device__ double block_sum32(double v, double *sm)
 /* app_MG_residual (num.f:128-175 pattern) in FP64: res = L[u] - rhs at the
  * relaxed points, D = -res and C for the next smoothing block of this
  * level, and call_rr_app's norm (per-box RMS, max over boxes) reduced by the
- * last CTA to finish. */
+ * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
                                                       pgb_trace *trace)
@@ -928,12 +928,13 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
             res[p] = r;
             wd[p] = d2f(-r);
             wc[p] = c;
-            acc = fma(r, r, acc);
+            if (norm_out) acc = fma(r, r, acc);
          }
          zm = uc;
          uc = zp;
       }
    }
+   if (!norm_out) return;
    acc = block_sum32(acc, sm);
    if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
    __threadfence();

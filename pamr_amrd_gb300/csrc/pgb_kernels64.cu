@@ -465,9 +465,51 @@ __device__ double fwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0
 }
 #undef ACC
 
+/* fwr of the residual in FP32 for the mixed form: the same weights and sums
+ * over D, the FP32 copy of -res that the mixed form's residual pass leaves
+ * at the points where it writes res (0 wherever res is 0). The restricted
+ * residual only steers the coarse-grid correction, so FP32 is enough; the
+ * FP64 residual of the finest level still decides convergence. */
+__device__ double fwr_d32(const float *dd, int nx1, int ny1, int nz1, int i0, int j0, int k0)
+{
+   const int sy = nx1, sz = nx1 * ny1;
+   const int p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
+   bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
+   int s0, s1, s2, n0, n1;
+   float scale;
+   if (ii && jj && kk) {
+      s0 = sz; s1 = sy; s2 = 1; n0 = n1 = 3; scale = 1.f / 64.f;
+   } else if (ii && jj) {
+      s0 = 0; s1 = sy; s2 = 1; n0 = 1; n1 = 3; scale = 1.f / 16.f;
+   } else if (jj && kk) {
+      s0 = 0; s1 = sy; s2 = sz; n0 = 1; n1 = 3; scale = 1.f / 16.f;
+   } else if (ii && kk) {
+      s0 = 0; s1 = 1; s2 = sz; n0 = 1; n1 = 3; scale = 1.f / 16.f;
+   } else if (ii || jj || kk) {
+      s0 = 0; s1 = 0; s2 = ii ? 1 : (jj ? sy : sz); n0 = n1 = 1; scale = 0.25f;
+   } else
+      return -(double)dd[p];
+   float acc = 0.f;
+#pragma unroll
+   for (int a = 0; a < 3; a++) {
+      if (a >= n0) break;
+      const int da = n0 == 3 ? a - 1 : 0;
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+         if (b >= n1) break;
+         const int db = n1 == 3 ? b - 1 : 0;
+         const float wab = (float)((da == 0 ? 2 : 1) * (db == 0 ? 2 : 1) >> (n0 == 1 ? 1 : 0) >> (n1 == 1 ? 1 : 0));
+         const float *r = dd + p + da * s0 + db * s1;
+         acc = __fmaf_rn(wab, __fadd_rn(__fadd_rn(r[-s2], 2.f * r[0]), r[s2]), acc);
+      }
+   }
+   return -(double)__fmul_rn(acc, scale);
+}
+
 /* local_transfer delta = +1 (src/transfer.c:1126-1149): per grid function
- * straight injection, half weighting or full weighting */
-__global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, int field_mask)
+ * straight injection, half weighting or full weighting; res32 = 1 (mixed
+ * form) takes the full weighting of the residual from its FP32 copy */
+__global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, int field_mask, int res32)
 {
    const pgb_restrict_op o = ops[blockIdx.z];
    const pgb_dbox &s = boxes[o.src_box];
@@ -482,6 +524,7 @@ __global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, in
          double v;
          if (op == 1) v = u[lin(s, i0, j0, k0)];
          else if (op == 2) v = hwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
+         else if (res32 && f == PGB_F_RES) v = fwr_d32(s.w32[PGB_W32_D], s.n[0], s.n[1], s.n[2], i0, j0, k0);
          else v = fwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
          d.f[f][pd] = v;
       }
@@ -599,7 +642,8 @@ extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, v
    return check("copy");
 }
 
-extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, void *stream)
+extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, int res32,
+                              void *stream)
 {
    const pgb_restrict_op *h = (const pgb_restrict_op *)p->h_ops, *d = (const pgb_restrict_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
@@ -608,7 +652,8 @@ extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int fiel
          const int m = n - c0 < 65535 ? n - c0 : 65535;
          dim3 g;
          plane_grid(h + p->batch_start[bt] + c0, m, g);
-         k_restrict<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, field_mask);
+         k_restrict<<<g, 256, 0, (cudaStream_t)stream>>>(boxes, d + p->batch_start[bt] + c0, field_mask,
+                                                         res32);
          LAUNCHED(1);
       }
    }

@@ -42,6 +42,7 @@ struct pgb_solver {
    int prepared;            /* pgb_prepare ran after the last change of an input grid */
    int fuse[PGB_MAXLEV + 1]; /* mixed form: FP32 sweeps per launch on levels without syncs */
    int eslot[PGB_MAXLEV + 1]; /* mixed form: slot of E = 0 after a level's pre-smoothing block */
+   int res32[PGB_MAXLEV + 1]; /* mixed form: level's residual restricted from its FP32 copy */
    int tuned;               /* the autotuner has run */
    int dnext[PGB_MAXLEV + 1]; /* mixed form: pre-smoothing defect from the FP32 update (see
                                k_defect32) outside the cover tiles */
@@ -676,16 +677,38 @@ int pgb_prepare(pgb_solver *s)
       KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
    }
    for (L = s->h.nlev - 1; L >= 1; L--)
-      if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, s->stream));
+      if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, 0, s->stream));
    if (s->h.prm.precision == PGB_MIXED) {
       if (!s->tuned) {
          int rc = autotune(s);
          if (rc) return rc;
       }
-      /* FP32 correction arrays start at 0; the finest level's first
-       * pre-smoothing defect is the initial residual */
-      for (L = 1; L <= s->h.nlev; L++)
+      /* FP32 correction arrays start at 0 (D stays 0 wherever res is never
+       * computed); the finest level's first pre-smoothing defect is the
+       * initial residual */
+      for (L = 1; L <= s->h.nlev; L++) {
+         KC(pgb_k_clear(s->dbox, s->lv[L], (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS), s->stream));
          if (pgb_k_zero32(s->dbox, s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
+      }
+      /* A level's residual is restricted from its FP32 copy D = -res when no
+       * sync writes res there and the restriction of res is full weighting
+       * (D is 0 wherever res is not computed). The V-cycle's clear of res
+       * then only protects FP64 reads of res at points not rewritten in the
+       * same cycle, and there are none: the FAS right-hand side reads res
+       * at child-covered points, which the restriction rewrites first
+       * (test_plans.py checks that inclusion); the coarse correction and
+       * the interpolation rewrite what the interpolation and the update
+       * read. Such levels skip the clear; pgb_prepare clears once. */
+      for (L = 1; L <= s->h.nlev; L++) {
+         const pgb_hier *h = &s->h;
+         int i, ok = L == 1 || !h->sync[L][0].nops;
+         if (L > 1)
+            for (i = 0; i < h->inject[L - 1].nops && ok; i++) {
+               const int op = ((const pgb_restrict_op *)h->inject[L - 1].h_ops)[i].op[PGB_F_RES];
+               if (op != 0 && op != 3) ok = 0;
+            }
+         s->res32[L] = ok;
+      }
       if (pgb_k_residual_fast(s->dbox, s->lv[s->h.nlev], s->h.pde, s->sc,
                               norm_slot(s, s->h.nlev, N_RESID), 0, s->stream))
          return fail(11, "%s", pgb_dev_error32());
@@ -777,7 +800,7 @@ static int vcycle_fp64(pgb_solver *s)
           * out: it reads and writes the same values every cycle, and
           * pgb_prepare's build-time injection (same ops, same operator) has
           * already put them in place */
-         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->stream));
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), 0, s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
@@ -831,14 +854,20 @@ static int vcycle_mixed(pgb_solver *s)
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
    int L, Lf = h->nlev;
-   KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
+   /* clear_MG_vars: only where an FP64 read could see a value of an earlier
+    * cycle (see pgb_prepare) */
+   if (!s->res32[Lf])
+      KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
       if (L < Lf) {
-         KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
-                                  s->d_trace, s->stream));
+         /* this norm is only ever traced (the finest level's convergence
+          * norm comes from the residual after post-smoothing) */
+         KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc,
+                                  s->d_trace ? norm_slot(s, L + 1, N_RESID) : 0, s->d_trace, s->stream));
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
-         KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
-         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->stream));
+         if (!s->res32[L]) KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
+         if (h->inject[L].nops)
+            KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->res32[L + 1], s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));

@@ -53,3 +53,30 @@ def test_invalid_inputs_are_errors_not_exits():
     case.grids[0] = W.Grid(0, case.grids[0].bbox, case.grids[0].shape)
     with pytest.raises(PgbError):
         Solver(case, host_only=True)
+
+
+@pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=3),
+                                  lambda: W.poisson2d_uneven(seed=4, n=129, levels=5, min_boxes=8,
+                                                             max_boxes=16),
+                                  lambda: W.lapse2d_bo(65, seed=5, levels=4, step=120)]
+                         + [lambda p=p: G.load(p)[0] for p in G.files()],
+                         ids=["c3d65", "uneven129", "lapse65"] + [p.split("/")[-1][:-4] for p in G.files()])
+def test_child_covered_points_are_restricted(make):
+    """Every child-covered point (cmask_child on) of a level is written by
+    the restriction of res into it, so the FAS right-hand side never reads
+    a res value of an earlier cycle (the mixed form skips the clear of res
+    on levels whose residual is restricted from its FP32 copy)."""
+    s = Solver(make(), host_only=True)
+    for L in range(1, s.num_levels()):
+        ops = s.plan(3, L)
+        for idx in range(s.level_nbox(L)):
+            sh = s.box_info(L, idx)["shape"]
+            cm = s.cmask(L, idx, "child").reshape(sh[2], sh[1], sh[0]) != 0
+            covered = np.zeros_like(cm)
+            for r in ops:
+                if r[2] != L or r[3] != idx or r[14 + 2] == 0:   # dst level/box, op of res
+                    continue
+                i2, j2, k2, ni, nj, nk = r[7:13]
+                covered[k2 - 1:k2 - 1 + nk, j2 - 1:j2 - 1 + nj, i2 - 1:i2 - 1 + ni] = True
+            assert not np.any(cm & ~covered), (L, idx)
+    s.close()
