@@ -54,6 +54,7 @@ typedef struct {
    double *partial;            /* >= 2 * max tiles of any level */
    unsigned int *counter;      /* one word, zero between kernels */
    double *box_norm;           /* >= max boxes of any level */
+   long npartial;              /* entries of partial */
 } pgb_scratch;
 
 /* parameters of the coarsest-grid loop (amrd/mg.c:172-190) */
@@ -111,6 +112,11 @@ unsigned long long pgb_dev_launches32(void);
 int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover, void *stream);
 int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream);
 int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, int *slot, void *stream);
+/* the device solve loop's step: records the finest norm of cycle *it,
+ * counts the cycle and sets the while node's condition to pgb_solve's loop
+ * test ((it < min_iter || res > tol) && it < max_iter) */
+int pgb_k_solve_step(unsigned long long handle, const double *norm, double *hist, int *it, int min_iter,
+                     int max_iter, double tol, void *stream);
 int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot, void *stream);
 int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream);

@@ -80,6 +80,35 @@ __device__ __forceinline__ bool relaxed32(const pgb_dbox &b, int i, int j, int k
    return interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p]);
 }
 
+/* Plane split of a level's tiles: a kernel over lv.ntiles x split CTAs
+ * gives CTA b the planes [k0, k0 + nk) of tile b / split (split divides
+ * the tile depth). Levels with few tiles (a 65^3 box in tiles of 8 planes
+ * is 243 CTAs for 152 SMs) get enough CTAs to hide load latency. */
+struct tile_part {
+   pgb_tile tl;
+   int kk0, nk;   /* first plane within the tile, planes */
+};
+
+__device__ __forceinline__ tile_part tile_split(const pgb_tile *tiles, const pgb_dlevel &lv, int split)
+{
+   tile_part t;
+   t.tl = tiles[blockIdx.x / split];
+   const int kz = lv.dim == 3 ? lv.tz : 1, per = kz / split;
+   t.kk0 = (blockIdx.x % split) * per;
+   t.nk = per;
+   return t;
+}
+
+/* the split for a launch over n tiles of a level: the smallest power of
+ * two dividing the tile depth that gives at least 1216 CTAs (8 per SM) */
+static inline int split_for(const pgb_dlevel &lv, int n)
+{
+   const int kz = lv.dim == 3 ? lv.tz : 1;
+   int sp = 1;
+   while (sp < kz && (long)n * sp < 1216) sp *= 2;
+   return sp;
+}
+
 /* FP32 <-> FP64 conversions in integer arithmetic. A conversion
  * instruction issues on the FP64 pipe, which runs at 1/64 of the FP32 rate
  * here; these take the integer pipes instead. f2d is exact except that FP32
@@ -171,9 +200,10 @@ __device__ __forceinline__ double opjac(int pde, double t, double uc, double s, 
  * the level's cover tiles are visited: elsewhere rhs stays 0 and D is the
  * FP32 update k_defect32 made at the end of the previous post-smoothing. */
 __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                   double w0_r, int cover)
+                                                   double w0_r, int cover, int split)
 {
-   const pgb_tile tl = cover ? lv.ctiles[blockIdx.x] : lv.tiles[blockIdx.x];
+   const tile_part tp = tile_split(cover ? lv.ctiles : lv.tiles, lv, split);
+   const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
@@ -186,13 +216,14 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
    float *__restrict__ wd = b.w32[W_D];
    float *__restrict__ wc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   const int kz = dim == 3 ? lv.tz : 1;
-   long p = i + sy * j + sz * tl.k0;
-   double zm = (dim == 3 && tl.k0 > 0) ? u[p - sz] : 0.0, uc = u[p];
+   const int ks = tl.k0 + tp.kk0;
+   if (ks >= b.n[2]) return;
+   long p = i + sy * j + sz * ks;
+   double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
-      const int k = tl.k0 + kk;
-      if (kk >= kz || k >= b.n[2]) continue;
+      const int k = ks + kk;
+      if (kk >= tp.nk || k >= b.n[2]) continue;
       const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
       const int cm = b.cmask_child[p];
       const bool in = interior32(b, i, j, k, dim);
@@ -495,9 +526,10 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
  * pre-smoothing on a level whose points outside the cover tiles do not
  * change in between (no sync, no injection there). The next FP64 residual
  * (after that pre-smoothing) is computed from u itself. */
-__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot)
+__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split)
 {
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
@@ -507,11 +539,10 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
    float *__restrict__ dd = b.w32[W_D];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
-   const int kz = dim == 3 ? lv.tz : 1;
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
-      const int k = tl.k0 + kk;
-      if (kk >= kz || k >= b.n[2]) continue;
+      const int k = tl.k0 + tp.kk0 + kk;
+      if (kk >= tp.nk || k >= b.n[2]) continue;
       const long p = i + sy * j + sz * k;
       if (!relaxed32(b, i, j, k, p, dim)) continue;
       const float ec = e[p];
@@ -530,21 +561,21 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
  * res when E still holds the d2f(res) the interpolation wrote (the fused
  * sweeps copy unrelaxed points from slot to slot). */
 __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
-                                               int zslot)
+                                               int zslot, int split)
 {
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const int kz = lv.dim == 3 ? lv.tz : 1;
    double *__restrict__ u = b.f[PGB_F_U];
    const float *es = eslot(b, slot);
    float *e = eslot(b, zslot);
    const double *__restrict__ res = b.f[PGB_F_RES];
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
-      const int k = tl.k0 + kk;
-      if (kk >= kz || k >= b.n[2]) continue;
+      const int k = tl.k0 + tp.kk0 + kk;
+      if (kk >= tp.nk || k >= b.n[2]) continue;
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       double corr = f2d(es[p]);
       if (post && !relaxed32(b, i, j, k, p, lv.dim)) {
@@ -682,17 +713,18 @@ __device__ __forceinline__ double wsum64m(int n, const double *c, const double *
 
 /* Coarse half of the coarse-grid correction (amrd/mg.c:332-341) on the tiles
  * the interpolation reads: res = (f - lop)/w0_i in FP64, X = RN32(res). */
-__global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0)
+__global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0,
+                                                  int split)
 {
-   const pgb_tile tl = lv.ctiles[blockIdx.x];
+   const tile_part tp = tile_split(lv.ctiles, lv, split);
+   const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const int kz = lv.dim == 3 ? lv.tz : 1;
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
-      const int k = tl.k0 + kk;
-      if (kk >= kz || k >= b.n[2]) continue;
+      const int k = tl.k0 + tp.kk0 + kk;
+      if (kk >= tp.nk || k >= b.n[2]) continue;
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       const double r = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) * inv_w0;
       b.f[PGB_F_RES][p] = r;
@@ -897,11 +929,12 @@ __device__ double block_sum32(double v, double *sm)
  * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
-                                                      pgb_trace *trace)
+                                                      pgb_trace *trace, int split)
 {
    __shared__ double sm[32];
    __shared__ int last;
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const double *__restrict__ u = b.f[PGB_F_U];
@@ -913,14 +946,14 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    double acc = 0;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
-   const int kz = dim == 3 ? lv.tz : 1;
-   if (i < b.n[0] && j < b.n[1]) {
-      long p = i + sy * j + sz * tl.k0;
-      double zm = (dim == 3 && tl.k0 > 0) ? u[p - sz] : 0.0, uc = u[p];
+   const int ks = tl.k0 + tp.kk0;
+   if (i < b.n[0] && j < b.n[1] && ks < b.n[2]) {
+      long p = i + sy * j + sz * ks;
+      double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
       for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
-         const int k = tl.k0 + kk;
-         if (kk >= kz || k >= b.n[2]) continue;
+         const int k = ks + kk;
+         if (kk >= tp.nk || k >= b.n[2]) continue;
          const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
          if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
             float c;
@@ -948,7 +981,8 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    double lres = 0;
    for (int bx = 0; bx < lv.nbox; bx++) {
       double v = 0;
-      for (int q = lv.tile_start[bx] + t; q < lv.tile_start[bx + 1]; q += NT) v += __ldcg(&sc.partial[q]);
+      for (int q = lv.tile_start[bx] * split + t; q < lv.tile_start[bx + 1] * split; q += NT)
+         v += __ldcg(&sc.partial[q]);
       v = block_sum32(v, sm);
       if (t == 0) {
          const double r = sqrt(v / boxes[lv.box[bx]].count);
@@ -1179,20 +1213,34 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
    }
 }
 
+/* one step of the device solve loop (pgb_solve's host loop, amrd/mg.c's
+ * solve_elliptics iteration test) */
+__global__ void k_solve_step(cudaGraphConditionalHandle h, const double *norm, double *hist, int *it,
+                             int min_iter, int max_iter, double tol)
+{
+   const double r = *norm;
+   const int k = *it;
+   if (k < max_iter) hist[k] = r;
+   *it = k + 1;
+   cudaGraphSetConditional(h, ((k + 1 < min_iter || r > tol) && k + 1 < max_iter) ? 1u : 0u);
+}
+
 /* ------------------------------------------------------------ launchers -- */
 extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover,
                                 void *stream)
 {
    const int n = cover ? lv.nctiles : lv.ntiles;
    if (!n) return 0;
-   k_fas_defect<<<n, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r, cover);
+   const int sp = split_for(lv, n);
+   k_fas_defect<<<n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r, cover, sp);
    return check32("fas_defect");
 }
 
 extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream)
 {
    if (!lv.ntiles) return 0;
-   k_defect32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot);
+   const int sp = split_for(lv, lv.ntiles);
+   k_defect32<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot, sp);
    return check32("defect32");
 }
 
@@ -1242,11 +1290,21 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
    return 0;
 }
 
+extern "C" int pgb_k_solve_step(unsigned long long handle, const double *norm, double *hist, int *it,
+                                int min_iter, int max_iter, double tol, void *stream)
+{
+   k_solve_step<<<1, 1, 0, (cudaStream_t)stream>>>((cudaGraphConditionalHandle)handle, norm, hist, it,
+                                                   min_iter, max_iter, tol);
+   return check32("solve_step");
+}
+
 extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot,
                             void *stream)
 {
    if (!lv.ntiles) return 0;
-   k_update<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot);
+   const int sp = split_for(lv, lv.ntiles);
+   k_update<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot,
+                                                                               sp);
    return check32("update");
 }
 
@@ -1276,7 +1334,8 @@ extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, 
 extern "C" int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream)
 {
    if (!lv.nctiles) return 0;
-   k_cgc_mixed<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, inv_w0);
+   const int sp = split_for(lv, lv.nctiles);
+   k_cgc_mixed<<<lv.nctiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, inv_w0, sp);
    return check32("cgc_mixed");
 }
 
@@ -1323,8 +1382,10 @@ extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde
                                    double *norm_out, pgb_trace *trace, void *stream)
 {
    if (!lv.ntiles) return 0;
-   k_residual_fast<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
-                                                                                  norm_out, trace);
+   int sp = split_for(lv, lv.ntiles);
+   while (sp > 1 && (long)lv.ntiles * sp > sc.npartial) sp /= 2;   /* one partial sum per CTA */
+   k_residual_fast<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
+                                                                                       norm_out, trace, sp);
    return check32("residual_fast");
 }
 

@@ -49,6 +49,10 @@ struct pgb_solver {
    cudaGraphExec_t gexec;   /* one captured V-cycle (+ read-back of the residual) */
    int graph_ok;
    long long graph_kernels; /* kernel launches in the captured V-cycle */
+   cudaGraphExec_t sexec;   /* the solve loop: V-cycles under a conditional while node */
+   int solve_ok;            /* 1 built, -1 not available (host loop) */
+   double *d_hist;          /* finest residual after each cycle of a solve [max_iter] */
+   int *d_it;               /* cycles run by the device loop */
    cudaEvent_t ev0, ev1;
    int last_cycles;
    long last_citers;
@@ -404,6 +408,7 @@ static int setup_device(pgb_solver *s)
          return 10;
    }
    CU(cudaMalloc((void **)&s->sc.partial, sizeof(double) * 2 * (size_t)maxt));
+   s->sc.npartial = 2 * (long)maxt;
    CU(cudaMalloc((void **)&s->sc.counter, sizeof(unsigned int)));
    CU(cudaMemset(s->sc.counter, 0, sizeof(unsigned int)));
    CU(cudaMalloc((void **)&s->sc.box_norm, sizeof(double) * (size_t)maxbox));
@@ -413,6 +418,8 @@ static int setup_device(pgb_solver *s)
    s->snap_points = snap_pts;
    CU(cudaMalloc((void **)&s->d_snap, sizeof(double) * 2 * (size_t)(snap_pts ? snap_pts : 1)));
    CU(cudaMallocHost((void **)&s->h_res, sizeof(double) * 4));
+   CU(cudaMalloc((void **)&s->d_hist, sizeof(double) * (size_t)(h->prm.max_iter > 0 ? h->prm.max_iter : 1)));
+   CU(cudaMalloc((void **)&s->d_it, sizeof(int)));
    return 0;
 }
 
@@ -490,7 +497,10 @@ int pgb_destroy(pgb_solver *s)
       if (s->d_snap) cudaFree(s->d_snap);
       if (s->d_trace) cudaFree(s->d_trace);
       if (s->h_res) cudaFreeHost(s->h_res);
+      if (s->d_hist) cudaFree(s->d_hist);
+      if (s->d_it) cudaFree(s->d_it);
       if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
+      if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
       if (s->stream) {
          cudaEventDestroy(s->ev0);
          cudaEventDestroy(s->ev1);
@@ -627,7 +637,7 @@ static int autotune(pgb_solver *s)
             if (f == 2 && !can_fuse) continue;
             float ms = 0;
             int r;
-            for (r = 0; r < 4; r++) {   /* one warm-up, three timed */
+            for (r = 0; r < 9; r++) {   /* one warm-up, eight timed */
                if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));
                int slot = PGB_W32_E;
                KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, &slot, s->stream));
@@ -945,10 +955,66 @@ static int build_graph(pgb_solver *s)
    return 0;
 }
 
+/* The whole solve loop as one graph: a conditional while node whose body
+ * is one V-cycle and k_solve_step, which records the finest residual and
+ * sets the condition exactly as pgb_solve's host loop would decide, so the
+ * host waits once per solve instead of once per cycle. Where the runtime
+ * refuses the node, solve_ok = -1 and pgb_solve keeps the host loop. */
+static int build_solve_graph(pgb_solver *s)
+{
+   const pgb_hparams *p = &s->h.prm;
+   cudaGraph_t g = 0, body;
+   cudaGraphConditionalHandle hnd;
+   cudaGraphNode_t node;
+   struct cudaGraphNodeParams cp;
+   cudaError_t e;
+   int rc;
+   long long before = pgb_dev_launches() + pgb_dev_launches32();
+   if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail(10, "cudaGraphCreate");
+   memset(&cp, 0, sizeof(cp));
+   if (cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) goto refused;
+   cp.type = cudaGraphNodeTypeConditional;
+   cp.conditional.handle = hnd;
+   cp.conditional.type = cudaGraphCondTypeWhile;
+   cp.conditional.size = 1;
+   if (cudaGraphAddNode(&node, g, NULL, NULL, 0, &cp) != cudaSuccess) goto refused;
+   body = cp.conditional.phGraph_out[0];
+   if (cudaStreamBeginCaptureToGraph(s->stream, body, NULL, NULL, 0, cudaStreamCaptureModeThreadLocal) !=
+       cudaSuccess)
+      goto refused;
+   rc = vcycle_launch(s);
+   if (!rc && pgb_k_solve_step(hnd, norm_slot(s, s->h.nlev, N_RESID), s->d_hist, s->d_it, p->min_iter,
+                               p->max_iter, p->tol, s->stream))
+      rc = fail(10, "%s", pgb_dev_error32());
+   e = cudaStreamEndCapture(s->stream, &body);
+   g_captured += pgb_dev_launches() + pgb_dev_launches32() - before;   /* counted when replayed */
+   if (rc) {
+      cudaGraphDestroy(g);
+      return rc;
+   }
+   if (e != cudaSuccess) goto refused;
+   e = cudaGraphInstantiate(&s->sexec, g, 0);
+   cudaGraphDestroy(g);
+   if (e != cudaSuccess) {
+      cudaGetLastError();
+      s->solve_ok = -1;
+      return 0;
+   }
+   s->solve_ok = 1;
+   return 0;
+refused:
+   cudaGetLastError();
+   cudaGraphDestroy(g);
+   s->solve_ok = -1;
+   return 0;
+}
+
 static void drop_graph(pgb_solver *s)
 {
    if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
    s->graph_ok = 0;
+   if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
+   s->solve_ok = 0;
 }
 
 int pgb_vcycle(pgb_solver *s, double *res)
@@ -979,11 +1045,29 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    CU(cudaEventRecord(s->ev0, s->stream));
    if ((rc = pgb_prepare(s))) return rc;
-   while ((it < p->min_iter || res > p->tol) && it < p->max_iter) {
-      if ((rc = pgb_vcycle(s, &res))) return rc;
-      if (res_per_cycle && it < cap) res_per_cycle[it] = res;
-      it++;
+   if (!getenv("PGB_NO_GRAPH") && !getenv("PGB_HOST_LOOP") && p->max_iter > 0) {
+      if (!s->graph_ok && (rc = build_graph(s))) return rc;   /* also counts the cycle's kernels */
+      if (!s->solve_ok && (rc = build_solve_graph(s))) return rc;
    }
+   if (s->solve_ok > 0 && !getenv("PGB_NO_GRAPH") && !getenv("PGB_HOST_LOOP") && p->max_iter > 0) {
+      CU(cudaMemsetAsync(s->d_it, 0, sizeof(int), s->stream));
+      CU(cudaGraphLaunch(s->sexec, s->stream));
+      CU(cudaMemcpyAsync(s->h_res + 2, s->d_it, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+      CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double), cudaMemcpyDeviceToHost,
+                         s->stream));
+      CU(cudaStreamSynchronize(s->stream));
+      memcpy(&it, s->h_res + 2, sizeof(int));
+      res = s->h_res[0];
+      g_graph_replayed += (s->graph_kernels + 1) * it;
+      if (res_per_cycle && cap > 0 && it > 0)
+         CU(cudaMemcpy(res_per_cycle, s->d_hist, sizeof(double) * (size_t)(it < cap ? it : cap),
+                       cudaMemcpyDeviceToHost));
+   } else
+      while ((it < p->min_iter || res > p->tol) && it < p->max_iter) {
+         if ((rc = pgb_vcycle(s, &res))) return rc;
+         if (res_per_cycle && it < cap) res_per_cycle[it] = res;
+         it++;
+      }
    CU(cudaEventRecord(s->ev1, s->stream));
    CU(cudaMemcpyAsync(s->h_res + 1, s->d_citers, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
    CU(cudaStreamSynchronize(s->stream));
