@@ -853,6 +853,20 @@ static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
    return 0;
 }
 
+/* Levels below the finest whose residual is restricted from its FP32 copy
+ * (no sync of res) carry the defect after pre-smoothing in FP32,
+ * D - (lap E + C E) before the update (k_defect32), instead of a fresh FP64
+ * residual: nothing reads that level's FP64 res at relaxed points. The
+ * carried defect is exact up to FP32 rounding relative to the defect of
+ * this cycle, because the FAS pass recomputes D in FP64 on the whole level
+ * at the start of every cycle. Levels that carry D across cycles outside
+ * their cover tiles (dnext) keep the FP64 residual: two carries in a row
+ * would let FP32 rounding of early, large defects accumulate there. */
+static int defect32_level(const pgb_solver *s, int L)
+{
+   return L > 1 && L < s->h.nlev && s->res32[L] && !s->dnext[L] && s->h.prm.pre_swp > 0;
+}
+
 /* The mixed form of the V-cycle (same transfers and the same FP64 residual,
  * restriction and norm as vcycle_fp64; the arithmetic of each smoothing
  * block is described in pgb_kernels32.cu). The finest level's pre-smoothing
@@ -872,8 +886,9 @@ static int vcycle_mixed(pgb_solver *s)
       if (L < Lf) {
          /* this norm is only ever traced (the finest level's convergence
           * norm comes from the residual after post-smoothing) */
-         KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc,
-                                  s->d_trace ? norm_slot(s, L + 1, N_RESID) : 0, s->d_trace, s->stream));
+         if (!defect32_level(s, L + 1))
+            KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc,
+                                     s->d_trace ? norm_slot(s, L + 1, N_RESID) : 0, s->d_trace, s->stream));
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
          if (!s->res32[L]) KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
          if (h->inject[L].nops)
@@ -890,6 +905,7 @@ static int vcycle_mixed(pgb_solver *s)
       if (L > 1 && p->pre_swp > 0) {
          int slot = PGB_W32_E;
          if (sweeps32(s, L, p->pre_swp, &slot)) return 11;
+         if (defect32_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 0, slot, slot, s->stream));
          s->eslot[L] = slot;
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
