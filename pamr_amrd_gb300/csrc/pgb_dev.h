@@ -110,7 +110,9 @@ unsigned long long pgb_dev_launches_lb(void);    /* pgb_linbnd.cu */
 const char *pgb_dev_error32(void);
 unsigned long long pgb_dev_launches32(void);
 int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover, void *stream);
-int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream);
+/* D -= lap E + C E at relaxed points; with gate, only while *gate == gval */
+int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, const int *gate, int gval, void *stream);
+int pgb_k_flip(int *parity, void *stream);
 int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, int *slot, void *stream);
 /* the device solve loop's step: records the finest norm of cycle *it,
  * counts the cycle and sets the while node's condition to pgb_solve's loop
@@ -123,7 +125,7 @@ int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *strea
 int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream);
 int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream);
 int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
-                        double *norm_out, pgb_trace *trace, void *stream);
+                        double *norm_out, pgb_trace *trace, const int *gate, void *stream);
 int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
 int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                          pgb_coarsest_args a, pgb_trace *trace, void *stream);

@@ -526,8 +526,10 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
  * pre-smoothing on a level whose points outside the cover tiles do not
  * change in between (no sync, no injection there). The next FP64 residual
  * (after that pre-smoothing) is computed from u itself. */
-__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split)
+__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split,
+                                                 const int *gate, int gval)
 {
+   if (gate && *gate != gval) return;   /* the cycle parity leaves this pass out */
    const tile_part tp = tile_split(lv.tiles, lv, split);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
@@ -929,8 +931,9 @@ __device__ double block_sum32(double v, double *sm)
  * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
-                                                      pgb_trace *trace, int split)
+                                                      pgb_trace *trace, int split, const int *gate)
 {
+   if (gate && *gate) return;   /* the cycle parity leaves this pass out (no norm is read then) */
    __shared__ double sm[32];
    __shared__ int last;
    const tile_part tp = tile_split(lv.tiles, lv, split);
@@ -1213,6 +1216,15 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
    }
 }
 
+/* the cycle parity: 0 -> 1 -> 0 ... at the end of each mixed V-cycle */
+__global__ void k_flip(int *parity) { *parity ^= 1; }
+
+extern "C" int pgb_k_flip(int *parity, void *stream)
+{
+   k_flip<<<1, 1, 0, (cudaStream_t)stream>>>(parity);
+   return check32("flip");
+}
+
 /* one step of the device solve loop (pgb_solve's host loop, amrd/mg.c's
  * solve_elliptics iteration test) */
 __global__ void k_solve_step(cudaGraphConditionalHandle h, const double *norm, double *hist, int *it,
@@ -1236,11 +1248,13 @@ extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, d
    return check32("fas_defect");
 }
 
-extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, void *stream)
+extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, const int *gate, int gval,
+                              void *stream)
 {
    if (!lv.ntiles) return 0;
    const int sp = split_for(lv, lv.ntiles);
-   k_defect32<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot, sp);
+   k_defect32<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot, sp, gate,
+                                                                                 gval);
    return check32("defect32");
 }
 
@@ -1379,13 +1393,13 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
 }
 
 extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
-                                   double *norm_out, pgb_trace *trace, void *stream)
+                                   double *norm_out, pgb_trace *trace, const int *gate, void *stream)
 {
    if (!lv.ntiles) return 0;
    int sp = split_for(lv, lv.ntiles);
    while (sp > 1 && (long)lv.ntiles * sp > sc.npartial) sp /= 2;   /* one partial sum per CTA */
    k_residual_fast<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
-                                                                                       norm_out, trace, sp);
+                                                                                       norm_out, trace, sp, gate);
    return check32("residual_fast");
 }
 

@@ -52,6 +52,7 @@ struct pgb_solver {
    cudaGraphExec_t sexec;   /* the solve loop: V-cycles under a conditional while node */
    int solve_ok;            /* 1 built, -1 not available (host loop) */
    double *d_hist;          /* finest residual after each cycle of a solve [max_iter] */
+   int *d_parity;           /* mixed form: 0 / 1 for even / odd cycles of a solve */
    int *d_it;               /* cycles run by the device loop */
    cudaEvent_t ev0, ev1;
    int last_cycles;
@@ -420,6 +421,8 @@ static int setup_device(pgb_solver *s)
    CU(cudaMallocHost((void **)&s->h_res, sizeof(double) * 4));
    CU(cudaMalloc((void **)&s->d_hist, sizeof(double) * (size_t)(h->prm.max_iter > 0 ? h->prm.max_iter : 1)));
    CU(cudaMalloc((void **)&s->d_it, sizeof(int)));
+   CU(cudaMalloc((void **)&s->d_parity, sizeof(int)));
+   CU(cudaMemset(s->d_parity, 0, sizeof(int)));
    return 0;
 }
 
@@ -499,6 +502,7 @@ int pgb_destroy(pgb_solver *s)
       if (s->h_res) cudaFreeHost(s->h_res);
       if (s->d_hist) cudaFree(s->d_hist);
       if (s->d_it) cudaFree(s->d_it);
+      if (s->d_parity) cudaFree(s->d_parity);
       if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
       if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
       if (s->stream) {
@@ -641,7 +645,7 @@ static int autotune(pgb_solver *s)
                if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));
                int slot = PGB_W32_E;
                KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, &slot, s->stream));
-               KC32(pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0,
+               KC32(pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0, 0,
                                         s->stream));
             }
             CU(cudaEventRecord(s->ev1, s->stream));
@@ -720,7 +724,7 @@ int pgb_prepare(pgb_solver *s)
          s->res32[L] = ok;
       }
       if (pgb_k_residual_fast(s->dbox, s->lv[s->h.nlev], s->h.pde, s->sc,
-                              norm_slot(s, s->h.nlev, N_RESID), 0, s->stream))
+                              norm_slot(s, s->h.nlev, N_RESID), 0, 0, s->stream))
          return fail(11, "%s", pgb_dev_error32());
       /* Levels below the finest whose cover tiles are a minority, with no
        * sync between boxes: between a post-smoothing and the next
@@ -737,6 +741,7 @@ int pgb_prepare(pgb_solver *s)
       }
    }
    CU(cudaMemsetAsync(s->d_citers, 0, sizeof(int), s->stream));
+   CU(cudaMemsetAsync(s->d_parity, 0, sizeof(int), s->stream));   /* every solve starts on an even cycle */
    s->prepared = 1;
    return 0;
 }
@@ -853,18 +858,30 @@ static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
    return 0;
 }
 
-/* Levels below the finest whose residual is restricted from its FP32 copy
- * (no sync of res) carry the defect after pre-smoothing in FP32,
- * D - (lap E + C E) before the update (k_defect32), instead of a fresh FP64
- * residual: nothing reads that level's FP64 res at relaxed points. The
- * carried defect is exact up to FP32 rounding relative to the defect of
- * this cycle, because the FAS pass recomputes D in FP64 on the whole level
- * at the start of every cycle. Levels that carry D across cycles outside
- * their cover tiles (dnext) keep the FP64 residual: two carries in a row
- * would let FP32 rounding of early, large defects accumulate there. */
+/* Levels whose residual is restricted from its FP32 copy (no sync of res)
+ * carry the defect after pre-smoothing in FP32, D - (lap E + C E) before the
+ * update (k_defect32), instead of a fresh FP64 residual: nothing reads that
+ * level's FP64 res at relaxed points. The carried defect is exact up to
+ * FP32 rounding relative to the defect of this cycle, because D is
+ * recomputed in FP64 on the whole level once per cycle: by the FAS pass
+ * below the finest level, by the residual that ends the cycle on the
+ * finest. Levels that carry D across cycles outside their cover tiles
+ * (dnext) keep the FP64 residual: two carries in a row would let FP32
+ * rounding of early, large defects accumulate there. */
 static int defect32_level(const pgb_solver *s, int L)
 {
-   return L > 1 && L < s->h.nlev && s->res32[L] && !s->dnext[L] && s->h.prm.pre_swp > 0;
+   return L > 1 && s->res32[L] && !s->dnext[L] && s->h.prm.pre_swp > 0;
+}
+
+/* The dnext levels among them alternate: on even cycles of a solve the
+ * FP64 residual after pre-smoothing refreshes D on the whole level, on odd
+ * cycles D is carried in FP32 as above. Between two refreshes D is then
+ * carried through four updates, whose FP32 rounding stays far below the
+ * defect of the cycle. A device flag (d_parity, flipped at the end of each
+ * cycle) gates the two passes, so one captured cycle serves both. */
+static int alt_level(const pgb_solver *s, int L)
+{
+   return L > 1 && s->res32[L] && s->dnext[L] && s->h.prm.pre_swp > 0;
 }
 
 /* The mixed form of the V-cycle (same transfers and the same FP64 residual,
@@ -888,7 +905,8 @@ static int vcycle_mixed(pgb_solver *s)
           * norm comes from the residual after post-smoothing) */
          if (!defect32_level(s, L + 1))
             KC32(pgb_k_residual_fast(s->dbox, s->lv[L + 1], h->pde, s->sc,
-                                     s->d_trace ? norm_slot(s, L + 1, N_RESID) : 0, s->d_trace, s->stream));
+                                     s->d_trace ? norm_slot(s, L + 1, N_RESID) : 0, s->d_trace,
+                                     alt_level(s, L + 1) ? s->d_parity : 0, s->stream));
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
          if (!s->res32[L]) KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
          if (h->inject[L].nops)
@@ -905,7 +923,8 @@ static int vcycle_mixed(pgb_solver *s)
       if (L > 1 && p->pre_swp > 0) {
          int slot = PGB_W32_E;
          if (sweeps32(s, L, p->pre_swp, &slot)) return 11;
-         if (defect32_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->stream));
+         if (defect32_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
+         else if (alt_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->d_parity, 1, s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 0, slot, slot, s->stream));
          s->eslot[L] = slot;
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
@@ -917,7 +936,7 @@ static int vcycle_mixed(pgb_solver *s)
          KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
          if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream));
          if (sweeps32(s, L, p->pst_swp, &slot)) return 11;
-         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->stream));
+         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       } else if (lvl_coarsest(s, L)) {
@@ -932,8 +951,13 @@ static int vcycle_mixed(pgb_solver *s)
       }
       if (L == Lf)
          KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
-                                  s->d_trace, s->stream));
+                                  s->d_trace, 0, s->stream));
    }
+   for (L = 2; L <= Lf; L++)
+      if (alt_level(s, L)) {
+         KC32(pgb_k_flip(s->d_parity, s->stream));
+         break;
+      }
    return 0;
 }
 
