@@ -97,7 +97,10 @@ int pgb_get_grid_device(pgb_solver *s, int grid, double *u);
  * injections), then V-cycles until the finest residual is <= tol (at least
  * min_iter, at most max_iter cycles). Replaces solve_elliptics
  * (amrd/mg.c:20-79). res_per_cycle (may be NULL) receives up to cap
- * residuals. */
+ * residuals. The cycles and the stopping test run on the device (one CUDA
+ * graph with a conditional while node; the host waits once per solve);
+ * environment PGB_HOST_LOOP=1 tests on the host after every cycle instead,
+ * with the same results bit for bit. */
 int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycle, int cap);
 
 /* One FAS V-cycle; *res = finest-level residual. Replaces vcycle
