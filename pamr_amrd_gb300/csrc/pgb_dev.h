@@ -123,7 +123,8 @@ int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int z
 int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream);
 int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream);
-int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream);
+int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream, void *side,
+                       void *fork, void *join);
 int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
                         double *norm_out, pgb_trace *trace, const int *gate, void *stream);
 int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);

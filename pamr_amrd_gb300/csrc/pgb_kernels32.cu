@@ -1353,9 +1353,21 @@ extern "C" int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_
    return check32("cgc_mixed");
 }
 
-extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream)
+/* With one batch (ops with disjoint destinations) and a side stream, the
+ * FP64 edge kernel runs beside the FP32 kernel: they write disjoint points
+ * (the FP32 kernel leaves the face rows and x-ends of all-relaxed boxes to
+ * it) and only read the coarse level. fork/join are events without timing. */
+extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int slot, void *stream,
+                                  void *side, void *fork, void *join)
 {
    const pgb_interp_op *h = (const pgb_interp_op *)p->h_ops, *d = (const pgb_interp_op *)p->d_ops;
+   const bool par = side && p->nbatch == 1;
+   cudaStream_t es = par ? (cudaStream_t)side : (cudaStream_t)stream;
+   if (par) {
+      if (cudaEventRecord((cudaEvent_t)fork, (cudaStream_t)stream) != cudaSuccess ||
+          cudaStreamWaitEvent(es, (cudaEvent_t)fork, 0) != cudaSuccess)
+         return check32("interp_mixed fork");
+   }
    for (int bt = 0; bt < p->nbatch; bt++) {
       const int n = p->batch_start[bt + 1] - p->batch_start[bt];
       for (int c0 = 0; c0 < n; c0 += 65535) {
@@ -1384,10 +1396,15 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
             }
             long gy = mf + (2 * mr + 127) / 128;   /* face rows, then x-end chunks */
             k_interp_edges<<<dim3((unsigned)((mi + 127) / 128), (unsigned)(gy > 65535 ? 65535 : gy), (unsigned)m),
-                             128, 0, (cudaStream_t)stream>>>(d + p->batch_start[bt] + c0, boxes, dim, slot);
+                             128, 0, es>>>(d + p->batch_start[bt] + c0, boxes, dim, slot);
             if (check32("interp_edges")) return 1;
          }
       }
+   }
+   if (par) {
+      if (cudaEventRecord((cudaEvent_t)join, es) != cudaSuccess ||
+          cudaStreamWaitEvent((cudaStream_t)stream, (cudaEvent_t)join, 0) != cudaSuccess)
+         return check32("interp_mixed join");
    }
    return 0;
 }

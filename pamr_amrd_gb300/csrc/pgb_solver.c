@@ -55,6 +55,8 @@ struct pgb_solver {
    int *d_parity;           /* mixed form: 0 / 1 for even / odd cycles of a solve */
    int *d_it;               /* cycles run by the device loop */
    cudaEvent_t ev0, ev1;
+   cudaStream_t side;       /* second stream for independent kernels of a cycle */
+   cudaEvent_t evfork, evjoin;
    int last_cycles;
    long last_citers;
    double last_ms;
@@ -295,8 +297,11 @@ static int setup_device(pgb_solver *s)
    int i, f, L, d, maxt = 1, maxbox = 1;
    long snap_pts = 0;
    CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+   CU(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
    CU(cudaEventCreate(&s->ev0));
    CU(cudaEventCreate(&s->ev1));
+   CU(cudaEventCreateWithFlags(&s->evfork, cudaEventDisableTiming));
+   CU(cudaEventCreateWithFlags(&s->evjoin, cudaEventDisableTiming));
    /* arena layout: per box, 5 float64 grid functions then 2 byte masks */
    fo = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * (PGB_NF + 2));
    for (i = 0; i < h->nbox; i++) {
@@ -509,6 +514,11 @@ int pgb_destroy(pgb_solver *s)
          cudaEventDestroy(s->ev0);
          cudaEventDestroy(s->ev1);
          cudaStreamDestroy(s->stream);
+      }
+      if (s->side) {
+         cudaEventDestroy(s->evfork);
+         cudaEventDestroy(s->evjoin);
+         cudaStreamDestroy(s->side);
       }
    }
    free(s->hbox);
@@ -934,7 +944,9 @@ static int vcycle_mixed(pgb_solver *s)
       if (L > 1) {
          int slot = s->eslot[L];
          KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
-         if (h->interp[L].nops) KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream));
+         if (h->interp[L].nops)
+            KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream, s->side, s->evfork,
+                                    s->evjoin));
          if (sweeps32(s, L, p->pst_swp, &slot)) return 11;
          if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
