@@ -92,6 +92,51 @@ def cpu_round(nproc: int, seed0: int = 0, solve=_port_solve) -> dict:
     return {"solves": nproc, "wall_s": wall, "per_solve_s": statistics.median(per)}
 
 
+def cpu_model() -> str:
+    """the host CPU's model name (lscpu, else /proc/cpuinfo, else platform)"""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def solve_model_bytes(sv, nu1: int, nu2: int, b_sweep: float) -> dict:
+    """Algorithmic HBM bytes of one V(nu1,nu2) cycle of the FAS multigrid
+    (amrd/mg.c:84-201): per level with N interior points, nu1+nu2 sweeps of
+    b_sweep bytes per point, the residual (32), L_op (24), compute_MG_rhs (40)
+    and the coarse-grid correction (24); per restriction into a level, the
+    fine and coarse points of the three restricted fields (res, u, src: 8 B
+    each). The coarsest level's loop is counted per sweep with
+    coarsest_point_sweep_bytes. cmask traffic counts 0 (derivable from the box
+    table)."""
+    nlev = sv.num_levels()
+    n = []
+    for L in range(1, nlev + 1):
+        tot = 0
+        for b in range(sv.level_nbox(L)):
+            sh = sv.box_info(L, b)["shape"]
+            pts = 1
+            for d in sh:
+                pts *= max(d - 2, 1) if d > 1 else 1
+            tot += pts
+        n.append(tot)
+    per_cycle = sum(N * ((nu1 + nu2) * b_sweep + 32 + 24 + 40 + 24) for N in n[1:])
+    per_cycle += sum(3 * 8 * (n[L] + n[L - 1]) for L in range(1, nlev))
+    return {"bytes_per_cycle": float(per_cycle), "coarsest_point_sweep_bytes": float(n[0] * b_sweep),
+            "interior_points": n}
+
+
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -635,13 +680,30 @@ def main():
 
     roof["beyond_l2"] = sweep_beyond_l2(S, torch, np, peak)
 
+    # whole-solve roofline: algorithmic bytes of the cycles each form ran
+    # (FP32 sweeps count 16 B per point, FP64 ones 32) over the timed solve
+    solve_roof = None
+    try:
+        solve_roof = {}
+        for form, sv, tm, bsw in (("mixed", smx, tmx, 16.0), ("fp64", s64, tm64, 32.0)):
+            mb = solve_model_bytes(sv, case.params.pre_swp, case.params.pst_swp, bsw)
+            cyc = statistics.mean(tm["iters"])
+            citers = sv.stats()["coarsest_iters"]
+            byt = cyc * mb["bytes_per_cycle"] + citers * mb["coarsest_point_sweep_bytes"]
+            t = tm["total_ms"] / args.steps / 1e3
+            solve_roof[form] = {"bytes_per_solve": byt, "achieved_gbs": byt / t / 1e9,
+                                "frac": byt / t / 1e9 / peak, "coarsest_sweeps": citers}
+    except Exception as exc:   # a report, never a reason to lose the bench line
+        solve_roof = {"error": str(exc)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nproc = min(host_cores(), 32)
         cr = cpu_round(nproc)
         cpu = {"value": cr["solves"] / cr["wall_s"], "unit": UNIT, "cores": nproc, "kind": "port",
                "sample": f"{nproc} concurrent oracle-port solves of the workload "
-                         f"(median {cr['per_solve_s']:.1f} s per solve)"}
+                         f"(median {cr['per_solve_s']:.1f} s per solve)",
+               "per_core_value": 1.0 / cr["per_solve_s"], "cpu_model": cpu_model()}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -661,7 +723,8 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": tmx["launches"],
-                "roofline": roof, "cpu_baseline": cpu, "clocks": tmx["clocks"]}
+                "roofline": roof, "solve_roofline": solve_roof, "cpu_baseline": cpu,
+                "clocks": tmx["clocks"]}
         print(json.dumps(line))
     s64.close()
     smx.close()
