@@ -47,3 +47,35 @@ def test_amplitudes_beyond_existence_diverge_in_port():
     case.params.max_iter = 6
     p = portrun.solve(case)
     assert not (p["res"][-1] <= case.params.tol)
+
+
+LIVE_FAMILIES = {
+    "conformal3d_17_9_s11": lambda: W.conformal3d(17, 9, seed=11),
+    "conformal3d_33_17_s12": lambda: W.conformal3d(33, 17, seed=12),
+    "poisson3d_17_s13": lambda: W.poisson3d(17, seed=13),
+    "poisson2d_33_s14": lambda: W.poisson2d(33, seed=14),
+    "lapse2d_bo_33_L3_s15": lambda: W.lapse2d_bo(33, seed=15, levels=3, step=77),
+    "uneven_s16": lambda: W.poisson2d_uneven(seed=16, n=33, levels=4, min_boxes=2, max_boxes=5,
+                                             min_side=5, max_side=17),
+    "conformal3d_65_33_s21": lambda: W.conformal3d(65, 33, seed=21),
+    "poisson3d_33_s24": lambda: W.poisson3d(33, seed=24),
+    "lapse2d_bo_65_L4_s22": lambda: W.lapse2d_bo(65, seed=22, levels=4, step=333),
+    "uneven65_s23": lambda: W.poisson2d_uneven(seed=23, n=65, levels=5, min_boxes=8, max_boxes=16),
+}
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("name", sorted(LIVE_FAMILIES))
+def test_port_matches_reference_live_families(name):
+    """every operator and hierarchy family the workloads build, on seeds no
+    fixture uses: the port against the compiled reference, hook for hook"""
+    case = LIVE_FAMILIES[name]()
+    ref = refrun.run_reference(case)
+    p = portrun.solve(case, hook_cap=len(ref["hooks"]) + 10)
+    assert p["iters"] == ref["iters"]
+    for a, b in zip(p["u"], ref["u"]):
+        assert np.array_equal(a, b)
+    h, rh = p["hooks"], ref["hooks"]
+    assert len(h["kind"]) == len(rh)
+    for k in ("kind", "L", "idx", "norm"):
+        assert np.array_equal(h[k], rh[k])
