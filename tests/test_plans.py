@@ -44,6 +44,25 @@ def test_plans_match_reference_live(seed):
     _check_case(case, ref)
 
 
+PLAN_FAMILIES = {
+    "conformal3d_33_17_s31": lambda: W.conformal3d(33, 17, seed=31),
+    "poisson3d_17_s32": lambda: W.poisson3d(17, seed=32),
+    "lapse2d_bo_65_L4_s33": lambda: W.lapse2d_bo(65, seed=33, levels=4, step=5),
+    "uneven65_L5_s34": lambda: W.poisson2d_uneven(seed=34, n=65, levels=5, min_boxes=8, max_boxes=16),
+}
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("name", sorted(PLAN_FAMILIES))
+def test_plans_match_reference_live_families(name):
+    """the hierarchy, both cmask arrays and the whole m_util_r8 call sequence
+    of a solve against the compiled reference, for every hierarchy family"""
+    case = PLAN_FAMILIES[name]()
+    ref = refrun.run_reference(case, log_ops=True)
+    ref["ops"] = ref["ops"].astype(np.int64)
+    _check_case(case, ref)
+
+
 def test_invalid_inputs_are_errors_not_exits():
     case = W.poisson2d(17)
     case.params.interp_order = 3
