@@ -79,6 +79,64 @@ int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox,
                const int *grid_level, const double *grid_bbox, const pgb_mg_params *params,
                int flags, pgb_solver **out);
 
+/* ------------------------------------------------------ level operators -- */
+/* An elliptic operator for the device, registered by the application
+ * (additive: the reference keeps its operator in the host hooks
+ * app_L_op / app_MG_residual / app_MG_relax, include/amrd.h:137-159, which
+ * run per grid on host arrays; the GPU needs the same arithmetic on the
+ * device). The operator is two expressions:
+ *   lop  L[u]  of lap, u, s0..s<nsrc-1> and numbers, e.g. "lap - s0"
+ *   jac  dL/du of j0, u, s0.. and numbers,           e.g. "j0"
+ * lap is the 5-point (2-D) / 7-point (3-D) Laplacian of u written as the
+ * reference hooks form it, ((u+ - 2u + u-)/dx^2 + (..)/dy^2) + (..)/dz^2
+ * (examples/nbs/num.f:113-115); j0 = -2/dx^2 - 2/dy^2 [- 2/dz^2]
+ * (num.f:236); sK is the K-th source grid function at the point. +, -, *,
+ * / and unary minus with parentheses; equal precedence associates to the
+ * left and every operation rounds once in IEEE double, so an expression in
+ * the hook's order gives the hook's results bit for bit (nbs:
+ * "lap - (s0*s0 + s1*s1)", "j0"). Relaxation updates
+ * u <- u - (L[u] - rhs) / (dL/du) at each red, then black point
+ * (num.f:216-241). At most PGB_MAX_SOURCES sources, 31 operations and 8
+ * distinct constants per expression. */
+#define PGB_MAX_SOURCES 4
+typedef struct pgb_operator pgb_operator;
+int pgb_operator_create(int nsrc, const char *lop, const char *jac, pgb_operator **out);
+/* the built-in operators PGB_PDE_* as operator objects */
+int pgb_operator_builtin(int pde, pgb_operator **out);
+void pgb_operator_destroy(pgb_operator *op);
+int pgb_operator_nsrc(const pgb_operator *op);
+/* PGB_PDE_* when the program is one of the built-in operators (evaluated
+ * by compiled code, same arithmetic), 3 for any other program */
+int pgb_operator_kind(const pgb_operator *op);
+/* The operator at one point on the host, with the device's rounding: L[u]
+ * and dL/du from lap, j0, u and the source values s[0..nsrc-1] (either of
+ * L, J may be NULL). Lets host code (an application's own hooks on host
+ * copies of its grids) evaluate exactly what the device evaluates. */
+int pgb_operator_eval(const pgb_operator *op, double lap, double j0, double u, const double *s, double *L,
+                      double *J);
+
+/* Everything pgb_create takes, plus the level operator, the coarsest AMR
+ * level of the MG hierarchy (min_level: PAMR_build_mgh(min_lev, max_lev, tl),
+ * src/gh.c:1222; grids below it are ignored and the MG levels below it are
+ * coarsenings of its grids; amrd/mg.c:29 builds from the level
+ * solve_elliptics is given, amrd/evolve.c:454 from the finest alone) and
+ * the MG restriction of each source (restr_src[0] is params.restr_src). */
+typedef struct {
+   int dim;
+   const pgb_operator *op;      /* copied at creation */
+   int base_shape[3];
+   double base_bbox[6];
+   int ngrids;
+   const int *grid_level;
+   const double *grid_bbox;
+   pgb_mg_params params;
+   int min_level;               /* 1 = the whole AMR hierarchy */
+   int restr_src[PGB_MAX_SOURCES];
+   int flags;
+} pgb_create_args;
+void pgb_default_create_args(pgb_create_args *a);
+int pgb_create_ex(const pgb_create_args *a, pgb_solver **out);
+
 /* Frees the hierarchy and device memory (PAMR_destroy_mgh, src/pamr.c:383). */
 int pgb_destroy(pgb_solver *s);
 
@@ -92,6 +150,10 @@ int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src);
 int pgb_get_grid(pgb_solver *s, int grid, double *u);
 int pgb_set_grid_device(pgb_solver *s, int grid, const double *u, const double *src);
 int pgb_get_grid_device(pgb_solver *s, int grid, double *u);
+/* source k (0 <= k < the operator's source count) of an input grid;
+ * pgb_set_grid's src is source 0 */
+int pgb_set_source(pgb_solver *s, int grid, int k, const double *src);
+int pgb_set_source_device(pgb_solver *s, int grid, int k, const double *src);
 
 /* Full solve: rebuilds the MG-only data from the AMR grids (build_mgh's
  * injections), then V-cycles until the finest residual is <= tol (at least

@@ -28,33 +28,44 @@ static double lap(const oracle_grid *g, const double *v, int i, int j, int k, do
    return t;
 }
 
+int oracle_nsrc(int pde) { return pde == ORACLE_NBS ? 2 : 1; }
+
+/* the source values at point p */
+static void src_at(int pde, const double *const *src, long p, double *sv)
+{
+   int k;
+   for (k = 0; k < oracle_nsrc(pde); k++) sv[k] = src[k][p];
+}
+
 /* L[u] at one point */
-static double op_point(int pde, double t, double u, double s)
+static double op_point(int pde, double t, double u, const double *s)
 {
    double p2, p4;
    switch (pde) {
    case ORACLE_CONFORMAL:
       p2 = u * u;
       p4 = p2 * p2;
-      return t + TWO_PI * s * (p4 * u);
+      return t + TWO_PI * s[0] * (p4 * u);
    case ORACLE_LAPSE:
-      return t - s * u;
+      return t - s[0] * u;
+   case ORACLE_NBS:   /* num.f:113-116: ... - (phi_r(i,j,k)**2+phi_i(i,j,k)**2) */
+      return t - (s[0] * s[0] + s[1] * s[1]);
    default:
-      return t - s;
+      return t - s[0];
    }
 }
 
 /* dL/du at one point: the Laplacian diagonal j0 plus the source term */
-static double jac_point(int pde, double j0, double u, double s)
+static double jac_point(int pde, double j0, double u, const double *s)
 {
    double p2;
    switch (pde) {
    case ORACLE_CONFORMAL:
       p2 = u * u;
-      return j0 + TEN_PI * s * (p2 * p2);
+      return j0 + TEN_PI * s[0] * (p2 * p2);
    case ORACLE_LAPSE:
-      return j0 - s;
-   default:
+      return j0 - s[0];
+   default:   /* Poisson, nbs (num.f:236) */
       return j0;
    }
 }
@@ -77,7 +88,7 @@ static void bounds(const oracle_grid *g, int *ke, int *ks, double *dx2, double *
    }
 }
 
-void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, const double *src,
+void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, const double *const *src,
                 const double *cmask)
 {
    int i, j, k, ks, ke;
@@ -87,13 +98,16 @@ void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, cons
       for (j = 2; j <= g->shape[1] - 1; j++)
          for (k = ks; k <= ke; k++) {
             long p = IDX(g, i, j, k);
-            if (cmask[p] == ORACLE_CMASK_ON)
-               lv[p] = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], src[p]);
+            if (cmask[p] == ORACLE_CMASK_ON) {
+               double sv[4];
+               src_at(pde, src, p, sv);
+               lv[p] = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], sv);
+            }
          }
 }
 
 double oracle_residual(int pde, const oracle_grid *g, double *res, const double *rhs,
-                       const double *v, const double *src, const double *cmask)
+                       const double *v, const double *const *src, const double *cmask)
 {
    int i, j, k, ks, ke, sum = 0;
    double dx2, dy2, dz2, j0, norm = 0;
@@ -113,7 +127,7 @@ double oracle_residual(int pde, const oracle_grid *g, double *res, const double 
 }
 
 double oracle_relax(int pde, const oracle_grid *g, double *v, const double *rhs,
-                    const double *src, const double *cmask)
+                    const double *const *src, const double *cmask)
 {
    int i, j, k, ks, ke, pass, sum = 0;
    double dx2, dy2, dz2, j0, norm = 0, res, jac;
@@ -125,8 +139,10 @@ double oracle_relax(int pde, const oracle_grid *g, double *v, const double *rhs,
                long p = IDX(g, i, j, k);
                int par = (g->dim == 3) ? (i + j + k + pass) : (i + j + pass);
                if (par % 2 == 0 && cmask[p] == ORACLE_CMASK_ON) {
-                  res = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], src[p]) - rhs[p];
-                  jac = jac_point(pde, j0, v[p], src[p]);
+                  double sv[4];
+                  src_at(pde, src, p, sv);
+                  res = op_point(pde, lap(g, v, i, j, k, dx2, dy2, dz2), v[p], sv) - rhs[p];
+                  jac = jac_point(pde, j0, v[p], sv);
                   v[p] = v[p] - res / jac;
                   norm = norm + res * res;
                   sum = sum + 1;

@@ -12,8 +12,14 @@
 /* PDE kinds: L[u] = lap(u) + term(src,u)
  *   ORACLE_POISSON   : term = -src                  (lap u = rho)
  *   ORACLE_CONFORMAL : term = +2*pi*src*u^5         (Hamiltonian constraint, psi)
- *   ORACLE_LAPSE     : term = -src*u                (maximal-slicing lapse)  */
-enum { ORACLE_POISSON = 0, ORACLE_CONFORMAL = 1, ORACLE_LAPSE = 2 };
+ *   ORACLE_LAPSE     : term = -src*u                (maximal-slicing lapse)
+ *   ORACLE_NBS       : term = -(src0^2 + src1^2)    (the Newtonian boson star's
+ *                      potential V_xx+V_yy+V_zz - (phi_r^2+phi_i^2),
+ *                      examples/nbs/num.f:113-116; two sources) */
+enum { ORACLE_POISSON = 0, ORACLE_CONFORMAL = 1, ORACLE_LAPSE = 2, ORACLE_NBS = 3 };
+
+/* number of source grid functions a PDE kind reads */
+int oracle_nsrc(int pde);
 
 #define ORACLE_CMASK_ON 1.0
 
@@ -23,11 +29,12 @@ typedef struct {
    double dx[3];  /* x(2)-x(1) of the grid's coordinate arrays */
 } oracle_grid;
 
-void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, const double *src,
+/* src: oracle_nsrc(pde) source arrays */
+void oracle_lop(int pde, const oracle_grid *g, double *lv, const double *v, const double *const *src,
                 const double *cmask);
 double oracle_residual(int pde, const oracle_grid *g, double *res, const double *rhs,
-                       const double *v, const double *src, const double *cmask);
+                       const double *v, const double *const *src, const double *cmask);
 double oracle_relax(int pde, const oracle_grid *g, double *v, const double *rhs,
-                    const double *src, const double *cmask);
+                    const double *const *src, const double *cmask);
 
 #endif

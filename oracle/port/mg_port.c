@@ -24,7 +24,11 @@
 #define dmax(a, b) (((a) > (b)) ? (a) : (b))
 #define dmin(a, b) (((a) < (b)) ? (a) : (b))
 
-enum { G_SRC = 0, G_U, G_RES, G_LOP, G_RHS, G_CMASK, NGF };
+enum { G_SRC = 0, G_U, G_RES, G_LOP, G_RHS, G_CMASK, G_SRC1, G_SRC2, G_SRC3, NGF };
+/* source k of the operator (k < oracle_nsrc) */
+#define G_SRCK(k) ((k) ? G_SRC1 + (k) - 1 : G_SRC)
+static int is_src(int gf) { return gf == G_SRC || gf >= G_SRC1; }
+static int src_index(int gf) { return gf == G_SRC ? 0 : gf - G_SRC1 + 1; }
 
 typedef struct pgrid {
    struct pgrid *next;
@@ -60,6 +64,7 @@ static struct {
    int n_mg;
    int tf[NGF];           /* transfer bits of the current communication */
    int frozen;
+   int min_level;         /* coarsest AMR level of the MG hierarchy */
    double **sgh_bbox;     /* per AMR level: input bboxes in input order */
    int *sgh_num;
    port_result *r;
@@ -68,15 +73,26 @@ static struct {
 /* variable attributes (amrd/io.c:743-871 for this variable set) */
 static int mg_inject_of(int gf)
 {
+   if (is_src(gf)) {
+      const int k = src_index(gf);
+      if (k >= oracle_nsrc(P.c->pde)) return 0;   /* a source the operator does not have */
+      return k ? P.c->restr_srcx[k - 1] : P.c->restr_src;
+   }
    switch (gf) {
-   case G_SRC: return P.c->restr_src;
    case G_U: return P.c->restr_u;
    case G_RES: return P.c->restr_res;
    default: return 0;
    }
 }
-static int mg_noinj_to_amr(int gf) { return gf == G_SRC; }  /* hyperbolic var */
-static int in_amrh(int gf) { return gf == G_SRC || gf == G_U || gf == G_CMASK; }
+static int mg_noinj_to_amr(int gf) { return is_src(gf); }  /* hyperbolic vars */
+static int in_amrh(int gf) { return is_src(gf) || gf == G_U || gf == G_CMASK; }
+/* the fields a grid holds: every source the operator reads */
+static int used_fields(int mask)
+{
+   int k;
+   for (k = oracle_nsrc(P.c->pde); k < 4; k++) mask &= ~(1 << G_SRCK(k));
+   return mask;
+}
 
 /* misc.c:14-37 */
 static int fuzz_eq(double a, double b, double f) { return fabs(b - a) < f; }
@@ -608,7 +624,7 @@ static void build_mgh(void)
    P.frozen = 0;
    set_tf_bits(TF_MGH_INIT);
    P.frozen = 1;
-   for (l = P.n_amr; l >= 1; l--) {
+   for (l = P.n_amr; l >= P.min_level; l--) {
       cl--;
       /* replicate the AMR level (amr_to_mgh) */
       tmp[cl].dx[0] = P.amr[l].dx[0];
@@ -631,7 +647,7 @@ static void build_mgh(void)
             last = ng;
          }
       }
-      if (l > 1) continue;   /* rho_sp = 2: no MG levels between AMR levels */
+      if (l > P.min_level) continue;   /* rho_sp = 2: no MG levels between AMR levels */
       /* below the base: coarsen while islands allow it */
       cf = 1;
       n = -1;
@@ -672,7 +688,7 @@ static void build_mgh(void)
                for (ng = first.grids; ng;) {
                   pgrid *nx = ng->next;
                   ng->next = 0;
-                  alloc_fields(ng, (1 << NGF) - 1);
+                  alloc_fields(ng, used_fields((1 << NGF) - 1));
                   insert_grid(&tmp[cl], ng);
                   ng = nx;
                }
@@ -754,12 +770,13 @@ static double call_rr_app(int kind, int L, int comm_only)
    oracle_grid o;
    for (g = P.mg[L].grids; g; g = g->next) {
       if (g->comm || !comm_only) {
+         double *sv[4] = {g->gf[G_SRC], g->gf[G_SRC1], g->gf[G_SRC2], g->gf[G_SRC3]};
          to_ogrid(g, &o);
          if (kind == 0)
-            res = oracle_relax(P.c->pde, &o, g->gf[G_U], g->gf[G_RHS], g->gf[G_SRC], g->gf[G_CMASK]);
+            res = oracle_relax(P.c->pde, &o, g->gf[G_U], g->gf[G_RHS], (const double *const *)sv, g->gf[G_CMASK]);
          else
             res = oracle_residual(P.c->pde, &o, g->gf[G_RES], g->gf[G_RHS], g->gf[G_U],
-                                  g->gf[G_SRC], g->gf[G_CMASK]);
+                                  (const double *const *)sv, g->gf[G_CMASK]);
          hook_log(kind, L, grid_index(&P.mg[L], g), res);
          if (first) lres = res;
          lres = dmax(res, lres);
@@ -775,7 +792,8 @@ static void call_lop(int L)   /* call_app(app_L_op) amrd/util.c:39-50 */
    oracle_grid o;
    for (g = P.mg[L].grids; g; g = g->next) {
       to_ogrid(g, &o);
-      oracle_lop(P.c->pde, &o, g->gf[G_LOP], g->gf[G_U], g->gf[G_SRC], g->gf[G_CMASK]);
+      double *sv[4] = {g->gf[G_SRC], g->gf[G_SRC1], g->gf[G_SRC2], g->gf[G_SRC3]};
+      oracle_lop(P.c->pde, &o, g->gf[G_LOP], g->gf[G_U], (const double *const *)sv, g->gf[G_CMASK]);
       hook_log(2, L, grid_index(&P.mg[L], g), 0);
    }
 }
@@ -982,6 +1000,8 @@ int port_solve(const port_case *c, port_result *r)
    memcpy(P.bbox, c->base_bbox, sizeof(P.bbox));
    for (i = 0; i < c->ngrids; i++) P.n_amr = imax(P.n_amr, c->lev[i]);
    if (P.n_amr >= MAXLEV - 12) return 1;
+   P.min_level = c->min_level > 0 ? c->min_level : 1;
+   if (P.min_level > P.n_amr) return 1;
    /* level spacing: recalc_lev_info src/gh.c:54-81, ratio 2 */
    for (d = 0; d < 3; d++) {
       P.amr_dx[1][d] = d < P.dim ? (c->base_bbox[2 * d + 1] - c->base_bbox[2 * d]) / (c->base_shape[d] - 1) : 0;
@@ -1008,7 +1028,8 @@ int port_solve(const port_case *c, port_result *r)
          for (g = first.grids; g;) {
             pgrid *nx = g->next;
             g->next = 0;
-            alloc_fields(g, (1 << G_SRC) | (1 << G_U) | (1 << G_CMASK));
+            alloc_fields(g, used_fields((1 << G_SRC) | (1 << G_U) | (1 << G_CMASK) | (1 << G_SRC1) |
+                                        (1 << G_SRC2) | (1 << G_SRC3)));
             insert_grid(&P.amr[l], g);
             g = nx;
          }
@@ -1022,6 +1043,8 @@ int port_solve(const port_case *c, port_result *r)
       if (!m) return 2;
       memcpy(m->gf[G_U], c->u[i], sizeof(double) * (size_t)gsize(m));
       memcpy(m->gf[G_SRC], c->src[i], sizeof(double) * (size_t)gsize(m));
+      for (d = 1; d < oracle_nsrc(c->pde); d++)
+         memcpy(m->gf[G_SRCK(d)], c->srcx[d - 1][i], sizeof(double) * (size_t)gsize(m));
    }
 
    /* solve_elliptics amrd/mg.c:20-79 */

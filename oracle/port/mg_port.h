@@ -28,6 +28,11 @@ typedef struct {
    int restr_u, restr_res, restr_src;  /* 1 straight, 2 half weight, 3 full weight */
    int interp_order;                   /* 2 or 4 */
    int interp_buffer;                  /* PAMR default 2 (src/pamr.c:157) */
+   /* sources beyond the first (oracle_nsrc(pde) - 1 of them): srcx[k][i] is
+    * source k+1 of input grid i, restricted with restr_srcx[k] */
+   const double *const *srcx[3];
+   int restr_srcx[3];
+   int min_level;                      /* coarsest AMR level of the MG hierarchy (solve_elliptics' L) */
 } port_case;
 
 typedef struct {

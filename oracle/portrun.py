@@ -38,7 +38,9 @@ class _Case(C.Structure):
                 ("tol", C.c_double), ("crtol", C.c_double), ("w0_r", C.c_double),
                 ("w0_i", C.c_double), ("min_cwidth", C.c_int),
                 ("restr_u", C.c_int), ("restr_res", C.c_int), ("restr_src", C.c_int),
-                ("interp_order", C.c_int), ("interp_buffer", C.c_int)]
+                ("interp_order", C.c_int), ("interp_buffer", C.c_int),
+                ("srcx", C.POINTER(C.POINTER(C.c_double)) * 3), ("restr_srcx", C.c_int * 3),
+                ("min_level", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -91,6 +93,14 @@ def solve(case, hook_cap: int = 0) -> dict:
     c.min_cwidth = p.min_cwidth
     c.restr_u, c.restr_res, c.restr_src = p.restr_u, p.restr_res, p.restr_src
     c.interp_order, c.interp_buffer = p.interp_order, 2
+    keep = []
+    for k in range(1, case.nsrc):
+        sk = [np.ascontiguousarray(a, dtype=np.float64) for a in case.source(k)]
+        arr = (C.POINTER(C.c_double) * n)(*[a.ctypes.data_as(C.POINTER(C.c_double)) for a in sk])
+        keep.append((sk, arr))
+        c.srcx[k - 1] = C.cast(arr, C.POINTER(C.POINTER(C.c_double)))
+        c.restr_srcx[k - 1] = case.restr_src_k(k)
+    c.min_level = case.min_level
     res = np.zeros(max(1, p.max_iter))
     r = _Result()
     r.res = res.ctypes.data_as(C.POINTER(C.c_double))

@@ -43,10 +43,12 @@ typedef struct {
    double bbox[6];
    int shape[3];
    long n;
-   double *u, *src;
+   double *u, *src[4];
 } case_grid;
 
-static int c_dim, c_pde, c_ngrids;
+static int c_dim, c_pde, c_ngrids, c_nsrc, c_min_level;
+/* names of the source variables in the parameter file (oracle/refrun.py) */
+static const char *const SRC_NAMES[4] = {"rho", "rho1", "rho2", "rho3"};
 static case_grid *c_grids;
 
 /* --------------------------------------------------------------- output -- */
@@ -59,7 +61,7 @@ static void rec(int tag, const void *p, long nbytes)
 }
 
 /* ------------------------------------------------------------ hook state -- */
-static int gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src;
+static int gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src, gfn_srck[4];
 
 /* MG hierarchy map, captured at the first hook call */
 #define MAXG 4096
@@ -185,6 +187,15 @@ static void keep_mask(int kind, cur_grid *g)
    memcpy(m->m, g->gfs[gfn_cmask - 1], sizeof(double) * (size_t)n);
 }
 
+/* the MG instances of the sources on the hook's grid */
+static const double *const *grid_src(cur_grid *g)
+{
+   static double *sv[4];
+   int k;
+   for (k = 0; k < c_nsrc; k++) sv[k] = g->gfs[gfn_srck[k] - 1];
+   return (const double *const *)sv;
+}
+
 static double h_relax(void)
 {
    cur_grid g;
@@ -193,8 +204,7 @@ static double h_relax(void)
    ldptr(&g);
    to_ogrid(&g, &o);
    keep_mask(0, &g);
-   norm = oracle_relax(c_pde, &o, g.gfs[gfn_u - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_src - 1],
-                       g.gfs[gfn_cmask - 1]);
+   norm = oracle_relax(c_pde, &o, g.gfs[gfn_u - 1], g.gfs[gfn_rhs - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(0, &g, norm);
    return norm;
 }
@@ -207,7 +217,7 @@ static double h_residual(void)
    ldptr(&g);
    to_ogrid(&g, &o);
    norm = oracle_residual(c_pde, &o, g.gfs[gfn_res - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_u - 1],
-                          g.gfs[gfn_src - 1], g.gfs[gfn_cmask - 1]);
+                          grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(1, &g, norm);
    return norm;
 }
@@ -219,8 +229,7 @@ static void h_lop(void)
    ldptr(&g);
    to_ogrid(&g, &o);
    keep_mask(1, &g);
-   oracle_lop(c_pde, &o, g.gfs[gfn_lop - 1], g.gfs[gfn_u - 1], g.gfs[gfn_src - 1],
-              g.gfs[gfn_cmask - 1]);
+   oracle_lop(c_pde, &o, g.gfs[gfn_lop - 1], g.gfs[gfn_u - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(2, &g, 0);
 }
 
@@ -236,6 +245,8 @@ static void read_case(const char *path)
    c_dim = hdr[0];
    c_pde = hdr[1];
    c_ngrids = hdr[2];
+   c_min_level = hdr[3] > 0 ? hdr[3] : 1;
+   c_nsrc = oracle_nsrc(c_pde);
    c_grids = (case_grid *)calloc((size_t)c_ngrids, sizeof(case_grid));
    for (i = 0; i < c_ngrids; i++) {
       case_grid *g = &c_grids[i];
@@ -244,9 +255,14 @@ static void read_case(const char *path)
       if (fread(g->bbox, 8, 6, f) != 6) exit(2);
       g->n = (long)g->shape[0] * g->shape[1] * g->shape[2];
       g->u = (double *)malloc(sizeof(double) * (size_t)g->n);
-      g->src = (double *)malloc(sizeof(double) * (size_t)g->n);
       if (fread(g->u, 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
-      if (fread(g->src, 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+      {
+         int k;
+         for (k = 0; k < c_nsrc; k++) {
+            g->src[k] = (double *)malloc(sizeof(double) * (size_t)g->n);
+            if (fread(g->src[k], 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+         }
+      }
    }
    fclose(f);
 }
@@ -268,8 +284,8 @@ static case_grid *match_case_grid(int L, const double *bbox, const int *shape)
    return 0;
 }
 
-/* fill (dir=0) or read back (dir=1) u and the source on every AMR grid */
-static void amr_data(int dir, int gu, int gs)
+/* fill (dir=0) or read back (dir=1) u and the sources on every AMR grid */
+static void amr_data(int dir, int gu, const int *gs)
 {
    int L, valid, Lmax = PAMR_get_max_lev(PAMR_AMRH);
    for (L = 1; L <= Lmax; L++) {
@@ -281,8 +297,9 @@ static void amr_data(int dir, int gu, int gs)
          PAMR_get_g_attribs(&rank, &dim, shape, bbox, gw, &t, &ngfs, x, gfs);
          cg = match_case_grid(L, bbox, shape);
          if (dir == 0) {
+            int k;
             memcpy(gfs[gu - 1], cg->u, sizeof(double) * (size_t)cg->n);
-            memcpy(gfs[gs - 1], cg->src, sizeof(double) * (size_t)cg->n);
+            for (k = 0; k < c_nsrc; k++) memcpy(gfs[gs[k] - 1], cg->src[k], sizeof(double) * (size_t)cg->n);
          } else
             memcpy(cg->u, gfs[gu - 1], sizeof(double) * (size_t)cg->n);
          valid = PAMR_next_g();
@@ -295,13 +312,14 @@ static void amr_data(int dir, int gu, int gs)
  * gfns are matched first. */
 static void resolve(const double *p, int *out)
 {
-   int i, h, q;
-   int pref[6];
+   int i, h, q, np = 6;
+   int pref[9];
    pref[0] = gfn_src; pref[1] = gfn_u; pref[2] = gfn_res;
    pref[3] = gfn_lop; pref[4] = gfn_rhs; pref[5] = gfn_cmask;
+   for (q = 1; q < c_nsrc; q++) pref[np++] = gfn_srck[q];
    out[0] = out[1] = out[2] = -1;
    for (i = 0; i < n_mgmap; i++)
-      for (q = 0; q < 6; q++)
+      for (q = 0; q < np; q++)
          if (mgmap[i].gfs[pref[q] - 1] == p) {
             out[0] = mgmap[i].L;
             out[1] = mgmap[i].idx;
@@ -322,7 +340,7 @@ int main(int argc, char **argv)
 {
    int i, num, *lev;
    double *bbox;
-   int gu_amr, gs_amr;
+   int gu_amr, gs_amr[4], k;
    int amr_lc = 0, amr_width = -1;
    if (argc < 4) {
       fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops [interp:lc:width]]\n", argv[0]);
@@ -360,14 +378,21 @@ int main(int argc, char **argv)
    }
 
    gu_amr = PAMR_get_gfn("u", PAMR_AMRH, 1);
-   gs_amr = PAMR_get_gfn("rho", PAMR_AMRH, 1);
+   for (k = 0; k < c_nsrc; k++) {
+      gs_amr[k] = PAMR_get_gfn((char *)SRC_NAMES[k], PAMR_AMRH, 1);
+      gfn_srck[k] = PAMR_get_gfn((char *)SRC_NAMES[k], PAMR_MGH, 0);
+      if (gs_amr[k] < 0 || gfn_srck[k] < 0) {
+         fprintf(stderr, "ref_mg: source variable %s missing\n", SRC_NAMES[k]);
+         return 3;
+      }
+   }
    gfn_u = PAMR_get_gfn("u", PAMR_MGH, 0);
    gfn_res = PAMR_get_gfn("u_res", PAMR_MGH, 0);
    gfn_lop = PAMR_get_gfn("u_lop", PAMR_MGH, 0);
    gfn_rhs = PAMR_get_gfn("u_rhs", PAMR_MGH, 0);
    gfn_cmask = PAMR_get_gfn("cmask", PAMR_MGH, 0);
    gfn_src = PAMR_get_gfn("rho", PAMR_MGH, 0);
-   if (gu_amr < 0 || gs_amr < 0 || gfn_u < 0 || gfn_res < 0 || gfn_lop < 0 || gfn_rhs < 0 ||
+   if (gu_amr < 0 || gfn_u < 0 || gfn_res < 0 || gfn_lop < 0 || gfn_rhs < 0 ||
        gfn_cmask < 0 || gfn_src < 0) {
       fprintf(stderr, "ref_mg: missing variable definitions\n");
       return 3;
@@ -386,7 +411,7 @@ int main(int argc, char **argv)
          return 3;
       }
    } else
-      solve_elliptics(1, 1, 0);
+      solve_elliptics(c_min_level, 1, 0);
    mur8_log_enabled = 0;
 
    amr_data(1, gu_amr, gs_amr);
@@ -394,7 +419,8 @@ int main(int argc, char **argv)
    fout = fopen(argv[3], "wb");
    if (!fout) return 4;
    {
-      int gf[6] = {gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src};
+      int gf[9] = {gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src, 0, 0, 0};
+      for (k = 1; k < c_nsrc; k++) gf[5 + k] = gfn_srck[k];
       rec(1, &AMRD_curr_MG_iter, 4);
       rec(2, gf, sizeof(gf));
       rec(3, hlog, (long)sizeof(hook_rec) * n_hlog);

@@ -10,7 +10,8 @@ reference's ``init_context`` (amrd/io.c:36) reads: one elliptic variable
 ``u`` (mg_sync, mg_interp2, HW restriction) whose residual ``u_res`` uses
 full weighting, and one source ``rho`` defined as a hyperbolic variable so
 it lives in both hierarchies and is restricted onto pure MG levels
-(examples/nbs/nbs.fparam pattern).
+(examples/nbs/nbs.fparam pattern). Operators with several sources (the nbs
+potential reads phi_r and phi_i) get ``rho1``, ``rho2`` .. beside ``rho``.
 """
 from __future__ import annotations
 
@@ -25,6 +26,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(HERE, "_ref", "ref_mg")
 
 _OP_NAME = {1: "STRAIGHT", 2: "HW", 3: "FW"}
+# the gfns ref_main.c reports, in its order (src1.. only for operators with several sources)
+GFN_KEYS = ("u", "res", "lop", "rhs", "cmask", "src", "src1", "src2", "src3")
+# source variables as oracle/ref_main.c names them
+SRC_NAMES = ("rho", "rho1", "rho2", "rho3")
 
 
 def available() -> bool:
@@ -49,8 +54,8 @@ def param_file(case, amr_interp_order: int = 0) -> str:
         "num_evo_tl := 2",
         "rho_sp := 2",
         "rho_tm := 2",
-        'num_hyperbolic_vars := 1',
-        'hyperbolic_vars := [ "rho" ]',
+        f'num_hyperbolic_vars := {case.nsrc}',
+        'hyperbolic_vars := [ ' + " ".join(f'"{n}"' for n in SRC_NAMES[:case.nsrc]) + ' ]',
         'num_elliptic_vars := 1',
         'elliptic_vars := [ "u" ]',
         "num_mg_sync := 1",
@@ -69,7 +74,8 @@ def param_file(case, amr_interp_order: int = 0) -> str:
         "min_mg_cwidth := [" + " ".join(str(p.min_cwidth) for _ in range(dim)) + "]",
     ]
     hw, fw = [], []
-    for name, op in (("u", p.restr_u), ("rho", p.restr_src), ("u_res", p.restr_res)):
+    srcs = [(SRC_NAMES[k], case.restr_src_k(k)) for k in range(case.nsrc)]
+    for name, op in [("u", p.restr_u)] + srcs + [("u_res", p.restr_res)]:
         if op == 2:
             hw.append(name)
         elif op == 3:
@@ -92,12 +98,15 @@ def param_file(case, amr_interp_order: int = 0) -> str:
 
 
 def case_bytes(case) -> bytes:
-    out = [struct.pack("<4i", case.dim, case.pde, len(case.grids), 0)]
-    for g, u, s in zip(case.grids, case.u0, case.src):
+    """header (dim, pde, grids, coarsest AMR level of the MG hierarchy),
+    then per grid level, shape, bbox, u and each source"""
+    out = [struct.pack("<4i", case.dim, case.pde, len(case.grids), case.min_level)]
+    for i, (g, u) in enumerate(zip(case.grids, case.u0)):
         bb = list(g.bbox) + [0.0] * (6 - len(g.bbox))
         out.append(struct.pack("<4i6d", g.level, *g.shape, *bb))
         out.append(np.ascontiguousarray(u, dtype="<f8").tobytes())
-        out.append(np.ascontiguousarray(s, dtype="<f8").tobytes())
+        for k in range(case.nsrc):
+            out.append(np.ascontiguousarray(case.source(k)[i], dtype="<f8").tobytes())
     return b"".join(out)
 
 
@@ -142,8 +151,8 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         if tag == 1:
             res["iters"] = struct.unpack("<i", p)[0]
         elif tag == 2:
-            res["gfn"] = dict(zip(("u", "res", "lop", "rhs", "cmask", "src"),
-                                  struct.unpack("<6i", p)))
+            v = struct.unpack(f"<{len(p) // 4}i", p)
+            res["gfn"] = {k: g for k, g in zip(GFN_KEYS, v) if g > 0}
         elif tag == 3:
             a = np.frombuffer(p, dtype=np.dtype([("kind", "<i4"), ("L", "<i4"), ("idx", "<i4"),
                                                  ("pad", "<i4"), ("norm", "<f8")]))

@@ -22,7 +22,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"], "pgb_noalloc.cu": ["-fmad=false"],
               "pgb_mutil_ex.cu": ["-fmad=false"], "pgb_bo.cu": ["-fmad=false"], "pgb_diss.cu": ["-fmad=false"], "pgb_linbnd.cu": ["-fmad=false"], "pgb_kernels32.cu": [],
               "pgb_net.cu": []}
-C_SOURCES = ["pgb_plan.c", "pgb_solver.c"]
+C_SOURCES = ["pgb_plan.c", "pgb_solver.c", "pgb_op.c"]
 
 
 def cuda_home() -> str:

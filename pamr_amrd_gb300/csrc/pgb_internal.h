@@ -19,8 +19,36 @@ extern "C" {
 #endif
 
 /* grid functions, in PAMR gfn order for the AMRD variable set
- * (hyperbolic source first, then f, f_res, f_lop, f_rhs; amrd/io.c:708-937) */
-enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, PGB_NF = 5 };
+ * (hyperbolic source first, then f, f_res, f_lop, f_rhs; amrd/io.c:708-937);
+ * sources 1..3 of an operator with several source fields follow (their
+ * arrays exist only when the operator reads them) */
+enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, PGB_F_SRC1 = 5,
+       PGB_NF = 8 };
+#define PGB_NSRC_MAX 4
+#define PGB_SRC_FIELD(k) ((k) ? PGB_F_SRC1 + (k) - 1 : PGB_F_SRC)
+/* field mask of sources 0..n-1 */
+#define PGB_SRC_MASK(n) ((1 << PGB_F_SRC) | ((((1 << ((n) > 1 ? (n) - 1 : 0)) - 1)) << PGB_F_SRC1))
+
+/* Device form of a level operator L[u] = (program of lap u, u, sources)
+ * and its diagonal dL/du: a short stack program of one-byte instructions
+ * (low 4 bits opcode, high 4 bits argument: source or constant index),
+ * evaluated left to right in IEEE double arithmetic, one rounding per
+ * operation, so that an operator written in the order of an application's
+ * hook (e.g. examples/nbs/num.f:113-116) rounds exactly like it. kind
+ * selects a compiled form for the built-in operators (same arithmetic). */
+#define PGB_PROG_MAX 32
+#define PGB_PROG_CONST 8
+#define PGB_PROG_STACK 8
+enum { PGB_P_END = 0, PGB_P_LAP, PGB_P_J0, PGB_P_U, PGB_P_SRC, PGB_P_CONST, PGB_P_ADD, PGB_P_SUB,
+       PGB_P_MUL, PGB_P_DIV, PGB_P_NEG };
+enum { PGB_OPK_POISSON = 0, PGB_OPK_CONFORMAL = 1, PGB_OPK_LAPSE = 2, PGB_OPK_PROGRAM = 3 };
+typedef struct {
+   int kind;                            /* PGB_OPK_* */
+   int nsrc;                            /* source fields the operator reads (0..PGB_NSRC_MAX) */
+   unsigned char lcode[PGB_PROG_MAX];   /* L[u] */
+   unsigned char jcode[PGB_PROG_MAX];   /* dL/du */
+   double cst[PGB_PROG_CONST];
+} pgb_dop;
 
 #define PGB_MAXLEV 48
 
@@ -38,6 +66,7 @@ enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, 
 
 typedef struct {
    double *f[PGB_NF];
+   const pgb_dop *op;            /* the level operator (device copy) */
    const uint8_t *cmask_child;   /* set_cmask_child, amrd/mg.c:362-426 */
    const uint8_t *cmask_bdy;     /* set_cmask_bdy, amrd/mg.c:432-488 */
    float *w32[PGB_NW32];         /* mixed form: correction, defect, Jacobian term, coarse correction,

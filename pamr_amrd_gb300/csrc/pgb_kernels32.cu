@@ -35,6 +35,7 @@
 #include <stdio.h>
 #include "pgb_dev.h"
 #include "pgb_opgrid.cuh"
+#include "pgb_op.cuh"
 
 static __thread char g_err32[256];
 static unsigned long long g_launches32 = 0;
@@ -55,6 +56,14 @@ static int check32(const char *what)
 extern "C" const char *pgb_dev_error32(void) { return g_err32; }
 
 #define NT (PGB_TX * PGB_TY)
+
+/* launches the instantiation of an operator kernel for the level
+ * operator's form: compiled built-in (PROG = false) or program (true) */
+#define OPLAUNCH(kern, pde, grid, blk, smem, st, ...)                                   \
+   do {                                                                                 \
+      if ((pde) == PGB_OPK_PROGRAM) kern<true><<<(grid), (blk), (smem), (st)>>>(__VA_ARGS__); \
+      else kern<false><<<(grid), (blk), (smem), (st)>>>(__VA_ARGS__);                   \
+   } while (0)
 #define TWO_PI 6.283185307179586
 
 /* the FP32 arrays of a box: correction, defect, Jacobian term, coarse correction */
@@ -177,8 +186,14 @@ __device__ __forceinline__ double lapw(const pgb_dbox &b, const double *u, long 
 /* L[u] from lap u for the three operators (Poisson t - s, conformal factor
  * t + 2 pi s u^5, lapse t - s u; num.f:85-123 pattern) and, in c, the FP32
  * derivative of the non-Laplacian part (5 * 2 pi s u^4, -s, 0) */
-__device__ __forceinline__ double opjac(int pde, double t, double uc, double s, float &c)
+template <bool PROG>
+__device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, double t, double uc, double s,
+                                        float &c)
 {
+   if (PROG) {   /* an application's operator program (pgb_op.cuh) */
+      c = d2f(__dsub_rn(pgb_prog_J(b, uc, s, p), b.j0));
+      return pgb_prog_L(b, t, uc, s, p);
+   }
    if (pde == 1) {
       double p2 = uc * uc, a = TWO_PI * s * (p2 * p2);
       c = 5.f * d2f(a);
@@ -199,6 +214,7 @@ __device__ __forceinline__ double opjac(int pde, double t, double uc, double s, 
  * E is 0 on entry (every block ends by clearing it). With cover = 1 only
  * the level's cover tiles are visited: elsewhere rhs stays 0 and D is the
  * FP32 update k_defect32 made at the end of the previous post-smoothing. */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                    double w0_r, int cover, int split)
 {
@@ -231,7 +247,7 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
       double r = 0.0;
       if (in && (cm || rl)) {
          float c;
-         const double l = opjac(pde, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c);
+         const double l = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c);
          if (cm) r = fma(-res[p], w0_r, l);
          if (rl) {
             wd[p] = d2f(r - l);
@@ -929,6 +945,7 @@ __device__ double block_sum32(double v, double *sm)
  * relaxed points, D = -res and C for the next smoothing block of this
  * level, and call_rr_app's norm (per-box RMS, max over boxes) reduced by the
  * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
                                                       pgb_trace *trace, int split, const int *gate)
@@ -960,7 +977,7 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
          const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
          if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
             float c;
-            const double r = opjac(pde, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c) - rhs[p];
+            const double r = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c) - rhs[p];
             res[p] = r;
             wd[p] = d2f(-r);
             wc[p] = c;
@@ -1010,6 +1027,7 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
 
 /* L_op + compute_MG_rhs (amrd/mg.c:271-314) on the cover tiles of the
  * coarsest level, which the coarsest-grid loop smooths by itself */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                      double w0_r)
 {
@@ -1029,7 +1047,7 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
       const int cm = b.cmask_child[p];
       float c;
       if (cm && interior32(b, i, j, k, lv.dim))
-         lopv = opjac(pde, lapm(b, u, p, sy, sz, lv.dim), u[p], b.f[PGB_F_SRC][p], c);
+         lopv = opjac<PROG>(pde, b, p, lapm(b, u, p, sy, sz, lv.dim), u[p], b.f[PGB_F_SRC][p], c);
       b.f[PGB_F_RHS][p] = cm ? fma(-b.f[PGB_F_RES][p], w0_r, lopv) : 0.0;
       b.f[PGB_F_LOP][p] = u[p];
    }
@@ -1054,6 +1072,7 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
  * against MG_max_citer. */
 #define CM_MAXB 16
 #define CMT 256
+template <bool PROG>
 __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                         const pgb_copy_op *sync_ops, int nsync,
                                                         pgb_coarsest_args a, pgb_trace *trace)
@@ -1121,7 +1140,7 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
          for (int q = t; q < nrel; q += CMT) {
             const int p = lst[q < ncol[c][0] ? q : n - nrel + q];
             float cv;
-            const double r = opjac(pde, lapm(bx, u, p, sy, sz, dim), u[p], src[p], cv) - rhs[p];
+            const double r = opjac<PROG>(pde, bx, p, lapm(bx, u, p, sy, sz, dim), u[p], src[p], cv) - rhs[p];
             d[p] = d2f(-r);
             cj[p] = cv;
             acc = fma(r, r, acc);
@@ -1244,7 +1263,8 @@ extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, d
    const int n = cover ? lv.nctiles : lv.ntiles;
    if (!n) return 0;
    const int sp = split_for(lv, n);
-   k_fas_defect<<<n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r, cover, sp);
+   OPLAUNCH(k_fas_defect, pde, n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r, cover,
+            sp);
    return check32("fas_defect");
 }
 
@@ -1415,8 +1435,8 @@ extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde
    if (!lv.ntiles) return 0;
    int sp = split_for(lv, lv.ntiles);
    while (sp > 1 && (long)lv.ntiles * sp > sc.npartial) sp /= 2;   /* one partial sum per CTA */
-   k_residual_fast<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
-                                                                                       norm_out, trace, sp, gate);
+   OPLAUNCH(k_residual_fast, pde, lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, sc,
+            norm_out, trace, sp, gate);
    return check32("residual_fast");
 }
 
@@ -1424,7 +1444,7 @@ extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                   void *stream)
 {
    if (!lv.nctiles) return 0;
-   k_lop_rhs_fast<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   OPLAUNCH(k_lop_rhs_fast, pde, lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r);
    return check32("lop_rhs_fast");
 }
 
@@ -1437,10 +1457,11 @@ extern "C" int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pd
    static int attr_set = 0;
    if (a.smem_points <= 0 || a.ncoarse > CM_MAXB || smem > 200 * 1024) return 1;
    if (!attr_set) {
-      cudaFuncSetAttribute(k_coarsest_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      cudaFuncSetAttribute(k_coarsest_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      cudaFuncSetAttribute(k_coarsest_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       attr_set = 1;
    }
-   k_coarsest_mixed<<<1, CMT, smem, (cudaStream_t)stream>>>(
-      boxes, lv, pde, (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
+   OPLAUNCH(k_coarsest_mixed, pde, 1, CMT, smem, (cudaStream_t)stream, boxes, lv, pde,
+            (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
    return check32("coarsest_mixed") ? -1 : 0;
 }

@@ -20,6 +20,7 @@
 #include <string.h>
 #include "pgb_dev.h"
 #include "pgb_opgrid.cuh"
+#include "pgb_op.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -52,6 +53,14 @@ extern "C" int pgb_dev_sync(void *stream)
 }
 
 #define NT (PGB_TX * PGB_TY)
+
+/* launches the instantiation of an operator kernel for the level
+ * operator's form: compiled built-in (PROG = false) or program (true) */
+#define OPLAUNCH(kern, pde, grid, blk, smem, st, ...)                                   \
+   do {                                                                                 \
+      if ((pde) == PGB_OPK_PROGRAM) kern<true><<<(grid), (blk), (smem), (st)>>>(__VA_ARGS__); \
+      else kern<false><<<(grid), (blk), (smem), (st)>>>(__VA_ARGS__);                   \
+   } while (0)
 
 /* ------------------------------------------------------------ operators -- */
 /* 2*pi and 5*2*pi, the constants of the conformal-factor hook */
@@ -91,24 +100,31 @@ __device__ __forceinline__ double lap64(const pgb_dbox &b, const double *u, long
    return t;
 }
 
-__device__ __forceinline__ double op64(int pde, double t, double u, double s)
+/* L[u] at point p of box b from t = lap u: the built-in operators in the
+ * order of their hooks, or the box's operator program (pgb_op.cuh) */
+template <bool PROG>
+__device__ __forceinline__ double op64(int pde, const pgb_dbox &b, long p, double t, double u, double s)
 {
-   if (pde == 1) {
+   if (PROG) return pgb_prog_L(b, t, u, s, p);
+   if (pde == PGB_OPK_CONFORMAL) {
       double p2 = u * u, p4 = p2 * p2;
       return t + TWO_PI * s * (p4 * u);
    }
-   if (pde == 2) return t - s * u;
+   if (pde == PGB_OPK_LAPSE) return t - s * u;
    return t - s;
 }
 
-__device__ __forceinline__ double jac64(int pde, double j0, double u, double s)
+/* dL/du at point p (the relaxation's Newton diagonal) */
+template <bool PROG>
+__device__ __forceinline__ double jac64(int pde, const pgb_dbox &b, long p, double u, double s)
 {
-   if (pde == 1) {
+   if (PROG) return pgb_prog_J(b, u, s, p);
+   if (pde == PGB_OPK_CONFORMAL) {
       double p2 = u * u;
-      return j0 + TEN_PI * s * (p2 * p2);
+      return b.j0 + TEN_PI * s * (p2 * p2);
    }
-   if (pde == 2) return j0 - s;
-   return j0;
+   if (pde == PGB_OPK_LAPSE) return b.j0 - s;
+   return b.j0;
 }
 
 __device__ __forceinline__ bool interior(const pgb_dbox &b, int i, int j, int k, int dim)
@@ -186,6 +202,7 @@ __device__ bool last_block(pgb_scratch sc, int *flag)
 
 /* ---------------------------------------------------------------- relax -- */
 /* one colour pass of relax (num.f:216-241); pass 1 finalizes the norm */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                               int pass, pgb_scratch sc, double *norm_out,
                                               pgb_trace *trace)
@@ -208,8 +225,8 @@ __global__ void __launch_bounds__(NT) k_relax(const pgb_dbox *boxes, pgb_dlevel 
       long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
       double uc = u[p], s = src[p];
-      double res = op64(pde, lap64(b, u, p, dim), uc, s) - rhs[p];
-      double jac = jac64(pde, b.j0, uc, s);
+      double res = op64<PROG>(pde, b, p, lap64(b, u, p, dim), uc, s) - rhs[p];
+      double jac = jac64<PROG>(pde, b, p, uc, s);
       u[p] = uc - res / jac;
       acc += res * res;
    }
@@ -225,15 +242,16 @@ extern "C" int pgb_k_relax(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_sc
    dim3 blk(PGB_TX, PGB_TY);
    cudaStream_t st = (cudaStream_t)stream;
    if (lv.nrtiles == 0) return 0;
-   k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 0, sc, norm_out, trace);
+   OPLAUNCH(k_relax, pde, lv.nrtiles, blk, 0, st, boxes, lv, pde, 0, sc, norm_out, trace);
    LAUNCHED(1);
-   k_relax<<<lv.nrtiles, blk, 0, st>>>(boxes, lv, pde, 1, sc, norm_out, trace);
+   OPLAUNCH(k_relax, pde, lv.nrtiles, blk, 0, st, boxes, lv, pde, 1, sc, norm_out, trace);
    LAUNCHED(1);
    return check("relax");
 }
 
 /* ------------------------------------------------------------- residual -- */
 /* residual (num.f:129-161): res = L[u] - rhs where cmask is ON */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                  pgb_scratch sc, double *norm_out,
                                                  pgb_trace *trace)
@@ -253,7 +271,7 @@ __global__ void __launch_bounds__(NT) k_residual(const pgb_dbox *boxes, pgb_dlev
       if (!interior(b, i, j, k, dim)) continue;
       long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
-      double r = op64(pde, lap64(b, u, p, dim), u[p], src[p]) - rhs[p];
+      double r = op64<PROG>(pde, b, p, lap64(b, u, p, dim), u[p], src[p]) - rhs[p];
       res[p] = r;
       acc += r * r;
    }
@@ -267,8 +285,8 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
                               double *norm_out, pgb_trace *trace, void *stream)
 {
    if (lv.ntiles == 0) return 0;
-   k_residual<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, sc,
-                                                                             norm_out, trace);
+   OPLAUNCH(k_residual, pde, lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, sc,
+            norm_out, trace);
    LAUNCHED(1);
    return check("residual");
 }
@@ -300,6 +318,7 @@ __global__ void __launch_bounds__(NT) k_clear(const pgb_dbox *boxes, pgb_dlevel 
  * with compute_MG_rhs (amrd/mg.c:271-314): rhs = cmask ? -res*w0_r + lop : 0,
  * then lop = u, on the level's cover tiles (every child-covered point lies in
  * one; elsewhere rhs keeps the 0 pgb_prepare wrote and lop is never read). */
+template <bool PROG>
 __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                 double w0_r)
 {
@@ -308,7 +327,7 @@ __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dleve
       double lopv = 0;
       int cm = b.cmask_child[p];
       if (cm && interior(b, i, j, k, lv.dim))
-         lopv = op64(pde, lap64(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
+         lopv = op64<PROG>(pde, b, p, lap64(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
       b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
       b.f[PGB_F_LOP][p] = u[p];
    })
@@ -339,7 +358,7 @@ extern "C" int pgb_k_lop_rhs(const pgb_dbox *boxes, pgb_dlevel lv, int pde, doub
                              void *stream)
 {
    if (!lv.nctiles) return 0;
-   k_lop_rhs<<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   OPLAUNCH(k_lop_rhs, pde, lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r);
    LAUNCHED(1);
    return check("lop_rhs");
 }
@@ -719,6 +738,7 @@ __device__ unsigned long long block_xor(unsigned long long v, unsigned long long
    return v;
 }
 
+template <bool PROG>
 __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                  const pgb_copy_op *sync_ops, int nsync,
                                                  pgb_coarsest_args a, pgb_trace *trace)
@@ -752,8 +772,8 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
                double *u = bx.f[PGB_F_U];
                double uc = u[p], s = bx.f[PGB_F_SRC][p];
-               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
-               double jac = jac64(pde, bx.j0, uc, s);
+               double r = op64<PROG>(pde, bx, p, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
+               double jac = jac64<PROG>(pde, bx, p, uc, s);
                u[p] = uc - r / jac;
                acc += r * r;
             }
@@ -882,6 +902,7 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
 #define PGB_CL 8
 #define CLT 512
 #define MAXCB 8
+template <bool PROG>
 __global__ void __cluster_dims__(PGB_CL, 1, 1) __launch_bounds__(CLT)
    k_coarsest_cl(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_coarsest_args a,
                  pgb_trace *trace)
@@ -927,8 +948,8 @@ __global__ void __cluster_dims__(PGB_CL, 1, 1) __launch_bounds__(CLT)
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
                double *u = bx.f[PGB_F_U];
                double uc = u[p], s = bx.f[PGB_F_SRC][p];
-               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
-               double jac = jac64(pde, bx.j0, uc, s);
+               double r = op64<PROG>(pde, bx, p, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
+               double jac = jac64<PROG>(pde, bx, p, uc, s);
                double nu = uc - r / jac;
                u[p] = nu;
                acc[c] += r * r;
@@ -1046,6 +1067,7 @@ __global__ void __cluster_dims__(PGB_CL, 1, 1) __launch_bounds__(CLT)
  * removes the global-memory round trips from every sweep. Same iteration,
  * same cycle skip and same results as k_coarsest. */
 #define CS_MAXB 16
+template <bool PROG>
 __global__ void __launch_bounds__(CT) k_coarsest_smem(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       const pgb_copy_op *sync_ops, int nsync,
                                                       pgb_coarsest_args a, pgb_trace *trace)
@@ -1109,8 +1131,8 @@ __global__ void __launch_bounds__(CT) k_coarsest_smem(const pgb_dbox *boxes, pgb
                long p = i + sy * j + sz * k;
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
                double uc = u[p], s = src[p];
-               double r = op64(pde, lap64(bx, u, p, dim), uc, s) - rhs[p];
-               double jac = jac64(pde, bx.j0, uc, s);
+               double r = op64<PROG>(pde, bx, p, lap64(bx, u, p, dim), uc, s) - rhs[p];
+               double jac = jac64<PROG>(pde, bx, p, uc, s);
                u[p] = uc - r / jac;
                acc += r * r;
             }
@@ -1228,19 +1250,19 @@ extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, con
    if (want_smem && a.smem_points > 0 && a.ncoarse <= CS_MAXB && smem <= 200 * 1024) {
       static int attr_set = 0;
       if (!attr_set) {
-         cudaFuncSetAttribute(k_coarsest_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+         cudaFuncSetAttribute(k_coarsest_smem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+         cudaFuncSetAttribute(k_coarsest_smem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
          attr_set = 1;
       }
-      k_coarsest_smem<<<1, CT, smem, (cudaStream_t)stream>>>(
-         boxes, lv, pde, (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
+      OPLAUNCH(k_coarsest_smem, pde, 1, CT, smem, (cudaStream_t)stream, boxes, lv, pde,
+               (const pgb_copy_op *)sync->d_ops, sync->nops, a, trace);
       LAUNCHED(1);
    } else if (want_cl && sync->nops == 0 && lv.nbox <= MAXCB) {
-      k_coarsest_cl<<<PGB_CL, CLT, 0, (cudaStream_t)stream>>>(boxes, lv, pde, a, trace);
+      OPLAUNCH(k_coarsest_cl, pde, PGB_CL, CLT, 0, (cudaStream_t)stream, boxes, lv, pde, a, trace);
       LAUNCHED(1);
    } else {
-      k_coarsest<<<1, CT, 0, (cudaStream_t)stream>>>(boxes, lv, pde,
-                                                     (const pgb_copy_op *)sync->d_ops, sync->nops,
-                                                     a, trace);
+      OPLAUNCH(k_coarsest, pde, 1, CT, 0, (cudaStream_t)stream, boxes, lv, pde, (const pgb_copy_op *)sync->d_ops,
+               sync->nops, a, trace);
       LAUNCHED(1);
    }
    return check("coarsest");

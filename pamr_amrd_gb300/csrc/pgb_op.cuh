@@ -1,0 +1,78 @@
+/*
+ * Device evaluation of a level operator (pgb_dop, pgb_internal.h): the
+ * program of L[u] and of dL/du at one point, every operation rounded once
+ * in IEEE double (explicit _rn intrinsics, so no FMA contraction whatever
+ * the translation unit's -fmad setting). Shared by the FP64 kernels and the
+ * FP64 passes of the mixed form.
+ */
+#ifndef PGB_OP_CUH
+#define PGB_OP_CUH
+
+#include "pgb_internal.h"
+
+/* the source values an operator reads at point p of box b; s0 is passed
+ * in (some kernels hold it in shared memory), the others come from the
+ * box's source arrays */
+struct pgb_srcv {
+   double s0, s1, s2, s3;
+};
+
+static __device__ __forceinline__ pgb_srcv pgb_load_src(int nsrc, const pgb_dbox &b, long p, double s0)
+{
+   pgb_srcv v;
+   v.s0 = s0;
+   v.s1 = nsrc > 1 ? b.f[PGB_F_SRC1][p] : 0.0;
+   v.s2 = nsrc > 2 ? b.f[PGB_F_SRC1 + 1][p] : 0.0;
+   v.s3 = nsrc > 3 ? b.f[PGB_F_SRC1 + 2][p] : 0.0;
+   return v;
+}
+
+/* runs one program; lapv/j0 are the values of the names lap and j0 */
+static __device__ __noinline__ double pgb_prog_run(const unsigned char *code, const double *cst, double lapv, double j0,
+                                            double u, pgb_srcv s)
+{
+   double st[PGB_PROG_STACK];
+   double top = 0.0;
+   int sp = 0;
+   for (int q = 0; q < PGB_PROG_MAX; q++) {
+      const unsigned c = code[q];
+      const unsigned opc = c & 15u, arg = c >> 4;
+      double v;
+      if (opc == PGB_P_END) break;
+      switch (opc) {
+      case PGB_P_LAP: v = lapv; break;
+      case PGB_P_J0: v = j0; break;
+      case PGB_P_U: v = u; break;
+      case PGB_P_SRC: v = arg == 0 ? s.s0 : arg == 1 ? s.s1 : arg == 2 ? s.s2 : s.s3; break;
+      case PGB_P_CONST: v = cst[arg]; break;
+      case PGB_P_NEG: top = -top; continue;
+      default: {
+         const double a = st[--sp];
+         if (opc == PGB_P_ADD) top = __dadd_rn(a, top);
+         else if (opc == PGB_P_SUB) top = __dsub_rn(a, top);
+         else if (opc == PGB_P_MUL) top = __dmul_rn(a, top);
+         else top = __ddiv_rn(a, top);
+         continue;
+      }
+      }
+      if (q > 0) st[sp++] = top;   /* push the old top (nothing lies below the first value) */
+      top = v;
+   }
+   return top;
+}
+
+/* L[u] and dL/du of a program operator at point p of box b (the box
+ * carries a device pointer to its level operator) */
+static __device__ __forceinline__ double pgb_prog_L(const pgb_dbox &b, double lapv, double u, double s0, long p)
+{
+   const pgb_dop *o = b.op;
+   return pgb_prog_run(o->lcode, o->cst, lapv, b.j0, u, pgb_load_src(o->nsrc, b, p, s0));
+}
+
+static __device__ __forceinline__ double pgb_prog_J(const pgb_dbox &b, double u, double s0, long p)
+{
+   const pgb_dop *o = b.op;
+   return pgb_prog_run(o->jcode, o->cst, 0.0, b.j0, u, pgb_load_src(o->nsrc, b, p, s0));
+}
+
+#endif

@@ -685,12 +685,17 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    h->ngrids = ngrids;
    for (d = 0; d < 3; d++) h->base_shape[d] = d < dim ? base_shape[d] : 1;
    for (d = 0; d < 6; d++) h->base_bbox[d] = d < 2 * dim ? base_bbox[d] : 0;
+   if (prm->min_level < 1) { snprintf(h->err, sizeof(h->err), "min_level must be >= 1"); return 1; }
    for (i = 0; i < ngrids; i++) {
       if (grid_level[i] < 1 || grid_level[i] >= PGB_MAXLEV / 2) {
          snprintf(h->err, sizeof(h->err), "grid %d: level out of range", i);
          return 1;
       }
       h->n_amr = imax(h->n_amr, grid_level[i]);
+   }
+   if (prm->min_level > h->n_amr) {
+      snprintf(h->err, sizeof(h->err), "min_level %d above the finest level %d", prm->min_level, h->n_amr);
+      return 1;
    }
    /* recalc_lev_info src/gh.c:54-81, refinement ratio 2 */
    for (d = 0; d < 3; d++) {
@@ -699,7 +704,8 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    }
    /* AMR levels: build_sgh then compose_cgh, each inserting in bbox order */
    h->grid_box = (int *)malloc(sizeof(int) * (size_t)ngrids);
-   for (l = 1; l <= h->n_amr; l++) {
+   for (i = 0; i < ngrids; i++) h->grid_box[i] = -1;   /* grids below min_level stay outside */
+   for (l = prm->min_level; l <= h->n_amr; l++) {
       int *first = (int *)malloc(sizeof(int) * (size_t)ngrids), nf = 0;
       amr_list[l] = (int *)malloc(sizeof(int) * (size_t)ngrids);
       amr_n[l] = 0;
@@ -723,21 +729,24 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    }
    /* MG hierarchy: build_mgh src/gh.c:1222-1365 */
    cl = PGB_MAXLEV + 1;
-   for (l = h->n_amr; l >= 1; l--) {
+   for (l = h->n_amr; l >= prm->min_level; l--) {
+      const int lmin = prm->min_level;
       cl--;
       tmp_n[cl] = amr_n[l];
       tmp_list[cl] = (int *)malloc(sizeof(int) * (size_t)amr_n[l]);
       memcpy(tmp_list[cl], amr_list[l], sizeof(int) * (size_t)amr_n[l]);
       tmp_amr[cl] = 1;
       for (d = 0; d < 3; d++) tmp_dx[cl][d] = amr_dx[l][d];
-      if (l > 1) continue;
+      if (l > lmin) continue;
       {
+         /* below the coarsest AMR level of the MG hierarchy (build_mgh's
+          * min_lev, src/gh.c:1285-1340): coarsen that level's sgh boxes */
          int cf = 1, more = 1, nsgh = 0;
          double *sgh = (double *)malloc(sizeof(double) * 2 * dim * (size_t)ngrids);
          double *island = (double *)malloc(sizeof(double) * (size_t)ngrids);
          /* save_sgh_bboxes src/gh.c:273-301: input order */
          for (i = 0; i < ngrids; i++)
-            if (grid_level[i] == 1) {
+            if (grid_level[i] == lmin) {
                for (d = 0; d < 2 * dim; d++) sgh[2 * dim * nsgh + d] = grid_bbox[6 * i + d];
                nsgh++;
             }
@@ -745,9 +754,9 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
             int num = 0, *first, nf = 0;
             double ldx[3];
             cf *= 2;
-            calc_island_no(h, sgh, nsgh, island, amr_dx[1], cf);
+            calc_island_no(h, sgh, nsgh, island, amr_dx[lmin], cf);
             first = (int *)malloc(sizeof(int) * (size_t)nsgh);
-            for (d = 0; d < 3; d++) ldx[d] = amr_dx[1][d] * cf;
+            for (d = 0; d < 3; d++) ldx[d] = amr_dx[lmin][d] * cf;
             for (i = 0; i < nsgh; i++)
                if (island[i] != 0) {
                   double gb[6] = {0, 0, 0, 0, 0, 0};
@@ -788,7 +797,7 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
          if (i == 1) h->boxes[lv->box[b]].coarsest = 1;
       }
    }
-   for (l = 1; l <= h->n_amr; l++) free(amr_list[l]);
+   for (l = prm->min_level; l <= h->n_amr; l++) free(amr_list[l]);
    /* AMR-level boxes keep coarsest = 0 except on MG level 1 (gh.c:1137, 1357) */
    for (i = 0; i < h->nbox; i++) {
       pgb_hbox *b = &h->boxes[i];
@@ -813,11 +822,14 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
    memset(ops_inj_mg, 0, sizeof(ops_inj_mg));
    memset(ops_sync, 0, sizeof(ops_sync));
    memset(ops_int, 0, sizeof(ops_int));
-   ops_init[PGB_F_SRC] = prm->restr_src;    /* in both hierarchies, mg_inject set */
+   for (i = 0; i < (prm->nsrc > 1 ? prm->nsrc : 1); i++) {
+      const int op = i ? prm->restr_srck[i] : prm->restr_src;
+      ops_init[PGB_SRC_FIELD(i)] = op;      /* in both hierarchies, mg_inject set */
+      ops_inj_mg[PGB_SRC_FIELD(i)] = op;    /* sources have mg_noinj_to_amr = 1 */
+   }
    ops_init[PGB_F_U] = prm->restr_u;
-   ops_inj[PGB_F_U] = prm->restr_u;         /* the source has mg_noinj_to_amr = 1 */
+   ops_inj[PGB_F_U] = prm->restr_u;
    ops_inj[PGB_F_RES] = prm->restr_res;
-   ops_inj_mg[PGB_F_SRC] = prm->restr_src;
    ops_inj_mg[PGB_F_U] = prm->restr_u;
    ops_inj_mg[PGB_F_RES] = prm->restr_res;
    ops_sync[PGB_F_U] = 1;
@@ -843,7 +855,7 @@ static int amr_level_to_mg(const pgb_hier *h, int L)
 {
    int l, k = 0;
    for (l = 1; l <= h->nlev; l++)
-      if (h->lev[l].in_amrh && ++k == L) return l;
+      if (h->lev[l].in_amrh && ++k == L - h->prm.min_level + 1) return l;
    return 0;
 }
 

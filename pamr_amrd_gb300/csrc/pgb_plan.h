@@ -45,6 +45,9 @@ typedef struct {
    int restr_u, restr_res, restr_src;
    int interp_order, interp_buffer;
    int precision;
+   int nsrc;                          /* source fields (>= 1 allocated) */
+   int restr_srck[PGB_NSRC_MAX];      /* MG restriction of each source (restr_srck[0] = restr_src) */
+   int min_level;                     /* coarsest AMR level of the MG hierarchy (PAMR_build_mgh's min_lev) */
 } pgb_hparams;
 
 typedef struct pgb_hier {

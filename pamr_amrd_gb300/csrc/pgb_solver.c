@@ -22,6 +22,9 @@ enum { N_RELAX_DN = 0, N_RELAX_UP = 1, N_RESID = 2, N_COARSE = 3, N_SLOTS = 4 };
 
 struct pgb_solver {
    pgb_hier h;
+   pgb_dop dop;             /* the level operator (kind also in h.pde) */
+   pgb_dop *d_dop;          /* its device copy, which every box points to */
+   int nsrc;                /* source fields allocated per box (>= 1) */
    int host_only;
    cudaStream_t stream;
    char *arena;
@@ -309,6 +312,7 @@ static int setup_device(pgb_solver *s)
       size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       for (f = 0; f < PGB_NF; f++) {
          fo[i * (PGB_NF + 2) + f] = off;
+         if (f >= PGB_F_SRC1 && f - PGB_F_SRC1 + 1 >= s->nsrc) continue;   /* source the operator does not read */
          off = align256(off + 8 * n);
       }
       fo[i * (PGB_NF + 2) + PGB_NF] = off;
@@ -328,6 +332,8 @@ static int setup_device(pgb_solver *s)
       }
    }
    s->arena_bytes = off;
+   CU(cudaMalloc((void **)&s->d_dop, sizeof(pgb_dop)));
+   CU(cudaMemcpy(s->d_dop, &s->dop, sizeof(pgb_dop), cudaMemcpyHostToDevice));
    CU(cudaMalloc((void **)&s->arena, off));
    CU(cudaMemset(s->arena, 0, off));
    s->hbox = (pgb_dbox *)calloc((size_t)h->nbox, sizeof(pgb_dbox));
@@ -336,7 +342,11 @@ static int setup_device(pgb_solver *s)
       pgb_dbox *db = &s->hbox[i];
       size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       double dx2[3] = {1, 1, 1};
-      for (f = 0; f < PGB_NF; f++) db->f[f] = (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
+      for (f = 0; f < PGB_NF; f++)
+         db->f[f] = (f >= PGB_F_SRC1 && f - PGB_F_SRC1 + 1 >= s->nsrc)
+                       ? 0
+                       : (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
+      db->op = s->d_dop;
       if (w32o)
          for (f = 0; f < PGB_NW32; f++) db->w32[f] = (float *)(s->arena + w32o[i * PGB_NW32 + f]);
       db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
@@ -431,21 +441,40 @@ static int setup_device(pgb_solver *s)
    return 0;
 }
 
-int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox, int ngrids,
-               const int *grid_level, const double *grid_bbox, const pgb_mg_params *params,
-               int flags, pgb_solver **out)
+const pgb_dop *pgb_operator_device_form(const pgb_operator *op);
+
+void pgb_default_create_args(pgb_create_args *a)
+{
+   int k;
+   memset(a, 0, sizeof(*a));
+   pgb_default_params(&a->params);
+   a->min_level = 1;
+   for (k = 0; k < PGB_NSRC_MAX; k++) a->restr_src[k] = PGB_HW_RESTR;
+}
+
+int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
 {
    pgb_solver *s;
    pgb_hparams hp;
-   int rc;
+   const pgb_mg_params *params = &a->params;
+   int rc, k, nsrc;
    *out = 0;
-   if (pde < 0 || pde > 2) return fail(1, "unknown pde kind %d", pde);
+   if (!a->op) return fail(1, "no level operator (pgb_operator_create / pgb_operator_builtin)");
+   nsrc = pgb_operator_device_form(a->op)->nsrc;
    if (params->interp_order != 2 && params->interp_order != 4)
       return fail(1, "interp_order must be 2 or 4");
    if (params->restr_u < 0 || params->restr_u > 3 || params->restr_res < 0 ||
        params->restr_res > 3 || params->restr_src < 0 || params->restr_src > 3)
       return fail(1, "restriction operators must be 0..3");
+   for (k = 1; k < nsrc; k++)
+      if (a->restr_src[k] < 0 || a->restr_src[k] > 3) return fail(1, "restriction operators must be 0..3");
+   if (params->precision != PGB_FP64 && params->precision != PGB_MIXED)
+      return fail(1, "precision must be PGB_FP64 or PGB_MIXED");
    s = (pgb_solver *)calloc(1, sizeof(*s));
+   if (!s) return fail(10, "out of host memory");
+   s->dop = *pgb_operator_device_form(a->op);
+   s->nsrc = nsrc > 1 ? nsrc : 1;
+   memset(&hp, 0, sizeof(hp));
    hp.pre_swp = params->pre_swp;
    hp.pst_swp = params->pst_swp;
    hp.max_iter = params->max_iter;
@@ -462,22 +491,50 @@ int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox,
    hp.interp_order = params->interp_order;
    hp.interp_buffer = params->interp_buffer;
    hp.precision = params->precision;
-   if (hp.precision != PGB_FP64 && hp.precision != PGB_MIXED)
-      return fail(1, "precision must be PGB_FP64 or PGB_MIXED");
-   rc = pgb_hier_build(&s->h, dim, pde, base_shape, base_bbox, ngrids, grid_level, grid_bbox, &hp);
+   hp.nsrc = s->nsrc;
+   hp.restr_srck[0] = params->restr_src;
+   for (k = 1; k < PGB_NSRC_MAX; k++) hp.restr_srck[k] = a->restr_src[k];
+   hp.min_level = a->min_level > 0 ? a->min_level : 1;
+   rc = pgb_hier_build(&s->h, a->dim, s->dop.kind, a->base_shape, a->base_bbox, a->ngrids, a->grid_level,
+                       a->grid_bbox, &hp);
    if (rc) {
       fail(2, "hierarchy: %s", s->h.err);
       pgb_hier_free(&s->h);
       free(s);
       return 2;
    }
-   s->host_only = (flags & PGB_HOST_ONLY) != 0;
+   s->host_only = (a->flags & PGB_HOST_ONLY) != 0;
    if (!s->host_only && (rc = setup_device(s))) {
       pgb_destroy(s);
       return rc;
    }
    *out = s;
    return 0;
+}
+
+int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox, int ngrids,
+               const int *grid_level, const double *grid_bbox, const pgb_mg_params *params,
+               int flags, pgb_solver **out)
+{
+   pgb_create_args a;
+   pgb_operator *op = 0;
+   int rc, d;
+   *out = 0;
+   if (pde < 0 || pde > 2) return fail(1, "unknown pde kind %d", pde);
+   if (pgb_operator_builtin(pde, &op)) return fail(1, "%s", g_err);
+   pgb_default_create_args(&a);
+   a.dim = dim;
+   a.op = op;
+   for (d = 0; d < 3; d++) a.base_shape[d] = d < dim ? base_shape[d] : 1;
+   for (d = 0; d < 6; d++) a.base_bbox[d] = d < 2 * dim ? base_bbox[d] : 0;
+   a.ngrids = ngrids;
+   a.grid_level = grid_level;
+   a.grid_bbox = grid_bbox;
+   a.params = *params;
+   a.flags = flags;
+   rc = pgb_create_ex(&a, out);
+   pgb_operator_destroy(op);
+   return rc;
 }
 
 int pgb_destroy(pgb_solver *s)
@@ -496,6 +553,7 @@ int pgb_destroy(pgb_solver *s)
          if (s->d_snap_off[L]) cudaFree(s->d_snap_off[L]);
       }
       if (s->arena) cudaFree(s->arena);
+      if (s->d_dop) cudaFree(s->d_dop);
       if (s->dbox) cudaFree(s->dbox);
       if (s->sc.partial) cudaFree(s->sc.partial);
       if (s->sc.counter) cudaFree(s->sc.counter);
@@ -533,6 +591,8 @@ void *pgb_stream(pgb_solver *s) { return (void *)s->stream; }
 static int grid_box(const pgb_solver *s, int grid, const pgb_hbox **b)
 {
    if (grid < 0 || grid >= s->h.ngrids) return fail(3, "grid %d out of range", grid);
+   if (s->h.grid_box[grid] < 0)
+      return fail(3, "grid %d lies below the hierarchy's coarsest AMR level %d", grid, s->h.prm.min_level);
    *b = &s->h.boxes[s->h.grid_box[grid]];
    return 0;
 }
@@ -562,6 +622,34 @@ static int copy_grid(pgb_solver *s, int grid, const double *u, const double *src
       CU(cudaStreamSynchronize(s->stream));
    }
    return 0;
+}
+
+static int copy_source(pgb_solver *s, int grid, int k, const double *src, enum cudaMemcpyKind kin)
+{
+   const pgb_hbox *b = 0;
+   const pgb_dbox *db;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (grid_box(s, grid, &b)) return 3;
+   if (k < 0 || k >= s->nsrc) return fail(3, "source %d: the operator reads %d source(s)", k, s->dop.nsrc);
+   db = &s->hbox[s->h.grid_box[grid]];
+   CU(cudaMemcpyAsync(db->f[PGB_SRC_FIELD(k)], src, sizeof(double) * (size_t)b->shape[0] * b->shape[1] * b->shape[2],
+                      kin, s->stream));
+   return 0;
+}
+
+int pgb_set_source(pgb_solver *s, int grid, int k, const double *src)
+{
+   int rc;
+   s->prepared = 0;
+   rc = copy_source(s, grid, k, src, cudaMemcpyHostToDevice);
+   if (!rc) CU(cudaStreamSynchronize(s->stream));
+   return rc;
+}
+
+int pgb_set_source_device(pgb_solver *s, int grid, int k, const double *src)
+{
+   s->prepared = 0;
+   return copy_source(s, grid, k, src, cudaMemcpyDeviceToDevice);
 }
 
 int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src)
@@ -697,7 +785,7 @@ int pgb_prepare(pgb_solver *s)
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    for (L = 1; L <= s->h.nlev; L++) {
       int mask = (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS);
-      if (!s->h.lev[L].in_amrh) mask |= (1 << PGB_F_U) | (1 << PGB_F_SRC);
+      if (!s->h.lev[L].in_amrh) mask |= (1 << PGB_F_U) | PGB_SRC_MASK(s->nsrc);
       KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
    }
    for (L = s->h.nlev - 1; L >= 1; L--)
@@ -825,7 +913,7 @@ static int vcycle_fp64(pgb_solver *s)
           * out: it reads and writes the same values every cycle, and
           * pgb_prepare's build-time injection (same ops, same operator) has
           * already put them in place */
-         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), 0, s->stream));
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), 0, s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
@@ -920,7 +1008,7 @@ static int vcycle_mixed(pgb_solver *s)
          if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
          if (!s->res32[L]) KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
          if (h->inject[L].nops)
-            KC(pgb_k_restrict(s->dbox, &h->inject[L], ~(1 << PGB_F_SRC), s->res32[L + 1], s->stream));
+            KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), s->res32[L + 1], s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
@@ -1205,20 +1293,34 @@ int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order)
 
 /* ------------------------------------------------------------ checkpoint -- */
 /* File layout (little-endian as written by the host): "PGBCKPT1", int32
- * version, dim, pde, ngrids; per input grid int32 level, shape[3], double
- * bbox[6], then u and the source (float64, x fastest). */
+ * version, dim, operator kind, ngrids, source count, 0, then a 64-bit hash
+ * of the operator's program; per input grid int32 level, shape[3], double
+ * bbox[6], then u and each source (float64, x fastest). Grids below the
+ * hierarchy's coarsest AMR level are not part of it and are skipped. */
 #define CKPT_MAGIC "PGBCKPT1"
-#define CKPT_VERSION 1
+#define CKPT_VERSION 2
+
+static unsigned long long dop_hash(const pgb_dop *d)
+{
+   const unsigned char *p = (const unsigned char *)d;
+   unsigned long long h = 1469598103934665603ull;
+   size_t i;
+   for (i = 0; i < sizeof(*d); i++) h = (h ^ p[i]) * 1099511628211ull;
+   return h;
+}
 
 int pgb_checkpoint_save(pgb_solver *s, const char *path)
 {
    FILE *f;
    int g, rc = 0;
-   const int hdr[4] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids};
+   const int hdr[6] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids, s->nsrc, 0};
+   const unsigned long long oh = dop_hash(&s->dop);
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (!(f = fopen(path, "wb"))) return fail(5, "checkpoint: cannot open %s for writing", path);
-   if (fwrite(CKPT_MAGIC, 1, 8, f) != 8 || fwrite(hdr, sizeof(int), 4, f) != 4) rc = fail(5, "checkpoint: write failed");
+   if (fwrite(CKPT_MAGIC, 1, 8, f) != 8 || fwrite(hdr, sizeof(int), 6, f) != 6 || fwrite(&oh, 8, 1, f) != 1)
+      rc = fail(5, "checkpoint: write failed");
    for (g = 0; g < s->h.ngrids && !rc; g++) {
+      if (s->h.grid_box[g] < 0) continue;
       const pgb_hbox *b = &s->h.boxes[s->h.grid_box[g]];
       const pgb_dbox *db = &s->hbox[s->h.grid_box[g]];
       const size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
@@ -1231,9 +1333,9 @@ int pgb_checkpoint_save(pgb_solver *s, const char *path)
       }
       if (fwrite(meta, sizeof(int), 4, f) != 4 || fwrite(b->bbox, sizeof(double), 6, f) != 6)
          rc = fail(5, "checkpoint: write failed");
-      for (k = 0; k < 2 && !rc; k++) {
-         if (cudaMemcpyAsync(buf, db->f[k ? PGB_F_SRC : PGB_F_U], sizeof(double) * n, cudaMemcpyDeviceToHost,
-                             s->stream) != cudaSuccess ||
+      for (k = 0; k <= s->nsrc && !rc; k++) {   /* u, then the sources */
+         if (cudaMemcpyAsync(buf, db->f[k ? PGB_SRC_FIELD(k - 1) : PGB_F_U], sizeof(double) * n,
+                             cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
              cudaStreamSynchronize(s->stream) != cudaSuccess)
             rc = fail(11, "checkpoint: device read failed");
          else if (fwrite(buf, sizeof(double), n, f) != n)
@@ -1245,25 +1347,35 @@ int pgb_checkpoint_save(pgb_solver *s, const char *path)
    return rc;
 }
 
+/* Reads and checks the whole file before anything is copied to the device;
+ * a copy that then fails (a CUDA error) can leave earlier grids restored. */
 int pgb_checkpoint_load(pgb_solver *s, const char *path)
 {
    FILE *f;
    char magic[8];
-   int hdr[4], g, rc = 0, ng = s->h.ngrids;
+   int hdr[6], g, k, rc = 0, ng = s->h.ngrids;
+   const int nf = s->nsrc + 1;
+   unsigned long long oh = 0;
    double **buf;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (!(f = fopen(path, "rb"))) return fail(5, "checkpoint: cannot open %s", path);
-   if (fread(magic, 1, 8, f) != 8 || memcmp(magic, CKPT_MAGIC, 8) || fread(hdr, sizeof(int), 4, f) != 4) {
+   if (fread(magic, 1, 8, f) != 8 || memcmp(magic, CKPT_MAGIC, 8) || fread(hdr, sizeof(int), 6, f) != 6 ||
+       fread(&oh, 8, 1, f) != 1) {
       fclose(f);
       return fail(6, "checkpoint: %s is not a checkpoint", path);
    }
-   if (hdr[0] != CKPT_VERSION || hdr[1] != s->h.dim || hdr[2] != s->h.pde || hdr[3] != ng) {
+   if (hdr[0] != CKPT_VERSION || hdr[1] != s->h.dim || hdr[2] != s->h.pde || hdr[3] != ng ||
+       hdr[4] != s->nsrc || oh != dop_hash(&s->dop)) {
       fclose(f);
-      return fail(6, "checkpoint: version, dimension, equation or grid count differ from the solver's");
+      return fail(6, "checkpoint: version, dimension, operator or grid count differ from the solver's");
    }
-   /* the whole file is read and checked before the solver's data changes */
-   buf = (double **)calloc(2 * (size_t)ng, sizeof(double *));
+   buf = (double **)calloc((size_t)nf * (size_t)(ng ? ng : 1), sizeof(double *));
+   if (!buf) {
+      fclose(f);
+      return fail(10, "checkpoint: host buffer");
+   }
    for (g = 0; g < ng && !rc; g++) {
+      if (s->h.grid_box[g] < 0) continue;
       const pgb_hbox *b = &s->h.boxes[s->h.grid_box[g]];
       const size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       int meta[4];
@@ -1277,16 +1389,20 @@ int pgb_checkpoint_load(pgb_solver *s, const char *path)
          rc = fail(6, "checkpoint: grid %d differs from the solver's hierarchy", g);
          break;
       }
-      buf[2 * g] = (double *)malloc(sizeof(double) * n);
-      buf[2 * g + 1] = (double *)malloc(sizeof(double) * n);
-      if (!buf[2 * g] || !buf[2 * g + 1])
-         rc = fail(10, "checkpoint: host buffer");
-      else if (fread(buf[2 * g], sizeof(double), n, f) != n || fread(buf[2 * g + 1], sizeof(double), n, f) != n)
-         rc = fail(6, "checkpoint: truncated");
+      for (k = 0; k < nf && !rc; k++) {
+         double *v = (double *)malloc(sizeof(double) * n);
+         buf[(size_t)nf * g + k] = v;
+         if (!v) rc = fail(10, "checkpoint: host buffer");
+         else if (fread(v, sizeof(double), n, f) != n) rc = fail(6, "checkpoint: truncated");
+      }
    }
    fclose(f);
-   for (g = 0; g < ng && !rc; g++) rc = pgb_set_grid(s, g, buf[2 * g], buf[2 * g + 1]);
-   for (g = 0; g < 2 * ng; g++) free(buf[g]);
+   for (g = 0; g < ng && !rc; g++) {
+      if (s->h.grid_box[g] < 0) continue;
+      rc = pgb_set_grid(s, g, buf[(size_t)nf * g], buf[(size_t)nf * g + 1]);
+      for (k = 1; k < s->nsrc && !rc; k++) rc = pgb_set_source(s, g, k, buf[(size_t)nf * g + 1 + k]);
+   }
+   for (g = 0; g < nf * ng; g++) free(buf[g]);
    free(buf);
    return rc;
 }

@@ -33,6 +33,14 @@ class MGParams(C.Structure):
                 ("precision", C.c_int)]
 
 
+class CreateArgs(C.Structure):
+    _fields_ = [("dim", C.c_int), ("op", C.c_void_p), ("base_shape", C.c_int * 3),
+                ("base_bbox", C.c_double * 6), ("ngrids", C.c_int),
+                ("grid_level", C.POINTER(C.c_int)), ("grid_bbox", C.POINTER(C.c_double)),
+                ("params", MGParams), ("min_level", C.c_int), ("restr_src", C.c_int * 4),
+                ("flags", C.c_int)]
+
+
 def lib(build: bool = True):
     """Loads libpamr_gb300.so (building it first if needed)."""
     global _lib
@@ -47,6 +55,16 @@ def lib(build: bool = True):
         L.pgb_last_error.restype = C.c_char_p
         L.pgb_create.argtypes = [C.c_int, C.c_int, ip, dp, C.c_int, ip, dp, C.POINTER(MGParams),
                                  C.c_int, C.POINTER(vp)]
+        L.pgb_create_ex.argtypes = [C.POINTER(CreateArgs), C.POINTER(vp)]
+        L.pgb_default_create_args.argtypes = [C.POINTER(CreateArgs)]
+        L.pgb_operator_create.argtypes = [C.c_int, C.c_char_p, C.c_char_p, C.POINTER(vp)]
+        L.pgb_operator_builtin.argtypes = [C.c_int, C.POINTER(vp)]
+        L.pgb_operator_destroy.argtypes = [vp]
+        L.pgb_operator_kind.argtypes = [vp]
+        L.pgb_operator_nsrc.argtypes = [vp]
+        L.pgb_operator_eval.argtypes = [vp, C.c_double, C.c_double, C.c_double, dp, dp, dp]
+        L.pgb_set_source.argtypes = [vp, C.c_int, C.c_int, dp]
+        L.pgb_set_source_device.argtypes = [vp, C.c_int, C.c_int, vp]
         L.pgb_destroy.argtypes = [vp]
         L.pgb_grid_shape.argtypes = [vp, C.c_int, ip]
         L.pgb_set_grid.argtypes = [vp, C.c_int, dp, dp]
@@ -106,26 +124,76 @@ def params_from(case: Case) -> MGParams:
     return m
 
 
+class Operator:
+    """A level operator: a built-in PDE kind, or the expressions an
+    application registers (pgb_operator_create)."""
+
+    def __init__(self, pde: int = None, nsrc: int = 1, lop: str = None, jac: str = None):
+        L = lib()
+        h = C.c_void_p()
+        if lop is None:
+            _check(L.pgb_operator_builtin(pde, C.byref(h)))
+        else:
+            _check(L.pgb_operator_create(nsrc, lop.encode(), jac.encode(), C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def for_case(cls, case: Case) -> "Operator":
+        from .workloads import OPERATORS
+        if case.pde in OPERATORS:
+            n, lop, jac = OPERATORS[case.pde]
+            return cls(nsrc=n, lop=lop, jac=jac)
+        return cls(pde=case.pde)
+
+    def kind(self) -> int:
+        return lib().pgb_operator_kind(self.h)
+
+    def close(self):
+        if self.h:
+            lib().pgb_operator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Solver:
     """One AMR hierarchy on the GPU (or, with host_only, just its plans)."""
 
-    def __init__(self, case: Case, host_only: bool = False):
+    def __init__(self, case: Case, host_only: bool = False, op: Operator = None):
         L = lib()
         self.case = case
         n = len(case.grids)
-        lev = (C.c_int * n)(*[g.level for g in case.grids])
+        self._lev = (C.c_int * n)(*[g.level for g in case.grids])
         bb = np.zeros((n, 6))
         for i, g in enumerate(case.grids):
             bb[i, :len(g.bbox)] = g.bbox
         self._bb = np.ascontiguousarray(bb)
-        shape = (C.c_int * 3)(*case.base_shape)
-        bbox = (C.c_double * 6)(*(list(case.base_bbox) + [0.0] * (6 - len(case.base_bbox))))
-        self._params = params_from(case)
+        op = op or Operator.for_case(case)
+        a = CreateArgs()
+        L.pgb_default_create_args(C.byref(a))
+        a.dim = case.dim
+        a.op = op.h
+        for d in range(3):
+            a.base_shape[d] = case.base_shape[d]
+        for d, v in enumerate(list(case.base_bbox) + [0.0] * (6 - len(case.base_bbox))):
+            a.base_bbox[d] = v
+        a.ngrids = n
+        a.grid_level = self._lev
+        a.grid_bbox = _dp(self._bb)
+        a.params = params_from(case)
+        a.min_level = case.min_level
+        for k in range(1, case.nsrc):
+            a.restr_src[k] = case.restr_src_k(k)
+        a.flags = 1 if host_only else 0
         h = C.c_void_p()
-        _check(L.pgb_create(case.dim, case.pde, shape, bbox, n, lev, _dp(self._bb),
-                            C.byref(self._params), 1 if host_only else 0, C.byref(h)))
+        _check(L.pgb_create_ex(C.byref(a), C.byref(h)))
         self.h = h
         self.host_only = host_only
+        self.op_kind = op.kind()
 
     def close(self):
         if self.h:
@@ -139,13 +207,21 @@ class Solver:
             pass
 
     # ------------------------------------------------------------- data --
+    def _in_hierarchy(self, i: int) -> bool:
+        return self.case.grids[i].level >= self.case.min_level
+
     def set_inputs(self, u=None, src=None):
         u = u if u is not None else self.case.u0
         src = src if src is not None else self.case.src
         for i, (a, s) in enumerate(zip(u, src)):
+            if not self._in_hierarchy(i):
+                continue
             a = np.ascontiguousarray(a, dtype=np.float64)
             s = np.ascontiguousarray(s, dtype=np.float64)
             _check(lib().pgb_set_grid(self.h, i, _dp(a), _dp(s)))
+            for k in range(1, self.case.nsrc):
+                sk = np.ascontiguousarray(self.case.source(k)[i], dtype=np.float64)
+                _check(lib().pgb_set_source(self.h, i, k, _dp(sk)))
 
     def get_u(self):
         out = []
@@ -153,7 +229,10 @@ class Solver:
             a = np.empty(g.size)
             out.append(a)
         for i, a in enumerate(out):
-            _check(lib().pgb_get_grid(self.h, i, _dp(a)))
+            if self._in_hierarchy(i):
+                _check(lib().pgb_get_grid(self.h, i, _dp(a)))
+            else:   # outside the MG hierarchy: unchanged by a solve
+                a[:] = self.case.u0[i]
         return out
 
     # ------------------------------------------------------------ solve --
@@ -203,9 +282,15 @@ class Solver:
         L.pgb_checkpoint_load.argtypes = [C.c_void_p, C.c_char_p]
         _check(L.pgb_checkpoint_load(self.h, path.encode()))
 
-    def set_inputs_device(self, u_ptrs, src_ptrs):
+    def set_inputs_device(self, u_ptrs, src_ptrs, extra_src_ptrs=()):
+        """device pointers per grid: u, source 0, and (extra_src_ptrs[k-1][i])
+        source k"""
         for i, (a, b) in enumerate(zip(u_ptrs, src_ptrs)):
+            if not self._in_hierarchy(i):
+                continue
             _check(lib().pgb_set_grid_device(self.h, i, a, b))
+            for k, ptrs in enumerate(extra_src_ptrs, start=1):
+                _check(lib().pgb_set_source_device(self.h, i, k, ptrs[i]))
 
     def stream(self) -> int:
         return lib().pgb_stream(self.h)

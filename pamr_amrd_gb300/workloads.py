@@ -35,8 +35,15 @@ from typing import List, Sequence, Tuple
 
 import numpy as np
 
-POISSON, CONFORMAL, LAPSE = 0, 1, 2
-PDE_NAMES = {POISSON: "poisson", CONFORMAL: "conformal", LAPSE: "lapse"}
+POISSON, CONFORMAL, LAPSE, NBS = 0, 1, 2, 3
+PDE_NAMES = {POISSON: "poisson", CONFORMAL: "conformal", LAPSE: "lapse", NBS: "nbs"}
+
+# Operators that are not built into the library, as the level-operator
+# expressions an application registers (pgb_operator_create): source count,
+# L[u], dL/du. NBS is the Newtonian boson star's potential equation
+# V_xx + V_yy + V_zz - (phi_r^2 + phi_i^2) = 0 (examples/nbs/num.f:85-246),
+# sources phi_r and phi_i, in the hook's order of operations.
+OPERATORS = {NBS: (2, "lap - (s0*s0 + s1*s1)", "j0")}
 
 # transfer operators (values of PAMR's transfer bits, include/pamr.h:92-105)
 STRAIGHT_INJECT, HW_RESTR, FW_RESTR = 1, 2, 3
@@ -112,10 +119,28 @@ class Case:
     u0: List[np.ndarray]
     src: List[np.ndarray]
     params: MGParams
+    # sources 1.. of operators with several (src_extra[k-1][i] = source k of grid i)
+    src_extra: List[List[np.ndarray]] = dataclasses.field(default_factory=list)
+    restr_src_extra: List[int] = dataclasses.field(default_factory=list)
+    # coarsest AMR level of the MG hierarchy (solve_elliptics(L, ...), amrd/mg.c:20)
+    min_level: int = 1
 
     @property
     def num_levels(self) -> int:
         return max(g.level for g in self.grids)
+
+    @property
+    def nsrc(self) -> int:
+        return OPERATORS[self.pde][0] if self.pde in OPERATORS else 1
+
+    def source(self, k: int) -> List[np.ndarray]:
+        """source k of every grid"""
+        return self.src if k == 0 else self.src_extra[k - 1]
+
+    def restr_src_k(self, k: int) -> int:
+        if k == 0:
+            return self.params.restr_src
+        return self.restr_src_extra[k - 1] if len(self.restr_src_extra) >= k else self.params.restr_src
 
     def level_dx(self, level: int) -> List[float]:
         return [(self.base_bbox[2 * d + 1] - self.base_bbox[2 * d]) / (self.base_shape[d] - 1)
@@ -158,23 +183,28 @@ def initial_residual_norm(case: Case) -> float:
     lf = case.num_levels
     dx = case.level_dx(lf)
     best = 0.0
-    for g, u, s in zip(case.grids, case.u0, case.src):
+    for i, (g, u, s) in enumerate(zip(case.grids, case.u0, case.src)):
         if g.level != lf:
             continue
         v = u.reshape(g.shape[2], g.shape[1], g.shape[0])
         f = s.reshape(v.shape)
+        f1 = case.src_extra[0][i].reshape(v.shape) if case.pde == NBS else None
         c = v[..., 1:-1, 1:-1] if case.dim == 2 else v[1:-1, 1:-1, 1:-1]
         if case.dim == 2:
             t = ((v[:, 1:-1, 2:] - 2 * c + v[:, 1:-1, :-2]) / (dx[0] * dx[0]) +
                  (v[:, 2:, 1:-1] - 2 * c + v[:, :-2, 1:-1]) / (dx[1] * dx[1]))
             fs = f[:, 1:-1, 1:-1]
+            fs1 = f1[:, 1:-1, 1:-1] if f1 is not None else None
         else:
             t = ((v[1:-1, 1:-1, 2:] - 2 * c + v[1:-1, 1:-1, :-2]) / (dx[0] * dx[0]) +
                  (v[1:-1, 2:, 1:-1] - 2 * c + v[1:-1, :-2, 1:-1]) / (dx[1] * dx[1]) +
                  (v[2:, 1:-1, 1:-1] - 2 * c + v[:-2, 1:-1, 1:-1]) / (dx[2] * dx[2]))
             fs = f[1:-1, 1:-1, 1:-1]
+            fs1 = f1[1:-1, 1:-1, 1:-1] if f1 is not None else None
         if case.pde == POISSON:
             r = t - fs
+        elif case.pde == NBS:
+            r = t - (fs * fs + fs1 * fs1)
         elif case.pde == CONFORMAL:
             r = t + 2 * math.pi * fs * c ** 5
         else:
@@ -366,3 +396,84 @@ def poisson2d_uneven(seed: int = 0, n: int = 129, levels: int = 5, min_boxes: in
     case = Case(f"poisson2d_uneven_s{seed}", POISSON, 2, (n, n, 1), bbox, grids, u0, src,
                 params or MGParams())
     return _finish(case, rel_tol)
+
+
+def _nbs_fields(g: Grid, dim: int, stars):
+    """phi_r, phi_i of a few Gaussian boson-star profiles
+    A exp(-r^2/w^2) (cos, sin)(k . x + phase) on grid g"""
+    x, y, z = _mesh(g, dim)
+    pr = np.zeros((g.shape[2], g.shape[1], g.shape[0]))
+    pi_ = np.zeros_like(pr)
+    for (a, w, c, kv, ph) in stars:
+        r2 = (x - c[0]) ** 2 + (y - c[1]) ** 2
+        arg = kv[0] * x + kv[1] * y + ph
+        if dim == 3:
+            r2 = r2 + (z - c[2]) ** 2
+            arg = arg + kv[2] * z
+        env = a * np.exp(-r2 / (w * w))
+        pr = pr + env * np.cos(arg)
+        pi_ = pi_ + env * np.sin(arg)
+    return (np.ascontiguousarray(pr).reshape(-1), np.ascontiguousarray(pi_).reshape(-1))
+
+
+def _nbs_stars(rng: SplitMix64, dim: int, count: int, half: float):
+    stars = []
+    for _ in range(count):
+        a = rng.uniform(0.2, 1.0)
+        w = rng.uniform(0.1, 0.25) * half
+        c = tuple(rng.uniform(-0.4, 0.4) * half for _ in range(dim))
+        kv = tuple(rng.uniform(-2.0, 2.0) / w for _ in range(dim))
+        stars.append((a, w, c, kv, rng.uniform(0, 2 * math.pi)))
+    return stars
+
+
+def nbs3d(n: int = 65, m: int = 33, seed: int = 0, levels: int = 2, rel_tol: float = 1e-10,
+          params: MGParams | None = None) -> Case:
+    """The Newtonian boson star's potential (examples/nbs): V_xx + V_yy + V_zz
+    = phi_r^2 + phi_i^2 on [-1,1]^3, V = 0 on the boundary and as the initial
+    guess; n^3 base grid plus nested 2:1 levels of m^3 boxes centred on the
+    origin; phi = sum of 3 seeded Gaussian wave packets. Two sources, an
+    operator the library does not build in: the application registers it as
+    "lap - (s0*s0 + s1*s1)" (OPERATORS[NBS])."""
+    rng = SplitMix64(0x5EED0006 + seed)
+    stars = _nbs_stars(rng, 3, 3, 1.0)
+    bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    dx1 = 2.0 / (n - 1)
+    grids = [Grid(1, bbox, (n, n, n))]
+    for lev in range(2, levels + 1):
+        dx = dx1 / 2 ** (lev - 1)
+        h = 0.5 * (m - 1) * dx
+        grids.append(_grid_from_bbox(lev, (-h, h, -h, h, -h, h), [dx] * 3, 3))
+    f = [_nbs_fields(g, 3, stars) for g in grids]
+    case = Case(f"nbs3d_{n}_{m}" + ("" if levels == 2 else f"_L{levels}") + f"_s{seed}", NBS, 3,
+                (n, n, n), bbox, grids, [np.zeros(g.size) for g in grids], [a for a, _ in f],
+                params or MGParams(), src_extra=[[b for _, b in f]])
+    return _finish(case, rel_tol)
+
+
+def nbs2d_uneven(seed: int = 0, n: int = 65, levels: int = 3, min_boxes: int = 3,
+                 max_boxes: int = 8, min_side: int = 9, max_side: int = 33,
+                 rel_tol: float = 1e-10, params: MGParams | None = None) -> Case:
+    """the nbs potential on an uneven 2-D hierarchy (poisson2d_uneven's box
+    layout: odd sides aligned to parent lines and clipped to the parent),
+    phi_r and phi_i as in nbs3d"""
+    base = poisson2d_uneven(seed, n=n, levels=levels, min_boxes=min_boxes, max_boxes=max_boxes,
+                            min_side=min_side, max_side=max_side, rel_tol=0, params=params, nblobs=1)
+    rng = SplitMix64(0x5EED0007 + seed)
+    stars = _nbs_stars(rng, 2, 4, 1.0)
+    f = [_nbs_fields(g, 2, stars) for g in base.grids]
+    case = Case(f"nbs2d_uneven_s{seed}", NBS, 2, base.base_shape, base.base_bbox, base.grids,
+                [np.zeros(g.size) for g in base.grids], [a for a, _ in f], base.params,
+                src_extra=[[b for _, b in f]])
+    return _finish(case, rel_tol)
+
+
+def with_min_level(case: Case, level: int) -> Case:
+    """the case solved on the MG hierarchy built from AMR level `level` up
+    (solve_elliptics(level, ...), amrd/mg.c:20; level = the finest is the
+    hierarchy of the V-cycle inside the evolution iteration,
+    amrd/evolve.c:454); grids below it keep their values"""
+    case.min_level = level
+    case.name += f"_min{level}"
+    return case
+

@@ -11,6 +11,7 @@ from pamr_amrd_gb300.solver import (PLAN_INJECT, PLAN_INJECT_INIT, PLAN_INTERP, 
 
 KIND_COPY, KIND_INTERP, KIND_HWR, KIND_FWR = 1, 2, 3, 4
 F_SRC, F_U, F_RES = 0, 1, 2
+F_SRC1 = 5   # sources 1..3 of an operator with several (library field order)
 
 
 def _shape(s: Solver, L: int, idx: int):
@@ -38,10 +39,10 @@ def expand(s: Solver, which: int, L: int, gfn: dict, field: int | None = None):
             out.append(_row(KIND_COPY, (Ls, si, g), (Ld, di, g), iv))
         elif which in (PLAN_INJECT, PLAN_INJECT_INIT):
             irho = r[13]
-            for f in range(5):
+            # local_transfer walks grid functions in PAMR gfn order (src/transfer.c:997)
+            fields = sorted((f for f in range(8) if r[14 + f]), key=lambda f: gfn[f])
+            for f in fields:
                 op = r[14 + f]
-                if not op:
-                    continue
                 g = gfn[f]
                 iv = list(n1) + list(n2) + list(r[4:13]) + [irho] * 3 + [1] * 3
                 if op == 1:
@@ -87,4 +88,8 @@ def expected_calls(s: Solver, gfn: dict, ncycles: int, pre: int, pst: int):
 
 def reference_gfns(ref: dict) -> dict:
     g = ref["gfn"]
-    return {F_SRC: g["src"], F_U: g["u"], F_RES: g["res"]}
+    out = {F_SRC: g["src"], F_U: g["u"], F_RES: g["res"]}
+    for k in (1, 2, 3):
+        if f"src{k}" in g:
+            out[F_SRC1 + k - 1] = g[f"src{k}"]
+    return out

@@ -7,7 +7,9 @@ the transfer (AMR level, boundary width, order) and the points the
 reference's PAMR_interp / PAMR_AMR_bdy_interp changed, with their values. The others store the case (grids,
 parameters, initial u and source) and what the reference's solve produced: V-cycle count, every relax/residual/L_op hook
 call with its norm, the MG hierarchy, the cmask arrays, the final u on every
-grid and the m_util_r8 call log of the whole solve.
+grid and the m_util_r8 call log of the whole solve. Cases with an
+application operator (two sources) or an MG hierarchy built from an AMR
+level above the base also store the second source and that level.
 
 usage: python tests/golden/make_golden.py [--all]   (needs oracle/_ref/ref_mg)
 Writes the fixtures that are missing; --all rewrites every one.
@@ -39,6 +41,15 @@ def cases():
                            max_side=33),
         W.lapse2d_bo(17, seed=0, levels=3),
         W.lapse2d_bo(17, seed=1, levels=3, step=100),
+        # an application operator with two sources (the nbs potential)
+        W.nbs3d(17, 9, seed=0),
+        W.nbs2d_uneven(seed=1, n=33, levels=3, min_boxes=2, max_boxes=4, min_side=5, max_side=17),
+        # MG hierarchies built from an AMR level above the base
+        # (solve_elliptics(L, ...) with L > 1; L = finest as at amrd/evolve.c:454)
+        W.with_min_level(W.lapse2d_bo(33, seed=2, levels=3, step=40), 2),
+        W.with_min_level(W.lapse2d_bo(33, seed=3, levels=3, step=80), 3),
+        W.with_min_level(W.poisson2d_uneven(seed=2, n=65, levels=4, min_boxes=3, max_boxes=8,
+                                            min_side=9, max_side=33), 3),
     ]
 
 
@@ -94,6 +105,8 @@ def save(case, ref, path):
         base_shape=np.array(case.base_shape), base_bbox=np.array(case.base_bbox),
         grids=grids,
         u0=np.concatenate(case.u0), src=np.concatenate(case.src),
+        src1=np.concatenate(case.source(1)) if case.nsrc > 1 else np.zeros(0),
+        min_level=case.min_level,
         params=np.array([p.pre_swp, p.pst_swp, p.max_iter, p.min_iter, p.max_citer,
                          p.min_cwidth, p.restr_u, p.restr_res, p.restr_src, p.interp_order]),
         fparams=np.array([p.tol, p.crtol, p.w0_r, p.w0_i]),
@@ -102,7 +115,7 @@ def save(case, ref, path):
         hook_idx=h["idx"].astype(np.int16), hook_norm=h["norm"],
         mgh=mgh, masks_meta=masks_meta, masks=masks,
         u=np.concatenate(ref["u"]),
-        gfn=np.array([ref["gfn"][k] for k in ("u", "res", "lop", "rhs", "cmask", "src")]),
+        gfn=np.array([ref["gfn"][k] for k in refrun.GFN_KEYS if k in ref["gfn"]]),
         ops=ref["ops"].astype(np.int16) if len(ref["ops"]) else np.zeros((0, 34), np.int16),
     )
 

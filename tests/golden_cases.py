@@ -67,6 +67,10 @@ def load(path: str):
                   tuple(int(v) for v in z["base_shape"]),
                   tuple(float(v) for v in z["base_bbox"]), grids,
                   split(z["u0"]), split(z["src"]), params)
+    if "src1" in z.files and len(z["src1"]):
+        case.src_extra = [split(z["src1"])]
+    if "min_level" in z.files:
+        case.min_level = int(z["min_level"])
     masks = []
     off = 0
     for kind, L, idx in z["masks_meta"]:
@@ -84,7 +88,8 @@ def load(path: str):
                 for r in z["mgh"]],
         "masks": masks,
         "u": split(z["u"]),
-        "gfn": dict(zip(("u", "res", "lop", "rhs", "cmask", "src"), (int(v) for v in z["gfn"]))),
+        "gfn": dict(zip(("u", "res", "lop", "rhs", "cmask", "src", "src1", "src2", "src3"),
+                        (int(v) for v in z["gfn"]))),
         "ops": z["ops"].astype(np.int64),
     }
     return case, ref
