@@ -172,6 +172,27 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
  * since the last pgb_prepare. */
 int pgb_prepare(pgb_solver *s);
 int pgb_vcycle(pgb_solver *s, double *res);
+/* pgb_prepare with flags: PGB_PREPARE_KEEP_MG_DATA leaves u and the sources
+ * of the pure MG levels as stored with pgb_box_set instead of injecting
+ * them from the AMR levels (an MG hierarchy that already exists, as PAMR
+ * keeps it between the vcycle calls of amrd/evolve.c:471-487) */
+#define PGB_PREPARE_KEEP_MG_DATA 1
+int pgb_prepare_ex(pgb_solver *s, int flags);
+
+/* Grid functions of one box of the MG hierarchy (level, index in PAMR
+ * grid-list order, as pgb_box_info), host arrays: PGB_FIELD_U the elliptic
+ * variable f, _RES f_res, _LOP f_lop, _RHS f_rhs, PGB_FIELD_SRC + k
+ * source k -- the MG-hierarchy gfs of PAMR_get_g_attribs with
+ * PAMR_get_gfn(name, PAMR_MGH, 0) (src/pamr.c:1706-1762). Setting a box
+ * makes the next pgb_vcycle start with pgb_prepare (use pgb_prepare_ex
+ * first to keep MG-level data). */
+#define PGB_FIELD_U 0
+#define PGB_FIELD_RES 1
+#define PGB_FIELD_LOP 2
+#define PGB_FIELD_RHS 3
+#define PGB_FIELD_SRC 4
+int pgb_box_set(pgb_solver *s, int level, int idx, int field, const double *in);
+int pgb_box_get(pgb_solver *s, int level, int idx, int field, double *out);
 
 /* The solver's CUDA stream (cudaStream_t) for callers that order their own
  * work around it. */

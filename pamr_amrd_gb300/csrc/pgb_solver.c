@@ -778,17 +778,21 @@ int pgb_level_tuning(pgb_solver *s, int L, int *tile_planes, int *sweeps_per_lau
 
 /* initialisation the reference performs while building the MG hierarchy
  * (build_mgh src/gh.c:1222-1365): MG-only grid functions start at zero and
- * pure MG levels receive u and the source by TF_MGH_INIT injection */
-int pgb_prepare(pgb_solver *s)
+ * pure MG levels receive u and the source by TF_MGH_INIT injection; with
+ * PGB_PREPARE_KEEP_MG_DATA the MG-only levels keep the u and sources the
+ * caller stored (pgb_box_set), as an existing MG hierarchy holds them
+ * between vcycle calls (amrd/evolve.c:471-487) */
+int pgb_prepare_ex(pgb_solver *s, int flags)
 {
    int L;
+   const int keep = (flags & PGB_PREPARE_KEEP_MG_DATA) != 0;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    for (L = 1; L <= s->h.nlev; L++) {
       int mask = (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS);
-      if (!s->h.lev[L].in_amrh) mask |= (1 << PGB_F_U) | PGB_SRC_MASK(s->nsrc);
+      if (!s->h.lev[L].in_amrh && !keep) mask |= (1 << PGB_F_U) | PGB_SRC_MASK(s->nsrc);
       KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
    }
-   for (L = s->h.nlev - 1; L >= 1; L--)
+   for (L = s->h.nlev - 1; L >= 1 && !keep; L--)
       if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, 0, s->stream));
    if (s->h.prm.precision == PGB_MIXED) {
       if (!s->tuned) {
@@ -842,6 +846,50 @@ int pgb_prepare(pgb_solver *s)
    CU(cudaMemsetAsync(s->d_parity, 0, sizeof(int), s->stream));   /* every solve starts on an even cycle */
    s->prepared = 1;
    return 0;
+}
+
+int pgb_prepare(pgb_solver *s) { return pgb_prepare_ex(s, 0); }
+
+/* ------------------------------------------------------ box-level data -- */
+/* field of pgb_box_set / pgb_box_get -> grid function */
+static int box_field(const pgb_solver *s, int field, int *f)
+{
+   if (field == PGB_FIELD_U) *f = PGB_F_U;
+   else if (field == PGB_FIELD_RES) *f = PGB_F_RES;
+   else if (field == PGB_FIELD_LOP) *f = PGB_F_LOP;
+   else if (field == PGB_FIELD_RHS) *f = PGB_F_RHS;
+   else if (field >= PGB_FIELD_SRC && field < PGB_FIELD_SRC + s->nsrc) *f = PGB_SRC_FIELD(field - PGB_FIELD_SRC);
+   else return fail(3, "unknown field %d", field);
+   return 0;
+}
+
+static int box_copy(pgb_solver *s, int L, int idx, int field, const double *in, double *out)
+{
+   const pgb_hbox *b;
+   int f;
+   size_t n;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (L < 1 || L > s->h.nlev || idx < 0 || idx >= s->h.lev[L].nbox) return fail(3, "no box %d on level %d", idx, L);
+   if (box_field(s, field, &f)) return 3;
+   b = &s->h.boxes[s->h.lev[L].box[idx]];
+   n = sizeof(double) * (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+   if (in) {
+      s->prepared = 0;
+      CU(cudaMemcpyAsync(s->hbox[s->h.lev[L].box[idx]].f[f], in, n, cudaMemcpyHostToDevice, s->stream));
+   } else
+      CU(cudaMemcpyAsync(out, s->hbox[s->h.lev[L].box[idx]].f[f], n, cudaMemcpyDeviceToHost, s->stream));
+   CU(cudaStreamSynchronize(s->stream));
+   return 0;
+}
+
+int pgb_box_set(pgb_solver *s, int L, int idx, int field, const double *in)
+{
+   return box_copy(s, L, idx, field, in, 0);
+}
+
+int pgb_box_get(pgb_solver *s, int L, int idx, int field, double *out)
+{
+   return box_copy(s, L, idx, field, 0, out);
 }
 
 

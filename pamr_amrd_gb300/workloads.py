@@ -416,11 +416,11 @@ def _nbs_fields(g: Grid, dim: int, stars):
     return (np.ascontiguousarray(pr).reshape(-1), np.ascontiguousarray(pi_).reshape(-1))
 
 
-def _nbs_stars(rng: SplitMix64, dim: int, count: int, half: float):
+def _nbs_stars(rng: SplitMix64, dim: int, count: int, half: float, wmin: float = 0.1, wmax: float = 0.25):
     stars = []
     for _ in range(count):
         a = rng.uniform(0.2, 1.0)
-        w = rng.uniform(0.1, 0.25) * half
+        w = rng.uniform(wmin, wmax) * half
         c = tuple(rng.uniform(-0.4, 0.4) * half for _ in range(dim))
         kv = tuple(rng.uniform(-2.0, 2.0) / w for _ in range(dim))
         stars.append((a, w, c, kv, rng.uniform(0, 2 * math.pi)))
@@ -460,7 +460,7 @@ def nbs2d_uneven(seed: int = 0, n: int = 65, levels: int = 3, min_boxes: int = 3
     base = poisson2d_uneven(seed, n=n, levels=levels, min_boxes=min_boxes, max_boxes=max_boxes,
                             min_side=min_side, max_side=max_side, rel_tol=0, params=params, nblobs=1)
     rng = SplitMix64(0x5EED0007 + seed)
-    stars = _nbs_stars(rng, 2, 4, 1.0)
+    stars = _nbs_stars(rng, 2, 6, 1.0, 0.25, 0.5)   # wide enough that every refined box sees them
     f = [_nbs_fields(g, 2, stars) for g in base.grids]
     case = Case(f"nbs2d_uneven_s{seed}", NBS, 2, base.base_shape, base.base_bbox, base.grids,
                 [np.zeros(g.size) for g in base.grids], [a for a, _ in f], base.params,
