@@ -987,10 +987,11 @@ static int same_bbox(const double *a, const double *b, int dim)
    return 1;
 }
 
-int port_solve(const port_case *c, port_result *r)
+/* the AMR hierarchy of c with u and the sources filled in (PAMR_compose_hierarchy
+ * plus the application's data); 0 on success */
+static int port_compose(const port_case *c, port_result *r)
 {
-   int i, l, d, it;
-   double res;
+   int i, l, d;
    pgrid *g;
    if (c->dim < 2 || c->dim > 3 || c->ngrids < 1) return 1;
    memset(&P, 0, sizeof(P));
@@ -1046,7 +1047,36 @@ int port_solve(const port_case *c, port_result *r)
       for (d = 1; d < oracle_nsrc(c->pde); d++)
          memcpy(m->gf[G_SRCK(d)], c->srcx[d - 1][i], sizeof(double) * (size_t)gsize(m));
    }
+   return 0;
+}
 
+/* frees the AMR hierarchy */
+static void port_free(void)
+{
+   int l;
+   pgrid *g;
+   for (l = 1; l <= P.n_amr; l++) {
+      g = P.amr[l].grids;
+      while (g) {
+         pgrid *n = g->next;
+         int h;
+         for (h = 0; h < NGF; h++) if (g->own[h]) free(g->gf[h]);
+         for (h = 0; h < P.dim; h++) free(g->x[h]);
+         free(g);
+         g = n;
+      }
+      free(P.sgh_bbox[l]);
+   }
+   free(P.sgh_bbox);
+   free(P.sgh_num);
+}
+
+int port_solve(const port_case *c, port_result *r)
+{
+   int i, it, rc;
+   double res;
+   pgrid *g;
+   if ((rc = port_compose(c, r))) return rc;
    /* solve_elliptics amrd/mg.c:20-79 */
    build_mgh();
    if (r) r->n_levels = P.n_mg;
@@ -1065,19 +1095,6 @@ int port_solve(const port_case *c, port_result *r)
          if (same_bbox(g->bbox, &c->bbox[6 * i], P.dim))
             memcpy(c->u[i], g->gf[G_U], sizeof(double) * (size_t)gsize(g));
    }
-   for (l = 1; l <= P.n_amr; l++) {
-      g = P.amr[l].grids;
-      while (g) {
-         pgrid *n = g->next;
-         int h;
-         for (h = 0; h < NGF; h++) if (g->own[h]) free(g->gf[h]);
-         for (h = 0; h < P.dim; h++) free(g->x[h]);
-         free(g);
-         g = n;
-      }
-      free(P.sgh_bbox[l]);
-   }
-   free(P.sgh_bbox);
-   free(P.sgh_num);
+   port_free();
    return 0;
 }

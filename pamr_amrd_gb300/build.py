@@ -17,6 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpamr_gb300.so")
 LIB_F77 = os.path.join(os.path.dirname(LIB), "libpamr_gb300_f77.so")
+# the drop-in multigrid module (amrd/mg.c's entry points over libpamr_gb300):
+# a shared library and a static archive (AMRD applications link static libs)
+LIB_AMRD_MG = os.path.join(HERE, "libamrd_mg_gb300.so")
+LIB_AMRD_MG_A = os.path.join(HERE, "libamrd_mg_gb300.a")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = {"pgb_kernels64.cu": ["-fmad=false"], "pgb_noalloc.cu": ["-fmad=false"],
@@ -93,6 +97,30 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: " + r.stdout + r.stderr)
+    # the drop-in multigrid module: PAMR_* / AMRD_* stay undefined here and
+    # resolve against the application's libpamr / libamrd when it links
+    msrc = os.path.join(CSRC, "amrd_mg_gb300.c")
+    mobj = os.path.join(OBJ, "amrd_mg_gb300.c.o")
+    mdeps = [msrc, os.path.join(CSRC, "amrd_abi.h"), os.path.join(ROOT, "include", "amrd_mg_gb300.h")] + headers
+    if force or _stale(mobj, mdeps):
+        cmd = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-Wall", "-I" + CSRC, "-I" + os.path.join(ROOT, "include"),
+               "-c", msrc, "-o", mobj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build failed: " + r.stdout + r.stderr)
+    if force or _stale(LIB_AMRD_MG, [mobj, LIB]):
+        libdir = os.path.join(cuda, "lib64")
+        cmd = ["gcc", "-shared", "-o", LIB_AMRD_MG, mobj, "-L" + HERE, "-lpamr_gb300", "-L" + libdir, "-lcudart",
+               "-lm", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + libdir]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: " + r.stdout + r.stderr)
+    if force or _stale(LIB_AMRD_MG_A, [mobj]):
+        if os.path.exists(LIB_AMRD_MG_A):
+            os.remove(LIB_AMRD_MG_A)
+        r = subprocess.run(["ar", "rcs", LIB_AMRD_MG_A, mobj], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("ar failed: " + r.stdout + r.stderr)
     return LIB
 
 

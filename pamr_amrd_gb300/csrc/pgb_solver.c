@@ -835,8 +835,10 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
        * first one is computed here. */
       for (L = 2; L < s->h.nlev; L++) {
          const pgb_hier *h = &s->h;
+         /* not on levels with coarsest boxes: their coarsest-grid loop
+          * changes u after the post-smoothing, so D cannot be carried */
          s->dnext[L] = h->prm.pre_swp > 0 && !h->sync[L][0].nops && !h->sync[L][1].nops &&
-                       2 * s->lv[L].nctiles < s->lv[L].ntiles;
+                       2 * s->lv[L].nctiles < s->lv[L].ntiles && !lvl_coarsest(s, L);
          if (s->dnext[L] &&
              pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, h->prm.w0_r, 0, s->stream))
             return fail(11, "%s", pgb_dev_error32());
@@ -1087,7 +1089,12 @@ static int vcycle_mixed(pgb_solver *s)
          if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
          KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
-      } else if (lvl_coarsest(s, L)) {
+      }
+      /* the coarsest-grid loop (amrd/mg.c:172-190) wherever coarsest boxes
+       * are: on MG level 1, and above it in hierarchies whose base has
+       * several islands that stop coarsening at different levels (a
+       * hierarchy built from a refined AMR level) */
+      if (lvl_coarsest(s, L)) {
          pgb_coarsest_args a;
          int rc;
          coarsest_args(s, L, &a);

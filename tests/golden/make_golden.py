@@ -53,6 +53,43 @@ def cases():
     ]
 
 
+def dropin_cases():
+    """(case, mode, arg, level) of the drop-in application fixtures
+    (tests/dropin/nbs_app.c built over the reference's PAMR/AMRD with
+    amrd/mg.c): mode 0 solve_elliptics(level, 1, 0); mode 1 PAMR_build_mgh
+    of the finest level and `arg` vcycle calls with the finest sources
+    changed between them"""
+    small = dict(n=33, levels=3, min_boxes=2, max_boxes=4, min_side=5, max_side=17)
+    return [
+        (W.nbs2d_uneven(seed=1, **small), 0, 0, 1),
+        (W.nbs3d(17, 9, seed=0), 0, 0, 1),
+        (W.nbs2d_uneven(seed=2, **small), 0, 0, 2),
+        (W.nbs2d_uneven(seed=1, **small), 1, 4, 0),
+        (W.nbs3d(17, 9, seed=4, levels=3), 1, 3, 0),
+    ]
+
+
+def save_dropin(case, mode, arg, level, out, path):
+    """the case (as save() stores it) and what the application wrote: cycle
+    count, residuals, u and cmask of every AMR grid in PAMR order"""
+    from tests.dropin import dropin as D
+    res = out["res"] if mode == 1 else D.finest_residuals(out)
+    grids = np.array([[g.level] + list(g.shape) + list(g.bbox) + [0.0] * (6 - len(g.bbox))
+                      for g in case.grids])
+    p = case.params
+    og = np.array([[g["level"], *g["shape"], *g["bbox"]] for g in out["grids"]])
+    np.savez_compressed(
+        path, name=np.array(case.name), pde=case.pde, dim=case.dim,
+        base_shape=np.array(case.base_shape), base_bbox=np.array(case.base_bbox), grids=grids,
+        u0=np.concatenate(case.u0), src=np.concatenate(case.src), src1=np.concatenate(case.source(1)),
+        params=np.array([p.pre_swp, p.pst_swp, p.max_iter, p.min_iter, p.max_citer,
+                         p.min_cwidth, p.restr_u, p.restr_res, p.restr_src, p.interp_order]),
+        fparams=np.array([p.tol, p.crtol, p.w0_r, p.w0_i]),
+        mode=mode, arg=arg, level=level, iters=out["iters"], res=res, out_grids=og,
+        out_u=np.concatenate([g["u"] for g in out["grids"]]),
+        out_cmask=np.concatenate([g["cmask"] for g in out["grids"]]).astype(np.uint8))
+
+
 def interp_cases():
     """(case with seeded random u, (lc, AMR boundary width, order)) for the
     AMR-hierarchy interpolation fixtures"""
@@ -131,6 +168,14 @@ def main():
         save(c, ref, path)
         print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
               f"{len(ref['ops'])} m_util_r8 calls, {os.path.getsize(path) // 1024} KiB")
+    from tests.dropin import dropin as D
+    for c, mode, arg, level in dropin_cases():
+        path = os.path.join(HERE, f"dropin_{c.name}_m{mode}_a{arg}_L{level}.npz")
+        if os.path.exists(path) and "--all" not in sys.argv:
+            continue
+        out = D.run(D.REF_APP, c, mode=mode, arg=arg, level=level)
+        save_dropin(c, mode, arg, level, out, path)
+        print(f"{os.path.basename(path)}: {out['iters']} cycles, {os.path.getsize(path) // 1024} KiB")
     for c, spec, seed in interp_cases():
         lc, w, o = spec
         path = os.path.join(HERE, f"amr_interp_{c.name}_L{lc}_w{w}_o{o}.npz")

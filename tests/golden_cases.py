@@ -16,7 +16,44 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def files():
     """the solve fixtures"""
     return sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith("amr_interp_"))
+                  if not os.path.basename(f).startswith(("amr_interp_", "dropin_")))
+
+
+def dropin_files():
+    """the drop-in application fixtures"""
+    return sorted(glob.glob(os.path.join(GOLDEN, "dropin_*.npz")))
+
+
+def load_dropin(path: str):
+    """(case, mode, arg, level, what the reference build of the application
+    wrote: iters, residuals, and u / cmask per AMR grid in PAMR order)"""
+    z = np.load(path)
+    dim = int(z["dim"])
+    grids = []
+    for row in z["grids"]:
+        lev, s0, s1, s2 = (int(v) for v in row[:4])
+        grids.append(W.Grid(lev, tuple(float(v) for v in row[4:4 + 2 * dim]), (s0, s1, s2)))
+    ip = [int(v) for v in z["params"]]
+    fp = [float(v) for v in z["fparams"]]
+    params = W.MGParams(pre_swp=ip[0], pst_swp=ip[1], max_iter=ip[2], min_iter=ip[3],
+                        max_citer=ip[4], min_cwidth=ip[5], restr_u=ip[6], restr_res=ip[7],
+                        restr_src=ip[8], interp_order=ip[9], tol=fp[0], crtol=fp[1],
+                        w0_r=fp[2], w0_i=fp[3])
+    offs = np.cumsum([0] + [g.size for g in grids])
+    split = lambda a: [a[offs[i]:offs[i + 1]].copy() for i in range(len(grids))]  # noqa: E731
+    case = W.Case(str(z["name"]), int(z["pde"]), dim, tuple(int(v) for v in z["base_shape"]),
+                  tuple(float(v) for v in z["base_bbox"]), grids, split(z["u0"]), split(z["src"]), params,
+                  src_extra=[split(z["src1"])])
+    og, out = z["out_grids"], []
+    off = 0
+    for row in og:
+        n = int(row[1] * row[2] * row[3])
+        out.append({"level": int(row[0]), "shape": tuple(int(v) for v in row[1:4]),
+                    "bbox": tuple(float(v) for v in row[4:10]), "u": z["out_u"][off:off + n].copy(),
+                    "cmask": z["out_cmask"][off:off + n].astype(np.float64)})
+        off += n
+    ref = {"iters": int(z["iters"]), "res": z["res"].copy(), "grids": out}
+    return case, int(z["mode"]), int(z["arg"]), int(z["level"]), ref
 
 
 def interp_files():
