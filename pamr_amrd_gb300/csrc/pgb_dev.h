@@ -30,6 +30,10 @@ typedef struct {
    const pgb_tile *ctiles;     /* tiles holding a child-covered point or a point some
                                   interpolation to the next finer level reads */
    const pgb_tile *ztiles;     /* 32 x 8 x ztz columns (one-pass marching sweep, 3-D) */
+   const pgb_tile *mtiles;     /* mtx x 14 x mtz columns (TMA-staged one-pass sweep, 3-D) */
+   const void *tmaps;          /* its tensor maps (8 per box), or 0 where the level cannot use it */
+   int *err;                   /* device word a timed-out wait of that sweep sets */
+   int nmtiles, mtx, mtz;
    int ntiles, nrtiles, nbox, nctiles, nztiles;
    int tz, rtz, ztz;           /* planes per tile (3-D) of the tile lists */
    int dim;
@@ -114,6 +118,8 @@ int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
 int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, const int *gate, int gval, void *stream);
 int pgb_k_flip(int *parity, void *stream);
 int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, int fuse, int *slot, void *stream);
+/* tensor maps of the TMA-staged sweep (8 per box); 0, or 1 where unavailable */
+int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps);
 /* the device solve loop's step: records the finest norm of cycle *it,
  * counts the cycle and sets the while node's condition to pgb_solve's loop
  * test ((it < min_iter || res > tol) && it < max_iter) */

@@ -72,6 +72,9 @@ typedef struct {
    float *w32[PGB_NW32];         /* mixed form: correction, defect, Jacobian term, coarse correction,
                                   * second correction buffer (fused sweeps write it) */
    int n[3];                     /* Nx, Ny, Nz (Nz = 1 in 2-D) */
+   int wy;                       /* FP32 arrays: row pitch (Nx rounded up to 4 floats, so every row
+                                  * starts on 16 bytes: vector and TMA loads) */
+   long wz;                      /* FP32 arrays: plane pitch wy * Ny */
    int flags;
    int level;
    int count;                    /* # interior points with cmask_bdy ON (norm divisor) */

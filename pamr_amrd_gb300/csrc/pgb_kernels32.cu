@@ -30,6 +30,7 @@
  * multiply-adds, products with 1/dx^2, and FP32 wherever the value only
  * steers the smoother. Nothing here is compared bit for bit.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -75,6 +76,12 @@ enum { W_E = PGB_W32_E, W_D = 1, W_C = 2, W_X = 3, W_E2 = PGB_W32_E2 };
 __device__ __forceinline__ float *eslot(const pgb_dbox &b, int sl)
 {
    return sl == W_E2 ? b.w32[W_E2] : b.w32[W_E];
+}
+
+/* index into a box's FP32 arrays (rows padded to the pitch wy) */
+__device__ __forceinline__ long wq(const pgb_dbox &b, int i, int j, int k)
+{
+   return i + (long)b.wy * j + b.wz * k;
 }
 
 __device__ __forceinline__ bool interior32(const pgb_dbox &b, int i, int j, int k, int dim)
@@ -234,10 +241,10 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int ks = tl.k0 + tp.kk0;
    if (ks >= b.n[2]) return;
-   long p = i + sy * j + sz * ks;
+   long p = i + sy * j + sz * ks, q = wq(b, i, j, ks);
    double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
-   for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
+   for (int kk = 0; kk < PGB_TZ; kk++, p += sz, q += b.wz) {
       const int k = ks + kk;
       if (kk >= tp.nk || k >= b.n[2]) continue;
       const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
@@ -250,8 +257,8 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
          const double l = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c);
          if (cm) r = fma(-res[p], w0_r, l);
          if (rl) {
-            wd[p] = d2f(r - l);
-            wc[p] = c;
+            wd[q] = d2f(r - l);
+            wc[q] = c;
          }
       } else if (cm)
          r = -res[p] * w0_r;
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
    float *__restrict__ e = b.w32[W_E];
    const float *__restrict__ dd = b.w32[W_D];
    const float *__restrict__ cc = b.w32[W_C];
-   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1], wy = b.wy, wz = b.wz;
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
    const float j0 = b.fj0;
    const int j = tl.j0 + threadIdx.y;
@@ -302,11 +309,11 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
       const int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
       const int i = tl.i0 + 2 * threadIdx.x + par;
       if (!interior32(b, i, j, k, dim)) continue;
-      const long p = i + sy * j + sz * k;
+      const long p = i + sy * j + sz * k, q = i + wy * j + wz * k;
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
       const bool d3 = dim == 3;
-      e[p] = gs32(e[p], e[p - 1], e[p + 1], e[p - sy], e[p + sy], d3 ? e[p - sz] : 0.f, d3 ? e[p + sz] : 0.f,
-                  cc[p], dd[p], ix, iy, iz, j0, d3);
+      e[q] = gs32(e[q], e[q - 1], e[q + 1], e[q - wy], e[q + wy], d3 ? e[q - wz] : 0.f, d3 ? e[q + wz] : 0.f,
+                  cc[q], dd[q], ix, iy, iz, j0, d3);
    }
 }
 
@@ -347,7 +354,7 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
       const int gi = gi0 + x, gj = gj0 + y, gk = gk0 + z;
       float v = 0.f;
       if (gi >= 0 && gi < b.n[0] && gj >= 0 && gj < b.n[1] && gk >= 0 && gk < b.n[2])
-         v = e[gi + sy * gj + sz * gk];
+         v = e[wq(b, gi, gj, gk)];
       se[x + SX * (y + SY * z)] = v;
    }
    __syncthreads();
@@ -372,8 +379,9 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
          if (!allbdy && !b.cmask_bdy[p]) continue;
          const int sp = x + SX * (y + SY * z);
          const bool d3 = dim == 3;
+         const long qw = wq(b, gi, gj, gk);
          se[sp] = gs32(se[sp], se[sp - 1], se[sp + 1], se[sp - SX], se[sp + SX], d3 ? se[sp - SX * SY] : 0.f,
-                       d3 ? se[sp + SX * SY] : 0.f, cc[p], dd[p], ix, iy, iz, j0, d3);
+                       d3 ? se[sp + SX * SY] : 0.f, cc[qw], dd[qw], ix, iy, iz, j0, d3);
       }
       __syncthreads();
    }
@@ -381,7 +389,7 @@ __global__ void __launch_bounds__(NT) k_sweep32(const pgb_dbox *boxes, pgb_dleve
       const int x = q % PGB_TX, y = (q / PGB_TX) % PGB_TY, z = q / (PGB_TX * PGB_TY);
       const int gi = tl.i0 + x, gj = tl.j0 + y, gk = tl.k0 + z;
       if (gi < b.n[0] && gj < b.n[1] && gk < b.n[2])
-         eo[gi + sy * gj + sz * gk] = se[(x + H) + SX * ((y + H) + SY * (z + hz))];
+         eo[wq(b, gi, gj, gk)] = se[(x + H) + SX * ((y + H) + SY * (z + hz))];
    }
 }
 
@@ -442,7 +450,7 @@ __global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlev
       lany[u] = q < PL;
       lin[u] = lany[u] && gi >= 0 && gi < n0 && gj >= 0 && gj < n1;
       lso[u] = 4 * q;
-      lgo[u] = lin[u] ? gi + n0 * gj : 0;
+      lgo[u] = lin[u] ? gi + bp->wy * gj : 0;   /* FP32 arrays: padded pitch */
    }
    int rso[2][2], rgo[2][2], rpar[2];   /* [pass][parity] */
    bool rok[2][2];
@@ -462,11 +470,11 @@ __global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlev
    const int sxs = 2 + t % PGB_TX, sys_ = 2 + t / PGB_TX;
    const bool sok = gi0 + sxs < n0 && gj0 + sys_ < n1;
    const int sso = sys_ * ZX + sxs;
-   const long sgo = (long)(gi0 + sxs) + (long)n0 * (gj0 + sys_);
+   const long sgo = (long)(gi0 + sxs) + (long)bp->wy * (gj0 + sys_);
 
    auto fetch = [&](int k) {   /* plane k's copies (none outside the box or past what the chunk reads) */
       if (k < 0 || k >= n2 || k > k1 + 1) return;
-      const long koff = sz * k;
+      const long koff = bp->wz * k;
       const uint32_t r = 4u * (uint32_t)((k & (ZR - 1)) * PL);
 #pragma unroll
       for (int u = 0; u < 2; u++)
@@ -509,13 +517,295 @@ __global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlev
       __syncthreads();
 #pragma unroll
       for (int kw = k - 2; kw < k; kw++)   /* planes finished at this step */
-         if (kw >= k0 && kw < k1 && sok) eo[sgo + sz * kw] = se[(kw & (ZR - 1)) * PL + sso];
+         if (kw >= k0 && kw < k1 && sok) eo[sgo + bp->wz * kw] = se[(kw & (ZR - 1)) * PL + sso];
    }
    cp_async_wait_all();
 }
 #undef ZX
 #undef ZY
 #undef ZR
+
+/* ------------------------------------------- one-pass sweep, TMA-staged -- */
+/* One red-black sweep in one pass over memory on 3-D levels, the planes
+ * staged by the Tensor Memory Accelerator. A CTA owns an output column of
+ * TXO x TYO points (x start a multiple of 4, so that every TMA load starts
+ * on 16 bytes: the FP32 rows are padded to 16-byte pitches) and marches
+ * through MTZ planes of it. Each plane of the old correction (slot src,
+ * TXO+8 x TYO+4 points around the column), of D and of C (TXO+8 x TYO+2)
+ * arrives by one cp.async.bulk.tensor 3-D tile load per array into a ring
+ * of R plane slots, completion counted on the slot's mbarrier; loads run
+ * R-3 planes ahead of use and fill out-of-box coordinates with zeros.
+ * Step k: the first colour of plane k on the column grown by one point
+ * (from the old second-colour values around it), then the second colour
+ * of plane k-1 on the column (from the new first-colour values of planes
+ * k-2 .. k), then plane k-1 is final and stored to slot dst (8-byte
+ * stores, one point pair per thread). Thread (tx, ty) owns the point pair
+ * x = i0 - 2 + 2 tx, +1 of row y = j0 - 1 + ty: one point of each colour,
+ * its x neighbours in the pair and the next thread's (shuffles). As in the
+ * other fused kernels no CTA writes the slot the others read, the grown
+ * first colour is recomputed identically by the CTAs that share it, and
+ * every update is gs32, so the result equals the in-place colour passes
+ * bit for bit. Every mbarrier wait is bounded (globaltimer, ~1 s); on
+ * timeout the CTA sets *err, lets the loads it issued land and returns.
+ * Boxes must have their whole interior relaxed (PGB_BOX_BDY_INTERIOR). */
+#define MT_R 6           /* ring slots (planes) */
+#define MT_TYO 14        /* output rows per column */
+
+__device__ __forceinline__ uint32_t mt_saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t mt_ns()
+{
+   uint64_t t;
+   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+   return t;
+}
+
+__device__ __forceinline__ bool mt_try(uint64_t *bar, uint32_t phase)
+{
+   uint32_t ok;
+   asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                " selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(mt_saddr(bar)), "r"(phase)
+                : "memory");
+   return ok != 0;
+}
+
+__device__ __forceinline__ bool mt_wait(uint64_t *bar, uint32_t phase)
+{
+   const uint64_t t0 = mt_ns();
+   while (!mt_try(bar, phase))
+      if (mt_ns() - t0 > 1000000000ull) return false;
+   return true;
+}
+
+/* 3-D tile of a tensor map into shared memory, completion on bar */
+__device__ __forceinline__ void mt_load(float *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
+{
+   asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(mt_saddr(dst)),
+                "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(mt_saddr(bar))
+                : "memory");
+}
+
+template <int TXO>
+struct mt_shape {
+   static constexpr int PX = (TXO + 4) / 2, PY = MT_TYO + 2, NTH = PX * PY;
+   static constexpr int EW = TXO + 8, EH = MT_TYO + 4, DH = MT_TYO + 2;
+   static constexpr int ESZ = (EW * EH + 31) / 32 * 32, DSZ = (EW * DH + 31) / 32 * 32;
+   static constexpr int SLOT = ESZ + 2 * DSZ;                 /* floats per ring slot (128-byte multiple) */
+   static constexpr unsigned EBYTES = 4u * EW * EH, DBYTES = 4u * EW * DH;
+   static constexpr size_t SMEM = 4ul * MT_R * SLOT + 8ul * MT_R;
+};
+
+template <int TXO>
+__global__ void __launch_bounds__(mt_shape<TXO>::NTH) k_sweep32t(const pgb_dbox *boxes, pgb_dlevel lv,
+                                                                 const CUtensorMap *maps, int src, int dst,
+                                                                 int *err)
+{
+   typedef mt_shape<TXO> S;
+   extern __shared__ __align__(128) float sm[];
+   uint64_t *bar = (uint64_t *)(sm + MT_R * S::SLOT);
+   __shared__ int s_abort;
+   const pgb_tile tl = lv.mtiles[blockIdx.x];
+   const pgb_dbox *bp = boxes + tl.box;
+   const int n0 = bp->n[0], n1 = bp->n[1], n2 = bp->n[2];
+   const long wy = bp->wy, wz = bp->wz;
+   float *__restrict__ eo = bp->w32[dst];
+   const float ix = bp->fidx2[0], iy = bp->fidx2[1], iz = bp->fidx2[2], j0 = bp->fj0;
+   const CUtensorMap *me = maps + 8 * tl.box + (src == W_E2 ? 1 : 0), *md = maps + 8 * tl.box + 2,
+                     *mc = maps + 8 * tl.box + 3;
+   const int i0 = tl.i0, jb = tl.j0, kb = tl.k0, ke = min(tl.k0 + lv.mtz, n2);   /* planes [kb, ke) written */
+   const int tx = threadIdx.x, ty = threadIdx.y, t = tx + S::PX * ty;
+   const int lane = t & 31;
+   /* the thread's pair in the staged E plane: columns ex, ex + 1 of row ey */
+   const int ex = 2 + 2 * tx, ey = 1 + ty;
+   const int gx = i0 - 4 + ex, gy = jb - 2 + ey;   /* global x, y of the pair's first point */
+   const bool row_red = ey >= 1 && ey <= S::DH, row_blk = ey >= 2 && ey <= S::DH - 1;
+   const bool yin = gy >= 1 && gy <= n1 - 2;
+   if (t == 0) {
+      s_abort = 0;
+      for (int r = 0; r < MT_R; r++)
+         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mt_saddr(bar + r)), "r"(1) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   __syncthreads();
+   /* plane m lives in slot (m - kb + 2) % R; its phase flips with each reuse */
+   const int m0 = kb - 2, mlast = min(ke + 1, n2 - 1);
+   auto slot_of = [&](int m) { return (m - m0) % MT_R; };
+   auto issue = [&](int m) {   /* thread 0 */
+      if (m < 0 || m > mlast) return;
+      float *sl = sm + slot_of(m) * S::SLOT;
+      uint64_t *b = bar + slot_of(m);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mt_saddr(b)),
+                   "r"(S::EBYTES + 2 * S::DBYTES) : "memory");
+      mt_load(sl, me, i0 - 4, jb - 2, m, b);
+      mt_load(sl + S::ESZ, md, i0 - 4, jb - 1, m, b);
+      mt_load(sl + S::ESZ + S::DSZ, mc, i0 - 4, jb - 1, m, b);
+   };
+   int waited = m0 - 1;   /* planes up to here have landed */
+   auto await = [&](int m) -> bool {   /* all threads; plane m (and earlier) usable after this */
+      if (m > mlast) m = mlast;
+      if (m <= waited) return true;
+      if (t == 0) {
+         for (int q = waited + 1; q <= m; q++)
+            if (q >= 0 && !s_abort && !mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1)) {
+               s_abort = 1;
+               *err = 1;
+            }
+      }
+      __syncthreads();
+      waited = m;
+      return !s_abort;
+   };
+   auto bail = [&]() {   /* lets every load issued so far land (bounded), then returns */
+      if (t == 0)
+         for (int q = max(waited + 1, 0); q <= min(mlast, waited + MT_R); q++)
+            mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1);
+      __syncthreads();
+   };
+   if (t == 0)
+      for (int m = m0; m < m0 + MT_R; m++) issue(m);
+
+   /* one colour at plane k: the pair member with (x + y + k) odd (first
+    * colour, num.f:220 parity in 0-based indices) or even (second) */
+   auto relax = [&](int k, int second) {
+      float *pe = sm + slot_of(k) * S::SLOT;
+      const float *pm = sm + slot_of(k - 1) * S::SLOT, *pp = sm + slot_of(k + 1) * S::SLOT;
+      const float *pd = pe + S::ESZ, *pc = pe + S::ESZ + S::DSZ;
+      const int o = ey * S::EW + ex;
+      const float2 v = *reinterpret_cast<const float2 *>(pe + o);
+      const float left = __shfl_up_sync(0xffffffffu, v.y, 1), right = __shfl_down_sync(0xffffffffu, v.x, 1);
+      const int odd = (gx + gy + k) & 1;               /* gx even: the first point's colour */
+      const int mem = second ? odd : odd ^ 1;          /* 0: the first point of the pair, 1: the second */
+      const int xl = ex + mem, gxx = gx + mem;
+      const bool region = second ? (row_blk && xl >= 4 && xl <= TXO + 3) : (row_red && xl >= 3 && xl <= TXO + 4);
+      if (!region || k < 1 || k > n2 - 2 || !yin || gxx < 1 || gxx > n0 - 2) return;
+      const int c = o + mem;
+      const float ec = mem ? v.y : v.x, xm = mem ? v.x : left, xp = mem ? right : v.y;
+      const int od = c - S::EW;   /* D and C planes start one row later */
+      pe[c] = gs32(ec, xm, xp, pe[c - S::EW], pe[c + S::EW], pm[c], pp[c], pc[od], pd[od], ix, iy, iz, j0, true);
+      (void)lane;
+   };
+
+   for (int k = kb - 1; k <= ke; k++) {
+      if (!await(k + 1)) {
+         bail();
+         return;
+      }
+      relax(k, 0);
+      __syncthreads();
+      if (k - 1 >= kb) {
+         relax(k - 1, 1);
+         __syncthreads();
+         /* plane k-1 is final: store the column (in-box points) */
+         const int kw = k - 1;
+         if (row_blk && tx >= 1 && tx <= TXO / 2 && gy < n1 && gx < n0) {
+            const float *pe = sm + slot_of(kw) * S::SLOT;
+            const float2 v = *reinterpret_cast<const float2 *>(pe + ey * S::EW + ex);
+            float *g = eo + gx + wy * gy + wz * kw;
+            if (gx + 1 < n0) *reinterpret_cast<float2 *>(g) = v;
+            else g[0] = v.x;
+         }
+      }
+      /* plane k-2's slot is free once every thread is past this step */
+      __syncthreads();
+      if (t == 0 && k - 2 >= m0) {
+         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+         issue(k - 2 + MT_R);
+      }
+   }
+}
+
+/* Tensor maps of the TMA sweep: per box, for the output widths 60 and 28,
+ * the old correction in slot 0 and slot 4, D and C (3-D tiles of the
+ * padded FP32 arrays; out-of-box coordinates read as zero). */
+#include <cudaTypedefs.h>
+
+static int mt_encode(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap *m, const float *base, const pgb_dbox &b,
+                     int w, int h)
+{
+   cuuint64_t dims[3] = {(cuuint64_t)b.n[0], (cuuint64_t)b.n[1], (cuuint64_t)b.n[2]};
+   cuuint64_t strides[2] = {(cuuint64_t)b.wy * 4, (cuuint64_t)b.wz * 4};
+   cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1}, es[3] = {1, 1, 1};
+   CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)base, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+   return r != CUDA_SUCCESS;
+}
+
+/* builds 8 maps per box (widths 60, 28 x slot 0, slot 4, D, C) in device
+ * memory; returns 0, or 1 when the driver has no tensor-map encoder or a
+ * box is not 3-D (the TMA sweep is then not offered) */
+extern "C" int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps)
+{
+   static PFN_cuTensorMapEncodeTiled_v12000 enc = 0;
+   *d_maps = 0;
+   if (!enc) {
+      cudaDriverEntryPointQueryResult q;
+      void *fn = 0;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+              cudaSuccess ||
+          q != cudaDriverEntryPointSuccess || !fn) {
+         cudaGetLastError();
+         return 1;
+      }
+      enc = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+   }
+   CUtensorMap *h = (CUtensorMap *)calloc((size_t)nbox * 8, sizeof(CUtensorMap));
+   int bad = 0;
+   for (int i = 0; i < nbox && !bad; i++) {
+      const pgb_dbox &b = hbox[i];
+      if (b.n[2] < 3 || !b.w32[W_E]) {
+         bad = 1;
+         break;
+      }
+      const int txo[2] = {60, 28};
+      for (int v = 0; v < 2 && !bad; v++) {
+         CUtensorMap *m = h + 8 * i + 4 * v;
+         const int w = txo[v] + 8;
+         bad |= mt_encode(enc, m + 0, b.w32[W_E], b, w, MT_TYO + 4);
+         bad |= mt_encode(enc, m + 1, b.w32[W_E2], b, w, MT_TYO + 4);
+         bad |= mt_encode(enc, m + 2, b.w32[W_D], b, w, MT_TYO + 2);
+         bad |= mt_encode(enc, m + 3, b.w32[W_C], b, w, MT_TYO + 2);
+      }
+   }
+   if (!bad && cudaMalloc(d_maps, sizeof(CUtensorMap) * 8 * (size_t)nbox) == cudaSuccess)
+      bad = cudaMemcpy(*d_maps, h, sizeof(CUtensorMap) * 8 * (size_t)nbox, cudaMemcpyHostToDevice) != cudaSuccess;
+   else
+      bad = 1;
+   free(h);
+   if (bad) {
+      if (*d_maps) cudaFree(*d_maps);
+      *d_maps = 0;
+      cudaGetLastError();
+      return 1;
+   }
+   return 0;
+}
+
+/* one TMA sweep of level lv from slot src into slot dst; maps from
+ * pgb_tmaps_build, txo the output width the level's tile list was made for */
+static int sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const void *maps, int src, int dst, int *err,
+                    cudaStream_t st)
+{
+   if (!lv.nmtiles) return 0;
+   static int attr = 0;
+   if (!attr) {
+      cudaFuncSetAttribute(k_sweep32t<60>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt_shape<60>::SMEM);
+      cudaFuncSetAttribute(k_sweep32t<28>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt_shape<28>::SMEM);
+      attr = 1;
+   }
+   /* the maps of width 60 sit at 8 i + 0..3, of width 28 at 8 i + 4..7 */
+   const CUtensorMap *m = (const CUtensorMap *)maps;
+   if (lv.mtx == 60)
+      k_sweep32t<60><<<lv.nmtiles, dim3(mt_shape<60>::PX, mt_shape<60>::PY), mt_shape<60>::SMEM, st>>>(
+         boxes, lv, m, src, dst, err);
+   else
+      k_sweep32t<28><<<lv.nmtiles, dim3(mt_shape<28>::PX, mt_shape<28>::PY), mt_shape<28>::SMEM, st>>>(
+         boxes, lv, m + 4, src, dst, err);
+   return check32("sweep32t");
+}
 
 /* E = the correction in slot src, over the level's tiles (the end of an
  * odd number of fused sweep launches) */
@@ -532,8 +822,8 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
    for (int kk = 0; kk < kz; kk++) {
       const int k = tl.k0 + kk;
       if (k >= b.n[2]) break;
-      const long p = i + sy * j + sz * k;
-      e[p] = a[p];
+      const long q = wq(b, i, j, k);
+      e[q] = a[q];
    }
 }
 
@@ -561,12 +851,13 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
    for (int kk = 0; kk < PGB_TZ; kk++) {
       const int k = tl.k0 + tp.kk0 + kk;
       if (kk >= tp.nk || k >= b.n[2]) continue;
-      const long p = i + sy * j + sz * k;
+      const long p = i + sy * j + sz * k, q = wq(b, i, j, k);
       if (!relaxed32(b, i, j, k, p, dim)) continue;
-      const float ec = e[p];
-      float t = (e[p + 1] - 2.f * ec + e[p - 1]) * ix + (e[p + sy] - 2.f * ec + e[p - sy]) * iy;
-      if (dim == 3) t += (e[p + sz] - 2.f * ec + e[p - sz]) * iz;
-      dd[p] = dd[p] - (t + cc[p] * ec);
+      const long wy = b.wy, wz = b.wz;
+      const float ec = e[q];
+      float t = (e[q + 1] - 2.f * ec + e[q - 1]) * ix + (e[q + wy] - 2.f * ec + e[q - wy]) * iy;
+      if (dim == 3) t += (e[q + wz] - 2.f * ec + e[q - wz]) * iz;
+      dd[q] = dd[q] - (t + cc[q] * ec);
    }
 }
 
@@ -594,14 +885,14 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
    for (int kk = 0; kk < PGB_TZ; kk++) {
       const int k = tl.k0 + tp.kk0 + kk;
       if (kk >= tp.nk || k >= b.n[2]) continue;
-      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
-      double corr = f2d(es[p]);
+      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k), q = wq(b, i, j, k);
+      double corr = f2d(es[q]);
       if (post && !relaxed32(b, i, j, k, p, lv.dim)) {
          const double r = res[p];
          corr += r - f2d(d2f(r));
       }
       u[p] += corr;
-      e[p] = 0.f;
+      e[q] = 0.f;
    }
 }
 
@@ -617,14 +908,20 @@ __global__ void __launch_bounds__(NT) k_zero32(const pgb_dbox *boxes, pgb_dlevel
    for (int kk = 0; kk < PGB_TZ; kk++) {
       const int k = tl.k0 + kk;
       if (kk >= kz || k >= b.n[2]) continue;
-      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
-      for (int f = 0; f < 4; f++) b.w32[f][p] = 0.f;
+      const long q = wq(b, i, j, k);
+      for (int f = 0; f < 4; f++) b.w32[f][q] = 0.f;
    }
 }
 
 __device__ __forceinline__ long lin32(const pgb_dbox &b, int i1, int j1, int k1)
 {
    return (i1 - 1) + (long)b.n[0] * ((j1 - 1) + (long)b.n[1] * (k1 - 1));
+}
+
+/* the same 1-based point in the box's FP32 arrays */
+__device__ __forceinline__ long lin32w(const pgb_dbox &b, int i1, int j1, int k1)
+{
+   return wq(b, i1 - 1, j1 - 1, k1 - 1);
 }
 
 /* FP32 copy of the correction in slot `slot` along a sync plan (PAMR_sync
@@ -635,8 +932,8 @@ __global__ void k_copy32(const pgb_dbox *boxes, const pgb_copy_op *ops, int slot
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    OP_PLANES(o.ni, o.nj, o.nk, {
-      eslot(d, slot)[lin32(d, o.i2 + a, o.j2 + bb, o.k2 + c)] =
-         eslot(s, slot)[lin32(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
+      eslot(d, slot)[lin32w(d, o.i2 + a, o.j2 + bb, o.k2 + c)] =
+         eslot(s, slot)[lin32w(s, o.i1 + a, o.j1 + bb, o.k1 + c)];
    })
 }
 
@@ -746,7 +1043,7 @@ __global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dle
       const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       const double r = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) * inv_w0;
       b.f[PGB_F_RES][p] = r;
-      b.w32[W_X][p] = d2f(r);
+      b.w32[W_X][wq(b, i, j, k)] = d2f(r);
    }
 }
 
@@ -800,7 +1097,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
       if (dim != 3) az[0] = 0;
       for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
          const int fi = o.i2 + a;
-         const long pd = lin32(d, fi, fj, fk);
+         const long pd = lin32(d, fi, fj, fk), pw = lin32w(d, fi, fj, fk);
          bool fp64;
          if (allrel) {
             if (face || fi == 1 || fi == d.n[0]) continue;   /* k_interp_edges */
@@ -810,7 +1107,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
          if (fp64) {
             const double v = interp_point64(o, s, a, bb, c, dim);
             d.f[PGB_F_RES][pd] = v;
-            eslot(d, slot)[pd] = d2f(v);
+            eslot(d, slot)[pw] = d2f(v);
             continue;
          }
          int ax[4];
@@ -820,12 +1117,12 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
             float jv[4];
             for (int qq = 0; qq < ny; qq++) {
                float iv[4];
-               for (int pp = 0; pp < nx; pp++) iv[pp] = x[lin32(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
+               for (int pp = 0; pp < nx; pp++) iv[pp] = x[lin32w(s, o.i1i + ax[pp], o.j1i + ay[qq], o.k1i + az[r])];
                jv[qq] = wsum32(nx, cx, iv);
             }
             kv[r] = wsum32(ny, cy, jv);
          }
-         eslot(d, slot)[pd] = wsum32(nz, cz, kv);
+         eslot(d, slot)[pw] = wsum32(nz, cz, kv);
       }
    }
 }
@@ -845,6 +1142,7 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
    double *__restrict__ res = d.f[PGB_F_RES];
    const long sny = s.n[0], snz = (long)s.n[0] * s.n[1];
    const long dny = d.n[0], dnz = (long)d.n[0] * d.n[1];
+   const long swy = s.wy, swz = s.wz, dwy = d.wy, dwz = d.wz;   /* FP32 pitches */
    for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
       const int bb = row % o.njb, c = row / o.njb;
       const int fj = o.j2 + bb, fk = o.k2 + c;
@@ -854,9 +1152,12 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
       const long oy = (ty & 1) ? sny : 0, oz = (tz & 1) ? snz : 0;
       const long rowc = (o.j1i - 1 + (ty >> 1)) * sny + (dim == 3 ? (o.k1i - 1 + (tz >> 1)) * snz : 0);
       const long rowf = (long)(fj - 1) * dny + (long)(fk - 1) * dnz;
+      const long oyw = (ty & 1) ? swy : 0, ozw = (tz & 1) ? swz : 0;
+      const long rowcw = (o.j1i - 1 + (ty >> 1)) * swy + (dim == 3 ? (o.k1i - 1 + (tz >> 1)) * swz : 0);
+      const long rowfw = (long)(fj - 1) * dwy + (long)(fk - 1) * dwz;
       for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
          const int fi = o.i2 + a;
-         const long pd = rowf + fi - 1;
+         const long pd = rowf + fi - 1, pw = rowfw + fi - 1;
          const int tx = o.i2b - 1 + a, ox = tx & 1;
          if (allrel) {
             if (face || fi == 1 || fi == d.n[0]) continue;   /* k_interp_edges */
@@ -865,13 +1166,13 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
             const double v = 0.125 * (((c0[0] + c0[ox]) + (c0[oy] + c0[ox + oy])) +
                                       ((c0[oz] + c0[ox + oz]) + (c0[oy + oz] + c0[ox + oy + oz])));
             res[pd] = v;
-            e[pd] = d2f(v);
+            e[pw] = d2f(v);
             continue;
          }
-         const float *c0 = x + rowc + (o.i1i - 1 + (tx >> 1));
-         const float v = ((c0[0] + c0[ox]) + (c0[oy] + c0[ox + oy])) +
-                         ((c0[oz] + c0[ox + oz]) + (c0[oy + oz] + c0[ox + oy + oz]));
-         e[pd] = 0.125f * v;
+         const float *c0 = x + rowcw + (o.i1i - 1 + (tx >> 1));
+         const float v = ((c0[0] + c0[ox]) + (c0[oyw] + c0[ox + oyw])) +
+                         ((c0[ozw] + c0[ox + ozw]) + (c0[oyw + ozw] + c0[ox + oyw + ozw]));
+         e[pw] = 0.125f * v;
       }
    }
 }
@@ -906,7 +1207,7 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
          const long pd = lin32(d, o.i2 + a, fj, fk);
          const double v = interp_point64(o, s, a, bb, c, dim);
          d.f[PGB_F_RES][pd] = v;
-         eslot(d, slot)[pd] = d2f(v);
+         eslot(d, slot)[lin32w(d, o.i2 + a, fj, fk)] = d2f(v);
       }
       return;
    }
@@ -922,7 +1223,7 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
       const long pd = lin32(d, o.i2 + a, fj, fk);
       const double v = interp_point64(o, s, a, bb, c, dim);
       d.f[PGB_F_RES][pd] = v;
-      eslot(d, slot)[pd] = d2f(v);
+      eslot(d, slot)[lin32w(d, o.i2 + a, fj, fk)] = d2f(v);
    }
 }
 
@@ -968,10 +1269,10 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    const int ks = tl.k0 + tp.kk0;
    if (i < b.n[0] && j < b.n[1] && ks < b.n[2]) {
-      long p = i + sy * j + sz * ks;
+      long p = i + sy * j + sz * ks, q = wq(b, i, j, ks);
       double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
 #pragma unroll
-      for (int kk = 0; kk < PGB_TZ; kk++, p += sz) {
+      for (int kk = 0; kk < PGB_TZ; kk++, p += sz, q += b.wz) {
          const int k = ks + kk;
          if (kk >= tp.nk || k >= b.n[2]) continue;
          const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
@@ -979,8 +1280,8 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
             float c;
             const double r = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c) - rhs[p];
             res[p] = r;
-            wd[p] = d2f(-r);
-            wc[p] = c;
+            wd[q] = d2f(-r);
+            wc[q] = c;
             if (norm_out) acc = fma(r, r, acc);
          }
          zm = uc;
@@ -1305,6 +1606,14 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
    }
    /* fused launches alternate between the two correction slots */
    while (done < nsweep) {
+      if ((fuse == 4 || fuse == 5) && lv.dim == 3 && lv.tmaps && lv.nmtiles) {
+         if (sweep32t(boxes, lv, lv.tmaps, src, dst, lv.err, (cudaStream_t)stream)) return 1;
+         done += 1;
+         const int t = src;
+         src = dst;
+         dst = t;
+         continue;
+      }
       if (fuse == 3 && lv.dim == 3) {
          k_sweep32z<<<lv.nztiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src, dst);
          done += 1;

@@ -489,12 +489,14 @@ __device__ double fwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0
  * at the points where it writes res (0 wherever res is 0). The restricted
  * residual only steers the coarse-grid correction, so FP32 is enough; the
  * FP64 residual of the finest level still decides convergence. */
-__device__ double fwr_d32(const float *dd, int nx1, int ny1, int nz1, int i0, int j0, int k0)
+__device__ double fwr_d32(const float *dd, int wy, long wz, int nx1, int ny1, int nz1, int i0, int j0, int k0)
 {
-   const int sy = nx1, sz = nx1 * ny1;
-   const int p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
+   const int sy = wy;
+   const long sz = wz;   /* the FP32 arrays' padded pitches */
+   const long p = (i0 - 1) + (long)sy * (j0 - 1) + sz * (k0 - 1);
    bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
-   int s0, s1, s2, n0, n1;
+   long s0, s1, s2;
+   int n0, n1;
    float scale;
    if (ii && jj && kk) {
       s0 = sz; s1 = sy; s2 = 1; n0 = n1 = 3; scale = 1.f / 64.f;
@@ -543,7 +545,7 @@ __global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, in
          double v;
          if (op == 1) v = u[lin(s, i0, j0, k0)];
          else if (op == 2) v = hwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
-         else if (res32 && f == PGB_F_RES) v = fwr_d32(s.w32[PGB_W32_D], s.n[0], s.n[1], s.n[2], i0, j0, k0);
+         else if (res32 && f == PGB_F_RES) v = fwr_d32(s.w32[PGB_W32_D], s.wy, s.wz, s.n[0], s.n[1], s.n[2], i0, j0, k0);
          else v = fwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
          d.f[f][pd] = v;
       }

@@ -56,6 +56,9 @@ struct pgb_solver {
    int solve_ok;            /* 1 built, -1 not available (host loop) */
    double *d_hist;          /* finest residual after each cycle of a solve [max_iter] */
    int *d_parity;           /* mixed form: 0 / 1 for even / odd cycles of a solve */
+   void *d_tmaps;           /* mixed form, 3-D: tensor maps of the TMA-staged sweep (0: unavailable) */
+   int *d_err;              /* set by a device wait that timed out */
+   int mtx[PGB_MAXLEV + 1]; /* output width of the TMA sweep's columns per level (60 or 28) */
    int *d_it;               /* cycles run by the device loop */
    cudaEvent_t ev0, ev1;
    cudaStream_t side;       /* second stream for independent kernels of a cycle */
@@ -210,6 +213,45 @@ static int make_tiles(const pgb_hier *h, int L, int tx, int tz, pgb_tile **out, 
    return n;
 }
 
+/* tiles of tx x ty x tz points over the boxes of one level */
+static int make_tiles2(const pgb_hier *h, int L, int tx, int ty, int tz, pgb_tile **out, int *start)
+{
+   int b, n = 0, cap = 64;
+   pgb_tile *t = (pgb_tile *)malloc(sizeof(pgb_tile) * (size_t)cap);
+   for (b = 0; b < h->lev[L].nbox; b++) {
+      const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+      int i, j, k;
+      start[b] = n;
+      for (k = 0; k < bx->shape[2]; k += tz)
+         for (j = 0; j < bx->shape[1]; j += ty)
+            for (i = 0; i < bx->shape[0]; i += tx) {
+               if (n == cap) {
+                  cap *= 2;
+                  t = (pgb_tile *)realloc(t, sizeof(pgb_tile) * (size_t)cap);
+               }
+               t[n].box = h->lev[L].box[b];
+               t[n].i0 = i;
+               t[n].j0 = j;
+               t[n].k0 = k;
+               t[n].slot = n;
+               n++;
+            }
+   }
+   start[h->lev[L].nbox] = n;
+   *out = t;
+   return n;
+}
+
+/* the TMA-staged sweep needs tensor maps and boxes whose interior is all relaxed */
+static int level_tma_ok(const pgb_solver *s, int L)
+{
+   int b;
+   if (!s->d_tmaps || s->h.dim != 3) return 0;
+   for (b = 0; b < s->h.lev[L].nbox; b++)
+      if (!(s->h.boxes[s->h.lev[L].box[b]].flags & PGB_BOX_BDY_INTERIOR)) return 0;
+   return 1;
+}
+
 static int upload_plan(pgb_plan *p, size_t opsz)
 {
    if (!p->nops) return 0;
@@ -235,9 +277,13 @@ static int level_tables(pgb_solver *s, int L, int tz)
    int *rts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
    int *zts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
    int rtz = tz, ztz = h->dim == 3 ? 4 * tz : 1;
+   const int mtx = s->mtx[L] ? s->mtx[L] : 60, mtz = 32;
+   pgb_tile *mt = 0;
+   int *mts = (int *)malloc(sizeof(int) * (size_t)(nb + 1));
    int nt = make_tiles(h, L, PGB_TX, tz, &t, ts);
    int nrt = make_tiles(h, L, 2 * PGB_TX, rtz, &rt, rts);
    int nzt = make_tiles(h, L, PGB_TX, ztz, &zt, zts);
+   int nmt = h->dim == 3 ? make_tiles2(h, L, mtx, 14, mtz, &mt, mts) : 0;
    size_t b0 = 0, b1 = align256(sizeof(pgb_tile) * (size_t)nt);
    size_t b2 = b1 + align256(sizeof(pgb_tile) * (size_t)nrt);
    size_t b3 = b2 + align256(sizeof(int) * (size_t)(nb + 1));
@@ -248,9 +294,10 @@ static int level_tables(pgb_solver *s, int L, int tz)
    nct = make_cover_tiles(h, L, t, nt, tz, &ct);
    b6 = b5 + align256(sizeof(pgb_tile) * (size_t)(nct ? nct : 1));
    size_t b7 = b6 + align256(sizeof(pgb_tile) * (size_t)nzt);
+   size_t b8 = b7 + align256(sizeof(pgb_tile) * (size_t)(nmt ? nmt : 1));
    if (s->d_tables[L]) cudaFree(s->d_tables[L]);
    s->d_tables[L] = 0;
-   if (cudaMalloc(&s->d_tables[L], b7) != cudaSuccess) {
+   if (cudaMalloc(&s->d_tables[L], b8) != cudaSuccess) {
       rc = fail(10, "cudaMalloc of the level tables failed");
       goto out;
    }
@@ -261,7 +308,8 @@ static int level_tables(pgb_solver *s, int L, int tz)
        cudaMemcpy(dt + b2, ts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
        cudaMemcpy(dt + b3, rts, sizeof(int) * (size_t)(nb + 1), cudaMemcpyHostToDevice) ||
        cudaMemcpy(dt + b4, h->lev[L].box, sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice) ||
-       cudaMemcpy(dt + b6, zt, sizeof(pgb_tile) * (size_t)nzt, cudaMemcpyHostToDevice)) {
+       cudaMemcpy(dt + b6, zt, sizeof(pgb_tile) * (size_t)nzt, cudaMemcpyHostToDevice) ||
+       (nmt && cudaMemcpy(dt + b7, mt, sizeof(pgb_tile) * (size_t)nmt, cudaMemcpyHostToDevice))) {
       rc = fail(10, "upload of the level tables failed");
       goto out;
    }
@@ -275,6 +323,12 @@ static int level_tables(pgb_solver *s, int L, int tz)
    s->lv[L].ztiles = (const pgb_tile *)(dt + b6);
    s->lv[L].nztiles = nzt;
    s->lv[L].ztz = ztz;
+   s->lv[L].mtiles = (const pgb_tile *)(dt + b7);
+   s->lv[L].nmtiles = nmt;
+   s->lv[L].mtx = mtx;
+   s->lv[L].mtz = mtz;
+   s->lv[L].tmaps = level_tma_ok(s, L) ? s->d_tmaps : 0;
+   s->lv[L].err = s->d_err;
    s->lv[L].ntiles = nt;
    s->lv[L].nrtiles = nrt;
    s->lv[L].nbox = nb;
@@ -290,6 +344,8 @@ out:
    free(ts);
    free(rts);
    free(zts);
+   free(mt);
+   free(mts);
    return rc;
 }
 
@@ -324,7 +380,8 @@ static int setup_device(pgb_solver *s)
       w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * PGB_NW32);
       for (i = 0; i < h->nbox; i++) {
          const pgb_hbox *b = &h->boxes[i];
-         size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+         /* rows padded to a multiple of 4 floats (16 bytes) */
+         size_t n = (size_t)((b->shape[0] + 3) & ~3) * b->shape[1] * b->shape[2];
          for (f = 0; f < PGB_NW32; f++) {
             w32o[i * PGB_NW32 + f] = off;
             off = align256(off + 4 * n);
@@ -354,6 +411,8 @@ static int setup_device(pgb_solver *s)
       CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
       CU(cudaMemcpy((void *)db->cmask_bdy, b->bdy_mask, n, cudaMemcpyHostToDevice));
       for (d = 0; d < 3; d++) db->n[d] = b->shape[d];
+      db->wy = (b->shape[0] + 3) & ~3;
+      db->wz = (long)db->wy * b->shape[1];
       db->flags = b->flags;
       db->level = b->level;
       db->count = b->count;
@@ -375,6 +434,10 @@ static int setup_device(pgb_solver *s)
    free(w32o);
    CU(cudaMalloc((void **)&s->dbox, sizeof(pgb_dbox) * (size_t)h->nbox));
    CU(cudaMemcpy(s->dbox, s->hbox, sizeof(pgb_dbox) * (size_t)h->nbox, cudaMemcpyHostToDevice));
+   CU(cudaMalloc((void **)&s->d_err, sizeof(int)));
+   CU(cudaMemset(s->d_err, 0, sizeof(int)));
+   if (h->prm.precision == PGB_MIXED && h->dim == 3 && !getenv("PGB_NO_TMA"))
+      pgb_tmaps_build(s->hbox, h->nbox, &s->d_tmaps);   /* 1 (no maps): the TMA sweep is not offered */
 
    /* per-level tables: tiles, relax tiles, tile starts, box lists */
    for (L = 1; L <= h->nlev; L++) {
@@ -566,6 +629,8 @@ int pgb_destroy(pgb_solver *s)
       if (s->d_hist) cudaFree(s->d_hist);
       if (s->d_it) cudaFree(s->d_it);
       if (s->d_parity) cudaFree(s->d_parity);
+      if (s->d_tmaps) cudaFree(s->d_tmaps);
+      if (s->d_err) cudaFree(s->d_err);
       if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
       if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
       if (s->stream) {
@@ -713,13 +778,18 @@ static int autotune(pgb_solver *s)
    int L, changed = 0;
    int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
    s->tuned = 1;
-   if (force && force[0] >= '0' && force[0] <= '3' && !force[1]) {
+   if (force && force[0] >= '0' && force[0] <= '5' && !force[1]) {
       /* one sweep shape on every level instead of the measured choice */
       for (L = 2; L <= h->nlev; L++) {
          int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
          int f = force[0] - '0';
          if (f == 3 && h->dim != 3) f = 1;
+         if ((f == 4 || f == 5) && !level_tma_ok(s, L)) f = 1;
          s->fuse[L] = f == 2 && !can_fuse ? 1 : f;
+         if (f == 4 || f == 5) {
+            s->mtx[L] = f == 4 ? 60 : 28;
+            if (level_tables(s, L, s->lv[L].tz)) return 10;
+         }
       }
       drop_graph(s);
       return 0;
@@ -727,16 +797,23 @@ static int autotune(pgb_solver *s)
    if ((env && !strcmp(env, "0")) || nsw < 1) return 0;
    for (L = 2; L <= h->nlev; L++) {
       static const int tzs[4] = {8, 4, 2, 1};
-      int ntz = h->dim == 3 ? 4 : 1, a, f, best_tz = s->lv[L].tz, best_f = s->fuse[L];
+      int ntz = h->dim == 3 ? 4 : 1, a, f, best_tz = s->lv[L].tz, best_f = s->fuse[L], best_mtx = 60;
       int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
+      const int tma = level_tma_ok(s, L);
       float best = 1e30f;
       for (a = 0; a < ntz; a++) {
          if (h->dim == 3 && tzs[a] != s->lv[L].tz) {
             if (level_tables(s, L, tzs[a])) return 10;
             changed = 1;
          }
-         for (f = 0; f <= (h->dim == 3 ? 3 : can_fuse ? 2 : 1); f++) {
+         for (f = 0; f <= (h->dim == 3 ? 5 : can_fuse ? 2 : 1); f++) {
             if (f == 2 && !can_fuse) continue;
+            if (f >= 4) {   /* the TMA-staged sweep, columns 60 or 28 wide */
+               if (!tma) continue;
+               s->mtx[L] = f == 4 ? 60 : 28;
+               if (level_tables(s, L, tzs[a])) return 10;
+               changed = 1;
+            }
             float ms = 0;
             int r;
             for (r = 0; r < 9; r++) {   /* one warm-up, eight timed */
@@ -753,10 +830,12 @@ static int autotune(pgb_solver *s)
                best = ms;
                best_tz = s->lv[L].tz;
                best_f = f;
+               best_mtx = f >= 4 ? s->mtx[L] : 60;
             }
          }
       }
-      if (best_tz != s->lv[L].tz) {
+      if (best_tz != s->lv[L].tz || s->mtx[L] != best_mtx) {
+         s->mtx[L] = best_mtx;
          if (level_tables(s, L, best_tz)) return 10;
          changed = 1;
       }
@@ -1098,8 +1177,12 @@ static int vcycle_mixed(pgb_solver *s)
          pgb_coarsest_args a;
          int rc;
          coarsest_args(s, L, &a);
-         rc = pgb_k_coarsest_mixed(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace,
-                                   s->stream);
+         /* the FP32 SOR defect correction is made for one coarsest grid;
+          * several (islands of a refined level's grids, often thin strips)
+          * take the FP64 Gauss-Seidel loop of the reference */
+         rc = a.ncoarse == 1 ? pgb_k_coarsest_mixed(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a,
+                                                    s->d_trace, s->stream)
+                             : 1;
          if (rc < 0) return fail(11, "%s", pgb_dev_error32());
          if (rc > 0)   /* too large for one CTA's shared memory: the FP64 loop */
             KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
@@ -1228,6 +1311,14 @@ int pgb_vcycle(pgb_solver *s, double *res)
    }
    CU(cudaStreamSynchronize(s->stream));
    *res = s->h_res[0];
+   if (s->d_tmaps) {   /* a TMA sweep's wait that timed out leaves a flag */
+      int err = 0;
+      CU(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+      if (err) {
+         CU(cudaMemset(s->d_err, 0, sizeof(int)));
+         return fail(12, "a device wait for staged data timed out (TMA sweep); results are not valid");
+      }
+   }
    return 0;
 }
 
@@ -1265,9 +1356,18 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
       }
    CU(cudaEventRecord(s->ev1, s->stream));
    CU(cudaMemcpyAsync(s->h_res + 1, s->d_citers, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+   CU(cudaMemcpyAsync(s->h_res + 3, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
    CU(cudaStreamSynchronize(s->stream));
    CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
    memcpy(&ci, s->h_res + 1, sizeof(int));
+   {
+      int err = 0;
+      memcpy(&err, s->h_res + 3, sizeof(int));
+      if (err) {
+         CU(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
+         return fail(12, "a device wait for staged data timed out (TMA sweep); results are not valid");
+      }
+   }
    s->last_cycles = it;
    s->last_citers = ci;
    s->last_ms = ms;

@@ -66,7 +66,7 @@ def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
     u1 = s.get_u()
     shapes = [s.level_tuning(L) for L in range(2, s.num_levels() + 1)]
     s.close()
-    assert all(tz in (1, 2, 4, 8) and f in (0, 1, 2, 3) for tz, f in shapes), shapes
+    assert all(tz in (1, 2, 4, 8) and f in (0, 1, 2, 3, 4, 5) for tz, f in shapes), shapes
     monkeypatch.setenv("PGB_AUTOTUNE", "0")
     s = Solver(case)
     s.set_inputs()
@@ -81,15 +81,17 @@ def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
     assert max(float(np.max(np.abs(a - b))) for a, b in zip(u1, u2)) <= 1e-13 * umax
 
 
-@pytest.mark.parametrize("fuse", ["1", "2", "3"])
+@pytest.mark.parametrize("fuse", ["1", "2", "3", "4", "5"])
 @pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=1),
-                                  lambda: W.lapse2d_bo(129, seed=1, levels=4, step=40)],
-                         ids=["c3d65", "lapse129"])
+                                  lambda: W.lapse2d_bo(129, seed=1, levels=4, step=40),
+                                  lambda: W.poisson3d(129, seed=3)],
+                         ids=["c3d65", "lapse129", "p3d129"])
 def test_fused_sweeps_equal_colour_passes(monkeypatch, make, fuse):
-    """Sweeps fused in shared memory (one or two per launch, or one marching
-    through the planes) read the old correction from one buffer and write
-    the other: the solution is that of the in-place colour passes bit for
-    bit, on every repetition."""
+    """Sweeps fused in shared memory (one or two per launch, one marching
+    through the planes, or one marching with TMA-staged planes in columns 60
+    or 28 wide) read the old correction from one buffer and write the
+    other: the solution is that of the in-place colour passes bit for bit,
+    on every repetition."""
     case = make()
     case.params.precision = 1
 
