@@ -633,10 +633,15 @@ __global__ void __launch_bounds__(mt_shape<TXO>::NTH) k_sweep32t(const pgb_dbox 
    /* plane m lives in slot (m - kb + 2) % R; its phase flips with each reuse */
    const int m0 = kb - 2, mlast = min(ke + 1, n2 - 1);
    auto slot_of = [&](int m) { return (m - m0) % MT_R; };
+   int last_issued = m0 - 1;   /* thread 0: the newest plane whose slot a load or arrival was issued for */
    auto issue = [&](int m) {   /* thread 0 */
-      if (m < 0 || m > mlast) return;
-      float *sl = sm + slot_of(m) * S::SLOT;
       uint64_t *b = bar + slot_of(m);
+      last_issued = m;
+      if (m < 0 || m > mlast) {   /* nothing to load: complete the slot's phase anyway */
+         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mt_saddr(b)) : "memory");
+         return;
+      }
+      float *sl = sm + slot_of(m) * S::SLOT;
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mt_saddr(b)),
                    "r"(S::EBYTES + 2 * S::DBYTES) : "memory");
       mt_load(sl, me, i0 - 4, jb - 2, m, b);
@@ -647,20 +652,21 @@ __global__ void __launch_bounds__(mt_shape<TXO>::NTH) k_sweep32t(const pgb_dbox 
    auto await = [&](int m) -> bool {   /* all threads; plane m (and earlier) usable after this */
       if (m > mlast) m = mlast;
       if (m <= waited) return true;
-      if (t == 0) {
-         for (int q = waited + 1; q <= m; q++)
-            if (q >= 0 && !s_abort && !mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1)) {
-               s_abort = 1;
-               *err = 1;
-            }
+      bool ok = true;
+      for (int q = waited + 1; q <= m && ok; q++)   /* every thread observes the completion itself */
+         if (q >= 0 && !mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1)) ok = false;
+      if (!ok) {
+         s_abort = 1;
+         *err = 1;
       }
       __syncthreads();
+      if (s_abort) return false;
       waited = m;
-      return !s_abort;
+      return true;
    };
-   auto bail = [&]() {   /* lets every load issued so far land (bounded), then returns */
+   auto bail = [&]() {   /* lets every load still in flight land (bounded), then returns */
       if (t == 0)
-         for (int q = max(waited + 1, 0); q <= min(mlast, waited + MT_R); q++)
+         for (int q = max(waited + 1, 0); q <= min(mlast, last_issued); q++)
             mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1);
       __syncthreads();
    };
