@@ -64,32 +64,50 @@ def max_over_ranks(x: float, dist, torch, device: str) -> float:
 
 
 # ------------------------------------------------------------ CPU side --
-def _port_solve(seed: int) -> float:
+def _pin(seed: int):
+    """one solve per core: the process that solves seed s runs on core s mod n"""
+    try:
+        cores = sorted(os.sched_getaffinity(0))
+        os.sched_setaffinity(0, {cores[seed % len(cores)]})
+    except (AttributeError, OSError):
+        pass
+
+
+def _port_solve(seed: int, keep_u: bool = False):
     from oracle import portrun
+    _pin(seed)
     t = time.perf_counter()
-    portrun.solve(_case(seed))
-    return time.perf_counter() - t
+    r = portrun.solve(_case(seed), fast=True)
+    return time.perf_counter() - t, (r["u"] if keep_u else None)
 
 
-def _port_solve_poisson3d(seed: int) -> float:
+def _port_solve_keep(seed: int):
+    return _port_solve(seed, keep_u=seed == 0)
+
+
+def _port_solve_poisson3d(seed: int):
     from oracle import portrun
     from pamr_amrd_gb300 import workloads as W
+    _pin(seed)
     t = time.perf_counter()
-    portrun.solve(W.poisson3d(129, seed=seed))
-    return time.perf_counter() - t
+    portrun.solve(W.poisson3d(129, seed=seed), fast=True)
+    return time.perf_counter() - t, None
 
 
 def cpu_round(nproc: int, seed0: int = 0, solve=_port_solve) -> dict:
     """one bounded sample: nproc oracle-port solves of the workload, one per
-    host core, in parallel (spawned processes)"""
+    host core (pinned), in parallel (spawned processes); the port is built
+    -O3 -march=native for this (portrun.LIB_FAST)"""
     from oracle import portrun
-    portrun.build()
+    portrun.build(fast=True)
     ctx = mp.get_context("spawn")
     t = time.perf_counter()
     with ctx.Pool(nproc) as pool:
-        per = pool.map(solve, [seed0 + i for i in range(nproc)])
+        out = pool.map(solve, [seed0 + i for i in range(nproc)])
     wall = time.perf_counter() - t
-    return {"solves": nproc, "wall_s": wall, "per_solve_s": statistics.median(per)}
+    per = [o[0] for o in out]
+    u0 = next((o[1] for o in out if o[1] is not None), None)
+    return {"solves": nproc, "wall_s": wall, "per_solve_s": statistics.median(per), "u_seed0": u0}
 
 
 def cpu_model() -> str:
@@ -251,8 +269,9 @@ LAPSE_WORKLOAD = ("lapse2d_bo_257_L4: maximal-slicing lapse lap(alpha) = alpha*S
 def _lapse_port_solve(seed: int) -> float:
     from oracle import portrun
     from pamr_amrd_gb300 import workloads as W
+    _pin(seed)
     t = time.perf_counter()
-    portrun.solve(W.lapse2d_bo(257, seed=seed, levels=4))
+    portrun.solve(W.lapse2d_bo(257, seed=seed, levels=4), fast=True)
     return time.perf_counter() - t
 
 
@@ -351,7 +370,7 @@ def lapse_main(args):
     if not args.no_cpu_baseline:
         nproc = min(host_cores(), 16)
         from oracle import portrun
-        portrun.build()
+        portrun.build(fast=True)
         ctx = mp.get_context("spawn")
         t0 = time.perf_counter()
         with ctx.Pool(nproc) as pool:
@@ -396,7 +415,10 @@ def learned_main(args):
     n = 129
     h = 20.0 / (n - 1)
     t0 = time.perf_counter()
-    blobs, U = Lm.make_dataset(n, range(args.pairs), torch)
+    if args.pairs_from == "sequence":   # pairs along time-stepped runs, 20 coarse steps each
+        blobs, U = Lm.make_sequence_dataset(n, range((args.pairs + 19) // 20), 20, torch)
+    else:
+        blobs, U = Lm.make_dataset(n, range(args.pairs), torch)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     gain = Lm.fit_gain(n, blobs, U, torch)
@@ -491,13 +513,51 @@ def learned_main(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 guess + f32/f64 solve",
             "data": "synthetic (seeded rho; training seeds 0..pairs-1, timed on held-out seeds 100000+)",
             "config": {"workload": LEARNED_WORKLOAD, "l2": "flushed between steps (512 MiB write)",
-                       "pairs": args.pairs, "epochs": args.epochs, "lr": args.lr},
+                       "pairs": args.pairs, "pairs_from": args.pairs_from, "epochs": args.epochs, "lr": args.lr},
             "forms": out, "cpu_baseline": cpu, "predict_ms": ev[0].elapsed_time(ev[1]) / 10,
             "guess_error_vs_solution": {"max_rel": statistics.mean(e[0] for e in errs),
                                         "l2_rel": statistics.mean(e[1] for e in errs)},
             "training": {"dataset_s": t_data, "train_s": t_train, "epoch_loss": losses,
                          "params": model.net.num_params()}}
     print(json.dumps(line))
+
+
+def other_workload(S, make, torch, np, flush, steps: int, warmup: int) -> dict:
+    """solves/s of both forms on one more workload (device-resident inputs,
+    L2 flushed between steps, CUDA events on the solver's stream) and the
+    mixed form's error against the FP64 form"""
+    out = {}
+    sols = {}
+    for prec, form in ((0, "fp64"), (1, "mixed")):
+        case = make()
+        case.params.precision = prec
+        sv = S.Solver(case)
+        d_u0 = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.u0]
+        d_src = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in case.src]
+        st = torch.cuda.ExternalStream(sv.stream())
+        times, iters = [], []
+        for k in range(warmup + steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            sv.set_inputs_device([t.data_ptr() for t in d_u0], [t.data_ptr() for t in d_src])
+            r = sv.solve()
+            e1.record(st)
+            e1.synchronize()
+            if k >= warmup:
+                times.append(e0.elapsed_time(e1))
+                iters.append(r["iters"])
+        sols[form] = sv.get_u()
+        out[form] = {"solves_per_s": 1e3 * steps / sum(times), "vcycles_per_solve": statistics.mean(iters),
+                     "converged": r["res_final"] <= case.params.tol}
+        sv.close()
+    umax = max(float(np.max(np.abs(a))) for a in sols["fp64"])
+    out["speedup_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["error_vs_fp64_gpu_form_max_rel"] = max(float(np.max(np.abs(a - b))) for a, b in
+                                                zip(sols["mixed"], sols["fp64"])) / umax
+    out["points"] = make().total_points()
+    return out
 
 
 # ---------------------------------------------------------------- main --
@@ -513,6 +573,9 @@ def main():
                          "lapse_bo: the lapse solves of a Berger-Oliger sequence")
     ap.add_argument("--bo-steps", type=int, default=400, help="coarse steps of the sequence (lapse_bo)")
     ap.add_argument("--pairs", type=int, default=2000, help="training pairs (poisson3d_learned)")
+    ap.add_argument("--pairs-from", default="sequence", choices=["sequence", "seeds"],
+                    help="training pairs from time-stepped runs with drifting sources (20 steps per run, each "
+                         "solve started from the last) or from independent seeded sources (poisson3d_learned)")
     ap.add_argument("--epochs", type=int, default=4, help="training epochs (poisson3d_learned)")
     ap.add_argument("--lr", type=float, default=1e-3, help="peak learning rate (poisson3d_learned)")
     args = ap.parse_args()
@@ -624,8 +687,11 @@ def main():
         return {"total_ms": total, "iters": iters, "finals": finals, "wall_ms": wall,
                 "launches": launches, "clocks": ck}
 
+    # clocks sampled over both timed loops (the FP64 loop alone lasts seconds)
+    clk = Clocks(torch.cuda.current_device()) if rank == 0 else None
     tm64 = timed(s64, "fp64")
-    tmx = timed(smx, "mixed", clocks=True)
+    tmx = timed(smx, "mixed")
+    clocks = clk.stop() if clk else None
     value = world * args.steps / (tmx["total_ms"] / 1e3)
     fp64_value = world * args.steps / (tm64["total_ms"] / 1e3)
     ms_per_step = tmx["total_ms"] / args.steps
@@ -657,6 +723,19 @@ def main():
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_total = max_over_ranks(sum(e2e_ms), dist, torch, "cuda")
     e2e_value = world * args.steps / (e2e_total / 1e3)
+
+    # configs 1 and 3 of the same metric beside the headline workload: the
+    # 129^2 Poisson grid and the uneven 5-level hierarchy, both forms
+    extra = {}
+    if rank == 0:
+        from pamr_amrd_gb300 import workloads as W
+        for name, make in (("config1_poisson2d_129", lambda: W.poisson2d(129, seed=0)),
+                           ("config3_poisson2d_uneven", lambda: W.poisson2d_uneven(seed=0))):
+            try:
+                extra[name] = other_workload(S, make, torch, np, flush, steps=max(3, min(args.steps, 20)),
+                                             warmup=args.warmup)
+            except Exception as exc:   # a report, never a reason to lose the bench line
+                extra[name] = {"error": str(exc)}
 
     # roofline of the dominant smoother: FP32 sweep of the mixed form on the
     # 129^3 level (and the FP64 sweep of the plain form beside it)
@@ -697,13 +776,22 @@ def main():
         solve_roof = {"error": str(exc)}
 
     cpu = None
+    err_oracle = None
     if rank == 0 and not args.no_cpu_baseline:
         nproc = min(host_cores(), 32)
-        cr = cpu_round(nproc)
+        cr = cpu_round(nproc, solve=_port_solve_keep)
         cpu = {"value": cr["solves"] / cr["wall_s"], "unit": UNIT, "cores": nproc, "kind": "port",
                "sample": f"{nproc} concurrent oracle-port solves of the workload "
                          f"(median {cr['per_solve_s']:.1f} s per solve)",
-               "per_core_value": 1.0 / cr["per_solve_s"], "cpu_model": cpu_model()}
+               "per_core_value": 1.0 / cr["per_solve_s"], "cpu_model": cpu_model(),
+               "build": "oracle port, gcc -O3 -march=native -ffp-contract=off, one process per core, pinned"}
+        if cr["u_seed0"] is not None:   # the same seed as the GPU solves (rank 0)
+            omax = max(float(np.max(np.abs(a))) for a in cr["u_seed0"])
+            err_oracle = {
+                "fp64": {"max_abs": max(float(np.max(np.abs(a - b))) for a, b in zip(u64, cr["u_seed0"])),
+                         "bit_identical": all(np.array_equal(a, b) for a, b in zip(u64, cr["u_seed0"]))},
+                "mixed": {"max_abs": max(float(np.max(np.abs(a - b))) for a, b in zip(umx, cr["u_seed0"]))}}
+            err_oracle["mixed"]["max_rel"] = err_oracle["mixed"]["max_abs"] / omax
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -718,13 +806,17 @@ def main():
                 "vcycles_per_solve": statistics.mean(tmx["iters"]),
                 "fp64_vcycles_per_solve": statistics.mean(tm64["iters"]),
                 "converged": converged,
-                "error_vs_fp64_oracle": {"max_abs": emax, "max_rel": emax / umax, "l2": el2},
+                "error_vs_fp64_gpu_form": {"max_abs": emax, "max_rel": emax / umax, "l2": el2},
+                "error_vs_fp64_oracle": err_oracle,
+                "learned_guess_in_timed_solves": False,
+                "other_configs": extra,
                 "wall_ms_timed": tmx["wall_ms"],
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": tmx["launches"],
                 "roofline": roof, "solve_roofline": solve_roof, "cpu_baseline": cpu,
-                "clocks": tmx["clocks"]}
+                "clocks": clocks,
+                "ms_x_median_sm_mhz": (ms_per_step * clocks["sm_mhz"]) if clocks and clocks.get("sm_mhz") else None}
         print(json.dumps(line))
     s64.close()
     smx.close()

@@ -268,7 +268,11 @@ int pgb_plan_dump(const pgb_solver *s, int which, int level, int *rows, int cap)
 /* No counterpart in the reference. The residual of ONE grid,
  * res = L[u] - rhs at interior points where cmask is ON (cmask = NULL: all
  * interior points), and its RMS norm written to *norm (device double), as
- * app_MG_residual computes them -- for callers that cannot allocate device
+ * app_MG_residual computes them. cmask is one byte per point, nonzero =
+ * AMRD_CMASK_ON (PAMR keeps cmask as doubles 1.0 / 0.0: convert); points
+ * where it is 0 and the grid's boundary points are not written. With no ON
+ * point the norm is 0/0, NaN, as the reference hook's sqrt(norm/sum)
+ * (examples/nbs/num.f:158). For callers that cannot allocate device
  * memory when they need it: applications that own and budget all device
  * memory themselves (as PAMR owns all grid memory), and callers that must
  * not let a cudaMalloc/cudaFree synchronize the device between their
@@ -420,6 +424,12 @@ int pgb_net_predict(pgb_net *net, const double *rho, double *u, void *stream);
  * whose shape is right but whose amplitude is off gets the amplitude from
  * the equation. Runs on the device (no host synchronisation). */
 int pgb_net_rescale(pgb_net *net, const double *rho, double *u, double h, void *stream);
+/* pgb_net_rescale is also the guess's guard: a guess that is not finite
+ * (any NaN or Inf), is zero, or needs an amplitude factor outside
+ * [1/16, 16] is replaced on the device by u = 0, the plain solve's initial
+ * guess, so a corrupt prediction costs nothing but the prediction; this
+ * returns how many guesses were replaced so far */
+int pgb_net_rejected_guesses(pgb_net *net, long *count);
 int pgb_net_loss_grad(pgb_net *net, const double *rho, const float *u_target, double *loss, void *stream);
 int pgb_net_train_step(pgb_net *net, const double *rho, const float *u_target, float lr, double *loss,
                        void *stream);

@@ -11,10 +11,11 @@
 #   tests/dropin/nbs_app.c, env_ref.c          the drop-in test application
 # The shipped binaries under lib/ and bin/ are never read or linked.
 #
-# usage: oracle/build_ref.sh [reference dir]   (default /root/reference)
+# usage: oracle/build_ref.sh [reference dir]
+#        (default $PAMR_REFERENCE_DIR, else a "reference" directory beside the repository)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-${PAMR_REFERENCE_DIR:-/root/reference}}"
+REF="${1:-${PAMR_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/amrd/mg.c" ]; then
   echo "build_ref: reference sources not found at $REF" >&2

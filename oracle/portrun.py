@@ -14,17 +14,23 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "port", "libmgport.so")
+# the same sources built for the timed CPU baseline: -O3 and the host's own
+# instruction set (-ffp-contract=off keeps the arithmetic; the parity checker
+# uses LIB, built without machine-specific flags so that x86 and Arm agree)
+LIB_FAST = os.path.join(HERE, "port", "libmgport_fast.so")
 SOURCES = [os.path.join(HERE, "port", "mg_port.c"), os.path.join(HERE, "mg_ops.c"),
            os.path.join(HERE, "m_util_r8.c"), os.path.join(HERE, "bo_ops.c")]
 
 
-def build(force: bool = False) -> str:
+def build(force: bool = False, fast: bool = False) -> str:
+    lib = LIB_FAST if fast else LIB
     newest = max(os.path.getmtime(s) for s in SOURCES)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-std=gnu11", "-fPIC",
-               "-shared", "-o", LIB] + SOURCES + ["-lm"]
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        opt = ["-O3", "-march=native"] if fast else ["-O2"]
+        cmd = ["gcc"] + opt + ["-ffp-contract=off", "-fno-fast-math", "-std=gnu11", "-fPIC",
+                               "-shared", "-o", lib] + SOURCES + ["-lm"]
         subprocess.run(cmd, check=True)
-    return LIB
+    return lib
 
 
 class _Case(C.Structure):
@@ -50,23 +56,23 @@ class _Result(C.Structure):
                 ("hk_idx", C.POINTER(C.c_int)), ("hk_norm", C.POINTER(C.c_double))]
 
 
-_lib = None
+_libs = {}
 
 
-def _load():
-    global _lib
-    if _lib is None:
-        _lib = C.CDLL(build())
-        _lib.port_solve.argtypes = [C.POINTER(_Case), C.POINTER(_Result)]
-        _lib.port_solve.restype = C.c_int
-    return _lib
+def _load(fast: bool = False):
+    if fast not in _libs:
+        L = C.CDLL(build(fast=fast))
+        L.port_solve.argtypes = [C.POINTER(_Case), C.POINTER(_Result)]
+        L.port_solve.restype = C.c_int
+        _libs[fast] = L
+    return _libs[fast]
 
 
-def solve(case, hook_cap: int = 0) -> dict:
+def solve(case, hook_cap: int = 0, fast: bool = False) -> dict:
     """Solves ``case`` with the oracle port. Returns the solution per input
     grid, the V-cycle count, per-cycle finest residuals and (if hook_cap>0)
     the hook log (kind 0 relax, 1 residual, 2 lop; level; grid index; norm)."""
-    lib = _load()
+    lib = _load(fast)
     n = len(case.grids)
     p = case.params
     lev = (C.c_int * n)(*[g.level for g in case.grids])

@@ -83,6 +83,14 @@ void dmhwr3d_(double *u1, double *u2, int *nx1, int *ny1, int *nz1, int *nx2, in
               int *si1, int *sj1, int *sk1, int *si2, int *sj2, int *sk2, double *chr1, double *ex,
               int *do_ex)
 {
+   /* the Fortran masks the stencil legs by chr1 for any nonzero do_ex but
+    * zeroes excised centres only for do_ex = 1 (src/m_util_r8.f:681-715);
+    * the device kernels implement do_ex 0 and 1, so other values are refused
+    * before anything is written */
+   if (*do_ex != 0 && *do_ex != 1) {
+      fprintf(stderr, "dmhwr3d: do_ex = %d is not supported (0 or 1); u2 unchanged\n", *do_ex);
+      return;
+   }
    RESTRICT_BODY("dmhwr3d", pgb_dmhwr3d, pgb_dmhwr3d_ex)
 }
 

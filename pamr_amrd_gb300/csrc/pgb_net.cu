@@ -807,7 +807,10 @@ __global__ void k_out_store(const float *up, double *u, int n, double s_out, pgb
  * spacing h): with A = -lap (symmetric positive definite), the factor that
  * minimises |alpha u - u*|_A is alpha = <u, rho> / <u, lap u>. This kernel
  * accumulates the two sums over the interior points in FP64; k_scale_guess
- * applies alpha (1 when the denominator is zero). */
+ * applies alpha, or -- when the guess is not finite (a NaN or Inf anywhere
+ * makes a sum so), is zero, or its alpha is outside [1/16, 16], which a
+ * trained net's guess never needs -- replaces the guess by u = 0, the plain
+ * solve's initial guess, and counts the rejection in dots[2]. */
 __global__ void k_energy_dots(const double *rho, const double *u, int n, double inv_h2, double *dots)
 {
    __shared__ double sm[2][8];
@@ -835,10 +838,14 @@ __global__ void k_energy_dots(const double *rho, const double *u, int n, double 
    }
 }
 
-__global__ void k_scale_guess(double *u, long nn, const double *dots)
+__global__ void k_scale_guess(double *u, long nn, double *dots)
 {
-   const double alpha = dots[1] != 0.0 ? dots[0] / dots[1] : 1.0;
-   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x) u[q] *= alpha;
+   const double a = dots[0], b = dots[1];
+   const double alpha = b != 0.0 ? a / b : 0.0;
+   const bool ok = isfinite(a) && isfinite(b) && b != 0.0 && isfinite(alpha) && alpha >= 0.0625 && alpha <= 16.0;
+   if (!ok && blockIdx.x == 0 && threadIdx.x == 0) dots[2] += 1.0;
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x)
+      u[q] = ok ? u[q] * alpha : 0.0;
 }
 
 /* MSE over points 1..n-2: loss += sum (up - ut/s_out)^2 / N, gup = dloss/dup */
@@ -1201,7 +1208,7 @@ struct pgb_net {
    bf16 *act[NACT], *grad[NACT];
    float *up, *gup, *r32;
    double *d_loss;
-   double *d_dots;                /* energy-norm scaling sums */
+   double *d_dots;                /* energy-norm scaling sums, and the count of rejected guesses */
    int *d_err;
    long step;
    int bias_free;
@@ -1290,7 +1297,7 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
              cudaMalloc((void **)&net->r32, net->g[0].vtot * 4) == cudaSuccess &&
              cudaMemset(net->r32, 0, net->g[0].vtot * 4) == cudaSuccess &&
              cudaMalloc((void **)&net->d_loss, 8) == cudaSuccess && cudaMalloc((void **)&net->d_err, 4) == cudaSuccess &&
-             cudaMalloc((void **)&net->d_dots, 16) == cudaSuccess;
+             cudaMalloc((void **)&net->d_dots, 24) == cudaSuccess && cudaMemset(net->d_dots, 0, 24) == cudaSuccess;
    for (int l = 0; l < NTC && ok; l++)
       ok = cudaMalloc((void **)&net->img[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess &&
            cudaMalloc((void **)&net->img_adj[l], 27L * TC_CIN[l] * TC_COUT[l] * 2) == cudaSuccess;
@@ -1434,7 +1441,7 @@ extern "C" int pgb_net_rescale(pgb_net *net, const double *rho, double *u, doubl
 {
    cudaStream_t st = (cudaStream_t)stream;
    if (!(h > 0)) return arg_err("pgb_net_rescale: spacing must be positive");
-   if (cudaMemsetAsync(net->d_dots, 0, 16, st) != cudaSuccess) return check_net("net memset");
+   if (cudaMemsetAsync(net->d_dots, 0, 16, st) != cudaSuccess) return check_net("net memset");   /* keeps dots[2] */
    const long nn = (long)net->n * net->n * net->n;
    NETK((k_energy_dots<<<GRID_1D, 256, 0, st>>>(rho, u, net->n, 1.0 / (h * h), net->d_dots)), "net energy dots");
    NETK((k_scale_guess<<<GRID_1D, 256, 0, st>>>(u, nn, net->d_dots)), "net scale guess");
@@ -1546,3 +1553,14 @@ extern "C" int pgb_net_train_step(pgb_net *net, const double *rho, const float *
    if (repack(net, st)) return 11;
    return loss ? read_loss(net, loss, st) : 0;
 }
+
+/* how many guesses pgb_net_rescale has replaced by u = 0 so far */
+extern "C" int pgb_net_rejected_guesses(pgb_net *net, long *count)
+{
+   double v = 0;
+   if (cudaMemcpy(&v, net->d_dots + 2, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return check_net("net rejected count");
+   *count = (long)v;
+   return 0;
+}
+

@@ -30,6 +30,7 @@ def _bind():
     L.pgb_net_params.argtypes = [_vp, C.c_int, C.POINTER(C.c_float), C.c_int]
     L.pgb_net_predict.argtypes = [_vp, _vp, _vp, _vp]
     L.pgb_net_rescale.argtypes = [_vp, _vp, _vp, C.c_double, _vp]
+    L.pgb_net_rejected_guesses.argtypes = [_vp, C.POINTER(C.c_long)]
     L.pgb_net_loss_grad.argtypes = [_vp, _vp, _vp, _dp, _vp]
     L.pgb_net_train_step.argtypes = [_vp, _vp, _vp, C.c_float, _dp, _vp]
     L.pgb_conv3d_geometry.argtypes = [C.c_int] * 3 + [_vp, _vp]
@@ -119,8 +120,14 @@ class Net:
         _check(lib().pgb_net_predict(self.h, rho_ptr, u_ptr, stream))
 
     def rescale(self, rho_ptr: int, u_ptr: int, h: float, stream=None):
-        """energy-norm optimal amplitude of the guess (pgb_net_rescale)"""
+        """energy-norm optimal amplitude of the guess (pgb_net_rescale); a
+        guess that is not finite or needs an absurd amplitude becomes u = 0"""
         _check(lib().pgb_net_rescale(self.h, rho_ptr, u_ptr, h, stream))
+
+    def rejected_guesses(self) -> int:
+        n = C.c_long()
+        _check(lib().pgb_net_rejected_guesses(self.h, C.byref(n)))
+        return n.value
 
     def loss_grad(self, rho_ptr: int, ut_ptr: int, stream=None) -> float:
         loss = C.c_double()
@@ -210,6 +217,60 @@ def make_dataset(n: int, seeds, torch, cycles: int = 12, precision: int = 1):
         torch.cuda.synchronize()
         U[k] = u.float()
         blobs.append(b)
+    s.close()
+    return blobs, U
+
+
+def moving_blobs(seed: int, step: int, dt: float = 0.05):
+    """the poisson3d source of `seed` with its Gaussians drifting: centre
+    c + v t at t = step dt, with seeded velocities v in U(-1, 1)^3 (units of
+    the domain [-10, 10]^3 per unit time) -- the source a time-stepped run
+    hands its elliptic solve at each coarse step"""
+    from . import workloads as W
+    rng = W.SplitMix64(0x5EED0009 + seed)
+    out = []
+    for (a, w, c) in W.poisson3d_blobs(seed):
+        v = (rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-1, 1))
+        t = step * dt
+        out.append((a, w, tuple(c[d] + v[d] * t for d in range(3))))
+    return out
+
+
+def make_sequence_dataset(n: int, runs, steps: int, torch, cycles: int = 12, precision: int = 1):
+    """(rho, u) training pairs the plain multigrid produces along
+    time-stepped runs, as the elliptic solves of a Berger-Oliger evolution
+    (amrd/evolve.c:279-288) would: for each run (seed) and coarse step, the
+    drifting source of moving_blobs is solved by `cycles` V-cycles started
+    from the previous step's solution (AMRD starts each solve from the last
+    one), and the pair is kept; u as FP32 on the device"""
+    import copy
+    from . import workloads as W
+    from .solver import Solver
+    case = copy.deepcopy(W.poisson3d(n, seed=0, rel_tol=0))
+    case.params.precision = precision
+    case.params.tol = 0.0
+    case.params.max_iter = cycles
+    case.params.min_iter = cycles
+    s = Solver(case)
+    runs = list(runs)
+    u = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    blobs, U = [], torch.empty(len(runs) * steps, n ** 3, dtype=torch.float32, device="cuda")
+    st = torch.cuda.ExternalStream(s.stream())
+    torch.cuda.synchronize()
+    k = 0
+    for seed in runs:
+        u.zero_()
+        for step in range(steps):
+            b = moving_blobs(seed, step)
+            with torch.cuda.stream(st):   # ordered before the solver's copy of it
+                rho = rho_on_device(n, b, torch)
+            s.set_inputs_device([u.data_ptr()], [rho.data_ptr()])
+            s.solve()
+            _check(lib().pgb_get_grid_device(s.h, 0, u.data_ptr()))
+            torch.cuda.synchronize()
+            U[k] = u.float()
+            blobs.append(b)
+            k += 1
     s.close()
     return blobs, U
 

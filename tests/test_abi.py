@@ -38,3 +38,21 @@ def test_fortran_abi_dropin_exports_m_util_r8_symbols():
     L = ctypes.CDLL(build.LIB_F77)
     for name in ("dmcopy3d_", "dmhwr3d_", "dmfwr3d_", "dminterp3d_", "dmdiss3d_", "linbnd3d_"):
         assert hasattr(L, name), name
+
+
+def test_fortran_abi_half_weighting_refuses_unsupported_do_ex():
+    """dmhwr3d masks its stencil legs for any nonzero do_ex but zeroes
+    excised centres only for do_ex = 1 (src/m_util_r8.f:681-715); the
+    drop-in implements 0 and 1 and leaves u2 unchanged for other values,
+    before any device work (so this runs without a GPU)"""
+    import numpy as np
+    build.build()
+    L = ctypes.CDLL(build.LIB_F77)
+    u1 = np.arange(125, dtype=np.float64)
+    u2 = np.full(27, -3.5)
+    chr1 = np.zeros(125)
+    ip = lambda v: ctypes.byref(ctypes.c_int(v))  # noqa: E731
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    args = [dp(u1), dp(u2)] + [ip(v) for v in (5, 5, 5, 3, 3, 3, 1, 1, 1, 1, 1, 1, 3, 3, 3, 2, 2, 2, 1, 1, 1)]
+    L.dmhwr3d_(*args, dp(chr1), ctypes.byref(ctypes.c_double(1.0)), ip(-1))
+    assert np.all(u2 == -3.5)

@@ -46,8 +46,10 @@ def test_mixed_matches_reference_fixture(path):
 @pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=3),
                                   lambda: W.poisson2d_uneven(seed=4, n=129, levels=5, min_boxes=8,
                                                              max_boxes=16),
-                                  lambda: W.lapse2d_bo(65, seed=5, levels=4, step=120)],
-                         ids=["c3d65", "uneven129", "lapse65"])
+                                  lambda: W.lapse2d_bo(65, seed=5, levels=4, step=120),
+                                  lambda: W.poisson2d_uneven(seed=0),
+                                  lambda: W.poisson2d_uneven(seed=4)],
+                         ids=["c3d65", "uneven129", "lapse65", "config3_s0", "config3_s4"])
 def test_mixed_matches_oracle_port(make):
     case = make()
     p = portrun.solve(case)

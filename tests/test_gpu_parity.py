@@ -61,11 +61,15 @@ LARGER = [
     lambda: W.poisson2d_uneven(seed=0, n=129, levels=5, min_boxes=8, max_boxes=24),
     lambda: W.lapse2d_bo(65, seed=2, levels=4),
     lambda: W.lapse2d_bo(65, seed=3, levels=4, step=300),
+    # the batched uneven hierarchy at its stated size: 129^2 base + 4 levels
+    # of 8-64 boxes each (116-149 boxes)
+    lambda: W.poisson2d_uneven(seed=0),
+    lambda: W.poisson2d_uneven(seed=3),
 ]
 
 
 @pytest.mark.parametrize("make", LARGER, ids=["p2d129", "p2d257", "c3d33", "c3d65", "uneven129",
-                                              "lapse65", "lapse65_t300"])
+                                              "lapse65", "lapse65_t300", "config3_s0", "config3_s3"])
 def test_fp64_matches_oracle_port(make):
     case = make()
     r = _solve(case)
