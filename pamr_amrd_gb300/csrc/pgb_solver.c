@@ -988,11 +988,23 @@ static int smooth(pgb_solver *s, int L, int nsweep, int slot)
 }
 
 /* fills the coarsest-grid loop's arguments for level L */
+/* the mixed form smooths MG level 1 in FP64 exactly as the FP64 form does
+ * (pre- and post-smoothing, then the reference's coarsest-grid loop) when
+ * it holds several coarsest grids: the islands a refined level's grids
+ * coarsen to, often thin strips, for which the FP32 SOR defect correction
+ * of one grid is no substitute */
+static int fp64_level1(const pgb_solver *s)
+{
+   int b, n = 0;
+   for (b = 0; b < s->h.lev[1].nbox; b++) n += s->h.boxes[s->h.lev[1].box[b]].coarsest != 0;
+   return s->h.prm.precision == PGB_MIXED && n > 1;
+}
+
 static void coarsest_args(pgb_solver *s, int L, pgb_coarsest_args *a)
 {
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
-   int b, mixed = p->precision == PGB_MIXED, nmax = 0, d;
+   int b, mixed = p->precision == PGB_MIXED && !(L == 1 && fp64_level1(s)), nmax = 0, d;
    memset(a, 0, sizeof(*a));
    a->start_iter = mixed ? 0 : p->pst_swp;
    a->max_citer = p->max_citer;
@@ -1147,6 +1159,7 @@ static int vcycle_mixed(pgb_solver *s)
        * in, where the post-smoothing block starts, and that block zeroes
        * PGB_W32_E again (which the captured graph relies on) */
       s->eslot[L] = PGB_W32_E;
+      if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pre_swp, N_RELAX_DN)) return 11;
       if (L > 1 && p->pre_swp > 0) {
          int slot = PGB_W32_E;
          if (sweeps32(s, L, p->pre_swp, &slot)) return 11;
@@ -1169,6 +1182,7 @@ static int vcycle_mixed(pgb_solver *s)
          KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       }
+      if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pst_swp, N_RELAX_UP)) return 11;
       /* the coarsest-grid loop (amrd/mg.c:172-190) wherever coarsest boxes
        * are: on MG level 1, and above it in hierarchies whose base has
        * several islands that stop coarsening at different levels (a
@@ -1180,9 +1194,9 @@ static int vcycle_mixed(pgb_solver *s)
          /* the FP32 SOR defect correction is made for one coarsest grid;
           * several (islands of a refined level's grids, often thin strips)
           * take the FP64 Gauss-Seidel loop of the reference */
-         rc = a.ncoarse == 1 ? pgb_k_coarsest_mixed(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a,
-                                                    s->d_trace, s->stream)
-                             : 1;
+         rc = a.ncoarse == 1 && !(L == 1 && fp64_level1(s))
+                 ? pgb_k_coarsest_mixed(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream)
+                 : 1;
          if (rc < 0) return fail(11, "%s", pgb_dev_error32());
          if (rc > 0)   /* too large for one CTA's shared memory: the FP64 loop */
             KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
