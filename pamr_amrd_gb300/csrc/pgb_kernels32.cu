@@ -530,25 +530,40 @@ __global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlev
  * staged by the Tensor Memory Accelerator. A CTA owns an output column of
  * TXO x TYO points (x start a multiple of 4, so that every TMA load starts
  * on 16 bytes: the FP32 rows are padded to 16-byte pitches) and marches
- * through MTZ planes of it. Each plane of the old correction (slot src,
- * TXO+8 x TYO+4 points around the column), of D and of C (TXO+8 x TYO+2)
- * arrives by one cp.async.bulk.tensor 3-D tile load per array into a ring
- * of R plane slots, completion counted on the slot's mbarrier; loads run
- * R-3 planes ahead of use and fill out-of-box coordinates with zeros.
- * Step k: the first colour of plane k on the column grown by one point
- * (from the old second-colour values around it), then the second colour
- * of plane k-1 on the column (from the new first-colour values of planes
- * k-2 .. k), then plane k-1 is final and stored to slot dst (8-byte
- * stores, one point pair per thread). Thread (tx, ty) owns the point pair
- * x = i0 - 2 + 2 tx, +1 of row y = j0 - 1 + ty: one point of each colour,
- * its x neighbours in the pair and the next thread's (shuffles). As in the
- * other fused kernels no CTA writes the slot the others read, the grown
- * first colour is recomputed identically by the CTAs that share it, and
- * every update is gs32, so the result equals the in-place colour passes
- * bit for bit. Every mbarrier wait is bounded (globaltimer, ~1 s); on
- * timeout the CTA sets *err, lets the loads it issued land and returns.
- * Boxes must have their whole interior relaxed (PGB_BOX_BDY_INTERIOR). */
-#define MT_R 6           /* ring slots (planes) */
+ * through MTZ planes of it (MTZ even). Each plane of the old correction
+ * (slot src, TXO+8 x TYO+4 points around the column), of D and of C
+ * (TXO+8 x TYO+2) arrives by one cp.async.bulk.tensor 3-D tile load per
+ * array into a ring of R = 8 plane slots, completion counted on the slot's
+ * mbarrier; loads run R-2 planes ahead of use and fill out-of-box
+ * coordinates with zeros.
+ *
+ * Each thread owns a point pair (x, x+1) of one row y of the column grown by
+ * one point, with x + y even, so that at plane k the first colour (num.f:220
+ * parity, 0-based: x + y + k odd) is the pair's first member for odd k and
+ * its second for even k, for every thread alike. At plane step k a thread
+ * updates its member c of the first colour at (c, k), from the old
+ * second-colour values around it, then the second colour at (c, k-1),
+ * whose z neighbours are the new first-colour values at (c, k-2) and (c, k)
+ * it computed two steps ago and just now, whose x neighbour inside the pair
+ * is the other member's new value at k-1 (one step ago), and whose old value
+ * is the z neighbour the first-colour update read. The old values at
+ * (other member, k) and (c, k-1) are the ones the previous step loaded as
+ * its z and x neighbours. Only first-colour results go to shared memory
+ * (the neighbours read them one step later); plane k-1 is final after the
+ * second-colour update and is stored from registers. Within a step no
+ * thread reads what another writes, so one barrier per step suffices; it
+ * also frees plane k-1's slot for the load of plane k-1+R. The loop is
+ * unrolled over the ring, so that slots and colours are constants and every
+ * shared-memory access is one register plus an immediate; the two
+ * half-warps of a warp hold neighbouring rows (whose pairs start one point
+ * apart), which keeps the stride-2 accesses free of bank conflicts.
+ *
+ * No CTA writes the slot the others read and every update is gs32 on the
+ * same operands, so the result equals the in-place colour passes bit for
+ * bit. Every mbarrier wait is bounded (globaltimer, ~1 s); on timeout the
+ * CTA sets *err, lets the loads it issued land and returns. Boxes must have
+ * their whole interior relaxed (PGB_BOX_BDY_INTERIOR). */
+#define MT_R 8           /* ring slots (planes); the step loop is unrolled over them */
 #define MT_TYO 14        /* output rows per column */
 
 __device__ __forceinline__ uint32_t mt_saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -571,8 +586,11 @@ __device__ __forceinline__ bool mt_try(uint64_t *bar, uint32_t phase)
    return ok != 0;
 }
 
+/* bounded wait for the phase of parity `phase`; the clock is read only when
+ * the first try fails */
 __device__ __forceinline__ bool mt_wait(uint64_t *bar, uint32_t phase)
 {
+   if (mt_try(bar, phase)) return true;
    const uint64_t t0 = mt_ns();
    while (!mt_try(bar, phase))
       if (mt_ns() - t0 > 1000000000ull) return false;
@@ -590,135 +608,133 @@ __device__ __forceinline__ void mt_load(float *dst, const CUtensorMap *map, int 
 
 template <int TXO>
 struct mt_shape {
-   static constexpr int PX = (TXO + 4) / 2, PY = MT_TYO + 2, NTH = PX * PY;
+   static constexpr int PX = (TXO + 4) / 2, PY = MT_TYO + 2, NTH = PX * PY, HX = PX / 16;
    static constexpr int EW = TXO + 8, EH = MT_TYO + 4, DH = MT_TYO + 2;
    static constexpr int ESZ = (EW * EH + 31) / 32 * 32, DSZ = (EW * DH + 31) / 32 * 32;
    static constexpr int SLOT = ESZ + 2 * DSZ;                 /* floats per ring slot (128-byte multiple) */
    static constexpr unsigned EBYTES = 4u * EW * EH, DBYTES = 4u * EW * DH;
    static constexpr size_t SMEM = 4ul * MT_R * SLOT + 8ul * MT_R;
+   static constexpr int MINB = TXO >= 60 ? 2 : 3;             /* CTAs per SM the shared memory allows */
+   static_assert(PX % 16 == 0 && PY % 2 == 0, "half-warps hold 16 pairs of one row");
 };
 
 template <int TXO>
-__global__ void __launch_bounds__(mt_shape<TXO>::NTH) k_sweep32t(const pgb_dbox *boxes, pgb_dlevel lv,
-                                                                 const CUtensorMap *maps, int src, int dst,
-                                                                 int *err)
+__global__ void __launch_bounds__(mt_shape<TXO>::NTH, mt_shape<TXO>::MINB)
+   k_sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const CUtensorMap *maps, int src, int dst, int *err)
 {
    typedef mt_shape<TXO> S;
+   constexpr int EW = S::EW, SL = S::SLOT, DO = S::ESZ - EW, CO = S::ESZ + S::DSZ - EW;   /* D, C of a point: +DO, +CO */
    extern __shared__ __align__(128) float sm[];
-   uint64_t *bar = (uint64_t *)(sm + MT_R * S::SLOT);
-   __shared__ int s_abort;
+   uint64_t *bar = (uint64_t *)(sm + MT_R * SL);
    const pgb_tile tl = lv.mtiles[blockIdx.x];
    const pgb_dbox *bp = boxes + tl.box;
    const int n0 = bp->n[0], n1 = bp->n[1], n2 = bp->n[2];
-   const long wy = bp->wy, wz = bp->wz;
-   float *__restrict__ eo = bp->w32[dst];
    const float ix = bp->fidx2[0], iy = bp->fidx2[1], iz = bp->fidx2[2], j0 = bp->fj0;
    const CUtensorMap *me = maps + 8 * tl.box + (src == W_E2 ? 1 : 0), *md = maps + 8 * tl.box + 2,
                      *mc = maps + 8 * tl.box + 3;
    const int i0 = tl.i0, jb = tl.j0, kb = tl.k0, ke = min(tl.k0 + lv.mtz, n2);   /* planes [kb, ke) written */
-   const int tx = threadIdx.x, ty = threadIdx.y, t = tx + S::PX * ty;
-   const int lane = t & 31;
-   /* the thread's pair in the staged E plane: columns ex, ex + 1 of row ey */
-   const int ex = 2 + 2 * tx, ey = 1 + ty;
-   const int gx = i0 - 4 + ex, gy = jb - 2 + ey;   /* global x, y of the pair's first point */
-   const bool row_red = ey >= 1 && ey <= S::DH, row_blk = ey >= 2 && ey <= S::DH - 1;
+   if (kb & 1) {   /* the unrolled colours assume an even first plane */
+      if (threadIdx.x == 0) *err = 2;
+      return;
+   }
+   const int t = threadIdx.x, w = t >> 5;
+   const int tx = (w % S::HX) * 16 + (t & 15), ty = 2 * (w / S::HX) + ((t >> 4) & 1);
+   const int gy = jb - 1 + ty, xs = i0 - 2 + 2 * tx + (gy & 1);   /* the pair: (xs, xs+1) of row gy, xs + gy even */
+   float *const s0 = sm + (1 + ty) * EW + 2 + 2 * tx + (gy & 1);  /* the first member in slot 0's E plane */
    const bool yin = gy >= 1 && gy <= n1 - 2;
+   const bool xin0 = yin && xs >= 1 && xs <= n0 - 2, xin1 = yin && xs >= 0 && xs <= n0 - 3;
+   /* first colour on x in [i0-1, i0+TXO]; second colour and the store on the output column */
+   const bool rr0 = xs >= i0 - 1 && xs <= i0 + TXO, rr1 = xs + 1 >= i0 - 1 && xs + 1 <= i0 + TXO;
+   const bool orow = ty >= 1 && ty <= S::PY - 2 && gy < n1;
+   const bool out0 = orow && xs >= i0 && xs <= i0 + TXO - 1 && xs < n0;
+   const bool out1 = orow && xs + 1 >= i0 && xs + 1 <= i0 + TXO - 1 && xs + 1 < n0;
+   float *gp = bp->w32[dst] + (out0 || out1 ? xs + bp->wy * gy : 0);
+   const long wz = bp->wz;
    if (t == 0) {
-      s_abort = 0;
       for (int r = 0; r < MT_R; r++)
          asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mt_saddr(bar + r)), "r"(1) : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
    }
    __syncthreads();
-   /* plane m lives in slot (m - kb + 2) % R; its phase flips with each reuse */
+   /* plane m lives in slot (m - m0) % R; its phase parity flips with each reuse */
    const int m0 = kb - 2, mlast = min(ke + 1, n2 - 1);
-   auto slot_of = [&](int m) { return (m - m0) % MT_R; };
    int last_issued = m0 - 1;   /* thread 0: the newest plane whose slot a load or arrival was issued for */
    auto issue = [&](int m) {   /* thread 0 */
-      uint64_t *b = bar + slot_of(m);
+      uint64_t *b = bar + ((m - m0) & (MT_R - 1));
       last_issued = m;
       if (m < 0 || m > mlast) {   /* nothing to load: complete the slot's phase anyway */
          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mt_saddr(b)) : "memory");
          return;
       }
-      float *sl = sm + slot_of(m) * S::SLOT;
+      float *sl = sm + ((m - m0) & (MT_R - 1)) * SL;
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mt_saddr(b)),
                    "r"(S::EBYTES + 2 * S::DBYTES) : "memory");
       mt_load(sl, me, i0 - 4, jb - 2, m, b);
       mt_load(sl + S::ESZ, md, i0 - 4, jb - 1, m, b);
       mt_load(sl + S::ESZ + S::DSZ, mc, i0 - 4, jb - 1, m, b);
    };
-   int waited = m0 - 1;   /* planes up to here have landed */
-   auto await = [&](int m) -> bool {   /* all threads; plane m (and earlier) usable after this */
-      if (m > mlast) m = mlast;
-      if (m <= waited) return true;
-      bool ok = true;
-      for (int q = waited + 1; q <= m && ok; q++)   /* every thread observes the completion itself */
-         if (q >= 0 && !mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1)) ok = false;
-      if (!ok) {
-         s_abort = 1;
-         *err = 1;
-      }
-      __syncthreads();
-      if (s_abort) return false;
-      waited = m;
-      return true;
-   };
-   auto bail = [&]() {   /* lets every load still in flight land (bounded), then returns */
-      if (t == 0)
-         for (int q = max(waited + 1, 0); q <= min(mlast, last_issued); q++)
-            mt_wait(bar + slot_of(q), ((q - m0) / MT_R) & 1);
-      __syncthreads();
-   };
    if (t == 0)
       for (int m = m0; m < m0 + MT_R; m++) issue(m);
+   /* planes kb-2 and kb-1 (slots 0 and 1) before the first step */
+   bool ok = true;
+   int waited = m0 - 1;   /* planes up to here have landed (each thread observes it itself) */
+   for (int q = m0; q <= min(kb - 1, mlast); q++) {
+      if (q >= 0 && !mt_wait(bar + (q - m0), 0)) ok = false;
+      waited = q;
+   }
+   /* old values carried between steps: (other member, k) and (c, k-1) */
+   float zprev = s0[SL + 1], aprev = s0[0];
+   float rp1 = 0.f, rp2 = 0.f;   /* new first-colour values: (other member, k-1), (c, k-2) */
+   gp += wz * (long)(kb - 3);   /* advanced to plane k-1 at each step */
 
-   /* one colour at plane k: the pair member with (x + y + k) odd (first
-    * colour, num.f:220 parity in 0-based indices) or even (second) */
-   auto relax = [&](int k, int second) {
-      float *pe = sm + slot_of(k) * S::SLOT;
-      const float *pm = sm + slot_of(k - 1) * S::SLOT, *pp = sm + slot_of(k + 1) * S::SLOT;
-      const float *pd = pe + S::ESZ, *pc = pe + S::ESZ + S::DSZ;
-      const int o = ey * S::EW + ex;
-      const float2 v = *reinterpret_cast<const float2 *>(pe + o);
-      const float left = __shfl_up_sync(0xffffffffu, v.y, 1), right = __shfl_down_sync(0xffffffffu, v.x, 1);
-      const int odd = (gx + gy + k) & 1;               /* gx even: the first point's colour */
-      const int mem = second ? odd : odd ^ 1;          /* 0: the first point of the pair, 1: the second */
-      const int xl = ex + mem, gxx = gx + mem;
-      const bool region = second ? (row_blk && xl >= 4 && xl <= TXO + 3) : (row_red && xl >= 3 && xl <= TXO + 4);
-      if (!region || k < 1 || k > n2 - 2 || !yin || gxx < 1 || gxx > n0 - 2) return;
-      const int c = o + mem;
-      const float ec = mem ? v.y : v.x, xm = mem ? v.x : left, xp = mem ? right : v.y;
-      const int od = c - S::EW;   /* D and C planes start one row later */
-      pe[c] = gs32(ec, xm, xp, pe[c - S::EW], pe[c + S::EW], pm[c], pp[c], pc[od], pd[od], ix, iy, iz, j0, true);
-      (void)lane;
-   };
-
-   for (int k = kb - 1; k <= ke; k++) {
-      if (!await(k + 1)) {
-         bail();
-         return;
-      }
-      relax(k, 0);
-      __syncthreads();
-      if (k - 1 >= kb) {
-         relax(k - 1, 1);
-         __syncthreads();
-         /* plane k-1 is final: store the column (in-box points) */
-         const int kw = k - 1;
-         if (row_blk && tx >= 1 && tx <= TXO / 2 && gy < n1 && gx < n0) {
-            const float *pe = sm + slot_of(kw) * S::SLOT;
-            const float2 v = *reinterpret_cast<const float2 *>(pe + ey * S::EW + ex);
-            float *g = eo + gx + wy * gy + wz * kw;
-            if (gx + 1 < n0) *reinterpret_cast<float2 *>(g) = v;
-            else g[0] = v.x;
+   /* step s: plane k = kb - 1 + s, slot (s + 1) % R; colour member mem = s % 2 */
+   for (int sb = 0;; sb += MT_R) {
+      const uint32_t ph = (sb / MT_R) & 1;
+#pragma unroll
+      for (int u = 0; u < MT_R; u++) {
+         const int s = sb + u, k = kb - 1 + s;
+         if (k > ke) return;
+         const int mem = u & 1;
+         const int jk = ((u + 1) & (MT_R - 1)) * SL, jm = (u & (MT_R - 1)) * SL, jp = ((u + 2) & (MT_R - 1)) * SL;
+         if (k + 1 <= mlast) {   /* plane k+1 in slot (s + 2) % R */
+            if (!mt_wait(bar + ((u + 2) & (MT_R - 1)), ph ^ (u + 2 >= MT_R ? 1u : 0u))) ok = false;
+            waited = k + 1;
          }
-      }
-      /* plane k-2's slot is free once every thread is past this step */
-      __syncthreads();
-      if (t == 0 && k - 2 >= m0) {
-         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-         issue(k - 2 + MT_R);
+         float *pc = s0 + mem;   /* the member c of the first colour at plane k */
+         /* first colour at (c, k) */
+         const float ec = pc[jk], ea = zprev, ezm = aprev;
+         const float eb = mem ? pc[jk + 1] : pc[jk - 1];
+         const float zp = pc[jp];
+         float rk = gs32(ec, mem ? ea : eb, mem ? eb : ea, pc[jk - EW], pc[jk + EW], ezm, zp, pc[jk + CO],
+                         pc[jk + DO], ix, iy, iz, j0, true);
+         if (!((mem ? xin1 : xin0) && k >= 1 && k <= n2 - 2)) rk = ec;
+         if (mem ? rr1 : rr0) pc[jk] = rk;
+         /* second colour at (c, k-1); then plane k-1 of the pair is final */
+         gp += wz;
+         if (s >= 2) {
+            const float fb = mem ? pc[jm + 1] : pc[jm - 1];
+            float bk = gs32(ezm, mem ? rp1 : fb, mem ? fb : rp1, pc[jm - EW], pc[jm + EW], rp2, rk, pc[jm + CO],
+                            pc[jm + DO], ix, iy, iz, j0, true);
+            if (!((mem ? xin1 : xin0) && k >= 2 && k <= n2 - 1)) bk = ezm;
+            if (out0) gp[0] = mem ? rp1 : bk;
+            if (out1) gp[1] = mem ? bk : rp1;
+         }
+         zprev = zp;
+         aprev = ea;
+         rp2 = rp1;
+         rp1 = rk;
+         if (!ok) *err = 1;
+         if (__syncthreads_or(!ok)) {   /* a load never landed: let the issued ones land, return */
+            if (t == 0)
+               for (int q = max(waited + 1, 0); q <= min(mlast, last_issued); q++)
+                  mt_wait(bar + ((q - m0) & (MT_R - 1)), ((q - m0) / MT_R) & 1);
+            return;
+         }
+         /* plane k-1's slot is free: every thread is past step k */
+         if (t == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k - 1 + MT_R);
+         }
       }
    }
 }
@@ -805,10 +821,10 @@ static int sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const void *maps, int 
    /* the maps of width 60 sit at 8 i + 0..3, of width 28 at 8 i + 4..7 */
    const CUtensorMap *m = (const CUtensorMap *)maps;
    if (lv.mtx == 60)
-      k_sweep32t<60><<<lv.nmtiles, dim3(mt_shape<60>::PX, mt_shape<60>::PY), mt_shape<60>::SMEM, st>>>(
+      k_sweep32t<60><<<lv.nmtiles, mt_shape<60>::NTH, mt_shape<60>::SMEM, st>>>(
          boxes, lv, m, src, dst, err);
    else
-      k_sweep32t<28><<<lv.nmtiles, dim3(mt_shape<28>::PX, mt_shape<28>::PY), mt_shape<28>::SMEM, st>>>(
+      k_sweep32t<28><<<lv.nmtiles, mt_shape<28>::NTH, mt_shape<28>::SMEM, st>>>(
          boxes, lv, m + 4, src, dst, err);
    return check32("sweep32t");
 }
