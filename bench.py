@@ -251,7 +251,9 @@ def sweep_beyond_l2(S, torch, np, peak, n: int = 385):
     sv.set_inputs_device([z.data_ptr()], [z.data_ptr()])
     sv.prepare()
     L = sv.num_levels()
+    torch.cuda.nvtx.range_push("time_relax_beyond_l2")
     ms, by = sv.time_relax(L, reps=10)
+    torch.cuda.nvtx.range_pop()
     tz, fuse = sv.level_tuning(L)
     sv.close()
     gbs = by / (ms / 1e3) / 1e9
