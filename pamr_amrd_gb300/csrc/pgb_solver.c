@@ -59,7 +59,7 @@ struct pgb_solver {
    void *d_tmaps;           /* mixed form, 3-D: tensor maps of the TMA-staged sweep (0: unavailable) */
    int *d_err;              /* set by a device wait that timed out */
    int mtx[PGB_MAXLEV + 1]; /* output width of the TMA sweep's columns per level (60 or 28) */
-   int mtz[PGB_MAXLEV + 1]; /* planes per column of the TMA sweep per level (16, 32 or 64; even) */
+   int mtz[PGB_MAXLEV + 1]; /* planes per column of the TMA sweep per level (4 to 64; even) */
    int *d_it;               /* cycles run by the device loop */
    cudaEvent_t ev0, ev1;
    cudaStream_t side;       /* second stream for independent kernels of a cycle */
@@ -771,11 +771,11 @@ static int sync_field(pgb_solver *s, const pgb_plan *p, int field)
  * sweep per launch or, on levels without a sync between sweeps, two, the
  * one-pass z-marching sweep and (3-D, boxes relaxed on their whole
  * interior) the TMA-staged one-pass sweep with columns 60 or 28 wide and
- * 16, 32 or 64 planes deep, and keeps the fastest. No choice changes a
+ * 4 to 64 planes deep, and keeps the fastest. No choice changes a
  * computed value (the sweeps are the same Gauss-Seidel sweeps; only the
  * norm's summation order follows the tiles). PGB_AUTOTUNE=0 keeps the
  * defaults; PGB_SWEEP_FUSE=0..5 forces one sweep kernel on every level
- * (PGB_SWEEP_MTZ=16/32/64 the TMA columns' depth with 4 or 5). */
+ * (PGB_SWEEP_MTZ=4/8/16/32/64 the TMA columns' depth with 4 or 5). */
 static int autotune(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
@@ -794,7 +794,10 @@ static int autotune(pgb_solver *s)
          if (f == 4 || f == 5) {
             const char *mz = getenv("PGB_SWEEP_MTZ");
             s->mtx[L] = f == 4 ? 60 : 28;
-            s->mtz[L] = mz && (!strcmp(mz, "16") || !strcmp(mz, "32") || !strcmp(mz, "64")) ? atoi(mz) : 32;
+            s->mtz[L] = mz && (!strcmp(mz, "4") || !strcmp(mz, "8") || !strcmp(mz, "16") || !strcmp(mz, "32") ||
+                               !strcmp(mz, "64"))
+                           ? atoi(mz)
+                           : 32;
             if (level_tables(s, L, s->lv[L].tz)) return 10;
          }
       }
@@ -804,7 +807,7 @@ static int autotune(pgb_solver *s)
    if ((env && !strcmp(env, "0")) || nsw < 1) return 0;
    for (L = 2; L <= h->nlev; L++) {
       static const int tzs[4] = {8, 4, 2, 1};
-      static const int mzs[3] = {16, 32, 64};
+      static const int mzs[5] = {4, 8, 16, 32, 64};
       int ntz = h->dim == 3 ? 4 : 1, a, f, best_tz = s->lv[L].tz, best_f = s->fuse[L], best_mtx = 60, best_mtz = 32;
       int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
       const int tma = level_tma_ok(s, L);
@@ -815,14 +818,14 @@ static int autotune(pgb_solver *s)
             changed = 1;
          }
          /* candidates: f < 4 once each; the TMA-staged sweep (f 4, 5: columns
-          * 60 or 28 wide) with columns of 16, 32 and 64 planes */
-         for (int c = 0; c <= (h->dim == 3 ? 9 : can_fuse ? 2 : 1); c++) {
-            f = c < 4 ? c : 4 + (c - 4) / 3;
+          * 60 or 28 wide) with columns of 4 to 64 planes */
+         for (int c = 0; c <= (h->dim == 3 ? 13 : can_fuse ? 2 : 1); c++) {
+            f = c < 4 ? c : 4 + (c - 4) / 5;
             if (f == 2 && !can_fuse) continue;
             if (f >= 4) {
                if (!tma) continue;
                s->mtx[L] = f == 4 ? 60 : 28;
-               s->mtz[L] = mzs[(c - 4) % 3];
+               s->mtz[L] = mzs[(c - 4) % 5];
                if (level_tables(s, L, tzs[a])) return 10;
                changed = 1;
             }
