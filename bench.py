@@ -220,15 +220,15 @@ def measured_peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
-    """dram bytes per FP32 sweep (two colour passes) of the 129^3 level from
-    the committed ncu summary (profiles/k_relax32_129cube_traffic.txt:
-    'bytes_per_sweep=<n>'), if any"""
-    p = os.path.join(ROOT, "profiles", "k_relax32_129cube_traffic.txt")
+def ncu_traffic(summary: str):
+    """DRAM bytes (read + write) per launch of a kernel, from a committed ncu
+    summary under profiles/ (its line 'dram_bytes_per_launch: <n>'), or
+    None where there is none"""
+    p = os.path.join(ROOT, "profiles", summary)
     try:
         for line in open(p):
-            if line.startswith("bytes_per_sweep="):
-                return float(line.split("=", 1)[1])
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
@@ -751,8 +751,8 @@ def main():
     achieved = bytes_sweep / (ms_sweep / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": ncu_traffic(), "peak_source": peak_kind,
-            "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level)",
+            "frac": achieved / peak, "traffic": ncu_traffic("k_sweep32t_129cube_level.md"), "peak_source": peak_kind,
+            "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level; k_sweep32t, TMA-staged one pass)",
             "tuned": dict(zip(("tile_planes", "sweeps_per_launch"), smx.level_tuning(big))),
             "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep,
             "fp64_sweep": {"kernel": "k_relax (FP64 Newton-GS sweep, 129^3 level)",
@@ -760,6 +760,7 @@ def main():
                            "achieved_gbs": bytes64_sweep / (ms64_sweep / 1e3) / 1e9}}
 
     roof["beyond_l2"] = sweep_beyond_l2(S, torch, np, peak)
+    roof["beyond_l2"]["traffic"] = ncu_traffic("k_sweep32t_385cube.md")
 
     # whole-solve roofline: algorithmic bytes of the cycles each form ran
     # (FP32 sweeps count 16 B per point, FP64 ones 32) over the timed solve

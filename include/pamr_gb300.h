@@ -210,6 +210,19 @@ int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *d
  * transfer lists and dminterp3d arithmetic as the reference, bit-exact. */
 int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order);
 
+/* Regrid: replaces the data transfer of PAMR_compose_hierarchy onto a new
+ * hierarchy (init_new_cgh, src/gh.c:934-1045, called at src/pamr.c:311).
+ * dst is a solver created on the hierarchy after the regrid, src the solver
+ * of the hierarchy it replaces (same dimension and source count). For every
+ * AMR level L of dst, coarse to fine: if L >= min_level (the first level the
+ * reference recomposes), u and the sources are interpolated (order 2 or 4,
+ * the variables' regrid_transfer order) from src's level L-1 over dst's
+ * whole level L; then on every level they are copied from src's grids of
+ * level L where they overlap dst's. Same transfer lists and dminterp3d /
+ * dmcopy3d arithmetic as the reference, bit-exact. Points of dst that
+ * neither transfer reaches keep their values. Both solvers stay usable. */
+int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level);
+
 /* Checkpoint and restart of the device hierarchy's elliptic data (no
  * counterpart format in the reference, whose checkpoints are SDF files of
  * every grid function written through bbhutil, src/pamr.c:1908-1978,

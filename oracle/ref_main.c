@@ -18,7 +18,11 @@
  *   2. fills u and the source on time level 1,
  *   3. calls solve_elliptics(1,1,0) (amrd/mg.c:20), or with interp:lc:width
  *      one PAMR_interp (width 0) or PAMR_AMR_bdy_interp (width > 0) of u
- *      from AMR level lc to lc+1 instead,
+ *      from AMR level lc to lc+1 instead, or with regrid:min_lev:new.bin a
+ *      second PAMR_compose_hierarchy (src/pamr.c:257) over levels min_lev..
+ *      of the grids of new.bin, whose init_new_cgh (src/gh.c:934) moves u
+ *      and the sources (regrid_transfer order from the parameter file) onto
+ *      the new grids, which are then written out (tag 9-11),
  * while the application hooks (pattern of examples/nbs/nbs.c:301-351) log
  * every relax/residual norm, the MG hierarchy, the cmask arrays, and (with
  * log_ops) every m_util_r8 call with its index arguments.
@@ -341,12 +345,19 @@ int main(int argc, char **argv)
    int i, num, *lev;
    double *bbox;
    int gu_amr, gs_amr[4], k;
-   int amr_lc = 0, amr_width = -1;
+   int amr_lc = 0, amr_width = -1, regrid_min = 0;
+   char regrid_case[1024] = "";
    if (argc < 4) {
-      fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops [interp:lc:width]]\n", argv[0]);
+      fprintf(stderr, "usage: %s pfile case.bin out.bin [log_ops [interp:lc:width | regrid:min_lev:new.bin]]\n",
+              argv[0]);
       return 2;
    }
-   if (argc > 5 && sscanf(argv[5], "interp:%d:%d", &amr_lc, &amr_width) != 2) {
+   if (argc > 5 && !strncmp(argv[5], "regrid:", 7)) {
+      if (sscanf(argv[5], "regrid:%d:%1000s", &regrid_min, regrid_case) != 2 || regrid_min < 1) {
+         fprintf(stderr, "ref_mg: bad regrid mode %s\n", argv[5]);
+         return 2;
+      }
+   } else if (argc > 5 && sscanf(argv[5], "interp:%d:%d", &amr_lc, &amr_width) != 2) {
       fprintf(stderr, "ref_mg: bad interpolation mode %s\n", argv[5]);
       return 2;
    }
@@ -400,6 +411,48 @@ int main(int argc, char **argv)
    amr_data(0, gu_amr, gs_amr);
 
    mur8_log_enabled = (argc > 4 && atoi(argv[4]));
+   if (regrid_min > 0) {
+      /* the regrid: the new grids of levels >= regrid_min, composed over the
+       * current hierarchy (the levels below stay) */
+      int n2 = 0, nl2 = 1, j;
+      read_case(regrid_case);   /* the new grids (their data is not used) */
+      lev = (int *)realloc(lev, sizeof(int) * (size_t)c_ngrids);
+      bbox = (double *)realloc(bbox, sizeof(double) * 6 * (size_t)c_ngrids);
+      for (i = 0; i < c_ngrids; i++) {
+         if (c_grids[i].lev > nl2) nl2 = c_grids[i].lev;
+         if (c_grids[i].lev >= regrid_min) {
+            lev[n2] = c_grids[i].lev;
+            memcpy(&bbox[2 * c_dim * n2], c_grids[i].bbox, sizeof(double) * 2 * (size_t)c_dim);
+            n2++;
+         }
+      }
+      if (!PAMR_compose_hierarchy(regrid_min, nl2, n2, lev, bbox, 0.0)) {
+         fprintf(stderr, "ref_mg: regrid PAMR_compose_hierarchy failed\n");
+         return 3;
+      }
+      fout = fopen(argv[3], "wb");
+      if (!fout) return 4;
+      for (j = 1; j <= PAMR_get_max_lev(PAMR_AMRH); j++) {
+         int valid = PAMR_init_s_iter(j, PAMR_AMRH, 0);
+         while (valid) {
+            int rank, dim, gw[6], ngfs, shape[3] = {1, 1, 1};
+            double t, *x[3], gb[6] = {0, 0, 0, 0, 0, 0}, *gfs[PAMR_MAX_GFNS];
+            struct { int L, shape[3]; double bbox[6]; } r;
+            long n;
+            PAMR_get_g_attribs(&rank, &dim, shape, gb, gw, &t, &ngfs, x, gfs);
+            n = (long)shape[0] * shape[1] * shape[2];
+            r.L = j;
+            memcpy(r.shape, shape, sizeof(r.shape));
+            memcpy(r.bbox, gb, sizeof(r.bbox));
+            rec(9, &r, sizeof(r));
+            rec(10, gfs[gu_amr - 1], 8 * n);
+            for (k = 0; k < c_nsrc; k++) rec(11, gfs[gs_amr[k] - 1], 8 * n);
+            valid = PAMR_next_g();
+         }
+      }
+      fclose(fout);
+      return 0;
+   }
    if (amr_width >= 0) {
       /* instead of the solve: one AMR-hierarchy interpolation of u (time
        * level 1) from level amr_lc to amr_lc+1, over the whole overlap

@@ -36,10 +36,12 @@ def available() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def param_file(case, amr_interp_order: int = 0) -> str:
+def param_file(case, amr_interp_order: int = 0, transfer_order: int = 0) -> str:
     """AMRD run-time parameters of ``case``; amr_interp_order 2 or 4 also
     lists u in amr_interp2/amr_interp4 (its AMR interpolation order,
-    amrd/io.c:771-772)"""
+    amrd/io.c:771-772); transfer_order 2 or 4 lists u and the sources in
+    amr_transfer2/amr_transfer4 (their regrid_transfer order,
+    amrd/io.c:778-779)"""
     p = case.params
     dim = case.dim
     lines = [
@@ -94,6 +96,10 @@ def param_file(case, amr_interp_order: int = 0) -> str:
         raise ValueError("AMRD's coarse-grid correction interpolates with mg_interp2 only")
     if amr_interp_order:
         lines += [f"num_amr_interp{amr_interp_order} := 1", f'amr_interp{amr_interp_order} := [ "u" ]']
+    if transfer_order:
+        names = ["u"] + list(SRC_NAMES[:case.nsrc])
+        lines += [f"num_amr_transfer{transfer_order} := {len(names)}",
+                  f"amr_transfer{transfer_order} := [ " + " ".join(f'"{n}"' for n in names) + " ]"]
     return "\n".join(lines) + "\n"
 
 
@@ -120,13 +126,17 @@ def _records(buf: bytes):
 
 
 def run_reference(case, log_ops: bool = False, workdir: str | None = None,
-                  timeout: float = 3600, amr_interp=None) -> dict:
+                  timeout: float = 3600, amr_interp=None, regrid=None) -> dict:
     """Runs ref_mg on ``case``; returns iterations, hook log, MG hierarchy,
     cmask arrays, final u per input grid and (optionally) the m_util_r8 op log.
     With amr_interp = (lc, width, order) the solve is replaced by one
     PAMR_interp (width 0) or PAMR_AMR_bdy_interp (width > 0) of u from AMR
     level lc to lc+1 with interpolation order 2 or 4; "u" then holds the
-    AMR grids after it."""
+    AMR grids after it. With regrid = (new_case, min_lev, order) the solve is
+    replaced by a second PAMR_compose_hierarchy over levels min_lev.. of
+    new_case's grids, u and the sources transferred with that
+    regrid_transfer order; "regrid" then lists every AMR grid after it
+    (level, shape, bbox, u, sources) in PAMR's order."""
     if not available():
         raise RuntimeError("oracle/_ref/ref_mg is not built (oracle/build_ref.sh)")
     with tempfile.TemporaryDirectory(dir=workdir) as td:
@@ -134,10 +144,15 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         cf = os.path.join(td, "case.bin")
         of = os.path.join(td, "out.bin")
         with open(pf, "w") as f:
-            f.write(param_file(case, amr_interp[2] if amr_interp else 0))
+            f.write(param_file(case, amr_interp[2] if amr_interp else 0, regrid[2] if regrid else 0))
         with open(cf, "wb") as f:
             f.write(case_bytes(case))
         extra = ["1" if log_ops else "0"] + ([f"interp:{amr_interp[0]}:{amr_interp[1]}"] if amr_interp else [])
+        if regrid:
+            nf = os.path.join(td, "new.bin")
+            with open(nf, "wb") as f:
+                f.write(case_bytes(regrid[0]))
+            extra = ["1" if log_ops else "0", f"regrid:{regrid[1]}:{nf}"]
         r = subprocess.run([REF_BIN, pf, cf, of] + extra,
                            capture_output=True, text=True, timeout=timeout, cwd=td)
         if r.returncode != 0:
@@ -145,7 +160,7 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         with open(of, "rb") as f:
             buf = f.read()
     res = {"iters": 0, "hooks": None, "mgh": [], "masks": [], "u": [], "ops": [],
-           "stdout": r.stdout}
+           "regrid": [], "stdout": r.stdout}
     pending_mask = None
     for tag, p in _records(buf):
         if tag == 1:
@@ -173,6 +188,14 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         elif tag == 8:
             v = np.frombuffer(p, dtype="<i4").copy()
             res["ops"].append(v)
+        elif tag == 9:
+            L, s0, s1, s2 = struct.unpack_from("<4i", p)
+            res["regrid"].append({"L": L, "shape": (s0, s1, s2), "bbox": struct.unpack_from("<6d", p, 16),
+                                  "u": None, "src": []})
+        elif tag == 10:
+            res["regrid"][-1]["u"] = np.frombuffer(p, dtype="<f8").copy()
+        elif tag == 11:
+            res["regrid"][-1]["src"].append(np.frombuffer(p, dtype="<f8").copy())
     if res["ops"]:
         res["ops"] = np.stack(res["ops"])
     return res

@@ -874,6 +874,56 @@ int pgb_plan_amr_interp(pgb_hier *h, int lc, int amr_bdy_width, int order, pgb_p
    return h->err[0] ? 2 : 0;
 }
 
+/* init_new_cgh (src/gh.c:934-1045) for AMR level Ln of the hierarchy hn
+ * built after a regrid, from the hierarchy ho it replaces: with interp set,
+ * the interpolation of order `order` from ho's level Ln-1 (owned, extended
+ * by one point: build_owned_gsl(.., 0, 1)) into every grid of hn's level Ln
+ * (build_complete_gsl), then the copies from ho's level Ln (owned) into
+ * hn's level Ln where the grids overlap. The two transfers run through the
+ * same gsl algebra and op lists as PAMR_interp and PAMR_sync, on a joint box
+ * list: ho's boxes first, then hn's (box index + ho->nbox). A level missing
+ * from ho gives an empty plan. Returns 0, or 1 with err filled. */
+int pgb_plan_regrid(const pgb_hier *ho, const pgb_hier *hn, int Ln, int order, int interp, pgb_plan *pi,
+                    pgb_plan *pc, char *err, size_t errlen)
+{
+   pgb_hier t;
+   int ops[PGB_NF], f, b, rc = 0;
+   const int mo1 = Ln - 1 >= ho->prm.min_level ? amr_level_to_mg(ho, Ln - 1) : 0;
+   const int mo = amr_level_to_mg(ho, Ln), mn = amr_level_to_mg(hn, Ln);
+   memset(pi, 0, sizeof(*pi));
+   memset(pc, 0, sizeof(*pc));
+   if (!mn) {
+      snprintf(err, errlen, "AMR level %d is not in the new hierarchy", Ln);
+      return 1;
+   }
+   memset(&t, 0, sizeof(t));
+   t.dim = hn->dim;
+   t.pde = hn->pde;
+   memcpy(t.base_shape, hn->base_shape, sizeof(t.base_shape));
+   memcpy(t.base_bbox, hn->base_bbox, sizeof(t.base_bbox));
+   t.prm = hn->prm;
+   t.nbox = ho->nbox + hn->nbox;
+   t.boxes = (pgb_hbox *)malloc(sizeof(pgb_hbox) * (size_t)t.nbox);   /* shallow: masks and x stay theirs */
+   memcpy(t.boxes, ho->boxes, sizeof(pgb_hbox) * (size_t)ho->nbox);
+   memcpy(t.boxes + ho->nbox, hn->boxes, sizeof(pgb_hbox) * (size_t)hn->nbox);
+   t.nlev = 3;
+   if (mo1) t.lev[1] = ho->lev[mo1];
+   if (mo) t.lev[2] = ho->lev[mo];
+   t.lev[3] = hn->lev[mn];
+   t.lev[3].box = (int *)malloc(sizeof(int) * (size_t)(hn->lev[mn].nbox + 1));
+   for (b = 0; b < hn->lev[mn].nbox; b++) t.lev[3].box[b] = hn->lev[mn].box[b] + ho->nbox;
+   for (f = 0; f < PGB_NF; f++) ops[f] = order;
+   if (interp && mo1) plan_comm(&t, COMM_INTERP, 1, 3, 0, 1, 0, ops, pi);
+   if (!t.err[0] && mo) plan_comm(&t, COMM_SYNC, 2, 3, 0, 0, 0, 0, pc);
+   if (t.err[0]) {
+      snprintf(err, errlen, "%s", t.err);
+      rc = 1;
+   }
+   free(t.lev[3].box);
+   free(t.boxes);
+   return rc;
+}
+
 void pgb_plan_release(pgb_plan *p)
 {
    free(p->batch_start);

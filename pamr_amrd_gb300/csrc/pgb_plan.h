@@ -76,6 +76,12 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
                    int ngrids, const int *grid_level, const double *grid_bbox,
                    const pgb_hparams *prm);
 void pgb_hier_free(pgb_hier *h);
+
+/* regrid transfers into AMR level Ln of hn from ho (init_new_cgh,
+ * src/gh.c:934-1045): interpolation from ho's level Ln-1 (when interp) and
+ * copies from ho's level Ln, over the joint box list ho's boxes, then hn's */
+int pgb_plan_regrid(const pgb_hier *ho, const pgb_hier *hn, int Ln, int order, int interp, pgb_plan *pi,
+                    pgb_plan *pc, char *err, size_t errlen);
 /* PAMR_interp / PAMR_AMR_bdy_interp (src/pamr.c:623-661) from AMR level lc
  * to lc+1 as an interpolation op list of the given order (2 or 4); the
  * caller releases it with pgb_plan_release (host side) */

@@ -1477,6 +1477,62 @@ int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order)
    return rc;
 }
 
+/* Regrid (PAMR_compose_hierarchy's init_new_cgh, src/gh.c:934-1045): u and
+ * the sources of every AMR level of dst, a solver built on the hierarchy
+ * after a regrid, from src, the solver of the hierarchy it replaces. Level
+ * by level, coarse to fine: on levels >= min_level the interpolation from
+ * src's next coarser level over the whole new level, then on every level
+ * the copies from src's grids of the same level where they overlap (the
+ * reference keeps the levels below the recomposed range as they are, which
+ * the copies reproduce on unchanged grids). Both transfers read src only.
+ * Points of a new level that neither covers keep dst's values. */
+int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level)
+{
+   pgb_dbox *joint = 0;
+   int rc = 0, Ln, f, namr = 0, l;
+   if (dst->host_only || src->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (dst == src) return fail(3, "regrid: source and destination are the same solver");
+   if (order != 2 && order != 4) return fail(3, "interpolation order must be 2 or 4");
+   if (dst->h.dim != src->h.dim || dst->nsrc != src->nsrc)
+      return fail(3, "regrid: the solvers differ in dimension or source count");
+   if (min_level < 1) return fail(3, "regrid: min_level must be >= 1");
+   for (l = 1; l <= dst->h.nlev; l++) namr += dst->h.lev[l].in_amrh ? 1 : 0;
+   if (cudaStreamSynchronize(src->stream) != cudaSuccess) return fail(11, "regrid: source stream");
+   if (cudaMalloc((void **)&joint, sizeof(pgb_dbox) * (size_t)(src->h.nbox + dst->h.nbox)) != cudaSuccess)
+      return fail(10, "regrid: device box table");
+   if (cudaMemcpyAsync(joint, src->dbox, sizeof(pgb_dbox) * (size_t)src->h.nbox, cudaMemcpyDeviceToDevice,
+                       dst->stream) != cudaSuccess ||
+       cudaMemcpyAsync(joint + src->h.nbox, dst->dbox, sizeof(pgb_dbox) * (size_t)dst->h.nbox,
+                       cudaMemcpyDeviceToDevice, dst->stream) != cudaSuccess)
+      rc = fail(10, "regrid: device box table");
+   for (Ln = dst->h.prm.min_level; !rc && Ln < dst->h.prm.min_level + namr; Ln++) {
+      pgb_plan pi, pc;
+      char err[256];
+      if (pgb_plan_regrid(&src->h, &dst->h, Ln, order, Ln >= min_level, &pi, &pc, err, sizeof(err))) {
+         rc = fail(3, "regrid: %s", err);
+      } else if (upload_plan(&pi, sizeof(pgb_interp_op)) || upload_plan(&pc, sizeof(pgb_copy_op))) {
+         rc = fail(10, "regrid: plan upload");
+      } else {
+         /* the fields the AMR hierarchy carries: u and every source */
+         for (f = 0; f < 1 + dst->nsrc && !rc; f++) {
+            const int field = f ? PGB_SRC_FIELD(f - 1) : PGB_F_U;
+            if ((pi.nops && pgb_k_interp(joint, &pi, field, dst->h.dim, dst->stream)) ||
+                (pc.nops && pgb_k_copy(joint, &pc, field, dst->stream)))
+               rc = fail(11, "regrid: transfer kernels failed");
+         }
+         if (!rc && cudaStreamSynchronize(dst->stream) != cudaSuccess) rc = fail(11, "regrid: transfer failed");
+      }
+      free_plan_dev(&pi);
+      free_plan_dev(&pc);
+      pgb_plan_release(&pi);
+      pgb_plan_release(&pc);
+   }
+   cudaStreamSynchronize(dst->stream);
+   cudaFree(joint);
+   dst->prepared = 0;   /* u and the sources changed */
+   return rc;
+}
+
 /* ------------------------------------------------------------ checkpoint -- */
 /* File layout (little-endian as written by the host): "PGBCKPT1", int32
  * version, dim, operator kind, ngrids, source count, 0, then a 64-bit hash

@@ -235,6 +235,22 @@ class Solver:
                 a[:] = self.case.u0[i]
         return out
 
+    def get_sources(self):
+        """every source of every input grid in the hierarchy (None for grids
+        below it): out[k][i] = source k of grid i"""
+        out = [[None] * len(self.case.grids) for _ in range(self.case.nsrc)]
+        for L in range(1, self.num_levels() + 1):
+            for idx in range(self.level_nbox(L)):
+                info = self.box_info(L, idx)
+                g = info["amr_grid"]
+                if g < 0 or out[0][g] is not None:
+                    continue
+                for k in range(self.case.nsrc):
+                    a = np.empty(self.case.grids[g].size)
+                    _check(lib().pgb_box_get(self.h, L, idx, 4 + k, _dp(a)))
+                    out[k][g] = a
+        return out
+
     # ------------------------------------------------------------ solve --
     def solve(self):
         cap = max(1, self.case.params.max_iter)
@@ -271,6 +287,15 @@ class Solver:
     def amr_interp(self, lc: int, amr_bdy_width: int = 0, order: int = 2):
         """PAMR_interp (width 0) / PAMR_AMR_bdy_interp of u from AMR level lc to lc+1"""
         _check(lib().pgb_amr_interp(self.h, lc, amr_bdy_width, order))
+
+    def regrid_from(self, old: "Solver", order: int = 2, min_level: int = 2):
+        """u and the sources of this solver's AMR levels from ``old``, the
+        solver of the hierarchy before the regrid (pgb_regrid: PAMR's
+        init_new_cgh transfers, interpolation from level L-1 on levels >=
+        min_level, then copies from level L)"""
+        L = lib()
+        L.pgb_regrid.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        _check(L.pgb_regrid(self.h, old.h, order, min_level))
 
     def checkpoint_save(self, path: str):
         L = lib()

@@ -468,6 +468,59 @@ def nbs2d_uneven(seed: int = 0, n: int = 65, levels: int = 3, min_boxes: int = 3
     return _finish(case, rel_tol)
 
 
+def _sub_grid(rng: SplitMix64, parent: Grid, level: int, dim: int, min_cells: int, max_cells: int) -> Grid:
+    """a level-`level` grid inside `parent` (one level coarser), on its
+    lattice: between min_cells and max_cells parent cells per side"""
+    box = []
+    dx = []
+    for d in range(dim):
+        pn = parent.shape[d]
+        dxp = (parent.bbox[2 * d + 1] - parent.bbox[2 * d]) / (pn - 1)
+        cells = rng.randint(min_cells, max(min_cells, min(max_cells, pn - 1)))
+        p0 = rng.randint(0, pn - 1 - cells)
+        box += [parent.bbox[2 * d] + p0 * dxp, parent.bbox[2 * d] + (p0 + cells) * dxp]
+        dx.append(dxp / 2)
+    return _grid_from_bbox(level, box, dx, dim)
+
+
+def regrid_pair(seed: int = 0, dim: int = 2, n: int = 33, finer: bool = False):
+    """an AMR hierarchy and the one a regrid replaces it with, as PAMR's
+    compose_hierarchy sees them (levels 2.. recomposed, the base grid kept).
+    Old: level 2 grids A, B, C (B may overlap A), level 3 grids in A and B.
+    New: level 2 keeps A and C and adds D; level 3 keeps the old grid in A
+    and adds two inside A (overlapping it or not); with finer, a new level 4
+    inside the kept level-3 grid. Every new grid of level L lies inside an
+    old grid of level L-1, so the interpolation reaches all its points, and
+    inside a new grid of level L-1 (proper nesting). Old u and sources are
+    seeded random numbers (``regrid_data``); new ones start at zero."""
+    rng = SplitMix64(0x5EED0007 + seed)
+    bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)[:2 * dim]
+    shape = (n, n, n if dim == 3 else 1)
+    base = Grid(1, bbox, shape)
+    lo, hi = (3, (n - 1) // 2) if dim == 2 else (2, (n - 1) // 2)
+    a, b, c = (_sub_grid(rng, base, 2, dim, lo, hi) for _ in range(3))
+    a3 = _sub_grid(rng, a, 3, dim, lo, hi)
+    b3 = _sub_grid(rng, b, 3, dim, lo, hi)
+    old = [base, a, b, c, a3, b3]
+    d = _sub_grid(rng, base, 2, dim, lo, hi)
+    new = [base, a, c, d, a3] + [_sub_grid(rng, a, 3, dim, lo, hi) for _ in range(2)]
+    if finer:
+        new.append(_sub_grid(rng, a3, 4, dim, 2, hi))
+    prm = MGParams()
+    mk = lambda name, grids: Case(name, POISSON, dim, shape, bbox, grids,
+                                  [np.zeros(g.size) for g in grids], [np.zeros(g.size) for g in grids], prm)
+    tag = f"regrid{dim}d_{n}_s{seed}" + ("_L4" if finer else "")
+    return mk(tag + "_old", old), mk(tag + "_new", new)
+
+
+def regrid_data(case: Case, seed: int) -> Case:
+    """seeded random u and source on every grid of `case` (in place)"""
+    rng = np.random.default_rng(seed)
+    case.u0 = [rng.standard_normal(g.size) for g in case.grids]
+    case.src = [rng.standard_normal(g.size) for g in case.grids]
+    return case
+
+
 def with_min_level(case: Case, level: int) -> Case:
     """the case solved on the MG hierarchy built from AMR level `level` up
     (solve_elliptics(level, ...), amrd/mg.c:20; level = the finest is the

@@ -2,6 +2,9 @@
 own multigrid solve (oracle/_ref/ref_mg, compiled from the reference's C
 sources by oracle/build_ref.sh) on small seeded cases.
 
+The regrid_* fixtures store an old and a new grid list, the seed of the old
+grids' random u and source, (min_lev, order), and u and the source the
+reference's PAMR_compose_hierarchy left on the new grids it recomposed.
 The amr_interp_* fixtures store a case's grids, the seed of its random u,
 the transfer (AMR level, boundary width, order) and the points the
 reference's PAMR_interp / PAMR_AMR_bdy_interp changed, with their values. The others store the case (grids,
@@ -126,6 +129,39 @@ def save_interp(case, spec, seed, u_after, path):
                         grids=grids, seed=seed, spec=np.array(spec), idx=idx, val=after[idx])
 
 
+def regrid_cases():
+    """(old case with seeded random u and source, new case, data seed,
+    (min_lev, order)) for the regrid fixtures"""
+    out = []
+    for seed, dim, n, finer, order in ((1, 2, 33, False, 2), (2, 2, 33, True, 4), (3, 3, 17, False, 2),
+                                       (4, 3, 17, True, 4)):
+        old, new = W.regrid_pair(seed=seed, dim=dim, n=n, finer=finer)
+        W.regrid_data(old, 100 + seed)
+        out.append((old, new, 100 + seed, (2, order)))
+    return out
+
+
+def save_regrid(old, new, seed, spec, ref, path):
+    """both grid lists, the data seed, (min_lev, order), and u and the source
+    the reference's regrid left on every new grid of level >= min_lev (in the
+    new case's grid order); the grids below keep the old data"""
+    def table(case):
+        return np.array([[g.level] + list(g.shape) + list(g.bbox) + [0.0] * (6 - len(g.bbox))
+                         for g in case.grids])
+    us, ss = [], []
+    for g in new.grids:
+        if g.level < spec[0]:
+            continue
+        hit = [r for r in ref["regrid"] if r["L"] == g.level and r["shape"] == g.shape and
+               np.allclose(r["bbox"][:2 * new.dim], g.bbox, rtol=0, atol=1e-12)]
+        assert len(hit) == 1, (g, len(hit))
+        us.append(hit[0]["u"])
+        ss.append(hit[0]["src"][0])
+    np.savez_compressed(path, name=np.array(new.name), dim=new.dim, base_shape=np.array(new.base_shape),
+                        base_bbox=np.array(new.base_bbox), old=table(old), new=table(new), seed=seed,
+                        spec=np.array(spec), u=np.concatenate(us), src=np.concatenate(ss))
+
+
 def save(case, ref, path):
     p = case.params
     grids = np.array([[g.level] + list(g.shape) + list(g.bbox) + [0.0] * (6 - len(g.bbox))
@@ -185,6 +221,15 @@ def main():
         save_interp(c, spec, seed, ref["u"], path)
         changed = sum(int(np.sum(a != b)) for a, b in zip(ref["u"], c.u0))
         print(f"{os.path.basename(path)}: {changed} points interpolated, {os.path.getsize(path) // 1024} KiB")
+
+    for old, new, seed, spec in regrid_cases():
+        path = os.path.join(HERE, f"{new.name[:-4]}_m{spec[0]}_o{spec[1]}.npz")
+        if os.path.exists(path) and "--all" not in sys.argv:
+            continue
+        ref = refrun.run_reference(old, regrid=(new, spec[0], spec[1]))
+        save_regrid(old, new, seed, spec, ref, path)
+        print(f"{os.path.basename(path)}: {len(ref['regrid'])} grids after the regrid, "
+              f"{os.path.getsize(path) // 1024} KiB")
 
 
 if __name__ == "__main__":

@@ -16,7 +16,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def files():
     """the solve fixtures"""
     return sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("amr_interp_", "dropin_")))
+                  if not os.path.basename(f).startswith(("amr_interp_", "dropin_", "regrid")))
 
 
 def dropin_files():
@@ -81,6 +81,47 @@ def load_interp(path: str):
     offs = np.cumsum([0] + [g.size for g in grids])
     u = [after[offs[i]:offs[i + 1]].copy() for i in range(len(grids))]
     return case, tuple(int(v) for v in z["spec"]), u
+
+
+def regrid_files():
+    """the regrid fixtures"""
+    return sorted(glob.glob(os.path.join(GOLDEN, "regrid*.npz")))
+
+
+def load_regrid(path: str):
+    """(old case with the fixture's seeded u and source, new case with zero
+    data, (min_lev, order), u and source the reference's regrid left on every
+    new grid: the old data on the kept grids below min_lev)"""
+    z = np.load(path)
+    dim = int(z["dim"])
+
+    def grids(table):
+        out = []
+        for row in table:
+            lev, s0, s1, s2 = (int(v) for v in row[:4])
+            out.append(W.Grid(lev, tuple(float(v) for v in row[4:4 + 2 * dim]), (s0, s1, s2)))
+        return out
+    shape = tuple(int(v) for v in z["base_shape"])
+    bbox = tuple(float(v) for v in z["base_bbox"])
+    name = str(z["name"])
+    og, ng = grids(z["old"]), grids(z["new"])
+    old = W.Case(name[:-4] + "_old", W.POISSON, dim, shape, bbox, og, [np.zeros(g.size) for g in og],
+                 [np.zeros(g.size) for g in og], W.MGParams())
+    W.regrid_data(old, int(z["seed"]))
+    new = W.Case(name, W.POISSON, dim, shape, bbox, ng, [np.zeros(g.size) for g in ng],
+                 [np.zeros(g.size) for g in ng], W.MGParams())
+    min_lev, order = (int(v) for v in z["spec"])
+    u, src, off = [], [], 0
+    for g in ng:
+        if g.level < min_lev:   # kept: the old grid's data
+            i = next(i for i, o in enumerate(og) if o.level == g.level and o.shape == g.shape and o.bbox == g.bbox)
+            u.append(old.u0[i].copy())
+            src.append(old.src[i].copy())
+        else:
+            u.append(z["u"][off:off + g.size].copy())
+            src.append(z["src"][off:off + g.size].copy())
+            off += g.size
+    return old, new, (min_lev, order), u, src
 
 
 def load(path: str):
