@@ -126,6 +126,10 @@ int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps);
 int pgb_k_solve_step(unsigned long long handle, const double *norm, double *hist, int *it, int min_iter,
                      int max_iter, double tol, void *stream);
 int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot, void *stream);
+/* pgb_k_defect32 (defect = 1, gated like it) and pgb_k_update in one pass;
+ * zslot must differ from slot */
+int pgb_k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot, int defect,
+                        const int *gate, int gval, void *stream);
 int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream);
 int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0, void *stream);

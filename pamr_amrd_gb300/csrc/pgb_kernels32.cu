@@ -854,6 +854,18 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
  * pre-smoothing on a level whose points outside the cover tiles do not
  * change in between (no sync, no injection there). The next FP64 residual
  * (after that pre-smoothing) is computed from u itself. */
+/* D - (lap E + C E) at point q of E (rows of pitch wy, planes wz): the one
+ * expression of the FP32 defect carry, shared by k_defect32 and
+ * k_update_defect so that both round alike */
+__device__ __forceinline__ float defect32_at(const float *__restrict__ e, long q, long wy, long wz, float c,
+                                             float d, float ix, float iy, float iz, int dim)
+{
+   const float ec = e[q];
+   float t = (e[q + 1] - 2.f * ec + e[q - 1]) * ix + (e[q + wy] - 2.f * ec + e[q - wy]) * iy;
+   if (dim == 3) t += (e[q + wz] - 2.f * ec + e[q - wz]) * iz;
+   return d - (t + c * ec);
+}
+
 __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split,
                                                  const int *gate, int gval)
 {
@@ -875,11 +887,7 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
       if (kk >= tp.nk || k >= b.n[2]) continue;
       const long p = i + sy * j + sz * k, q = wq(b, i, j, k);
       if (!relaxed32(b, i, j, k, p, dim)) continue;
-      const long wy = b.wy, wz = b.wz;
-      const float ec = e[q];
-      float t = (e[q + 1] - 2.f * ec + e[q - 1]) * ix + (e[q + wy] - 2.f * ec + e[q - wy]) * iy;
-      if (dim == 3) t += (e[q + wz] - 2.f * ec + e[q - wz]) * iz;
-      dd[q] = dd[q] - (t + cc[q] * ec);
+      dd[q] = defect32_at(e, q, b.wy, b.wz, cc[q], dd[q], ix, iy, iz, dim);
    }
 }
 
@@ -915,6 +923,44 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
       }
       u[p] += corr;
       e[q] = 0.f;
+   }
+}
+
+/* k_defect32 and k_update in one pass, for blocks whose update zeroes the
+ * other slot (zslot != slot): the defect reads E's stencil in slot while
+ * the update writes zeros only to zslot. The defect part runs unless the
+ * cycle parity gate leaves it out (gate && *gate != gval); with defect = 0
+ * this is k_update. Same arithmetic as the two kernels. */
+__global__ void __launch_bounds__(NT) k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
+                                                      int zslot, int split, int defect, const int *gate, int gval)
+{
+   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const pgb_tile tl = tp.tl;
+   const pgb_dbox b = boxes[tl.box];
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const bool dfx = defect && (!gate || *gate == gval);
+   double *__restrict__ u = b.f[PGB_F_U];
+   const float *__restrict__ es = eslot(b, slot);
+   float *__restrict__ ez = eslot(b, zslot);
+   const double *__restrict__ res = b.f[PGB_F_RES];
+   const float *__restrict__ cc = b.w32[W_C];
+   float *__restrict__ dd = b.w32[W_D];
+   const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
+#pragma unroll
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      const int k = tl.k0 + tp.kk0 + kk;
+      if (kk >= tp.nk || k >= b.n[2]) continue;
+      const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k), q = wq(b, i, j, k);
+      const bool rel = relaxed32(b, i, j, k, p, lv.dim);
+      if (dfx && rel) dd[q] = defect32_at(es, q, b.wy, b.wz, cc[q], dd[q], ix, iy, iz, lv.dim);
+      double corr = f2d(es[q]);
+      if (post && !rel) {
+         const double r = res[p];
+         corr += r - f2d(d2f(r));
+      }
+      u[p] += corr;
+      ez[q] = 0.f;
    }
 }
 
@@ -1671,6 +1717,20 @@ extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int 
    k_update<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot,
                                                                                sp);
    return check32("update");
+}
+
+extern "C" int pgb_k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot, int zslot,
+                                   int defect, const int *gate, int gval, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   if (zslot == slot) {
+      snprintf(g_err32, sizeof(g_err32), "update_defect: the zeroed slot is the one read");
+      return 1;
+   }
+   const int sp = split_for(lv, lv.ntiles);
+   k_update_defect<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot,
+                                                                                      sp, defect, gate, gval);
+   return check32("update_defect");
 }
 
 extern "C" int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)

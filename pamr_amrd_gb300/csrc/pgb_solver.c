@@ -1124,6 +1124,15 @@ static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
  * finest. Levels that carry D across cycles outside their cover tiles
  * (dnext) keep the FP64 residual: two carries in a row would let FP32
  * rounding of early, large defects accumulate there. */
+/* the FP32 defect carry and the update of a block in one kernel (where the
+ * update's zeros go to the slot the defect does not read); PGB_NO_FUSED_UPDATE=1
+ * keeps the two kernels */
+static int fused_update(const pgb_solver *s)
+{
+   (void)s;
+   return !getenv("PGB_NO_FUSED_UPDATE");
+}
+
 static int defect32_level(const pgb_solver *s, int L)
 {
    return L > 1 && s->res32[L] && !s->dnext[L] && s->h.prm.pre_swp > 0;
@@ -1172,18 +1181,29 @@ static int vcycle_mixed(pgb_solver *s)
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
       }
       /* the correction slots: every cycle starts each level from E = 0 in
-       * PGB_W32_E; the pre-smoothing block leaves E = 0 in the slot it ends
-       * in, where the post-smoothing block starts, and that block zeroes
-       * PGB_W32_E again (which the captured graph relies on) */
+       * PGB_W32_E; the pre-smoothing block leaves E = 0 in the slot the
+       * post-smoothing block starts from (the slot it ended in, or the other
+       * one where its update also carries the defect), and that block
+       * zeroes PGB_W32_E again (which the captured graph relies on) */
       s->eslot[L] = PGB_W32_E;
       if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pre_swp, N_RELAX_DN)) return 11;
       if (L > 1 && p->pre_swp > 0) {
          int slot = PGB_W32_E;
+         const int dmode = defect32_level(s, L) ? 1 : alt_level(s, L) ? 2 : 0;
          if (sweeps32(s, L, p->pre_swp, &slot)) return 11;
-         if (defect32_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
-         else if (alt_level(s, L)) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->d_parity, 1, s->stream));
-         KC32(pgb_k_update(s->dbox, s->lv[L], 0, slot, slot, s->stream));
-         s->eslot[L] = slot;
+         if (dmode && s->fuse[L] > 0 && fused_update(s)) {   /* sweeps that alternate the slots */
+            /* defect and update in one pass: E = 0 goes to the other slot,
+             * where the post-smoothing block then starts */
+            const int z = slot == PGB_W32_E ? PGB_W32_E2 : PGB_W32_E;
+            KC32(pgb_k_update_defect(s->dbox, s->lv[L], 0, slot, z, 1, dmode == 2 ? s->d_parity : 0, 1,
+                                     s->stream));
+            s->eslot[L] = z;
+         } else {
+            if (dmode == 1) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
+            else if (dmode == 2) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, s->d_parity, 1, s->stream));
+            KC32(pgb_k_update(s->dbox, s->lv[L], 0, slot, slot, s->stream));
+            s->eslot[L] = slot;
+         }
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       }
    }
@@ -1195,8 +1215,12 @@ static int vcycle_mixed(pgb_solver *s)
             KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream, s->side, s->evfork,
                                     s->evjoin));
          if (sweeps32(s, L, p->pst_swp, &slot)) return 11;
-         if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
-         KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
+         if (s->dnext[L] && slot != PGB_W32_E && fused_update(s)) {
+            KC32(pgb_k_update_defect(s->dbox, s->lv[L], 1, slot, PGB_W32_E, 1, 0, 0, s->stream));
+         } else {
+            if (s->dnext[L]) KC32(pgb_k_defect32(s->dbox, s->lv[L], slot, 0, 0, s->stream));
+            KC32(pgb_k_update(s->dbox, s->lv[L], 1, slot, PGB_W32_E, s->stream));
+         }
          if (sync_field(s, &h->sync[L][1], PGB_F_U)) return 11;
       }
       if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pst_swp, N_RELAX_UP)) return 11;

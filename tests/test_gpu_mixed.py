@@ -78,9 +78,12 @@ def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
     assert r1["iters"] == r2["iters"]
     # the tile depth sets the cover tiles, where the FAS defect is computed
     # afresh instead of carried over in FP32: a few points take the other
-    # path, so the solutions agree to rounding, not bit for bit
+    # path, so the solutions agree to rounding, not bit for bit (measured
+    # 5e-14 to 4e-13 of max |u| over the autotuner's timing-dependent
+    # choices, while both lie 1.2e-11 from the FP64 form's solution of this
+    # 1e-10-converged solve)
     umax = max(float(np.max(np.abs(a))) for a in u2)
-    assert max(float(np.max(np.abs(a - b))) for a, b in zip(u1, u2)) <= 1e-13 * umax
+    assert max(float(np.max(np.abs(a - b))) for a, b in zip(u1, u2)) <= 1e-12 * umax
 
 
 @pytest.mark.parametrize("fuse", ["1", "2", "3", "4", "5"])
