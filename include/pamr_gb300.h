@@ -96,9 +96,13 @@ int pgb_create(int dim, int pde, const int *base_shape, const double *base_bbox,
  * the hook's order gives the hook's results bit for bit (nbs:
  * "lap - (s0*s0 + s1*s1)", "j0"). Relaxation updates
  * u <- u - (L[u] - rhs) / (dL/du) at each red, then black point
- * (num.f:216-241). At most PGB_MAX_SOURCES sources, 31 operations and 8
+ * (num.f:216-241). A solver with several elliptic variables takes one
+ * operator per variable: u is the equation's own variable and u0..u3 the
+ * variables' values at the same point; relaxation updates the variables
+ * in order at each point, each from the others' current values. At most PGB_MAX_SOURCES sources, 31 operations and 8
  * distinct constants per expression. */
 #define PGB_MAX_SOURCES 4
+#define PGB_MAX_VARS 4
 typedef struct pgb_operator pgb_operator;
 int pgb_operator_create(int nsrc, const char *lop, const char *jac, pgb_operator **out);
 /* the built-in operators PGB_PDE_* as operator objects */
@@ -114,6 +118,12 @@ int pgb_operator_kind(const pgb_operator *op);
  * copies of its grids) evaluate exactly what the device evaluates. */
 int pgb_operator_eval(const pgb_operator *op, double lap, double j0, double u, const double *s, double *L,
                       double *J);
+/* the same with several elliptic variables: the value of every variable at
+ * the point in uv[0..3] (u0..u3), var the equation's own variable (u) */
+int pgb_operator_eval_vars(const pgb_operator *op, int var, double lapv, double j0, const double *uv,
+                           const double *s, double *L, double *J);
+/* 1 + the highest variable index the operator names (u0..u3), 0 if none */
+int pgb_operator_vars(const pgb_operator *op);
 
 /* Everything pgb_create takes, plus the level operator, the coarsest AMR
  * level of the MG hierarchy (min_level: PAMR_build_mgh(min_lev, max_lev, tl),
@@ -133,6 +143,13 @@ typedef struct {
    int min_level;               /* 1 = the whole AMR hierarchy */
    int restr_src[PGB_MAX_SOURCES];
    int flags;
+   /* several elliptic variables solved together (AMRD_num_elliptic_vars,
+    * amrd/mg.c:248-314): nvar (1..PGB_MAX_VARS) and the operator of each
+    * variable v >= 1 in var_op[v] (op is variable 0's); FP64 form only.
+    * Every variable takes the same transfer operators (restr_u, restr_res,
+    * mg_sync, interp_order) */
+   int nvar;
+   const pgb_operator *var_op[PGB_MAX_VARS];
 } pgb_create_args;
 void pgb_default_create_args(pgb_create_args *a);
 int pgb_create_ex(const pgb_create_args *a, pgb_solver **out);
@@ -154,6 +171,10 @@ int pgb_get_grid_device(pgb_solver *s, int grid, double *u);
  * pgb_set_grid's src is source 0 */
 int pgb_set_source(pgb_solver *s, int grid, int k, const double *src);
 int pgb_set_source_device(pgb_solver *s, int grid, int k, const double *src);
+/* elliptic variable v (0 <= v < nvar) of an input grid; v = 0 is the u of
+ * pgb_set_grid / pgb_get_grid */
+int pgb_set_var(pgb_solver *s, int grid, int v, const double *u);
+int pgb_get_var(pgb_solver *s, int grid, int v, double *u);
 
 /* Full solve: rebuilds the MG-only data from the AMR grids (build_mgh's
  * injections), then V-cycles until the finest residual is <= tol (at least
@@ -191,6 +212,8 @@ int pgb_prepare_ex(pgb_solver *s, int flags);
 #define PGB_FIELD_LOP 2
 #define PGB_FIELD_RHS 3
 #define PGB_FIELD_SRC 4
+/* the U..RHS fields of elliptic variable v >= 1: PGB_FIELD_VAR(v) + PGB_FIELD_U..RHS */
+#define PGB_FIELD_VAR(v) (16 + 4 * ((v) - 1))
 int pgb_box_set(pgb_solver *s, int level, int idx, int field, const double *in);
 int pgb_box_get(pgb_solver *s, int level, int idx, int field, double *out);
 

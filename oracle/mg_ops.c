@@ -28,7 +28,8 @@ static double lap(const oracle_grid *g, const double *v, int i, int j, int k, do
    return t;
 }
 
-int oracle_nsrc(int pde) { return pde == ORACLE_NBS ? 2 : 1; }
+int oracle_nsrc(int pde) { return pde == ORACLE_NBS || pde == ORACLE_COUPLED ? 2 : 1; }
+int oracle_nvar(int pde) { return pde == ORACLE_COUPLED ? 2 : 1; }
 
 /* the source values at point p */
 static void src_at(int pde, const double *const *src, long p, double *sv)
@@ -145,6 +146,84 @@ double oracle_relax(int pde, const oracle_grid *g, double *v, const double *rhs,
                   jac = jac_point(pde, j0, v[p], sv);
                   v[p] = v[p] - res / jac;
                   norm = norm + res * res;
+                  sum = sum + 1;
+               }
+            }
+   return sqrt(norm / sum);
+}
+
+/* ------------------------------------------------ two elliptic variables -- */
+/* L of variable q of the coupled pair at point p (t its Laplacian) */
+static double op_coupled(int q, double t, double u, double w, const double *s)
+{
+   if (q == 0) return t - s[0] * (u - w) - s[1];
+   return t - s[0] * (w - u);
+}
+
+void oracle_lop_n(int pde, const oracle_grid *g, double *const *lv, const double *const *v,
+                  const double *const *src, const double *cmask)
+{
+   int i, j, k, ks, ke, q;
+   double dx2, dy2, dz2, j0;
+   (void)pde;
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (i = 2; i <= g->shape[0] - 1; i++)
+      for (j = 2; j <= g->shape[1] - 1; j++)
+         for (k = ks; k <= ke; k++) {
+            long p = IDX(g, i, j, k);
+            if (cmask[p] == ORACLE_CMASK_ON) {
+               double sv[4], u = v[0][p], w = v[1][p];
+               src_at(ORACLE_COUPLED, src, p, sv);
+               for (q = 0; q < 2; q++)
+                  lv[q][p] = op_coupled(q, lap(g, v[q], i, j, k, dx2, dy2, dz2), u, w, sv);
+            }
+         }
+}
+
+double oracle_residual_n(int pde, const oracle_grid *g, double *const *res, const double *const *rhs,
+                         const double *const *v, const double *const *src, const double *cmask)
+{
+   int i, j, k, ks, ke, q, sum = 0;
+   double dx2, dy2, dz2, j0, norm = 0;
+   oracle_lop_n(pde, g, res, v, src, cmask);
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (i = 2; i <= g->shape[0] - 1; i++)
+      for (j = 2; j <= g->shape[1] - 1; j++)
+         for (k = ks; k <= ke; k++) {
+            long p = IDX(g, i, j, k);
+            if (cmask[p] == ORACLE_CMASK_ON) {
+               for (q = 0; q < 2; q++) {
+                  res[q][p] = res[q][p] - rhs[q][p];
+                  norm = norm + res[q][p] * res[q][p];
+               }
+               sum = sum + 1;
+            }
+         }
+   return sqrt(norm / sum);
+}
+
+double oracle_relax_n(int pde, const oracle_grid *g, double *const *v, const double *const *rhs,
+                      const double *const *src, const double *cmask)
+{
+   int i, j, k, ks, ke, pass, q, sum = 0;
+   double dx2, dy2, dz2, j0, norm = 0, res, jac;
+   (void)pde;
+   bounds(g, &ke, &ks, &dx2, &dy2, &dz2, &j0);
+   for (pass = 0; pass <= 1; pass++)
+      for (i = 2; i <= g->shape[0] - 1; i++)
+         for (j = 2; j <= g->shape[1] - 1; j++)
+            for (k = ks; k <= ke; k++) {
+               long p = IDX(g, i, j, k);
+               int par = (g->dim == 3) ? (i + j + k + pass) : (i + j + pass);
+               if (par % 2 == 0 && cmask[p] == ORACLE_CMASK_ON) {
+                  double sv[4];
+                  src_at(ORACLE_COUPLED, src, p, sv);
+                  for (q = 0; q < 2; q++) {   /* u, then w from the new u */
+                     res = op_coupled(q, lap(g, v[q], i, j, k, dx2, dy2, dz2), v[0][p], v[1][p], sv) - rhs[q][p];
+                     jac = j0 - sv[0];
+                     v[q][p] = v[q][p] - res / jac;
+                     norm = norm + res * res;
+                  }
                   sum = sum + 1;
                }
             }

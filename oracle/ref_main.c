@@ -47,10 +47,12 @@ typedef struct {
    double bbox[6];
    int shape[3];
    long n;
-   double *u, *src[4];
+   double *u, *uv[2], *src[4];   /* u = uv[0]; uv[1]: the second elliptic variable */
 } case_grid;
 
-static int c_dim, c_pde, c_ngrids, c_nsrc, c_min_level;
+static int c_dim, c_pde, c_ngrids, c_nsrc, c_min_level, c_nvar;
+/* names of the elliptic variables in the parameter file (oracle/refrun.py) */
+static const char *const VAR_NAMES[2] = {"u", "w"};
 /* names of the source variables in the parameter file (oracle/refrun.py) */
 static const char *const SRC_NAMES[4] = {"rho", "rho1", "rho2", "rho3"};
 static case_grid *c_grids;
@@ -66,6 +68,8 @@ static void rec(int tag, const void *p, long nbytes)
 
 /* ------------------------------------------------------------ hook state -- */
 static int gfn_u, gfn_res, gfn_lop, gfn_rhs, gfn_cmask, gfn_src, gfn_srck[4];
+/* MG gfns of every elliptic variable (index 0 = gfn_u .. gfn_rhs) */
+static int gfn_uv[2], gfn_resv[2], gfn_lopv[2], gfn_rhsv[2];
 
 /* MG hierarchy map, captured at the first hook call */
 #define MAXG 4096
@@ -208,7 +212,12 @@ static double h_relax(void)
    ldptr(&g);
    to_ogrid(&g, &o);
    keep_mask(0, &g);
-   norm = oracle_relax(c_pde, &o, g.gfs[gfn_u - 1], g.gfs[gfn_rhs - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
+   if (c_nvar > 1) {
+      double *v[2] = {g.gfs[gfn_uv[0] - 1], g.gfs[gfn_uv[1] - 1]};
+      const double *r[2] = {g.gfs[gfn_rhsv[0] - 1], g.gfs[gfn_rhsv[1] - 1]};
+      norm = oracle_relax_n(c_pde, &o, v, r, grid_src(&g), g.gfs[gfn_cmask - 1]);
+   } else
+      norm = oracle_relax(c_pde, &o, g.gfs[gfn_u - 1], g.gfs[gfn_rhs - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(0, &g, norm);
    return norm;
 }
@@ -220,8 +229,14 @@ static double h_residual(void)
    double norm;
    ldptr(&g);
    to_ogrid(&g, &o);
-   norm = oracle_residual(c_pde, &o, g.gfs[gfn_res - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_u - 1],
-                          grid_src(&g), g.gfs[gfn_cmask - 1]);
+   if (c_nvar > 1) {
+      double *rs[2] = {g.gfs[gfn_resv[0] - 1], g.gfs[gfn_resv[1] - 1]};
+      const double *r[2] = {g.gfs[gfn_rhsv[0] - 1], g.gfs[gfn_rhsv[1] - 1]};
+      const double *v[2] = {g.gfs[gfn_uv[0] - 1], g.gfs[gfn_uv[1] - 1]};
+      norm = oracle_residual_n(c_pde, &o, rs, r, v, grid_src(&g), g.gfs[gfn_cmask - 1]);
+   } else
+      norm = oracle_residual(c_pde, &o, g.gfs[gfn_res - 1], g.gfs[gfn_rhs - 1], g.gfs[gfn_u - 1],
+                             grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(1, &g, norm);
    return norm;
 }
@@ -233,7 +248,12 @@ static void h_lop(void)
    ldptr(&g);
    to_ogrid(&g, &o);
    keep_mask(1, &g);
-   oracle_lop(c_pde, &o, g.gfs[gfn_lop - 1], g.gfs[gfn_u - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
+   if (c_nvar > 1) {
+      double *l[2] = {g.gfs[gfn_lopv[0] - 1], g.gfs[gfn_lopv[1] - 1]};
+      const double *v[2] = {g.gfs[gfn_uv[0] - 1], g.gfs[gfn_uv[1] - 1]};
+      oracle_lop_n(c_pde, &o, l, v, grid_src(&g), g.gfs[gfn_cmask - 1]);
+   } else
+      oracle_lop(c_pde, &o, g.gfs[gfn_lop - 1], g.gfs[gfn_u - 1], grid_src(&g), g.gfs[gfn_cmask - 1]);
    hook_log(2, &g, 0);
 }
 
@@ -251,6 +271,7 @@ static void read_case(const char *path)
    c_ngrids = hdr[2];
    c_min_level = hdr[3] > 0 ? hdr[3] : 1;
    c_nsrc = oracle_nsrc(c_pde);
+   c_nvar = oracle_nvar(c_pde);
    c_grids = (case_grid *)calloc((size_t)c_ngrids, sizeof(case_grid));
    for (i = 0; i < c_ngrids; i++) {
       case_grid *g = &c_grids[i];
@@ -258,8 +279,14 @@ static void read_case(const char *path)
       if (fread(g->shape, 4, 3, f) != 3) exit(2);
       if (fread(g->bbox, 8, 6, f) != 6) exit(2);
       g->n = (long)g->shape[0] * g->shape[1] * g->shape[2];
-      g->u = (double *)malloc(sizeof(double) * (size_t)g->n);
-      if (fread(g->u, 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+      {
+         int q;
+         for (q = 0; q < c_nvar; q++) {   /* every elliptic variable, then the sources */
+            g->uv[q] = (double *)malloc(sizeof(double) * (size_t)g->n);
+            if (fread(g->uv[q], 8, (size_t)g->n, f) != (size_t)g->n) exit(2);
+         }
+         g->u = g->uv[0];
+      }
       {
          int k;
          for (k = 0; k < c_nsrc; k++) {
@@ -289,6 +316,7 @@ static case_grid *match_case_grid(int L, const double *bbox, const int *shape)
 }
 
 /* fill (dir=0) or read back (dir=1) u and the sources on every AMR grid */
+static int g_amr_var[2];   /* AMR gfns (time level 1) of the elliptic variables */
 static void amr_data(int dir, int gu, const int *gs)
 {
    int L, valid, Lmax = PAMR_get_max_lev(PAMR_AMRH);
@@ -303,9 +331,13 @@ static void amr_data(int dir, int gu, const int *gs)
          if (dir == 0) {
             int k;
             memcpy(gfs[gu - 1], cg->u, sizeof(double) * (size_t)cg->n);
+            for (k = 1; k < c_nvar; k++) memcpy(gfs[g_amr_var[k] - 1], cg->uv[k], sizeof(double) * (size_t)cg->n);
             for (k = 0; k < c_nsrc; k++) memcpy(gfs[gs[k] - 1], cg->src[k], sizeof(double) * (size_t)cg->n);
-         } else
+         } else {
+            int k;
             memcpy(cg->u, gfs[gu - 1], sizeof(double) * (size_t)cg->n);
+            for (k = 1; k < c_nvar; k++) memcpy(cg->uv[k], gfs[g_amr_var[k] - 1], sizeof(double) * (size_t)cg->n);
+         }
          valid = PAMR_next_g();
       }
    }
@@ -403,6 +435,19 @@ int main(int argc, char **argv)
    gfn_rhs = PAMR_get_gfn("u_rhs", PAMR_MGH, 0);
    gfn_cmask = PAMR_get_gfn("cmask", PAMR_MGH, 0);
    gfn_src = PAMR_get_gfn("rho", PAMR_MGH, 0);
+   gfn_uv[0] = gfn_u; gfn_resv[0] = gfn_res; gfn_lopv[0] = gfn_lop; gfn_rhsv[0] = gfn_rhs;
+   for (k = 1; k < c_nvar; k++) {
+      char nm[32];
+      g_amr_var[k] = PAMR_get_gfn((char *)VAR_NAMES[k], PAMR_AMRH, 1);
+      gfn_uv[k] = PAMR_get_gfn((char *)VAR_NAMES[k], PAMR_MGH, 0);
+      snprintf(nm, sizeof(nm), "%s_res", VAR_NAMES[k]); gfn_resv[k] = PAMR_get_gfn(nm, PAMR_MGH, 0);
+      snprintf(nm, sizeof(nm), "%s_lop", VAR_NAMES[k]); gfn_lopv[k] = PAMR_get_gfn(nm, PAMR_MGH, 0);
+      snprintf(nm, sizeof(nm), "%s_rhs", VAR_NAMES[k]); gfn_rhsv[k] = PAMR_get_gfn(nm, PAMR_MGH, 0);
+      if (g_amr_var[k] < 0 || gfn_uv[k] < 0 || gfn_resv[k] < 0 || gfn_lopv[k] < 0 || gfn_rhsv[k] < 0) {
+         fprintf(stderr, "ref_mg: elliptic variable %s missing\n", VAR_NAMES[k]);
+         return 3;
+      }
+   }
    if (gu_amr < 0 || gfn_u < 0 || gfn_res < 0 || gfn_lop < 0 || gfn_rhs < 0 ||
        gfn_cmask < 0 || gfn_src < 0) {
       fprintf(stderr, "ref_mg: missing variable definitions\n");
@@ -494,6 +539,8 @@ int main(int argc, char **argv)
       rec(6, masks[i].m, 8L * masks[i].n);
    }
    for (i = 0; i < c_ngrids; i++) rec(7, c_grids[i].u, 8 * c_grids[i].n);
+   for (k = 1; k < c_nvar; k++)   /* the other elliptic variables, grid by grid */
+      for (i = 0; i < c_ngrids; i++) rec(12, c_grids[i].uv[k], 8 * c_grids[i].n);
    {
       for (i = 0; i < mur8_log_n; i++) {
          int r[4 + 6 + MUR8_NARGS];

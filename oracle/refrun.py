@@ -30,6 +30,8 @@ _OP_NAME = {1: "STRAIGHT", 2: "HW", 3: "FW"}
 GFN_KEYS = ("u", "res", "lop", "rhs", "cmask", "src", "src1", "src2", "src3")
 # source variables as oracle/ref_main.c names them
 SRC_NAMES = ("rho", "rho1", "rho2", "rho3")
+# elliptic variables as oracle/ref_main.c names them
+VAR_NAMES = ("u", "w")
 
 
 def available() -> bool:
@@ -58,12 +60,12 @@ def param_file(case, amr_interp_order: int = 0, transfer_order: int = 0) -> str:
         "rho_tm := 2",
         f'num_hyperbolic_vars := {case.nsrc}',
         'hyperbolic_vars := [ ' + " ".join(f'"{n}"' for n in SRC_NAMES[:case.nsrc]) + ' ]',
-        'num_elliptic_vars := 1',
-        'elliptic_vars := [ "u" ]',
-        "num_mg_sync := 1",
-        'mg_sync := [ "u" ]',
-        "num_mg_interp2 := 1",
-        'mg_interp2 := [ "u" ]',
+        f'num_elliptic_vars := {case.nvar}',
+        'elliptic_vars := [ ' + " ".join(f'"{n}"' for n in VAR_NAMES[:case.nvar]) + ' ]',
+        f"num_mg_sync := {case.nvar}",
+        'mg_sync := [ ' + " ".join(f'"{n}"' for n in VAR_NAMES[:case.nvar]) + ' ]',
+        f"num_mg_interp2 := {case.nvar}",
+        'mg_interp2 := [ ' + " ".join(f'"{n}"' for n in VAR_NAMES[:case.nvar]) + ' ]',
         f"MG_pre_swp := {p.pre_swp}",
         f"MG_pst_swp := {p.pst_swp}",
         f"MG_max_iter := {p.max_iter}",
@@ -77,15 +79,16 @@ def param_file(case, amr_interp_order: int = 0, transfer_order: int = 0) -> str:
     ]
     hw, fw = [], []
     srcs = [(SRC_NAMES[k], case.restr_src_k(k)) for k in range(case.nsrc)]
-    for name, op in [("u", p.restr_u)] + srcs + [("u_res", p.restr_res)]:
+    ell = [(n, p.restr_u) for n in VAR_NAMES[:case.nvar]] + [(n + "_res", p.restr_res) for n in VAR_NAMES[:case.nvar]]
+    for name, op in ell + srcs:
         if op == 2:
             hw.append(name)
         elif op == 3:
             fw.append(name)
         elif op != 0:
             raise ValueError("the AMRD parameter interface offers HW or FW restriction only")
-    # u_res defaults to HW (amrd/io.c:865); it is listed only to select FW
-    hw = [n for n in hw if n != "u_res"]
+    # f_res defaults to HW (amrd/io.c:865); it is listed only to select FW
+    hw = [n for n in hw if not n.endswith("_res")]
     if hw:
         lines += [f"num_mg_hw_restr := {len(hw)}",
                   "mg_hw_restr := [ " + " ".join(f'"{n}"' for n in hw) + " ]"]
@@ -111,6 +114,8 @@ def case_bytes(case) -> bytes:
         bb = list(g.bbox) + [0.0] * (6 - len(g.bbox))
         out.append(struct.pack("<4i6d", g.level, *g.shape, *bb))
         out.append(np.ascontiguousarray(u, dtype="<f8").tobytes())
+        for v in range(1, case.nvar):
+            out.append(np.ascontiguousarray(case.var(v)[i], dtype="<f8").tobytes())
         for k in range(case.nsrc):
             out.append(np.ascontiguousarray(case.source(k)[i], dtype="<f8").tobytes())
     return b"".join(out)
@@ -160,7 +165,7 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         with open(of, "rb") as f:
             buf = f.read()
     res = {"iters": 0, "hooks": None, "mgh": [], "masks": [], "u": [], "ops": [],
-           "regrid": [], "stdout": r.stdout}
+           "regrid": [], "u_extra": [], "stdout": r.stdout}
     pending_mask = None
     for tag, p in _records(buf):
         if tag == 1:
@@ -188,6 +193,8 @@ def run_reference(case, log_ops: bool = False, workdir: str | None = None,
         elif tag == 8:
             v = np.frombuffer(p, dtype="<i4").copy()
             res["ops"].append(v)
+        elif tag == 12:   # the other elliptic variables, grid by grid
+            res["u_extra"].append(np.frombuffer(p, dtype="<f8").copy())
         elif tag == 9:
             L, s0, s1, s2 = struct.unpack_from("<4i", p)
             res["regrid"].append({"L": L, "shape": (s0, s1, s2), "bbox": struct.unpack_from("<6d", p, 16),

@@ -38,6 +38,7 @@ typedef struct {
    int tz, rtz, ztz;           /* planes per tile (3-D) of the tile lists */
    int dim;
    int level;
+   int nvar;                   /* elliptic variables (1..PGB_NVAR_MAX) */
 } pgb_dlevel;
 
 /* device-side trace of every norm a hook would return (kind 0 relax,

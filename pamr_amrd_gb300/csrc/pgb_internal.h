@@ -23,9 +23,23 @@ extern "C" {
  * sources 1..3 of an operator with several source fields follow (their
  * arrays exist only when the operator reads them) */
 enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, PGB_F_SRC1 = 5,
-       PGB_NF = 8 };
+       PGB_F_VAR1 = 8, PGB_NF = 20 };
 #define PGB_NSRC_MAX 4
 #define PGB_SRC_FIELD(k) ((k) ? PGB_F_SRC1 + (k) - 1 : PGB_F_SRC)
+/* Elliptic variables (AMRD_num_elliptic_vars, amrd/mg.c:248): variable 0
+ * uses PGB_F_U..PGB_F_RHS, variable v > 0 the four fields from
+ * PGB_F_VAR1 + 4 (v - 1) in the same order (their arrays exist only for the
+ * solver's variables). PGB_FV(v, f) maps f in {U, RES, LOP, RHS}. */
+#define PGB_NVAR_MAX 4
+#define PGB_FV(v, f) ((v) ? PGB_F_VAR1 + 4 * ((v) - 1) + ((f) - PGB_F_U) : (f))
+/* field mask of f over variables 0..n-1 */
+#define PGB_VMASK(n, f) pgb_vmask((n), (f))
+static inline int pgb_vmask(int n, int f)
+{
+   int m = 0, v;
+   for (v = 0; v < n; v++) m |= 1 << PGB_FV(v, f);
+   return m;
+}
 /* field mask of sources 0..n-1 */
 #define PGB_SRC_MASK(n) ((1 << PGB_F_SRC) | ((((1 << ((n) > 1 ? (n) - 1 : 0)) - 1)) << PGB_F_SRC1))
 
@@ -39,6 +53,8 @@ enum { PGB_F_SRC = 0, PGB_F_U = 1, PGB_F_RES = 2, PGB_F_LOP = 3, PGB_F_RHS = 4, 
 #define PGB_PROG_MAX 32
 #define PGB_PROG_CONST 8
 #define PGB_PROG_STACK 8
+/* PGB_P_U's argument: 0 = the variable the equation belongs to, 1 + k =
+ * variable k (expression names u0..u3) */
 enum { PGB_P_END = 0, PGB_P_LAP, PGB_P_J0, PGB_P_U, PGB_P_SRC, PGB_P_CONST, PGB_P_ADD, PGB_P_SUB,
        PGB_P_MUL, PGB_P_DIV, PGB_P_NEG };
 enum { PGB_OPK_POISSON = 0, PGB_OPK_CONFORMAL = 1, PGB_OPK_LAPSE = 2, PGB_OPK_PROGRAM = 3 };

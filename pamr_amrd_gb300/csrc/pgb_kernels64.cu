@@ -200,6 +200,52 @@ __device__ bool last_block(pgb_scratch sc, int *flag)
    return *flag != 0;
 }
 
+/* ------------------------------------------------ several variables -- */
+/* The hooks of an application with several elliptic variables update them
+ * point by point (AMRD calls one relax per grid for all of them, amrd/mg.c:
+ * 135-141): at each point of the colour, variable 0, 1, ... in turn, each
+ * from the others' current values at the point; the norm sums every
+ * variable's squared residual. Program operators only (one per variable,
+ * b.op[v]). */
+__device__ __forceinline__ void load_vars(const pgb_dbox &b, int nvar, long p, double *uv)
+{
+   for (int v = 0; v < nvar; v++) uv[v] = b.f[PGB_FV(v, PGB_F_U)][p];
+}
+
+/* Gauss-Seidel at point p over the variables; returns the sum of the
+ * squared in-sweep residuals */
+__device__ double relax_vars(const pgb_dbox &b, int nvar, long p, int dim)
+{
+   double uv[PGB_NVAR_MAX], acc = 0;
+   const pgb_srcv sv = pgb_load_src(b.op->nsrc, b, p, b.f[PGB_F_SRC][p]);
+   load_vars(b, nvar, p, uv);
+   for (int v = 0; v < nvar; v++) {
+      double *u = b.f[PGB_FV(v, PGB_F_U)];
+      const double r = pgb_prog_Lv(b, v, lap64(b, u, p, dim), uv, sv) - b.f[PGB_FV(v, PGB_F_RHS)][p];
+      const double jac = pgb_prog_Jv(b, v, uv, sv);
+      uv[v] = uv[v] - r / jac;
+      u[p] = uv[v];
+      acc += r * r;
+   }
+   return acc;
+}
+
+/* residual of every variable at point p (res_v = L_v - rhs_v); returns the
+ * sum of their squares */
+__device__ double residual_vars(const pgb_dbox &b, int nvar, long p, int dim)
+{
+   double uv[PGB_NVAR_MAX], acc = 0;
+   const pgb_srcv sv = pgb_load_src(b.op->nsrc, b, p, b.f[PGB_F_SRC][p]);
+   load_vars(b, nvar, p, uv);
+   for (int v = 0; v < nvar; v++) {
+      const double r = pgb_prog_Lv(b, v, lap64(b, b.f[PGB_FV(v, PGB_F_U)], p, dim), uv, sv) -
+                       b.f[PGB_FV(v, PGB_F_RHS)][p];
+      b.f[PGB_FV(v, PGB_F_RES)][p] = r;
+      acc += r * r;
+   }
+   return acc;
+}
+
 /* ---------------------------------------------------------------- relax -- */
 /* one colour pass of relax (num.f:216-241); pass 1 finalizes the norm */
 template <bool PROG>
@@ -224,6 +270,10 @@ __global__ void __launch_bounds__(NT) k_relax(const pgb_dbox *boxes, pgb_dlevel 
       if (!interior(b, i, j, k, dim)) continue;
       long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      if (PROG && lv.nvar > 1) {
+         acc += relax_vars(b, lv.nvar, p, dim);
+         continue;
+      }
       double uc = u[p], s = src[p];
       double res = op64<PROG>(pde, b, p, lap64(b, u, p, dim), uc, s) - rhs[p];
       double jac = jac64<PROG>(pde, b, p, uc, s);
@@ -271,6 +321,10 @@ __global__ void __launch_bounds__(NT) k_residual(const pgb_dbox *boxes, pgb_dlev
       if (!interior(b, i, j, k, dim)) continue;
       long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      if (PROG && lv.nvar > 1) {
+         acc += residual_vars(b, lv.nvar, p, dim);
+         continue;
+      }
       double r = op64<PROG>(pde, b, p, lap64(b, u, p, dim), u[p], src[p]) - rhs[p];
       res[p] = r;
       acc += r * r;
@@ -292,8 +346,8 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
 }
 
 /* ------------------------------------------------ pointwise level passes -- */
-#define FOR_TILE_POINTS(body) FOR_TILE_POINTS_IN(lv.tiles, body)
-#define FOR_TILE_POINTS_IN(list, body)                                               \
+#define FOR_TILE_POINTS(...) FOR_TILE_POINTS_IN(lv.tiles, __VA_ARGS__)
+#define FOR_TILE_POINTS_IN(list, ...)                                                \
    const pgb_tile tl = (list)[blockIdx.x];                                           \
    const pgb_dbox b = boxes[tl.box];                                                 \
    int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;                              \
@@ -303,7 +357,7 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
          int k = tl.k0 + kk;                                                         \
          if (kk >= kz || k >= b.n[2]) continue;                                      \
          long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);                         \
-         body                                                                        \
+         __VA_ARGS__                                                                 \
       }
 
 __global__ void __launch_bounds__(NT) k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask)
@@ -323,13 +377,26 @@ __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dleve
                                                 double w0_r)
 {
    FOR_TILE_POINTS_IN(lv.ctiles, {
-      const double *u = b.f[PGB_F_U];
-      double lopv = 0;
-      int cm = b.cmask_child[p];
-      if (cm && interior(b, i, j, k, lv.dim))
-         lopv = op64<PROG>(pde, b, p, lap64(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
-      b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
-      b.f[PGB_F_LOP][p] = u[p];
+      const int cm = b.cmask_child[p];
+      if (PROG && lv.nvar > 1) {   /* every variable from the same values of all */
+         double uv[PGB_NVAR_MAX], lv_[PGB_NVAR_MAX];
+         const pgb_srcv sv = pgb_load_src(b.op->nsrc, b, p, b.f[PGB_F_SRC][p]);
+         const bool in = cm && interior(b, i, j, k, lv.dim);
+         load_vars(b, lv.nvar, p, uv);
+         for (int v = 0; v < lv.nvar; v++)
+            lv_[v] = in ? pgb_prog_Lv(b, v, lap64(b, b.f[PGB_FV(v, PGB_F_U)], p, lv.dim), uv, sv) : 0.0;
+         for (int v = 0; v < lv.nvar; v++) {
+            b.f[PGB_FV(v, PGB_F_RHS)][p] = cm ? -b.f[PGB_FV(v, PGB_F_RES)][p] * w0_r + lv_[v] : 0.0;
+            b.f[PGB_FV(v, PGB_F_LOP)][p] = uv[v];
+         }
+      } else {
+         const double *u = b.f[PGB_F_U];
+         double lopv = 0;
+         if (cm && interior(b, i, j, k, lv.dim))
+            lopv = op64<PROG>(pde, b, p, lap64(b, u, p, lv.dim), u[p], b.f[PGB_F_SRC][p]);
+         b.f[PGB_F_RHS][p] = cm ? -b.f[PGB_F_RES][p] * w0_r + lopv : 0.0;
+         b.f[PGB_F_LOP][p] = u[p];
+      }
    })
 }
 
@@ -338,13 +405,18 @@ __global__ void __launch_bounds__(NT) k_lop_rhs(const pgb_dbox *boxes, pgb_dleve
 __global__ void __launch_bounds__(NT) k_cgc_coarse(const pgb_dbox *boxes, pgb_dlevel lv,
                                                    double w0_i)
 {
-   FOR_TILE_POINTS_IN(lv.ctiles, { b.f[PGB_F_RES][p] = (b.f[PGB_F_U][p] - b.f[PGB_F_LOP][p]) / w0_i; })
+   FOR_TILE_POINTS_IN(lv.ctiles, {
+      for (int v = 0; v < lv.nvar; v++)
+         b.f[PGB_FV(v, PGB_F_RES)][p] = (b.f[PGB_FV(v, PGB_F_U)][p] - b.f[PGB_FV(v, PGB_F_LOP)][p]) / w0_i;
+   })
 }
 
 /* compute_cgc second half (amrd/mg.c:345-354): f += res */
 __global__ void __launch_bounds__(NT) k_add_res(const pgb_dbox *boxes, pgb_dlevel lv)
 {
-   FOR_TILE_POINTS({ b.f[PGB_F_U][p] += b.f[PGB_F_RES][p]; })
+   FOR_TILE_POINTS({
+      for (int v = 0; v < lv.nvar; v++) b.f[PGB_FV(v, PGB_F_U)][p] += b.f[PGB_FV(v, PGB_F_RES)][p];
+   })
 }
 
 extern "C" int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask, void *stream)
@@ -772,6 +844,10 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
                if (par) continue;
                long p = i + (long)bx.n[0] * (j + (long)bx.n[1] * k);
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
+               if (PROG && lv.nvar > 1) {
+                  acc += relax_vars(bx, lv.nvar, p, dim);
+                  continue;
+               }
                double *u = bx.f[PGB_F_U];
                double uc = u[p], s = bx.f[PGB_F_SRC][p];
                double r = op64<PROG>(pde, bx, p, lap64(bx, u, p, dim), uc, s) - bx.f[PGB_F_RHS][p];
@@ -808,8 +884,9 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
          for (long q = t; q < np; q += CT) {
             int aa, bb, cc;
             unflat(q, op.ni, op.nj, aa, bb, cc);
-            d.f[PGB_F_U][lin(d, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
-               s.f[PGB_F_U][lin(s, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
+            for (int v = 0; v < lv.nvar; v++)
+               d.f[PGB_FV(v, PGB_F_U)][lin(d, op.i2 + aa, op.j2 + bb, op.k2 + cc)] =
+                  s.f[PGB_FV(v, PGB_F_U)][lin(s, op.i1 + aa, op.j1 + bb, op.k1 + cc)];
          }
          __syncthreads();
       }
@@ -836,12 +913,14 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
             const pgb_dbox bx = boxes[lv.box[b]];
             if (!(bx.flags & PGB_BOX_COARSEST)) continue;
             long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-            for (long q = t; q < n; q += CT) {
-               double v = bx.f[PGB_F_U][q];
-               unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-               h ^= mix64(bits ^ mix64((unsigned long long)(off + q) + 0x9E3779B97F4A7C15ull));
-               if (iter == verify_at && saved[off + q] != v) s_flag = 1;
-            }
+            for (int w = 0; w < lv.nvar; w++)   /* the state: every variable */
+               for (long q = t; q < n; q += CT) {
+                  const long o = w * a.snap_points + off + q;
+                  double v = bx.f[PGB_FV(w, PGB_F_U)][q];
+                  unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+                  h ^= mix64(bits ^ mix64((unsigned long long)o + 0x9E3779B97F4A7C15ull));
+                  if (iter == verify_at && saved[o] != v) s_flag = 1;
+               }
             off += n;
          }
       }
@@ -875,7 +954,8 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
                const pgb_dbox bx = boxes[lv.box[b]];
                if (!(bx.flags & PGB_BOX_COARSEST)) continue;
                long n = (long)bx.n[0] * bx.n[1] * bx.n[2];
-               for (long q = t; q < n; q += CT) saved[off + q] = bx.f[PGB_F_U][q];
+               for (int w = 0; w < lv.nvar; w++)
+                  for (long q = t; q < n; q += CT) saved[w * a.snap_points + off + q] = bx.f[PGB_FV(w, PGB_F_U)][q];
                off += n;
             }
             period = found;
@@ -1247,8 +1327,8 @@ extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, con
 {
    size_t smem = (size_t)a.smem_points * 4 * sizeof(double);
    const char *force = getenv("PGB_COARSEST_KERNEL");   /* smem | cluster | single (experiments) */
-   int want_smem = !force || !strcmp(force, "smem");
-   int want_cl = !force || !strcmp(force, "cluster");
+   int want_smem = (!force || !strcmp(force, "smem")) && lv.nvar == 1;
+   int want_cl = (!force || !strcmp(force, "cluster")) && lv.nvar == 1;   /* one variable only */
    if (want_smem && a.smem_points > 0 && a.ncoarse <= CS_MAXB && smem <= 200 * 1024) {
       static int attr_set = 0;
       if (!attr_set) {

@@ -11,6 +11,10 @@
  *    L[u]  = expression of lap, u, s0..s3 and numeric constants
  *    dL/du = expression of j0, u, s0..s3 and numeric constants
  *
+ * (with several elliptic variables, one such pair per variable: u is the
+ * equation's own variable and u0..u3 name variable k at the same point, as
+ * an application's hooks couple their variables point by point)
+ *
  * where lap is the 5/7-point Laplacian of u as the hook pattern forms it
  * (num.f:113-115), j0 its diagonal -2/dx^2 - 2/dy^2 [- 2/dz^2] (num.f:236),
  * and sK the K-th source grid function at the point. Operators of equal
@@ -130,10 +134,12 @@ static void primary(cparse *c, int neg)
       if (!strcmp(id, "lap") && c->allow_lap) emit(c, PGB_P_LAP, 0, 1);
       else if (!strcmp(id, "j0") && !c->allow_lap) emit(c, PGB_P_J0, 0, 1);
       else if (!strcmp(id, "u")) emit(c, PGB_P_U, 0, 1);
+      else if (id[0] == 'u' && isdigit((unsigned char)id[1]) && !id[2] && id[1] - '0' < PGB_NVAR_MAX)
+         emit(c, PGB_P_U, 1 + (id[1] - '0'), 1);
       else if (id[0] == 's' && isdigit((unsigned char)id[1]) && !id[2] && id[1] - '0' < c->nsrc)
          emit(c, PGB_P_SRC, id[1] - '0', 1);
       else {
-         perr(c, "unknown name (lap in L, j0 in dL/du, u, s0.. below the source count)");
+         perr(c, "unknown name (lap in L, j0 in dL/du, u, u0..u3, s0.. below the source count)");
          return;
       }
       if (neg) emit(c, PGB_P_NEG, 0, 0);
@@ -301,7 +307,7 @@ const pgb_dop *pgb_operator_device_form(const pgb_operator *op) { return &op->d;
 /* Host evaluation of a program at one point, with the same single rounding
  * per operation as the device. */
 static double prog_eval_host(const unsigned char *code, const double *cst, double lapv, double j0, double u,
-                          const double *s)
+                             const double *uv, const double *s)
 {
    double st[PGB_PROG_STACK + 1];
    int sp = 0, q;
@@ -310,7 +316,7 @@ static double prog_eval_host(const unsigned char *code, const double *cst, doubl
       switch (opc) {
       case PGB_P_LAP: st[sp++] = lapv; break;
       case PGB_P_J0: st[sp++] = j0; break;
-      case PGB_P_U: st[sp++] = u; break;
+      case PGB_P_U: st[sp++] = arg ? (uv ? uv[arg - 1] : 0.0) : u; break;
       case PGB_P_SRC: st[sp++] = s[arg]; break;
       case PGB_P_CONST: st[sp++] = cst[arg]; break;
       case PGB_P_ADD: sp--; st[sp - 1] = st[sp - 1] + st[sp]; break;
@@ -331,8 +337,31 @@ int pgb_operator_eval(const pgb_operator *op, double lapv, double j0, double u, 
    int k;
    if (!op) return 1;
    for (k = 0; k < op->d.nsrc; k++) sv[k] = s[k];
-   if (L) *L = prog_eval_host(op->d.lcode, op->d.cst, lapv, j0, u, sv);
-   if (J) *J = prog_eval_host(op->d.jcode, op->d.cst, lapv, j0, u, sv);
+   if (L) *L = prog_eval_host(op->d.lcode, op->d.cst, lapv, j0, u, 0, sv);
+   if (J) *J = prog_eval_host(op->d.jcode, op->d.cst, lapv, j0, u, 0, sv);
    return 0;
+}
+
+int pgb_operator_eval_vars(const pgb_operator *op, int var, double lapv, double j0, const double *uv,
+                           const double *s, double *L, double *J)
+{
+   double sv[PGB_NSRC_MAX] = {0, 0, 0, 0};
+   int k;
+   if (!op || var < 0 || var >= PGB_NVAR_MAX || !uv) return 1;
+   for (k = 0; k < op->d.nsrc; k++) sv[k] = s[k];
+   if (L) *L = prog_eval_host(op->d.lcode, op->d.cst, lapv, j0, uv[var], uv, sv);
+   if (J) *J = prog_eval_host(op->d.jcode, op->d.cst, lapv, j0, uv[var], uv, sv);
+   return 0;
+}
+
+/* 1 + the highest variable index an operator names (u0..u3), 0 if none */
+int pgb_operator_vars(const pgb_operator *op)
+{
+   int q, n = 0;
+   const unsigned char *codes[2] = {op->d.lcode, op->d.jcode};
+   for (int c = 0; c < 2; c++)
+      for (q = 0; q < PGB_PROG_MAX && (codes[c][q] & 15) != PGB_P_END; q++)
+         if ((codes[c][q] & 15) == PGB_P_U && (codes[c][q] >> 4) > n) n = codes[c][q] >> 4;
+   return n;
 }
 

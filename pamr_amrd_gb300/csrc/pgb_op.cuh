@@ -27,9 +27,11 @@ static __device__ __forceinline__ pgb_srcv pgb_load_src(int nsrc, const pgb_dbox
    return v;
 }
 
-/* runs one program; lapv/j0 are the values of the names lap and j0 */
+/* runs one program; lapv/j0 are the values of the names lap and j0, u
+ * the equation's own variable, uv[k] variable k (the names u0..u3; uv = 0
+ * with one variable, where u0 is u) */
 static __device__ __noinline__ double pgb_prog_run(const unsigned char *code, const double *cst, double lapv, double j0,
-                                            double u, pgb_srcv s)
+                                            double u, const double *uv, pgb_srcv s)
 {
    double st[PGB_PROG_STACK];
    double top = 0.0;
@@ -42,7 +44,7 @@ static __device__ __noinline__ double pgb_prog_run(const unsigned char *code, co
       switch (opc) {
       case PGB_P_LAP: v = lapv; break;
       case PGB_P_J0: v = j0; break;
-      case PGB_P_U: v = u; break;
+      case PGB_P_U: v = arg && uv ? uv[arg - 1] : u; break;
       case PGB_P_SRC: v = arg == 0 ? s.s0 : arg == 1 ? s.s1 : arg == 2 ? s.s2 : s.s3; break;
       case PGB_P_CONST: v = cst[arg]; break;
       case PGB_P_NEG: top = -top; continue;
@@ -66,13 +68,28 @@ static __device__ __noinline__ double pgb_prog_run(const unsigned char *code, co
 static __device__ __forceinline__ double pgb_prog_L(const pgb_dbox &b, double lapv, double u, double s0, long p)
 {
    const pgb_dop *o = b.op;
-   return pgb_prog_run(o->lcode, o->cst, lapv, b.j0, u, pgb_load_src(o->nsrc, b, p, s0));
+   return pgb_prog_run(o->lcode, o->cst, lapv, b.j0, u, 0, pgb_load_src(o->nsrc, b, p, s0));
 }
 
 static __device__ __forceinline__ double pgb_prog_J(const pgb_dbox &b, double u, double s0, long p)
 {
    const pgb_dop *o = b.op;
-   return pgb_prog_run(o->jcode, o->cst, 0.0, b.j0, u, pgb_load_src(o->nsrc, b, p, s0));
+   return pgb_prog_run(o->jcode, o->cst, 0.0, b.j0, u, 0, pgb_load_src(o->nsrc, b, p, s0));
+}
+
+/* the same for variable v of a solver with several elliptic variables: its
+ * operator is b.op[v], uv[k] holds variable k at the point */
+static __device__ __forceinline__ double pgb_prog_Lv(const pgb_dbox &b, int v, double lapv, const double *uv,
+                                                     pgb_srcv s)
+{
+   const pgb_dop *o = b.op + v;
+   return pgb_prog_run(o->lcode, o->cst, lapv, b.j0, uv[v], uv, s);
+}
+
+static __device__ __forceinline__ double pgb_prog_Jv(const pgb_dbox &b, int v, const double *uv, pgb_srcv s)
+{
+   const pgb_dop *o = b.op + v;
+   return pgb_prog_run(o->jcode, o->cst, 0.0, b.j0, uv[v], uv, s);
 }
 
 #endif

@@ -827,13 +827,15 @@ int pgb_hier_build(pgb_hier *h, int dim, int pde, const int *base_shape, const d
       ops_init[PGB_SRC_FIELD(i)] = op;      /* in both hierarchies, mg_inject set */
       ops_inj_mg[PGB_SRC_FIELD(i)] = op;    /* sources have mg_noinj_to_amr = 1 */
    }
-   ops_init[PGB_F_U] = prm->restr_u;
-   ops_inj[PGB_F_U] = prm->restr_u;
-   ops_inj[PGB_F_RES] = prm->restr_res;
-   ops_inj_mg[PGB_F_U] = prm->restr_u;
-   ops_inj_mg[PGB_F_RES] = prm->restr_res;
-   ops_sync[PGB_F_U] = 1;
-   ops_int[PGB_F_RES] = prm->interp_order;
+   for (i = 0; i < (prm->nvar > 1 ? prm->nvar : 1); i++) {   /* every elliptic variable alike */
+      ops_init[PGB_FV(i, PGB_F_U)] = prm->restr_u;
+      ops_inj[PGB_FV(i, PGB_F_U)] = prm->restr_u;
+      ops_inj[PGB_FV(i, PGB_F_RES)] = prm->restr_res;
+      ops_inj_mg[PGB_FV(i, PGB_F_U)] = prm->restr_u;
+      ops_inj_mg[PGB_FV(i, PGB_F_RES)] = prm->restr_res;
+      ops_sync[PGB_FV(i, PGB_F_U)] = 1;
+      ops_int[PGB_FV(i, PGB_F_RES)] = prm->interp_order;
+   }
    (void)ops_sync;
    for (l = 1; l <= nl; l++) {
       plan_comm(h, COMM_SYNC, l, l, 1, 0, 0, 0, &h->sync[l][0]);

@@ -48,6 +48,7 @@ typedef struct {
    int nsrc;                          /* source fields (>= 1 allocated) */
    int restr_srck[PGB_NSRC_MAX];      /* MG restriction of each source (restr_srck[0] = restr_src) */
    int min_level;                     /* coarsest AMR level of the MG hierarchy (PAMR_build_mgh's min_lev) */
+   int nvar;                          /* elliptic variables (1..PGB_NVAR_MAX) */
 } pgb_hparams;
 
 typedef struct pgb_hier {

@@ -23,8 +23,10 @@ enum { N_RELAX_DN = 0, N_RELAX_UP = 1, N_RESID = 2, N_COARSE = 3, N_SLOTS = 4 };
 struct pgb_solver {
    pgb_hier h;
    pgb_dop dop;             /* the level operator (kind also in h.pde) */
-   pgb_dop *d_dop;          /* its device copy, which every box points to */
+   pgb_dop *d_dop;          /* device copies of the variables' operators, which every box points to */
    int nsrc;                /* source fields allocated per box (>= 1) */
+   int nvar;                /* elliptic variables (AMRD_num_elliptic_vars) */
+   pgb_dop dops[PGB_NVAR_MAX]; /* operator of each variable (dops[0] = dop) */
    int host_only;
    cudaStream_t stream;
    char *arena;
@@ -337,6 +339,7 @@ static int level_tables(pgb_solver *s, int L, int tz)
    s->lv[L].rtz = rtz;
    s->lv[L].dim = h->dim;
    s->lv[L].level = L;
+   s->lv[L].nvar = s->nvar;
 out:
    free(t);
    free(rt);
@@ -348,6 +351,15 @@ out:
    free(mt);
    free(mts);
    return rc;
+}
+
+/* grid functions a box of this solver carries: variable 0's and those of
+ * its other elliptic variables, the sources its operators read */
+static int field_used(const pgb_solver *s, int f)
+{
+   if (f >= PGB_F_VAR1) return 1 + (f - PGB_F_VAR1) / 4 < s->nvar;
+   if (f >= PGB_F_SRC1) return f - PGB_F_SRC1 + 1 < s->nsrc;
+   return 1;
 }
 
 static int setup_device(pgb_solver *s)
@@ -369,7 +381,7 @@ static int setup_device(pgb_solver *s)
       size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       for (f = 0; f < PGB_NF; f++) {
          fo[i * (PGB_NF + 2) + f] = off;
-         if (f >= PGB_F_SRC1 && f - PGB_F_SRC1 + 1 >= s->nsrc) continue;   /* source the operator does not read */
+         if (!field_used(s, f)) continue;   /* source the operator does not read, variable it lacks */
          off = align256(off + 8 * n);
       }
       fo[i * (PGB_NF + 2) + PGB_NF] = off;
@@ -390,8 +402,8 @@ static int setup_device(pgb_solver *s)
       }
    }
    s->arena_bytes = off;
-   CU(cudaMalloc((void **)&s->d_dop, sizeof(pgb_dop)));
-   CU(cudaMemcpy(s->d_dop, &s->dop, sizeof(pgb_dop), cudaMemcpyHostToDevice));
+   CU(cudaMalloc((void **)&s->d_dop, sizeof(pgb_dop) * (size_t)s->nvar));
+   CU(cudaMemcpy(s->d_dop, s->dops, sizeof(pgb_dop) * (size_t)s->nvar, cudaMemcpyHostToDevice));
    CU(cudaMalloc((void **)&s->arena, off));
    CU(cudaMemset(s->arena, 0, off));
    s->hbox = (pgb_dbox *)calloc((size_t)h->nbox, sizeof(pgb_dbox));
@@ -400,10 +412,7 @@ static int setup_device(pgb_solver *s)
       pgb_dbox *db = &s->hbox[i];
       size_t n = (size_t)b->shape[0] * b->shape[1] * b->shape[2];
       double dx2[3] = {1, 1, 1};
-      for (f = 0; f < PGB_NF; f++)
-         db->f[f] = (f >= PGB_F_SRC1 && f - PGB_F_SRC1 + 1 >= s->nsrc)
-                       ? 0
-                       : (double *)(s->arena + fo[i * (PGB_NF + 2) + f]);
+      for (f = 0; f < PGB_NF; f++) db->f[f] = field_used(s, f) ? (double *)(s->arena + fo[i * (PGB_NF + 2) + f]) : 0;
       db->op = s->d_dop;
       if (w32o)
          for (f = 0; f < PGB_NW32; f++) db->w32[f] = (float *)(s->arena + w32o[i * PGB_NW32 + f]);
@@ -496,7 +505,7 @@ static int setup_device(pgb_solver *s)
    CU(cudaMemset(s->d_norms, 0, sizeof(double) * N_SLOTS * (size_t)(h->nlev + 1)));
    CU(cudaMalloc((void **)&s->d_citers, sizeof(int)));
    s->snap_points = snap_pts;
-   CU(cudaMalloc((void **)&s->d_snap, sizeof(double) * 2 * (size_t)(snap_pts ? snap_pts : 1)));
+   CU(cudaMalloc((void **)&s->d_snap, sizeof(double) * 2 * (size_t)s->nvar * (size_t)(snap_pts ? snap_pts : 1)));
    CU(cudaMallocHost((void **)&s->h_res, sizeof(double) * 4));
    CU(cudaMalloc((void **)&s->d_hist, sizeof(double) * (size_t)(h->prm.max_iter > 0 ? h->prm.max_iter : 1)));
    CU(cudaMalloc((void **)&s->d_it, sizeof(int)));
@@ -513,6 +522,7 @@ void pgb_default_create_args(pgb_create_args *a)
    memset(a, 0, sizeof(*a));
    pgb_default_params(&a->params);
    a->min_level = 1;
+   a->nvar = 1;
    for (k = 0; k < PGB_NSRC_MAX; k++) a->restr_src[k] = PGB_HW_RESTR;
 }
 
@@ -521,10 +531,26 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
    pgb_solver *s;
    pgb_hparams hp;
    const pgb_mg_params *params = &a->params;
-   int rc, k, nsrc;
+   int rc, k, nsrc, v;
+   const int nvar = a->nvar > 1 ? a->nvar : 1;
+   const pgb_operator *ops[PGB_NVAR_MAX];
    *out = 0;
    if (!a->op) return fail(1, "no level operator (pgb_operator_create / pgb_operator_builtin)");
+   if (nvar > PGB_NVAR_MAX) return fail(1, "at most %d elliptic variables", PGB_NVAR_MAX);
+   ops[0] = a->op;
    nsrc = pgb_operator_device_form(a->op)->nsrc;
+   for (v = 0; v < nvar; v++) {
+      if (v) {
+         if (!a->var_op[v]) return fail(1, "no operator for elliptic variable %d", v);
+         ops[v] = a->var_op[v];
+         if (pgb_operator_device_form(ops[v])->nsrc > nsrc) nsrc = pgb_operator_device_form(ops[v])->nsrc;
+      }
+      if (pgb_operator_vars(ops[v]) > nvar)
+         return fail(1, "the operator of variable %d names u%d, beyond the %d variable(s)", v,
+                     pgb_operator_vars(ops[v]) - 1, nvar);
+   }
+   if (nvar > 1 && a->params.precision != PGB_FP64)
+      return fail(1, "the mixed form carries one elliptic variable: several take PGB_FP64");
    if (params->interp_order != 2 && params->interp_order != 4)
       return fail(1, "interp_order must be 2 or 4");
    if (params->restr_u < 0 || params->restr_u > 3 || params->restr_res < 0 ||
@@ -538,6 +564,13 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
    if (!s) return fail(10, "out of host memory");
    s->dop = *pgb_operator_device_form(a->op);
    s->nsrc = nsrc > 1 ? nsrc : 1;
+   s->nvar = nvar;
+   for (v = 0; v < nvar; v++) {   /* every variable's program reads the solver's sources */
+      s->dops[v] = *pgb_operator_device_form(ops[v]);
+      s->dops[v].nsrc = s->nsrc;
+      if (nvar > 1) s->dops[v].kind = PGB_OPK_PROGRAM;   /* the program path handles the coupling */
+   }
+   if (nvar > 1) s->dop.kind = PGB_OPK_PROGRAM;
    memset(&hp, 0, sizeof(hp));
    hp.pre_swp = params->pre_swp;
    hp.pst_swp = params->pst_swp;
@@ -559,6 +592,7 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
    hp.restr_srck[0] = params->restr_src;
    for (k = 1; k < PGB_NSRC_MAX; k++) hp.restr_srck[k] = a->restr_src[k];
    hp.min_level = a->min_level > 0 ? a->min_level : 1;
+   hp.nvar = nvar;
    rc = pgb_hier_build(&s->h, a->dim, s->dop.kind, a->base_shape, a->base_bbox, a->ngrids, a->grid_level,
                        a->grid_bbox, &hp);
    if (rc) {
@@ -718,6 +752,29 @@ int pgb_set_source_device(pgb_solver *s, int grid, int k, const double *src)
    return copy_source(s, grid, k, src, cudaMemcpyDeviceToDevice);
 }
 
+/* elliptic variable v of an input grid, in (u) or out (uout) */
+static int copy_var(pgb_solver *s, int grid, int v, const double *u, double *uout)
+{
+   const pgb_hbox *b = 0;
+   const pgb_dbox *db;
+   size_t n;
+   if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
+   if (grid_box(s, grid, &b)) return 3;
+   if (v < 0 || v >= s->nvar) return fail(3, "variable %d: the solver has %d", v, s->nvar);
+   db = &s->hbox[s->h.grid_box[grid]];
+   n = sizeof(double) * (size_t)b->shape[0] * b->shape[1] * b->shape[2];
+   if (u) {
+      s->prepared = 0;
+      CU(cudaMemcpyAsync(db->f[PGB_FV(v, PGB_F_U)], u, n, cudaMemcpyHostToDevice, s->stream));
+   }
+   if (uout) CU(cudaMemcpyAsync(uout, db->f[PGB_FV(v, PGB_F_U)], n, cudaMemcpyDeviceToHost, s->stream));
+   CU(cudaStreamSynchronize(s->stream));
+   return 0;
+}
+
+int pgb_set_var(pgb_solver *s, int grid, int v, const double *u) { return copy_var(s, grid, v, u, 0); }
+int pgb_get_var(pgb_solver *s, int grid, int v, double *u) { return copy_var(s, grid, v, 0, u); }
+
 int pgb_set_grid(pgb_solver *s, int grid, const double *u, const double *src)
 {
    int rc;
@@ -760,6 +817,15 @@ static int relax(pgb_solver *s, int L, int slot)
 static int sync_field(pgb_solver *s, const pgb_plan *p, int field)
 {
    if (p->nops) KC(pgb_k_copy(s->dbox, p, field, s->stream));
+   return 0;
+}
+
+/* the same for field f (U..RHS) of every elliptic variable */
+static int sync_vars(pgb_solver *s, const pgb_plan *p, int f)
+{
+   int v;
+   for (v = 0; v < s->nvar; v++)
+      if (sync_field(s, p, PGB_FV(v, f))) return 11;
    return 0;
 }
 
@@ -884,8 +950,8 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
    const int keep = (flags & PGB_PREPARE_KEEP_MG_DATA) != 0;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    for (L = 1; L <= s->h.nlev; L++) {
-      int mask = (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS);
-      if (!s->h.lev[L].in_amrh && !keep) mask |= (1 << PGB_F_U) | PGB_SRC_MASK(s->nsrc);
+      int mask = PGB_VMASK(s->nvar, PGB_F_RES) | PGB_VMASK(s->nvar, PGB_F_LOP) | PGB_VMASK(s->nvar, PGB_F_RHS);
+      if (!s->h.lev[L].in_amrh && !keep) mask |= PGB_VMASK(s->nvar, PGB_F_U) | PGB_SRC_MASK(s->nsrc);
       KC(pgb_k_clear(s->dbox, s->lv[L], mask, s->stream));
    }
    for (L = s->h.nlev - 1; L >= 1 && !keep; L--)
@@ -957,6 +1023,8 @@ static int box_field(const pgb_solver *s, int field, int *f)
    else if (field == PGB_FIELD_LOP) *f = PGB_F_LOP;
    else if (field == PGB_FIELD_RHS) *f = PGB_F_RHS;
    else if (field >= PGB_FIELD_SRC && field < PGB_FIELD_SRC + s->nsrc) *f = PGB_SRC_FIELD(field - PGB_FIELD_SRC);
+   else if (field >= PGB_FIELD_VAR(1) && field < PGB_FIELD_VAR(s->nvar))   /* variables 1.. */
+      *f = PGB_FV(1 + (field - PGB_FIELD_VAR(1)) / 4, PGB_F_U + (field - PGB_FIELD_VAR(1)) % 4);
    else return fail(3, "unknown field %d", field);
    return 0;
 }
@@ -999,7 +1067,7 @@ static int smooth(pgb_solver *s, int L, int nsweep, int slot)
    int it;
    for (it = 0; it < nsweep; it++) {
       if (relax(s, L, slot)) return 11;
-      if (sync_field(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
+      if (sync_vars(s, &h->sync[L][it ? 1 : 0], PGB_F_U)) return 11;
    }
    return 0;
 }
@@ -1059,20 +1127,22 @@ static int vcycle_fp64(pgb_solver *s)
    const pgb_hparams *p = &h->prm;
    int L, Lf = h->nlev;
    /* clear_MG_vars(Lf) amrd/mg.c:91 */
-   KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
+   const int nv = s->nvar;
+   KC(pgb_k_clear(s->dbox, s->lv[Lf],
+                  PGB_VMASK(nv, PGB_F_RES) | PGB_VMASK(nv, PGB_F_RHS) | PGB_VMASK(nv, PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
       if (L < Lf) {
          KC(pgb_k_residual(s->dbox, s->lv[L + 1], h->pde, s->sc, norm_slot(s, L + 1, N_RESID),
                            s->d_trace, s->stream));
-         if (sync_field(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;   /* set_res_sync */
+         if (sync_vars(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;   /* set_res_sync */
          /* clear_MG_vars(L): rhs and lop are rewritten by lop_rhs below */
-         KC(pgb_k_clear(s->dbox, s->lv[L], 1 << PGB_F_RES, s->stream));
+         KC(pgb_k_clear(s->dbox, s->lv[L], PGB_VMASK(nv, PGB_F_RES), s->stream));
          /* the source restriction of MG-only levels (TF_INJECT_TO_MG_LEV) is left
           * out: it reads and writes the same values every cycle, and
           * pgb_prepare's build-time injection (same ops, same operator) has
           * already put them in place */
          if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), 0, s->stream));
-         if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
+         if (sync_vars(s, &h->sync[L][0], PGB_F_U)) return 11;
          KC(pgb_k_lop_rhs(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
       }
       if (smooth(s, L, p->pre_swp, N_RELAX_DN)) return 11;
@@ -1080,7 +1150,8 @@ static int vcycle_fp64(pgb_solver *s)
    for (L = 1; L <= Lf; L++) {
       if (L > 1) {
          KC(pgb_k_cgc_coarse(s->dbox, s->lv[L - 1], p->w0_i, s->stream));
-         if (h->interp[L].nops) KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_F_RES, h->dim, s->stream));
+         for (int v = 0; v < nv && h->interp[L].nops; v++)
+            KC(pgb_k_interp(s->dbox, &h->interp[L], PGB_FV(v, PGB_F_RES), h->dim, s->stream));
          KC(pgb_k_add_res(s->dbox, s->lv[L], s->stream));
       }
       if (smooth(s, L, p->pst_swp, N_RELAX_UP)) return 11;
@@ -1114,6 +1185,15 @@ static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
    return 0;
 }
 
+/* the FP32 defect carry and the update of a block in one kernel (where the
+ * update's zeros go to the slot the defect does not read); PGB_NO_FUSED_UPDATE=1
+ * keeps the two kernels */
+static int fused_update(const pgb_solver *s)
+{
+   (void)s;
+   return !getenv("PGB_NO_FUSED_UPDATE");
+}
+
 /* Levels whose residual is restricted from its FP32 copy (no sync of res)
  * carry the defect after pre-smoothing in FP32, D - (lap E + C E) before the
  * update (k_defect32), instead of a fresh FP64 residual: nothing reads that
@@ -1124,15 +1204,6 @@ static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
  * finest. Levels that carry D across cycles outside their cover tiles
  * (dnext) keep the FP64 residual: two carries in a row would let FP32
  * rounding of early, large defects accumulate there. */
-/* the FP32 defect carry and the update of a block in one kernel (where the
- * update's zeros go to the slot the defect does not read); PGB_NO_FUSED_UPDATE=1
- * keeps the two kernels */
-static int fused_update(const pgb_solver *s)
-{
-   (void)s;
-   return !getenv("PGB_NO_FUSED_UPDATE");
-}
-
 static int defect32_level(const pgb_solver *s, int L)
 {
    return L > 1 && s->res32[L] && !s->dnext[L] && s->h.prm.pre_swp > 0;
@@ -1490,10 +1561,11 @@ int pgb_amr_interp(pgb_solver *s, int lc, int amr_bdy_width, int order)
       return fail(3, "%s", s->h.err);
    }
    rc = upload_plan(&p, sizeof(pgb_interp_op));
-   if (!rc && p.nops) {
-      if (pgb_k_interp(s->dbox, &p, PGB_F_U, s->h.dim, s->stream) ||
-          cudaStreamSynchronize(s->stream) != cudaSuccess)
-         rc = fail(11, "AMR interpolation failed");
+   if (!rc && p.nops) {   /* every elliptic variable */
+      int v;
+      for (v = 0; v < s->nvar && !rc; v++)
+         if (pgb_k_interp(s->dbox, &p, PGB_FV(v, PGB_F_U), s->h.dim, s->stream)) rc = fail(11, "AMR interpolation failed");
+      if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = fail(11, "AMR interpolation failed");
    }
    free_plan_dev(&p);
    pgb_plan_release(&p);
@@ -1517,8 +1589,8 @@ int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level)
    if (dst->host_only || src->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (dst == src) return fail(3, "regrid: source and destination are the same solver");
    if (order != 2 && order != 4) return fail(3, "interpolation order must be 2 or 4");
-   if (dst->h.dim != src->h.dim || dst->nsrc != src->nsrc)
-      return fail(3, "regrid: the solvers differ in dimension or source count");
+   if (dst->h.dim != src->h.dim || dst->nsrc != src->nsrc || dst->nvar != src->nvar)
+      return fail(3, "regrid: the solvers differ in dimension, source or variable count");
    if (min_level < 1) return fail(3, "regrid: min_level must be >= 1");
    for (l = 1; l <= dst->h.nlev; l++) namr += dst->h.lev[l].in_amrh ? 1 : 0;
    if (cudaStreamSynchronize(src->stream) != cudaSuccess) return fail(11, "regrid: source stream");
@@ -1537,9 +1609,9 @@ int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level)
       } else if (upload_plan(&pi, sizeof(pgb_interp_op)) || upload_plan(&pc, sizeof(pgb_copy_op))) {
          rc = fail(10, "regrid: plan upload");
       } else {
-         /* the fields the AMR hierarchy carries: u and every source */
-         for (f = 0; f < 1 + dst->nsrc && !rc; f++) {
-            const int field = f ? PGB_SRC_FIELD(f - 1) : PGB_F_U;
+         /* the fields the AMR hierarchy carries: every elliptic variable and every source */
+         for (f = 0; f < dst->nvar + dst->nsrc && !rc; f++) {
+            const int field = f < dst->nvar ? PGB_FV(f, PGB_F_U) : PGB_SRC_FIELD(f - dst->nvar);
             if ((pi.nops && pgb_k_interp(joint, &pi, field, dst->h.dim, dst->stream)) ||
                 (pc.nops && pgb_k_copy(joint, &pc, field, dst->stream)))
                rc = fail(11, "regrid: transfer kernels failed");
@@ -1577,6 +1649,7 @@ static unsigned long long dop_hash(const pgb_dop *d)
 
 int pgb_checkpoint_save(pgb_solver *s, const char *path)
 {
+   if (s->nvar > 1) return fail(3, "checkpoint: one elliptic variable only");
    FILE *f;
    int g, rc = 0;
    const int hdr[6] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids, s->nsrc, 0};
@@ -1617,6 +1690,7 @@ int pgb_checkpoint_save(pgb_solver *s, const char *path)
  * a copy that then fails (a CUDA error) can leave earlier grids restored. */
 int pgb_checkpoint_load(pgb_solver *s, const char *path)
 {
+   if (s->nvar > 1) return fail(3, "checkpoint: one elliptic variable only");
    FILE *f;
    char magic[8];
    int hdr[6], g, k, rc = 0, ng = s->h.ngrids;
@@ -1791,7 +1865,7 @@ int pgb_plan_dump(const pgb_solver *s, int which, int L, int *rows, int cap)
          sb = o->src_box; db = o->dst_box;
          r[4] = o->i1; r[5] = o->j1; r[6] = o->k1; r[7] = o->i2; r[8] = o->j2; r[9] = o->k2;
          r[10] = o->ni; r[11] = o->nj; r[12] = o->nk; r[13] = o->irho;
-         for (f = 0; f < PGB_NF; f++) r[14 + f] = o->op[f];
+         for (f = 0; f < PGB_F_VAR1; f++) r[14 + f] = o->op[f];   /* variable 0 and the sources */
       } else {
          const pgb_interp_op *o = (const pgb_interp_op *)p->h_ops + i;
          sb = o->src_box; db = o->dst_box;

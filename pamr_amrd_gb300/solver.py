@@ -38,7 +38,7 @@ class CreateArgs(C.Structure):
                 ("base_bbox", C.c_double * 6), ("ngrids", C.c_int),
                 ("grid_level", C.POINTER(C.c_int)), ("grid_bbox", C.POINTER(C.c_double)),
                 ("params", MGParams), ("min_level", C.c_int), ("restr_src", C.c_int * 4),
-                ("flags", C.c_int)]
+                ("flags", C.c_int), ("nvar", C.c_int), ("var_op", C.c_void_p * 4)]
 
 
 def lib(build: bool = True):
@@ -138,8 +138,12 @@ class Operator:
         self.h = h
 
     @classmethod
-    def for_case(cls, case: Case) -> "Operator":
-        from .workloads import OPERATORS
+    def for_case(cls, case: Case, var: int = 0) -> "Operator":
+        """the operator of elliptic variable `var` of the case"""
+        from .workloads import OPERATORS, VAR_OPERATORS
+        if case.pde in VAR_OPERATORS:
+            n, pairs = VAR_OPERATORS[case.pde]
+            return cls(nsrc=n, lop=pairs[var][0], jac=pairs[var][1])
         if case.pde in OPERATORS:
             n, lop, jac = OPERATORS[case.pde]
             return cls(nsrc=n, lop=lop, jac=jac)
@@ -189,6 +193,10 @@ class Solver:
         for k in range(1, case.nsrc):
             a.restr_src[k] = case.restr_src_k(k)
         a.flags = 1 if host_only else 0
+        a.nvar = case.nvar
+        self._var_ops = [Operator.for_case(case, v) for v in range(1, case.nvar)]
+        for v, o in enumerate(self._var_ops, start=1):
+            a.var_op[v] = o.h
         h = C.c_void_p()
         _check(L.pgb_create_ex(C.byref(a), C.byref(h)))
         self.h = h
@@ -222,6 +230,9 @@ class Solver:
             for k in range(1, self.case.nsrc):
                 sk = np.ascontiguousarray(self.case.source(k)[i], dtype=np.float64)
                 _check(lib().pgb_set_source(self.h, i, k, _dp(sk)))
+            for v in range(1, self.case.nvar):
+                uv = np.ascontiguousarray(self.case.var(v)[i], dtype=np.float64)
+                _check(lib().pgb_set_var(self.h, i, v, _dp(uv)))
 
     def get_u(self):
         out = []
@@ -249,6 +260,21 @@ class Solver:
                     a = np.empty(self.case.grids[g].size)
                     _check(lib().pgb_box_get(self.h, L, idx, 4 + k, _dp(a)))
                     out[k][g] = a
+        return out
+
+    def get_vars(self):
+        """every elliptic variable on every input grid: out[v][i]"""
+        out = [self.get_u()]
+        for v in range(1, self.case.nvar):
+            vals = []
+            for i, g in enumerate(self.case.grids):
+                a = np.empty(g.size)
+                if self._in_hierarchy(i):
+                    _check(lib().pgb_get_var(self.h, i, v, _dp(a)))
+                else:
+                    a[:] = self.case.var(v)[i]
+                vals.append(a)
+            out.append(vals)
         return out
 
     # ------------------------------------------------------------ solve --

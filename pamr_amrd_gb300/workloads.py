@@ -29,13 +29,14 @@ Workloads (names carry their sizes):
 """
 from __future__ import annotations
 
+import copy
 import dataclasses
 import math
 from typing import List, Sequence, Tuple
 
 import numpy as np
 
-POISSON, CONFORMAL, LAPSE, NBS = 0, 1, 2, 3
+POISSON, CONFORMAL, LAPSE, NBS, COUPLED = 0, 1, 2, 3, 4
 PDE_NAMES = {POISSON: "poisson", CONFORMAL: "conformal", LAPSE: "lapse", NBS: "nbs"}
 
 # Operators that are not built into the library, as the level-operator
@@ -44,6 +45,12 @@ PDE_NAMES = {POISSON: "poisson", CONFORMAL: "conformal", LAPSE: "lapse", NBS: "n
 # V_xx + V_yy + V_zz - (phi_r^2 + phi_i^2) = 0 (examples/nbs/num.f:85-246),
 # sources phi_r and phi_i, in the hook's order of operations.
 OPERATORS = {NBS: (2, "lap - (s0*s0 + s1*s1)", "j0")}
+# operators of several elliptic variables solved together: (sources, one
+# (L, dL/du) pair per variable); COUPLED is two variables u, w with
+#   L_u = lap u - s0 (u - w) - s1,   L_w = lap w - s0 (w - u),
+# s0 >= 0 coupling them (a negative semi-definite coupling, so the system
+# stays definite), s1 the source
+VAR_OPERATORS = {COUPLED: (2, (("lap - s0*(u - u1) - s1", "j0 - s0"), ("lap - s0*(u - u0)", "j0 - s0")))}
 
 # transfer operators (values of PAMR's transfer bits, include/pamr.h:92-105)
 STRAIGHT_INJECT, HW_RESTR, FW_RESTR = 1, 2, 3
@@ -124,6 +131,8 @@ class Case:
     restr_src_extra: List[int] = dataclasses.field(default_factory=list)
     # coarsest AMR level of the MG hierarchy (solve_elliptics(L, ...), amrd/mg.c:20)
     min_level: int = 1
+    # elliptic variables 1.. of operators with several (u_extra[v-1][i] = variable v of grid i)
+    u_extra: List[List[np.ndarray]] = dataclasses.field(default_factory=list)
 
     @property
     def num_levels(self) -> int:
@@ -131,7 +140,17 @@ class Case:
 
     @property
     def nsrc(self) -> int:
+        if self.pde in VAR_OPERATORS:
+            return VAR_OPERATORS[self.pde][0]
         return OPERATORS[self.pde][0] if self.pde in OPERATORS else 1
+
+    @property
+    def nvar(self) -> int:
+        return len(VAR_OPERATORS[self.pde][1]) if self.pde in VAR_OPERATORS else 1
+
+    def var(self, v: int) -> List[np.ndarray]:
+        """initial values of elliptic variable v on every grid"""
+        return self.u0 if v == 0 else self.u_extra[v - 1]
 
     def source(self, k: int) -> List[np.ndarray]:
         """source k of every grid"""
@@ -188,7 +207,7 @@ def initial_residual_norm(case: Case) -> float:
             continue
         v = u.reshape(g.shape[2], g.shape[1], g.shape[0])
         f = s.reshape(v.shape)
-        f1 = case.src_extra[0][i].reshape(v.shape) if case.pde == NBS else None
+        f1 = case.src_extra[0][i].reshape(v.shape) if case.pde in (NBS, COUPLED) else None
         c = v[..., 1:-1, 1:-1] if case.dim == 2 else v[1:-1, 1:-1, 1:-1]
         if case.dim == 2:
             t = ((v[:, 1:-1, 2:] - 2 * c + v[:, 1:-1, :-2]) / (dx[0] * dx[0]) +
@@ -201,6 +220,20 @@ def initial_residual_norm(case: Case) -> float:
                  (v[2:, 1:-1, 1:-1] - 2 * c + v[:-2, 1:-1, 1:-1]) / (dx[2] * dx[2]))
             fs = f[1:-1, 1:-1, 1:-1]
             fs1 = f1[1:-1, 1:-1, 1:-1] if f1 is not None else None
+        if case.pde == COUPLED:   # both variables' residuals in one norm
+            w = case.u_extra[0][i].reshape(v.shape)
+            cw = w[..., 1:-1, 1:-1] if case.dim == 2 else w[1:-1, 1:-1, 1:-1]
+            if case.dim == 2:
+                tw = ((w[:, 1:-1, 2:] - 2 * cw + w[:, 1:-1, :-2]) / (dx[0] * dx[0]) +
+                      (w[:, 2:, 1:-1] - 2 * cw + w[:, :-2, 1:-1]) / (dx[1] * dx[1]))
+            else:
+                tw = ((w[1:-1, 1:-1, 2:] - 2 * cw + w[1:-1, 1:-1, :-2]) / (dx[0] * dx[0]) +
+                      (w[1:-1, 2:, 1:-1] - 2 * cw + w[1:-1, :-2, 1:-1]) / (dx[1] * dx[1]) +
+                      (w[2:, 1:-1, 1:-1] - 2 * cw + w[:-2, 1:-1, 1:-1]) / (dx[2] * dx[2]))
+            ru = t - fs * (c - cw) - fs1
+            rw = tw - fs * (cw - c)
+            best = max(best, float(np.sqrt(np.mean(ru * ru + rw * rw))))
+            continue
         if case.pde == POISSON:
             r = t - fs
         elif case.pde == NBS:
@@ -519,6 +552,33 @@ def regrid_data(case: Case, seed: int) -> Case:
     case.u0 = [rng.standard_normal(g.size) for g in case.grids]
     case.src = [rng.standard_normal(g.size) for g in case.grids]
     return case
+
+
+def coupled_from(base: Case, seed: int = 0, rel_tol: float = 1e-10) -> Case:
+    """the coupled two-variable system (VAR_OPERATORS[COUPLED]) on the grids
+    of `base`: coupling s0 = 1 + three seeded Gaussians of amplitude U(0, 4),
+    source s1 = four seeded Gaussians of amplitude U(-1, 1), widths U(0.1, 0.3)
+    of the domain half-width; both variables start at 0"""
+    rng = SplitMix64(0x5EED0008 + seed)
+    half = 0.5 * (base.base_bbox[1] - base.base_bbox[0])
+    cen = [0.5 * (base.base_bbox[2 * d] + base.base_bbox[2 * d + 1]) for d in range(base.dim)]
+
+    def blobs(n, lo, hi):
+        out = []
+        for _ in range(n):
+            a = rng.uniform(lo, hi)
+            w = rng.uniform(0.1, 0.3) * half
+            c = tuple(cen[d] + rng.uniform(-0.5, 0.5) * half for d in range(base.dim)) + (0.0,) * (3 - base.dim)
+            out.append((a, w, c))
+        return out
+    b0, b1 = blobs(3, 0.0, 4.0), blobs(4, -1.0, 1.0)
+    grids = base.grids
+    s0 = [1.0 + _gaussians(g, base.dim, b0) for g in grids]
+    s1 = [_gaussians(g, base.dim, b1) for g in grids]
+    case = Case(f"coupled_{base.name}", COUPLED, base.dim, base.base_shape, base.base_bbox, grids,
+                [np.zeros(g.size) for g in grids], s0, copy.deepcopy(base.params),
+                src_extra=[s1], u_extra=[[np.zeros(g.size) for g in grids]], min_level=base.min_level)
+    return _finish(case, rel_tol)
 
 
 def with_min_level(case: Case, level: int) -> Case:

@@ -2,6 +2,8 @@
 own multigrid solve (oracle/_ref/ref_mg, compiled from the reference's C
 sources by oracle/build_ref.sh) on small seeded cases.
 
+The coupled_* fixtures are solve fixtures of two elliptic variables solved
+together (the second variable's initial and final values beside the first).
 The regrid_* fixtures store an old and a new grid list, the seed of the old
 grids' random u and source, (min_lev, order), and u and the source the
 reference's PAMR_compose_hierarchy left on the new grids it recomposed.
@@ -53,6 +55,17 @@ def cases():
         W.with_min_level(W.lapse2d_bo(33, seed=3, levels=3, step=80), 3),
         W.with_min_level(W.poisson2d_uneven(seed=2, n=65, levels=4, min_boxes=3, max_boxes=8,
                                             min_side=9, max_side=33), 3),
+    ]
+
+
+def coupled_cases():
+    """two elliptic variables solved together (workloads.VAR_OPERATORS[COUPLED])
+    on a single grid, nested boxes in 3-D and an uneven multi-box hierarchy"""
+    return [
+        W.coupled_from(W.poisson2d(33, seed=0), seed=1),
+        W.coupled_from(W.conformal3d(17, 9, seed=0), seed=2),
+        W.coupled_from(W.poisson2d_uneven(seed=1, n=33, levels=3, min_boxes=2, max_boxes=4, min_side=5,
+                                          max_side=17), seed=3),
     ]
 
 
@@ -190,6 +203,9 @@ def save(case, ref, path):
         u=np.concatenate(ref["u"]),
         gfn=np.array([ref["gfn"][k] for k in refrun.GFN_KEYS if k in ref["gfn"]]),
         ops=ref["ops"].astype(np.int16) if len(ref["ops"]) else np.zeros((0, 34), np.int16),
+        # the second elliptic variable of a coupled case: initial and final values
+        u1_0=np.concatenate(case.var(1)) if case.nvar > 1 else np.zeros(0),
+        u1=np.concatenate(ref["u_extra"]) if case.nvar > 1 else np.zeros(0),
     )
 
 
@@ -204,6 +220,14 @@ def main():
         save(c, ref, path)
         print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
               f"{len(ref['ops'])} m_util_r8 calls, {os.path.getsize(path) // 1024} KiB")
+    for c in coupled_cases():
+        path = os.path.join(HERE, f"{c.name}__{len(c.grids)}g_{c.params.min_cwidth}cw.npz")
+        if os.path.exists(path) and "--all" not in sys.argv:
+            continue
+        ref = refrun.run_reference(c)
+        save(c, ref, path)
+        print(f"{os.path.basename(path)}: {ref['iters']} V-cycles, {len(ref['hooks'])} hook calls, "
+              f"{os.path.getsize(path) // 1024} KiB")
     from tests.dropin import dropin as D
     for c, mode, arg, level in dropin_cases():
         path = os.path.join(HERE, f"dropin_{c.name}_m{mode}_a{arg}_L{level}.npz")

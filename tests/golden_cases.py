@@ -16,7 +16,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def files():
     """the solve fixtures"""
     return sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("amr_interp_", "dropin_", "regrid")))
+                  if not os.path.basename(f).startswith(("amr_interp_", "dropin_", "regrid", "coupled_")))
 
 
 def dropin_files():
@@ -81,6 +81,11 @@ def load_interp(path: str):
     offs = np.cumsum([0] + [g.size for g in grids])
     u = [after[offs[i]:offs[i + 1]].copy() for i in range(len(grids))]
     return case, tuple(int(v) for v in z["spec"]), u
+
+
+def coupled_files():
+    """solve fixtures of two elliptic variables (load them with load())"""
+    return sorted(glob.glob(os.path.join(GOLDEN, "coupled_*.npz")))
 
 
 def regrid_files():
@@ -149,6 +154,8 @@ def load(path: str):
         case.src_extra = [split(z["src1"])]
     if "min_level" in z.files:
         case.min_level = int(z["min_level"])
+    if "u1_0" in z.files and len(z["u1_0"]):   # the second elliptic variable
+        case.u_extra = [split(z["u1_0"])]
     masks = []
     off = 0
     for kind, L, idx in z["masks_meta"]:
@@ -169,6 +176,7 @@ def load(path: str):
         "gfn": dict(zip(("u", "res", "lop", "rhs", "cmask", "src", "src1", "src2", "src3"),
                         (int(v) for v in z["gfn"]))),
         "ops": z["ops"].astype(np.int64),
+        "u_extra": [split(z["u1"])] if "u1" in z.files and len(z["u1"]) else [],
     }
     return case, ref
 
