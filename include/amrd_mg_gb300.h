@@ -67,6 +67,15 @@ void extend_cmask_bdy(int L, int hier, int num);
  * convention) with a message printed. */
 int amrd_set_device_MG_operator(int nsrc, char **src_names, char *lop, char *jac);
 
+/* With several elliptic variables (AMRD_num_elliptic_vars > 1): the device
+ * operator of variable var (1.., the order of AMRD_elliptic_vars), on the
+ * sources registered above; u is that variable, u0..u3 the variables at the
+ * same point (pamr_gb300.h). Variable 0's operator is the one registered by
+ * amrd_set_device_MG_operator. solve_elliptics solves them together
+ * (FP64 form); vcycle carries one variable. Returns 1, or 0 with a
+ * message. */
+int amrd_set_device_MG_var_operator(int var, char *lop, char *jac);
+
 /* 0 (default): every operation in FP64, bit-identical to the reference;
  * 1: FP32 smoothing and prolongation inside FP64 defect correction
  * (pamr_gb300.h, PGB_MIXED). Returns 1, or 0 for another value. */

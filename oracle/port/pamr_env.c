@@ -15,6 +15,9 @@
  * and "cmask", one time level. gfn numbering of this environment:
  *   u 1 (AMR) / 2 (MG), rho 3 / 4, rho1 5 / 6, u_res 7, u_lop 8, u_rhs 9,
  *   cmask 10 / 11.
+ * A coupled case adds a second elliptic variable "w" on the AMR grids (gfn
+ * 12, kept here beside the port's grids; its MG instances are not built, so
+ * only solve_elliptics runs on such a case).
  */
 #include "mg_port.c"
 #include "../../tests/dropin/dropin_case.h"
@@ -49,6 +52,18 @@ static int *E_lev;
 static double *E_bbox;
 static double **E_u, **E_src, **E_src1;
 static const double *E_srcx[1][4096];
+/* the second elliptic variable of a coupled case, per AMR grid */
+static int E_nw;
+static const void *E_wg[4096];
+static double *E_w[4096];
+
+static double *w_of(const void *g)
+{
+   int i;
+   for (i = 0; i < E_nw; i++)
+      if (E_wg[i] == g) return E_w[i];
+   return 0;
+}
 
 int env_init(const char *case_path, const char *param_path)
 {
@@ -91,6 +106,27 @@ int env_init(const char *case_path, const char *param_path)
    E_case.interp_buffer = 2;
    E_case.min_level = 1;
    if (port_compose(&E_case, 0)) return 3;
+   if (dc.coupled) {   /* w on every AMR grid, from the case */
+      int l;
+      AMRD_num_elliptic_vars = 2;
+      AMRD_elliptic_vars[1] = "w";
+      E_nw = 0;
+      for (l = 1; l <= P.n_amr; l++)
+         for (pgrid *g = P.amr[l].grids; g; g = g->next) {
+            long n = (long)g->shape[0] * g->shape[1] * g->shape[2];
+            for (i = 0; i < dc.ngrids; i++) {
+               int same = dc.lev[i] == l, q;
+               for (q = 0; q < 2 * dc.dim && same; q++)
+                  if (fabs(dc.bbox[6 * i + q] - g->bbox[q]) > 1e-9 * (1 + fabs(g->bbox[q]))) same = 0;
+               if (same) break;
+            }
+            if (i == dc.ngrids || E_nw >= 4096) return 4;
+            E_wg[E_nw] = g;
+            E_w[E_nw] = (double *)malloc(sizeof(double) * (size_t)n);
+            memcpy(E_w[E_nw], dc.w[i], sizeof(double) * (size_t)n);
+            E_nw++;
+         }
+   }
    AMRD_MG_pre_swp = E_case.pre_swp;
    AMRD_MG_pst_swp = E_case.pst_swp;
    AMRD_MG_max_iter = E_case.max_iter;
@@ -173,9 +209,10 @@ int PAMR_get_g_attribs(int *rank, int *dim, int *shape, double *bbox, int *ghost
       x[d] = g->x[d];
    }
    *t = 0;
-   *ngfs = 11;
-   for (d = 0; d < 11; d++) gfs[d] = 0;
+   *ngfs = 12;
+   for (d = 0; d < 12; d++) gfs[d] = 0;
    if (E_it.hier == 1) {
+      gfs[11] = w_of(g);
       gfs[0] = g->gf[G_U];
       gfs[2] = g->gf[G_SRC];
       gfs[4] = g->gf[G_SRC1];
@@ -198,7 +235,7 @@ int PAMR_get_gfn(char *name, int hier, int tl)
       const char *n;
       int amr, mg;
    } tab[] = {{"u", 1, 2}, {"rho", 3, 4}, {"rho1", 5, 6}, {"u_res", 0, 7}, {"u_lop", 0, 8},
-              {"u_rhs", 0, 9}, {"cmask", 10, 11}};
+              {"u_rhs", 0, 9}, {"cmask", 10, 11}, {"w", 12, 0}};
    int i;
    for (i = 0; i < (int)(sizeof(tab) / sizeof(tab[0])); i++)
       if (!strcmp(name, tab[i].n)) {
@@ -240,10 +277,10 @@ int PAMR_get_var_attribs(char *name, int *in_amrh, int *in_mgh, int *num_tl, int
    *num_tl = 1;
    *mg_interp = *mg_sync = *mg_noinj_to_amr = 0;
    *in_amrh = *in_mgh = 1;
-   if (!strcmp(name, "u")) {
+   if (!strcmp(name, "u") || (E_nw && !strcmp(name, "w"))) {
       *mg_inject = P.c->restr_u;
       *mg_sync = 1;
-   } else if (!strcmp(name, "u_res")) {
+   } else if (!strcmp(name, "u_res") || (E_nw && !strcmp(name, "w_res"))) {
       *in_amrh = 0;
       *mg_inject = P.c->restr_res;
       *mg_interp = P.c->interp_order;
@@ -253,7 +290,8 @@ int PAMR_get_var_attribs(char *name, int *in_amrh, int *in_mgh, int *num_tl, int
    } else if (!strcmp(name, "rho1")) {
       *mg_inject = P.c->restr_srcx[0];
       *mg_noinj_to_amr = 1;
-   } else if (!strcmp(name, "u_lop") || !strcmp(name, "u_rhs")) {
+   } else if (!strcmp(name, "u_lop") || !strcmp(name, "u_rhs") ||
+              (E_nw && (!strcmp(name, "w_lop") || !strcmp(name, "w_rhs")))) {
       *in_amrh = 0;
       *mg_inject = 0;
    } else if (!strcmp(name, "cmask")) {

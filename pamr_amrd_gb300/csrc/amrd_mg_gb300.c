@@ -23,7 +23,9 @@
  * finest come back.
  *
  * Limits (each reported by a message and AMRD_stop, as AMRD reports
- * errors): one elliptic variable; save_tre = 0; no periodic boundaries;
+ * errors): up to four elliptic variables in solve_elliptics (FP64 form,
+ * every variable with the first one's MG transfers), one in vcycle;
+ * save_tre = 0; no periodic boundaries;
  * no t0 initialisation hook or constraint-data variables (AMRD_is_t0 runs
  * of generate_id with app_elliptic_vars_t0_init / MG_cnst_data); one MPI
  * rank; mg_sync and mg_interp2 set on the variable (the reference
@@ -43,13 +45,14 @@
 static struct {
    /* registration */
    pgb_operator *op;
+   pgb_operator *var_op[PGB_MAX_VARS];   /* elliptic variables 1.. (var_op[0] unused) */
    char *src_names[MAXSRC];
    int nsrc;
    int precision;
    int op_generation;
    /* the cached device hierarchy and what it was built from */
    pgb_solver *s;
-   int dim, L, ngrids, generation;
+   int dim, L, ngrids, generation, nvar;
    int *lev;
    double *bbox;            /* 6 per grid */
    pgb_mg_params prm;
@@ -106,6 +109,27 @@ int amrd_set_device_MG_operator(int nsrc, char **src_names, char *lop, char *jac
    }
    G.op = op;
    G.nsrc = nsrc;
+   G.op_generation++;
+   return 1;
+}
+
+int amrd_set_device_MG_var_operator(int var, char *lop, char *jac)
+{
+   pgb_operator *op = 0;
+   if (var < 1 || var >= PGB_MAX_VARS) {
+      printf("amrd_set_device_MG_var_operator: error ... variable %d (1..%d)\n", var, PGB_MAX_VARS - 1);
+      return 0;
+   }
+   if (!G.op) {
+      printf("amrd_set_device_MG_var_operator: error ... register variable 0 (amrd_set_device_MG_operator) first\n");
+      return 0;
+   }
+   if (pgb_operator_create(G.nsrc, lop, jac, &op)) {
+      printf("amrd_set_device_MG_var_operator: error ... %s\n", pgb_last_error());
+      return 0;
+   }
+   if (G.var_op[var]) pgb_operator_destroy(G.var_op[var]);
+   G.var_op[var] = op;
    G.op_generation++;
    return 1;
 }
@@ -213,6 +237,15 @@ static void read_params(pgb_mg_params *p, int *restr_src)
    p->restr_u = a.mg_inject;
    p->restr_res = ar.mg_inject;
    p->interp_order = ar.mg_interp;
+   for (k = 1; k < AMRD_num_elliptic_vars; k++) {   /* the others take the same transfers */
+      vattr b, br;
+      const char *vk = AMRD_elliptic_vars[k];
+      snprintf(res_name, sizeof(res_name), "%s_res", vk);
+      if (!var_attr(vk, &b) || !var_attr(res_name, &br)) stop("cannot read an elliptic variable's attributes", vk);
+      if (b.mg_sync != a.mg_sync || b.mg_inject != a.mg_inject || b.mg_noinj_to_amr != a.mg_noinj_to_amr ||
+          br.mg_inject != ar.mg_inject || br.mg_interp != ar.mg_interp)
+         stop("every elliptic variable must take the first one's MG transfers on the device", vk);
+   }
    for (k = 0; k < G.nsrc; k++) {
       vattr s;
       if (!var_attr(G.src_names[k], &s)) stop("unknown source variable", G.src_names[k]);
@@ -276,7 +309,11 @@ static void ensure_solver(int L, int Lf)
    double *bbox, gbb[6] = {0, 0, 0, 0, 0, 0}, dx[3] = {1, 1, 1}, dt;
    pgrid g;
    if (!G.op) stop("no device operator registered (amrd_set_device_MG_operator)", "");
-   if (AMRD_num_elliptic_vars != 1) stop("exactly one elliptic variable is supported on the device", "");
+   if (AMRD_num_elliptic_vars < 1 || AMRD_num_elliptic_vars > PGB_MAX_VARS)
+      stop("the device solves 1 to 4 elliptic variables", "");
+   for (i = 1; i < AMRD_num_elliptic_vars; i++)
+      if (!G.var_op[i]) stop("no device operator for an elliptic variable (amrd_set_device_MG_var_operator)",
+                             AMRD_elliptic_vars[i]);
    read_params(&p, restr);
    /* dimension and base shape from a level-1 grid's context */
    if (!PAMR_init_s_iter(1, ABI_PAMR_AMRH, 1) || !attribs(&g)) stop("no AMR hierarchy", "");
@@ -286,6 +323,7 @@ static void ensure_solver(int L, int Lf)
    for (d = 0; d < dim; d++) shape[d] = (int)floor((gbb[2 * d + 1] - gbb[2 * d]) / dx[d] + 0.5) + 1;
    n = read_sgh(L, Lf, dim, &lev, &bbox);
    if (G.s && G.dim == dim && G.L == L && G.ngrids == n && G.generation == G.op_generation &&
+       G.nvar == AMRD_num_elliptic_vars &&
        !memcmp(G.lev, lev, sizeof(int) * (size_t)n) && !memcmp(G.bbox, bbox, sizeof(double) * 6 * (size_t)n) &&
        !memcmp(&G.prm, &p, sizeof(p)) && !memcmp(G.restr_src, restr, sizeof(restr)) &&
        !memcmp(G.base_shape, shape, sizeof(shape)) && !memcmp(G.base_bbox, gbb, sizeof(gbb))) {
@@ -307,10 +345,13 @@ static void ensure_solver(int L, int Lf)
       a.params = p;
       a.min_level = L;
       for (i = 1; i < MAXSRC; i++) a.restr_src[i] = restr[i];
+      a.nvar = AMRD_num_elliptic_vars;
+      for (i = 1; i < a.nvar; i++) a.var_op[i] = G.var_op[i];
       if (!ok_pgb(pgb_create_ex(&a, &G.s), "building the device hierarchy")) return;
    }
    G.dim = dim;
    G.L = L;
+   G.nvar = AMRD_num_elliptic_vars;
    G.ngrids = n;
    G.lev = lev;
    G.bbox = bbox;
@@ -374,7 +415,7 @@ void solve_elliptics(int L, int tl, int save_tre)
    int Lf = PAMR_get_max_lev(ABI_PAMR_AMRH), l, k, iters = 0, cap;
    double res = 0;
    const char *var;
-   int gu, gs[MAXSRC], gcm = 0;
+   int gu, gs[MAXSRC], gcm = 0, gv[PGB_MAX_VARS], v;
 
    if ((AMRD_num_elliptic_vars == 0 && !AMRD_is_t0) ||
        (AMRD_num_elliptic_vars == 0 && AMRD_num_elliptic_vars_t0 == 0 && AMRD_is_t0))
@@ -385,6 +426,8 @@ void solve_elliptics(int L, int tl, int save_tre)
    ensure_solver(L, Lf);
    var = AMRD_elliptic_vars[0];
    gu = gfn(var, ABI_PAMR_AMRH, var_tl(var, tl));
+   for (v = 1; v < G.nvar; v++)
+      gv[v] = gfn(AMRD_elliptic_vars[v], ABI_PAMR_AMRH, var_tl(AMRD_elliptic_vars[v], tl));
    for (k = 0; k < G.nsrc; k++) gs[k] = gfn(G.src_names[k], ABI_PAMR_AMRH, var_tl(G.src_names[k], tl));
    if (AMRD_cmask_gfn > 0) gcm = AMRD_cmask_gfn;
    /* copy in */
@@ -400,6 +443,7 @@ void solve_elliptics(int L, int tl, int save_tre)
             stop("grid shapes differ from the device hierarchy's", "");
          ok_pgb(pgb_set_grid(G.s, i, g.gfs[gu - 1], G.nsrc ? g.gfs[gs[0] - 1] : 0), "copying a grid");
          for (k = 1; k < G.nsrc; k++) ok_pgb(pgb_set_source(G.s, i, k, g.gfs[gs[k] - 1]), "copying a source");
+         for (v = 1; v < G.nvar; v++) ok_pgb(pgb_set_var(G.s, i, v, g.gfs[gv[v] - 1]), "copying a variable");
          valid = PAMR_next_g();
       }
    }
@@ -420,6 +464,7 @@ void solve_elliptics(int L, int tl, int save_tre)
          attribs(&g);
          i = grid_index(l, &g);
          ok_pgb(pgb_get_grid(G.s, i, g.gfs[gu - 1]), "reading a grid back");
+         for (v = 1; v < G.nvar; v++) ok_pgb(pgb_get_var(G.s, i, v, g.gfs[gv[v] - 1]), "reading a variable back");
          if (gcm && iters > 0) put_bdy_mask(G.mg_level[i], G.mg_idx[i], g.gfs[gcm - 1]);
          valid = PAMR_next_g();
       }
@@ -442,7 +487,7 @@ double vcycle(int giter, int save_tre)
    (void)giter;
    if (save_tre) stop("vcycle: save_tre is not supported on the device", "");
    if (Lmg < 1) stop("vcycle: no MG hierarchy (PAMR_build_mgh first)", "");
-   if (AMRD_num_elliptic_vars != 1) stop("exactly one elliptic variable is supported on the device", "");
+   if (AMRD_num_elliptic_vars != 1) stop("vcycle: the device's single V-cycle carries one elliptic variable", "");
    gm = gfn(var, ABI_PAMR_MGH, 0);
    if (var_attr(var, &a)) num_tl = a.num_tl;
    /* which AMR levels the MG hierarchy replicates: an MG grid of an AMR

@@ -60,7 +60,7 @@ def write_case(case, path: str, mode: int = 0, arg: int = 0, level: int = 1):
     p = case.params
     if case.nsrc != 2:
         raise ValueError("the drop-in application reads two sources")
-    out = [struct.pack("<8i", case.dim, len(case.grids), mode, arg, level, 0, 0, 0)]
+    out = [struct.pack("<8i", case.dim, len(case.grids), mode, arg, level, int(case.nvar == 2), 0, 0)]
     out.append(struct.pack("<6d", *(list(case.base_bbox) + [0.0] * (6 - len(case.base_bbox)))))
     out.append(struct.pack("<4i", *case.base_shape, 0))
     out.append(struct.pack("<10i", p.pre_swp, p.pst_swp, p.max_iter, p.min_iter, p.max_citer, p.min_cwidth,
@@ -68,13 +68,13 @@ def write_case(case, path: str, mode: int = 0, arg: int = 0, level: int = 1):
     out.append(struct.pack("<4d", p.tol, p.crtol, p.w0_r, p.w0_i))
     for i, g in enumerate(case.grids):
         out.append(struct.pack("<4i6d", g.level, *g.shape, *(list(g.bbox) + [0.0] * (6 - len(g.bbox)))))
-        for a in (case.u0[i], case.src[i], case.source(1)[i]):
+        for a in [case.u0[i]] + [case.var(v)[i] for v in range(1, case.nvar)] + [case.src[i], case.source(1)[i]]:
             out.append(np.ascontiguousarray(a, dtype="<f8").tobytes())
     with open(path, "wb") as f:
         f.write(b"".join(out))
 
 
-def parse(buf: bytes) -> dict:
+def parse(buf: bytes, nvar: int = 1) -> dict:
     iters, nres = struct.unpack_from("<2i", buf, 0)
     off = 8
     res = np.frombuffer(buf, dtype="<f8", count=nres, offset=off).copy()
@@ -95,7 +95,11 @@ def parse(buf: bytes) -> dict:
         off += 8 * n
         cm = np.frombuffer(buf, dtype="<f8", count=n, offset=off).copy()
         off += 8 * n
-        grids.append({"level": lev, "shape": (s0, s1, s2), "bbox": bb, "u": u, "cmask": cm})
+        grid = {"level": lev, "shape": (s0, s1, s2), "bbox": bb, "u": u, "cmask": cm}
+        if nvar == 2:   # the second elliptic variable of a coupled case
+            grid["w"] = np.frombuffer(buf, dtype="<f8", count=n, offset=off).copy()
+            off += 8 * n
+        grids.append(grid)
     return {"iters": iters, "res": res, "hooks": rec, "grids": grids}
 
 
@@ -112,7 +116,7 @@ def run(binary: str, case, mode: int = 0, arg: int = 0, level: int = 1, env=None
         if r.returncode != 0:
             raise RuntimeError(f"{os.path.basename(binary)} failed ({r.returncode}): {r.stdout[-3000:]} {r.stderr[-3000:]}")
         with open(of, "rb") as f:
-            out = parse(f.read())
+            out = parse(f.read(), case.nvar)
     out["stdout"] = r.stdout
     return out
 

@@ -3,7 +3,8 @@
  * environment: AMRD's init_context reads the parameter file (amrd/io.c:36,
  * variable definitions and MG parameters), PAMR_compose_hierarchy builds
  * the AMR hierarchy (src/pamr.c:259), and u and the two sources are filled
- * on time level 1 of every AMR grid. Linked with the reference's C sources
+ * on time level 1 of every AMR grid (and the second elliptic variable w in
+ * coupled cases). Linked with the reference's C sources
  * (compiled here by tests/dropin/dropin.py from the reference tree, with the
  * oracle's single-rank shims) -- with amrd/mg.c for the golden run.
  *
@@ -47,7 +48,7 @@ int env_init(const char *case_path, const char *param_path)
    for (l = 1; l <= nlev; l++) {
       int valid = PAMR_init_s_iter(l, PAMR_AMRH, 0);
       const int gu = PAMR_get_gfn("u", PAMR_AMRH, 1), g0 = PAMR_get_gfn("rho", PAMR_AMRH, 1),
-                g1 = PAMR_get_gfn("rho1", PAMR_AMRH, 1);
+                g1 = PAMR_get_gfn("rho1", PAMR_AMRH, 1), gw_ = c.coupled ? PAMR_get_gfn("w", PAMR_AMRH, 1) : 0;
       while (valid) {
          int rank, dim, gw[6], ngfs, shape[3] = {1, 1, 1};
          double t, *x[3], bbox[6], *gfs[PAMR_MAX_GFNS];
@@ -58,6 +59,7 @@ int env_init(const char *case_path, const char *param_path)
             if (c.lev[i] == l && same_bbox(c.bbox + 6 * i, bbox, dim)) break;
          if (i == c.ngrids) return 4;
          memcpy(gfs[gu - 1], c.u[i], sizeof(double) * (size_t)n);
+         if (c.coupled) memcpy(gfs[gw_ - 1], c.w[i], sizeof(double) * (size_t)n);
          memcpy(gfs[g0 - 1], c.src0[i], sizeof(double) * (size_t)n);
          memcpy(gfs[g1 - 1], c.src1[i], sizeof(double) * (size_t)n);
          valid = PAMR_next_g();

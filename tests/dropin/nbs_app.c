@@ -3,7 +3,9 @@
  *
  * Its elliptic equation is the Newtonian boson star's potential,
  * V_xx + V_yy + V_zz - (phi_r^2 + phi_i^2) = 0 (examples/nbs/num.f:85-246),
- * with V = "u" and phi_r, phi_i = "rho", "rho1". Like examples/nbs/nbs.c it
+ * with V = "u" and phi_r, phi_i = "rho", "rho1"; or, in coupled cases, two
+ * elliptic variables u and w solved together (the coupled pair of
+ * oracle/mg_ops.h, sources "rho", "rho1"), whose hooks handle both. Like examples/nbs/nbs.c it
  * installs host hooks for relax / residual / L_op (here the checker's C
  * restatement of num.f, oracle/mg_ops.c), reads and writes its grids only
  * through the PAMR API, and calls the multigrid module through the
@@ -93,6 +95,8 @@ static void hlog_add(int kind, int L, double norm)
    nh++;
 }
 
+static int coupled;   /* two elliptic variables (u, w) */
+
 static double nbs_MG_relax(void)
 {
    cur g;
@@ -103,7 +107,12 @@ static double nbs_MG_relax(void)
    ogrid(&g, &o);
    src[0] = MGF("rho");
    src[1] = MGF("rho1");
-   n = oracle_relax(ORACLE_NBS, &o, MGF("u"), MGF("u_rhs"), src, MGF("cmask"));
+   if (coupled) {
+      double *v[2] = {MGF("u"), MGF("w")};
+      const double *r[2] = {MGF("u_rhs"), MGF("w_rhs")};
+      n = oracle_relax_n(ORACLE_COUPLED, &o, v, r, src, MGF("cmask"));
+   } else
+      n = oracle_relax(ORACLE_NBS, &o, MGF("u"), MGF("u_rhs"), src, MGF("cmask"));
    hlog_add(0, g.L, n);
    return n;
 }
@@ -118,7 +127,12 @@ static double nbs_MG_residual(void)
    ogrid(&g, &o);
    src[0] = MGF("rho");
    src[1] = MGF("rho1");
-   n = oracle_residual(ORACLE_NBS, &o, MGF("u_res"), MGF("u_rhs"), MGF("u"), src, MGF("cmask"));
+   if (coupled) {
+      double *rs[2] = {MGF("u_res"), MGF("w_res")};
+      const double *r[2] = {MGF("u_rhs"), MGF("w_rhs")}, *v[2] = {MGF("u"), MGF("w")};
+      n = oracle_residual_n(ORACLE_COUPLED, &o, rs, r, v, src, MGF("cmask"));
+   } else
+      n = oracle_residual(ORACLE_NBS, &o, MGF("u_res"), MGF("u_rhs"), MGF("u"), src, MGF("cmask"));
    hlog_add(1, g.L, n);
    return n;
 }
@@ -132,7 +146,12 @@ static void nbs_L_op(void)
    ogrid(&g, &o);
    src[0] = MGF("rho");
    src[1] = MGF("rho1");
-   oracle_lop(ORACLE_NBS, &o, MGF("u_lop"), MGF("u"), src, MGF("cmask"));
+   if (coupled) {
+      double *l[2] = {MGF("u_lop"), MGF("w_lop")};
+      const double *v[2] = {MGF("u"), MGF("w")};
+      oracle_lop_n(ORACLE_COUPLED, &o, l, v, src, MGF("cmask"));
+   } else
+      oracle_lop(ORACLE_NBS, &o, MGF("u_lop"), MGF("u"), src, MGF("cmask"));
 }
 
 static void nbs_var_clear(void) {}
@@ -176,6 +195,7 @@ int main(int argc, char **argv)
       mode = h[2];
       arg = h[3];
       L = h[4];
+      coupled = h[5];
    }
    if (env_init(argv[1], argv[2])) {
       fprintf(stderr, "nbs_app: environment set-up failed\n");
@@ -185,7 +205,11 @@ int main(int argc, char **argv)
    {
       /* the one line an application adds: its operator, for the device */
       char *src[2] = {"rho", "rho1"};
-      if (!amrd_set_device_MG_operator(2, src, "lap - (s0*s0 + s1*s1)", "j0")) return 4;
+      if (coupled) {   /* one operator per elliptic variable: u, then w */
+         if (!amrd_set_device_MG_operator(2, src, "lap - s0*(u - u1) - s1", "j0 - s0")) return 4;
+         if (!amrd_set_device_MG_var_operator(1, "lap - s0*(u - u0)", "j0 - s0")) return 4;
+      } else if (!amrd_set_device_MG_operator(2, src, "lap - (s0*s0 + s1*s1)", "j0"))
+         return 4;
       if (getenv("NBS_APP_MIXED") && !amrd_set_device_MG_precision(1)) return 4;
    }
 #endif
@@ -220,6 +244,7 @@ int main(int argc, char **argv)
    for (l = 1; l <= PAMR_get_max_lev(ABI_PAMR_AMRH); l++) {
       int valid = PAMR_init_s_iter(l, ABI_PAMR_AMRH, 0);
       const int gu = PAMR_get_gfn("u", ABI_PAMR_AMRH, 1), gc = PAMR_get_gfn("cmask", ABI_PAMR_AMRH, 1);
+      const int gw_ = coupled ? PAMR_get_gfn("w", ABI_PAMR_AMRH, 1) : 0;
       while (valid) {
          cur g;
          long n;
@@ -230,6 +255,7 @@ int main(int argc, char **argv)
          fwrite(g.bbox, 8, 6, fo);
          fwrite(g.gfs[gu - 1], 8, (size_t)n, fo);
          fwrite(g.gfs[gc - 1], 8, (size_t)n, fo);
+         if (coupled) fwrite(g.gfs[gw_ - 1], 8, (size_t)n, fo);
          valid = PAMR_next_g();
       }
    }

@@ -82,6 +82,9 @@ def dropin_cases():
         (W.nbs2d_uneven(seed=2, **small), 0, 0, 2),
         (W.nbs2d_uneven(seed=1, **small), 1, 4, 0),
         (W.nbs3d(17, 9, seed=4, levels=3), 1, 3, 0),
+        # two elliptic variables solved together (the coupled pair)
+        (W.coupled_from(W.nbs2d_uneven(seed=1, **small), seed=4), 0, 0, 1),
+        (W.coupled_from(W.nbs3d(17, 9, seed=0), seed=5), 0, 0, 1),
     ]
 
 
@@ -103,7 +106,10 @@ def save_dropin(case, mode, arg, level, out, path):
         fparams=np.array([p.tol, p.crtol, p.w0_r, p.w0_i]),
         mode=mode, arg=arg, level=level, iters=out["iters"], res=res, out_grids=og,
         out_u=np.concatenate([g["u"] for g in out["grids"]]),
-        out_cmask=np.concatenate([g["cmask"] for g in out["grids"]]).astype(np.uint8))
+        out_cmask=np.concatenate([g["cmask"] for g in out["grids"]]).astype(np.uint8),
+        # the second elliptic variable of a coupled case: initial, and as written
+        u1_0=np.concatenate(case.var(1)) if case.nvar > 1 else np.zeros(0),
+        out_w=np.concatenate([g["w"] for g in out["grids"]]) if case.nvar > 1 else np.zeros(0))
 
 
 def interp_cases():

@@ -44,6 +44,8 @@ def load_dropin(path: str):
     case = W.Case(str(z["name"]), int(z["pde"]), dim, tuple(int(v) for v in z["base_shape"]),
                   tuple(float(v) for v in z["base_bbox"]), grids, split(z["u0"]), split(z["src"]), params,
                   src_extra=[split(z["src1"])])
+    if "u1_0" in z.files and len(z["u1_0"]):   # a coupled case's second variable
+        case.u_extra = [split(z["u1_0"])]
     og, out = z["out_grids"], []
     off = 0
     for row in og:
@@ -51,6 +53,8 @@ def load_dropin(path: str):
         out.append({"level": int(row[0]), "shape": tuple(int(v) for v in row[1:4]),
                     "bbox": tuple(float(v) for v in row[4:10]), "u": z["out_u"][off:off + n].copy(),
                     "cmask": z["out_cmask"][off:off + n].astype(np.float64)})
+        if "out_w" in z.files and len(z["out_w"]):
+            out[-1]["w"] = z["out_w"][off:off + n].copy()
         off += n
     ref = {"iters": int(z["iters"]), "res": z["res"].copy(), "grids": out}
     return case, int(z["mode"]), int(z["arg"]), int(z["level"]), ref
