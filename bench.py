@@ -220,6 +220,19 @@ def measured_peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+# the FP32 sweep kernel of each value the mixed form's autotuner reports
+# (pgb_level_tuning's sweeps_per_launch), and the committed ncu summaries
+# that hold its DRAM bytes per launch on the workload's 129^3 level and on
+# the 385^3 grid
+SWEEP_KERNELS = {0: "k_relax32, one launch per colour pass", 1: "k_sweep32<1>, one sweep per launch",
+                 2: "k_sweep32<2>, two sweeps per launch", 3: "k_sweep32z, one-pass plane marching",
+                 4: "k_sweep32t<60>, TMA-staged one pass", 5: "k_sweep32t<28>, TMA-staged one pass",
+                 6: "k_sweep32t2<24>, TMA-staged, two sweeps per pass",
+                 7: "k_sweep32t2<56>, TMA-staged, two sweeps per pass"}
+SWEEP_PROFILE_129 = {5: "k_sweep32t_129cube_level.md", 6: "k_sweep32t2_129cube_level.md"}
+SWEEP_PROFILE_385 = {4: "k_sweep32t_385cube.md"}
+
+
 def ncu_traffic(summary: str):
     """DRAM bytes (read + write) per launch of a kernel, from a committed ncu
     summary under profiles/ (its line 'dram_bytes_per_launch: <n>'), or
@@ -748,19 +761,29 @@ def main():
     ms_sweep, bytes_sweep = smx.time_relax(big, reps=20)
     torch.cuda.nvtx.range_pop()
     ms64_sweep, bytes64_sweep = s64.time_relax(big, reps=10)
-    achieved = bytes_sweep / (ms_sweep / 1e3) / 1e9
+    tz, fuse = smx.level_tuning(big)
+    # a launch of the two-sweep kernels moves a sweep's algorithmic bytes
+    # (E read + write, D, C) once and runs two sweeps
+    per_launch = 2 if fuse in (2, 6, 7) and smx.case.params.pre_swp >= 2 else 1
+    ms_launch = per_launch * ms_sweep
+    achieved = bytes_sweep / (ms_launch / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    prof = SWEEP_PROFILE_129.get(fuse)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": ncu_traffic("k_sweep32t_129cube_level.md"), "peak_source": peak_kind,
-            "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level; k_sweep32t, TMA-staged one pass)",
-            "tuned": dict(zip(("tile_planes", "sweeps_per_launch"), smx.level_tuning(big))),
+            "frac": achieved / peak, "traffic": ncu_traffic(prof) if prof else None, "peak_source": peak_kind,
+            "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level; "
+                      + SWEEP_KERNELS.get(fuse, str(fuse)) + ")",
+            "tuned": {"tile_planes": tz, "sweeps_per_launch": fuse},
+            "sweeps_per_launch": per_launch, "ms_per_launch": ms_launch, "bytes_per_launch": bytes_sweep,
+            "sweep_equivalent_gbs": bytes_sweep / (ms_sweep / 1e3) / 1e9,
             "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep,
             "fp64_sweep": {"kernel": "k_relax (FP64 Newton-GS sweep, 129^3 level)",
                            "ms_per_sweep": ms64_sweep,
                            "achieved_gbs": bytes64_sweep / (ms64_sweep / 1e3) / 1e9}}
 
     roof["beyond_l2"] = sweep_beyond_l2(S, torch, np, peak)
-    roof["beyond_l2"]["traffic"] = ncu_traffic("k_sweep32t_385cube.md")
+    prof = SWEEP_PROFILE_385.get(roof["beyond_l2"]["tuned"]["sweeps_per_launch"])
+    roof["beyond_l2"]["traffic"] = ncu_traffic(prof) if prof else None
 
     # whole-solve roofline: algorithmic bytes of the cycles each form ran
     # (FP32 sweeps count 16 B per point, FP64 ones 32) over the timed solve

@@ -565,6 +565,7 @@ __global__ void __launch_bounds__(NT) k_sweep32z(const pgb_dbox *boxes, pgb_dlev
  * their whole interior relaxed (PGB_BOX_BDY_INTERIOR). */
 #define MT_R 8           /* ring slots (planes); the step loop is unrolled over them */
 #define MT_TYO 14        /* output rows per column */
+#define MT_NMAPS 16      /* tensor maps per box: 4 per column width (60, 28 one sweep; 24, 56 two) */
 
 __device__ __forceinline__ uint32_t mt_saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -630,8 +631,8 @@ __global__ void __launch_bounds__(mt_shape<TXO>::NTH, mt_shape<TXO>::MINB)
    const pgb_dbox *bp = boxes + tl.box;
    const int n0 = bp->n[0], n1 = bp->n[1], n2 = bp->n[2];
    const float ix = bp->fidx2[0], iy = bp->fidx2[1], iz = bp->fidx2[2], j0 = bp->fj0;
-   const CUtensorMap *me = maps + 8 * tl.box + (src == W_E2 ? 1 : 0), *md = maps + 8 * tl.box + 2,
-                     *mc = maps + 8 * tl.box + 3;
+   const CUtensorMap *me = maps + MT_NMAPS * tl.box + (src == W_E2 ? 1 : 0), *md = maps + MT_NMAPS * tl.box + 2,
+                     *mc = maps + MT_NMAPS * tl.box + 3;
    const int i0 = tl.i0, jb = tl.j0, kb = tl.k0, ke = min(tl.k0 + lv.mtz, n2);   /* planes [kb, ke) written */
    if (kb & 1) {   /* the unrolled colours assume an even first plane */
       if (threadIdx.x == 0) *err = 2;
@@ -739,9 +740,195 @@ __global__ void __launch_bounds__(mt_shape<TXO>::NTH, mt_shape<TXO>::MINB)
    }
 }
 
-/* Tensor maps of the TMA sweep: per box, for the output widths 60 and 28,
- * the old correction in slot 0 and slot 4, D and C (3-D tiles of the
- * padded FP32 arrays; out-of-box coordinates read as zero). */
+/* ----------------------------------- two sweeps per launch, TMA-staged -- */
+/* Two red-black sweeps of k_sweep32t's kind in one pass over memory: the
+ * second sweep trails the first by two planes inside the same CTA. A CTA
+ * owns an output column of TXO x TYO points; the first sweep runs on the
+ * column grown by 3 points (first colour) and 2 (second colour), the second
+ * on the column grown by 1 (first colour) and the column itself (second
+ * colour), so every value the second sweep reads is the first sweep's final
+ * value, computed identically by the CTAs that share it. E is staged grown
+ * by 4 points (TXO+8 x TYO+8), D and C by 3; plane slots live until the
+ * second sweep's last read of them (planes k-3 .. k+1 at step k), so loads
+ * run 4 planes ahead in the ring of 8.
+ *
+ * Each thread owns a point pair (x, x+1) of one row with x + y even, as in
+ * k_sweep32t, and at step k works on the member c of the first colour at
+ * plane k, which is also the first colour at k-2: first sweep, first
+ * colour at (c, k) and second colour at (c, k-1) (written back to its slot,
+ * where the second sweep reads it); second sweep, first colour at (c, k-2)
+ * from the first sweep's final values (its z neighbours (c, k-3) and
+ * (c, k-1) and its in-pair x neighbour are first-sweep second-colour values
+ * this thread computed in the last three steps, registers), then second
+ * colour at (c, k-3) (z neighbours and in-pair x neighbour: second-sweep
+ * first-colour values of the last three steps), and plane k-3 of the pair
+ * is final and stored from registers. Within a step no thread reads what
+ * another writes, so one barrier per step suffices. Every update is gs32,
+ * so the result equals two in-place sweeps of colour passes bit for bit.
+ * Waits are bounded as in k_sweep32t. */
+template <int TXO>
+struct mt2_shape {
+   static constexpr int PX = (TXO + 8) / 2, PY = MT_TYO + 6, NTH = PX * PY, HX = PX / 16;
+   static constexpr int EW = TXO + 8, EH = MT_TYO + 8, DH = MT_TYO + 6;
+   static constexpr int ESZ = (EW * EH + 31) / 32 * 32, DSZ = (EW * DH + 31) / 32 * 32;
+   static constexpr int SLOT = ESZ + 2 * DSZ;
+   static constexpr unsigned EBYTES = 4u * EW * EH, DBYTES = 4u * EW * DH;
+   static constexpr size_t SMEM = 4ul * MT_R * SLOT + 8ul * MT_R;
+   static constexpr int MINB = TXO >= 56 ? 1 : 3;
+   static_assert(PX % 16 == 0 && PY % 2 == 0, "half-warps hold 16 pairs of one row");
+};
+
+template <int TXO>
+__global__ void __launch_bounds__(mt2_shape<TXO>::NTH, mt2_shape<TXO>::MINB)
+   k_sweep32t2(const pgb_dbox *boxes, pgb_dlevel lv, const CUtensorMap *maps, int src, int dst, int *err)
+{
+   typedef mt2_shape<TXO> S;
+   constexpr int EW = S::EW, SL = S::SLOT, DO = S::ESZ - EW, CO = S::ESZ + S::DSZ - EW;
+   extern __shared__ __align__(128) float sm[];
+   uint64_t *bar = (uint64_t *)(sm + MT_R * SL);
+   const pgb_tile tl = lv.mtiles[blockIdx.x];
+   const pgb_dbox *bp = boxes + tl.box;
+   const int n0 = bp->n[0], n1 = bp->n[1], n2 = bp->n[2];
+   const float ix = bp->fidx2[0], iy = bp->fidx2[1], iz = bp->fidx2[2], j0 = bp->fj0;
+   const CUtensorMap *me = maps + MT_NMAPS * tl.box + (src == W_E2 ? 1 : 0), *md = maps + MT_NMAPS * tl.box + 2,
+                     *mc = maps + MT_NMAPS * tl.box + 3;
+   const int i0 = tl.i0, jb = tl.j0, kb = tl.k0, ke = min(tl.k0 + lv.mtz, n2);   /* planes [kb, ke) written */
+   if (kb & 1) {   /* the unrolled colours assume an even first plane */
+      if (threadIdx.x == 0) *err = 2;
+      return;
+   }
+   const int t = threadIdx.x, w = t >> 5;
+   const int tx = (w % S::HX) * 16 + (t & 15), ty = 2 * (w / S::HX) + ((t >> 4) & 1);
+   const int gy = jb - 3 + ty, xs = i0 - 4 + 2 * tx + (gy & 1);   /* the pair: (xs, xs+1) of row gy, xs + gy even */
+   float *const s0 = sm + (1 + ty) * EW + 2 * tx + (gy & 1);      /* the first member in slot 0's E plane */
+   const bool yin = gy >= 1 && gy <= n1 - 2;
+   const bool xin0 = yin && xs >= 1 && xs <= n0 - 2, xin1 = yin && xs >= 0 && xs <= n0 - 3;
+   /* the column grown by h points holds member x */
+   auto grown = [&](int x, int h) {
+      return x >= i0 - h && x <= i0 + TXO - 1 + h && gy >= jb - h && gy <= jb + MT_TYO - 1 + h;
+   };
+   const bool g3_0 = grown(xs, 3), g3_1 = grown(xs + 1, 3), g2_0 = grown(xs, 2), g2_1 = grown(xs + 1, 2);
+   const bool g1_0 = grown(xs, 1), g1_1 = grown(xs + 1, 1);
+   const bool out0 = grown(xs, 0) && xs < n0 && gy < n1, out1 = grown(xs + 1, 0) && xs + 1 < n0 && gy < n1;
+   float *gp = bp->w32[dst] + (out0 || out1 ? xs + bp->wy * gy : 0);
+   const long wz = bp->wz;
+   if (t == 0) {
+      for (int r = 0; r < MT_R; r++)
+         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mt_saddr(bar + r)), "r"(1) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   __syncthreads();
+   const int m0 = kb - 4, mlast = min(ke + 3, n2 - 1);
+   int last_issued = m0 - 1;
+   auto issue = [&](int m) {   /* thread 0 */
+      uint64_t *b = bar + ((m - m0) & (MT_R - 1));
+      last_issued = m;
+      if (m < 0 || m > mlast) {
+         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mt_saddr(b)) : "memory");
+         return;
+      }
+      float *sl = sm + ((m - m0) & (MT_R - 1)) * SL;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mt_saddr(b)),
+                   "r"(S::EBYTES + 2 * S::DBYTES) : "memory");
+      mt_load(sl, me, i0 - 4, jb - 4, m, b);
+      mt_load(sl + S::ESZ, md, i0 - 4, jb - 3, m, b);
+      mt_load(sl + S::ESZ + S::DSZ, mc, i0 - 4, jb - 3, m, b);
+   };
+   if (t == 0)
+      for (int m = m0; m < m0 + MT_R; m++) issue(m);
+   bool ok = true;
+   int waited = m0 - 1;
+   for (int q = m0; q <= min(kb - 3, mlast); q++) {   /* planes kb-4, kb-3 (slots 0, 1) */
+      if (q >= 0 && !mt_wait(bar + (q - m0), 0)) ok = false;
+      waited = q;
+   }
+   float zprev = s0[SL + 1], aprev = s0[0];
+   float rp1 = 0.f, rp2 = 0.f;   /* first sweep, first colour: (other member, k-1), (c, k-2) */
+   float b0 = 0.f, b1 = 0.f;     /* first sweep, second colour: (other member, k-2), (c, k-3) */
+   float q1 = 0.f, q2 = 0.f;     /* second sweep, first colour: (other member, k-3), (c, k-4) */
+   gp += wz * (long)(kb - 7);   /* advanced to plane k-3 at each step */
+
+   /* step s: plane k = kb - 3 + s, slot (s + 1) % R; colour member mem = s % 2 */
+   for (int sb = 0;; sb += MT_R) {
+      const uint32_t ph = (sb / MT_R) & 1;
+#pragma unroll
+      for (int u = 0; u < MT_R; u++) {
+         const int s = sb + u, k = kb - 3 + s;
+         if (k > ke + 2) return;
+         const int mem = u & 1;
+         const int jk = ((u + 1) & (MT_R - 1)) * SL, jm = (u & (MT_R - 1)) * SL, jp = ((u + 2) & (MT_R - 1)) * SL;
+         const int jm2 = ((u + MT_R - 1) & (MT_R - 1)) * SL, jm3 = ((u + MT_R - 2) & (MT_R - 1)) * SL;
+         if (k + 1 <= mlast) {
+            if (!mt_wait(bar + ((u + 2) & (MT_R - 1)), ph ^ (u + 2 >= MT_R ? 1u : 0u))) ok = false;
+            waited = k + 1;
+         }
+         float *pc = s0 + mem;
+         const bool xin = mem ? xin1 : xin0;
+         /* first sweep, first colour at (c, k) */
+         const float ec = pc[jk], ea = zprev, ezm = aprev;
+         const float eb = mem ? pc[jk + 1] : pc[jk - 1];
+         const float zp = pc[jp];
+         float rk = gs32(ec, mem ? ea : eb, mem ? eb : ea, pc[jk - EW], pc[jk + EW], ezm, zp, pc[jk + CO],
+                         pc[jk + DO], ix, iy, iz, j0, true);
+         if (!(xin && k >= 1 && k <= n2 - 2)) rk = ec;
+         if (mem ? g3_1 : g3_0) pc[jk] = rk;
+         /* first sweep, second colour at (c, k-1), kept in its slot */
+         float bk = ezm;
+         if (s >= 2) {
+            const float fb = mem ? pc[jm + 1] : pc[jm - 1];
+            bk = gs32(ezm, mem ? rp1 : fb, mem ? fb : rp1, pc[jm - EW], pc[jm + EW], rp2, rk, pc[jm + CO], pc[jm + DO],
+                      ix, iy, iz, j0, true);
+            if (!(xin && k >= 2 && k <= n2 - 1)) bk = ezm;
+            if (mem ? g2_1 : g2_0) pc[jm] = bk;
+         }
+         /* second sweep, first colour at (c, k-2) */
+         float q = 0.f;
+         gp += wz;
+         if (s >= 4) {
+            const float old = pc[jm2];
+            const float fb2 = mem ? pc[jm2 + 1] : pc[jm2 - 1];
+            q = gs32(old, mem ? b0 : fb2, mem ? fb2 : b0, pc[jm2 - EW], pc[jm2 + EW], b1, bk, pc[jm2 + CO],
+                     pc[jm2 + DO], ix, iy, iz, j0, true);
+            if (!(xin && k >= 3 && k <= n2)) q = old;
+            if (mem ? g1_1 : g1_0) pc[jm2] = q;
+         }
+         /* second sweep, second colour at (c, k-3); plane k-3 is final */
+         if (s >= 6 && k - 3 < ke) {
+            const float fb3 = mem ? pc[jm3 + 1] : pc[jm3 - 1];
+            float b2 = gs32(b1, mem ? q1 : fb3, mem ? fb3 : q1, pc[jm3 - EW], pc[jm3 + EW], q2, q, pc[jm3 + CO],
+                            pc[jm3 + DO], ix, iy, iz, j0, true);
+            if (!(xin && k >= 4 && k <= n2 + 1)) b2 = b1;
+            if (out0) gp[0] = mem ? q1 : b2;
+            if (out1) gp[1] = mem ? b2 : q1;
+         }
+         zprev = zp;
+         aprev = ea;
+         rp2 = rp1;
+         rp1 = rk;
+         b1 = b0;
+         b0 = bk;
+         q2 = q1;
+         q1 = q;
+         if (!ok) *err = 1;
+         if (__syncthreads_or(!ok)) {   /* a load never landed: let the issued ones land, return */
+            if (t == 0)
+               for (int qq = max(waited + 1, 0); qq <= min(mlast, last_issued); qq++)
+                  mt_wait(bar + ((qq - m0) & (MT_R - 1)), ((qq - m0) / MT_R) & 1);
+            return;
+         }
+         /* plane k-3's slot is free: every thread is past step k */
+         if (t == 0 && s >= 2) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k - 3 + MT_R);
+         }
+      }
+   }
+}
+
+/* Tensor maps of the TMA sweeps: per box, for the column widths 60 and 28
+ * (one sweep per launch) and 24 and 56 (two), the old correction in slot 0
+ * and slot 4, D and C (3-D tiles of the padded FP32 arrays; out-of-box
+ * coordinates read as zero). */
 #include <cudaTypedefs.h>
 
 static int mt_encode(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap *m, const float *base, const pgb_dbox &b,
@@ -756,7 +943,7 @@ static int mt_encode(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap *m, cons
    return r != CUDA_SUCCESS;
 }
 
-/* builds 8 maps per box (widths 60, 28 x slot 0, slot 4, D, C) in device
+/* builds MT_NMAPS maps per box (widths 60, 28, 24, 56 x slot 0, slot 4, D, C) in device
  * memory; returns 0, or 1 when the driver has no tensor-map encoder or a
  * box is not 3-D (the TMA sweep is then not offered) */
 extern "C" int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps)
@@ -774,7 +961,7 @@ extern "C" int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps)
       }
       enc = (PFN_cuTensorMapEncodeTiled_v12000)fn;
    }
-   CUtensorMap *h = (CUtensorMap *)calloc((size_t)nbox * 8, sizeof(CUtensorMap));
+   CUtensorMap *h = (CUtensorMap *)calloc((size_t)nbox * MT_NMAPS, sizeof(CUtensorMap));
    int bad = 0;
    for (int i = 0; i < nbox && !bad; i++) {
       const pgb_dbox &b = hbox[i];
@@ -782,18 +969,19 @@ extern "C" int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps)
          bad = 1;
          break;
       }
-      const int txo[2] = {60, 28};
-      for (int v = 0; v < 2 && !bad; v++) {
-         CUtensorMap *m = h + 8 * i + 4 * v;
+      /* E grown by 2 rows (one sweep) or 4 (two), D and C by 1 or 3 */
+      const int txo[4] = {60, 28, 24, 56}, grow[4] = {2, 2, 4, 4};
+      for (int v = 0; v < 4 && !bad; v++) {
+         CUtensorMap *m = h + MT_NMAPS * i + 4 * v;
          const int w = txo[v] + 8;
-         bad |= mt_encode(enc, m + 0, b.w32[W_E], b, w, MT_TYO + 4);
-         bad |= mt_encode(enc, m + 1, b.w32[W_E2], b, w, MT_TYO + 4);
-         bad |= mt_encode(enc, m + 2, b.w32[W_D], b, w, MT_TYO + 2);
-         bad |= mt_encode(enc, m + 3, b.w32[W_C], b, w, MT_TYO + 2);
+         bad |= mt_encode(enc, m + 0, b.w32[W_E], b, w, MT_TYO + 2 * grow[v]);
+         bad |= mt_encode(enc, m + 1, b.w32[W_E2], b, w, MT_TYO + 2 * grow[v]);
+         bad |= mt_encode(enc, m + 2, b.w32[W_D], b, w, MT_TYO + 2 * grow[v] - 2);
+         bad |= mt_encode(enc, m + 3, b.w32[W_C], b, w, MT_TYO + 2 * grow[v] - 2);
       }
    }
-   if (!bad && cudaMalloc(d_maps, sizeof(CUtensorMap) * 8 * (size_t)nbox) == cudaSuccess)
-      bad = cudaMemcpy(*d_maps, h, sizeof(CUtensorMap) * 8 * (size_t)nbox, cudaMemcpyHostToDevice) != cudaSuccess;
+   if (!bad && cudaMalloc(d_maps, sizeof(CUtensorMap) * MT_NMAPS * (size_t)nbox) == cudaSuccess)
+      bad = cudaMemcpy(*d_maps, h, sizeof(CUtensorMap) * MT_NMAPS * (size_t)nbox, cudaMemcpyHostToDevice) != cudaSuccess;
    else
       bad = 1;
    free(h);
@@ -806,8 +994,9 @@ extern "C" int pgb_tmaps_build(const pgb_dbox *hbox, int nbox, void **d_maps)
    return 0;
 }
 
-/* one TMA sweep of level lv from slot src into slot dst; maps from
- * pgb_tmaps_build, txo the output width the level's tile list was made for */
+/* one TMA sweep of level lv from slot src into slot dst (two with the
+ * column widths 24 and 56); maps from pgb_tmaps_build, lv.mtx the column
+ * width the level's tile list was made for */
 static int sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const void *maps, int src, int dst, int *err,
                     cudaStream_t st)
 {
@@ -816,16 +1005,20 @@ static int sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const void *maps, int 
    if (!attr) {
       cudaFuncSetAttribute(k_sweep32t<60>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt_shape<60>::SMEM);
       cudaFuncSetAttribute(k_sweep32t<28>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt_shape<28>::SMEM);
+      cudaFuncSetAttribute(k_sweep32t2<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt2_shape<24>::SMEM);
+      cudaFuncSetAttribute(k_sweep32t2<56>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mt2_shape<56>::SMEM);
       attr = 1;
    }
-   /* the maps of width 60 sit at 8 i + 0..3, of width 28 at 8 i + 4..7 */
+   /* per box, the maps of width 60 sit at MT_NMAPS i + 0..3, 28 at 4..7, 24 at 8..11, 56 at 12..15 */
    const CUtensorMap *m = (const CUtensorMap *)maps;
    if (lv.mtx == 60)
-      k_sweep32t<60><<<lv.nmtiles, mt_shape<60>::NTH, mt_shape<60>::SMEM, st>>>(
-         boxes, lv, m, src, dst, err);
+      k_sweep32t<60><<<lv.nmtiles, mt_shape<60>::NTH, mt_shape<60>::SMEM, st>>>(boxes, lv, m, src, dst, err);
+   else if (lv.mtx == 28)
+      k_sweep32t<28><<<lv.nmtiles, mt_shape<28>::NTH, mt_shape<28>::SMEM, st>>>(boxes, lv, m + 4, src, dst, err);
+   else if (lv.mtx == 24)
+      k_sweep32t2<24><<<lv.nmtiles, mt2_shape<24>::NTH, mt2_shape<24>::SMEM, st>>>(boxes, lv, m + 8, src, dst, err);
    else
-      k_sweep32t<28><<<lv.nmtiles, mt_shape<28>::NTH, mt_shape<28>::SMEM, st>>>(
-         boxes, lv, m + 4, src, dst, err);
+      k_sweep32t2<56><<<lv.nmtiles, mt2_shape<56>::NTH, mt2_shape<56>::SMEM, st>>>(boxes, lv, m + 12, src, dst, err);
    return check32("sweep32t");
 }
 
@@ -1649,7 +1842,9 @@ extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, co
 
 /* nsweep FP32 sweeps of level L: fuse = 0 two global-memory colour passes
  * per sweep (in place, slot W_E); 1 or 2 = sweeps per launch of the
- * shared-memory kernel, 3 = the one-pass marching kernel (3-D). The fused
+ * shared-memory kernel, 3 = the one-pass marching kernel (3-D), 4 or 5 =
+ * the TMA-staged sweep, 6 or 7 = two TMA-staged sweeps per launch (an odd
+ * last sweep runs alone in the shared-memory kernel). The fused
  * kernels read one slot and write the other; *slot says where the
  * correction starts and, on return, where it ends, which the block's
  * consumers (sync, defect, update) read. */
@@ -1674,9 +1869,10 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
    }
    /* fused launches alternate between the two correction slots */
    while (done < nsweep) {
-      if ((fuse == 4 || fuse == 5) && lv.dim == 3 && lv.tmaps && lv.nmtiles) {
+      if ((fuse == 4 || fuse == 5 || ((fuse == 6 || fuse == 7) && nsweep - done >= 2)) && lv.dim == 3 && lv.tmaps &&
+          lv.nmtiles) {
          if (sweep32t(boxes, lv, lv.tmaps, src, dst, lv.err, (cudaStream_t)stream)) return 1;
-         done += 1;
+         done += fuse >= 6 ? 2 : 1;
          const int t = src;
          src = dst;
          dst = t;

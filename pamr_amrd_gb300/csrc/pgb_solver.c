@@ -840,8 +840,14 @@ static int sync_vars(pgb_solver *s, const pgb_plan *p, int f)
  * 4 to 64 planes deep, and keeps the fastest. No choice changes a
  * computed value (the sweeps are the same Gauss-Seidel sweeps; only the
  * norm's summation order follows the tiles). PGB_AUTOTUNE=0 keeps the
- * defaults; PGB_SWEEP_FUSE=0..5 forces one sweep kernel on every level
- * (PGB_SWEEP_MTZ=4/8/16/32/64 the TMA columns' depth with 4 or 5). */
+ * defaults; PGB_SWEEP_FUSE=0..7 forces one sweep kernel on every level
+ * (PGB_SWEEP_MTZ=4/8/16/32/64 the TMA columns' depth with 4 to 7). */
+/* the column width of the TMA sweep kernels f = 4..7 */
+static int mtx_of(int f)
+{
+   return f == 4 ? 60 : f == 5 ? 28 : f == 6 ? 24 : 56;
+}
+
 static int autotune(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
@@ -849,17 +855,18 @@ static int autotune(pgb_solver *s)
    int L, changed = 0;
    int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
    s->tuned = 1;
-   if (force && force[0] >= '0' && force[0] <= '5' && !force[1]) {
+   if (force && force[0] >= '0' && force[0] <= '7' && !force[1]) {
       /* one sweep shape on every level instead of the measured choice */
       for (L = 2; L <= h->nlev; L++) {
          int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
          int f = force[0] - '0';
          if (f == 3 && h->dim != 3) f = 1;
-         if ((f == 4 || f == 5) && !level_tma_ok(s, L)) f = 1;
+         if (f >= 6 && !can_fuse) f -= 2;
+         if (f >= 4 && !level_tma_ok(s, L)) f = 1;
          s->fuse[L] = f == 2 && !can_fuse ? 1 : f;
-         if (f == 4 || f == 5) {
+         if (f >= 4) {
             const char *mz = getenv("PGB_SWEEP_MTZ");
-            s->mtx[L] = f == 4 ? 60 : 28;
+            s->mtx[L] = mtx_of(f);
             s->mtz[L] = mz && (!strcmp(mz, "4") || !strcmp(mz, "8") || !strcmp(mz, "16") || !strcmp(mz, "32") ||
                                !strcmp(mz, "64"))
                            ? atoi(mz)
@@ -884,13 +891,14 @@ static int autotune(pgb_solver *s)
             changed = 1;
          }
          /* candidates: f < 4 once each; the TMA-staged sweep (f 4, 5: columns
-          * 60 or 28 wide) with columns of 4 to 64 planes */
-         for (int c = 0; c <= (h->dim == 3 ? 13 : can_fuse ? 2 : 1); c++) {
+          * 60 or 28 wide) and two of them per launch (f 6, 7: columns 24 or
+          * 56 wide) with columns of 4 to 64 planes */
+         for (int c = 0; c <= (h->dim == 3 ? 23 : can_fuse ? 2 : 1); c++) {
             f = c < 4 ? c : 4 + (c - 4) / 5;
-            if (f == 2 && !can_fuse) continue;
+            if ((f == 2 || f >= 6) && !can_fuse) continue;
             if (f >= 4) {
                if (!tma) continue;
-               s->mtx[L] = f == 4 ? 60 : 28;
+               s->mtx[L] = mtx_of(f);
                s->mtz[L] = mzs[(c - 4) % 5];
                if (level_tables(s, L, tzs[a])) return 10;
                changed = 1;

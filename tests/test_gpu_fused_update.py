@@ -32,7 +32,7 @@ def _run(monkeypatch, case, off, fuse):
     return r["iters"], r["res"].copy(), u
 
 
-@pytest.mark.parametrize("fuse", ["1", "2", "5"])
+@pytest.mark.parametrize("fuse", ["1", "2", "5", "6"])
 @pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=2),
                                   lambda: W.poisson2d_uneven(seed=1, n=129, levels=5, min_boxes=8, max_boxes=24),
                                   lambda: W.lapse2d_bo(65, seed=2, levels=4),

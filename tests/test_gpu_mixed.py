@@ -86,17 +86,17 @@ def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
     assert max(float(np.max(np.abs(a - b))) for a, b in zip(u1, u2)) <= 1e-12 * umax
 
 
-@pytest.mark.parametrize("fuse", ["1", "2", "3", "4", "5"])
+@pytest.mark.parametrize("fuse", ["1", "2", "3", "4", "5", "6", "7"])
 @pytest.mark.parametrize("make", [lambda: W.conformal3d(65, 33, seed=1),
                                   lambda: W.lapse2d_bo(129, seed=1, levels=4, step=40),
                                   lambda: W.poisson3d(129, seed=3)],
                          ids=["c3d65", "lapse129", "p3d129"])
 def test_fused_sweeps_equal_colour_passes(monkeypatch, make, fuse):
     """Sweeps fused in shared memory (one or two per launch, one marching
-    through the planes, or one marching with TMA-staged planes in columns 60
-    or 28 wide) read the old correction from one buffer and write the
-    other: the solution is that of the in-place colour passes bit for bit,
-    on every repetition."""
+    through the planes, one marching with TMA-staged planes in columns 60
+    or 28 wide, or two marching in columns 24 or 56 wide) read the old
+    correction from one buffer and write the other: the solution is that of
+    the in-place colour passes bit for bit, on every repetition."""
     case = make()
     case.params.precision = 1
 
@@ -119,3 +119,34 @@ def test_fused_sweeps_equal_colour_passes(monkeypatch, make, fuse):
         assert i1 == i2
         for a, b in zip(u1, u2):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("fuse,mtz,swp", [("6", "4", (3, 2)), ("7", "64", (2, 3)), ("6", "16", (4, 4)),
+                                          ("7", "8", (1, 1))])
+def test_two_sweep_columns_equal_colour_passes(monkeypatch, fuse, mtz, swp):
+    """Two TMA-staged sweeps per launch over columns of 4 to 64 planes, with
+    odd sweep counts (the last sweep of a block then runs alone in the
+    shared-memory kernel) and a single sweep per block: bit for bit the
+    in-place colour passes."""
+    case = W.conformal3d(65, 33, seed=4)
+    case.params.precision = 1
+    case.params.pre_swp, case.params.pst_swp = swp
+
+    def run(env):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        s = Solver(copy.deepcopy(case))
+        s.set_inputs()
+        r = s.solve()
+        out = (r["iters"], r["res"].copy(), s.get_u())
+        s.close()
+        for k in env:
+            monkeypatch.delenv(k)
+        return out
+
+    i1, r1, u1 = run({"PGB_SWEEP_FUSE": fuse, "PGB_SWEEP_MTZ": mtz})
+    i2, r2, u2 = run({"PGB_AUTOTUNE": "0"})
+    assert i1 == i2
+    assert np.array_equal(r1, r2)
+    for a, b in zip(u1, u2):
+        assert np.array_equal(a, b)
