@@ -762,11 +762,11 @@ def main():
     torch.cuda.nvtx.range_pop()
     ms64_sweep, bytes64_sweep = s64.time_relax(big, reps=10)
     tz, fuse = smx.level_tuning(big)
-    # a launch of the two-sweep kernels moves a sweep's algorithmic bytes
-    # (E read + write, D, C) once and runs two sweeps
+    # algorithmic bytes count 16 B per relaxed point per sweep; a launch of
+    # the two-sweep kernels runs two sweeps (and streams E, D and C once)
     per_launch = 2 if fuse in (2, 6, 7) and smx.case.params.pre_swp >= 2 else 1
     ms_launch = per_launch * ms_sweep
-    achieved = bytes_sweep / (ms_launch / 1e3) / 1e9
+    achieved = per_launch * bytes_sweep / (ms_launch / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     prof = SWEEP_PROFILE_129.get(fuse)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -774,8 +774,7 @@ def main():
             "kernel": "FP32 red+black sweep on the correction as the V-cycle runs it (129^3 level; "
                       + SWEEP_KERNELS.get(fuse, str(fuse)) + ")",
             "tuned": {"tile_planes": tz, "sweeps_per_launch": fuse},
-            "sweeps_per_launch": per_launch, "ms_per_launch": ms_launch, "bytes_per_launch": bytes_sweep,
-            "sweep_equivalent_gbs": bytes_sweep / (ms_sweep / 1e3) / 1e9,
+            "sweeps_per_launch": per_launch, "ms_per_launch": ms_launch, "bytes_per_launch": per_launch * bytes_sweep,
             "ms_per_sweep": ms_sweep, "bytes_per_sweep": bytes_sweep,
             "fp64_sweep": {"kernel": "k_relax (FP64 Newton-GS sweep, 129^3 level)",
                            "ms_per_sweep": ms64_sweep,
