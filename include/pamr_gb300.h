@@ -276,7 +276,10 @@ int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
  * pgb_prepare: tile depth in planes, and the FP32 sweep kernel (0 = one
  * launch per colour pass, 1 or 2 = sweeps per launch staged in shared
  * memory, 3 = one sweep per launch in one pass over memory, marching
- * through the tile's planes; 3-D levels); no reference counterpart. */
+ * through the tile's planes, 4 or 5 = one sweep per launch with planes
+ * staged by TMA in columns 60 or 28 points wide, 6 or 7 = two sweeps per
+ * launch staged by TMA in columns 24 or 56 points wide; 3-7 on 3-D levels
+ * only); no reference counterpart. */
 int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per_launch);
 
 /* Norm trace: when enabled, every norm a hook would return is recorded

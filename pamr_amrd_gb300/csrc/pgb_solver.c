@@ -941,7 +941,7 @@ int pgb_level_tuning(pgb_solver *s, int L, int *tile_planes, int *sweeps_per_lau
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (L < 1 || L > s->h.nlev) return fail(3, "level %d out of range", L);
    if (tile_planes) *tile_planes = s->lv[L].tz;
-   if (sweeps_per_launch)   /* 0: one launch per colour pass; 3: one-pass z-marching sweep */
+   if (sweeps_per_launch)   /* the sweep mode (pamr_gb300.h lists them) */
       *sweeps_per_launch = (s->fuse[L] == 2 && (s->h.sync[L][0].nops || s->h.sync[L][1].nops)) ? 1 : s->fuse[L];
    return 0;
 }
