@@ -848,6 +848,41 @@ static int mtx_of(int f)
    return f == 4 ? 60 : f == 5 ? 28 : f == 6 ? 24 : 56;
 }
 
+/* Time one candidate as the V-cycle runs it: eight smoothing blocks of `nsw`
+ * sweeps, each with its residual pass, captured into a graph and replayed
+ * (one warm-up replay, one timed). Timing direct launches instead would
+ * measure the host's launch rate on small levels, where a launch's kernel
+ * time is a few microseconds. */
+static int time_candidate(pgb_solver *s, int L, int nsw, int f, float *ms)
+{
+   const pgb_hier *h = &s->h;
+   cudaGraph_t g = 0;
+   cudaGraphExec_t ge = 0;
+   int r, bad = 0;
+   CU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+   for (r = 0; r < 8 && !bad; r++) {
+      int slot = PGB_W32_E;
+      bad = pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, &slot, s->stream) ||
+            pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0, 0, s->stream);
+   }
+   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+   if (bad) {
+      if (g) cudaGraphDestroy(g);
+      return fail(11, "%s", pgb_dev_error32());
+   }
+   if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+   if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
+   if (e == cudaSuccess) e = cudaEventRecord(s->ev0, s->stream);
+   if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
+   if (e == cudaSuccess) e = cudaEventRecord(s->ev1, s->stream);
+   if (e == cudaSuccess) e = cudaEventSynchronize(s->ev1);
+   if (e == cudaSuccess) e = cudaEventElapsedTime(ms, s->ev0, s->ev1);
+   if (ge) cudaGraphExecDestroy(ge);
+   if (g) cudaGraphDestroy(g);
+   if (e != cudaSuccess) return fail(10, "autotuner graph: %s", cudaGetErrorString(e));
+   return 0;
+}
+
 static int autotune(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
@@ -904,17 +939,7 @@ static int autotune(pgb_solver *s)
                changed = 1;
             }
             float ms = 0;
-            int r;
-            for (r = 0; r < 9; r++) {   /* one warm-up, eight timed */
-               if (r == 1) CU(cudaEventRecord(s->ev0, s->stream));
-               int slot = PGB_W32_E;
-               KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsw, f, &slot, s->stream));
-               KC32(pgb_k_residual_fast(s->dbox, s->lv[L], h->pde, s->sc, norm_slot(s, L, N_RESID), 0, 0,
-                                        s->stream));
-            }
-            CU(cudaEventRecord(s->ev1, s->stream));
-            CU(cudaEventSynchronize(s->ev1));
-            CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            if (time_candidate(s, L, nsw, f, &ms)) return 10;
             if (ms < best) {
                best = ms;
                best_tz = s->lv[L].tz;
