@@ -282,6 +282,16 @@ int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
  * only); no reference counterpart. */
 int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per_launch);
 
+/* Mixed form: MG levels 1..n (the return value; 0 when none) whose V-cycle
+ * passes run as one launch of the small-level kernel, a thread-block
+ * cluster of *cluster_ctas CTAs (levels of at most PGB_TAIL_POINTS points,
+ * 6000 unless set). Off unless the environment sets PGB_TAIL=1 (it gives
+ * the same bits and was measured slower than one launch per pass on
+ * GB300); pgb_level_tuning reports sweep mode 8 for those levels. Known
+ * after the first pgb_prepare. No reference counterpart (the reference
+ * relaxes grid by grid on the host). */
+int pgb_tail_levels(const pgb_solver *s, int *cluster_ctas);
+
 /* Norm trace: when enabled, every norm a hook would return is recorded
  * (kind 0 relax, 1 residual, 2 = skipped coarsest iterations; level; box;
  * repeat; norm) -- the device counterpart of MG_trace (amrd/mg.c:138-195). */

@@ -50,7 +50,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda = cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OBJ, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "pamr_gb300.h"))
     jobs, objs = [], []
     for src, extra in CU_SOURCES.items():

@@ -142,6 +142,63 @@ int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_
 int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                          pgb_coarsest_args a, pgb_trace *trace, void *stream);
 
+/* The small-level kernel (mixed form). The V-cycle's passes over its small
+ * levels (residual, restriction, FAS right-hand side, colour passes, defect
+ * carry and update, coarsest-grid loop, coarse-grid correction and
+ * interpolation) are recorded, not launched, while recording is on: each
+ * launcher above appends a step with its arguments and launch geometry.
+ * pgb_k_tail then runs every step in one launch of one thread-block
+ * cluster, the cluster's CTAs sharing each step's blocks and meeting at a
+ * cluster barrier between steps. The program travels as the kernel's
+ * parameter (it stays in the launch, or in the graph node that captured
+ * it). Each step runs the body of the kernel it replaces, so every value is
+ * the same bit for bit. */
+#define PGB_TAIL_MAXLEV 8
+#define PGB_TAIL_MAXSTEP 224
+typedef struct {
+   unsigned char kind, lev, bar, solo;  /* step kind, index into lv[], barrier after it (0 none,
+                                           1 the cluster's, 2 CTA 0's), run by CTA 0 alone */
+   int a[6];                            /* integer arguments of the kernel it replaces */
+   int gx, gy, gz;                      /* that kernel's grid */
+   const void *ptr;                     /* op list or gate */
+   double d;                            /* w0_r or 1/w0_i */
+} pgb_tail_step;
+
+typedef struct {
+   int nstep, nlev, pde, ncsync;
+   size_t smem;                         /* dynamic shared memory (the coarsest-grid loop) */
+   size_t prog_off;                     /* where the kernel keeps its copy of this program in shared
+                                           memory (after the coarsest loop's), 0: read in place */
+   size_t smem_total;                   /* dynamic shared memory of the launch */
+   int nbox_copy;                       /* boxes of the box table copied to shared memory (0: none) */
+   int grid;                            /* 0: one cluster (hardware barrier); 1: one CTA per SM in a
+                                           cooperative launch, meeting at a counter in global memory */
+   unsigned int *bar_cnt;               /* that counter (zeroed before each launch) */
+   int *err;                            /* set to 4 when a wait at it runs out (about 0.5 s) */
+   pgb_dlevel lv[PGB_TAIL_MAXLEV];
+   pgb_coarsest_args ca;                /* the coarsest-grid loop's arguments */
+   const pgb_copy_op *csync;            /* and its sync ops */
+   pgb_tail_step step[PGB_TAIL_MAXSTEP];
+} pgb_tail_prog;
+
+void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox);
+/* steps recorded from now on run in CTA 0 alone (levels so small that one
+ * CTA's L1 holds them: consecutive such steps meet at a CTA barrier) */
+void pgb_tail_set_solo(int on);
+/* stops recording; 1 when a pass could not be recorded (pgb_dev_error32 says which) */
+int pgb_tail_end(void);
+int pgb_tail_recording(void);
+/* the FP64-file passes (pgb_kernels64.cu) while recording */
+int pgb_tail_add_restrict(const pgb_plan *p, int field_mask, int res32);
+int pgb_tail_add_clear(pgb_dlevel lv, int mask);
+/* runs a recorded program on a cluster of ncta CTAs */
+int pgb_k_tail(const pgb_dbox *boxes, const pgb_tail_prog *p, int ncta, pgb_scratch sc, void *stream);
+/* CTAs of a launch in grid mode: one per SM */
+int pgb_tail_grid_ctas(void);
+/* the largest cluster (16, 8, 4, 2 or 1 CTAs) the device schedules for the
+ * small-level kernel with smem bytes of dynamic shared memory; 0 if none */
+int pgb_tail_max_cluster(size_t smem);
+
 #ifdef __cplusplus
 }
 #endif

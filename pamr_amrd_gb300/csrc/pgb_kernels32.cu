@@ -34,9 +34,12 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
 #include "pgb_dev.h"
 #include "pgb_opgrid.cuh"
 #include "pgb_op.cuh"
+#include "pgb_weights.cuh"
 
 static __thread char g_err32[256];
 static unsigned long long g_launches32 = 0;
@@ -56,7 +59,31 @@ static int check32(const char *what)
 
 extern "C" const char *pgb_dev_error32(void) { return g_err32; }
 
+/* the small-level kernel's program being recorded (per host thread), 0 when
+ * not recording (pgb_dev.h, pgb_tail_begin) */
+static __thread pgb_tail_prog *g_tp = 0;
+static __thread int g_tp_bad = 0, g_tp_solo = 0;
+
+/* a pass the small-level kernel does not run: recording fails */
+static int tail_refuse(void)
+{
+   g_tp_bad = 2;
+   return 1;
+}
+
 #define NT (PGB_TX * PGB_TY)
+
+/* Pointers a kernel body reads or writes through: restrict-qualified in the
+ * standalone kernels, plain in the small-level kernel (k_tail), where one
+ * step writes what another step of the same launch reads, so the loads must
+ * stay on the coherent path. */
+template <bool TAIL, class X> struct rp {
+   typedef X *__restrict__ t;
+};
+template <class X> struct rp<true, X> {
+   typedef X *t;
+};
+#define RP(X) typename rp<TAIL, X>::t
 
 /* launches the instantiation of an operator kernel for the level
  * operator's form: compiled built-in (PROG = false) or program (true) */
@@ -98,19 +125,20 @@ __device__ __forceinline__ bool relaxed32(const pgb_dbox &b, int i, int j, int k
 
 /* Plane split of a level's tiles: a kernel over lv.ntiles x split CTAs
  * gives CTA b the planes [k0, k0 + nk) of tile b / split (split divides
- * the tile depth). Levels with few tiles (a 65^3 box in tiles of 8 planes
+ * the tile depth; bx is the CTA's index, blockIdx.x in a standalone launch).
+ * Levels with few tiles (a 65^3 box in tiles of 8 planes
  * is 243 CTAs for 152 SMs) get enough CTAs to hide load latency. */
 struct tile_part {
    pgb_tile tl;
    int kk0, nk;   /* first plane within the tile, planes */
 };
 
-__device__ __forceinline__ tile_part tile_split(const pgb_tile *tiles, const pgb_dlevel &lv, int split)
+__device__ __forceinline__ tile_part tile_split(const pgb_tile *tiles, const pgb_dlevel &lv, int split, int bx)
 {
    tile_part t;
-   t.tl = tiles[blockIdx.x / split];
+   t.tl = tiles[bx / split];
    const int kz = lv.dim == 3 ? lv.tz : 1, per = kz / split;
-   t.kk0 = (blockIdx.x % split) * per;
+   t.kk0 = (bx % split) * per;
    t.nk = per;
    return t;
 }
@@ -221,23 +249,23 @@ __device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, doub
  * E is 0 on entry (every block ends by clearing it). With cover = 1 only
  * the level's cover tiles are visited: elsewhere rhs stays 0 and D is the
  * FP32 update k_defect32 made at the end of the previous post-smoothing. */
-template <bool PROG>
-__global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                   double w0_r, int cover, int split)
+template <bool PROG, bool TAIL>
+__device__ __forceinline__ void fas_defect_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
+                                             double w0_r, int cover, int split)
 {
-   const tile_part tp = tile_split(cover ? lv.ctiles : lv.tiles, lv, split);
+   const tile_part tp = tile_split(cover ? lv.ctiles : lv.tiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const double *__restrict__ u = b.f[PGB_F_U];
-   const double *__restrict__ src = b.f[PGB_F_SRC];
-   const double *__restrict__ res = b.f[PGB_F_RES];
-   double *__restrict__ rhs = b.f[PGB_F_RHS];
-   double *__restrict__ lop = b.f[PGB_F_LOP];
-   float *__restrict__ wd = b.w32[W_D];
-   float *__restrict__ wc = b.w32[W_C];
+   RP(const double) u = b.f[PGB_F_U];
+   RP(const double) src = b.f[PGB_F_SRC];
+   RP(const double) res = b.f[PGB_F_RES];
+   RP(double) rhs = b.f[PGB_F_RHS];
+   RP(double) lop = b.f[PGB_F_LOP];
+   RP(float) wd = b.w32[W_D];
+   RP(float) wc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int ks = tl.k0 + tp.kk0;
    if (ks >= b.n[2]) return;
@@ -269,6 +297,13 @@ __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dl
    }
 }
 
+template <bool PROG>
+__global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                   double w0_r, int cover, int split)
+{
+   fas_defect_b<PROG, false>(hw_blk(), boxes, lv, pde, w0_r, cover, split);
+}
+
 /* The Gauss-Seidel update of one point of lap E + C E = D, FP32, written
  * with explicit roundings so that every kernel that relaxes (colour passes
  * from global memory, fused sweeps in shared memory) computes the same
@@ -289,14 +324,15 @@ __device__ __forceinline__ float gs32(float ec, float xm, float xp, float ym, fl
  * global memory (the level's E, D, C stay in L2 between passes); relax
  * tiles are 64 points wide, a thread updates one point of the active colour
  * per row (parity as num.f:220) */
-__global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, int pass)
+template <bool TAIL>
+__device__ __forceinline__ void relax32_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pass)
 {
-   const pgb_tile tl = lv.rtiles[blockIdx.x];
+   const pgb_tile tl = lv.rtiles[vb.x];
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
-   float *__restrict__ e = b.w32[W_E];
-   const float *__restrict__ dd = b.w32[W_D];
-   const float *__restrict__ cc = b.w32[W_C];
+   RP(float) e = b.w32[W_E];
+   RP(const float) dd = b.w32[W_D];
+   RP(const float) cc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1], wy = b.wy, wz = b.wz;
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
    const float j0 = b.fj0;
@@ -315,6 +351,11 @@ __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dleve
       e[q] = gs32(e[q], e[q - 1], e[q + 1], e[q - wy], e[q + wy], d3 ? e[q - wz] : 0.f, d3 ? e[q + wz] : 0.f,
                   cc[q], dd[q], ix, iy, iz, j0, d3);
    }
+}
+
+__global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, int pass)
+{
+   relax32_b<false>(hw_blk(), boxes, lv, pass);
 }
 
 /* The same sweeps staged in shared memory: NS red-black sweeps in one launch.
@@ -1024,22 +1065,28 @@ static int sweep32t(const pgb_dbox *boxes, pgb_dlevel lv, const void *maps, int 
 
 /* E = the correction in slot src, over the level's tiles (the end of an
  * odd number of fused sweep launches) */
-__global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel lv, int src)
+template <bool TAIL>
+__device__ __forceinline__ void copy_e_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int src)
 {
-   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_tile tl = lv.tiles[vb.x];
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int kz = lv.dim == 3 ? lv.tz : 1;
-   const float *__restrict__ a = eslot(b, src);
-   float *__restrict__ e = b.w32[W_E];
+   RP(const float) a = eslot(b, src);
+   RP(float) e = b.w32[W_E];
    for (int kk = 0; kk < kz; kk++) {
       const int k = tl.k0 + kk;
       if (k >= b.n[2]) break;
       const long q = wq(b, i, j, k);
       e[q] = a[q];
    }
+}
+
+__global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel lv, int src)
+{
+   copy_e_b<false>(hw_blk(), boxes, lv, src);
 }
 
 /* D = D - (lap E + C E) at the relaxed points, FP32, before the update that
@@ -1050,7 +1097,7 @@ __global__ void __launch_bounds__(NT) k_copy_e(const pgb_dbox *boxes, pgb_dlevel
 /* D - (lap E + C E) at point q of E (rows of pitch wy, planes wz): the one
  * expression of the FP32 defect carry, shared by k_defect32 and
  * k_update_defect so that both round alike */
-__device__ __forceinline__ float defect32_at(const float *__restrict__ e, long q, long wy, long wz, float c,
+__device__ __forceinline__ float defect32_at(const float *e, long q, long wy, long wz, float c,
                                              float d, float ix, float iy, float iz, int dim)
 {
    const float ec = e[q];
@@ -1059,19 +1106,20 @@ __device__ __forceinline__ float defect32_at(const float *__restrict__ e, long q
    return d - (t + c * ec);
 }
 
-__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split,
-                                                 const int *gate, int gval)
+template <bool TAIL>
+__device__ __forceinline__ void defect32_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int slot,
+                                           int split, const int *gate, int gval)
 {
    if (gate && *gate != gval) return;   /* the cycle parity leaves this pass out */
-   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const float *__restrict__ e = eslot(b, slot);
-   const float *__restrict__ cc = b.w32[W_C];
-   float *__restrict__ dd = b.w32[W_D];
+   RP(const float) e = eslot(b, slot);
+   RP(const float) cc = b.w32[W_C];
+   RP(float) dd = b.w32[W_D];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
 #pragma unroll
@@ -1084,6 +1132,12 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
    }
 }
 
+__global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, int split,
+                                                 const int *gate, int gval)
+{
+   defect32_b<false>(hw_blk(), boxes, lv, slot, split, gate, gval);
+}
+
 /* End of a smoothing block: u += E (FP64, E from the slot the sweeps
  * ended in) and E = 0 in slot zslot, where the next block starts (the same
  * slot costs no extra traffic). After an
@@ -1092,18 +1146,19 @@ __global__ void __launch_bounds__(NT) k_defect32(const pgb_dbox *boxes, pgb_dlev
  * plus whatever a sync of E brought in: u += res + (E - d2f(res)), exactly
  * res when E still holds the d2f(res) the interpolation wrote (the fused
  * sweeps copy unrelaxed points from slot to slot). */
-__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
-                                               int zslot, int split)
+template <bool TAIL>
+__device__ __forceinline__ void update_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int post,
+                                         int slot, int zslot, int split)
 {
-   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   double *__restrict__ u = b.f[PGB_F_U];
+   RP(double) u = b.f[PGB_F_U];
    const float *es = eslot(b, slot);
    float *e = eslot(b, zslot);
-   const double *__restrict__ res = b.f[PGB_F_RES];
+   RP(const double) res = b.f[PGB_F_RES];
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
       const int k = tl.k0 + tp.kk0 + kk;
@@ -1119,26 +1174,33 @@ __global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel
    }
 }
 
+__global__ void __launch_bounds__(NT) k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
+                                               int zslot, int split)
+{
+   update_b<false>(hw_blk(), boxes, lv, post, slot, zslot, split);
+}
+
 /* k_defect32 and k_update in one pass, for blocks whose update zeroes the
  * other slot (zslot != slot): the defect reads E's stencil in slot while
  * the update writes zeros only to zslot. The defect part runs unless the
  * cycle parity gate leaves it out (gate && *gate != gval); with defect = 0
  * this is k_update. Same arithmetic as the two kernels. */
-__global__ void __launch_bounds__(NT) k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
-                                                      int zslot, int split, int defect, const int *gate, int gval)
+template <bool TAIL>
+__device__ __forceinline__ void update_defect_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int post,
+                                                int slot, int zslot, int split, int defect, const int *gate, int gval)
 {
-   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
    const bool dfx = defect && (!gate || *gate == gval);
-   double *__restrict__ u = b.f[PGB_F_U];
-   const float *__restrict__ es = eslot(b, slot);
-   float *__restrict__ ez = eslot(b, zslot);
-   const double *__restrict__ res = b.f[PGB_F_RES];
-   const float *__restrict__ cc = b.w32[W_C];
-   float *__restrict__ dd = b.w32[W_D];
+   RP(double) u = b.f[PGB_F_U];
+   RP(const float) es = eslot(b, slot);
+   RP(float) ez = eslot(b, zslot);
+   RP(const double) res = b.f[PGB_F_RES];
+   RP(const float) cc = b.w32[W_C];
+   RP(float) dd = b.w32[W_D];
    const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
 #pragma unroll
    for (int kk = 0; kk < PGB_TZ; kk++) {
@@ -1155,6 +1217,12 @@ __global__ void __launch_bounds__(NT) k_update_defect(const pgb_dbox *boxes, pgb
       u[p] += corr;
       ez[q] = 0.f;
    }
+}
+
+__global__ void __launch_bounds__(NT) k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int post, int slot,
+                                                      int zslot, int split, int defect, const int *gate, int gval)
+{
+   update_defect_b<false>(hw_blk(), boxes, lv, post, slot, zslot, split, defect, gate, gval);
 }
 
 /* zero the four FP32 arrays (pgb_prepare) */
@@ -1289,10 +1357,10 @@ __device__ __forceinline__ double wsum64m(int n, const double *c, const double *
 
 /* Coarse half of the coarse-grid correction (amrd/mg.c:332-341) on the tiles
  * the interpolation reads: res = (f - lop)/w0_i in FP64, X = RN32(res). */
-__global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0,
-                                                  int split)
+__device__ __forceinline__ void cgc_mixed_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv,
+                                            double inv_w0, int split)
 {
-   const tile_part tp = tile_split(lv.ctiles, lv, split);
+   const tile_part tp = tile_split(lv.ctiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
@@ -1308,11 +1376,18 @@ __global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dle
    }
 }
 
+__global__ void __launch_bounds__(NT) k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_w0,
+                                                  int split)
+{
+   cgc_mixed_b(hw_blk(), boxes, lv, inv_w0, split);
+}
+
 /* FP64 interpolation of the coarse res at window point (a, bb, c) of op o
  * (dminterp3d's line order: i, then j, then k) */
+template <bool TAIL>
 __device__ __noinline__ double interp_point64(const pgb_interp_op &o, const pgb_dbox &s, int a, int bb, int c, int dim)
 {
-   const double *__restrict__ u = s.f[PGB_F_RES];
+   RP(const double) u = s.f[PGB_F_RES];
    int ax[4], ay[4], az[4];
    double cx[4], cy[4], cz[4], kv[4];
    const int nx = stencil64m(o.i2b - 1 + a, o.irho, o.nii, o.ord, ax, cx);
@@ -1340,14 +1415,16 @@ __device__ __noinline__ double interp_point64(const pgb_interp_op &o, const pgb_
  * small fraction of the FP32 rate, so FP64 points are kept in dense warps:
  * on boxes whose interior is all relaxed this kernel leaves the face rows
  * and the two x-ends of the other rows to k_interp_edges. */
-__global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim, int slot)
+template <bool TAIL>
+__device__ __forceinline__ void interp_mixed_b(const vblk &vb, const pgb_dbox *boxes, const pgb_interp_op *ops, int dim,
+                                               int slot)
 {
-   const pgb_interp_op o = ops[blockIdx.z];
+   const pgb_interp_op o = ops[vb.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    const bool allrel = d.flags & PGB_BOX_BDY_INTERIOR;
-   const float *__restrict__ x = s.w32[W_X];
-   for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
+   RP(const float) x = s.w32[W_X];
+   for (int row = vb.y; row < o.njb * o.nkb; row += vb.gy) {
       const int bb = row % o.njb, c = row / o.njb;
       const int fj = o.j2 + bb, fk = o.k2 + c;
       const bool face = fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]));
@@ -1356,7 +1433,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
       const int ny = stencil32(o.j2b - 1 + bb, o.irho, o.nji, o.ord, ay, cy);
       const int nz = dim == 3 ? stencil32(o.k2b - 1 + c, o.irho, o.nki, o.ord, az, cz) : 1;
       if (dim != 3) az[0] = 0;
-      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+      for (int a = vb.x * vb.nt + vb.lt; a < o.nib; a += vb.gx * vb.nt) {
          const int fi = o.i2 + a;
          const long pd = lin32(d, fi, fj, fk), pw = lin32w(d, fi, fj, fk);
          bool fp64;
@@ -1366,7 +1443,7 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
          } else
             fp64 = !relaxed32(d, fi - 1, fj - 1, fk - 1, pd, dim);
          if (fp64) {
-            const double v = interp_point64(o, s, a, bb, c, dim);
+            const double v = interp_point64<TAIL>(o, s, a, bb, c, dim);
             d.f[PGB_F_RES][pd] = v;
             eslot(d, slot)[pw] = d2f(v);
             continue;
@@ -1388,23 +1465,29 @@ __global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, 
    }
 }
 
+__global__ void k_interp_mixed(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim, int slot)
+{
+   interp_mixed_b<false>(hw_blk(), boxes, ops, dim, slot);
+}
+
 /* k_interp_mixed for ops of ratio 2 and linear order (every MG hierarchy
  * with the default interpolation): the FP32 value of a fine point is the mean
  * of its (up to 8 distinct) coarse corners, counted with multiplicity. */
-__global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim,
-                                                         int slot)
+template <bool TAIL>
+__device__ __forceinline__ void interp_lin2_b(const vblk &vb, const pgb_dbox *boxes, const pgb_interp_op *ops, int dim,
+                                              int slot)
 {
-   const pgb_interp_op o = ops[blockIdx.z];
+   const pgb_interp_op o = ops[vb.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    const bool allrel = d.flags & PGB_BOX_BDY_INTERIOR;
-   const float *__restrict__ x = s.w32[W_X];
-   float *__restrict__ e = eslot(d, slot);
-   double *__restrict__ res = d.f[PGB_F_RES];
+   RP(const float) x = s.w32[W_X];
+   RP(float) e = eslot(d, slot);
+   RP(double) res = d.f[PGB_F_RES];
    const long sny = s.n[0], snz = (long)s.n[0] * s.n[1];
    const long dny = d.n[0], dnz = (long)d.n[0] * d.n[1];
    const long swy = s.wy, swz = s.wz, dwy = d.wy, dwz = d.wz;   /* FP32 pitches */
-   for (int row = blockIdx.y; row < o.njb * o.nkb; row += gridDim.y) {
+   for (int row = vb.y; row < o.njb * o.nkb; row += vb.gy) {
       const int bb = row % o.njb, c = row / o.njb;
       const int fj = o.j2 + bb, fk = o.k2 + c;
       const bool face = fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]));
@@ -1416,7 +1499,7 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
       const long oyw = (ty & 1) ? swy : 0, ozw = (tz & 1) ? swz : 0;
       const long rowcw = (o.j1i - 1 + (ty >> 1)) * swy + (dim == 3 ? (o.k1i - 1 + (tz >> 1)) * swz : 0);
       const long rowfw = (long)(fj - 1) * dwy + (long)(fk - 1) * dwz;
-      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+      for (int a = vb.x * vb.nt + vb.lt; a < o.nib; a += vb.gx * vb.nt) {
          const int fi = o.i2 + a;
          const long pd = rowf + fi - 1, pw = rowfw + fi - 1;
          const int tx = o.i2b - 1 + a, ox = tx & 1;
@@ -1438,17 +1521,25 @@ __global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, c
    }
 }
 
+__global__ void __launch_bounds__(128, 8) k_interp_lin2(const pgb_dbox *boxes, const pgb_interp_op *ops, int dim,
+                                                         int slot)
+{
+   interp_lin2_b<false>(hw_blk(), boxes, ops, dim, slot);
+}
+
 /* The FP64 points of ops into boxes whose interior is all relaxed: the rows
  * on a box face (j or k at the box boundary), blockIdx.y < 2*(njb+nkb)
  * picking the face and the row on it, and, for the remaining blockIdx.y,
  * the two x-ends (fi = 1, n) of the other rows, one per thread. */
-__global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, int dim, int slot)
+template <bool TAIL>
+__device__ __forceinline__ void interp_edges_b(const vblk &vb, const pgb_interp_op *ops, const pgb_dbox *boxes, int dim,
+                                               int slot)
 {
-   const pgb_interp_op o = ops[blockIdx.z];
+   const pgb_interp_op o = ops[vb.z];
    const pgb_dbox &s = boxes[o.src_box];
    const pgb_dbox &d = boxes[o.dst_box];
    if (!(d.flags & PGB_BOX_BDY_INTERIOR)) return;
-   const int y = blockIdx.y, nface = 2 * (o.njb + o.nkb);
+   const int y = vb.y, nface = 2 * (o.njb + o.nkb);
    if (y < nface) {
       int bb, c;
       if (y < 2 * o.nkb) {
@@ -1464,17 +1555,17 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
       }
       if (bb < 0 || bb >= o.njb || c < 0 || c >= o.nkb) return;
       const int fj = o.j2 + bb, fk = o.k2 + c;
-      for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < o.nib; a += gridDim.x * blockDim.x) {
+      for (int a = vb.x * vb.nt + vb.lt; a < o.nib; a += vb.gx * vb.nt) {
          const long pd = lin32(d, o.i2 + a, fj, fk);
-         const double v = interp_point64(o, s, a, bb, c, dim);
+         const double v = interp_point64<TAIL>(o, s, a, bb, c, dim);
          d.f[PGB_F_RES][pd] = v;
          eslot(d, slot)[lin32w(d, o.i2 + a, fj, fk)] = d2f(v);
       }
       return;
    }
-   if (blockIdx.x) return;
+   if (vb.x) return;
    const int rows = o.njb * o.nkb;
-   for (int q = (y - nface) * blockDim.x + threadIdx.x; q < 2 * rows; q += (gridDim.y - nface) * blockDim.x) {
+   for (int q = (y - nface) * vb.nt + vb.lt; q < 2 * rows; q += (vb.gy - nface) * vb.nt) {
       const int row = q >> 1;
       const int a = (q & 1) ? d.n[0] - o.i2 : 1 - o.i2;
       if (a < 0 || a >= o.nib) continue;
@@ -1482,10 +1573,15 @@ __global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, 
       const int fj = o.j2 + bb, fk = o.k2 + c;
       if (fj == 1 || fj == d.n[1] || (dim == 3 && (fk == 1 || fk == d.n[2]))) continue;
       const long pd = lin32(d, o.i2 + a, fj, fk);
-      const double v = interp_point64(o, s, a, bb, c, dim);
+      const double v = interp_point64<TAIL>(o, s, a, bb, c, dim);
       d.f[PGB_F_RES][pd] = v;
       eslot(d, slot)[lin32w(d, o.i2 + a, fj, fk)] = d2f(v);
    }
+}
+
+__global__ void k_interp_edges(const pgb_interp_op *ops, const pgb_dbox *boxes, int dim, int slot)
+{
+   interp_edges_b<false>(hw_blk(), ops, boxes, dim, slot);
 }
 
 __device__ double block_sum32(double v, double *sm)
@@ -1507,24 +1603,24 @@ __device__ double block_sum32(double v, double *sm)
  * relaxed points, D = -res and C for the next smoothing block of this
  * level, and call_rr_app's norm (per-box RMS, max over boxes) reduced by the
  * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
-template <bool PROG>
-__global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                      pgb_scratch sc, double *norm_out,
-                                                      pgb_trace *trace, int split, const int *gate)
+template <bool PROG, bool TAIL>
+__device__ __forceinline__ void residual_fast_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
+                                                const pgb_scratch &sc, double *norm_out, pgb_trace *trace, int split,
+                                                const int *gate)
 {
    if (gate && *gate) return;   /* the cycle parity leaves this pass out (no norm is read then) */
    __shared__ double sm[32];
    __shared__ int last;
-   const tile_part tp = tile_split(lv.tiles, lv, split);
+   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
    const pgb_tile tl = tp.tl;
    const pgb_dbox b = boxes[tl.box];
    const int dim = lv.dim;
-   const double *__restrict__ u = b.f[PGB_F_U];
-   const double *__restrict__ rhs = b.f[PGB_F_RHS];
-   const double *__restrict__ src = b.f[PGB_F_SRC];
-   double *__restrict__ res = b.f[PGB_F_RES];
-   float *__restrict__ wd = b.w32[W_D];
-   float *__restrict__ wc = b.w32[W_C];
+   RP(const double) u = b.f[PGB_F_U];
+   RP(const double) rhs = b.f[PGB_F_RHS];
+   RP(const double) src = b.f[PGB_F_SRC];
+   RP(double) res = b.f[PGB_F_RES];
+   RP(float) wd = b.w32[W_D];
+   RP(float) wc = b.w32[W_C];
    const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    double acc = 0;
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
@@ -1551,11 +1647,11 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    }
    if (!norm_out) return;
    acc = block_sum32(acc, sm);
-   if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[blockIdx.x] = acc;
+   if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[vb.x] = acc;
    __threadfence();
    __syncthreads();
    if (threadIdx.x == 0 && threadIdx.y == 0)
-      last = (atomicAdd(sc.counter, 1u) == gridDim.x * gridDim.y - 1);
+      last = (atomicAdd(sc.counter, 1u) == (unsigned)(vb.gx * vb.gy) - 1);
    __syncthreads();
    if (!last) return;
    /* call_rr_app: per-box RMS, max over boxes */
@@ -1587,13 +1683,21 @@ __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb
    }
 }
 
+template <bool PROG>
+__global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                      pgb_scratch sc, double *norm_out,
+                                                      pgb_trace *trace, int split, const int *gate)
+{
+   residual_fast_b<PROG, false>(hw_blk(), boxes, lv, pde, sc, norm_out, trace, split, gate);
+}
+
 /* L_op + compute_MG_rhs (amrd/mg.c:271-314) on the cover tiles of the
  * coarsest level, which the coarsest-grid loop smooths by itself */
 template <bool PROG>
-__global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                     double w0_r)
+__device__ __forceinline__ void lop_rhs_fast_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
+                                               double w0_r)
 {
-   const pgb_tile tl = lv.ctiles[blockIdx.x];
+   const pgb_tile tl = lv.ctiles[vb.x];
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
@@ -1613,6 +1717,13 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
       b.f[PGB_F_RHS][p] = cm ? fma(-b.f[PGB_F_RES][p], w0_r, lopv) : 0.0;
       b.f[PGB_F_LOP][p] = u[p];
    }
+}
+
+template <bool PROG>
+__global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                     double w0_r)
+{
+   lop_rhs_fast_b<PROG>(hw_blk(), boxes, lv, pde, w0_r);
 }
 
 /* The coarsest-grid loop of the mixed form (amrd/mg.c:172-190: relax the
@@ -1635,14 +1746,14 @@ __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_
 #define CM_MAXB 16
 #define CMT 256
 template <bool PROG>
-__global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
-                                                        const pgb_copy_op *sync_ops, int nsync,
-                                                        pgb_coarsest_args a, pgb_trace *trace)
+__device__ __forceinline__ void coarsest_mixed_b(const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
+                                                 const pgb_copy_op *sync_ops, int nsync, const pgb_coarsest_args &a,
+                                                 pgb_trace *trace, int t)
 {
    extern __shared__ double dsm[];
    __shared__ double sm[32];
    __shared__ int cb[CM_MAXB], coff[CM_MAXB + 1], ncol[CM_MAXB][2], ncb_s;
-   const int t = threadIdx.x, dim = lv.dim;
+   const int dim = lv.dim;
    const bool d3 = dim == 3;
    if (t == 0) {
       int n = 0, o = 0;
@@ -1797,11 +1908,20 @@ __global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, p
    }
 }
 
+template <bool PROG>
+__global__ void __launch_bounds__(CMT) k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
+                                                        const pgb_copy_op *sync_ops, int nsync,
+                                                        pgb_coarsest_args a, pgb_trace *trace)
+{
+   coarsest_mixed_b<PROG>(boxes, lv, pde, sync_ops, nsync, a, trace, threadIdx.x);
+}
+
 /* the cycle parity: 0 -> 1 -> 0 ... at the end of each mixed V-cycle */
 __global__ void k_flip(int *parity) { *parity ^= 1; }
 
 extern "C" int pgb_k_flip(int *parity, void *stream)
 {
+   if (g_tp) return tail_refuse();
    k_flip<<<1, 1, 0, (cudaStream_t)stream>>>(parity);
    return check32("flip");
 }
@@ -1818,6 +1938,355 @@ __global__ void k_solve_step(cudaGraphConditionalHandle h, const double *norm, d
    cudaGraphSetConditional(h, ((k + 1 < min_iter || r > tol) && k + 1 < max_iter) ? 1u : 0u);
 }
 
+/* ----------------------------------------------------- small-level kernel -- */
+/* The passes of the V-cycle over the small levels (pgb_dev.h: pgb_tail_prog)
+ * as steps of one launch. One thread-block cluster of up to 16 CTAs of
+ * 32 x 8 threads runs them in order: the CTAs share each step's blocks (the
+ * blocks of the standalone launch the step replaces, strided over the
+ * cluster), the coarsest-grid loop runs in CTA 0 as it does alone, and a
+ * cluster barrier (release/acquire at cluster scope) separates a step from
+ * the next one that reads what it wrote. Every CTA runs every step and
+ * every barrier: the program is a kernel parameter, the same for all, and no
+ * thread leaves early. On the small levels each standalone launch costs
+ * more than its work; a cluster barrier costs about 0.2 us. */
+enum {
+   TS_FAS, TS_RELAX, TS_COPYE, TS_DEFECT, TS_UPDATE, TS_UPDDEF, TS_RESID, TS_LOPRHS, TS_CGC, TS_LIN2, TS_IMIX,
+   TS_EDGES, TS_RESTRICT, TS_CLEAR, TS_COARSEST
+};
+
+__device__ __forceinline__ void cluster_barrier()
+{
+   asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;\n" ::: "memory");
+}
+
+/* grid mode: every CTA adds one to the counter and waits until it reaches
+ * target (the k-th barrier of a launch waits for k x the CTAs); the wait is
+ * bounded (about 0.5 s of globaltimer), after which it sets *err and goes on */
+__device__ __forceinline__ void grid_barrier(unsigned int *cnt, unsigned int target, int *err)
+{
+   __syncthreads();
+   if (threadIdx.x == 0 && threadIdx.y == 0) {
+      __threadfence();
+      atomicAdd(cnt, 1u);
+      unsigned long long t0 = 0;
+      for (int spin = 0;; spin++) {
+         unsigned int v;
+         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+         if (v >= target) break;
+         if (spin == 64) t0 = mt_ns();
+         if (spin > 64 && mt_ns() - t0 > 500000000ull) {
+            atomicExch(err, 4);
+            break;
+         }
+      }
+   }
+   __syncthreads();
+}
+
+template <bool PROG>
+__global__ void __launch_bounds__(NT, 1) k_tail(const pgb_dbox *boxes, const __grid_constant__ pgb_tail_prog Pk,
+                                                pgb_scratch sc)
+{
+   const int lt = threadIdx.x + PGB_TX * threadIdx.y;
+   const pgb_tail_prog *Pp = &Pk;
+   if (Pk.prog_off) {
+      /* the program, the box table and the levels' tile and box lists in
+       * shared memory: a step's blocks then reach their tile and box without
+       * a trip to L2 before their first data load */
+      extern __shared__ __align__(16) unsigned char tail_sm[];
+      pgb_tail_prog *c = (pgb_tail_prog *)(tail_sm + Pk.prog_off);
+      const long long *from = (const long long *)&Pk;
+      long long *to = (long long *)c;
+      for (int i = lt; i < (int)(sizeof(pgb_tail_prog) / 8); i += NT) to[i] = from[i];
+      __syncthreads();   /* before thread 0 points the copy's levels at their lists */
+      unsigned char *q = tail_sm + Pk.prog_off + (sizeof(pgb_tail_prog) + 15) / 16 * 16;
+      if (Pk.nbox_copy) {
+         const int *bf = (const int *)boxes;
+         int *bt = (int *)q;
+         for (int i = lt; i < (int)(Pk.nbox_copy * sizeof(pgb_dbox) / 4); i += NT) bt[i] = bf[i];
+         boxes = (const pgb_dbox *)q;
+         q += (Pk.nbox_copy * sizeof(pgb_dbox) + 15) / 16 * 16;
+      }
+      for (int li = 0; li < Pk.nlev; li++) {
+         const pgb_dlevel &g = Pk.lv[li];
+         const int *src[4] = {(const int *)g.tiles, (const int *)g.rtiles, (const int *)g.ctiles, g.box};
+         const int nw[4] = {g.ntiles * (int)(sizeof(pgb_tile) / 4), g.nrtiles * (int)(sizeof(pgb_tile) / 4),
+                            g.nctiles * (int)(sizeof(pgb_tile) / 4), g.nbox};
+         for (int a = 0; a < 4; a++) {
+            int *d = (int *)q;
+            for (int i = lt; i < nw[a]; i += NT) d[i] = src[a][i];
+            if (lt == 0) {
+               if (a == 0) c->lv[li].tiles = (const pgb_tile *)d;
+               else if (a == 1) c->lv[li].rtiles = (const pgb_tile *)d;
+               else if (a == 2) c->lv[li].ctiles = (const pgb_tile *)d;
+               else c->lv[li].box = d;
+            }
+            q += ((size_t)nw[a] * 4 + 15) / 16 * 16;
+         }
+      }
+      __syncthreads();
+      Pp = c;
+   }
+   const pgb_tail_prog &P = *Pp;
+   unsigned int nbar = 0;
+   for (int s = 0; s < P.nstep; s++) {
+      const pgb_tail_step &st = P.step[s];
+      const pgb_dlevel &lv = P.lv[st.lev];
+      if (st.kind == TS_COARSEST) {
+         if (blockIdx.x == 0) coarsest_mixed_b<PROG>(boxes, lv, P.pde, P.csync, P.ncsync, P.ca, 0, lt);
+      } else if (!st.solo || blockIdx.x == 0) {
+         const int nv = st.gx * st.gy * st.gz, v0 = st.solo ? 0 : blockIdx.x, dv = st.solo ? 1 : gridDim.x;
+         for (int v = v0; v < nv; v += dv) {
+            vblk vb;
+            vb.x = v % st.gx;
+            vb.y = (v / st.gx) % st.gy;
+            vb.z = v / (st.gx * st.gy);
+            vb.gx = st.gx;
+            vb.gy = st.gy;
+            vb.gz = st.gz;
+            vb.lt = lt;
+            vb.nt = NT;
+            switch (st.kind) {
+            case TS_FAS: fas_defect_b<PROG, true>(vb, boxes, lv, P.pde, st.d, st.a[0], st.a[1]); break;
+            case TS_RELAX: relax32_b<true>(vb, boxes, lv, st.a[0]); break;
+            case TS_COPYE: copy_e_b<true>(vb, boxes, lv, st.a[0]); break;
+            case TS_DEFECT: defect32_b<true>(vb, boxes, lv, st.a[0], st.a[1], (const int *)st.ptr, st.a[2]); break;
+            case TS_UPDATE: update_b<true>(vb, boxes, lv, st.a[0], st.a[1], st.a[2], st.a[3]); break;
+            case TS_UPDDEF:
+               update_defect_b<true>(vb, boxes, lv, st.a[0], st.a[1], st.a[2], st.a[3], st.a[4], (const int *)st.ptr,
+                                     st.a[5]);
+               break;
+            case TS_RESID:
+               residual_fast_b<PROG, true>(vb, boxes, lv, P.pde, sc, 0, 0, st.a[0], (const int *)st.ptr);
+               break;
+            case TS_LOPRHS: lop_rhs_fast_b<PROG>(vb, boxes, lv, P.pde, st.d); break;
+            case TS_CGC: cgc_mixed_b(vb, boxes, lv, st.d, st.a[0]); break;
+            case TS_LIN2: interp_lin2_b<true>(vb, boxes, (const pgb_interp_op *)st.ptr, st.a[0], st.a[1]); break;
+            case TS_IMIX: interp_mixed_b<true>(vb, boxes, (const pgb_interp_op *)st.ptr, st.a[0], st.a[1]); break;
+            case TS_EDGES: interp_edges_b<true>(vb, (const pgb_interp_op *)st.ptr, boxes, st.a[0], st.a[1]); break;
+            case TS_RESTRICT: restrict_b(vb, boxes, (const pgb_restrict_op *)st.ptr, st.a[0], st.a[1]); break;
+            case TS_CLEAR: clear_b(vb, boxes, lv, st.a[0]); break;
+            default: break;
+            }
+         }
+      }
+      if (st.bar == 1) {
+         if (P.grid)
+            grid_barrier(P.bar_cnt, ++nbar * gridDim.x, P.err);
+         else
+            cluster_barrier();
+      } else if (st.bar == 2 && blockIdx.x == 0)   /* between two steps of CTA 0 alone */
+         __syncthreads();
+   }
+}
+
+
+extern "C" void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox)
+{
+   memset(p, 0, sizeof(*p));
+   p->pde = pde;
+   p->nbox_copy = nbox;
+   g_tp = p;
+   g_tp_bad = 0;
+   g_tp_solo = 0;
+}
+
+extern "C" void pgb_tail_set_solo(int on) { g_tp_solo = on != 0; }
+
+extern "C" int pgb_tail_end(void)
+{
+   pgb_tail_prog *P = g_tp;
+   g_tp = 0;
+   /* barriers: CTA 0's own between two of its solo steps, the cluster's
+    * wherever work changes hands (and after the last step nothing) */
+   if (P && !g_tp_bad && !getenv("PGB_TAIL_GLOBALPROG")) {
+      /* shared memory: the coarsest loop's, then the program, the box table
+       * (unless it is large) and the levels' tile and box lists */
+      size_t q = (P->smem + 15) / 16 * 16 + 16;
+      P->prog_off = q;
+      q += (sizeof(pgb_tail_prog) + 15) / 16 * 16;
+      if ((size_t)P->nbox_copy * sizeof(pgb_dbox) > 48 * 1024) P->nbox_copy = 0;
+      q += ((size_t)P->nbox_copy * sizeof(pgb_dbox) + 15) / 16 * 16;
+      for (int li = 0; li < P->nlev; li++) {
+         const pgb_dlevel &g = P->lv[li];
+         q += ((size_t)g.ntiles * sizeof(pgb_tile) + 15) / 16 * 16 + ((size_t)g.nrtiles * sizeof(pgb_tile) + 15) / 16 * 16 +
+              ((size_t)g.nctiles * sizeof(pgb_tile) + 15) / 16 * 16 + ((size_t)g.nbox * 4 + 15) / 16 * 16;
+      }
+      P->smem_total = q;
+      if (q > 200 * 1024) P->prog_off = 0;   /* does not fit: read in place */
+   } else if (P)
+      P->nbox_copy = 0;
+   if (P && !g_tp_bad)
+      for (int i = 0; i < P->nstep; i++) {
+         pgb_tail_step *t = &P->step[i];
+         if (i + 1 == P->nstep)
+            t->bar = 0;
+         else if (t->bar)
+            t->bar = t->solo && P->step[i + 1].solo ? 2 : 1;
+      }
+   if (g_tp_bad) {
+      snprintf(g_err32, sizeof(g_err32), "small-level kernel: %s",
+               g_tp_bad == 1 ? "more than PGB_TAIL_MAXSTEP steps or PGB_TAIL_MAXLEV levels"
+                             : "a pass it cannot run (FP64 coarsest loop, sync copy or fork)");
+      return 1;
+   }
+   return 0;
+}
+
+extern "C" int pgb_tail_recording(void) { return g_tp != 0; }
+
+/* a new step (barrier after it) on level lv (0: none) */
+static pgb_tail_step *tadd(int kind, const pgb_dlevel *lv)
+{
+   pgb_tail_prog *P = g_tp;
+   int li = 0;
+   if (P->nstep >= PGB_TAIL_MAXSTEP) {
+      g_tp_bad = 1;
+      return 0;
+   }
+   if (lv) {
+      for (li = 0; li < P->nlev; li++)
+         if (P->lv[li].level == lv->level) break;
+      if (li == P->nlev) {
+         if (P->nlev >= PGB_TAIL_MAXLEV) {
+            g_tp_bad = 1;
+            return 0;
+         }
+         P->lv[P->nlev++] = *lv;
+      }
+   }
+   pgb_tail_step *t = &P->step[P->nstep++];
+   memset(t, 0, sizeof(*t));
+   t->kind = (unsigned char)kind;
+   t->lev = (unsigned char)li;
+   t->bar = 1;
+   t->solo = (unsigned char)(g_tp_solo || kind == TS_COARSEST);
+   t->gx = t->gy = t->gz = 1;
+   return t;
+}
+
+
+#define TADD(t, kind, lvp)                       \
+   pgb_tail_step *t = tadd((kind), (lvp));       \
+   if (!t) return 1
+
+extern "C" int pgb_tail_add_restrict(const pgb_plan *p, int field_mask, int res32)
+{
+   const pgb_restrict_op *h = (const pgb_restrict_op *)p->h_ops, *d = (const pgb_restrict_op *)p->d_ops;
+   for (int bt = 0; bt < p->nbatch; bt++) {
+      const int n = p->batch_start[bt + 1] - p->batch_start[bt];
+      for (int c0 = 0; c0 < n; c0 += 65535) {
+         const int m = n - c0 < 65535 ? n - c0 : 65535;
+         dim3 g;
+         plane_grid(h + p->batch_start[bt] + c0, m, g);
+         TADD(t, TS_RESTRICT, 0);
+         t->ptr = d + p->batch_start[bt] + c0;
+         t->a[0] = field_mask;
+         t->a[1] = res32;
+         t->gx = (int)g.x;
+         t->gy = (int)g.y;
+         t->gz = (int)g.z;
+      }
+   }
+   return 0;
+}
+
+extern "C" int pgb_tail_add_clear(pgb_dlevel lv, int mask)
+{
+   TADD(t, TS_CLEAR, &lv);
+   t->a[0] = mask;
+   t->gx = lv.ntiles;
+   return 0;
+}
+
+static int tail_attr_set[2];
+
+template <bool PROG>
+static cudaError_t tail_attrs()
+{
+   if (tail_attr_set[PROG]) return cudaSuccess;
+   cudaError_t e = cudaFuncSetAttribute(k_tail<PROG>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail<PROG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   if (e == cudaSuccess) tail_attr_set[PROG] = 1;
+   return e;
+}
+
+template <bool PROG>
+static cudaError_t tail_launch(const pgb_dbox *boxes, const pgb_tail_prog *p, int ncta, pgb_scratch sc,
+                               cudaStream_t st)
+{
+   cudaLaunchConfig_t cfg;
+   cudaLaunchAttribute at[1];
+   memset(&cfg, 0, sizeof(cfg));
+   memset(at, 0, sizeof(at));
+   if (p->grid) {
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+   } else {
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)ncta;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+   }
+   cfg.gridDim = dim3((unsigned)ncta);
+   cfg.blockDim = dim3(PGB_TX, PGB_TY);
+   cfg.dynamicSmemBytes = p->prog_off ? p->smem_total : p->smem;
+   cfg.stream = st;
+   cfg.attrs = at;
+   cfg.numAttrs = 1;
+   cudaError_t e = tail_attrs<PROG>();
+   if (e != cudaSuccess) return e;
+   return cudaLaunchKernelEx(&cfg, k_tail<PROG>, boxes, *p, sc);
+}
+
+extern "C" int pgb_tail_grid_ctas(void)
+{
+   int dev = 0, n = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+   return n;
+}
+
+extern "C" int pgb_k_tail(const pgb_dbox *boxes, const pgb_tail_prog *p, int ncta, pgb_scratch sc, void *stream)
+{
+   if (!p->nstep) return 0;
+   if (p->grid && cudaMemsetAsync(p->bar_cnt, 0, sizeof(unsigned int), (cudaStream_t)stream) != cudaSuccess)
+      return check32("tail counter");
+   const cudaError_t e = p->pde == PGB_OPK_PROGRAM ? tail_launch<true>(boxes, p, ncta, sc, (cudaStream_t)stream)
+                                                   : tail_launch<false>(boxes, p, ncta, sc, (cudaStream_t)stream);
+   if (e != cudaSuccess) {
+      snprintf(g_err32, sizeof(g_err32), "small-level kernel: %s", cudaGetErrorString(e));
+      return 1;
+   }
+   return check32("tail");
+}
+
+extern "C" int pgb_tail_max_cluster(size_t smem)
+{
+   if (tail_attrs<false>() != cudaSuccess || tail_attrs<true>() != cudaSuccess) return 0;
+   for (int cs = 16; cs >= 1; cs /= 2) {
+      cudaLaunchConfig_t cfg;
+      cudaLaunchAttribute at[1];
+      memset(&cfg, 0, sizeof(cfg));
+      memset(at, 0, sizeof(at));
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)cs;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)cs);
+      cfg.blockDim = dim3(PGB_TX, PGB_TY);
+      cfg.dynamicSmemBytes = smem;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n0 = 0, n1 = 0;
+      if (cudaOccupancyMaxActiveClusters(&n0, k_tail<false>, &cfg) == cudaSuccess &&
+          cudaOccupancyMaxActiveClusters(&n1, k_tail<true>, &cfg) == cudaSuccess && n0 >= 1 && n1 >= 1)
+         return cs;
+      cudaGetLastError();
+   }
+   return 0;
+}
+
 /* ------------------------------------------------------------ launchers -- */
 extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, int cover,
                                 void *stream)
@@ -1825,6 +2294,14 @@ extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, d
    const int n = cover ? lv.nctiles : lv.ntiles;
    if (!n) return 0;
    const int sp = split_for(lv, n);
+   if (g_tp) {
+      TADD(t, TS_FAS, &lv);
+      t->a[0] = cover;
+      t->a[1] = sp;
+      t->d = w0_r;
+      t->gx = n * sp;
+      return 0;
+   }
    OPLAUNCH(k_fas_defect, pde, n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r, cover,
             sp);
    return check32("fas_defect");
@@ -1835,6 +2312,15 @@ extern "C" int pgb_k_defect32(const pgb_dbox *boxes, pgb_dlevel lv, int slot, co
 {
    if (!lv.ntiles) return 0;
    const int sp = split_for(lv, lv.ntiles);
+   if (g_tp) {
+      TADD(t, TS_DEFECT, &lv);
+      t->a[0] = slot;
+      t->a[1] = sp;
+      t->a[2] = gval;
+      t->ptr = gate;
+      t->gx = lv.ntiles * sp;
+      return 0;
+   }
    k_defect32<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, slot, sp, gate,
                                                                                  gval);
    return check32("defect32");
@@ -1853,6 +2339,22 @@ extern "C" int pgb_k_sweep32(const pgb_dbox *boxes, pgb_dlevel lv, int nsweep, i
 {
    int done = 0, src = *slot, dst = src == W_E ? W_E2 : W_E;
    if (!lv.ntiles) return 0;
+   if (g_tp) {   /* the small-level kernel relaxes by colour passes in place */
+      if (fuse > 0) return tail_refuse();
+      if (src != W_E) {
+         TADD(t, TS_COPYE, &lv);
+         t->a[0] = src;
+         t->gx = lv.ntiles;
+         *slot = W_E;
+      }
+      for (; done < nsweep; done++)
+         for (int pass = 0; pass < 2; pass++) {
+            TADD(t, TS_RELAX, &lv);
+            t->a[0] = pass;
+            t->gx = lv.nrtiles;
+         }
+      return 0;
+   }
    if (fuse <= 0) {   /* in place, one launch per colour pass */
       if (src != W_E) {
          k_copy_e<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, src);
@@ -1910,6 +2412,15 @@ extern "C" int pgb_k_update(const pgb_dbox *boxes, pgb_dlevel lv, int post, int 
 {
    if (!lv.ntiles) return 0;
    const int sp = split_for(lv, lv.ntiles);
+   if (g_tp) {
+      TADD(t, TS_UPDATE, &lv);
+      t->a[0] = post;
+      t->a[1] = slot;
+      t->a[2] = zslot;
+      t->a[3] = sp;
+      t->gx = lv.ntiles * sp;
+      return 0;
+   }
    k_update<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot,
                                                                                sp);
    return check32("update");
@@ -1924,6 +2435,18 @@ extern "C" int pgb_k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pos
       return 1;
    }
    const int sp = split_for(lv, lv.ntiles);
+   if (g_tp) {
+      TADD(t, TS_UPDDEF, &lv);
+      t->a[0] = post;
+      t->a[1] = slot;
+      t->a[2] = zslot;
+      t->a[3] = sp;
+      t->a[4] = defect;
+      t->a[5] = gval;
+      t->ptr = gate;
+      t->gx = lv.ntiles * sp;
+      return 0;
+   }
    k_update_defect<<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, post, slot, zslot,
                                                                                       sp, defect, gate, gval);
    return check32("update_defect");
@@ -1931,6 +2454,7 @@ extern "C" int pgb_k_update_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pos
 
 extern "C" int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
 {
+   if (g_tp) return tail_refuse();
    if (!lv.ntiles) return 0;
    k_zero32<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
    return check32("zero32");
@@ -1938,6 +2462,7 @@ extern "C" int pgb_k_zero32(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
 
 extern "C" int pgb_k_copy32(const pgb_dbox *boxes, const pgb_plan *p, int slot, void *stream)
 {
+   if (g_tp) return tail_refuse();
    const pgb_copy_op *h = (const pgb_copy_op *)p->h_ops, *d = (const pgb_copy_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
       const int n = p->batch_start[bt + 1] - p->batch_start[bt];
@@ -1956,6 +2481,13 @@ extern "C" int pgb_k_cgc_mixed(const pgb_dbox *boxes, pgb_dlevel lv, double inv_
 {
    if (!lv.nctiles) return 0;
    const int sp = split_for(lv, lv.nctiles);
+   if (g_tp) {
+      TADD(t, TS_CGC, &lv);
+      t->a[0] = sp;
+      t->d = inv_w0;
+      t->gx = lv.nctiles * sp;
+      return 0;
+   }
    k_cgc_mixed<<<lv.nctiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, inv_w0, sp);
    return check32("cgc_mixed");
 }
@@ -1968,6 +2500,43 @@ extern "C" int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int 
                                   void *side, void *fork, void *join)
 {
    const pgb_interp_op *h = (const pgb_interp_op *)p->h_ops, *d = (const pgb_interp_op *)p->d_ops;
+   if (g_tp) {   /* no fork: the two kernels of a batch as steps with no barrier between them */
+      for (int bt = 0; bt < p->nbatch; bt++) {
+         const int n = p->batch_start[bt + 1] - p->batch_start[bt];
+         for (int c0 = 0; c0 < n; c0 += 65535) {
+            const int m = n - c0 < 65535 ? n - c0 : 65535;
+            const pgb_interp_op *hb = h + p->batch_start[bt] + c0;
+            dim3 g;
+            long mr = 1, mf = 1;
+            int lin2 = 1, mi = 1;
+            row_grid(hb, m, g);
+            for (int i = 0; i < m; i++) {
+               if ((long)hb[i].njb * hb[i].nkb > mr) mr = (long)hb[i].njb * hb[i].nkb;
+               if (hb[i].irho != 2 || (hb[i].ord != 2 && (hb[i].nii >= 4 || hb[i].nji >= 4 || (dim == 3 && hb[i].nki >= 4))))
+                  lin2 = 0;
+               if (hb[i].nib > mi) mi = hb[i].nib;
+               if (2L * (hb[i].njb + hb[i].nkb) > mf) mf = 2L * (hb[i].njb + hb[i].nkb);
+            }
+            TADD(t, lin2 ? TS_LIN2 : TS_IMIX, 0);
+            t->ptr = d + p->batch_start[bt] + c0;
+            t->a[0] = dim;
+            t->a[1] = slot;
+            t->gx = (int)g.x;
+            t->gy = (int)g.y;
+            t->gz = (int)g.z;
+            t->bar = 0;   /* the edge step writes other points and reads only the coarse level */
+            long gy = mf + (2 * mr + 127) / 128;
+            TADD(t2, TS_EDGES, 0);
+            t2->ptr = d + p->batch_start[bt] + c0;
+            t2->a[0] = dim;
+            t2->a[1] = slot;
+            t2->gx = (mi + 127) / 128;
+            t2->gy = (int)(gy > 65535 ? 65535 : gy);
+            t2->gz = m;
+         }
+      }
+      return 0;
+   }
    const bool par = side && p->nbatch == 1;
    cudaStream_t es = par ? (cudaStream_t)side : (cudaStream_t)stream;
    if (par) {
@@ -2022,6 +2591,14 @@ extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde
    if (!lv.ntiles) return 0;
    int sp = split_for(lv, lv.ntiles);
    while (sp > 1 && (long)lv.ntiles * sp > sc.npartial) sp /= 2;   /* one partial sum per CTA */
+   if (g_tp) {   /* a residual whose norm nothing reads */
+      if (norm_out || trace) return tail_refuse();
+      TADD(t, TS_RESID, &lv);
+      t->a[0] = sp;
+      t->ptr = gate;
+      t->gx = lv.ntiles * sp;
+      return 0;
+   }
    OPLAUNCH(k_residual_fast, pde, lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, sc,
             norm_out, trace, sp, gate);
    return check32("residual_fast");
@@ -2031,6 +2608,12 @@ extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                   void *stream)
 {
    if (!lv.nctiles) return 0;
+   if (g_tp) {
+      TADD(t, TS_LOPRHS, &lv);
+      t->d = w0_r;
+      t->gx = lv.nctiles;
+      return 0;
+   }
    OPLAUNCH(k_lop_rhs_fast, pde, lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r);
    return check32("lop_rhs_fast");
 }
@@ -2043,6 +2626,16 @@ extern "C" int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pd
    const size_t smem = (size_t)a.smem_points * (sizeof(double) + 3 * sizeof(float) + sizeof(int));
    static int attr_set = 0;
    if (a.smem_points <= 0 || a.ncoarse > CM_MAXB || smem > 200 * 1024) return 1;
+   if (g_tp) {   /* one coarsest loop per program, run by CTA 0 */
+      if (trace || g_tp->ca.res_out) return tail_refuse() ? -1 : -1;
+      TADD(t, TS_COARSEST, &lv);
+      (void)t;
+      g_tp->ca = a;
+      g_tp->csync = (const pgb_copy_op *)sync->d_ops;
+      g_tp->ncsync = sync->nops;
+      if (smem > g_tp->smem) g_tp->smem = smem;
+      return 0;
+   }
    if (!attr_set) {
       cudaFuncSetAttribute(k_coarsest_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       cudaFuncSetAttribute(k_coarsest_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

@@ -21,6 +21,7 @@
 #include "pgb_dev.h"
 #include "pgb_opgrid.cuh"
 #include "pgb_op.cuh"
+#include "pgb_weights.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -31,6 +32,15 @@ extern "C" const char *pgb_dev_error(void) { return g_err; }
 extern "C" unsigned long long pgb_dev_launches(void) { return g_launches; }
 
 #define LAUNCHED(n) (g_launches += (unsigned long long)(n))
+
+/* while the small-level kernel records (pgb_dev.h): an FP64 pass it runs is
+ * recorded (rc = 0 or 1 returned), one it cannot run refuses */
+static int tail_note(int rc, const char *what)
+{
+   if (rc) snprintf(g_err, sizeof(g_err), "%s: %s", what, pgb_dev_error32());
+   return rc;
+}
+#define TAIL_REFUSE(what)                                                                 do {                                                                                       if (pgb_tail_recording()) {                                                                snprintf(g_err, sizeof(g_err), "%s: not a pass of the small-level kernel", what);          return 1;                                                                            }                                                                                    } while (0)
 
 static int check(const char *what)
 {
@@ -66,23 +76,6 @@ extern "C" int pgb_dev_sync(void *stream)
 /* 2*pi and 5*2*pi, the constants of the conformal-factor hook */
 #define TWO_PI 6.283185307179586
 #define TEN_PI 31.41592653589793
-
-/* RN(x/d) for a divisor whose correctly rounded reciprocal r = RN(1/d) is
- * known. q0 = RN(x*r) is within two ulps of x/d; one FMA correction step
- * q1 = RN(q0 + RN(x - q0*d)*r) leaves it within one ulp (faithful); with a
- * faithful quotient and r = RN(1/d), Markstein's theorem (P. Markstein, IBM
- * J. Res. Dev. 34, 1990; Muller et al., Handbook of Floating-Point
- * Arithmetic, 2018, sec. 4.7) makes the second step RN(x/d) exactly, barring
- * overflow and underflow. Five FP64 operations instead of a full division;
- * the GPU tests compare every result path with IEEE division. */
-__device__ __forceinline__ double div_known(double x, double d, double r)
-{
-   double q = __dmul_rn(x, r);
-   double e = __fma_rn(-q, d, x);
-   q = __fma_rn(e, r, q);
-   e = __fma_rn(-q, d, x);
-   return __fma_rn(e, r, q);
-}
 
 /* one term of num.f:113-115: num/dx^2 (a product when 1/dx^2 is exact) */
 __device__ __forceinline__ double dterm(const pgb_dbox &b, double num, int d)
@@ -362,10 +355,7 @@ extern "C" int pgb_k_residual(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb
 
 __global__ void __launch_bounds__(NT) k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask)
 {
-   FOR_TILE_POINTS({
-      for (int f = 0; f < PGB_NF; f++)
-         if ((mask >> f) & 1) b.f[f][p] = 0;
-   })
+   clear_b(hw_blk(), boxes, lv, mask);
 }
 
 /* app_L_op (num.f:85-123, lop = L[u] at interior cmask-child points) fused
@@ -422,6 +412,7 @@ __global__ void __launch_bounds__(NT) k_add_res(const pgb_dbox *boxes, pgb_dleve
 extern "C" int pgb_k_clear(const pgb_dbox *boxes, pgb_dlevel lv, int mask, void *stream)
 {
    if (!lv.ntiles) return 0;
+   if (pgb_tail_recording()) return tail_note(pgb_tail_add_clear(lv, mask), "clear");
    k_clear<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, mask);
    LAUNCHED(1);
    return check("clear");
@@ -450,21 +441,6 @@ extern "C" int pgb_k_add_res(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
 }
 
 /* --------------------------------------------------------- op-list passes -- */
-/* point q of an ni x nj x nk segment -> (a,b,c) */
-__device__ __forceinline__ void unflat(long q, int ni, int nj, int &a, int &bb, int &c)
-{
-   a = (int)(q % ni);
-   long r = q / ni;
-   bb = (int)(r % nj);
-   c = (int)(r / nj);
-}
-
-__device__ __forceinline__ long lin(const pgb_dbox &b, int i1, int j1, int k1)
-{
-   /* 1-based (Fortran) indices */
-   return (i1 - 1) + (long)b.n[0] * ((j1 - 1) + (long)b.n[1] * (k1 - 1));
-}
-
 /* dmcopy3d with unit strides (src/m_util_r8.f:20-50) */
 __global__ void k_copy(const pgb_dbox *boxes, const pgb_copy_op *ops, int field)
 {
@@ -476,152 +452,10 @@ __global__ void k_copy(const pgb_dbox *boxes, const pgb_copy_op *ops, int field)
    })
 }
 
-/* The weights of the half- and full-weighting stencils are powers of two,
- * so w*u is exact and RN(acc + w*u) == fma(w, u, acc): the FMA forms below
- * give the Fortran sums bit for bit (same left-to-right order) with fewer
- * FP64 instructions. Divisions by 4, 8, 16 and 64 are exact products; the
- * division by 12 uses div_known. */
-#define ACC(acc, w, v) __fma_rn((double)(w), (v), (acc))
-
-/* dmhwr3d (src/m_util_r8.f:649-723), do_ex = 0, at fine point (i0,j0,k0) */
-__device__ double hwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
-{
-   int w = 0;
-   double sum = 0;
-   long sy = nx1, sz = (long)nx1 * ny1;
-   long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
-   if (i0 > 1 && i0 <= nx1 - 1) {
-      w = w + 4;
-      sum = ACC(sum + u[p - 1], 2, u[p]) + u[p + 1];
-   }
-   if (j0 > 1 && j0 <= ny1 - 1) {
-      w = w + 4;
-      sum = ACC(sum + u[p - sy], 2, u[p]) + u[p + sy];
-   }
-   if (k0 > 1 && k0 <= nz1 - 1) {
-      w = w + 4;
-      sum = ACC(sum + u[p - sz], 2, u[p]) + u[p + sz];
-   }
-   if (w == 12) return div_known(sum, 12.0, 1.0 / 12.0);
-   if (w > 0) return sum * (w == 4 ? 0.25 : 0.125);
-   return u[p];
-}
-
-/* dmfwr3d (src/m_util_r8.f:733-830), do_ex = 0, at fine point (i0,j0,k0):
- * the 27-, 9- or 3-point sum in the Fortran order (outer offset first) */
-__device__ double fwr(const double *u, int nx1, int ny1, int nz1, int i0, int j0, int k0)
-{
-   const long sy = nx1, sz = (long)nx1 * ny1;
-   const long p = (i0 - 1) + sy * (j0 - 1) + sz * (k0 - 1);
-   bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
-   /* strides of the outer, middle and inner offsets of the sum */
-   long s0, s1, s2;
-   int n0, n1, n2;
-   double scale;
-   if (ii && jj && kk) {
-      s0 = sz; s1 = sy; s2 = 1; n0 = n1 = n2 = 3; scale = 1.0 / 64.0;
-   } else if (ii && jj) {
-      s0 = 0; s1 = sy; s2 = 1; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
-   } else if (jj && kk) {
-      s0 = 0; s1 = sy; s2 = sz; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
-   } else if (ii && kk) {
-      s0 = 0; s1 = 1; s2 = sz; n0 = 1; n1 = n2 = 3; scale = 1.0 / 16.0;
-   } else if (ii || jj || kk) {
-      s0 = 0; s1 = 0; s2 = ii ? 1 : (jj ? sy : sz); n0 = n1 = 1; n2 = 3; scale = 0.25;
-   } else
-      return u[p];
-   double acc = 0;
-   bool first = true;
-#pragma unroll
-   for (int a = 0; a < 3; a++) {
-      if (a >= n0) break;
-      int da = n0 == 3 ? a - 1 : 0;
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-         if (b >= n1) break;
-         int db = n1 == 3 ? b - 1 : 0;
-#pragma unroll
-         for (int c = 0; c < 3; c++) {
-            int dc = c - 1;
-            double v = u[p + da * s0 + db * s1 + dc * s2];
-            int w = (da == 0 ? 2 : 1) * (db == 0 ? 2 : 1) * (dc == 0 ? 2 : 1);
-            if (n0 == 1) w >>= 1;
-            if (n1 == 1) w >>= 1;
-            acc = first ? (w == 1 ? v : (double)w * v) : ACC(acc, w, v);
-            first = false;
-         }
-      }
-   }
-   return acc * scale;
-}
-#undef ACC
-
-/* fwr of the residual in FP32 for the mixed form: the same weights and sums
- * over D, the FP32 copy of -res that the mixed form's residual pass leaves
- * at the points where it writes res (0 wherever res is 0). The restricted
- * residual only steers the coarse-grid correction, so FP32 is enough; the
- * FP64 residual of the finest level still decides convergence. */
-__device__ double fwr_d32(const float *dd, int wy, long wz, int nx1, int ny1, int nz1, int i0, int j0, int k0)
-{
-   const int sy = wy;
-   const long sz = wz;   /* the FP32 arrays' padded pitches */
-   const long p = (i0 - 1) + (long)sy * (j0 - 1) + sz * (k0 - 1);
-   bool ii = i0 > 1 && i0 <= nx1 - 1, jj = j0 > 1 && j0 <= ny1 - 1, kk = k0 > 1 && k0 <= nz1 - 1;
-   long s0, s1, s2;
-   int n0, n1;
-   float scale;
-   if (ii && jj && kk) {
-      s0 = sz; s1 = sy; s2 = 1; n0 = n1 = 3; scale = 1.f / 64.f;
-   } else if (ii && jj) {
-      s0 = 0; s1 = sy; s2 = 1; n0 = 1; n1 = 3; scale = 1.f / 16.f;
-   } else if (jj && kk) {
-      s0 = 0; s1 = sy; s2 = sz; n0 = 1; n1 = 3; scale = 1.f / 16.f;
-   } else if (ii && kk) {
-      s0 = 0; s1 = 1; s2 = sz; n0 = 1; n1 = 3; scale = 1.f / 16.f;
-   } else if (ii || jj || kk) {
-      s0 = 0; s1 = 0; s2 = ii ? 1 : (jj ? sy : sz); n0 = n1 = 1; scale = 0.25f;
-   } else
-      return -(double)dd[p];
-   float acc = 0.f;
-#pragma unroll
-   for (int a = 0; a < 3; a++) {
-      if (a >= n0) break;
-      const int da = n0 == 3 ? a - 1 : 0;
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-         if (b >= n1) break;
-         const int db = n1 == 3 ? b - 1 : 0;
-         const float wab = (float)((da == 0 ? 2 : 1) * (db == 0 ? 2 : 1) >> (n0 == 1 ? 1 : 0) >> (n1 == 1 ? 1 : 0));
-         const float *r = dd + p + da * s0 + db * s1;
-         acc = __fmaf_rn(wab, __fadd_rn(__fadd_rn(r[-s2], 2.f * r[0]), r[s2]), acc);
-      }
-   }
-   return -(double)__fmul_rn(acc, scale);
-}
-
-/* local_transfer delta = +1 (src/transfer.c:1126-1149): per grid function
- * straight injection, half weighting or full weighting; res32 = 1 (mixed
- * form) takes the full weighting of the residual from its FP32 copy */
+/* local_transfer delta = +1 (restrict_b in pgb_weights.cuh) */
 __global__ void k_restrict(const pgb_dbox *boxes, const pgb_restrict_op *ops, int field_mask, int res32)
 {
-   const pgb_restrict_op o = ops[blockIdx.z];
-   const pgb_dbox &s = boxes[o.src_box];
-   const pgb_dbox &d = boxes[o.dst_box];
-   OP_PLANES(o.ni, o.nj, o.nk, {
-      const int i0 = o.i1 + a * o.irho, j0 = o.j1 + bb * o.irho, k0 = o.k1 + c * o.irho;
-      const long pd = lin(d, o.i2 + a, o.j2 + bb, o.k2 + c);
-      for (int f = 0; f < PGB_NF; f++) {
-         const int op = o.op[f];
-         if (!op || !((field_mask >> f) & 1)) continue;
-         const double *u = s.f[f];
-         double v;
-         if (op == 1) v = u[lin(s, i0, j0, k0)];
-         else if (op == 2) v = hwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
-         else if (res32 && f == PGB_F_RES) v = fwr_d32(s.w32[PGB_W32_D], s.wy, s.wz, s.n[0], s.n[1], s.n[2], i0, j0, k0);
-         else v = fwr(u, s.n[0], s.n[1], s.n[2], i0, j0, k0);
-         d.f[f][pd] = v;
-      }
-   })
+   restrict_b(hw_blk(), boxes, ops, field_mask, res32);
 }
 
 /* (j*1.0)/irho; for the ratio 2 of every MG hierarchy, the exact product j*0.5 */
@@ -721,6 +555,7 @@ __global__ void k_interp(const pgb_dbox *boxes, const pgb_interp_op *ops, int fi
 
 extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, void *stream)
 {
+   TAIL_REFUSE("copy");
    const pgb_copy_op *h = (const pgb_copy_op *)p->h_ops, *d = (const pgb_copy_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
       const int n = p->batch_start[bt + 1] - p->batch_start[bt];
@@ -738,6 +573,7 @@ extern "C" int pgb_k_copy(const pgb_dbox *boxes, const pgb_plan *p, int field, v
 extern "C" int pgb_k_restrict(const pgb_dbox *boxes, const pgb_plan *p, int field_mask, int res32,
                               void *stream)
 {
+   if (pgb_tail_recording()) return tail_note(pgb_tail_add_restrict(p, field_mask, res32), "restrict");
    const pgb_restrict_op *h = (const pgb_restrict_op *)p->h_ops, *d = (const pgb_restrict_op *)p->d_ops;
    for (int bt = 0; bt < p->nbatch; bt++) {
       const int n = p->batch_start[bt + 1] - p->batch_start[bt];
@@ -1325,6 +1161,7 @@ __global__ void __launch_bounds__(CT) k_coarsest_smem(const pgb_dbox *boxes, pgb
 extern "C" int pgb_k_coarsest(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                               pgb_coarsest_args a, pgb_trace *trace, void *stream)
 {
+   TAIL_REFUSE("coarsest");
    size_t smem = (size_t)a.smem_points * 4 * sizeof(double);
    const char *force = getenv("PGB_COARSEST_KERNEL");   /* smem | cluster | single (experiments) */
    int want_smem = (!force || !strcmp(force, "smem")) && lv.nvar == 1;

@@ -19,6 +19,37 @@
          __VA_ARGS__                                                                  \
       }
 
+/* A block as a kernel body sees it: a CTA of a standalone launch, or one
+ * work item of a step of the small-level kernel (k_tail in
+ * pgb_kernels32.cu), which runs the same bodies over a virtual grid. lt and
+ * nt are the thread's linear index and the threads per block; the 32 x 8
+ * tile bodies use threadIdx.x/y directly (k_tail has that shape). */
+struct vblk {
+   int x, y, z, gx, gy, gz, lt, nt;
+};
+
+__device__ __forceinline__ vblk hw_blk()
+{
+   vblk v;
+   v.x = blockIdx.x;
+   v.y = blockIdx.y;
+   v.z = blockIdx.z;
+   v.gx = gridDim.x;
+   v.gy = gridDim.y;
+   v.gz = gridDim.z;
+   v.lt = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+   v.nt = blockDim.x * blockDim.y * blockDim.z;
+   return v;
+}
+
+/* OP_PLANES over a vblk */
+#define OP_PLANES_V(vb, ni, nj, nk, ...)                                              \
+   for (int c = (vb).y; c < (nk); c += (vb).gy)                                      \
+      for (int q = (vb).x * (vb).nt + (vb).lt; q < (ni) * (nj); q += (vb).gx * (vb).nt) { \
+         const int a = q % (ni), bb = q / (ni);                                       \
+         __VA_ARGS__                                                                  \
+      }
+
 /* launch geometry of a batch of ops: planes (copy, restrict) or x-rows
  * (interp); grid z = ops of the batch */
 template <class T> static inline void plane_grid(const T *o, int n, dim3 &g)

@@ -69,6 +69,12 @@ struct pgb_solver {
    int last_cycles;
    long last_citers;
    double last_ms;
+   int tail_lc;             /* mixed form: levels 1..tail_lc run in the small-level kernel (0: none) */
+   int tail_ncta;           /* its cluster size */
+   int tail_solo;           /* levels 1..tail_solo of those run in one CTA (their steps need no cluster) */
+   int tail_grid;           /* 0: one cluster; else the CTAs of a cooperative launch (one per SM) */
+   unsigned int *d_tailbar; /* its barrier counter */
+   pgb_tail_prog *tail;     /* its program, recorded by each V-cycle launch or capture */
 };
 
 static __thread char g_err[512];
@@ -680,6 +686,8 @@ int pgb_destroy(pgb_solver *s)
       }
    }
    free(s->hbox);
+   free(s->tail);
+   if (s->d_tailbar) cudaFree(s->d_tailbar);
    pgb_hier_free(&s->h);
    free(s);
    return 0;
@@ -883,6 +891,73 @@ static int time_candidate(pgb_solver *s, int L, int nsw, int f, float *ms)
    return 0;
 }
 
+static int fp64_level1(const pgb_solver *s);
+static void coarsest_args(pgb_solver *s, int L, pgb_coarsest_args *a);
+
+/* The small-level kernel (pgb_dev.h, pgb_k_tail) takes the V-cycle's passes
+ * over MG levels 1..Lc: the largest Lc below the finest level such that
+ * every level up to it has at most PGB_TAIL_POINTS points (6000 unless set:
+ * a 17^3 grid; the FP64 passes of larger levels run faster spread over the
+ * whole GPU than on one cluster), no sync between its boxes, and no coarsest
+ * boxes above level 1, where one coarsest box fits the on-chip FP32 coarsest
+ * loop; at least two levels. Those levels relax by colour passes (their
+ * sweeps are not autotuned). Off unless PGB_TAIL=1: measured on GB300 it is
+ * slower than the V-cycle's own graph of one launch per pass (a graph node
+ * costs about what a barrier and one trip to L2 per step cost here), with
+ * the same bits. PGB_TAIL_GRID=1 meets at a counter across one CTA per SM
+ * instead of a cluster barrier; PGB_TAIL_SOLO=n runs the passes of levels
+ * of at most n points in CTA 0 alone. */
+static int tail_plan(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const char *env = getenv("PGB_TAIL"), *pts = getenv("PGB_TAIL_POINTS"), *sol = getenv("PGB_TAIL_SOLO");
+   const long maxp = pts ? atol(pts) : 6000, maxsolo = sol ? atol(sol) : 0;
+   const int nsw = h->prm.pre_swp + h->prm.pst_swp;
+   int L, b, Lc = 0, steps = 1;
+   pgb_coarsest_args a;
+   s->tail_lc = s->tail_solo = 0;
+   if (!env || strcmp(env, "1") || h->prm.precision != PGB_MIXED || s->nvar > 1 || h->nlev < 3 || fp64_level1(s))
+      return 0;
+   coarsest_args(s, 1, &a);
+   if (a.ncoarse != 1 || a.smem_points <= 0 ||
+       a.smem_points * (long)(sizeof(double) + 3 * sizeof(float) + sizeof(int)) > 200 * 1024)
+      return 0;
+   for (L = 1; L < h->nlev && L <= PGB_TAIL_MAXLEV; L++) {
+      long n = 0;
+      for (b = 0; b < h->lev[L].nbox; b++) {
+         const pgb_hbox *bx = &h->boxes[h->lev[L].box[b]];
+         n += (long)bx->shape[0] * bx->shape[1] * bx->shape[2];
+      }
+      if (n > maxp || h->sync[L][0].nops || h->sync[L][1].nops || (L > 1 && lvl_coarsest(s, L))) break;
+      if (n <= maxsolo && s->tail_solo == L - 1) s->tail_solo = L;
+      /* a bound on the steps a level adds (passes of the down and up sweep) */
+      steps += 10 + 2 * nsw + h->inject[L].nbatch + 2 * h->interp[L].nbatch;
+      if (steps > PGB_TAIL_MAXSTEP) break;
+      Lc = L;
+   }
+   if (Lc < 2) return 0;
+   if (s->tail_solo > Lc) s->tail_solo = Lc;
+   s->tail_ncta = pgb_tail_max_cluster((size_t)a.smem_points * (sizeof(double) + 3 * sizeof(float) + sizeof(int)));
+   if (s->tail_ncta < 1) return 0;
+   {
+      const char *gm = getenv("PGB_TAIL_GRID");
+      s->tail_grid = gm && !strcmp(gm, "1") ? pgb_tail_grid_ctas() : 0;
+      if (s->tail_grid && !s->d_tailbar && cudaMalloc((void **)&s->d_tailbar, sizeof(unsigned int)) != cudaSuccess)
+         return fail(10, "small-level kernel: barrier counter");
+   }
+   if (!s->tail && !(s->tail = (pgb_tail_prog *)malloc(sizeof(pgb_tail_prog))))
+      return fail(10, "small-level kernel: host buffer");
+   s->tail_lc = Lc;
+   for (L = 1; L <= Lc; L++) s->fuse[L] = 0;
+   return 0;
+}
+
+int pgb_tail_levels(const pgb_solver *s, int *cluster_ctas)
+{
+   if (cluster_ctas) *cluster_ctas = s->tail_lc ? s->tail_ncta : 0;
+   return s->tail_lc;
+}
+
 static int autotune(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
@@ -892,7 +967,7 @@ static int autotune(pgb_solver *s)
    s->tuned = 1;
    if (force && force[0] >= '0' && force[0] <= '7' && !force[1]) {
       /* one sweep shape on every level instead of the measured choice */
-      for (L = 2; L <= h->nlev; L++) {
+      for (L = s->tail_lc > 1 ? s->tail_lc + 1 : 2; L <= h->nlev; L++) {
          int can_fuse = !h->sync[L][0].nops && !h->sync[L][1].nops && nsw >= 2;
          int f = force[0] - '0';
          if (f == 3 && h->dim != 3) f = 1;
@@ -913,7 +988,7 @@ static int autotune(pgb_solver *s)
       return 0;
    }
    if ((env && !strcmp(env, "0")) || nsw < 1) return 0;
-   for (L = 2; L <= h->nlev; L++) {
+   for (L = s->tail_lc > 1 ? s->tail_lc + 1 : 2; L <= h->nlev; L++) {
       static const int tzs[4] = {8, 4, 2, 1};
       static const int mzs[5] = {4, 8, 16, 32, 64};
       int ntz = h->dim == 3 ? 4 : 1, a, f, best_tz = s->lv[L].tz, best_f = s->fuse[L], best_mtx = 60, best_mtz = 32;
@@ -966,7 +1041,9 @@ int pgb_level_tuning(pgb_solver *s, int L, int *tile_planes, int *sweeps_per_lau
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (L < 1 || L > s->h.nlev) return fail(3, "level %d out of range", L);
    if (tile_planes) *tile_planes = s->lv[L].tz;
-   if (sweeps_per_launch)   /* the sweep mode (pamr_gb300.h lists them) */
+   if (sweeps_per_launch && L <= s->tail_lc)   /* relaxed inside the small-level kernel */
+      *sweeps_per_launch = 8;
+   else if (sweeps_per_launch)   /* the sweep mode (pamr_gb300.h lists them) */
       *sweeps_per_launch = (s->fuse[L] == 2 && (s->h.sync[L][0].nops || s->h.sync[L][1].nops)) ? 1 : s->fuse[L];
    return 0;
 }
@@ -991,7 +1068,8 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
       if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, 0, s->stream));
    if (s->h.prm.precision == PGB_MIXED) {
       if (!s->tuned) {
-         int rc = autotune(s);
+         int rc = tail_plan(s);
+         if (!rc) rc = autotune(s);
          if (rc) return rc;
       }
       /* FP32 correction arrays start at 0 (D stays 0 wherever res is never
@@ -1264,12 +1342,17 @@ static int vcycle_mixed(pgb_solver *s)
    pgb_hier *h = &s->h;
    const pgb_hparams *p = &h->prm;
    int L, Lf = h->nlev;
+   /* levels 1..tail_lc as steps of one small-level kernel (recorded from
+    * the FAS pass of level tail_lc on the way down to its update on the way
+    * up; not while norms are traced) */
+   const int tail = s->tail_lc > 1 && !s->d_trace ? s->tail_lc : 0;
    /* clear_MG_vars: only where an FP64 read could see a value of an earlier
     * cycle (see pgb_prepare) */
    if (!s->res32[Lf])
       KC(pgb_k_clear(s->dbox, s->lv[Lf], (1 << PGB_F_RES) | (1 << PGB_F_RHS) | (1 << PGB_F_LOP), s->stream));
    for (L = Lf; L > 0; L--) {
       if (L < Lf) {
+         pgb_tail_set_solo(L + 1 <= s->tail_solo);   /* passes reading level L+1 */
          /* this norm is only ever traced (the finest level's convergence
           * norm comes from the residual after post-smoothing) */
          if (!defect32_level(s, L + 1))
@@ -1281,6 +1364,8 @@ static int vcycle_mixed(pgb_solver *s)
          if (h->inject[L].nops)
             KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), s->res32[L + 1], s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
+         if (L == tail) pgb_tail_begin(s->tail, h->pde, h->nbox);
+         pgb_tail_set_solo(L <= s->tail_solo);   /* passes over level L */
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
       }
@@ -1314,6 +1399,7 @@ static int vcycle_mixed(pgb_solver *s)
    for (L = 1; L <= Lf; L++) {
       if (L > 1) {
          int slot = s->eslot[L];
+         pgb_tail_set_solo(L <= s->tail_solo);   /* passes over levels L-1 and L */
          KC32(pgb_k_cgc_mixed(s->dbox, s->lv[L - 1], 1.0 / p->w0_i, s->stream));
          if (h->interp[L].nops)
             KC32(pgb_k_interp_mixed(s->dbox, &h->interp[L], h->dim, slot, s->stream, s->side, s->evfork,
@@ -1346,6 +1432,13 @@ static int vcycle_mixed(pgb_solver *s)
          if (rc > 0)   /* too large for one CTA's shared memory: the FP64 loop */
             KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
       }
+      if (L == tail) {
+         if (pgb_tail_end()) return fail(11, "%s", pgb_dev_error32());
+         s->tail->grid = s->tail_grid;
+         s->tail->bar_cnt = s->d_tailbar;
+         s->tail->err = s->d_err;
+         KC32(pgb_k_tail(s->dbox, s->tail, s->tail_grid ? s->tail_grid : s->tail_ncta, s->sc, s->stream));
+      }
       if (L == Lf)
          KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], h->pde, s->sc, norm_slot(s, Lf, N_RESID),
                                   s->d_trace, 0, s->stream));
@@ -1360,7 +1453,10 @@ static int vcycle_mixed(pgb_solver *s)
 
 static int vcycle_launch(pgb_solver *s)
 {
-   return s->h.prm.precision == PGB_MIXED ? vcycle_mixed(s) : vcycle_fp64(s);
+   if (s->h.prm.precision != PGB_MIXED) return vcycle_fp64(s);
+   const int rc = vcycle_mixed(s);
+   if (rc && pgb_tail_recording()) pgb_tail_end();   /* an error inside the recorded levels */
+   return rc;
 }
 
 /* The V-cycle's launches never depend on host-side values, so the whole

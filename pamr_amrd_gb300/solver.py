@@ -88,6 +88,7 @@ def lib(build: bool = True):
         L.pgb_launch_count.restype = C.c_longlong
         L.pgb_time_relax.argtypes = [vp, C.c_int, C.c_int, dp, dp]
         L.pgb_level_tuning.argtypes = [vp, C.c_int, ip, ip]
+        L.pgb_tail_levels.argtypes = [vp, ip]
         for name in ("pgb_dmcopy3d", "pgb_dmhwr3d", "pgb_dmfwr3d"):
             getattr(L, name).argtypes = [vp, vp] + [C.c_int] * 21 + [vp]
         L.pgb_dminterp3d.argtypes = [vp, vp] + [C.c_int] * 22 + [vp]
@@ -304,6 +305,13 @@ class Solver:
         tz, f = C.c_int(), C.c_int()
         _check(lib().pgb_level_tuning(self.h, L, C.byref(tz), C.byref(f)))
         return tz.value, f.value
+
+    def tail_levels(self):
+        """(MG levels 1..n run by the small-level kernel, its cluster's CTAs);
+        (0, 0) when every pass is a launch of its own"""
+        n = C.c_int()
+        lv = lib().pgb_tail_levels(self.h, C.byref(n))
+        return lv, n.value
 
     def time_relax(self, L: int, reps: int = 20):
         ms, by = C.c_double(), C.c_double()

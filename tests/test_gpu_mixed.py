@@ -68,7 +68,7 @@ def test_autotuned_launch_shapes_keep_the_solution(monkeypatch):
     u1 = s.get_u()
     shapes = [s.level_tuning(L) for L in range(2, s.num_levels() + 1)]
     s.close()
-    assert all(tz in (1, 2, 4, 8) and f in range(8) for tz, f in shapes), shapes
+    assert all(tz in (1, 2, 4, 8) and f in range(9) for tz, f in shapes), shapes
     monkeypatch.setenv("PGB_AUTOTUNE", "0")
     s = Solver(case)
     s.set_inputs()
