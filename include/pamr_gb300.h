@@ -250,7 +250,8 @@ int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level);
  * counterpart format in the reference, whose checkpoints are SDF files of
  * every grid function written through bbhutil, src/pamr.c:1908-1978,
  * 2042-2075): pgb_checkpoint_save writes, per input grid, its level, shape,
- * bounding box, u and source to `path`; pgb_checkpoint_load restores them
+ * bounding box, u of every elliptic variable and the sources to `path`;
+ * pgb_checkpoint_load restores them
  * into a solver created on the same hierarchy (checked bit for bit) and
  * fails without changing it when the file does not match. */
 int pgb_checkpoint_save(pgb_solver *s, const char *path);

@@ -1760,12 +1760,14 @@ int pgb_regrid(pgb_solver *dst, pgb_solver *src, int order, int min_level)
 
 /* ------------------------------------------------------------ checkpoint -- */
 /* File layout (little-endian as written by the host): "PGBCKPT1", int32
- * version, dim, operator kind, ngrids, source count, 0, then a 64-bit hash
- * of the operator's program; per input grid int32 level, shape[3], double
- * bbox[6], then u and each source (float64, x fastest). Grids below the
- * hierarchy's coarsest AMR level are not part of it and are skipped. */
+ * version, dim, operator kind, ngrids, source count, elliptic variables,
+ * then a 64-bit hash of the variables' operator programs; per input grid
+ * int32 level, shape[3], double bbox[6], then u of each variable and each
+ * source (float64, x fastest). Version 2 files (one variable, 0 in the
+ * variables' slot) load as well. Grids below the hierarchy's coarsest AMR
+ * level are not part of it and are skipped. */
 #define CKPT_MAGIC "PGBCKPT1"
-#define CKPT_VERSION 2
+#define CKPT_VERSION 3
 
 static unsigned long long dop_hash(const pgb_dop *d)
 {
@@ -1776,13 +1778,21 @@ static unsigned long long dop_hash(const pgb_dop *d)
    return h;
 }
 
+/* the operators of all variables (one variable: the hash of its operator) */
+static unsigned long long ops_hash(const pgb_solver *s)
+{
+   unsigned long long h = dop_hash(&s->dop);
+   int v;
+   for (v = 1; v < s->nvar; v++) h = h * 1099511628211ull ^ dop_hash(&s->dops[v]);
+   return h;
+}
+
 int pgb_checkpoint_save(pgb_solver *s, const char *path)
 {
-   if (s->nvar > 1) return fail(3, "checkpoint: one elliptic variable only");
    FILE *f;
    int g, rc = 0;
-   const int hdr[6] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids, s->nsrc, 0};
-   const unsigned long long oh = dop_hash(&s->dop);
+   const int hdr[6] = {CKPT_VERSION, s->h.dim, s->h.pde, s->h.ngrids, s->nsrc, s->nvar};
+   const unsigned long long oh = ops_hash(s);
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (!(f = fopen(path, "wb"))) return fail(5, "checkpoint: cannot open %s for writing", path);
    if (fwrite(CKPT_MAGIC, 1, 8, f) != 8 || fwrite(hdr, sizeof(int), 6, f) != 6 || fwrite(&oh, 8, 1, f) != 1)
@@ -1801,9 +1811,9 @@ int pgb_checkpoint_save(pgb_solver *s, const char *path)
       }
       if (fwrite(meta, sizeof(int), 4, f) != 4 || fwrite(b->bbox, sizeof(double), 6, f) != 6)
          rc = fail(5, "checkpoint: write failed");
-      for (k = 0; k <= s->nsrc && !rc; k++) {   /* u, then the sources */
-         if (cudaMemcpyAsync(buf, db->f[k ? PGB_SRC_FIELD(k - 1) : PGB_F_U], sizeof(double) * n,
-                             cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+      for (k = 0; k < s->nvar + s->nsrc && !rc; k++) {   /* u of each variable, then the sources */
+         if (cudaMemcpyAsync(buf, db->f[k >= s->nvar ? PGB_SRC_FIELD(k - s->nvar) : PGB_FV(k, PGB_F_U)],
+                             sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
              cudaStreamSynchronize(s->stream) != cudaSuccess)
             rc = fail(11, "checkpoint: device read failed");
          else if (fwrite(buf, sizeof(double), n, f) != n)
@@ -1819,11 +1829,10 @@ int pgb_checkpoint_save(pgb_solver *s, const char *path)
  * a copy that then fails (a CUDA error) can leave earlier grids restored. */
 int pgb_checkpoint_load(pgb_solver *s, const char *path)
 {
-   if (s->nvar > 1) return fail(3, "checkpoint: one elliptic variable only");
    FILE *f;
    char magic[8];
    int hdr[6], g, k, rc = 0, ng = s->h.ngrids;
-   const int nf = s->nsrc + 1;
+   const int nf = s->nsrc + s->nvar;
    unsigned long long oh = 0;
    double **buf;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
@@ -1833,10 +1842,10 @@ int pgb_checkpoint_load(pgb_solver *s, const char *path)
       fclose(f);
       return fail(6, "checkpoint: %s is not a checkpoint", path);
    }
-   if (hdr[0] != CKPT_VERSION || hdr[1] != s->h.dim || hdr[2] != s->h.pde || hdr[3] != ng ||
-       hdr[4] != s->nsrc || oh != dop_hash(&s->dop)) {
+   if (!(hdr[0] == CKPT_VERSION || (hdr[0] == 2 && hdr[5] == 0)) || hdr[1] != s->h.dim || hdr[2] != s->h.pde ||
+       hdr[3] != ng || hdr[4] != s->nsrc || (hdr[0] == 2 ? 1 : hdr[5]) != s->nvar || oh != ops_hash(s)) {
       fclose(f);
-      return fail(6, "checkpoint: version, dimension, operator or grid count differ from the solver's");
+      return fail(6, "checkpoint: version, dimension, operators, variable or grid count differ from the solver's");
    }
    buf = (double **)calloc((size_t)nf * (size_t)(ng ? ng : 1), sizeof(double *));
    if (!buf) {
@@ -1868,8 +1877,10 @@ int pgb_checkpoint_load(pgb_solver *s, const char *path)
    fclose(f);
    for (g = 0; g < ng && !rc; g++) {
       if (s->h.grid_box[g] < 0) continue;
-      rc = pgb_set_grid(s, g, buf[(size_t)nf * g], buf[(size_t)nf * g + 1]);
-      for (k = 1; k < s->nsrc && !rc; k++) rc = pgb_set_source(s, g, k, buf[(size_t)nf * g + 1 + k]);
+      const size_t o = (size_t)nf * g;
+      rc = pgb_set_grid(s, g, buf[o], buf[o + s->nvar]);
+      for (k = 1; k < s->nvar && !rc; k++) rc = pgb_set_var(s, g, k, buf[o + k]);
+      for (k = 1; k < s->nsrc && !rc; k++) rc = pgb_set_source(s, g, k, buf[o + s->nvar + k]);
    }
    for (g = 0; g < nf * ng; g++) free(buf[g]);
    free(buf);

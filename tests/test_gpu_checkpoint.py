@@ -59,3 +59,40 @@ def test_mismatched_or_foreign_files_are_refused(tmp_path):
         assert np.array_equal(x, y)
     small.close()
     other.close()
+
+
+def test_several_variables_restart_bit_for_bit(tmp_path):
+    """a solver of two coupled elliptic variables (reference fixture case)
+    checkpointed after three V-cycles: the restored solver holds both
+    variables bit for bit and finishes the solve exactly as the original"""
+    import golden_cases as G
+    case, _ = G.load(G.coupled_files()[0])
+    assert case.nvar == 2
+    a = Solver(case)
+    a.set_inputs()
+    for _ in range(3):
+        a.vcycle()
+    saved = a.get_vars()
+    path = str(tmp_path / "coupled.ckpt")
+    a.checkpoint_save(path)
+    ra = a.solve()
+    b = Solver(case)
+    b.set_inputs()
+    b.checkpoint_load(path)
+    for va, vb in zip(saved, b.get_vars()):
+        for x, y in zip(va, vb):
+            assert np.array_equal(x, y)
+    rb = b.solve()
+    assert ra["iters"] == rb["iters"]
+    for va, vb in zip(a.get_vars(), b.get_vars()):
+        for x, y in zip(va, vb):
+            assert np.array_equal(x, y)
+    # a one-variable checkpoint does not load into the two-variable solver
+    one = Solver(W.lapse2d_bo(33, seed=6, levels=3, steps=8))
+    one.set_inputs()
+    p1 = str(tmp_path / "one.ckpt")
+    one.checkpoint_save(p1)
+    with pytest.raises(PgbError):
+        b.checkpoint_load(p1)
+    for s in (a, b, one):
+        s.close()
