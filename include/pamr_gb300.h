@@ -286,9 +286,11 @@ int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per
 /* Mixed form: MG levels 1..n (the return value; 0 when none) whose V-cycle
  * passes run as one launch of the small-level kernel, a thread-block
  * cluster of *cluster_ctas CTAs (levels of at most PGB_TAIL_POINTS points,
- * 6000 unless set). Off unless the environment sets PGB_TAIL=1 (it gives
- * the same bits and was measured slower than one launch per pass on
- * GB300); pgb_level_tuning reports sweep mode 8 for those levels. Known
+ * 6000 unless set). Off unless the environment sets PGB_TAIL=1 (or
+ * PGB_TAIL=mini: one CTA, the levels' arrays in its shared memory, levels of
+ * at most 1500 points); it gives the same bits and was measured slower than
+ * one launch per pass on GB300. pgb_level_tuning reports sweep mode 8 for
+ * those levels. Known
  * after the first pgb_prepare. No reference counterpart (the reference
  * relaxes grid by grid on the host). */
 int pgb_tail_levels(const pgb_solver *s, int *cluster_ctas);

@@ -175,13 +175,18 @@ typedef struct {
                                            cooperative launch, meeting at a counter in global memory */
    unsigned int *bar_cnt;               /* that counter (zeroed before each launch) */
    int *err;                            /* set to 4 when a wait at it runs out (about 0.5 s) */
+   int mini;                            /* 1: one CTA, the levels' arrays staged in shared memory */
+   int nbox_all;                        /* boxes of the whole box table (copied when mini) */
+   size_t mini_off;                     /* where the staged arrays start in shared memory */
    pgb_dlevel lv[PGB_TAIL_MAXLEV];
    pgb_coarsest_args ca;                /* the coarsest-grid loop's arguments */
    const pgb_copy_op *csync;            /* and its sync ops */
    pgb_tail_step step[PGB_TAIL_MAXSTEP];
 } pgb_tail_prog;
 
-void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox);
+/* mini_bytes > 0: mini mode, the program's levels' arrays (that many bytes)
+ * staged in the shared memory of one CTA */
+void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox, size_t mini_bytes);
 /* steps recorded from now on run in CTA 0 alone (levels so small that one
  * CTA's L1 holds them: consecutive such steps meet at a CTA barrier) */
 void pgb_tail_set_solo(int on);

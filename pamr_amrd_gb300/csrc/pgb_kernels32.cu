@@ -1983,10 +1983,63 @@ __device__ __forceinline__ void grid_barrier(unsigned int *cnt, unsigned int tar
    __syncthreads();
 }
 
+/* Mini mode: the arrays of the program's levels staged in shared memory
+ * (in = 1: copied in and the shared box table pointed at them; in = 0:
+ * grid functions and FP32 arrays copied back). Every thread walks the same
+ * regions in the same order (levels, their boxes, fields, FP32 arrays,
+ * masks; 16-byte aligned), which is also the order the host sized them in. */
+__device__ void tail_stage(const pgb_tail_prog &P, const pgb_dbox *gboxes, pgb_dbox *sbt, unsigned char *m, int in,
+                           int lt)
+{
+   for (int li = 0; li < P.nlev; li++) {
+      const pgb_dlevel &g = P.lv[li];
+      for (int bi = 0; bi < g.nbox; bi++) {
+         const int gb = g.box[bi];
+         const pgb_dbox &gx = gboxes[gb];
+         const long n = (long)gx.n[0] * gx.n[1] * gx.n[2];
+         for (int f = 0; f < PGB_NF; f++) {
+            if (!gx.f[f]) continue;
+            long long *d = (long long *)m, *a = (long long *)gx.f[f];
+            if (in) {
+               for (long i = lt; i < n; i += NT) d[i] = a[i];
+               if (lt == 0) sbt[gb].f[f] = (double *)d;
+            } else
+               for (long i = lt; i < n; i += NT) a[i] = d[i];
+            m += (n * 8 + 15) / 16 * 16;
+         }
+         for (int w = 0; w < PGB_NW32; w++) {
+            if (!gx.w32[w]) continue;
+            const long nw = gx.wz * gx.n[2];
+            int *d = (int *)m, *a = (int *)gx.w32[w];
+            if (in) {
+               for (long i = lt; i < nw; i += NT) d[i] = a[i];
+               if (lt == 0) sbt[gb].w32[w] = (float *)d;
+            } else
+               for (long i = lt; i < nw; i += NT) a[i] = d[i];
+            m += (nw * 4 + 15) / 16 * 16;
+         }
+         for (int c = 0; c < 2; c++) {   /* the masks are only read */
+            const uint8_t *a = c ? gx.cmask_bdy : gx.cmask_child;
+            if (!a) continue;
+            if (in) {
+               uint8_t *d = (uint8_t *)m;
+               for (long i = lt; i < n; i += NT) d[i] = a[i];
+               if (lt == 0) {
+                  if (c) sbt[gb].cmask_bdy = d;
+                  else sbt[gb].cmask_child = d;
+               }
+            }
+            m += (n + 15) / 16 * 16;
+         }
+      }
+   }
+}
+
 template <bool PROG>
 __global__ void __launch_bounds__(NT, 1) k_tail(const pgb_dbox *boxes, const __grid_constant__ pgb_tail_prog Pk,
                                                 pgb_scratch sc)
 {
+   const pgb_dbox *const gboxes = boxes;
    const int lt = threadIdx.x + PGB_TX * threadIdx.y;
    const pgb_tail_prog *Pp = &Pk;
    if (Pk.prog_off) {
@@ -2025,6 +2078,10 @@ __global__ void __launch_bounds__(NT, 1) k_tail(const pgb_dbox *boxes, const __g
          }
       }
       __syncthreads();
+      if (Pk.mini) {   /* the levels' arrays into shared memory, the shared box table pointed at them */
+         tail_stage(Pk, gboxes, (pgb_dbox *)boxes, tail_sm + Pk.mini_off, 1, lt);
+         __syncthreads();
+      }
       Pp = c;
    }
    const pgb_tail_prog &P = *Pp;
@@ -2071,21 +2128,30 @@ __global__ void __launch_bounds__(NT, 1) k_tail(const pgb_dbox *boxes, const __g
          }
       }
       if (st.bar == 1) {
-         if (P.grid)
+         if (P.mini)
+            __syncthreads();
+         else if (P.grid)
             grid_barrier(P.bar_cnt, ++nbar * gridDim.x, P.err);
          else
             cluster_barrier();
       } else if (st.bar == 2 && blockIdx.x == 0)   /* between two steps of CTA 0 alone */
          __syncthreads();
    }
+   if (Pk.mini && Pk.prog_off) {   /* the results back to the device arrays */
+      extern __shared__ __align__(16) unsigned char tail_sm[];
+      __syncthreads();
+      tail_stage(Pk, gboxes, 0, tail_sm + Pk.mini_off, 0, lt);
+   }
 }
 
 
-extern "C" void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox)
+extern "C" void pgb_tail_begin(pgb_tail_prog *p, int pde, int nbox, size_t mini_bytes)
 {
    memset(p, 0, sizeof(*p));
    p->pde = pde;
-   p->nbox_copy = nbox;
+   p->nbox_copy = p->nbox_all = nbox;
+   p->mini = mini_bytes > 0;
+   p->mini_off = mini_bytes;   /* the staged bytes until the layout is known */
    g_tp = p;
    g_tp_bad = 0;
    g_tp_solo = 0;
@@ -2099,21 +2165,32 @@ extern "C" int pgb_tail_end(void)
    g_tp = 0;
    /* barriers: CTA 0's own between two of its solo steps, the cluster's
     * wherever work changes hands (and after the last step nothing) */
-   if (P && !g_tp_bad && !getenv("PGB_TAIL_GLOBALPROG")) {
+   if (P && !g_tp_bad && (P->mini || !getenv("PGB_TAIL_GLOBALPROG"))) {
       /* shared memory: the coarsest loop's, then the program, the box table
        * (unless it is large) and the levels' tile and box lists */
       size_t q = (P->smem + 15) / 16 * 16 + 16;
       P->prog_off = q;
       q += (sizeof(pgb_tail_prog) + 15) / 16 * 16;
-      if ((size_t)P->nbox_copy * sizeof(pgb_dbox) > 48 * 1024) P->nbox_copy = 0;
+      if (!P->mini && (size_t)P->nbox_copy * sizeof(pgb_dbox) > 48 * 1024) P->nbox_copy = 0;
       q += ((size_t)P->nbox_copy * sizeof(pgb_dbox) + 15) / 16 * 16;
       for (int li = 0; li < P->nlev; li++) {
          const pgb_dlevel &g = P->lv[li];
          q += ((size_t)g.ntiles * sizeof(pgb_tile) + 15) / 16 * 16 + ((size_t)g.nrtiles * sizeof(pgb_tile) + 15) / 16 * 16 +
               ((size_t)g.nctiles * sizeof(pgb_tile) + 15) / 16 * 16 + ((size_t)g.nbox * 4 + 15) / 16 * 16;
       }
+      if (P->mini) {   /* then the staged arrays */
+         const size_t staged = P->mini_off;
+         P->mini_off = q;
+         q += staged;
+      }
       P->smem_total = q;
-      if (q > 200 * 1024) P->prog_off = 0;   /* does not fit: read in place */
+      if (q > 200 * 1024) {
+         if (P->mini) {
+            snprintf(g_err32, sizeof(g_err32), "small-level kernel: %zu bytes of shared memory", q);
+            return 1;
+         }
+         P->prog_off = 0;   /* does not fit: read in place */
+      }
    } else if (P)
       P->nbox_copy = 0;
    if (P && !g_tp_bad)
@@ -2219,7 +2296,10 @@ static cudaError_t tail_launch(const pgb_dbox *boxes, const pgb_tail_prog *p, in
    cudaLaunchAttribute at[1];
    memset(&cfg, 0, sizeof(cfg));
    memset(at, 0, sizeof(at));
-   if (p->grid) {
+   if (p->mini) {
+      ncta = 1;
+      cfg.numAttrs = 0;
+   } else if (p->grid) {
       at[0].id = cudaLaunchAttributeCooperative;
       at[0].val.cooperative = 1;
    } else {
@@ -2233,7 +2313,7 @@ static cudaError_t tail_launch(const pgb_dbox *boxes, const pgb_tail_prog *p, in
    cfg.dynamicSmemBytes = p->prog_off ? p->smem_total : p->smem;
    cfg.stream = st;
    cfg.attrs = at;
-   cfg.numAttrs = 1;
+   cfg.numAttrs = p->mini ? 0 : 1;
    cudaError_t e = tail_attrs<PROG>();
    if (e != cudaSuccess) return e;
    return cudaLaunchKernelEx(&cfg, k_tail<PROG>, boxes, *p, sc);

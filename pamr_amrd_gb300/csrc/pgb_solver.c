@@ -73,6 +73,7 @@ struct pgb_solver {
    int tail_ncta;           /* its cluster size */
    int tail_solo;           /* levels 1..tail_solo of those run in one CTA (their steps need no cluster) */
    int tail_grid;           /* 0: one cluster; else the CTAs of a cooperative launch (one per SM) */
+   size_t tail_mini;        /* mini mode: bytes of the levels' arrays staged in one CTA's shared memory */
    unsigned int *d_tailbar; /* its barrier counter */
    pgb_tail_prog *tail;     /* its program, recorded by each V-cycle launch or capture */
 };
@@ -911,12 +912,15 @@ static int tail_plan(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
    const char *env = getenv("PGB_TAIL"), *pts = getenv("PGB_TAIL_POINTS"), *sol = getenv("PGB_TAIL_SOLO");
-   const long maxp = pts ? atol(pts) : 6000, maxsolo = sol ? atol(sol) : 0;
+   const int mini = env && !strcmp(env, "mini");
+   const long maxp = pts ? atol(pts) : mini ? 1500 : 6000, maxsolo = sol ? atol(sol) : 0;
+   size_t staged = 0;
    const int nsw = h->prm.pre_swp + h->prm.pst_swp;
    int L, b, Lc = 0, steps = 1;
    pgb_coarsest_args a;
    s->tail_lc = s->tail_solo = 0;
-   if (!env || strcmp(env, "1") || h->prm.precision != PGB_MIXED || s->nvar > 1 || h->nlev < 3 || fp64_level1(s))
+   s->tail_mini = 0;
+   if (!env || (strcmp(env, "1") && !mini) || h->prm.precision != PGB_MIXED || s->nvar > 1 || h->nlev < 3 || fp64_level1(s))
       return 0;
    coarsest_args(s, 1, &a);
    if (a.ncoarse != 1 || a.smem_points <= 0 ||
@@ -929,6 +933,21 @@ static int tail_plan(pgb_solver *s)
          n += (long)bx->shape[0] * bx->shape[1] * bx->shape[2];
       }
       if (n > maxp || h->sync[L][0].nops || h->sync[L][1].nops || (L > 1 && lvl_coarsest(s, L))) break;
+      if (mini) {   /* the level's arrays in one CTA's shared memory, laid out as the kernel stages them */
+         size_t add = 0;
+         int f;
+         for (b = 0; b < h->lev[L].nbox; b++) {
+            const pgb_dbox *db = &s->hbox[h->lev[L].box[b]];
+            const size_t np = (size_t)db->n[0] * db->n[1] * db->n[2];
+            for (f = 0; f < PGB_NF; f++)
+               if (db->f[f]) add += (np * 8 + 15) / 16 * 16;
+            for (f = 0; f < PGB_NW32; f++)
+               if (db->w32[f]) add += ((size_t)db->wz * db->n[2] * 4 + 15) / 16 * 16;
+            add += 2 * ((np + 15) / 16 * 16);
+         }
+         if (staged + add > 150 * 1024 || (size_t)h->nbox * sizeof(pgb_dbox) > 32 * 1024) break;
+         staged += add;
+      }
       if (n <= maxsolo && s->tail_solo == L - 1) s->tail_solo = L;
       /* a bound on the steps a level adds (passes of the down and up sweep) */
       steps += 10 + 2 * nsw + h->inject[L].nbatch + 2 * h->interp[L].nbatch;
@@ -937,7 +956,24 @@ static int tail_plan(pgb_solver *s)
    }
    if (Lc < 2) return 0;
    if (s->tail_solo > Lc) s->tail_solo = Lc;
-   s->tail_ncta = pgb_tail_max_cluster((size_t)a.smem_points * (sizeof(double) + 3 * sizeof(float) + sizeof(int)));
+   if (mini) {
+      /* recompute the staged bytes of exactly levels 1..Lc */
+      staged = 0;
+      for (L = 1; L <= Lc; L++)
+         for (b = 0; b < h->lev[L].nbox; b++) {
+            const pgb_dbox *db = &s->hbox[h->lev[L].box[b]];
+            const size_t np = (size_t)db->n[0] * db->n[1] * db->n[2];
+            int f;
+            for (f = 0; f < PGB_NF; f++)
+               if (db->f[f]) staged += (np * 8 + 15) / 16 * 16;
+            for (f = 0; f < PGB_NW32; f++)
+               if (db->w32[f]) staged += ((size_t)db->wz * db->n[2] * 4 + 15) / 16 * 16;
+            staged += 2 * ((np + 15) / 16 * 16);
+         }
+      s->tail_mini = staged;
+      s->tail_ncta = 1;
+   } else
+      s->tail_ncta = pgb_tail_max_cluster((size_t)a.smem_points * (sizeof(double) + 3 * sizeof(float) + sizeof(int)));
    if (s->tail_ncta < 1) return 0;
    {
       const char *gm = getenv("PGB_TAIL_GRID");
@@ -948,7 +984,13 @@ static int tail_plan(pgb_solver *s)
    if (!s->tail && !(s->tail = (pgb_tail_prog *)malloc(sizeof(pgb_tail_prog))))
       return fail(10, "small-level kernel: host buffer");
    s->tail_lc = Lc;
-   for (L = 1; L <= Lc; L++) s->fuse[L] = 0;
+   for (L = 1; L <= Lc; L++) {
+      s->fuse[L] = 0;
+      /* one CTA walks a step's blocks in turn: tiles of the full depth make
+       * them few (a 9^3 level is 4 tiles of 32 x 8 x 8 points) */
+      if (mini && h->dim == 3 && s->lv[L].tz != PGB_TZ && level_tables(s, L, PGB_TZ)) return 10;
+   }
+   if (mini) drop_graph(s);
    return 0;
 }
 
@@ -1364,7 +1406,7 @@ static int vcycle_mixed(pgb_solver *s)
          if (h->inject[L].nops)
             KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), s->res32[L + 1], s->stream));
          if (sync_field(s, &h->sync[L][0], PGB_F_U)) return 11;
-         if (L == tail) pgb_tail_begin(s->tail, h->pde, h->nbox);
+         if (L == tail) pgb_tail_begin(s->tail, h->pde, h->nbox, s->tail_mini);
          pgb_tail_set_solo(L <= s->tail_solo);   /* passes over level L */
          if (L == 1) KC32(pgb_k_lop_rhs_fast(s->dbox, s->lv[L], h->pde, p->w0_r, s->stream));
          else KC32(pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, p->w0_r, s->dnext[L], s->stream));
