@@ -17,14 +17,14 @@
  *      reference's last set_cmask_bdy leaves in it (amrd/mg.c:132, the MG
  *      cmask aliases the AMR one, src/gh.c:1139-1147).
  * vcycle(giter, save_tre) (amrd/mg.c:84-201) works on the MG hierarchy the
- * caller built with PAMR_build_mgh: u and the sources of every MG level are
- * copied from PAMR's MG grids (PAMR built or injected them there), one
- * V-cycle runs on the device, and u of every MG level and f_res of the
- * finest come back.
+ * caller built with PAMR_build_mgh: every elliptic variable's u and the
+ * sources of every MG level are copied from PAMR's MG grids (PAMR built or
+ * injected them there), one V-cycle runs on the device, and each variable's
+ * u on every MG level and its f_res on the finest come back.
  *
  * Limits (each reported by a message and AMRD_stop, as AMRD reports
- * errors): up to four elliptic variables in solve_elliptics (FP64 form,
- * every variable with the first one's MG transfers), one in vcycle;
+ * errors): up to four elliptic variables (FP64 form, every variable with
+ * the first one's MG transfers);
  * save_tre = 0; no periodic boundaries;
  * no t0 initialisation hook or constraint-data variables (AMRD_is_t0 runs
  * of generate_id with app_elliptic_vars_t0_init / MG_cnst_data); one MPI
@@ -481,13 +481,14 @@ double vcycle(int giter, int save_tre)
 {
    const char *var = AMRD_elliptic_vars[0];
    int Lmg = PAMR_get_max_lev(ABI_PAMR_MGH), Lamr = PAMR_get_max_lev(ABI_PAMR_AMRH);
-   int gm, L = 0, m, k, gms[MAXSRC], gres, num_tl = 1, tl;
+   int gm, L = 0, m, k, gms[MAXSRC], gres, num_tl = 1, tl, v, nv = AMRD_num_elliptic_vars;
+   int gmv[PGB_MAX_VARS], gresv[PGB_MAX_VARS];
    double res = 0;
    vattr a;
    (void)giter;
    if (save_tre) stop("vcycle: save_tre is not supported on the device", "");
    if (Lmg < 1) stop("vcycle: no MG hierarchy (PAMR_build_mgh first)", "");
-   if (AMRD_num_elliptic_vars != 1) stop("vcycle: the device's single V-cycle carries one elliptic variable", "");
+   if (nv < 1 || nv > PGB_MAX_VARS) stop("vcycle: 1 to 4 elliptic variables", "");
    gm = gfn(var, ABI_PAMR_MGH, 0);
    if (var_attr(var, &a)) num_tl = a.num_tl;
    /* which AMR levels the MG hierarchy replicates: an MG grid of an AMR
@@ -515,11 +516,14 @@ double vcycle(int giter, int save_tre)
    ensure_solver(L, Lamr);
    if (pgb_num_levels(G.s) != Lmg) stop("vcycle: the MG hierarchy differs from the device hierarchy", "");
    for (k = 0; k < G.nsrc; k++) gms[k] = gfn(G.src_names[k], ABI_PAMR_MGH, 0);
-   {
+   if (G.nvar != nv) stop("vcycle: the device hierarchy carries another number of elliptic variables", "");
+   for (v = 0; v < nv; v++) {   /* every elliptic variable and its f_res on the MG hierarchy */
       char rn[512];
-      snprintf(rn, sizeof(rn), "%s_res", var);
-      gres = gfn(rn, ABI_PAMR_MGH, 0);
+      gmv[v] = gfn(AMRD_elliptic_vars[v], ABI_PAMR_MGH, 0);
+      snprintf(rn, sizeof(rn), "%s_res", AMRD_elliptic_vars[v]);
+      gresv[v] = gfn(rn, ABI_PAMR_MGH, 0);
    }
+   gres = gresv[0];
    /* copy in every MG level's u and sources, in PAMR grid-list order */
    for (m = 1; m <= Lmg; m++) {
       int idx = 0, valid = PAMR_init_s_iter(m, ABI_PAMR_MGH, 0);
@@ -534,6 +538,8 @@ double vcycle(int giter, int save_tre)
          if (sh[0] != g.shape[0] || sh[1] != g.shape[1] || sh[2] != g.shape[2] || !same_bbox(bb, g.bbox, g.dim, dx))
             stop("vcycle: the MG hierarchy differs from the device hierarchy", "");
          ok_pgb(pgb_box_set(G.s, m, idx, PGB_FIELD_U, g.gfs[gm - 1]), "copying u");
+         for (v = 1; v < nv; v++)
+            ok_pgb(pgb_box_set(G.s, m, idx, PGB_FIELD_VAR(v) + PGB_FIELD_U, g.gfs[gmv[v] - 1]), "copying a variable");
          for (k = 0; k < G.nsrc; k++)
             ok_pgb(pgb_box_set(G.s, m, idx, PGB_FIELD_SRC + k, g.gfs[gms[k] - 1]), "copying a source");
          idx++;
@@ -551,6 +557,12 @@ double vcycle(int giter, int save_tre)
          attribs(&g);
          ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_U, g.gfs[gm - 1]), "reading u back");
          if (m == Lmg) ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_RES, g.gfs[gres - 1]), "reading f_res back");
+         for (v = 1; v < nv; v++) {
+            ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_VAR(v) + PGB_FIELD_U, g.gfs[gmv[v] - 1]), "reading a variable back");
+            if (m == Lmg)
+               ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_VAR(v) + PGB_FIELD_RES, g.gfs[gresv[v] - 1]),
+                      "reading a variable's f_res back");
+         }
          if (AMRD_cmask_mg_gfn > 0) put_bdy_mask(m, idx, g.gfs[AMRD_cmask_mg_gfn - 1]);
          idx++;
          valid = PAMR_next_g();
