@@ -193,10 +193,13 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
  * since the last pgb_prepare. */
 int pgb_prepare(pgb_solver *s);
 int pgb_vcycle(pgb_solver *s, double *res);
-/* pgb_prepare with flags: PGB_PREPARE_KEEP_MG_DATA leaves u and the sources
- * of the pure MG levels as stored with pgb_box_set instead of injecting
- * them from the AMR levels (an MG hierarchy that already exists, as PAMR
- * keeps it between the vcycle calls of amrd/evolve.c:471-487) */
+/* pgb_prepare with flags: PGB_PREPARE_KEEP_MG_DATA leaves u of the pure MG
+ * levels as stored with pgb_box_set instead of injecting it from the AMR
+ * levels (an MG hierarchy that already exists, as PAMR keeps it between the
+ * vcycle calls of amrd/evolve.c:471-487); their sources are injected from
+ * the level above, as the reference's vcycle does in its down sweep
+ * (src/pamr.c:677-680), so sources changed on the AMR levels since the
+ * hierarchy was built reach them */
 #define PGB_PREPARE_KEEP_MG_DATA 1
 int pgb_prepare_ex(pgb_solver *s, int flags);
 

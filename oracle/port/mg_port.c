@@ -24,7 +24,13 @@
 #define dmax(a, b) (((a) > (b)) ? (a) : (b))
 #define dmin(a, b) (((a) < (b)) ? (a) : (b))
 
-enum { G_SRC = 0, G_U, G_RES, G_LOP, G_RHS, G_CMASK, G_SRC1, G_SRC2, G_SRC3, NGF };
+enum { G_SRC = 0, G_U, G_RES, G_LOP, G_RHS, G_CMASK, G_SRC1, G_SRC2, G_SRC3, G_W, G_WRES, NGF };
+/* G_W, G_WRES: a second elliptic variable and its MG residual, carried (built,
+ * injected, synced, interpolated like u and u_res) but never relaxed here:
+ * only when port_carry_second_var(1) was called (the drop-in environment's
+ * coupled cases, whose solve runs elsewhere) */
+static int port_nw = 0;
+void port_carry_second_var(int on) { port_nw = on != 0; }
 /* source k of the operator (k < oracle_nsrc) */
 #define G_SRCK(k) ((k) ? G_SRC1 + (k) - 1 : G_SRC)
 static int is_src(int gf) { return gf == G_SRC || gf >= G_SRC1; }
@@ -81,16 +87,19 @@ static int mg_inject_of(int gf)
    switch (gf) {
    case G_U: return P.c->restr_u;
    case G_RES: return P.c->restr_res;
+   case G_W: return port_nw ? P.c->restr_u : 0;
+   case G_WRES: return port_nw ? P.c->restr_res : 0;
    default: return 0;
    }
 }
 static int mg_noinj_to_amr(int gf) { return is_src(gf); }  /* hyperbolic vars */
-static int in_amrh(int gf) { return is_src(gf) || gf == G_U || gf == G_CMASK; }
+static int in_amrh(int gf) { return is_src(gf) || gf == G_U || gf == G_CMASK || (port_nw && gf == G_W); }
 /* the fields a grid holds: every source the operator reads */
 static int used_fields(int mask)
 {
    int k;
    for (k = oracle_nsrc(P.c->pde); k < 4; k++) mask &= ~(1 << G_SRCK(k));
+   if (!port_nw) mask &= ~((1 << G_W) | (1 << G_WRES));
    return mask;
 }
 
@@ -111,10 +120,10 @@ static void set_tf_bits(int stage)
    for (gf = 0; gf < NGF; gf++) {
       op = 0;
       switch (stage) {
-      case TF_SYNC: op = (gf == G_U) ? 1 : 0; break;                       /* mg_sync = [u] */
+      case TF_SYNC: op = (gf == G_U || (port_nw && gf == G_W)) ? 1 : 0; break;   /* mg_sync = [u (w)] */
       case TF_INJECT: op = mg_noinj_to_amr(gf) ? 0 : mg_inject_of(gf); break;
       case TF_INJECT_TO_MG_LEV: op = mg_inject_of(gf); break;
-      case TF_INTERP: op = (gf == G_RES) ? P.c->interp_order : 0; break;  /* mg_interp2 = [u] */
+      case TF_INTERP: op = (gf == G_RES || (port_nw && gf == G_WRES)) ? P.c->interp_order : 0; break;   /* mg_interp2 */
       case TF_MGH_INIT: op = in_amrh(gf) ? mg_inject_of(gf) : 0; break;
       }
       P.tf[gf] = op;
@@ -641,8 +650,8 @@ static void build_mgh(void)
             ng->coarsest = 0;
             memset(ng->own, 0, sizeof(ng->own));
             ng->own_x = 0;
-            ng->gf[G_RES] = ng->gf[G_LOP] = ng->gf[G_RHS] = 0;
-            alloc_fields(ng, (1 << G_RES) | (1 << G_LOP) | (1 << G_RHS));
+            ng->gf[G_RES] = ng->gf[G_LOP] = ng->gf[G_RHS] = ng->gf[G_WRES] = 0;
+            alloc_fields(ng, used_fields((1 << G_RES) | (1 << G_LOP) | (1 << G_RHS) | (1 << G_WRES)));
             if (last) last->next = ng; else tmp[cl].grids = ng;
             last = ng;
          }
@@ -1030,7 +1039,7 @@ static int port_compose(const port_case *c, port_result *r)
             pgrid *nx = g->next;
             g->next = 0;
             alloc_fields(g, used_fields((1 << G_SRC) | (1 << G_U) | (1 << G_CMASK) | (1 << G_SRC1) |
-                                        (1 << G_SRC2) | (1 << G_SRC3)));
+                                        (1 << G_SRC2) | (1 << G_SRC3) | (1 << G_W)));
             insert_grid(&P.amr[l], g);
             g = nx;
          }

@@ -15,9 +15,10 @@
  * and "cmask", one time level. gfn numbering of this environment:
  *   u 1 (AMR) / 2 (MG), rho 3 / 4, rho1 5 / 6, u_res 7, u_lop 8, u_rhs 9,
  *   cmask 10 / 11.
- * A coupled case adds a second elliptic variable "w" on the AMR grids (gfn
- * 12, kept here beside the port's grids; its MG instances are not built, so
- * only solve_elliptics runs on such a case).
+ * A coupled case adds a second elliptic variable "w" (gfn 12 AMR / 13 MG)
+ * and its MG residual w_res (14), carried by the port's grids and MG
+ * hierarchy like u and u_res (port_carry_second_var), so that both
+ * solve_elliptics and vcycle run on such a case.
  */
 #include "mg_port.c"
 #include "../../tests/dropin/dropin_case.h"
@@ -52,18 +53,8 @@ static int *E_lev;
 static double *E_bbox;
 static double **E_u, **E_src, **E_src1;
 static const double *E_srcx[1][4096];
-/* the second elliptic variable of a coupled case, per AMR grid */
+/* a coupled case: a second elliptic variable */
 static int E_nw;
-static const void *E_wg[4096];
-static double *E_w[4096];
-
-static double *w_of(const void *g)
-{
-   int i;
-   for (i = 0; i < E_nw; i++)
-      if (E_wg[i] == g) return E_w[i];
-   return 0;
-}
 
 int env_init(const char *case_path, const char *param_path)
 {
@@ -105,12 +96,13 @@ int env_init(const char *case_path, const char *param_path)
    E_case.interp_order = 2;
    E_case.interp_buffer = 2;
    E_case.min_level = 1;
+   E_nw = dc.coupled != 0;
+   port_carry_second_var(E_nw);
    if (port_compose(&E_case, 0)) return 3;
    if (dc.coupled) {   /* w on every AMR grid, from the case */
       int l;
       AMRD_num_elliptic_vars = 2;
       AMRD_elliptic_vars[1] = "w";
-      E_nw = 0;
       for (l = 1; l <= P.n_amr; l++)
          for (pgrid *g = P.amr[l].grids; g; g = g->next) {
             long n = (long)g->shape[0] * g->shape[1] * g->shape[2];
@@ -120,11 +112,8 @@ int env_init(const char *case_path, const char *param_path)
                   if (fabs(dc.bbox[6 * i + q] - g->bbox[q]) > 1e-9 * (1 + fabs(g->bbox[q]))) same = 0;
                if (same) break;
             }
-            if (i == dc.ngrids || E_nw >= 4096) return 4;
-            E_wg[E_nw] = g;
-            E_w[E_nw] = (double *)malloc(sizeof(double) * (size_t)n);
-            memcpy(E_w[E_nw], dc.w[i], sizeof(double) * (size_t)n);
-            E_nw++;
+            if (i == dc.ngrids || !g->gf[G_W]) return 4;
+            memcpy(g->gf[G_W], dc.w[i], sizeof(double) * (size_t)n);
          }
    }
    AMRD_MG_pre_swp = E_case.pre_swp;
@@ -209,10 +198,10 @@ int PAMR_get_g_attribs(int *rank, int *dim, int *shape, double *bbox, int *ghost
       x[d] = g->x[d];
    }
    *t = 0;
-   *ngfs = 12;
-   for (d = 0; d < 12; d++) gfs[d] = 0;
+   *ngfs = 14;
+   for (d = 0; d < 14; d++) gfs[d] = 0;
    if (E_it.hier == 1) {
-      gfs[11] = w_of(g);
+      gfs[11] = g->gf[G_W];
       gfs[0] = g->gf[G_U];
       gfs[2] = g->gf[G_SRC];
       gfs[4] = g->gf[G_SRC1];
@@ -225,6 +214,8 @@ int PAMR_get_g_attribs(int *rank, int *dim, int *shape, double *bbox, int *ghost
       gfs[7] = g->gf[G_LOP];
       gfs[8] = g->gf[G_RHS];
       gfs[10] = g->gf[G_CMASK];
+      gfs[12] = g->gf[G_W];
+      gfs[13] = g->gf[G_WRES];
    }
    return 1;
 }
@@ -235,7 +226,7 @@ int PAMR_get_gfn(char *name, int hier, int tl)
       const char *n;
       int amr, mg;
    } tab[] = {{"u", 1, 2}, {"rho", 3, 4}, {"rho1", 5, 6}, {"u_res", 0, 7}, {"u_lop", 0, 8},
-              {"u_rhs", 0, 9}, {"cmask", 10, 11}, {"w", 12, 0}};
+              {"u_rhs", 0, 9}, {"cmask", 10, 11}, {"w", 12, 13}, {"w_res", 0, 14}};
    int i;
    for (i = 0; i < (int)(sizeof(tab) / sizeof(tab[0])); i++)
       if (!strcmp(name, tab[i].n)) {

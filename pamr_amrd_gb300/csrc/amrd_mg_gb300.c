@@ -20,7 +20,8 @@
  * caller built with PAMR_build_mgh: every elliptic variable's u and the
  * sources of every MG level are copied from PAMR's MG grids (PAMR built or
  * injected them there), one V-cycle runs on the device, and each variable's
- * u on every MG level and its f_res on the finest come back.
+ * u on every MG level, its f_res on the finest and the sources the cycle
+ * injected into the pure MG levels come back.
  *
  * Limits (each reported by a message and AMRD_stop, as AMRD reports
  * errors): up to four elliptic variables (FP64 form, every variable with
@@ -557,6 +558,10 @@ double vcycle(int giter, int save_tre)
          attribs(&g);
          ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_U, g.gfs[gm - 1]), "reading u back");
          if (m == Lmg) ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_RES, g.gfs[gres - 1]), "reading f_res back");
+         /* the sources the cycle injected into the pure MG levels, as the
+          * reference's vcycle leaves them in PAMR's MG grids */
+         for (k = 0; k < G.nsrc && m < Lmg; k++)
+            ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_SRC + k, g.gfs[gms[k] - 1]), "reading a source back");
          for (v = 1; v < nv; v++) {
             ok_pgb(pgb_box_get(G.s, m, idx, PGB_FIELD_VAR(v) + PGB_FIELD_U, g.gfs[gmv[v] - 1]), "reading a variable back");
             if (m == Lmg)

@@ -1108,6 +1108,17 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
    }
    for (L = s->h.nlev - 1; L >= 1 && !keep; L--)
       if (s->h.inject_init[L].nops) KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], ~0, 0, s->stream));
+   /* With the caller's MG-level data, the sources of the pure MG levels are
+    * still injected from the level above, top down: the reference's vcycle
+    * does so in its down sweep (PAMR_inject into a level outside the AMR
+    * hierarchy takes every variable's mg_inject, PAMR_TF_INJECT_TO_MG_LEV,
+    * src/pamr.c:667-685, 1886-1893), which matters when the caller changed
+    * the sources above since the hierarchy was built; the V-cycle itself
+    * leaves this injection out because within one solve it rewrites the
+    * same values. */
+   for (L = s->h.nlev - 1; L >= 1 && keep; L--)
+      if (!s->h.lev[L].in_amrh && s->h.inject_init[L].nops)
+         KC(pgb_k_restrict(s->dbox, &s->h.inject_init[L], PGB_SRC_MASK(s->nsrc), 0, s->stream));
    if (s->h.prm.precision == PGB_MIXED) {
       if (!s->tuned) {
          int rc = tail_plan(s);

@@ -88,6 +88,7 @@ def dropin_cases():
         # the coupled pair through vcycle on the finest level's MG hierarchy
         (W.coupled_from(W.nbs2d_uneven(seed=1, **small), seed=6), 1, 3, 0),
         (W.coupled_from(W.nbs3d(17, 9, seed=4, levels=3), seed=7), 1, 3, 0),
+        (W.coupled_from(W.nbs3d(17, 9, seed=4, levels=3), seed=7), 1, 1, 0),
     ]
 
 
