@@ -417,6 +417,48 @@ LEARNED_WORKLOAD = ("poisson3d_129: lap u = rho on [-10,10]^3, one 129^3 grid (6
                     "BF16 tensor-core encoder-decoder trained on multigrid-generated pairs")
 
 
+def stream_solves(sv, st, model, rhos, zero, torch, pipelined: bool) -> dict:
+    """solves/s of the sources in `rhos` solved back to back on solver sv
+    (stream st): from u = 0, or (pipelined) each from the net's guess, the
+    guess of source k+1 predicted on a second stream while solve k runs
+    (two guess buffers; the prediction into a buffer waits until the solver
+    has copied its previous content in)"""
+    import statistics as stats
+    n = len(rhos)
+    ps = torch.cuda.Stream()
+    gbuf = [torch.zeros_like(zero), torch.zeros_like(zero)]
+    ready = [torch.cuda.Event() for _ in range(2)]
+    taken = [torch.cuda.Event() for _ in range(2)]
+
+    def predict(k):
+        b = k % 2
+        with torch.cuda.stream(ps):
+            if k >= 2:
+                ps.wait_event(taken[b])
+            model.predict(rhos[k], gbuf[b], ps.cuda_stream)
+            ready[b].record(ps)
+
+    torch.cuda.synchronize()
+    if pipelined:
+        predict(0)
+    t0 = time.perf_counter()
+    iters = []
+    for k in range(n):
+        if pipelined:
+            if k + 1 < n:
+                predict(k + 1)
+            st.wait_event(ready[k % 2])
+            sv.set_inputs_device([gbuf[k % 2].data_ptr()], [rhos[k].data_ptr()])
+            taken[k % 2].record(st)
+        else:
+            sv.set_inputs_device([zero.data_ptr()], [rhos[k].data_ptr()])
+        iters.append(sv.solve()["iters"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    key = "guess_pipelined" if pipelined else "plain"
+    return {f"{key}_solves_per_s": n / wall, f"{key}_vcycles": stats.mean(iters)}
+
+
 def learned_main(args):
     """plain solves against solves started from the net's guess (prediction
     plus energy-norm rescale, timed with the solve), both precision forms,
@@ -483,6 +525,15 @@ def learned_main(args):
                 d = guess - u_plain
                 errs.append((float(d.abs().max() / u_plain.abs().max()),
                              float(d.norm() / u_plain.norm())))
+        # The same held-out sources as one stream of solves, back to back (no
+        # L2 flush, host wall clock over the whole stream): plain from u = 0,
+        # and with each guess predicted on a second stream while the solve
+        # before it runs (a stream of elliptic solves, as a Berger-Oliger run
+        # or an ensemble issues them; the small levels of a V-cycle leave
+        # most SMs idle, which the prediction fills)
+        stream_rates = stream_solves(sv, st, model, rhos[args.warmup:], zero, torch, pipelined=False)
+        if prec == 1:
+            stream_rates.update(stream_solves(sv, st, model, rhos[args.warmup:], zero, torch, pipelined=True))
         # the guess policy over the same sources: one plain solve first, then
         # guesses while they cut cycles
         pol = Lm.GuessPolicy()
@@ -499,7 +550,7 @@ def learned_main(args):
             "policy_solves_per_s": 1e3 * args.steps / pol_ms,
             "plain_vcycles": statistics.mean(i for _, i, _ in res["plain"]),
             "guess_vcycles": statistics.mean(i for _, i, _ in res["guess"]),
-            "policy_guessed_solves": used, "policy_enabled_at_end": pol.enabled,
+            "policy_guessed_solves": used, "policy_enabled_at_end": pol.enabled, "stream": stream_rates,
             "all_converged": all(c for _, _, c in res["plain"] + res["guess"])}
         sv.close()
     # prediction alone (forward + rescale)
@@ -530,6 +581,12 @@ def learned_main(args):
             "config": {"workload": LEARNED_WORKLOAD, "l2": "flushed between steps (512 MiB write)",
                        "pairs": args.pairs, "pairs_from": args.pairs_from, "epochs": args.epochs, "lr": args.lr},
             "forms": out, "cpu_baseline": cpu, "predict_ms": ev[0].elapsed_time(ev[1]) / 10,
+            # the spec ratio on a stream of solves (both back to back,
+            # no L2 flush): learned-guess mixed solver against plain FP64
+            "stream_ratio_vs_fp64_plain": {
+                "mixed_learned_guess_pipelined": out["mixed"]["stream"]["guess_pipelined_solves_per_s"] /
+                out["fp64"]["stream"]["plain_solves_per_s"],
+                "mixed_plain": out["mixed"]["stream"]["plain_solves_per_s"] / out["fp64"]["stream"]["plain_solves_per_s"]},
             "guess_error_vs_solution": {"max_rel": statistics.mean(e[0] for e in errs),
                                         "l2_rel": statistics.mean(e[1] for e in errs)},
             "training": {"dataset_s": t_data, "train_s": t_train, "epoch_loss": losses,

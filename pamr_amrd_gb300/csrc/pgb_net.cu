@@ -546,6 +546,11 @@ __global__ void __launch_bounds__(CZ_THREADS) k_conv_tcz(const __nv_bfloat16 *in
    if (warp == 0) tmem_dealloc(taddr, 2 * S::NCOL);
 }
 
+/* an upper bound on the CTAs of the persistent convolution (0: one wave of
+ * the whole GPU); a prediction running beside a solve leaves it the rest of
+ * the SMs (pgb_net_set_grid_cap) */
+static int g_tcz_cap = 0;
+
 template <int CIN, int COUT>
 static int launch_convz(const void *in, void *out, const void *wimg, const float *bias, const pgb_lvgeom &g,
                         int relu, int *err, cudaStream_t st)
@@ -564,7 +569,8 @@ static int launch_convz(const void *in, void *out, const void *wimg, const float
    int zc = 32;
    while (zc > 1 && (long)jt * ((g.D + zc - 1) / zc) < want) zc /= 2;
    const int nunit = jt * ((g.D + zc - 1) / zc);
-   const int grid = nunit < 152 * per_sm ? nunit : 152 * per_sm;
+   int grid = nunit < 152 * per_sm ? nunit : 152 * per_sm;
+   if (g_tcz_cap > 0 && grid > g_tcz_cap) grid = g_tcz_cap;
    k_conv_tcz<CIN, COUT><<<grid, CZ_THREADS, S::BYTES, st>>>((const __nv_bfloat16 *)in, (__nv_bfloat16 *)out,
                                                              (const __nv_bfloat16 *)wimg, bias, g, relu, jt, zc,
                                                              nunit, err);
@@ -1356,6 +1362,15 @@ static int bias_ranges(const pgb_net *net, long *off, long *cnt)
  * Adam step): the net is then positively homogeneous, net(c rho) = c
  * net(rho) for c > 0, which is what a guess of a linear equation's
  * solution should be */
+/* at most `ctas` CTAs for the persistent (z-marching) convolution of every
+ * net in the process, 0 for a full wave; results do not depend on it */
+extern "C" int pgb_net_set_grid_cap(int ctas)
+{
+   if (ctas < 0) return arg_err("pgb_net_set_grid_cap: negative");
+   g_tcz_cap = ctas;
+   return 0;
+}
+
 extern "C" int pgb_net_set_bias_free(pgb_net *net, int on)
 {
    net->bias_free = on;

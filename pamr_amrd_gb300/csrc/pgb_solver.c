@@ -56,6 +56,8 @@ struct pgb_solver {
    long long graph_kernels; /* kernel launches in the captured V-cycle */
    cudaGraphExec_t sexec;   /* the solve loop: V-cycles under a conditional while node */
    int solve_ok;            /* 1 built, -1 not available (host loop) */
+   cudaGraphExec_t pexec;   /* pgb_prepare's launches (after the autotuner ran), replayed by pgb_solve */
+   int prep_ok;             /* 1 built, -1 not available */
    double *d_hist;          /* finest residual after each cycle of a solve [max_iter] */
    int *d_parity;           /* mixed form: 0 / 1 for even / odd cycles of a solve */
    void *d_tmaps;           /* mixed form, 3-D: tensor maps of the TMA-staged sweep (0: unavailable) */
@@ -375,8 +377,18 @@ static int setup_device(pgb_solver *s)
    size_t off = 0, *fo, *w32o = 0;
    int i, f, L, d, maxt = 1, maxbox = 1;
    long snap_pts = 0;
-   CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-   CU(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+   {
+      /* the solver's streams at the device's greatest priority: a V-cycle
+       * is a chain of short dependent kernels, and work another stream runs
+       * beside it (the next solve's learned guess) should take the SMs its
+       * kernels leave free, not delay them (PGB_NO_STREAM_PRIORITY=1: the
+       * default priority) */
+      int least = 0, greatest = 0;
+      if (getenv("PGB_NO_STREAM_PRIORITY") || cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+         greatest = 0;
+      CU(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest));
+      CU(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest));
+   }
    CU(cudaEventCreate(&s->ev0));
    CU(cudaEventCreate(&s->ev1));
    CU(cudaEventCreateWithFlags(&s->evfork, cudaEventDisableTiming));
@@ -675,6 +687,7 @@ int pgb_destroy(pgb_solver *s)
       if (s->d_err) cudaFree(s->d_err);
       if (s->graph_ok) cudaGraphExecDestroy(s->gexec);
       if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
+      if (s->prep_ok > 0) cudaGraphExecDestroy(s->pexec);
       if (s->stream) {
          cudaEventDestroy(s->ev0);
          cudaEventDestroy(s->ev1);
@@ -1196,7 +1209,7 @@ static int box_field(const pgb_solver *s, int field, int *f)
 static int box_copy(pgb_solver *s, int L, int idx, int field, const double *in, double *out)
 {
    const pgb_hbox *b;
-   int f;
+   int f = 0;
    size_t n;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    if (L < 1 || L > s->h.nlev || idx < 0 || idx >= s->h.lev[L].nbox) return fail(3, "no box %d on level %d", idx, L);
@@ -1601,6 +1614,39 @@ static void drop_graph(pgb_solver *s)
    s->graph_ok = 0;
    if (s->solve_ok > 0) cudaGraphExecDestroy(s->sexec);
    s->solve_ok = 0;
+   if (s->prep_ok > 0) cudaGraphExecDestroy(s->pexec);
+   s->prep_ok = 0;
+}
+
+/* pgb_prepare's launches as one graph: every solve starts with the same
+ * clears, injections and first residual (after the autotuner's one-time
+ * timing, which is why the first pgb_prepare runs directly), so pgb_solve
+ * replays them instead of issuing some thirty launches from the host. */
+static int build_prepare_graph(pgb_solver *s)
+{
+   cudaGraph_t g = 0;
+   cudaError_t e;
+   int rc;
+   if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      s->prep_ok = -1;
+      return 0;
+   }
+   rc = pgb_prepare(s);
+   e = cudaStreamEndCapture(s->stream, &g);
+   if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+   }
+   if (e == cudaSuccess) e = cudaGraphInstantiate(&s->pexec, g, 0);
+   if (g) cudaGraphDestroy(g);
+   if (e != cudaSuccess) {
+      cudaGetLastError();
+      s->prep_ok = -1;
+      return 0;
+   }
+   s->prep_ok = 1;
+   return 0;
 }
 
 int pgb_vcycle(pgb_solver *s, double *res)
@@ -1630,32 +1676,66 @@ int pgb_vcycle(pgb_solver *s, double *res)
    return 0;
 }
 
+/* the end of pgb_solve once the stream is idle: the statistics (cycles in
+ * it, coarsest iterations and the device-timed error word in h_res) */
+static int solve_done(pgb_solver *s, int it, double res, int *iters, double *res_final)
+{
+   float ms = 0;
+   int ci = 0, err = 0;
+   CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+   memcpy(&ci, s->h_res + 1, sizeof(int));
+   memcpy(&err, s->h_res + 3, sizeof(int));
+   if (err) {
+      CU(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
+      return fail(12, "a device wait for staged data timed out (TMA sweep); results are not valid");
+   }
+   s->last_cycles = it;
+   s->last_citers = ci;
+   s->last_ms = ms;
+   if (iters) *iters = it;
+   if (res_final) *res_final = res;
+   return 0;
+}
+
 int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycle, int cap)
 {
    const pgb_hparams *p = &s->h.prm;
    double res = p->tol + 1;
-   int it = 0, rc, ci = 0;
-   float ms = 0;
+   int it = 0, rc;
    if (s->host_only) return fail(4, "solver was created with PGB_HOST_ONLY");
    CU(cudaEventRecord(s->ev0, s->stream));
-   if ((rc = pgb_prepare(s))) return rc;
+   if (!getenv("PGB_NO_GRAPH") && (p->precision != PGB_MIXED || s->tuned) && !s->prep_ok &&
+       (rc = build_prepare_graph(s)))
+      return rc;
+   if (s->prep_ok > 0 && !getenv("PGB_NO_GRAPH")) {
+      CU(cudaGraphLaunch(s->pexec, s->stream));
+      s->prepared = 1;
+   } else if ((rc = pgb_prepare(s)))
+      return rc;
    if (!getenv("PGB_NO_GRAPH") && !getenv("PGB_HOST_LOOP") && p->max_iter > 0) {
       if (!s->graph_ok && (rc = build_graph(s))) return rc;   /* also counts the cycle's kernels */
       if (!s->solve_ok && (rc = build_solve_graph(s))) return rc;
    }
    if (s->solve_ok > 0 && !getenv("PGB_NO_GRAPH") && !getenv("PGB_HOST_LOOP") && p->max_iter > 0) {
+      /* one wait for everything: the cycle count, the last norm and the
+       * norm history up to cap (entries past the count are not used) */
+      const int nh = cap < p->max_iter ? cap : p->max_iter;
       CU(cudaMemsetAsync(s->d_it, 0, sizeof(int), s->stream));
       CU(cudaGraphLaunch(s->sexec, s->stream));
+      CU(cudaEventRecord(s->ev1, s->stream));
       CU(cudaMemcpyAsync(s->h_res + 2, s->d_it, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
       CU(cudaMemcpyAsync(s->h_res, norm_slot(s, s->h.nlev, N_RESID), sizeof(double), cudaMemcpyDeviceToHost,
                          s->stream));
+      CU(cudaMemcpyAsync(s->h_res + 1, s->d_citers, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+      CU(cudaMemcpyAsync(s->h_res + 3, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+      if (res_per_cycle && nh > 0)
+         CU(cudaMemcpyAsync(res_per_cycle, s->d_hist, sizeof(double) * (size_t)nh, cudaMemcpyDeviceToHost,
+                            s->stream));
       CU(cudaStreamSynchronize(s->stream));
       memcpy(&it, s->h_res + 2, sizeof(int));
       res = s->h_res[0];
       g_graph_replayed += (s->graph_kernels + 1) * it;
-      if (res_per_cycle && cap > 0 && it > 0)
-         CU(cudaMemcpy(res_per_cycle, s->d_hist, sizeof(double) * (size_t)(it < cap ? it : cap),
-                       cudaMemcpyDeviceToHost));
+      return solve_done(s, it, res, iters, res_final);
    } else
       while ((it < p->min_iter || res > p->tol) && it < p->max_iter) {
          if ((rc = pgb_vcycle(s, &res))) return rc;
@@ -1666,22 +1746,7 @@ int pgb_solve(pgb_solver *s, int *iters, double *res_final, double *res_per_cycl
    CU(cudaMemcpyAsync(s->h_res + 1, s->d_citers, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
    CU(cudaMemcpyAsync(s->h_res + 3, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
    CU(cudaStreamSynchronize(s->stream));
-   CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-   memcpy(&ci, s->h_res + 1, sizeof(int));
-   {
-      int err = 0;
-      memcpy(&err, s->h_res + 3, sizeof(int));
-      if (err) {
-         CU(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
-         return fail(12, "a device wait for staged data timed out (TMA sweep); results are not valid");
-      }
-   }
-   s->last_cycles = it;
-   s->last_citers = ci;
-   s->last_ms = ms;
-   if (iters) *iters = it;
-   if (res_final) *res_final = res;
-   return 0;
+   return solve_done(s, it, res, iters, res_final);
 }
 
 int pgb_stats(const pgb_solver *s, int *vcycles, long *coarsest_iters, double *device_ms)

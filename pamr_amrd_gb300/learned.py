@@ -36,8 +36,16 @@ def _bind():
     L.pgb_conv3d_geometry.argtypes = [C.c_int] * 3 + [_vp, _vp]
     L.pgb_conv3d_pack_weights.argtypes = [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]
     L.pgb_conv3d_bf16.argtypes = [_vp] * 4 + [C.c_int] * 6 + [_vp, _vp]
+    L.pgb_net_set_grid_cap.argtypes = [C.c_int]
     _bound = True
     return L
+
+
+def set_grid_cap(ctas: int):
+    """at most `ctas` CTAs for the persistent tensor-core convolution (0: a
+    full wave): a prediction that runs beside a solve leaves it the other
+    SMs; the results do not depend on it"""
+    _check(_bind().pgb_net_set_grid_cap(ctas))
 
 
 def conv_lib():
