@@ -704,9 +704,10 @@ __device__ __forceinline__ void store8(bf16 *a, long idx, const float *v)
  * zero on the padding and margins, which nothing writes), converted once
  * per voxel: the first layer and its weight gradient read each value 27
  * times, at fixed offsets without bounds tests */
-__global__ void k_rho32(const double *rho, int n, float s_in, float *r32, pgb_lvgeom g)
+__global__ void k_rho32(const double *rho, int n, float s_in, const double *q, float *r32, pgb_lvgeom g)
 {
    const long nv = (long)g.W * g.H * g.D;
+   if (q) s_in = (float)(1.0 / fmax(*q, 1e-300));   /* the source's charge, computed on the device */
    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nv; q += gridDim.x * blockDim.x) {
       int x, y, z;
       xyz(q, g, x, y, z);
@@ -797,8 +798,10 @@ __global__ void k_out_fwd(const bf16 *a, const float *w, const float *b, float *
 
 /* u (n^3 FP64) = s_out * up on points 1..n-2 of the net volume, 0 on the
  * grid's boundary points */
-__global__ void k_out_store(const float *up, double *u, int n, double s_out, pgb_lvgeom g)
+__global__ void k_out_store(const float *up, double *u, int n, double s_out, const double *q, double gain,
+                            pgb_lvgeom g)
 {
+   if (q) s_out = gain * fmax(*q, 1e-300);
    const long nn = (long)n * n * n;
    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)nn; q += gridDim.x * blockDim.x) {
       const int z = q / (n * n), r = q - z * n * n, y = r / n, x = r - y * n;
@@ -1207,6 +1210,8 @@ struct pgb_net {
    int n;
    pgb_lvgeom g[NLEV];
    double s_in, s_out;
+   const double *d_q;             /* while set: the charge the scales come from, on the device */
+   double q_gain;                 /* s_out = q_gain * charge then */
    long np;                       /* parameter count */
    float *p, *gp, *m, *v;         /* parameters, gradients, Adam moments */
    long off_tc_w[NTC], off_tc_b[NTC], off_in_w, off_in_b, off_out_w, off_out_b;
@@ -1280,6 +1285,7 @@ extern "C" int pgb_net_create(int n, unsigned long long seed, pgb_net **out)
       return arg_err("pgb_net_create: n-1 must be a multiple of 32, 65 <= n <= 513");
    layer_table();
    pgb_net *net = (pgb_net *)calloc(1, sizeof(pgb_net));
+   if (!net) return arg_err("pgb_net_create: out of host memory");
    net->n = n;
    net->s_in = net->s_out = 1.0;
    for (int l = 0; l < NLEV; l++) {
@@ -1423,7 +1429,7 @@ static int forward(pgb_net *net, const double *rho, cudaStream_t st)
    bf16 **a = net->act;
    pgb_lvgeom *g = net->g;
 #define A(k, v) a[act_id(k, v)]
-   NETK((k_rho32<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->r32, g[0])), "net rho32");
+   NETK((k_rho32<<<GRID_1D, 256, 0, st>>>(rho, net->n, (float)net->s_in, net->d_q, net->r32, g[0])), "net rho32");
    NETK((k_in_fwd<<<(g[0].W * g[0].H * g[0].D + 255) / 256, 256, 0, st>>>(net->r32, net->p + net->off_in_w,
                                                                           net->p + net->off_in_b, A(K_E0, 0), g[0])),
         "net in");
@@ -1448,8 +1454,23 @@ extern "C" int pgb_net_predict(pgb_net *net, const double *rho, double *u, void 
 {
    cudaStream_t st = (cudaStream_t)stream;
    if (forward(net, rho, st)) return 11;
-   NETK((k_out_store<<<GRID_1D, 256, 0, st>>>(net->up, u, net->n, net->s_out, net->g[0])), "net store");
+   NETK((k_out_store<<<GRID_1D, 256, 0, st>>>(net->up, u, net->n, net->s_out, net->d_q, net->q_gain, net->g[0])),
+        "net store");
    return 0;
+}
+
+/* pgb_net_predict with the input and output scales taken from the source's
+ * charge q (a device value, e.g. h^3 sum |rho|, computed on the same stream):
+ * s_in = 1/q, s_out = gain q, so that the host never waits for the charge */
+extern "C" int pgb_net_predict_charge(pgb_net *net, const double *rho, double *u, const double *q, double gain,
+                                      void *stream)
+{
+   if (!q) return arg_err("pgb_net_predict_charge: no charge");
+   net->d_q = q;
+   net->q_gain = gain;
+   const int rc = pgb_net_predict(net, rho, u, stream);
+   net->d_q = 0;
+   return rc;
 }
 
 extern "C" int pgb_net_rescale(pgb_net *net, const double *rho, double *u, double h, void *stream)

@@ -29,6 +29,7 @@ def _bind():
     L.pgb_net_num_params.restype = C.c_long
     L.pgb_net_params.argtypes = [_vp, C.c_int, C.POINTER(C.c_float), C.c_int]
     L.pgb_net_predict.argtypes = [_vp, _vp, _vp, _vp]
+    L.pgb_net_predict_charge.argtypes = [_vp, _vp, _vp, _vp, C.c_double, _vp]
     L.pgb_net_rescale.argtypes = [_vp, _vp, _vp, C.c_double, _vp]
     L.pgb_net_rejected_guesses.argtypes = [_vp, C.POINTER(C.c_long)]
     L.pgb_net_loss_grad.argtypes = [_vp, _vp, _vp, _dp, _vp]
@@ -127,6 +128,11 @@ class Net:
     def predict(self, rho_ptr: int, u_ptr: int, stream=None):
         _check(lib().pgb_net_predict(self.h, rho_ptr, u_ptr, stream))
 
+    def predict_charge(self, rho_ptr: int, u_ptr: int, q_ptr: int, gain: float, stream=None):
+        """predict with s_in = 1/q, s_out = gain q read from the device value
+        at q_ptr (computed on the same stream)"""
+        _check(lib().pgb_net_predict_charge(self.h, rho_ptr, u_ptr, q_ptr, gain, stream))
+
     def rescale(self, rho_ptr: int, u_ptr: int, h: float, stream=None):
         """energy-norm optimal amplitude of the guess (pgb_net_rescale); a
         guess that is not finite or needs an absurd amplitude becomes u = 0"""
@@ -190,11 +196,17 @@ class Scaled:
 
     def predict(self, rho, u, stream=None, rescale: bool = True):
         """the guess of u for source rho (device tensors), its amplitude set
-        by the energy norm unless rescale is False"""
-        self._scale(rho)
-        self.net.predict(rho.data_ptr(), u.data_ptr(), stream)
-        if rescale:
-            self.net.rescale(rho.data_ptr(), u.data_ptr(), self.h, stream)
+        by the energy norm unless rescale is False. The charge that scales
+        rho and the guess is summed on the device, on the prediction's
+        stream, so the host does not wait for it."""
+        import torch
+        ts = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        with torch.cuda.stream(ts):
+            self._q = rho.abs().sum() * (self.h ** 3)   # kept until the next prediction
+            self.net.predict_charge(rho.data_ptr(), u.data_ptr(), self._q.data_ptr(), self.gain,
+                                    ts.cuda_stream)
+            if rescale:
+                self.net.rescale(rho.data_ptr(), u.data_ptr(), self.h, ts.cuda_stream)
 
 
 def make_dataset(n: int, seeds, torch, cycles: int = 12, precision: int = 1):
