@@ -145,9 +145,11 @@ typedef struct {
    int flags;
    /* several elliptic variables solved together (AMRD_num_elliptic_vars,
     * amrd/mg.c:248-314): nvar (1..PGB_MAX_VARS) and the operator of each
-    * variable v >= 1 in var_op[v] (op is variable 0's); FP64 form only.
-    * Every variable takes the same transfer operators (restr_u, restr_res,
-    * mg_sync, interp_order) */
+    * variable v >= 1 in var_op[v] (op is variable 0's); both forms (the
+    * mixed form smooths all variables' FP32 corrections point by point, with
+    * coupling coefficients from the programs' derivatives). Every variable
+    * takes the same transfer operators (restr_u, restr_res, mg_sync,
+    * interp_order) */
    int nvar;
    const pgb_operator *var_op[PGB_MAX_VARS];
 } pgb_create_args;
@@ -283,7 +285,8 @@ int pgb_time_relax(pgb_solver *s, int level, int reps, double *ms_per_sweep,
  * through the tile's planes, 4 or 5 = one sweep per launch with planes
  * staged by TMA in columns 60 or 28 points wide, 6 or 7 = two sweeps per
  * launch staged by TMA in columns 24 or 56 points wide; 3-7 on 3-D levels
- * only); no reference counterpart. */
+ * only; a solver with several elliptic variables runs the coupled colour
+ * passes and reports 0); no reference counterpart. */
 int pgb_level_tuning(pgb_solver *s, int level, int *tile_planes, int *sweeps_per_launch);
 
 /* Mixed form: MG levels 1..n (the return value; 0 when none) whose V-cycle

@@ -139,6 +139,16 @@ int pgb_k_interp_mixed(const pgb_dbox *boxes, const pgb_plan *p, int dim, int sl
 int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, pgb_scratch sc,
                         double *norm_out, pgb_trace *trace, const int *gate, void *stream);
 int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r, void *stream);
+/* the box tables of the variables of a mixed-form solve with several
+ * elliptic variables: t[v] is variable v's view (t[0] the solver's table) */
+typedef struct {
+   const pgb_dbox *t[PGB_NVAR_MAX];
+} pgb_vtabs;
+/* one colour pass of the coupled FP32 smoother over lv.nvar variables */
+int pgb_k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv, int pass, void *stream);
+/* the level's norm over the res of every elliptic variable (lv.nvar of them) */
+int pgb_k_norm_vars(const pgb_dbox *boxes, pgb_dlevel lv, pgb_scratch sc, double *norm_out, pgb_trace *trace,
+                    void *stream);
 int pgb_k_coarsest_mixed(const pgb_dbox *boxes, pgb_dlevel lv, int pde, const pgb_plan *sync,
                          pgb_coarsest_args a, pgb_trace *trace, void *stream);
 

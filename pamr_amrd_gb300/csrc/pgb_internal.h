@@ -64,6 +64,9 @@ typedef struct {
    unsigned char lcode[PGB_PROG_MAX];   /* L[u] */
    unsigned char jcode[PGB_PROG_MAX];   /* dL/du */
    double cst[PGB_PROG_CONST];
+   int nvread;   /* one-variable kernels (mixed form) running variable v of several: the
+                  * variables 0..nvread-1 the program names are read from the box's
+                  * variable fields at the point (0: the program names only u) */
 } pgb_dop;
 
 #define PGB_MAXLEV 48
@@ -87,6 +90,9 @@ typedef struct {
    const uint8_t *cmask_bdy;     /* set_cmask_bdy, amrd/mg.c:432-488 */
    float *w32[PGB_NW32];         /* mixed form: correction, defect, Jacobian term, coarse correction,
                                   * second correction buffer (fused sweeps write it) */
+   float *w32c;                  /* mixed form, several variables: dL/du_k of the box's variable for the
+                                  * variables in slots k = 1..nvar-1, one FP32 array each (same layout
+                                  * and pitch as w32, wz * Nz floats apart); 0 with one variable */
    int n[3];                     /* Nx, Ny, Nz (Nz = 1 in 2-D) */
    int wy;                       /* FP32 arrays: row pitch (Nx rounded up to 4 floats, so every row
                                   * starts on 16 bytes: vector and TMA loads) */

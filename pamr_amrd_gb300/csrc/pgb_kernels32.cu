@@ -221,10 +221,14 @@ __device__ __forceinline__ double lapw(const pgb_dbox &b, const double *u, long 
 /* L[u] from lap u for the three operators (Poisson t - s, conformal factor
  * t + 2 pi s u^5, lapse t - s u; num.f:85-123 pattern) and, in c, the FP32
  * derivative of the non-Laplacian part (5 * 2 pi s u^4, -s, 0) */
-template <bool PROG>
+template <bool PROG, bool VARS = false>
 __device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, double t, double uc, double s,
                                         float &c)
 {
+   if (PROG && VARS) {   /* one variable of several, over its view of the boxes */
+      c = d2f(__dsub_rn(pgb_prog_Jview(b, uc, s, p), b.j0));
+      return pgb_prog_Lview(b, t, uc, s, p);
+   }
    if (PROG) {   /* an application's operator program (pgb_op.cuh) */
       c = d2f(__dsub_rn(pgb_prog_J(b, uc, s, p), b.j0));
       return pgb_prog_L(b, t, uc, s, p);
@@ -242,6 +246,34 @@ __device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, doub
    return t - s;
 }
 
+/* Several elliptic variables: the coupling coefficients dL/du_k of the
+ * variable a box table's view holds, for the variables in slots
+ * k = 1..nvread-1, at FP32 point q (the coupled colour pass k_relax32_vars
+ * reads them). Out of line so that the one-variable instantiations keep
+ * their registers. */
+__device__ __noinline__ void store_coupling(const pgb_dop *o, double j0, double lapv, double u, const double *u1,
+                                            const double *u2, const double *u3, pgb_srcv sv, float *out,
+                                            long stride)
+{
+   double uv[PGB_NVAR_MAX];
+   uv[0] = u;
+   uv[1] = *u1;
+   uv[2] = o->nvread > 2 ? *u2 : 0.0;
+   uv[3] = o->nvread > 3 ? *u3 : 0.0;
+   for (int k = 1; k < PGB_NVAR_MAX; k++)
+      if (k < o->nvread) out[(k - 1) * stride] = d2f(pgb_prog_dvar(o->lcode, o->cst, lapv, j0, u, uv, sv, k));
+}
+
+__device__ __forceinline__ void coupling_at(const pgb_dbox &b, long p, long q, double lapv, double u, double s0)
+{
+   const pgb_dop *o = b.op;
+   if (o->nvread < 2) return;
+   const int nr = o->nvread;
+   store_coupling(o, b.j0, lapv, u, b.f[PGB_FV(1, PGB_F_U)] + p, nr > 2 ? b.f[PGB_FV(2, PGB_F_U)] + p : 0,
+                  nr > 3 ? b.f[PGB_FV(3, PGB_F_U)] + p : 0, pgb_load_src(o->nsrc, b, p, s0), b.w32c + q,
+                  b.wz * b.n[2]);
+}
+
 /* Down sweep, levels below the finest: app_L_op + compute_MG_rhs
  * (amrd/mg.c:271-314) fused with the FP64 defect of the pre-smoothing block:
  *     rhs = cmask_child ? -res*w0_r + L[u] : 0,   lop = u,
@@ -249,7 +281,7 @@ __device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, doub
  * E is 0 on entry (every block ends by clearing it). With cover = 1 only
  * the level's cover tiles are visited: elsewhere rhs stays 0 and D is the
  * FP32 update k_defect32 made at the end of the previous post-smoothing. */
-template <bool PROG, bool TAIL>
+template <bool PROG, bool TAIL, bool VARS = false>
 __device__ __forceinline__ void fas_defect_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
                                              double w0_r, int cover, int split)
 {
@@ -282,11 +314,13 @@ __device__ __forceinline__ void fas_defect_b(const vblk &vb, const pgb_dbox *box
       double r = 0.0;
       if (in && (cm || rl)) {
          float c;
-         const double l = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c);
+         const double lp = lapw(b, u, p, sy, uc, zm, zp, dim);
+         const double l = opjac<PROG, VARS>(pde, b, p, lp, uc, src[p], c);
          if (cm) r = fma(-res[p], w0_r, l);
          if (rl) {
             wd[q] = d2f(r - l);
             wc[q] = c;
+            if (VARS) coupling_at(b, p, q, lp, uc, src[p]);
          }
       } else if (cm)
          r = -res[p] * w0_r;
@@ -297,11 +331,11 @@ __device__ __forceinline__ void fas_defect_b(const vblk &vb, const pgb_dbox *box
    }
 }
 
-template <bool PROG>
+template <bool PROG, bool VARS = false>
 __global__ void __launch_bounds__(NT) k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                    double w0_r, int cover, int split)
 {
-   fas_defect_b<PROG, false>(hw_blk(), boxes, lv, pde, w0_r, cover, split);
+   fas_defect_b<PROG, false, VARS>(hw_blk(), boxes, lv, pde, w0_r, cover, split);
 }
 
 /* The Gauss-Seidel update of one point of lap E + C E = D, FP32, written
@@ -356,6 +390,48 @@ __device__ __forceinline__ void relax32_b(const vblk &vb, const pgb_dbox *boxes,
 __global__ void __launch_bounds__(NT) k_relax32(const pgb_dbox *boxes, pgb_dlevel lv, int pass)
 {
    relax32_b<false>(hw_blk(), boxes, lv, pass);
+}
+
+/* One colour pass of the coupled FP32 smoother of several elliptic
+ * variables: at each point of the colour, variable 0, 1, ... in turn, each
+ * from the others' current corrections at the point (the point-wise order
+ * of the FP64 form's relax over the variables), on
+ *     lap E_v + C_v E_v + sum_k C_vk E_k = D_v
+ * with C_vk the coupling coefficients of the FP64 passes (w32c, slot k of
+ * variable v's view holding variable k, or 0 where k = v). In place on
+ * each variable's E; vt.t[v] is variable v's view of the boxes. */
+__global__ void __launch_bounds__(NT) k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv, int pass)
+{
+   const pgb_tile tl = lv.rtiles[blockIdx.x];
+   const pgb_dbox b = vt.t[0][tl.box];
+   const int dim = lv.dim, nv = lv.nvar;
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1], wy = b.wy, wz = b.wz, cs = b.wz * b.n[2];
+   const float ix = b.fidx2[0], iy = b.fidx2[1], iz = b.fidx2[2];
+   const float j0 = b.fj0;
+   const int j = tl.j0 + threadIdx.y;
+   const int kz = dim == 3 ? lv.rtz : 1;
+   float *ev[PGB_NVAR_MAX];
+   for (int v = 0; v < PGB_NVAR_MAX; v++) ev[v] = v < nv ? vt.t[v][tl.box].w32[W_E] : 0;
+   for (int kk = 0; kk < PGB_TZ; kk++) {
+      if (kk >= kz) break;
+      const int k = tl.k0 + kk;
+      const int par = dim == 3 ? ((j + k + 1 + pass) & 1) : ((j + pass) & 1);
+      const int i = tl.i0 + 2 * threadIdx.x + par;
+      if (!interior32(b, i, j, k, dim)) continue;
+      const long p = i + sy * j + sz * k, q = i + wy * j + wz * k;
+      if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
+      const bool d3 = dim == 3;
+      for (int v = 0; v < PGB_NVAR_MAX; v++) {
+         if (v >= nv) break;
+         const pgb_dbox &bv = vt.t[v][tl.box];
+         float off = 0.f;
+         for (int k2 = 1; k2 < PGB_NVAR_MAX; k2++)
+            if (k2 < nv) off = __fmaf_rn(bv.w32c[(k2 - 1) * cs + q], ev[k2 == v ? 0 : k2][q], off);
+         float *e = ev[v];
+         e[q] = gs32(e[q], e[q - 1], e[q + 1], e[q - wy], e[q + wy], d3 ? e[q - wz] : 0.f, d3 ? e[q + wz] : 0.f,
+                     bv.w32[W_C][q], __fsub_rn(bv.w32[W_D][q], off), ix, iy, iz, j0, d3);
+      }
+   }
 }
 
 /* The same sweeps staged in shared memory: NS red-black sweeps in one launch.
@@ -1072,7 +1148,6 @@ __device__ __forceinline__ void copy_e_b(const vblk &vb, const pgb_dbox *boxes, 
    const pgb_dbox b = boxes[tl.box];
    const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
    if (i >= b.n[0] || j >= b.n[1]) return;
-   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
    const int kz = lv.dim == 3 ? lv.tz : 1;
    RP(const float) a = eslot(b, src);
    RP(float) e = b.w32[W_E];
@@ -1603,49 +1678,16 @@ __device__ double block_sum32(double v, double *sm)
  * relaxed points, D = -res and C for the next smoothing block of this
  * level, and call_rr_app's norm (per-box RMS, max over boxes) reduced by the
  * last CTA to finish; with norm_out = 0 (a norm nothing reads) no norm. */
-template <bool PROG, bool TAIL>
-__device__ __forceinline__ void residual_fast_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
-                                                const pgb_scratch &sc, double *norm_out, pgb_trace *trace, int split,
-                                                const int *gate)
+/* call_rr_app over a level (amrd/util.c:39-103): every CTA (split per
+ * tile) stores its sum of squared residuals; the CTA that arrives last turns
+ * them into per-box RMS values (divided by the box's relaxed-point count) and
+ * writes their maximum */
+__device__ __forceinline__ void level_rms(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv,
+                                          const pgb_scratch &sc, int split, double acc, double *norm_out,
+                                          pgb_trace *trace)
 {
-   if (gate && *gate) return;   /* the cycle parity leaves this pass out (no norm is read then) */
    __shared__ double sm[32];
    __shared__ int last;
-   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
-   const pgb_tile tl = tp.tl;
-   const pgb_dbox b = boxes[tl.box];
-   const int dim = lv.dim;
-   RP(const double) u = b.f[PGB_F_U];
-   RP(const double) rhs = b.f[PGB_F_RHS];
-   RP(const double) src = b.f[PGB_F_SRC];
-   RP(double) res = b.f[PGB_F_RES];
-   RP(float) wd = b.w32[W_D];
-   RP(float) wc = b.w32[W_C];
-   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
-   double acc = 0;
-   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
-   const int ks = tl.k0 + tp.kk0;
-   if (i < b.n[0] && j < b.n[1] && ks < b.n[2]) {
-      long p = i + sy * j + sz * ks, q = wq(b, i, j, ks);
-      double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
-#pragma unroll
-      for (int kk = 0; kk < PGB_TZ; kk++, p += sz, q += b.wz) {
-         const int k = ks + kk;
-         if (kk >= tp.nk || k >= b.n[2]) continue;
-         const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
-         if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
-            float c;
-            const double r = opjac<PROG>(pde, b, p, lapw(b, u, p, sy, uc, zm, zp, dim), uc, src[p], c) - rhs[p];
-            res[p] = r;
-            wd[q] = d2f(-r);
-            wc[q] = c;
-            if (norm_out) acc = fma(r, r, acc);
-         }
-         zm = uc;
-         uc = zp;
-      }
-   }
-   if (!norm_out) return;
    acc = block_sum32(acc, sm);
    if (threadIdx.x == 0 && threadIdx.y == 0) sc.partial[vb.x] = acc;
    __threadfence();
@@ -1683,17 +1725,92 @@ __device__ __forceinline__ void residual_fast_b(const vblk &vb, const pgb_dbox *
    }
 }
 
-template <bool PROG>
+template <bool PROG, bool TAIL, bool VARS = false>
+__device__ __forceinline__ void residual_fast_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
+                                                const pgb_scratch &sc, double *norm_out, pgb_trace *trace, int split,
+                                                const int *gate)
+{
+   if (gate && *gate) return;   /* the cycle parity leaves this pass out (no norm is read then) */
+   const tile_part tp = tile_split(lv.tiles, lv, split, vb.x);
+   const pgb_tile tl = tp.tl;
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   RP(const double) u = b.f[PGB_F_U];
+   RP(const double) rhs = b.f[PGB_F_RHS];
+   RP(const double) src = b.f[PGB_F_SRC];
+   RP(double) res = b.f[PGB_F_RES];
+   RP(float) wd = b.w32[W_D];
+   RP(float) wc = b.w32[W_C];
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   double acc = 0;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int ks = tl.k0 + tp.kk0;
+   if (i < b.n[0] && j < b.n[1] && ks < b.n[2]) {
+      long p = i + sy * j + sz * ks, q = wq(b, i, j, ks);
+      double zm = (dim == 3 && ks > 0) ? u[p - sz] : 0.0, uc = u[p];
+#pragma unroll
+      for (int kk = 0; kk < PGB_TZ; kk++, p += sz, q += b.wz) {
+         const int k = ks + kk;
+         if (kk >= tp.nk || k >= b.n[2]) continue;
+         const double zp = (dim == 3 && k + 1 < b.n[2]) ? u[p + sz] : 0.0;
+         if (interior32(b, i, j, k, dim) && ((b.flags & PGB_BOX_BDY_INTERIOR) || b.cmask_bdy[p])) {
+            float c;
+            const double lp = lapw(b, u, p, sy, uc, zm, zp, dim);
+            const double r = opjac<PROG, VARS>(pde, b, p, lp, uc, src[p], c) - rhs[p];
+            res[p] = r;
+            wd[q] = d2f(-r);
+            wc[q] = c;
+            if (VARS) coupling_at(b, p, q, lp, uc, src[p]);
+            if (norm_out) acc = fma(r, r, acc);
+         }
+         zm = uc;
+         uc = zp;
+      }
+   }
+   if (norm_out) level_rms(vb, boxes, lv, sc, split, acc, norm_out, trace);
+}
+
+template <bool PROG, bool VARS = false>
 __global__ void __launch_bounds__(NT) k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                       pgb_scratch sc, double *norm_out,
                                                       pgb_trace *trace, int split, const int *gate)
 {
-   residual_fast_b<PROG, false>(hw_blk(), boxes, lv, pde, sc, norm_out, trace, split, gate);
+   residual_fast_b<PROG, false, VARS>(hw_blk(), boxes, lv, pde, sc, norm_out, trace, split, gate);
+}
+
+/* The convergence norm of a level in a solve with several elliptic
+ * variables: each variable's residual pass (k_residual_fast over that
+ * variable's view of the boxes) has written its res; this pass sums every
+ * variable's squared residual at the relaxed points, the norm of the
+ * point-wise hooks of such an application (one sum over all variables per
+ * box, amrd/util.c:39-103). */
+__global__ void __launch_bounds__(NT) k_norm_vars(const pgb_dbox *boxes, pgb_dlevel lv, pgb_scratch sc,
+                                                  double *norm_out, pgb_trace *trace)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int kz = dim == 3 ? lv.tz : 1;
+   double acc = 0;
+   if (i < b.n[0] && j < b.n[1])
+      for (int kk = 0; kk < kz; kk++) {
+         const int k = tl.k0 + kk;
+         if (k >= b.n[2]) break;
+         const long p = i + (long)b.n[0] * (j + (long)b.n[1] * k);
+         if (!relaxed32(b, i, j, k, p, dim)) continue;
+         for (int v = 0; v < PGB_NVAR_MAX; v++)
+            if (v < lv.nvar) {
+               const double r = b.f[PGB_FV(v, PGB_F_RES)][p];
+               acc = fma(r, r, acc);
+            }
+      }
+   level_rms(hw_blk(), boxes, lv, sc, 1, acc, norm_out, trace);
 }
 
 /* L_op + compute_MG_rhs (amrd/mg.c:271-314) on the cover tiles of the
  * coarsest level, which the coarsest-grid loop smooths by itself */
-template <bool PROG>
+template <bool PROG, bool VARS = false>
 __device__ __forceinline__ void lop_rhs_fast_b(const vblk &vb, const pgb_dbox *boxes, const pgb_dlevel &lv, int pde,
                                                double w0_r)
 {
@@ -1713,17 +1830,17 @@ __device__ __forceinline__ void lop_rhs_fast_b(const vblk &vb, const pgb_dbox *b
       const int cm = b.cmask_child[p];
       float c;
       if (cm && interior32(b, i, j, k, lv.dim))
-         lopv = opjac<PROG>(pde, b, p, lapm(b, u, p, sy, sz, lv.dim), u[p], b.f[PGB_F_SRC][p], c);
+         lopv = opjac<PROG, VARS>(pde, b, p, lapm(b, u, p, sy, sz, lv.dim), u[p], b.f[PGB_F_SRC][p], c);
       b.f[PGB_F_RHS][p] = cm ? fma(-b.f[PGB_F_RES][p], w0_r, lopv) : 0.0;
       b.f[PGB_F_LOP][p] = u[p];
    }
 }
 
-template <bool PROG>
+template <bool PROG, bool VARS = false>
 __global__ void __launch_bounds__(NT) k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
                                                      double w0_r)
 {
-   lop_rhs_fast_b<PROG>(hw_blk(), boxes, lv, pde, w0_r);
+   lop_rhs_fast_b<PROG, VARS>(hw_blk(), boxes, lv, pde, w0_r);
 }
 
 /* The coarsest-grid loop of the mixed form (amrd/mg.c:172-190: relax the
@@ -2382,8 +2499,12 @@ extern "C" int pgb_k_fas_defect(const pgb_dbox *boxes, pgb_dlevel lv, int pde, d
       t->gx = n * sp;
       return 0;
    }
-   OPLAUNCH(k_fas_defect, pde, n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r, cover,
-            sp);
+   if (lv.nvar > 1)   /* one variable of several (a program operator) */
+      k_fas_defect<true, true><<<n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r, cover,
+                                                                                        sp);
+   else
+      OPLAUNCH(k_fas_defect, pde, n * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r, cover,
+               sp);
    return check32("fas_defect");
 }
 
@@ -2679,9 +2800,30 @@ extern "C" int pgb_k_residual_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde
       t->gx = lv.ntiles * sp;
       return 0;
    }
-   OPLAUNCH(k_residual_fast, pde, lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, sc,
-            norm_out, trace, sp, gate);
+   if (lv.nvar > 1)   /* one variable of several (a program operator) */
+      k_residual_fast<true, true><<<lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(
+         boxes, lv, pde, sc, norm_out, trace, sp, gate);
+   else
+      OPLAUNCH(k_residual_fast, pde, lv.ntiles * sp, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, sc,
+               norm_out, trace, sp, gate);
    return check32("residual_fast");
+}
+
+extern "C" int pgb_k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv, int pass, void *stream)
+{
+   if (!lv.nrtiles) return 0;
+   if (g_tp) return tail_refuse();
+   k_relax32_vars<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(vt, lv, pass);
+   return check32("relax32_vars");
+}
+
+extern "C" int pgb_k_norm_vars(const pgb_dbox *boxes, pgb_dlevel lv, pgb_scratch sc, double *norm_out,
+                               pgb_trace *trace, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   if (g_tp) return tail_refuse();
+   k_norm_vars<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, sc, norm_out, trace);
+   return check32("norm_vars");
 }
 
 extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_r,
@@ -2694,7 +2836,10 @@ extern "C" int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde,
       t->gx = lv.nctiles;
       return 0;
    }
-   OPLAUNCH(k_lop_rhs_fast, pde, lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r);
+   if (lv.nvar > 1)   /* one variable of several (a program operator) */
+      k_lop_rhs_fast<true, true><<<lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv, pde, w0_r);
+   else
+      OPLAUNCH(k_lop_rhs_fast, pde, lv.nctiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream, boxes, lv, pde, w0_r);
    return check32("lop_rhs_fast");
 }
 

@@ -33,6 +33,12 @@ struct pgb_solver {
    size_t arena_bytes;
    pgb_dbox *hbox;          /* host copy of the device box table */
    pgb_dbox *dbox;
+   /* mixed form with several elliptic variables: the box table as the
+    * one-variable kernels see variable v (vbox[0] = dbox): its U..RHS fields
+    * and variable 0's swapped, its own FP32 arrays, its operator renumbered
+    * to match (d_vdop[v]) */
+   pgb_dbox *vbox[PGB_NVAR_MAX];
+   pgb_dop *d_vdop;
    pgb_dlevel lv[PGB_MAXLEV + 1];
    void *d_tables[PGB_MAXLEV + 1];
    pgb_scratch sc;
@@ -371,11 +377,68 @@ static int field_used(const pgb_solver *s, int f)
    return 1;
 }
 
+/* The views of a mixed-form solver with several elliptic variables. The
+ * FP32 passes (sweeps, defect, update, coarse-grid correction,
+ * interpolation) and the FP64 passes of one variable (residual, FAS
+ * right-hand side) are one-variable kernels: run over the box table of view
+ * v, they read and write variable v. View v swaps the U, RES, LOP and RHS
+ * slots of variables 0 and v, points the FP32 arrays (and the coupling
+ * coefficients) at variable v's, and
+ * gives the boxes variable v's operator with its variable names renumbered
+ * by the same swap, so that the other variables it names are read from the
+ * slots that hold them (pgb_prog_vars, pgb_op.cuh). View 0 is the box table
+ * itself. */
+static int var_views(pgb_solver *s, const size_t *w32o, int per)
+{
+   const int nw32 = per * s->nvar;
+   const pgb_hier *h = &s->h;
+   pgb_dop vd[PGB_NVAR_MAX];
+   pgb_dbox *t;
+   int v, i, f, q, rc = 0;
+   for (v = 0; v < s->nvar; v++) {
+      vd[v] = s->dops[v];
+      for (q = 0; q < 2; q++) {
+         unsigned char *code = q ? vd[v].jcode : vd[v].lcode;
+         for (i = 0; i < PGB_PROG_MAX && (code[i] & 15) != PGB_P_END; i++) {
+            const int a = code[i] >> 4;
+            if ((code[i] & 15) == PGB_P_U && a >= 1) {   /* u<a-1>: variable a-1 sits in slot swap(a-1) */
+               const int k = a - 1, sk = k == 0 ? v : k == v ? 0 : k;
+               code[i] = (unsigned char)(((sk + 1) << 4) | PGB_P_U);
+            }
+         }
+      }
+   }
+   CU(cudaMalloc((void **)&s->d_vdop, sizeof(pgb_dop) * (size_t)s->nvar));
+   CU(cudaMemcpy(s->d_vdop, vd, sizeof(pgb_dop) * (size_t)s->nvar, cudaMemcpyHostToDevice));
+   t = (pgb_dbox *)malloc(sizeof(pgb_dbox) * (size_t)h->nbox);
+   if (!t) return fail(10, "out of host memory");
+   for (v = 1; v < s->nvar && !rc; v++) {
+      for (i = 0; i < h->nbox; i++) {
+         t[i] = s->hbox[i];
+         for (f = PGB_F_U; f <= PGB_F_RHS; f++) {
+            t[i].f[f] = s->hbox[i].f[PGB_FV(v, f)];
+            t[i].f[PGB_FV(v, f)] = s->hbox[i].f[f];
+         }
+         for (f = 0; f < PGB_NW32; f++) t[i].w32[f] = (float *)(s->arena + w32o[i * nw32 + v * per + f]);
+         t[i].w32c = (float *)(s->arena + w32o[i * nw32 + v * per + PGB_NW32]);
+         t[i].op = s->d_vdop + v;
+      }
+      if (cudaMalloc((void **)&s->vbox[v], sizeof(pgb_dbox) * (size_t)h->nbox) != cudaSuccess ||
+          cudaMemcpy(s->vbox[v], t, sizeof(pgb_dbox) * (size_t)h->nbox, cudaMemcpyHostToDevice) != cudaSuccess)
+         rc = fail(10, "variable views: out of device memory");
+   }
+   free(t);
+   return rc;
+}
+
 static int setup_device(pgb_solver *s)
 {
    pgb_hier *h = &s->h;
    size_t off = 0, *fo, *w32o = 0;
-   int i, f, L, d, maxt = 1, maxbox = 1;
+   int i, f, L, d, rc, maxt = 1, maxbox = 1;
+   /* mixed form: per box and variable PGB_NW32 FP32 arrays, and with several
+    * variables one block of nvar - 1 arrays of coupling coefficients */
+   const int per = PGB_NW32 + (s->nvar > 1), nw32 = per * s->nvar;
    long snap_pts = 0;
    {
       /* the solver's streams at the device's greatest priority: a V-cycle
@@ -409,14 +472,14 @@ static int setup_device(pgb_solver *s)
       off = align256(off + n);
    }
    if (h->prm.precision == PGB_MIXED) {
-      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * PGB_NW32);
+      w32o = (size_t *)malloc(sizeof(size_t) * (size_t)h->nbox * nw32);
       for (i = 0; i < h->nbox; i++) {
          const pgb_hbox *b = &h->boxes[i];
          /* rows padded to a multiple of 4 floats (16 bytes) */
          size_t n = (size_t)((b->shape[0] + 3) & ~3) * b->shape[1] * b->shape[2];
-         for (f = 0; f < PGB_NW32; f++) {
-            w32o[i * PGB_NW32 + f] = off;
-            off = align256(off + 4 * n);
+         for (f = 0; f < nw32; f++) {
+            w32o[i * nw32 + f] = off;
+            off = align256(off + 4 * n * (f % per == PGB_NW32 ? (size_t)(s->nvar - 1) : 1));
          }
       }
    }
@@ -434,7 +497,8 @@ static int setup_device(pgb_solver *s)
       for (f = 0; f < PGB_NF; f++) db->f[f] = field_used(s, f) ? (double *)(s->arena + fo[i * (PGB_NF + 2) + f]) : 0;
       db->op = s->d_dop;
       if (w32o)
-         for (f = 0; f < PGB_NW32; f++) db->w32[f] = (float *)(s->arena + w32o[i * PGB_NW32 + f]);
+         for (f = 0; f < PGB_NW32; f++) db->w32[f] = (float *)(s->arena + w32o[i * nw32 + f]);
+      if (w32o && s->nvar > 1) db->w32c = (float *)(s->arena + w32o[i * nw32 + PGB_NW32]);
       db->cmask_child = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF]);
       db->cmask_bdy = (const uint8_t *)(s->arena + fo[i * (PGB_NF + 2) + PGB_NF + 1]);
       CU(cudaMemcpy((void *)db->cmask_child, b->child_mask, n, cudaMemcpyHostToDevice));
@@ -460,12 +524,15 @@ static int setup_device(pgb_solver *s)
       db->fj0 = (float)db->j0;
    }
    free(fo);
-   free(w32o);
    CU(cudaMalloc((void **)&s->dbox, sizeof(pgb_dbox) * (size_t)h->nbox));
    CU(cudaMemcpy(s->dbox, s->hbox, sizeof(pgb_dbox) * (size_t)h->nbox, cudaMemcpyHostToDevice));
+   s->vbox[0] = s->dbox;
+   rc = w32o && s->nvar > 1 ? var_views(s, w32o, per) : 0;
+   free(w32o);
+   if (rc) return rc;
    CU(cudaMalloc((void **)&s->d_err, sizeof(int)));
    CU(cudaMemset(s->d_err, 0, sizeof(int)));
-   if (h->prm.precision == PGB_MIXED && h->dim == 3 && !getenv("PGB_NO_TMA"))
+   if (h->prm.precision == PGB_MIXED && h->dim == 3 && s->nvar == 1 && !getenv("PGB_NO_TMA"))
       pgb_tmaps_build(s->hbox, h->nbox, &s->d_tmaps);   /* 1 (no maps): the TMA sweep is not offered */
 
    /* per-level tables: tiles, relax tiles, tile starts, box lists */
@@ -568,8 +635,6 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
          return fail(1, "the operator of variable %d names u%d, beyond the %d variable(s)", v,
                      pgb_operator_vars(ops[v]) - 1, nvar);
    }
-   if (nvar > 1 && a->params.precision != PGB_FP64)
-      return fail(1, "the mixed form carries one elliptic variable: several take PGB_FP64");
    if (params->interp_order != 2 && params->interp_order != 4)
       return fail(1, "interp_order must be 2 or 4");
    if (params->restr_u < 0 || params->restr_u > 3 || params->restr_res < 0 ||
@@ -587,7 +652,10 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
    for (v = 0; v < nvar; v++) {   /* every variable's program reads the solver's sources */
       s->dops[v] = *pgb_operator_device_form(ops[v]);
       s->dops[v].nsrc = s->nsrc;
-      if (nvar > 1) s->dops[v].kind = PGB_OPK_PROGRAM;   /* the program path handles the coupling */
+      if (nvar > 1) {   /* the program path handles the coupling */
+         s->dops[v].kind = PGB_OPK_PROGRAM;
+         s->dops[v].nvread = nvar;
+      }
    }
    if (nvar > 1) s->dop.kind = PGB_OPK_PROGRAM;
    memset(&hp, 0, sizeof(hp));
@@ -672,6 +740,9 @@ int pgb_destroy(pgb_solver *s)
       if (s->arena) cudaFree(s->arena);
       if (s->d_dop) cudaFree(s->d_dop);
       if (s->dbox) cudaFree(s->dbox);
+      for (L = 1; L < PGB_NVAR_MAX; L++)
+         if (s->vbox[L]) cudaFree(s->vbox[L]);
+      if (s->d_vdop) cudaFree(s->d_vdop);
       if (s->sc.partial) cudaFree(s->sc.partial);
       if (s->sc.counter) cudaFree(s->sc.counter);
       if (s->sc.box_norm) cudaFree(s->sc.box_norm);
@@ -821,6 +892,24 @@ int pgb_get_grid_device(pgb_solver *s, int grid, double *u)
 
 /* ------------------------------------------------------------- V-cycle -- */
 static double *norm_slot(pgb_solver *s, int L, int k) { return s->d_norms + N_SLOTS * L + k; }
+
+/* The mixed form's residual pass over the finest level with its norm (and
+ * D = -res for the next pre-smoothing block): one pass, or with several
+ * elliptic variables one pass over each variable's view and the norm over
+ * all of them */
+static int finest_residual32(pgb_solver *s, pgb_trace *trace)
+{
+   const int Lf = s->h.nlev;
+   int v;
+   if (s->nvar == 1) {
+      KC32(pgb_k_residual_fast(s->dbox, s->lv[Lf], s->h.pde, s->sc, norm_slot(s, Lf, N_RESID), trace, 0, s->stream));
+      return 0;
+   }
+   for (v = 0; v < s->nvar; v++)
+      KC32(pgb_k_residual_fast(s->vbox[v], s->lv[Lf], s->h.pde, s->sc, 0, 0, 0, s->stream));
+   KC32(pgb_k_norm_vars(s->dbox, s->lv[Lf], s->sc, norm_slot(s, Lf, N_RESID), trace, s->stream));
+   return 0;
+}
 
 static int lvl_coarsest(const pgb_solver *s, int L)   /* is_coarsest amrd/mg.c:553-567 */
 {
@@ -1020,6 +1109,7 @@ static int autotune(pgb_solver *s)
    int L, changed = 0;
    int nsw = h->prm.pre_swp > h->prm.pst_swp ? h->prm.pre_swp : h->prm.pst_swp;
    s->tuned = 1;
+   if (s->nvar > 1) return 0;   /* several variables: one smoother (the coupled colour passes) */
    if (force && force[0] >= '0' && force[0] <= '7' && !force[1]) {
       /* one sweep shape on every level instead of the measured choice */
       for (L = s->tail_lc > 1 ? s->tail_lc + 1 : 2; L <= h->nlev; L++) {
@@ -1142,8 +1232,12 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
        * computed); the finest level's first pre-smoothing defect is the
        * initial residual */
       for (L = 1; L <= s->h.nlev; L++) {
-         KC(pgb_k_clear(s->dbox, s->lv[L], (1 << PGB_F_RES) | (1 << PGB_F_LOP) | (1 << PGB_F_RHS), s->stream));
-         if (pgb_k_zero32(s->dbox, s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
+         int v;
+         KC(pgb_k_clear(s->dbox, s->lv[L],
+                        PGB_VMASK(s->nvar, PGB_F_RES) | PGB_VMASK(s->nvar, PGB_F_LOP) | PGB_VMASK(s->nvar, PGB_F_RHS),
+                        s->stream));
+         for (v = 0; v < s->nvar; v++)
+            if (pgb_k_zero32(s->vbox[v], s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
       }
       /* A level's residual is restricted from its FP32 copy D = -res when no
        * sync writes res there and the restriction of res is full weighting
@@ -1162,11 +1256,9 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
                const int op = ((const pgb_restrict_op *)h->inject[L - 1].h_ops)[i].op[PGB_F_RES];
                if (op != 0 && op != 3) ok = 0;
             }
-         s->res32[L] = ok;
+         s->res32[L] = ok && s->nvar == 1;   /* several variables: res is restricted in FP64 */
       }
-      if (pgb_k_residual_fast(s->dbox, s->lv[s->h.nlev], s->h.pde, s->sc,
-                              norm_slot(s, s->h.nlev, N_RESID), 0, 0, s->stream))
-         return fail(11, "%s", pgb_dev_error32());
+      if (finest_residual32(s, 0)) return 11;
       /* Levels below the finest whose cover tiles are a minority, with no
        * sync between boxes: between a post-smoothing and the next
        * pre-smoothing their points outside the cover tiles do not change,
@@ -1176,7 +1268,7 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
          const pgb_hier *h = &s->h;
          /* not on levels with coarsest boxes: their coarsest-grid loop
           * changes u after the post-smoothing, so D cannot be carried */
-         s->dnext[L] = h->prm.pre_swp > 0 && !h->sync[L][0].nops && !h->sync[L][1].nops &&
+         s->dnext[L] = s->nvar == 1 && h->prm.pre_swp > 0 && !h->sync[L][0].nops && !h->sync[L][1].nops &&
                        2 * s->lv[L].nctiles < s->lv[L].ntiles && !lvl_coarsest(s, L);
          if (s->dnext[L] &&
              pgb_k_fas_defect(s->dbox, s->lv[L], h->pde, h->prm.w0_r, 0, s->stream))
@@ -1344,23 +1436,26 @@ static int vcycle_fp64(pgb_solver *s)
    return 0;
 }
 
-/* FP32 sweeps on the correction E of level L, synced between boxes like u;
- * the block starts from slot *slot, which receives the slot it ends in */
-static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot)
+/* FP32 sweeps on the correction E of level L, synced between boxes like u,
+ * over the box table `boxes` (the solver's, or a variable's view); the
+ * block starts from slot *slot, which receives the slot it ends in */
+static int sweeps32_on(pgb_solver *s, const pgb_dbox *boxes, int L, int nsweep, int *slot)
 {
    pgb_hier *h = &s->h;
    int it;
    if (!h->sync[L][0].nops && !h->sync[L][1].nops) {
-      KC32(pgb_k_sweep32(s->dbox, s->lv[L], nsweep, s->fuse[L], slot, s->stream));
+      KC32(pgb_k_sweep32(boxes, s->lv[L], nsweep, s->fuse[L], slot, s->stream));
       return 0;
    }
    for (it = 0; it < nsweep; it++) {
-      KC32(pgb_k_sweep32(s->dbox, s->lv[L], 1, s->fuse[L] == 2 ? 1 : s->fuse[L], slot, s->stream));
+      KC32(pgb_k_sweep32(boxes, s->lv[L], 1, s->fuse[L] == 2 ? 1 : s->fuse[L], slot, s->stream));
       if (h->sync[L][it ? 1 : 0].nops)
-         KC32(pgb_k_copy32(s->dbox, &h->sync[L][it ? 1 : 0], *slot, s->stream));
+         KC32(pgb_k_copy32(boxes, &h->sync[L][it ? 1 : 0], *slot, s->stream));
    }
    return 0;
 }
+
+static int sweeps32(pgb_solver *s, int L, int nsweep, int *slot) { return sweeps32_on(s, s->dbox, L, nsweep, slot); }
 
 /* the FP32 defect carry and the update of a block in one kernel (where the
  * update's zeros go to the slot the defect does not read); PGB_NO_FUSED_UPDATE=1
@@ -1517,9 +1612,95 @@ static int vcycle_mixed(pgb_solver *s)
    return 0;
 }
 
+/* FP32 sweeps of the coupled smoother of several variables on level L
+ * (colour passes in place on each variable's E, synced between boxes like
+ * u) */
+static int sweeps32_vars(pgb_solver *s, int L, int nsweep)
+{
+   pgb_hier *h = &s->h;
+   pgb_vtabs vt;
+   int it, v;
+   memset(&vt, 0, sizeof(vt));
+   for (v = 0; v < s->nvar; v++) vt.t[v] = s->vbox[v];
+   for (it = 0; it < nsweep; it++) {
+      KC32(pgb_k_relax32_vars(vt, s->lv[L], 0, s->stream));
+      KC32(pgb_k_relax32_vars(vt, s->lv[L], 1, s->stream));
+      for (v = 0; v < s->nvar && h->sync[L][it ? 1 : 0].nops; v++)
+         KC32(pgb_k_copy32(s->vbox[v], &h->sync[L][it ? 1 : 0], PGB_W32_E, s->stream));
+   }
+   return 0;
+}
+
+/* The mixed V-cycle of several elliptic variables. The one-variable passes
+ * run once per variable, over that variable's view of the boxes
+ * (var_views): residual, FAS right-hand side (each also leaving the
+ * variable's defect D, Jacobian term C and coupling coefficients), update,
+ * coarse-grid correction and interpolation. The smoothing blocks are the
+ * coupled FP32 smoother over all variables at once (k_relax32_vars: at each
+ * point variable after variable, as the FP64 form's relax), which keeps the
+ * smoothing of modes the coupling dominates, on coarse levels where s dx^2
+ * is large; clears, restrictions and syncs run once over the box table with
+ * every variable's fields, the coarsest grid takes the FP64 loop over all
+ * variables and the norm sums every variable's residual. The FP32 defect
+ * carry and FP32 residual restriction of the one-variable form, its fused
+ * and TMA sweeps and the small-level kernel are left out. */
+static int vcycle_mixed_vars(pgb_solver *s)
+{
+   pgb_hier *h = &s->h;
+   const pgb_hparams *p = &h->prm;
+   const int nv = s->nvar, Lf = h->nlev;
+   int L, v;
+   KC(pgb_k_clear(s->dbox, s->lv[Lf], PGB_VMASK(nv, PGB_F_RES) | PGB_VMASK(nv, PGB_F_RHS) | PGB_VMASK(nv, PGB_F_LOP),
+                  s->stream));
+   for (L = Lf; L > 0; L--) {
+      if (L < Lf) {
+         for (v = 0; v < nv; v++)
+            KC32(pgb_k_residual_fast(s->vbox[v], s->lv[L + 1], h->pde, s->sc, 0, 0, 0, s->stream));
+         if (s->d_trace)
+            KC32(pgb_k_norm_vars(s->dbox, s->lv[L + 1], s->sc, norm_slot(s, L + 1, N_RESID), s->d_trace, s->stream));
+         if (sync_vars(s, &h->sync[L + 1][0], PGB_F_RES)) return 11;
+         KC(pgb_k_clear(s->dbox, s->lv[L], PGB_VMASK(nv, PGB_F_RES), s->stream));
+         if (h->inject[L].nops) KC(pgb_k_restrict(s->dbox, &h->inject[L], ~PGB_SRC_MASK(s->nsrc), 0, s->stream));
+         if (sync_vars(s, &h->sync[L][0], PGB_F_U)) return 11;
+         for (v = 0; v < nv; v++) {
+            if (L == 1) KC32(pgb_k_lop_rhs_fast(s->vbox[v], s->lv[L], h->pde, p->w0_r, s->stream));
+            else KC32(pgb_k_fas_defect(s->vbox[v], s->lv[L], h->pde, p->w0_r, 0, s->stream));
+         }
+      }
+      if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pre_swp, N_RELAX_DN)) return 11;
+      if (L > 1 && p->pre_swp > 0) {
+         if (sweeps32_vars(s, L, p->pre_swp)) return 11;
+         for (v = 0; v < nv; v++) KC32(pgb_k_update(s->vbox[v], s->lv[L], 0, PGB_W32_E, PGB_W32_E, s->stream));
+         if (sync_vars(s, &h->sync[L][1], PGB_F_U)) return 11;
+      }
+   }
+   for (L = 1; L <= Lf; L++) {
+      if (L > 1) {
+         for (v = 0; v < nv; v++) {
+            KC32(pgb_k_cgc_mixed(s->vbox[v], s->lv[L - 1], 1.0 / p->w0_i, s->stream));
+            if (h->interp[L].nops)
+               KC32(pgb_k_interp_mixed(s->vbox[v], &h->interp[L], h->dim, PGB_W32_E, s->stream, s->side, s->evfork,
+                                       s->evjoin));
+         }
+         if (sweeps32_vars(s, L, p->pst_swp)) return 11;
+         for (v = 0; v < nv; v++) KC32(pgb_k_update(s->vbox[v], s->lv[L], 1, PGB_W32_E, PGB_W32_E, s->stream));
+         if (sync_vars(s, &h->sync[L][1], PGB_F_U)) return 11;
+      }
+      if (L == 1 && fp64_level1(s) && smooth(s, 1, p->pst_swp, N_RELAX_UP)) return 11;
+      if (lvl_coarsest(s, L)) {
+         pgb_coarsest_args a;
+         coarsest_args(s, L, &a);
+         KC(pgb_k_coarsest(s->dbox, s->lv[L], h->pde, &h->sync_coarsest[L], a, s->d_trace, s->stream));
+      }
+      if (L == Lf && finest_residual32(s, s->d_trace)) return 11;
+   }
+   return 0;
+}
+
 static int vcycle_launch(pgb_solver *s)
 {
    if (s->h.prm.precision != PGB_MIXED) return vcycle_fp64(s);
+   if (s->nvar > 1) return vcycle_mixed_vars(s);
    const int rc = vcycle_mixed(s);
    if (rc && pgb_tail_recording()) pgb_tail_end();   /* an error inside the recorded levels */
    return rc;
