@@ -74,6 +74,8 @@ typedef struct {
    long smem_points;           /* points of the level's coarsest boxes (on-chip kernel) */
    int ncoarse;                /* number of coarsest boxes on the level */
    double omega;               /* mixed form: over-relaxation factor of the loop */
+   int sor;                    /* mixed form, several variables: the FP64 loop solves each point's
+                                  variables together (Newton), over-relaxed by omega */
    int inner_sweeps;           /* mixed form: FP32 sweeps per FP64 defect correction */
    double *snap;               /* 2 x (points of the coarsest boxes) doubles */
    long snap_points;

@@ -223,6 +223,56 @@ __device__ double relax_vars(const pgb_dbox &b, int nvar, long p, int dim)
    return acc;
 }
 
+/* The mixed form's coarsest-grid loop with several variables: Newton at
+ * point p on all variables together (the point's nvar x nvar Jacobian: each
+ * program's diagonal and, by differentiating it, its coupling to the other
+ * variables; Gaussian elimination with partial pivoting), over-relaxed by
+ * om. Where the coupling dominates the diagonal (coarse grids of a large
+ * domain) the point-wise sweeps over one variable after the other reduce
+ * the modes it couples by little per sweep; this takes them in one.
+ * Returns the sum of the squared residuals before the update. */
+__device__ double relax_vars_block(const pgb_dbox &b, int nvar, long p, int dim, double om)
+{
+   double uv[PGB_NVAR_MAX], r[PGB_NVAR_MAX], J[PGB_NVAR_MAX][PGB_NVAR_MAX], acc = 0;
+   const pgb_srcv sv = pgb_load_src(b.op->nsrc, b, p, b.f[PGB_F_SRC][p]);
+   load_vars(b, nvar, p, uv);
+   for (int v = 0; v < nvar; v++) {
+      const pgb_dop *o = b.op + v;
+      const double lp = lap64(b, b.f[PGB_FV(v, PGB_F_U)], p, dim);
+      r[v] = pgb_prog_Lv(b, v, lp, uv, sv) - b.f[PGB_FV(v, PGB_F_RHS)][p];
+      acc += r[v] * r[v];
+      for (int k = 0; k < nvar; k++)
+         J[v][k] = k == v ? pgb_prog_Jv(b, v, uv, sv) : pgb_prog_dvar(o->lcode, o->cst, lp, b.j0, uv[v], uv, sv, k);
+   }
+   for (int c = 0; c < nvar; c++) {
+      int piv = c;
+      for (int i = c + 1; i < nvar; i++)
+         if (fabs(J[i][c]) > fabs(J[piv][c])) piv = i;
+      if (piv != c) {
+         for (int k = 0; k < nvar; k++) {
+            const double x = J[c][k];
+            J[c][k] = J[piv][k];
+            J[piv][k] = x;
+         }
+         const double x = r[c];
+         r[c] = r[piv];
+         r[piv] = x;
+      }
+      for (int i = c + 1; i < nvar; i++) {
+         const double f = J[i][c] / J[c][c];
+         for (int k = c; k < nvar; k++) J[i][k] -= f * J[c][k];
+         r[i] -= f * r[c];
+      }
+   }
+   for (int c = nvar - 1; c >= 0; c--) {
+      double x = r[c];
+      for (int k = c + 1; k < nvar; k++) x -= J[c][k] * r[k];
+      r[c] = x / J[c][c];
+   }
+   for (int v = 0; v < nvar; v++) b.f[PGB_FV(v, PGB_F_U)][p] = uv[v] - om * r[v];
+   return acc;
+}
+
 /* residual of every variable at point p (res_v = L_v - rhs_v); returns the
  * sum of their squares */
 __device__ double residual_vars(const pgb_dbox &b, int nvar, long p, int dim)
@@ -663,6 +713,7 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
    int iter = a.start_iter, nhist = 0;
    int verify_at = -1, period = 0;
    double *saved = a.snap;
+   double res_ck = 1e300;   /* over-relaxed loops: the norm at the last check */
    while (iter < a.max_citer && res > ctol) {
       double lres = 0;
       int first = 1;
@@ -681,7 +732,7 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
                long p = i + (long)bx.n[0] * (j + (long)bx.n[1] * k);
                if (!(bx.flags & PGB_BOX_BDY_INTERIOR) && !bx.cmask_bdy[p]) continue;
                if (PROG && lv.nvar > 1) {
-                  acc += relax_vars(bx, lv.nvar, p, dim);
+                  acc += a.sor ? relax_vars_block(bx, lv.nvar, p, dim, a.omega) : relax_vars(bx, lv.nvar, p, dim);
                   continue;
                }
                double *u = bx.f[PGB_F_U];
@@ -737,7 +788,15 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
       }
       iter++;
       if (!(iter < a.max_citer && res > ctol)) break;
-      if (a.stagnation_exit && iter > a.start_iter + 1 && res >= res_before) break;
+      if (a.stagnation_exit && iter > a.start_iter + 1) {
+         if (!a.sor && res >= res_before) break;
+         /* over-relaxed sweeps need not lower the norm every sweep: every
+          * 8 sweeps it must have fallen since the last check */
+         if (a.sor && (iter - a.start_iter) % 8 == 0) {
+            if (res >= res_ck) break;
+            res_ck = res;
+         }
+      }
 
       /* hash of the state; at a verification point compare with the save */
       unsigned long long h = 0;

@@ -1376,6 +1376,7 @@ static void coarsest_args(pgb_solver *s, int L, pgb_coarsest_args *a)
    }
    a->stagnation_exit = mixed;
    a->ctol_from_first = mixed;
+   a->sor = mixed && s->nvar > 1;
    /* red-black SOR factor of the model problem, 2/(1 + sin(pi h)) */
    a->omega = nmax > 3 ? 2.0 / (1.0 + sin(3.141592653589793 / (nmax - 1))) : 1.0;
    {
