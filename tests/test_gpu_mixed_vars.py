@@ -29,6 +29,7 @@ CASES = {
                                         seed=4),
     "nbs3d33": lambda: W.coupled_from(W.nbs3d(33, 17, seed=1), seed=5),
     "p3d65": lambda: W.coupled_from(W.poisson3d(65, seed=1), seed=2),
+    "c3d129": lambda: W.coupled_from(W.conformal3d(129, 65, seed=0), seed=1),
 }
 
 
