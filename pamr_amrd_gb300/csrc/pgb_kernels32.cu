@@ -410,8 +410,18 @@ __global__ void __launch_bounds__(NT) k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv
    const float j0 = b.fj0;
    const int j = tl.j0 + threadIdx.y;
    const int kz = dim == 3 ? lv.rtz : 1;
+   /* every variable's arrays, in registers (the loops over the variables
+    * unroll, so the indices are constants) */
    float *ev[PGB_NVAR_MAX];
-   for (int v = 0; v < PGB_NVAR_MAX; v++) ev[v] = v < nv ? vt.t[v][tl.box].w32[W_E] : 0;
+   const float *cv[PGB_NVAR_MAX], *dv[PGB_NVAR_MAX], *kv[PGB_NVAR_MAX];
+#pragma unroll
+   for (int v = 0; v < PGB_NVAR_MAX; v++) {
+      const pgb_dbox *bv = v < nv ? &vt.t[v][tl.box] : 0;
+      ev[v] = bv ? bv->w32[W_E] : 0;
+      cv[v] = bv ? bv->w32[W_C] : 0;
+      dv[v] = bv ? bv->w32[W_D] : 0;
+      kv[v] = bv ? bv->w32c : 0;
+   }
    for (int kk = 0; kk < PGB_TZ; kk++) {
       if (kk >= kz) break;
       const int k = tl.k0 + kk;
@@ -421,15 +431,16 @@ __global__ void __launch_bounds__(NT) k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv
       const long p = i + sy * j + sz * k, q = i + wy * j + wz * k;
       if (!(b.flags & PGB_BOX_BDY_INTERIOR) && !b.cmask_bdy[p]) continue;
       const bool d3 = dim == 3;
+#pragma unroll
       for (int v = 0; v < PGB_NVAR_MAX; v++) {
          if (v >= nv) break;
-         const pgb_dbox &bv = vt.t[v][tl.box];
          float off = 0.f;
+#pragma unroll
          for (int k2 = 1; k2 < PGB_NVAR_MAX; k2++)
-            if (k2 < nv) off = __fmaf_rn(bv.w32c[(k2 - 1) * cs + q], ev[k2 == v ? 0 : k2][q], off);
+            if (k2 < nv) off = __fmaf_rn(kv[v][(k2 - 1) * cs + q], ev[k2 == v ? 0 : k2][q], off);
          float *e = ev[v];
          e[q] = gs32(e[q], e[q - 1], e[q + 1], e[q - wy], e[q + wy], d3 ? e[q - wz] : 0.f, d3 ? e[q + wz] : 0.f,
-                     bv.w32[W_C][q], __fsub_rn(bv.w32[W_D][q], off), ix, iy, iz, j0, d3);
+                     cv[v][q], __fsub_rn(dv[v][q], off), ix, iy, iz, j0, d3);
       }
    }
 }
