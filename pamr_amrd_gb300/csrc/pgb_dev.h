@@ -146,6 +146,9 @@ int pgb_k_lop_rhs_fast(const pgb_dbox *boxes, pgb_dlevel lv, int pde, double w0_
 typedef struct {
    const pgb_dbox *t[PGB_NVAR_MAX];
 } pgb_vtabs;
+/* the coupling coefficients of the view's variable on a level, where they
+ * do not depend on the state (pgb_dop.cfixed; the passes skip them then) */
+int pgb_k_couplings(const pgb_dbox *boxes, pgb_dlevel lv, void *stream);
 /* one colour pass of the coupled FP32 smoother over lv.nvar variables */
 int pgb_k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv, int pass, void *stream);
 /* the level's norm over the res of every elliptic variable (lv.nvar of them) */

@@ -67,7 +67,11 @@ typedef struct {
    int nvread;   /* one-variable kernels (mixed form) running variable v of several: the
                   * variables 0..nvread-1 the program names are read from the box's
                   * variable fields at the point (0: the program names only u) */
+   int cfixed;   /* mixed form, several variables: no coupling coefficient dL/du_k depends
+                  * on lap or a variable (pgb_dop_couplings_fixed), so they are computed
+                  * once per pgb_prepare */
 } pgb_dop;
+int pgb_dop_couplings_fixed(const pgb_dop *d);
 
 #define PGB_MAXLEV 48
 

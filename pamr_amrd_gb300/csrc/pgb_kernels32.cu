@@ -264,14 +264,36 @@ __device__ __noinline__ void store_coupling(const pgb_dop *o, double j0, double 
       if (k < o->nvread) out[(k - 1) * stride] = d2f(pgb_prog_dvar(o->lcode, o->cst, lapv, j0, u, uv, sv, k));
 }
 
-__device__ __forceinline__ void coupling_at(const pgb_dbox &b, long p, long q, double lapv, double u, double s0)
+__device__ __forceinline__ void coupling_at(const pgb_dbox &b, long p, long q, double lapv, double u, double s0,
+                                            bool fill = false)
 {
    const pgb_dop *o = b.op;
-   if (o->nvread < 2) return;
+   if (o->nvread < 2 || (o->cfixed && !fill)) return;   /* fixed ones: k_couplings, once per prepare */
    const int nr = o->nvread;
    store_coupling(o, b.j0, lapv, u, b.f[PGB_FV(1, PGB_F_U)] + p, nr > 2 ? b.f[PGB_FV(2, PGB_F_U)] + p : 0,
                   nr > 3 ? b.f[PGB_FV(3, PGB_F_U)] + p : 0, pgb_load_src(o->nsrc, b, p, s0), b.w32c + q,
                   b.wz * b.n[2]);
+}
+
+/* The coupling coefficients of a level where they do not depend on the
+ * state (pgb_dop.cfixed): every relaxed point of the view's variable */
+__global__ void __launch_bounds__(NT) k_couplings(const pgb_dbox *boxes, pgb_dlevel lv)
+{
+   const pgb_tile tl = lv.tiles[blockIdx.x];
+   const pgb_dbox b = boxes[tl.box];
+   const int dim = lv.dim;
+   const int i = tl.i0 + threadIdx.x, j = tl.j0 + threadIdx.y;
+   const int kz = dim == 3 ? lv.tz : 1;
+   if (i >= b.n[0] || j >= b.n[1]) return;
+   const long sy = b.n[0], sz = (long)b.n[0] * b.n[1];
+   for (int kk = 0; kk < kz; kk++) {
+      const int k = tl.k0 + kk;
+      if (k >= b.n[2]) break;
+      const long p = i + sy * j + sz * k;
+      if (!relaxed32(b, i, j, k, p, dim)) continue;
+      const double *u = b.f[PGB_F_U];
+      coupling_at(b, p, wq(b, i, j, k), lapm(b, u, p, sy, sz, dim), u[p], b.f[PGB_F_SRC][p], true);
+   }
 }
 
 /* Down sweep, levels below the finest: app_L_op + compute_MG_rhs
@@ -2826,6 +2848,14 @@ extern "C" int pgb_k_relax32_vars(pgb_vtabs vt, pgb_dlevel lv, int pass, void *s
    if (g_tp) return tail_refuse();
    k_relax32_vars<<<lv.nrtiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(vt, lv, pass);
    return check32("relax32_vars");
+}
+
+extern "C" int pgb_k_couplings(const pgb_dbox *boxes, pgb_dlevel lv, void *stream)
+{
+   if (!lv.ntiles) return 0;
+   if (g_tp) return tail_refuse();
+   k_couplings<<<lv.ntiles, dim3(PGB_TX, PGB_TY), 0, (cudaStream_t)stream>>>(boxes, lv);
+   return check32("couplings");
 }
 
 extern "C" int pgb_k_norm_vars(const pgb_dbox *boxes, pgb_dlevel lv, pgb_scratch sc, double *norm_out,

@@ -354,6 +354,42 @@ int pgb_operator_eval_vars(const pgb_operator *op, int var, double lapv, double 
    return 0;
 }
 
+/* 1 when no derivative dL/du_k (k = 0..3, the names u0..u3) of the level
+ * operator's program depends on lap or on a variable: the program's
+ * values are followed abstractly (does it depend on the state, is its
+ * derivative nonzero, does the derivative depend on the state) through the
+ * rules of sums, products and quotients. The mixed form then computes its
+ * coupling coefficients once per pgb_prepare instead of in every pass. */
+int pgb_dop_couplings_fixed(const pgb_dop *d)
+{
+   int k;
+   for (k = 0; k < PGB_NVAR_MAX; k++) {
+      unsigned char dep[PGB_PROG_STACK + 1], dd[PGB_PROG_STACK + 1], ddep[PGB_PROG_STACK + 1];
+      int q, sp = 0;
+      for (q = 0; q < PGB_PROG_MAX && (d->lcode[q] & 15) != PGB_P_END; q++) {
+         const int opc = d->lcode[q] & 15, arg = d->lcode[q] >> 4;
+         if (opc == PGB_P_NEG) continue;
+         if (opc >= PGB_P_ADD && opc <= PGB_P_DIV) {
+            const int a = sp - 2, b = sp - 1;
+            if (a < 0) return 0;
+            ddep[a] = ddep[a] || ddep[b] || (opc == PGB_P_MUL && ((dd[a] && dep[b]) || (dd[b] && dep[a]))) ||
+                      (opc == PGB_P_DIV && ((dd[a] && dep[b]) || dd[b]));
+            dep[a] = dep[a] || dep[b];
+            dd[a] = dd[a] || dd[b];
+            sp--;
+            continue;
+         }
+         if (sp > PGB_PROG_STACK) return 0;
+         dep[sp] = opc == PGB_P_LAP || opc == PGB_P_U;
+         dd[sp] = opc == PGB_P_U && arg == k + 1;
+         ddep[sp] = 0;
+         sp++;
+      }
+      if (sp > 0 && ddep[sp - 1]) return 0;
+   }
+   return 1;
+}
+
 /* 1 + the highest variable index an operator names (u0..u3), 0 if none */
 int pgb_operator_vars(const pgb_operator *op)
 {

@@ -655,6 +655,7 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
       if (nvar > 1) {   /* the program path handles the coupling */
          s->dops[v].kind = PGB_OPK_PROGRAM;
          s->dops[v].nvread = nvar;
+         s->dops[v].cfixed = !getenv("PGB_COUPLINGS_EVERY_PASS") && pgb_dop_couplings_fixed(&s->dops[v]);
       }
    }
    if (nvar > 1) s->dop.kind = PGB_OPK_PROGRAM;
@@ -1236,8 +1237,11 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
          KC(pgb_k_clear(s->dbox, s->lv[L],
                         PGB_VMASK(s->nvar, PGB_F_RES) | PGB_VMASK(s->nvar, PGB_F_LOP) | PGB_VMASK(s->nvar, PGB_F_RHS),
                         s->stream));
-         for (v = 0; v < s->nvar; v++)
+         for (v = 0; v < s->nvar; v++) {
             if (pgb_k_zero32(s->vbox[v], s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
+            if (s->nvar > 1 && s->dops[v].cfixed && pgb_k_couplings(s->vbox[v], s->lv[L], s->stream))
+               return fail(11, "%s", pgb_dev_error32());
+         }
       }
       /* A level's residual is restricted from its FP32 copy D = -res when no
        * sync writes res there and the restriction of res is full weighting

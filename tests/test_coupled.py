@@ -63,3 +63,16 @@ def test_two_variable_hierarchy_builds_its_plans():
             assert np.array_equal(s.plan(which, L)[:, :14], one.plan(which, L)[:, :14])
     s.close()
     one.close()
+
+
+@pytest.mark.parametrize("lop,fixed", [("lap - s0*(u - u1) - s1", 1), ("lap - s0*(u - u0)", 1),
+                                       ("lap - u1/s0 + 2*s1", 1), ("lap - s0*u*u1", 0),
+                                       ("lap - s0/u1", 0), ("lap*u1", 0), ("lap - (u1 + s0)*(u1 - s0)", 0)])
+def test_fixed_coupling_coefficients_are_recognised(lop, fixed):
+    """the mixed form computes dL/du_k once per prepare only where no such
+    derivative of the program depends on lap or a variable"""
+    op = S.Operator(nsrc=2, lop=lop, jac="j0")
+    S.lib().pgb_operator_device_form.restype = C.c_void_p
+    S.lib().pgb_operator_device_form.argtypes = [C.c_void_p]
+    S.lib().pgb_dop_couplings_fixed.argtypes = [C.c_void_p]
+    assert S.lib().pgb_dop_couplings_fixed(S.lib().pgb_operator_device_form(op.h)) == fixed

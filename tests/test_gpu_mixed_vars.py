@@ -88,3 +88,16 @@ def test_mixed_several_variables_same_bits_in_every_launch_mode(monkeypatch):
         for a, b in zip(r["vars"], ref["vars"]):
             for x, y in zip(a, b):
                 assert np.array_equal(x, y)
+
+
+def test_fixed_couplings_once_per_prepare_change_no_bits(monkeypatch):
+    """the coupled pair's coefficients dL/du_k are sources only: computed once
+    per prepare (the default) or in every FP64 pass (PGB_COUPLINGS_EVERY_PASS=1),
+    the solve is the same bit for bit"""
+    case = CASES["c3d65"]()
+    ref = _solve(case, 1, monkeypatch, {"PGB_AUTOTUNE": "0", "PGB_COUPLINGS_EVERY_PASS": "1"})
+    r = _solve(case, 1, monkeypatch, {"PGB_AUTOTUNE": "0"})
+    assert r["iters"] == ref["iters"] and r["res_final"] == ref["res_final"]
+    for a, b in zip(r["vars"], ref["vars"]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
