@@ -70,8 +70,10 @@ typedef struct {
    int cfixed;   /* mixed form, several variables: no coupling coefficient dL/du_k depends
                   * on lap or a variable (pgb_dop_couplings_fixed), so they are computed
                   * once per pgb_prepare */
+   int jfixed;   /* the same for the Jacobian term dL/du - j0 (pgb_dop_jac_fixed) */
 } pgb_dop;
 int pgb_dop_couplings_fixed(const pgb_dop *d);
+int pgb_dop_jac_fixed(const pgb_dop *d);
 
 #define PGB_MAXLEV 48
 

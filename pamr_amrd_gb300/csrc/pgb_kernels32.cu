@@ -226,7 +226,7 @@ __device__ __forceinline__ double opjac(int pde, const pgb_dbox &b, long p, doub
                                         float &c)
 {
    if (PROG && VARS) {   /* one variable of several, over its view of the boxes */
-      c = d2f(__dsub_rn(pgb_prog_Jview(b, uc, s, p), b.j0));
+      if (!b.op->jfixed) c = d2f(__dsub_rn(pgb_prog_Jview(b, uc, s, p), b.j0));   /* else k_couplings' */
       return pgb_prog_Lview(b, t, uc, s, p);
    }
    if (PROG) {   /* an application's operator program (pgb_op.cuh) */
@@ -275,8 +275,9 @@ __device__ __forceinline__ void coupling_at(const pgb_dbox &b, long p, long q, d
                   b.wz * b.n[2]);
 }
 
-/* The coupling coefficients of a level where they do not depend on the
- * state (pgb_dop.cfixed): every relaxed point of the view's variable */
+/* The coupling coefficients (pgb_dop.cfixed) and the Jacobian term C
+ * (pgb_dop.jfixed) of a level where they do not depend on the state: every
+ * relaxed point of the view's variable */
 __global__ void __launch_bounds__(NT) k_couplings(const pgb_dbox *boxes, pgb_dlevel lv)
 {
    const pgb_tile tl = lv.tiles[blockIdx.x];
@@ -292,7 +293,9 @@ __global__ void __launch_bounds__(NT) k_couplings(const pgb_dbox *boxes, pgb_dle
       const long p = i + sy * j + sz * k;
       if (!relaxed32(b, i, j, k, p, dim)) continue;
       const double *u = b.f[PGB_F_U];
-      coupling_at(b, p, wq(b, i, j, k), lapm(b, u, p, sy, sz, dim), u[p], b.f[PGB_F_SRC][p], true);
+      const long q = wq(b, i, j, k);
+      if (b.op->cfixed) coupling_at(b, p, q, lapm(b, u, p, sy, sz, dim), u[p], b.f[PGB_F_SRC][p], true);
+      if (b.op->jfixed) b.w32[W_C][q] = d2f(__dsub_rn(pgb_prog_Jview(b, u[p], b.f[PGB_F_SRC][p], p), b.j0));
    }
 }
 
@@ -341,7 +344,7 @@ __device__ __forceinline__ void fas_defect_b(const vblk &vb, const pgb_dbox *box
          if (cm) r = fma(-res[p], w0_r, l);
          if (rl) {
             wd[q] = d2f(r - l);
-            wc[q] = c;
+            if (!VARS || !b.op->jfixed) wc[q] = c;
             if (VARS) coupling_at(b, p, q, lp, uc, src[p]);
          }
       } else if (cm)
@@ -1792,7 +1795,7 @@ __device__ __forceinline__ void residual_fast_b(const vblk &vb, const pgb_dbox *
             const double r = opjac<PROG, VARS>(pde, b, p, lp, uc, src[p], c) - rhs[p];
             res[p] = r;
             wd[q] = d2f(-r);
-            wc[q] = c;
+            if (!VARS || !b.op->jfixed) wc[q] = c;
             if (VARS) coupling_at(b, p, q, lp, uc, src[p]);
             if (norm_out) acc = fma(r, r, acc);
          }

@@ -390,6 +390,17 @@ int pgb_dop_couplings_fixed(const pgb_dop *d)
    return 1;
 }
 
+/* 1 when the value of the operator's dL/du program depends neither on
+ * lap nor on a variable (only on j0, the sources and constants): the
+ * mixed form then computes its Jacobian term once per pgb_prepare too */
+int pgb_dop_jac_fixed(const pgb_dop *d)
+{
+   int q;
+   for (q = 0; q < PGB_PROG_MAX && (d->jcode[q] & 15) != PGB_P_END; q++)
+      if ((d->jcode[q] & 15) == PGB_P_LAP || (d->jcode[q] & 15) == PGB_P_U) return 0;
+   return 1;
+}
+
 /* 1 + the highest variable index an operator names (u0..u3), 0 if none */
 int pgb_operator_vars(const pgb_operator *op)
 {

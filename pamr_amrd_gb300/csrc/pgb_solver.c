@@ -656,6 +656,7 @@ int pgb_create_ex(const pgb_create_args *a, pgb_solver **out)
          s->dops[v].kind = PGB_OPK_PROGRAM;
          s->dops[v].nvread = nvar;
          s->dops[v].cfixed = !getenv("PGB_COUPLINGS_EVERY_PASS") && pgb_dop_couplings_fixed(&s->dops[v]);
+         s->dops[v].jfixed = !getenv("PGB_COUPLINGS_EVERY_PASS") && pgb_dop_jac_fixed(&s->dops[v]);
       }
    }
    if (nvar > 1) s->dop.kind = PGB_OPK_PROGRAM;
@@ -1239,7 +1240,8 @@ int pgb_prepare_ex(pgb_solver *s, int flags)
                         s->stream));
          for (v = 0; v < s->nvar; v++) {
             if (pgb_k_zero32(s->vbox[v], s->lv[L], s->stream)) return fail(11, "%s", pgb_dev_error32());
-            if (s->nvar > 1 && s->dops[v].cfixed && pgb_k_couplings(s->vbox[v], s->lv[L], s->stream))
+            if (s->nvar > 1 && (s->dops[v].cfixed || s->dops[v].jfixed) &&
+                pgb_k_couplings(s->vbox[v], s->lv[L], s->stream))
                return fail(11, "%s", pgb_dev_error32());
          }
       }

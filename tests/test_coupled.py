@@ -76,3 +76,15 @@ def test_fixed_coupling_coefficients_are_recognised(lop, fixed):
     S.lib().pgb_operator_device_form.argtypes = [C.c_void_p]
     S.lib().pgb_dop_couplings_fixed.argtypes = [C.c_void_p]
     assert S.lib().pgb_dop_couplings_fixed(S.lib().pgb_operator_device_form(op.h)) == fixed
+
+
+@pytest.mark.parametrize("jac,fixed", [("j0 - s0", 1), ("j0", 1), ("j0 - s0*s1 + 3", 1), ("j0 - s0*u1", 0),
+                                       ("j0 + 5*u*u*u*u", 0)])
+def test_fixed_jacobian_terms_are_recognised(jac, fixed):
+    """likewise the Jacobian term dL/du - j0: once per prepare where the dL/du
+    program reads no variable (nor lap)"""
+    op = S.Operator(nsrc=2, lop="lap - s0*(u - u1) - s1", jac=jac)
+    S.lib().pgb_operator_device_form.restype = C.c_void_p
+    S.lib().pgb_operator_device_form.argtypes = [C.c_void_p]
+    S.lib().pgb_dop_jac_fixed.argtypes = [C.c_void_p]
+    assert S.lib().pgb_dop_jac_fixed(S.lib().pgb_operator_device_form(op.h)) == fixed

@@ -91,9 +91,9 @@ def test_mixed_several_variables_same_bits_in_every_launch_mode(monkeypatch):
 
 
 def test_fixed_couplings_once_per_prepare_change_no_bits(monkeypatch):
-    """the coupled pair's coefficients dL/du_k are sources only: computed once
-    per prepare (the default) or in every FP64 pass (PGB_COUPLINGS_EVERY_PASS=1),
-    the solve is the same bit for bit"""
+    """the coupled pair's coefficients dL/du_k and Jacobian terms are sources
+    only: computed once per prepare (the default) or in every FP64 pass
+    (PGB_COUPLINGS_EVERY_PASS=1), the solve is the same bit for bit"""
     case = CASES["c3d65"]()
     ref = _solve(case, 1, monkeypatch, {"PGB_AUTOTUNE": "0", "PGB_COUPLINGS_EVERY_PASS": "1"})
     r = _solve(case, 1, monkeypatch, {"PGB_AUTOTUNE": "0"})
