@@ -797,6 +797,7 @@ __global__ void __launch_bounds__(CT) k_coarsest(const pgb_dbox *boxes, pgb_dlev
             res_ck = res;
          }
       }
+      if (a.sor) continue;   /* no exact periods to skip outside the FP64 form's loop */
 
       /* hash of the state; at a verification point compare with the save */
       unsigned long long h = 0;
