@@ -43,14 +43,20 @@ def test_application_through_the_drop_in_matches_reference(path):
     assert float(np.max(np.abs(out["res"] - ref["res"]) / np.abs(ref["res"]))) < NORM_RTOL
 
 
-@pytest.mark.parametrize("path", [p for p in G.dropin_files() if "_m0_" in p and "coupled" not in p],
+@pytest.mark.parametrize("path", [p for p in G.dropin_files() if "_m0_" in p],
                          ids=lambda p: os.path.basename(p)[7:-4])
 def test_application_mixed_precision_through_the_drop_in(path):
     """amrd_set_device_MG_precision(1): FP32 smoothing inside FP64 defect
-    correction, converged and within 1e-9 of the reference's solution"""
+    correction, converged and within 1e-9 of the reference's solution (both
+    elliptic variables of a coupled case)"""
     case, mode, arg, level, ref = G.load_dropin(path)
+    if ref["res"][-1] > case.params.tol:
+        pytest.skip("the reference did not reach its tolerance on this case")
     out = D.run(D.build_device_app(), case, mode, arg, level, env={"NBS_APP_MIXED": "1"})
     assert out["res"][-1] <= case.params.tol
-    umax = max(float(np.max(np.abs(g["u"]))) for g in ref["grids"])
-    err = max(float(np.max(np.abs(a["u"] - b["u"]))) for a, b in zip(out["grids"], ref["grids"]))
-    assert err <= ERR_RTOL * umax, err / umax
+    for f in ("u", "w"):
+        if f not in ref["grids"][0]:
+            continue
+        umax = max(float(np.max(np.abs(g[f]))) for g in ref["grids"])
+        err = max(float(np.max(np.abs(a[f] - b[f]))) for a, b in zip(out["grids"], ref["grids"]))
+        assert err <= ERR_RTOL * umax, (f, err / umax)
